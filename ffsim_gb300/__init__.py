@@ -1,0 +1,46 @@
+"""ffsim_gb300: the statevector gate path of ffsim on one GB300 GPU.
+
+Drop-in counterparts of ``ffsim.apply_orbital_rotation``,
+``ffsim.apply_diag_coulomb_evolution``, ``ffsim.apply_num_op_sum_evolution``,
+``ffsim.apply_unitary`` for ``UCJOpSpinBalanced`` and
+``ffsim.linear_operator`` for ``DoubleFactorizedHamiltonian``, running
+hand-written sm_103a kernels through the C ABI in ``include/ffsim_gb300.h``.
+"""
+
+from ffsim_gb300 import contract, linalg, random, states
+from ffsim_gb300._state import dim, dims
+from ffsim_gb300.energy import LUCJEnergy, lucj_energy
+from ffsim_gb300.gates import (
+    apply_diag_coulomb_evolution,
+    apply_givens_rotation_in_place,
+    apply_num_op_sum_evolution,
+    apply_orbital_rotation,
+    apply_phase_shift_in_place,
+)
+from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian
+from ffsim_gb300.protocols import LinearOperator, apply_unitary, linear_operator
+from ffsim_gb300.states import hartree_fock_state, vdot
+from ffsim_gb300.variational import UCJOpSpinBalanced
+
+__all__ = [
+    "DoubleFactorizedHamiltonian",
+    "LUCJEnergy",
+    "LinearOperator",
+    "UCJOpSpinBalanced",
+    "apply_diag_coulomb_evolution",
+    "apply_givens_rotation_in_place",
+    "apply_num_op_sum_evolution",
+    "apply_orbital_rotation",
+    "apply_phase_shift_in_place",
+    "apply_unitary",
+    "contract",
+    "dim",
+    "dims",
+    "hartree_fock_state",
+    "linalg",
+    "linear_operator",
+    "lucj_energy",
+    "random",
+    "states",
+    "vdot",
+]

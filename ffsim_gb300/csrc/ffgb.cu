@@ -1,0 +1,1112 @@
+// Host orchestration and the C ABI (include/ffsim_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/ffsim_gb300.h"
+#include "common.h"
+#include "plan.h"
+
+namespace ffgb {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+static long long binom_h(int n, int k) {
+  if (k < 0 || n < 0 || k > n) return 0;
+  long long r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// per-device occupation-string tables
+// ---------------------------------------------------------------------------
+static std::mutex g_mu;
+static std::map<std::tuple<int, int, int>, unsigned*> g_strings;
+
+static int device_strings(int norb, int nocc, const unsigned** out) {
+  int dev = 0;
+  FFGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto key = std::make_tuple(dev, norb, nocc);
+  auto it = g_strings.find(key);
+  if (it != g_strings.end()) {
+    *out = it->second;
+    return FFGB_OK;
+  }
+  const long long n = binom_h(norb, nocc);
+  std::vector<unsigned> h((size_t)std::max<long long>(n, 1), 0u);
+  if (nocc == 0) {
+    h[0] = 0u;
+  } else {
+    unsigned x = (nocc >= 32) ? 0xffffffffu : ((1u << nocc) - 1u);
+    for (long long a = 0; a < n; ++a) {
+      h[(size_t)a] = x;
+      // next integer with the same popcount (ascending order)
+      unsigned c = x & (0u - x), r = x + c;
+      x = (((r ^ x) >> 2) / c) | r;
+    }
+  }
+  unsigned* d = nullptr;
+  FFGB_CUDA(cudaMalloc(&d, h.size() * sizeof(unsigned)));
+  FFGB_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
+  g_strings[key] = d;
+  *out = d;
+  return FFGB_OK;
+}
+
+static int num_sms() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 132;
+  }
+  return sms;
+}
+
+// ---------------------------------------------------------------------------
+// scratch carving
+// ---------------------------------------------------------------------------
+struct Scratch {
+  char* base;
+  size_t bytes, off = 0;
+  Scratch(void* b, size_t n) : base((char*)b), bytes(n) {}
+  void* take(size_t n) {
+    size_t o = (off + 255) & ~(size_t)255;
+    if (base == nullptr || o + n > bytes) return nullptr;
+    off = o + n;
+    return base + o;
+  }
+};
+
+static size_t extras_bytes(int norb, int na, int nb) {
+  long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;
+  long long m = std::max<long long>(std::max(da, db), 1);
+  return (size_t)m * 16 + (size_t)m * 8 + 4096 + 2048;
+}
+
+// ---------------------------------------------------------------------------
+// diagonal operator description (host)
+// ---------------------------------------------------------------------------
+struct DiagSpec {
+  int mode = DIAG_NONE;
+  int zrep = 0;
+  double row_same[FFGB_MAXN][FFGB_MAXN];
+  double col_same[FFGB_MAXN][FFGB_MAXN];
+  double cross[FFGB_MAXN][FFGB_MAXN];
+  DiagSpec() {
+    std::memset(row_same, 0, sizeof(row_same));
+    std::memset(col_same, 0, sizeof(col_same));
+    std::memset(cross, 0, sizeof(cross));
+  }
+  DiagSpec transposed() const {
+    DiagSpec d;
+    d.mode = mode;
+    d.zrep = zrep;
+    std::memcpy(d.row_same, col_same, sizeof(row_same));
+    std::memcpy(d.col_same, row_same, sizeof(col_same));
+    for (int i = 0; i < FFGB_MAXN; ++i)
+      for (int l = 0; l < FFGB_MAXN; ++l) d.cross[i][l] = cross[l][i];
+    return d;
+  }
+};
+
+// Diagonal Coulomb operator sum J^{st}_ij n_is n_jt / 2 (num rep) or the
+// Z-rep form, scaled by `scale`; rows = alpha, columns = beta.
+static DiagSpec diag_coulomb_spec(int norb, const double* aa, const double* ab, const double* bb,
+                                  int zrep, double scale, int mode) {
+  DiagSpec d;
+  d.mode = mode;
+  d.zrep = zrep;
+  const double f = zrep ? 0.25 * scale : scale;
+  for (int i = 0; i < norb; ++i)
+    for (int j = i; j < norb; ++j) {
+      double w = (i == j) ? (zrep ? 0.0 : 0.5) : 1.0;
+      if (aa) d.row_same[i][j] = f * w * aa[i * norb + j];
+      if (bb) d.col_same[i][j] = f * w * bb[i * norb + j];
+    }
+  if (ab)
+    for (int i = 0; i < norb; ++i)
+      for (int j = 0; j < norb; ++j) d.cross[i][j] = f * ab[i * norb + j];
+  return d;
+}
+
+static DiagSpec one_body_spec(int norb, const double* ca, const double* cb, double scale, int mode) {
+  DiagSpec d;
+  d.mode = mode;
+  for (int i = 0; i < norb; ++i) {
+    if (ca) d.row_same[i][i] = scale * ca[i];
+    if (cb) d.col_same[i][i] = scale * cb[i];
+  }
+  return d;
+}
+
+static void add_spec(DiagSpec& d, const DiagSpec& e) {
+  for (int i = 0; i < FFGB_MAXN; ++i)
+    for (int j = 0; j < FFGB_MAXN; ++j) {
+      d.row_same[i][j] += e.row_same[i][j];
+      d.col_same[i][j] += e.col_same[i][j];
+      d.cross[i][j] += e.cross[i][j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// one pass of the sector kernel
+// ---------------------------------------------------------------------------
+template <typename T>
+struct PassArgs {
+  const SectorPlan* plan = nullptr;  // plan of the rotated sector (null = identity)
+  int norb = 0, rot_nocc = 0, row_nocc = 0;
+  long long n_rows = 1;
+  const void* in = nullptr;
+  void* out = nullptr;
+  int out_op = OUT_STORE, layout = LAYOUT_SAME;
+  double alpha = 1.0;
+  const DiagSpec* diag = nullptr;
+  bool apply_dphase = true;
+  double* partials = nullptr;  // EXPECT
+  int* n_ctas = nullptr;
+};
+
+template <typename T>
+static int dispatch_sector(int nw, const SectorParams<T>& P, int grid, int block, int smem,
+                           cudaStream_t st) {
+  if constexpr (sizeof(T) == 8) {
+    return launch_sector<T, 0>(P, grid, block, smem, st);
+  } else {
+    switch (nw) {
+      case 0: return launch_sector<T, 0>(P, grid, block, smem, st);
+      case 1: return launch_sector<T, 1>(P, grid, block, smem, st);
+      case 2: return launch_sector<T, 2>(P, grid, block, smem, st);
+      case 3: return launch_sector<T, 3>(P, grid, block, smem, st);
+      case 4: return launch_sector<T, 4>(P, grid, block, smem, st);
+      case 5: return launch_sector<T, 5>(P, grid, block, smem, st);
+      case 6: return launch_sector<T, 6>(P, grid, block, smem, st);
+      case 7: return launch_sector<T, 7>(P, grid, block, smem, st);
+      case 8: return launch_sector<T, 8>(P, grid, block, smem, st);
+      case 9: return launch_sector<T, 9>(P, grid, block, smem, st);
+      case 10: return launch_sector<T, 10>(P, grid, block, smem, st);
+      case 11: return launch_sector<T, 11>(P, grid, block, smem, st);
+      case 12: return launch_sector<T, 12>(P, grid, block, smem, st);
+      case 13: return launch_sector<T, 13>(P, grid, block, smem, st);
+      case 14: return launch_sector<T, 14>(P, grid, block, smem, st);
+      case 15: return launch_sector<T, 15>(P, grid, block, smem, st);
+      case 16: return launch_sector<T, 16>(P, grid, block, smem, st);
+      default: return fail(FFGB_ERR_UNSUPPORTED, "no window kernel for this norb");
+    }
+  }
+}
+
+template <typename T>
+static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const int norb = A.norb;
+  if (norb > FFGB_MAXN) return fail(FFGB_ERR_UNSUPPORTED, "norb > 18 is not supported");
+  const long long dim_ll = binom_h(norb, A.rot_nocc);
+  if (dim_ll <= 0 || A.n_rows <= 0) return FFGB_OK;
+  const int dim = (int)dim_ll;
+  auto P = std::make_unique<SectorParams<T>>();
+  std::memset(P.get(), 0, sizeof(SectorParams<T>));
+  P->norb = norb;
+  P->nocc = A.rot_nocc;
+  P->dim = dim;
+  P->kind = KIND_IDENTITY;
+  int nw = 0;
+  if (A.plan && A.plan->kind != PLAN_IDENTITY) {
+    const SectorPlan& pl = *A.plan;
+    P->kind = pl.kind;
+    P->h = pl.h;
+    if (pl.kind == PLAN_TRIANGLE) {
+      P->n_tri = (int)pl.tri.size();
+      for (size_t g = 0; g < pl.tri.size(); ++g) {
+        P->tri[3 * g] = (T)pl.tri[g].c;
+        P->tri[3 * g + 1] = (T)pl.tri[g].s.real();
+        P->tri[3 * g + 2] = (T)pl.tri[g].s.imag();
+        P->tri_l[g] = (signed char)pl.tri_l[g];
+      }
+    } else {
+      auto put = [&](int w, const std::vector<Givens>& v) {
+        for (size_t g = 0; g < v.size(); ++g) {
+          P->win[w][3 * g] = (T)v[g].c;
+          P->win[w][3 * g + 1] = (T)v[g].s.real();
+          P->win[w][3 * g + 2] = (T)v[g].s.imag();
+        }
+      };
+      if (pl.kind == PLAN_FULL) {
+        put(0, pl.tri);
+      } else {
+        put(0, pl.b1);
+        put(1, pl.b2);
+        put(2, pl.a1);
+        put(3, pl.a2);
+        for (size_t i = 0; i < pl.cs.size(); ++i) {
+          const Pair2& p = pl.cs[i];
+          T* c = P->cs[i];
+          c[0] = (T)p.g00.real(); c[1] = (T)p.g00.imag();
+          c[2] = (T)p.g01.real(); c[3] = (T)p.g01.imag();
+          c[4] = (T)p.g10.real(); c[5] = (T)p.g10.imag();
+          c[6] = (T)p.g11.real(); c[7] = (T)p.g11.imag();
+        }
+      }
+      nw = norb;
+    }
+    if (A.apply_dphase) {
+      bool trivial = true;
+      for (int i = 0; i < norb; ++i) {
+        P->dphase[i][0] = (T)pl.diag[i].real();
+        P->dphase[i][1] = (T)pl.diag[i].imag();
+        if (std::abs(pl.diag[i] - cd(1.0)) > 1e-15) trivial = false;
+      }
+      P->has_dphase = trivial ? 0 : 1;
+    }
+  }
+  if (sizeof(T) == 8 && nw != 0) return fail(FFGB_ERR_ARG, "window plan requested for complex128");
+  const int diag_mode = A.diag ? A.diag->mode : DIAG_NONE;
+  P->n_rows = A.n_rows;
+  P->in = A.in;
+  P->out = A.out;
+  P->out_op = A.out_op;
+  P->layout = A.layout;
+  P->alpha_re = (T)A.alpha;
+  P->alpha_im = (T)0;
+  P->diag_mode = diag_mode;
+  P->chunk_bits = norb > 8 ? 8 : 4;
+  const bool need_col = P->has_dphase || diag_mode != DIAG_NONE;
+  if (need_col) {
+    const unsigned* cs = nullptr;
+    FFGB_TRY(device_strings(norb, A.rot_nocc, &cs));
+    P->col_strings = cs;
+  }
+  if (diag_mode != DIAG_NONE) {
+    const unsigned* rs = nullptr;
+    FFGB_TRY(device_strings(norb, A.row_nocc, &rs));
+    P->row_strings = rs;
+    P->row_norb = norb;
+    P->row_nocc = A.row_nocc;
+    P->zrep = A.diag->zrep;
+    std::memcpy(P->rsame, A.diag->row_same, sizeof(P->rsame));
+    std::memcpy(P->cross, A.diag->cross, sizeof(P->cross));
+    bool col_nonzero = false;
+    for (int i = 0; i < FFGB_MAXN && !col_nonzero; ++i)
+      for (int j = 0; j < FFGB_MAXN; ++j)
+        if (A.diag->col_same[i][j] != 0.0) col_nonzero = true;
+    if (col_nonzero) {
+      void* tab = scr.take((size_t)dim * sizeof(C));
+      double* same = (double*)scr.take(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
+      if (!tab || !same) return fail(FFGB_ERR_OOM, "scratch too small for the column table");
+      FFGB_CUDA(cudaMemcpyAsync(same, A.diag->col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN,
+                                cudaMemcpyHostToDevice, st));
+      col_table_kernel<T><<<(dim + 255) / 256, 256, 0, st>>>(P->col_strings, dim, norb, P->zrep,
+                                                             diag_mode, same, tab);
+      FFGB_CUDA(cudaGetLastError());
+      P->col_table = tab;
+    }
+  }
+  // rows per CTA
+  const int block = nw > 0 ? 192 : 256;
+  const size_t row_bytes = (size_t)dim * sizeof(C);
+  const Layout L0 = make_layout(sizeof(T), 0, dim, norb, P->chunk_bits, P->has_dphase, diag_mode);
+  const long long budget = 110 * 1024;
+  long long rmax = (budget - L0.total) / (long long)row_bytes;
+  if (rmax < 1) {
+    if ((long long)L0.total + (long long)row_bytes > 227 * 1024)
+      return fail(FFGB_ERR_UNSUPPORTED, "a sector row does not fit in shared memory");
+    rmax = 1;
+  }
+  const long long want = std::max<long long>(1, (A.n_rows + 2LL * num_sms() - 1) / (2LL * num_sms()));
+  int R = (int)std::min<long long>(std::min<long long>(rmax, want), 4096);
+  if (R < 1) R = 1;
+  P->rows_per_cta = R;
+  const Layout L = make_layout(sizeof(T), R, dim, norb, P->chunk_bits, P->has_dphase, diag_mode);
+  const long long grid = (A.n_rows + R - 1) / R;
+  if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "grid too large");
+  if (A.out_op == OUT_EXPECT) {
+    if (!A.partials) return fail(FFGB_ERR_ARG, "missing partials buffer");
+    P->partials = A.partials;
+  }
+  if (A.n_ctas) *A.n_ctas = (int)grid;
+  return dispatch_sector<T>(nw, *P, (int)grid, block, L.total, st);
+}
+
+// ---------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------
+static std::vector<cd> load_mat(const double* m, int n) {
+  std::vector<cd> v((size_t)n * n);
+  for (size_t i = 0; i < v.size(); ++i) v[i] = cd(m[2 * i], m[2 * i + 1]);
+  return v;
+}
+static std::vector<cd> dagger(const std::vector<cd>& m, int n) {
+  std::vector<cd> v((size_t)n * n);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) v[(size_t)r * n + c] = std::conj(m[(size_t)c * n + r]);
+  return v;
+}
+static std::vector<cd> matmul(const std::vector<cd>& a, const std::vector<cd>& b, int n) {
+  std::vector<cd> v((size_t)n * n, cd(0));
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < n; ++k) {
+      cd x = a[(size_t)r * n + k];
+      for (int c = 0; c < n; ++c) v[(size_t)r * n + c] += x * b[(size_t)k * n + c];
+    }
+  return v;
+}
+static std::vector<cd> eye(int n) {
+  std::vector<cd> v((size_t)n * n, cd(0));
+  for (int i = 0; i < n; ++i) v[(size_t)i * n + i] = 1.0;
+  return v;
+}
+
+template <typename T>
+static int make_plan(int norb, const std::vector<cd>& V, SectorPlan& plan) {
+  const bool windows = sizeof(T) == 4 && norb <= 16;
+  if (!plan_sector(norb, V.data(), windows, plan)) return fail(FFGB_ERR_NUMERIC, "plan failed");
+  if (plan.max_err > 1e-9) return fail(FFGB_ERR_NUMERIC, "orbital rotation is not unitary");
+  return FFGB_OK;
+}
+
+// Both sectors rotated, state (dim_a, dim_b) in `vec`; the result lands in
+// `vec` (two transposing passes through `tmp`).  Optional diagonal operator
+// applied in the second pass (rows = beta).
+template <typename T>
+static int rotate_both(void* vec, void* tmp, int norb, int na, int nb, const SectorPlan* pa,
+                       const SectorPlan* pb, const DiagSpec* diag_ab, Scratch& scr,
+                       cudaStream_t st) {
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  PassArgs<T> A;
+  A.plan = pb;
+  A.norb = norb;
+  A.rot_nocc = nb;
+  A.row_nocc = na;
+  A.n_rows = da;
+  A.in = vec;
+  A.out = tmp;
+  A.layout = LAYOUT_T;
+  FFGB_TRY(run_pass<T>(A, scr, st));
+  DiagSpec dt;
+  PassArgs<T> B;
+  B.plan = pa;
+  B.norb = norb;
+  B.rot_nocc = na;
+  B.row_nocc = nb;
+  B.n_rows = db;
+  B.in = tmp;
+  B.out = vec;
+  B.layout = LAYOUT_T;
+  if (diag_ab) {
+    dt = diag_ab->transposed();
+    B.diag = &dt;
+  }
+  return run_pass<T>(B, scr, st);
+}
+
+template <typename T>
+static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const double* ma,
+                                 const double* mb, Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  if (nb < 0) {  // spinless
+    if (!ma) return FFGB_OK;
+    SectorPlan p;
+    FFGB_TRY(make_plan<T>(norb, load_mat(ma, norb), p));
+    PassArgs<T> A;
+    A.plan = &p;
+    A.norb = norb;
+    A.rot_nocc = na;
+    A.row_nocc = 0;
+    A.n_rows = 1;
+    A.in = vec;
+    A.out = vec;
+    return run_pass<T>(A, scr, st);
+  }
+  SectorPlan pa, pb;
+  if (ma) FFGB_TRY(make_plan<T>(norb, load_mat(ma, norb), pa));
+  if (mb) FFGB_TRY(make_plan<T>(norb, load_mat(mb, norb), pb));
+  if (!ma && !mb) return FFGB_OK;
+  if (!ma) {  // beta only: rows are alpha strings, in place
+    PassArgs<T> A;
+    A.plan = &pb;
+    A.norb = norb;
+    A.rot_nocc = nb;
+    A.row_nocc = na;
+    A.n_rows = binom_h(norb, na);
+    A.in = vec;
+    A.out = vec;
+    return run_pass<T>(A, scr, st);
+  }
+  const size_t S = (size_t)binom_h(norb, na) * binom_h(norb, nb) * sizeof(C);
+  void* tmp = scr.take(S);
+  if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  return rotate_both<T>(vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, nullptr, scr, st);
+}
+
+// W(U) D W(U)^dag vec with D a diagonal phase operator (evolution)
+template <typename T>
+static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSpec& spec,
+                               const double* rot_a, const double* rot_b, Scratch& scr,
+                               cudaStream_t st) {
+  using C = typename CT<T>::type;
+  if (nb < 0) {  // spinless: one row
+    SectorPlan pu, pd;
+    if (rot_a) {
+      auto U = load_mat(rot_a, norb);
+      FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pd));
+      FFGB_TRY(make_plan<T>(norb, U, pu));
+    }
+    DiagSpec d = spec;
+    std::memcpy(d.col_same, spec.row_same, sizeof(d.col_same));
+    std::memset(d.row_same, 0, sizeof(d.row_same));
+    std::memset(d.cross, 0, sizeof(d.cross));
+    PassArgs<T> A;
+    A.plan = rot_a ? &pd : nullptr;
+    A.norb = norb;
+    A.rot_nocc = na;
+    A.row_nocc = 0;
+    A.n_rows = 1;
+    A.in = vec;
+    A.out = vec;
+    A.diag = &d;
+    FFGB_TRY(run_pass<T>(A, scr, st));
+    if (rot_a) {
+      PassArgs<T> B = A;
+      B.plan = &pu;
+      B.diag = nullptr;
+      FFGB_TRY(run_pass<T>(B, scr, st));
+    }
+    return FFGB_OK;
+  }
+  const long long da = binom_h(norb, na);
+  if (!rot_a && !rot_b) {
+    PassArgs<T> A;
+    A.norb = norb;
+    A.rot_nocc = nb;
+    A.row_nocc = na;
+    A.n_rows = da;
+    A.in = vec;
+    A.out = vec;
+    A.diag = &spec;
+    return run_pass<T>(A, scr, st);
+  }
+  SectorPlan pad, pbd, pau, pbu;
+  if (rot_a) {
+    auto U = load_mat(rot_a, norb);
+    FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pad));
+    FFGB_TRY(make_plan<T>(norb, U, pau));
+  }
+  if (rot_b) {
+    auto U = load_mat(rot_b, norb);
+    FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pbd));
+    FFGB_TRY(make_plan<T>(norb, U, pbu));
+  }
+  const size_t S = (size_t)da * binom_h(norb, nb) * sizeof(C);
+  void* tmp = scr.take(S);
+  if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  FFGB_TRY(rotate_both<T>(vec, tmp, norb, na, nb, rot_a ? &pad : nullptr, rot_b ? &pbd : nullptr,
+                          &spec, scr, st));
+  return rotate_both<T>(vec, tmp, norb, na, nb, rot_a ? &pau : nullptr, rot_b ? &pbu : nullptr,
+                        nullptr, scr, st);
+}
+
+// out (+)= W(rot) Z W(rot)^dag vec, Z real diagonal
+template <typename T>
+static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int nb,
+                               const DiagSpec& spec, const std::vector<cd>* rot, int accumulate,
+                               Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  if (!rot) {
+    PassArgs<T> A;
+    A.norb = norb;
+    A.rot_nocc = nb;
+    A.row_nocc = na;
+    A.n_rows = da;
+    A.in = vec;
+    A.out = out;
+    A.out_op = accumulate ? OUT_ACCUM : OUT_STORE;
+    A.diag = &spec;
+    return run_pass<T>(A, scr, st);
+  }
+  SectorPlan pd, pu;
+  FFGB_TRY(make_plan<T>(norb, dagger(*rot, norb), pd));
+  FFGB_TRY(make_plan<T>(norb, *rot, pu));
+  const size_t S = (size_t)da * db * sizeof(C);
+  void* t1 = scr.take(S);
+  void* t2 = scr.take(S);
+  if (!t1 || !t2) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
+  PassArgs<T> A;
+  A.norb = norb;
+  A.layout = LAYOUT_T;
+  A.plan = &pd;
+  A.rot_nocc = nb;
+  A.row_nocc = na;
+  A.n_rows = da;
+  A.in = vec;
+  A.out = t1;
+  FFGB_TRY(run_pass<T>(A, scr, st));
+  DiagSpec dt = spec.transposed();
+  PassArgs<T> B = A;
+  B.plan = &pd;
+  B.rot_nocc = na;
+  B.row_nocc = nb;
+  B.n_rows = db;
+  B.in = t1;
+  B.out = t2;
+  B.diag = &dt;
+  FFGB_TRY(run_pass<T>(B, scr, st));
+  A.plan = &pu;
+  A.in = t2;
+  A.out = t1;
+  FFGB_TRY(run_pass<T>(A, scr, st));
+  B.plan = &pu;
+  B.in = t1;
+  B.out = out;
+  B.diag = nullptr;
+  B.out_op = accumulate ? OUT_ACCUM : OUT_STORE;
+  return run_pass<T>(B, scr, st);
+}
+
+// <vec| W(V)^dag... : sum z |W(V) vec|^2 into dslot (device double)
+template <typename T>
+static int expectation_term(const void* vec, int norb, int na, int nb, const DiagSpec& spec,
+                            const std::vector<cd>& V, void* tmp, double* dslot, Scratch& scr,
+                            cudaStream_t st) {
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  SectorPlan pv;
+  FFGB_TRY(make_plan<T>(norb, V, pv));
+  const size_t mark = scr.off;
+  PassArgs<T> A;
+  A.norb = norb;
+  A.layout = LAYOUT_T;
+  A.plan = &pv;
+  A.rot_nocc = nb;
+  A.row_nocc = na;
+  A.n_rows = da;
+  A.in = vec;
+  A.out = tmp;
+  A.apply_dphase = false;  // |phi|^2 does not see the final orbital phases
+  FFGB_TRY(run_pass<T>(A, scr, st));
+  double* partials = (double*)scr.take(sizeof(double) * (size_t)std::max<long long>(db, 1));
+  if (!partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
+  DiagSpec dt = spec.transposed();
+  PassArgs<T> B = A;
+  B.rot_nocc = na;
+  B.row_nocc = nb;
+  B.n_rows = db;
+  B.in = tmp;
+  B.out = nullptr;
+  B.out_op = OUT_EXPECT;
+  B.diag = &dt;
+  B.partials = partials;
+  int nct = 0;
+  B.n_ctas = &nct;
+  FFGB_TRY(run_pass<T>(B, scr, st));
+  reduce_partials_kernel<<<1, 256, 0, st>>>(partials, nct, dslot, 0);
+  FFGB_CUDA(cudaGetLastError());
+  scr.off = mark;
+  return FFGB_OK;
+}
+
+// DF Hamiltonian terms as (Z spec, rotation V = term basis)
+struct Term {
+  DiagSpec spec;
+  std::vector<cd> rot;  // U (the linop is U Z U^dag)
+};
+
+static int df_terms(int norb, const double* one_body, int n_terms, const double* dcm,
+                    const double* rots, int zrep, std::vector<Term>& terms) {
+  terms.clear();
+  if (one_body) {
+    std::vector<cd> K = load_mat(one_body, norb);
+    std::vector<double> w;
+    std::vector<cd> vecs;
+    hermitian_eigh(norb, K.data(), w, vecs);
+    Term t;
+    t.spec = one_body_spec(norb, w.data(), w.data(), 1.0, DIAG_COEF);
+    t.rot = vecs;
+    terms.push_back(std::move(t));
+  }
+  for (int k = 0; k < n_terms; ++k) {
+    const double* J = dcm + (size_t)k * norb * norb;
+    Term t;
+    t.spec = diag_coulomb_spec(norb, J, J, J, zrep, 1.0, DIAG_COEF);
+    t.rot = load_mat(rots + (size_t)k * norb * norb * 2, norb);
+    terms.push_back(std::move(t));
+  }
+  return FFGB_OK;
+}
+
+static int check_shape(int dtype, int norb, int na, int nb) {
+  if (dtype != FFGB_C64 && dtype != FFGB_C128) return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
+  if (norb < 0 || norb > FFGB_MAXN) return fail(FFGB_ERR_UNSUPPORTED, "norb must be in [0, 18]");
+  if (na < 0 || na > norb || nb > norb) return fail(FFGB_ERR_ARG, "invalid electron numbers");
+  return FFGB_OK;
+}
+
+}  // namespace ffgb
+
+using namespace ffgb;
+
+template <typename T>
+static int givens_impl(void* vec, int norb, int na, int nb, int spin, double c, double sr, double si,
+                       int i, int j, cudaStream_t st) {
+  if (std::abs(i - j) != 1) return fail(FFGB_ERR_ARG, "Target orbitals must be adjacent.");
+  if (i < 0 || j < 0 || i >= norb || j >= norb) return fail(FFGB_ERR_ARG, "orbital index out of range");
+  const int nocc = spin == 0 ? na : nb;
+  const long long dim_other = nb < 0 ? 1 : binom_h(norb, spin == 0 ? nb : na);
+  // the kernel rotates (x: lower orbital occupied, y: upper occupied) with
+  // x <- c x + s y; the reference's slice1 holds strings with i occupied
+  double s_re = sr, s_im = si;
+  if (i > j) {  // slice1 = upper orbital occupied: s' = -conj(s)
+    s_re = -sr;
+    s_im = si;
+  }
+  const int l = std::min(i, j);
+  const long long npairs = binom_h(norb - 2, nocc - 1);
+  const long long total = npairs * dim_other;
+  if (total <= 0) return FFGB_OK;
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 8192);
+  givens_sector_kernel<T><<<blocks, 256, 0, st>>>((typename CT<T>::type*)vec, norb, nocc, dim_other,
+                                                  nb < 0 ? 1 : spin, l, (T)c, (T)s_re, (T)s_im);
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+
+template <typename T>
+static int df_expectation_impl(const void* vec, int norb, int na, int nb, const std::vector<Term>& terms,
+                               const std::vector<cd>* pre, double constant, double* energy,
+                               Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const size_t S = (size_t)binom_h(norb, na) * binom_h(norb, nb) * sizeof(C);
+  void* tmp = scr.take(S);
+  double* slots = (double*)scr.take(sizeof(double) * (terms.size() + 1));
+  if (!tmp || !slots) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  for (size_t k = 0; k < terms.size(); ++k) {
+    std::vector<cd> V = dagger(terms[k].rot, norb);
+    if (pre) V = matmul(V, *pre, norb);
+    FFGB_TRY(expectation_term<T>(vec, norb, na, nb, terms[k].spec, V, tmp, slots + k, scr, st));
+  }
+  std::vector<double> h(terms.size() + 1, 0.0);
+  if (!terms.empty())
+    FFGB_CUDA(cudaMemcpyAsync(h.data(), slots, sizeof(double) * terms.size(), cudaMemcpyDeviceToHost, st));
+  FFGB_CUDA(cudaStreamSynchronize(st));
+  double e = constant;
+  for (size_t k = 0; k < terms.size(); ++k) e += h[k];
+  *energy = e;
+  return FFGB_OK;
+}
+
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int ffgb_version(void) { return 100; }
+
+const char* ffgb_last_error(void) { return ffgb::g_err.c_str(); }
+
+int ffgb_givens_decomposition(const double* mat, int n, double tol, double* rot_cs, int* rot_ij,
+                              int* n_rot, double* diag) {
+  g_err.clear();
+  if (!mat || n < 0) return fail(FFGB_ERR_ARG, "mat must be a square matrix");
+  std::vector<RefGivens> rots;
+  std::vector<cd> d;
+  reference_givens_decomposition(n, load_mat(mat, n).data(), tol, rots, d);
+  for (size_t k = 0; k < rots.size(); ++k) {
+    rot_cs[3 * k] = rots[k].c;
+    rot_cs[3 * k + 1] = rots[k].s.real();
+    rot_cs[3 * k + 2] = rots[k].s.imag();
+    rot_ij[2 * k] = rots[k].i;
+    rot_ij[2 * k + 1] = rots[k].j;
+  }
+  *n_rot = (int)rots.size();
+  for (int i = 0; i < n; ++i) {
+    diag[2 * i] = d[i].real();
+    diag[2 * i + 1] = d[i].imag();
+  }
+  return FFGB_OK;
+}
+
+int ffgb_eigh(const double* mat, int n, double* eigvals, double* vecs) {
+  g_err.clear();
+  if (!mat || n < 0) return fail(FFGB_ERR_ARG, "invalid matrix");
+  std::vector<double> w;
+  std::vector<cd> v;
+  hermitian_eigh(n, load_mat(mat, n).data(), w, v);
+  for (int i = 0; i < n; ++i) eigvals[i] = w[i];
+  for (size_t i = 0; i < v.size(); ++i) {
+    vecs[2 * i] = v[i].real();
+    vecs[2 * i + 1] = v[i].imag();
+  }
+  return FFGB_OK;
+}
+
+int ffgb_debug_plan(const double* mat, int norb, int use_windows, double* out, int cap, int* len) {
+  g_err.clear();
+  SectorPlan p;
+  if (!plan_sector(norb, load_mat(mat, norb).data(), use_windows != 0, p))
+    return fail(FFGB_ERR_NUMERIC, "plan failed");
+  std::vector<double> o;
+  o.push_back(p.kind);
+  o.push_back(p.h);
+  o.push_back(p.max_err);
+  auto put_g = [&](const std::vector<Givens>& v) {
+    o.push_back((double)v.size());
+    for (auto& g : v) {
+      o.push_back(g.c);
+      o.push_back(g.s.real());
+      o.push_back(g.s.imag());
+    }
+  };
+  put_g(p.tri);
+  put_g(p.b1);
+  put_g(p.b2);
+  put_g(p.a1);
+  put_g(p.a2);
+  o.push_back((double)p.cs.size());
+  for (auto& c : p.cs) {
+    o.push_back(c.i);
+    o.push_back(c.j);
+    for (cd z : {c.g00, c.g01, c.g10, c.g11}) {
+      o.push_back(z.real());
+      o.push_back(z.imag());
+    }
+  }
+  o.push_back((double)p.diag.size());
+  for (cd z : p.diag) {
+    o.push_back(z.real());
+    o.push_back(z.imag());
+  }
+  if ((int)o.size() > cap) return fail(FFGB_ERR_ARG, "output buffer too small");
+  std::memcpy(out, o.data(), o.size() * sizeof(double));
+  *len = (int)o.size();
+  return FFGB_OK;
+}
+
+size_t ffgb_scratch_bytes(int op, int dtype, int norb, int na, int nb) {
+  const size_t el = dtype == FFGB_C128 ? 16 : 8;
+  const long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;
+  const size_t S = (size_t)da * db * el;
+  const size_t ex = extras_bytes(norb, na, nb) + 4096;
+  if (op == 1) return 2 * S + ex;
+  return S + ex;
+}
+
+#define FFGB_DISPATCH(dtype, call_f, call_d) \
+  ((dtype) == FFGB_C64 ? (call_f) : (call_d))
+
+int ffgb_apply_givens_rotation(void* vec, int dtype, int norb, int na, int nb, int spin, double c,
+                               double s_re, double s_im, int i, int j, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (spin != 0 && spin != 1) return fail(FFGB_ERR_ARG, "spin must be 0 (alpha) or 1 (beta)");
+  if (nb < 0 && spin != 0) return fail(FFGB_ERR_ARG, "spinless systems have one sector");
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype, givens_impl<float>(vec, norb, na, nb, spin, c, s_re, s_im, i, j, st),
+                       givens_impl<double>(vec, norb, na, nb, spin, c, s_re, s_im, i, j, st));
+}
+
+int ffgb_apply_phase_shift(void* vec, int dtype, int norb, int na, int nb, int spin, double pr,
+                           double pi, int orb, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (orb < 0 || orb >= norb) return fail(FFGB_ERR_ARG, "orbital index out of range");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nocc = (spin == 0 || nb < 0) ? na : nb;
+  const unsigned* strs = nullptr;
+  FFGB_TRY(device_strings(norb, nocc, &strs));
+  const long long da = binom_h(norb, na), db = nb < 0 ? 1 : binom_h(norb, nb);
+  const int sp = nb < 0 ? 0 : spin;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((da * db + 255) / 256, 8192));
+  if (dtype == FFGB_C64)
+    phase_shift_kernel<float><<<blocks, 256, 0, st>>>((float2*)vec, strs, da, db, sp, orb, (float)pr, (float)pi);
+  else
+    phase_shift_kernel<double><<<blocks, 256, 0, st>>>((double2*)vec, strs, da, db, sp, orb, pr, pi);
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+
+int ffgb_apply_orbital_rotation(void* vec, int dtype, int norb, int na, int nb, const double* ma,
+                                const double* mb, void* scratch, size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype, orbital_rotation_impl<float>(vec, norb, na, nb, ma, mb, scr, st),
+                       orbital_rotation_impl<double>(vec, norb, na, nb, ma, mb, scr, st));
+}
+
+int ffgb_apply_diag_coulomb_evolution(void* vec, int dtype, int norb, int na, int nb,
+                                      const double* aa, const double* ab, const double* bb,
+                                      double time, int zrep, const double* rot_a,
+                                      const double* rot_b, void* scratch, size_t scratch_bytes,
+                                      void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0 && zrep) return fail(FFGB_ERR_UNSUPPORTED, "Z representation needs a spinful system");
+  DiagSpec spec = diag_coulomb_spec(norb, aa, nb < 0 ? nullptr : ab, nb < 0 ? nullptr : bb, zrep,
+                                    -time, DIAG_PHASE);
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype,
+                       diag_evolution_impl<float>(vec, norb, na, nb, spec, rot_a, rot_b, scr, st),
+                       diag_evolution_impl<double>(vec, norb, na, nb, spec, rot_a, rot_b, scr, st));
+}
+
+int ffgb_apply_num_op_sum_evolution(void* vec, int dtype, int norb, int na, int nb,
+                                    const double* ca, const double* cb, double time,
+                                    const double* rot_a, const double* rot_b, void* scratch,
+                                    size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  DiagSpec spec = one_body_spec(norb, ca, nb < 0 ? nullptr : cb, -time, DIAG_PHASE);
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype,
+                       diag_evolution_impl<float>(vec, norb, na, nb, spec, rot_a, rot_b, scr, st),
+                       diag_evolution_impl<double>(vec, norb, na, nb, spec, rot_a, rot_b, scr, st));
+}
+
+int ffgb_ucj_spin_balanced_apply(void* vec, int dtype, int norb, int na, int nb, int n_reps,
+                                 const double* dcm, const double* rots, const double* final_rot,
+                                 void* scratch, size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "spin-balanced UCJ needs a spinful system");
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t el = dtype == FFGB_C128 ? 16 : 8;
+  void* tmp = scr.take((size_t)binom_h(norb, na) * binom_h(norb, nb) * el);
+  if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  std::vector<cd> current = eye(norb);
+  for (int k = 0; k < n_reps; ++k) {
+    std::vector<cd> U = load_mat(rots + (size_t)k * norb * norb * 2, norb);
+    std::vector<cd> V = matmul(dagger(U, norb), current, norb);
+    const double* J = dcm + (size_t)k * 2 * norb * norb;
+    DiagSpec spec = diag_coulomb_spec(norb, J, J + norb * norb, J, 0, 1.0, DIAG_PHASE);
+    SectorPlan p;
+    int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
+    if (s) return s;
+    s = dtype == FFGB_C64 ? rotate_both<float>(vec, tmp, norb, na, nb, &p, &p, &spec, scr, st)
+                          : rotate_both<double>(vec, tmp, norb, na, nb, &p, &p, &spec, scr, st);
+    if (s) return s;
+    current = U;
+  }
+  std::vector<cd> V = final_rot ? matmul(load_mat(final_rot, norb), current, norb) : current;
+  SectorPlan p;
+  int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
+  if (s) return s;
+  return dtype == FFGB_C64 ? rotate_both<float>(vec, tmp, norb, na, nb, &p, &p, nullptr, scr, st)
+                           : rotate_both<double>(vec, tmp, norb, na, nb, &p, &p, nullptr, scr, st);
+}
+
+int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, int na, int nb,
+                               const double* aa, const double* ab, const double* bb, int zrep,
+                               int accumulate, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "contraction needs a spinful system");
+  DiagSpec spec = diag_coulomb_spec(norb, aa, ab, bb, zrep, 1.0, DIAG_COEF);
+  char buf[1];
+  Scratch scr(nullptr, 0);
+  (void)buf;
+  cudaStream_t st = (cudaStream_t)stream;
+  // the column table needs scratch; use a small internal allocation per call
+  const size_t need = (size_t)binom_h(norb, nb) * 16 + 8192;
+  void* tmp = nullptr;
+  FFGB_CUDA(cudaMallocAsync(&tmp, need, st));
+  Scratch s2(tmp, need);
+  int s = FFGB_DISPATCH(dtype, rotated_matvec_impl<float>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st),
+                        rotated_matvec_impl<double>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st));
+  cudaFreeAsync(tmp, st);
+  return s;
+}
+
+int ffgb_contract_num_op_sum(const void* vec, void* out, int dtype, int norb, int na, int nb,
+                             const double* coeffs, int accumulate, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "contraction needs a spinful system");
+  DiagSpec spec = one_body_spec(norb, coeffs, coeffs, 1.0, DIAG_COEF);
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t need = (size_t)binom_h(norb, nb) * 16 + 8192;
+  void* tmp = nullptr;
+  FFGB_CUDA(cudaMallocAsync(&tmp, need, st));
+  Scratch s2(tmp, need);
+  int s = FFGB_DISPATCH(dtype, rotated_matvec_impl<float>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st),
+                        rotated_matvec_impl<double>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st));
+  cudaFreeAsync(tmp, st);
+  return s;
+}
+
+int ffgb_rotated_diag_matvec(const void* vec, void* out, int dtype, int norb, int na, int nb,
+                             const double* one_body, const double* mat, int zrep, const double* rot,
+                             int accumulate, void* scratch, size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "linear operator needs a spinful system");
+  DiagSpec spec;
+  spec.mode = DIAG_COEF;
+  if (mat) spec = diag_coulomb_spec(norb, mat, mat, mat, zrep, 1.0, DIAG_COEF);
+  if (one_body) add_spec(spec, one_body_spec(norb, one_body, one_body, 1.0, DIAG_COEF));
+  std::vector<cd> R;
+  if (rot) R = load_mat(rot, norb);
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype,
+                       rotated_matvec_impl<float>(vec, out, norb, na, nb, spec, rot ? &R : nullptr, accumulate, scr, st),
+                       rotated_matvec_impl<double>(vec, out, norb, na, nb, spec, rot ? &R : nullptr, accumulate, scr, st));
+}
+
+int ffgb_df_matvec(const void* vec, void* out, int dtype, int norb, int na, int nb,
+                   const double* one_body, int n_terms, const double* dcm, const double* rots,
+                   double constant, int zrep, void* scratch, size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "linear operator needs a spinful system");
+  if (vec == out) return fail(FFGB_ERR_ARG, "out must not alias vec");
+  std::vector<Term> terms;
+  df_terms(norb, one_body, n_terms, dcm, rots, zrep, terms);
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = binom_h(norb, na) * binom_h(norb, nb);
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+  if (dtype == FFGB_C64)
+    scale_copy_kernel<float><<<blocks, 256, 0, st>>>((const float2*)vec, (float2*)out, n, (float)constant, 0.f);
+  else
+    scale_copy_kernel<double><<<blocks, 256, 0, st>>>((const double2*)vec, (double2*)out, n, constant, 0.0);
+  FFGB_CUDA(cudaGetLastError());
+  for (const Term& t : terms) {
+    const size_t mark = scr.off;
+    int s = FFGB_DISPATCH(dtype,
+                          rotated_matvec_impl<float>(vec, out, norb, na, nb, t.spec, &t.rot, 1, scr, st),
+                          rotated_matvec_impl<double>(vec, out, norb, na, nb, t.spec, &t.rot, 1, scr, st));
+    if (s) return s;
+    scr.off = mark;
+  }
+  return FFGB_OK;
+}
+
+int ffgb_df_expectation(const void* vec, int dtype, int norb, int na, int nb, const double* one_body,
+                        int n_terms, const double* dcm, const double* rots, double constant,
+                        int zrep, const double* pre_rotation, double* energy_out, void* scratch,
+                        size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "expectation needs a spinful system");
+  std::vector<Term> terms;
+  df_terms(norb, one_body, n_terms, dcm, rots, zrep, terms);
+  std::vector<cd> pre;
+  if (pre_rotation) pre = load_mat(pre_rotation, norb);
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype,
+                       df_expectation_impl<float>(vec, norb, na, nb, terms, pre_rotation ? &pre : nullptr, constant, energy_out, scr, st),
+                       df_expectation_impl<double>(vec, norb, na, nb, terms, pre_rotation ? &pre : nullptr, constant, energy_out, scr, st));
+}
+
+int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na, int nb, int n_reps,
+                     const double* ucj_dcm, const double* ucj_rots, const double* ucj_final,
+                     const double* one_body, int n_terms, const double* dcm, const double* rots,
+                     double constant, double* energy_out, void* scratch, size_t scratch_bytes,
+                     void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "LUCJ energy needs a spinful system");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t el = dtype == FFGB_C128 ? 16 : 8;
+  const long long n = binom_h(norb, na) * binom_h(norb, nb);
+  if (vec_in) {
+    FFGB_CUDA(cudaMemcpyAsync(work, vec_in, (size_t)n * el, cudaMemcpyDeviceToDevice, st));
+  } else {
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+    if (dtype == FFGB_C64)
+      one_hot_kernel<float><<<blocks, 256, 0, st>>>((float2*)work, n);
+    else
+      one_hot_kernel<double><<<blocks, 256, 0, st>>>((double2*)work, n);
+    FFGB_CUDA(cudaGetLastError());
+  }
+  Scratch scr(scratch, scratch_bytes);
+  void* tmp = scr.take((size_t)n * el);
+  if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  std::vector<cd> current = eye(norb);
+  for (int k = 0; k < n_reps; ++k) {
+    std::vector<cd> U = load_mat(ucj_rots + (size_t)k * norb * norb * 2, norb);
+    std::vector<cd> V = matmul(dagger(U, norb), current, norb);
+    const double* J = ucj_dcm + (size_t)k * 2 * norb * norb;
+    DiagSpec spec = diag_coulomb_spec(norb, J, J + norb * norb, J, 0, 1.0, DIAG_PHASE);
+    SectorPlan p;
+    int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
+    if (s) return s;
+    s = dtype == FFGB_C64 ? rotate_both<float>(work, tmp, norb, na, nb, &p, &p, &spec, scr, st)
+                          : rotate_both<double>(work, tmp, norb, na, nb, &p, &p, &spec, scr, st);
+    if (s) return s;
+    current = U;
+  }
+  std::vector<cd> final_basis = ucj_final ? matmul(load_mat(ucj_final, norb), current, norb) : current;
+  std::vector<Term> terms;
+  df_terms(norb, one_body, n_terms, dcm, rots, 0, terms);
+  scr.off = 0;
+  return FFGB_DISPATCH(dtype,
+                       df_expectation_impl<float>(work, norb, na, nb, terms, &final_basis, constant, energy_out, scr, st),
+                       df_expectation_impl<double>(work, norb, na, nb, terms, &final_basis, constant, energy_out, scr, st));
+}
+
+int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out, void* stream) {
+  g_err.clear();
+  cudaStream_t st = (cudaStream_t)stream;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 1024));
+  double* part = nullptr;
+  FFGB_CUDA(cudaMallocAsync(&part, sizeof(double) * (2 * blocks + 2), st));
+  if (dtype == FFGB_C64)
+    vdot_kernel<float><<<blocks, 256, 0, st>>>((const float2*)x, (const float2*)y, n, part);
+  else if (dtype == FFGB_C128)
+    vdot_kernel<double><<<blocks, 256, 0, st>>>((const double2*)x, (const double2*)y, n, part);
+  else
+    return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
+  FFGB_CUDA(cudaGetLastError());
+  std::vector<double> h(2 * blocks);
+  FFGB_CUDA(cudaMemcpyAsync(h.data(), part, sizeof(double) * 2 * blocks, cudaMemcpyDeviceToHost, st));
+  FFGB_CUDA(cudaStreamSynchronize(st));
+  cudaFreeAsync(part, st);
+  double a = 0, b = 0;
+  for (int i = 0; i < blocks; ++i) {
+    a += h[2 * i];
+    b += h[2 * i + 1];
+  }
+  out[0] = a;
+  out[1] = b;
+  return FFGB_OK;
+}
+
+int ffgb_hartree_fock(void* vec, int dtype, long long n, void* stream) {
+  g_err.clear();
+  cudaStream_t st = (cudaStream_t)stream;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096));
+  if (dtype == FFGB_C64)
+    one_hot_kernel<float><<<blocks, 256, 0, st>>>((float2*)vec, n);
+  else
+    one_hot_kernel<double><<<blocks, 256, 0, st>>>((double2*)vec, n);
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+
+}  // extern "C"

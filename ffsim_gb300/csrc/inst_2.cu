@@ -1,0 +1,7 @@
+// Explicit instantiations of the sector kernel (split for parallel builds).
+#include "launch.cuh"
+
+namespace ffgb {
+template int launch_sector<float, 13>(const SectorParams<float>&, int, int, int, cudaStream_t);
+template int launch_sector<float, 14>(const SectorParams<float>&, int, int, int, cudaStream_t);
+}  // namespace ffgb

@@ -1,0 +1,708 @@
+// Device code of the sector kernels.
+//
+// A *pass* processes a 2-D array whose rows are complete state vectors of
+// one spin sector (the *rotated* sector, `dim` = C(norb, nocc) entries per
+// row) while the row index enumerates the strings of the other sector.  A
+// CTA stages `rows_per_cta` consecutive rows in shared memory, applies the
+// orbital-rotation plan of the rotated sector to every row, then runs the
+// epilogue: optional final orbital phases, optional diagonal operator
+// (phase exp(i f) or real coefficient f), and an output mode (store in the
+// same layout, store transposed, accumulate, or reduce sum f |v|^2).
+//
+// Storing transposed lets two passes rotate both spin sectors of a
+// (dim_a, dim_b) state with only row-contiguous reads: pass A rotates the
+// beta sector of each alpha row and writes the (dim_b, dim_a) transpose;
+// pass B rotates the alpha sector of each beta row and writes back.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define FFGB_MAXN 18
+#define FFGB_MAXTRI (FFGB_MAXN * (FFGB_MAXN - 1) / 2)
+#define FFGB_BST (FFGB_MAXN + 2)  // stride of the binomial table
+
+namespace ffgb {
+
+enum { OUT_STORE = 0, OUT_ACCUM = 1, OUT_EXPECT = 2, OUT_NONE = 3 };
+enum { LAYOUT_SAME = 0, LAYOUT_T = 1 };
+enum { DIAG_NONE = 0, DIAG_PHASE = 1, DIAG_COEF = 2 };
+enum { KIND_IDENTITY = 0, KIND_TRIANGLE = 1, KIND_FULL = 2, KIND_CSD = 3 };
+
+template <typename T>
+struct CT;
+template <>
+struct CT<float> {
+  using type = float2;
+};
+template <>
+struct CT<double> {
+  using type = double2;
+};
+
+template <typename T>
+struct SectorParams {
+  // rotated sector and its plan
+  int norb, nocc, dim;
+  int kind, h, n_tri;
+  T tri[FFGB_MAXTRI * 3];
+  signed char tri_l[FFGB_MAXTRI];
+  T win[4][28 * 3];
+  T cs[8][8];
+  int has_dphase;
+  T dphase[FFGB_MAXN][2];
+  // rows
+  long long n_rows;
+  int rows_per_cta;
+  int row_norb, row_nocc;
+  const unsigned* row_strings;
+  const unsigned* col_strings;
+  // io
+  const void* in;
+  void* out;
+  int out_op, layout;
+  T alpha_re, alpha_im;
+  // diagonal operator f(r, j) = F_R(r) + F_C(j) + sum_{i,l} cross[i][l] g_i(r) g_l(j)
+  int diag_mode, zrep;
+  double rsame[FFGB_MAXN][FFGB_MAXN];
+  double cross[FFGB_MAXN][FFGB_MAXN];
+  const void* col_table;
+  double* partials;
+  int chunk_bits;
+};
+
+struct Layout {
+  int binom, plan, tab, dt, xt, red, rows, total;
+  int nch, chunk_bits;
+};
+
+__host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
+
+// Shared-memory layout; identical on host and device.
+__host__ __device__ inline Layout make_layout(int tsize, int R, int dim, int col_norb,
+                                              int chunk_bits, int has_dphase, int diag_mode) {
+  Layout L;
+  int off = 0;
+  L.binom = off;
+  off += align16(FFGB_BST * FFGB_BST * 4);
+  L.plan = off;
+  off += align16((FFGB_MAXTRI * 3 + 4 * 28 * 3 + 64 + 2 * FFGB_MAXN) * tsize);
+  L.tab = off;
+  off += align16(256 * 2 + 256 * 4 + 16 * 4);
+  L.chunk_bits = chunk_bits;
+  L.nch = (col_norb + chunk_bits - 1) / chunk_bits;
+  if (L.nch < 1) L.nch = 1;
+  const int nent = L.nch << chunk_bits;
+  L.dt = off;
+  if (has_dphase) off += align16(nent * 2 * tsize);
+  L.xt = off;
+  if (diag_mode == DIAG_PHASE) off += align16(nent * 2 * tsize + 2 * FFGB_MAXN * 8 + 16);
+  if (diag_mode == DIAG_COEF) off += align16(nent * tsize + 2 * FFGB_MAXN * 8 + 16);
+  L.red = off;
+  off += align16(33 * 8);
+  L.rows = off;
+  off += align16(R * dim * 2 * tsize);
+  L.total = off;
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <typename C>
+__device__ __forceinline__ C cmake(double re, double im);
+template <>
+__device__ __forceinline__ float2 cmake<float2>(double re, double im) {
+  return make_float2((float)re, (float)im);
+}
+template <>
+__device__ __forceinline__ double2 cmake<double2>(double re, double im) {
+  return make_double2(re, im);
+}
+
+// exp(i theta) with theta in FP64, rounded once to the output type.
+__device__ __forceinline__ float2 phase_of(double theta, float2*) {
+  const double two_pi = 6.283185307179586476925286766559;
+  double r = theta - two_pi * rint(theta * 0.15915494309189533576888376337251);
+  float hi = (float)r;
+  float lo = (float)(r - (double)hi);
+  float s, c;
+  sincosf(hi, &s, &c);
+  return make_float2(c - s * lo, s + c * lo);
+}
+__device__ __forceinline__ double2 phase_of(double theta, double2*) {
+  double s, c;
+  sincos(theta, &s, &c);
+  return make_double2(c, s);
+}
+
+__device__ __forceinline__ int bn(const int* sB, int a, int b) {
+  return (b < 0 || a < 0 || b > a) ? 0 : sB[a * FFGB_BST + b];
+}
+
+// colexicographic unranking of a k-subset of nbits
+__device__ __forceinline__ unsigned unrank_colex(int t, int nbits, int k, const int* sB) {
+  unsigned s = 0;
+  for (int p = nbits - 1; p >= 0 && k > 0; --p) {
+    int c = bn(sB, p, k);
+    if (t >= c) {
+      s |= 1u << p;
+      t -= c;
+      --k;
+    }
+  }
+  return s;
+}
+
+// colexicographic rank = address among strings with the same popcount
+__device__ __forceinline__ int rank_colex(unsigned s, const int* sB) {
+  int r = 0, t = 0;
+  while (s) {
+    int p = __ffs(s) - 1;
+    s &= s - 1;
+    ++t;
+    r += bn(sB, p, t);
+  }
+  return r;
+}
+
+// rank contribution of bits of s placed at orbital offset `base_orb` with
+// `m0` electrons below them
+__device__ __forceinline__ int rank_shifted(unsigned s, int base_orb, int m0, const int* sB) {
+  int r = 0, t = m0;
+  while (s) {
+    int p = __ffs(s) - 1;
+    s &= s - 1;
+    ++t;
+    r += bn(sB, base_orb + p, t);
+  }
+  return r;
+}
+
+// rotation of a complex64 pair by [[c, s], [-conj(s), c]]:
+// x <- c x + s y, y <- -conj(s) x + c y
+__device__ __forceinline__ void rot_pair(float2& x, float2& y, float c, float sr, float si) {
+  float2 nx, ny;
+  nx.x = fmaf(c, x.x, fmaf(sr, y.x, -si * y.y));
+  nx.y = fmaf(c, x.y, fmaf(sr, y.y, si * y.x));
+  ny.x = fmaf(c, y.x, fmaf(-sr, x.x, -si * x.y));
+  ny.y = fmaf(c, y.y, fmaf(-sr, x.y, si * x.x));
+  x = nx;
+  y = ny;
+}
+
+}  // namespace ffgb
+
+namespace ffgb {
+#include "windows_gen.cuh"
+}
+
+namespace ffgb {
+
+// Distribute work items to warps so that each warp handles 32 items of one
+// class k (the register-array shape depends on k).
+template <class CountF, class Body>
+__device__ __forceinline__ void warp_tasks(int kbeg, int kend, CountF count, Body body) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  int t0 = 0;
+  for (int k = kbeg; k <= kend; ++k) {
+    const int n = count(k);
+    const int nt = (n + 31) >> 5;
+    int first = warp - (t0 % nw);
+    if (first < 0) first += nw;
+    for (int t = first; t < nt; t += nw) {
+      const int item = t * 32 + lane;
+      if (item < n) body(k, item);
+    }
+    t0 += nt;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the sector kernel
+// ---------------------------------------------------------------------------
+
+template <typename T, int NW>
+__global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
+    sector_kernel(const __grid_constant__ SectorParams<T> P) {
+  using C = typename CT<T>::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Layout L = make_layout((int)sizeof(T), P.rows_per_cta, P.dim, P.norb, P.chunk_bits,
+                               P.has_dphase, P.diag_mode);
+  int* sB = (int*)(smem + L.binom);
+  T* sPlan = (T*)(smem + L.plan);
+  unsigned short* sS2 = (unsigned short*)(smem + L.tab);
+  int* sRT = (int*)(smem + L.tab + 512);
+  int* sMoff = (int*)(smem + L.tab + 512 + 1024);
+  C* srow = (C*)(smem + L.rows);
+  double* sRed = (double*)(smem + L.red);
+
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const long long row0 = (long long)blockIdx.x * P.rows_per_cta;
+  long long rem = P.n_rows - row0;
+  const int R = (int)(rem < P.rows_per_cta ? rem : P.rows_per_cta);
+  const int dim = P.dim, norb = P.norb, nocc = P.nocc;
+
+  // binomial table
+  for (int idx = tid; idx < FFGB_BST * FFGB_BST; idx += nth) {
+    int a = idx / FFGB_BST, b = idx % FFGB_BST;
+    int v = 0;
+    if (b <= a) {
+      long long r = 1;
+      for (int i = 1; i <= b; ++i) r = r * (a - b + i) / i;
+      v = (int)r;
+    }
+    sB[idx] = v;
+  }
+  // plan coefficients
+  if (P.kind == KIND_TRIANGLE) {
+    for (int idx = tid; idx < P.n_tri * 3; idx += nth) sPlan[idx] = P.tri[idx];
+  } else if (P.kind == KIND_FULL || P.kind == KIND_CSD) {
+    for (int idx = tid; idx < 4 * 28 * 3; idx += nth) sPlan[idx] = (&P.win[0][0])[idx];
+    for (int idx = tid; idx < 64; idx += nth) sPlan[4 * 28 * 3 + idx] = (&P.cs[0][0])[idx];
+  }
+  // rows: contiguous block [row0, row0 + R) of the input
+  {
+    const C* src = (const C*)P.in + row0 * (long long)dim;
+    const int n = R * dim;
+    for (int idx = tid; idx < n; idx += nth) srow[idx] = src[idx];
+  }
+  __syncthreads();
+
+  // --------------------------------------------------------------- stages
+  if constexpr (NW == 0) {
+    if (P.kind == KIND_TRIANGLE && nocc >= 1 && nocc <= norb - 1) {
+      const int npairs = bn(sB, norb - 2, nocc - 1);
+      const int items = R * npairs;
+      for (int g = 0; g < P.n_tri; ++g) {
+        const int l = P.tri_l[g];
+        const T c = sPlan[3 * g], sr = sPlan[3 * g + 1], si = sPlan[3 * g + 2];
+        const unsigned lowmask = (1u << l) - 1u;
+        for (int item = tid; item < items; item += nth) {
+          const int rho = item / npairs, t = item - rho * npairs;
+          const unsigned p = unrank_colex(t, norb - 2, nocc - 1, sB);
+          const unsigned x = (p & lowmask) | (1u << l) | ((p >> l) << (l + 2));
+          const int rx = rank_colex(x, sB);
+          const int ry = rx + bn(sB, l, __popc(p & lowmask));
+          C* base = srow + (long long)rho * dim;
+          C a = base[rx], b = base[ry];
+          C na, nb;
+          na.x = c * a.x + sr * b.x - si * b.y;
+          na.y = c * a.y + sr * b.y + si * b.x;
+          nb.x = c * b.x - sr * a.x - si * a.y;
+          nb.y = c * b.y - sr * a.y + si * a.x;
+          base[rx] = na;
+          base[ry] = nb;
+        }
+        __syncthreads();
+      }
+    }
+  } else {
+    static_assert(NW == 0 || sizeof(T) == 4, "window kernels are complex64 only");
+    constexpr int H = (NW <= 8) ? NW : NW / 2;
+    constexpr int Q = NW - H;
+    const float* wp = (const float*)sPlan;
+    if constexpr (NW <= 8) {
+      // the whole sector is one window
+      for (int rho = tid; rho < R; rho += nth) WinDispatch<H>::contig(nocc, srow + (long long)rho * dim, wp);
+      __syncthreads();
+    } else {
+      // tables over subsets of the high half (Q bits)
+      if (tid <= Q) {
+        int o = 0;
+        for (int m = 0; m < tid; ++m) o += bn(sB, Q, m);
+        sMoff[tid] = o;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < (1 << Q); idx += nth) {
+        int m = 0;
+        while (m < Q && idx >= sMoff[m + 1]) ++m;
+        const int g = idx - sMoff[m];
+        const unsigned s2 = unrank_colex(g, Q, m, sB);
+        sS2[idx] = (unsigned short)s2;
+        const int m0 = nocc - m;
+        sRT[idx] = (m0 >= 0 && m0 <= H) ? rank_shifted(s2, H, m0, sB) : 0;
+      }
+      __syncthreads();
+      const int klo_low = max(0, nocc - Q), khi_low = min(H, nocc);
+      const int klo_high = max(0, nocc - H), khi_high = min(Q, nocc);
+      auto low_stage = [&](const float* gp) {
+        warp_tasks(
+            klo_low, khi_low, [&](int k) { return R * bn(sB, Q, nocc - k); },
+            [&](int k, int item) {
+              const int G = bn(sB, Q, nocc - k);
+              const int rho = item / G, g = item - rho * G;
+              const int base = rho * dim + sRT[sMoff[nocc - k] + g];
+              WinDispatch<H>::contig(k, srow + base, gp);
+            });
+        __syncthreads();
+      };
+      auto high_stage = [&](const float* gp) {
+        warp_tasks(
+            klo_high, khi_high, [&](int k) { return R * bn(sB, H, nocc - k); },
+            [&](int k, int item) {
+              const int G = bn(sB, H, nocc - k);
+              const int rho = item / G, g = item - rho * G;
+              WinDispatch<Q>::table(k, srow + rho * dim + g, sRT + sMoff[k], gp);
+            });
+        __syncthreads();
+      };
+      low_stage(wp + 0 * 84);
+      high_stage(wp + 1 * 84);
+      // cross-half rotations (i, H + i)
+      const float* csp = wp + 4 * 84;
+      for (int i = 0; i < H; ++i) {
+        const float g00r = csp[8 * i + 0], g00i = csp[8 * i + 1], g01r = csp[8 * i + 2],
+                    g01i = csp[8 * i + 3], g10r = csp[8 * i + 4], g10i = csp[8 * i + 5],
+                    g11r = csp[8 * i + 6], g11i = csp[8 * i + 7];
+        warp_tasks(
+            max(1, klo_low), khi_low, [&](int k) { return R * bn(sB, Q, nocc - k); },
+            [&](int k, int item) {
+              const int m = nocc - k;
+              const int G = bn(sB, Q, m);
+              const int rho = item / G, g = item - rho * G;
+              const unsigned s2 = sS2[sMoff[m] + g];
+              if ((s2 >> i) & 1u) return;
+              float2* bx = srow + rho * dim + sRT[sMoff[m] + g];
+              float2* by = srow + rho * dim + rank_shifted(s2 | (1u << i), H, k - 1, sB);
+              const int sg0 = __popc(s2 & ((1u << i) - 1u)) & 1;
+              WinDispatch<H>::cs(k, i, [&](int j, int jp, int par) {
+                const float sgn = ((par ^ sg0) & 1) ? -1.f : 1.f;
+                const float2 x = bx[j], y = by[jp];
+                float2 nx, ny;
+                nx.x = g00r * x.x - g00i * x.y + sgn * (g01r * y.x - g01i * y.y);
+                nx.y = g00r * x.y + g00i * x.x + sgn * (g01r * y.y + g01i * y.x);
+                ny.x = sgn * (g10r * x.x - g10i * x.y) + g11r * y.x - g11i * y.y;
+                ny.y = sgn * (g10r * x.y + g10i * x.x) + g11r * y.y + g11i * y.x;
+                bx[j] = nx;
+                by[jp] = ny;
+              });
+            });
+        __syncthreads();
+      }
+      low_stage(wp + 2 * 84);
+      high_stage(wp + 3 * 84);
+    }
+  }
+
+  // --------------------------------------------------------------- epilogue
+  const int cb = L.chunk_bits, nch = L.nch, nent = nch << cb;
+  const unsigned cmask = (1u << cb) - 1u;
+  C* sDT = (C*)(smem + L.dt);
+  if (P.has_dphase) {
+    for (int e = tid; e < nent; e += nth) {
+      const int c = e >> cb;
+      unsigned x = (unsigned)(e & cmask);
+      C ph = cmake<C>(1.0, 0.0);
+      while (x) {
+        const int b = __ffs(x) - 1;
+        x &= x - 1;
+        const int orb = c * cb + b;
+        if (orb < norb) {
+          C d;
+          d.x = P.dphase[orb][0];
+          d.y = P.dphase[orb][1];
+          ph = cmul(ph, d);
+        }
+      }
+      sDT[e] = ph;
+    }
+  }
+  C* sXP = (C*)(smem + L.xt);
+  T* sXC = (T*)(smem + L.xt);
+  double* sM = (double*)(smem + L.xt + (P.diag_mode == DIAG_PHASE ? align16(nent * 2 * (int)sizeof(T))
+                                                                   : align16(nent * (int)sizeof(T))));
+  const C* colP = (const C*)P.col_table;
+  const T* colZ = (const T*)P.col_table;
+  C* out = (C*)P.out;
+  double acc_d = 0.0;
+  float acc_f = 0.f, comp_f = 0.f;
+  __syncthreads();
+
+  for (int rho = 0; rho < R; ++rho) {
+    const long long r = row0 + rho;
+    T rowconst = 0;
+    if (P.diag_mode != DIAG_NONE) {
+      const unsigned rs = P.row_strings[r];
+      const int rn = P.row_norb;
+      // m[l] = sum_i cross[i][l] g_i(r); sM[0..norb) = weights, sM[MAXN] = row constant
+      if (tid < norb) {
+        double m = 0.0;
+        for (int i = 0; i < rn; ++i) {
+          const double gi = P.zrep ? ((rs >> i) & 1u ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
+          m += P.cross[i][tid] * gi;
+        }
+        sM[tid] = m;
+      }
+      if (tid == 32 || (nth <= 32 && tid == 0)) {
+        double f = 0.0;
+        for (int i = 0; i < rn; ++i) {
+          const double gi = P.zrep ? ((rs >> i) & 1u ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
+          if (gi == 0.0) continue;
+          for (int i2 = i; i2 < rn; ++i2) {
+            const double gj = P.zrep ? ((rs >> i2) & 1u ? -1.0 : 1.0) : (double)((rs >> i2) & 1u);
+            f += P.rsame[i][i2] * gi * gj;
+          }
+        }
+        sM[FFGB_MAXN] = f;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double f = sM[FFGB_MAXN];
+        if (P.zrep)
+          for (int l = 0; l < norb; ++l) f += sM[l];
+        sM[FFGB_MAXN + 1] = f;
+      }
+      __syncthreads();
+      const double wsc = P.zrep ? -2.0 : 1.0;
+      const double rc = sM[FFGB_MAXN + 1];
+      for (int e = tid; e < nent; e += nth) {
+        const int c = e >> cb;
+        unsigned x = (unsigned)(e & cmask);
+        double f = (c == 0) ? rc : 0.0;
+        while (x) {
+          const int b = __ffs(x) - 1;
+          x &= x - 1;
+          const int orb = c * cb + b;
+          if (orb < norb) f += wsc * sM[orb];
+        }
+        if (P.diag_mode == DIAG_PHASE) {
+          sXP[e] = phase_of(f, (C*)nullptr);
+        } else {
+          sXC[e] = (T)f;
+        }
+      }
+      __syncthreads();
+      rowconst = 0;
+    }
+    const C* vr = srow + (long long)rho * dim;
+    for (int j = tid; j < dim; j += nth) {
+      C v = vr[j];
+      unsigned s = 0;
+      if (P.has_dphase || P.diag_mode != DIAG_NONE) s = P.col_strings[j];
+      if (P.has_dphase) {
+        for (int c = 0; c < nch; ++c) v = cmul(v, sDT[(c << cb) + ((s >> (c * cb)) & cmask)]);
+      }
+      T z = (T)1;
+      if (P.diag_mode == DIAG_PHASE) {
+        C f = colP ? colP[j] : cmake<C>(1.0, 0.0);
+        for (int c = 0; c < nch; ++c) f = cmul(f, sXP[(c << cb) + ((s >> (c * cb)) & cmask)]);
+        v = cmul(v, f);
+      } else if (P.diag_mode == DIAG_COEF) {
+        z = colZ ? colZ[j] : (T)0;
+        for (int c = 0; c < nch; ++c) z += sXC[(c << cb) + ((s >> (c * cb)) & cmask)];
+        z += rowconst;
+        if (P.out_op != OUT_EXPECT) {
+          v.x *= z;
+          v.y *= z;
+        }
+      }
+      if (P.out_op == OUT_EXPECT) {
+        const T w = (v.x * v.x + v.y * v.y) * z;
+        if constexpr (sizeof(T) == 4) {
+          const float y = (float)w - comp_f;
+          const float t = acc_f + y;
+          comp_f = (t - acc_f) - y;
+          acc_f = t;
+        } else {
+          acc_d += (double)w;
+        }
+      } else if (P.out_op != OUT_NONE) {
+        const long long o = (P.layout == LAYOUT_SAME) ? r * (long long)dim + j : (long long)j * P.n_rows + r;
+        if (P.out_op == OUT_STORE) {
+          out[o] = v;
+        } else {
+          C a = out[o];
+          a.x += P.alpha_re * v.x - P.alpha_im * v.y;
+          a.y += P.alpha_re * v.y + P.alpha_im * v.x;
+          out[o] = a;
+        }
+      }
+    }
+    if (P.diag_mode != DIAG_NONE) __syncthreads();
+  }
+
+  if (P.out_op == OUT_EXPECT) {
+    double a = (sizeof(T) == 4) ? (double)acc_f - (double)comp_f : acc_d;
+    for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
+    if ((tid & 31) == 0) sRed[tid >> 5] = a;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int w = 0; w < (nth >> 5); ++w) s += sRed[w];
+      P.partials[blockIdx.x] = s;
+    }
+  }
+}
+
+
+// One adjacent rotation on one spin sector directly in global memory (the
+// counterpart of the reference's per-Givens row-pair sweep).  spin 0: the
+// sector indexes rows (stride dim_other), spin 1: columns.
+template <typename T>
+__global__ void givens_sector_kernel(typename CT<T>::type* __restrict__ vec, int norb, int nocc,
+                                     long long dim_other, int spin, int l, T c, T sr, T si) {
+  using C = typename CT<T>::type;
+  __shared__ int sB[FFGB_BST * FFGB_BST];
+  for (int idx = threadIdx.x; idx < FFGB_BST * FFGB_BST; idx += blockDim.x) {
+    int a = idx / FFGB_BST, b = idx % FFGB_BST;
+    long long r = 0;
+    if (b <= a) {
+      r = 1;
+      for (int i = 1; i <= b; ++i) r = r * (a - b + i) / i;
+    }
+    sB[idx] = (int)r;
+  }
+  __syncthreads();
+  if (nocc < 1 || nocc > norb - 1) return;
+  const long long npairs = bn(sB, norb - 2, nocc - 1);
+  const long long total = npairs * dim_other;
+  const int dim = bn(sB, norb, nocc);
+  const unsigned lowmask = (1u << l) - 1u;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    long long t, o;
+    if (spin == 0) {
+      t = idx / dim_other;
+      o = idx - t * dim_other;
+    } else {
+      o = idx / npairs;
+      t = idx - o * npairs;
+    }
+    const unsigned p = unrank_colex((int)t, norb - 2, nocc - 1, sB);
+    const unsigned x = (p & lowmask) | (1u << l) | ((p >> l) << (l + 2));
+    const int rx = rank_colex(x, sB);
+    const int ry = rx + bn(sB, l, __popc(p & lowmask));
+    const long long ax = spin == 0 ? (long long)rx * dim_other + o : o * dim + rx;
+    const long long ay = spin == 0 ? (long long)ry * dim_other + o : o * dim + ry;
+    C a = vec[ax], b = vec[ay], na, nb;
+    na.x = c * a.x + sr * b.x - si * b.y;
+    na.y = c * a.y + sr * b.y + si * b.x;
+    nb.x = c * b.x - sr * a.x - si * a.y;
+    nb.y = c * b.y - sr * a.y + si * a.x;
+    vec[ax] = na;
+    vec[ay] = nb;
+  }
+}
+
+// Multiply every amplitude whose sector string has orbital `orb` occupied.
+template <typename T>
+__global__ void phase_shift_kernel(typename CT<T>::type* __restrict__ vec, const unsigned* __restrict__ strings,
+                                   long long dim_a, long long dim_b, int spin, int orb, T pr, T pi) {
+  using C = typename CT<T>::type;
+  const long long total = dim_a * dim_b;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long a = idx / dim_b, b = idx - a * dim_b;
+    const unsigned s = strings[spin == 0 ? a : b];
+    if ((s >> orb) & 1u) {
+      C v = vec[idx], o;
+      o.x = pr * v.x - pi * v.y;
+      o.y = pr * v.y + pi * v.x;
+      vec[idx] = o;
+    }
+  }
+}
+
+// F_C(j) of the rotated sector: phase exp(i F) (mode 1) or coefficient F (mode 2)
+template <typename T>
+__global__ void col_table_kernel(const unsigned* __restrict__ strings, int dim, int norb, int zrep,
+                                 int mode, const double* __restrict__ same, void* out) {
+  using C = typename CT<T>::type;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= dim) return;
+  const unsigned s = strings[j];
+  double f = 0.0;
+  for (int i = 0; i < norb; ++i) {
+    const double gi = zrep ? ((s >> i) & 1u ? -1.0 : 1.0) : (double)((s >> i) & 1u);
+    if (gi == 0.0) continue;
+    for (int i2 = i; i2 < norb; ++i2) {
+      const double gj = zrep ? ((s >> i2) & 1u ? -1.0 : 1.0) : (double)((s >> i2) & 1u);
+      f += same[i * FFGB_MAXN + i2] * gi * gj;
+    }
+  }
+  if (mode == DIAG_PHASE)
+    ((C*)out)[j] = phase_of(f, (C*)nullptr);
+  else
+    ((T*)out)[j] = (T)f;
+}
+
+// deterministic sum of n doubles into out[slot]
+static __global__ void reduce_partials_kernel(const double* __restrict__ in, long long n, double* out, int slot) {
+  __shared__ double sh[256];
+  double a = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) a += in[i];
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[slot] = sh[0];
+}
+
+// partial sums of conj(x) y per CTA
+template <typename T>
+__global__ void vdot_kernel(const typename CT<T>::type* __restrict__ x,
+                            const typename CT<T>::type* __restrict__ y, long long n,
+                            double* __restrict__ partials) {
+  __shared__ double sr[32], si[32];
+  double ar = 0.0, ai = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double xr = x[i].x, xi = x[i].y, yr = y[i].x, yi = y[i].y;
+    ar += xr * yr + xi * yi;
+    ai += xr * yi - xi * yr;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    ar += __shfl_down_sync(0xffffffffu, ar, off);
+    ai += __shfl_down_sync(0xffffffffu, ai, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    sr[threadIdx.x >> 5] = ar;
+    si[threadIdx.x >> 5] = ai;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += sr[w];
+      b += si[w];
+    }
+    partials[2 * blockIdx.x] = a;
+    partials[2 * blockIdx.x + 1] = b;
+  }
+}
+
+template <typename T>
+__global__ void scale_copy_kernel(const typename CT<T>::type* __restrict__ x,
+                                  typename CT<T>::type* __restrict__ y, long long n, T ar, T ai) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    typename CT<T>::type v = x[i], o;
+    o.x = ar * v.x - ai * v.y;
+    o.y = ar * v.y + ai * v.x;
+    y[i] = o;
+  }
+}
+
+template <typename T>
+__global__ void one_hot_kernel(typename CT<T>::type* __restrict__ y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    typename CT<T>::type v;
+    v.x = (i == 0) ? (T)1 : (T)0;
+    v.y = (T)0;
+    y[i] = v;
+  }
+}
+
+}  // namespace ffgb

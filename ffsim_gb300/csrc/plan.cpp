@@ -1,0 +1,550 @@
+// Host-side planning of orbital rotations (see plan.h).
+#include "plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace ffgb {
+
+namespace {
+
+inline cd at(const std::vector<cd>& m, int n, int r, int c) { return m[(size_t)r * n + c]; }
+
+// One-sided (Hestenes) Jacobi SVD of a square n x n matrix A (row-major):
+// A = U diag(S) W^H, S descending.  Columns of U belonging to zero singular
+// values are completed to an orthonormal basis.
+void svd_jacobi(int n, const std::vector<cd>& A, std::vector<cd>& U, std::vector<double>& S,
+                std::vector<cd>& W) {
+  std::vector<cd> G = A;
+  W.assign((size_t)n * n, cd(0));
+  for (int i = 0; i < n; ++i) W[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 80; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < n; ++p) {
+      for (int q = p + 1; q < n; ++q) {
+        double alpha = 0, beta = 0;
+        cd gamma = 0;
+        for (int k = 0; k < n; ++k) {
+          cd gp = G[(size_t)k * n + p], gq = G[(size_t)k * n + q];
+          alpha += std::norm(gp);
+          beta += std::norm(gq);
+          gamma += std::conj(gp) * gq;
+        }
+        double ag = std::abs(gamma);
+        if (alpha == 0.0 || beta == 0.0 || ag <= 1e-17 * std::sqrt(alpha * beta)) continue;
+        off = std::max(off, ag / std::sqrt(alpha * beta));
+        double zeta = (beta - alpha) / (2.0 * ag);
+        double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+        double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
+        cd e = std::conj(gamma / ag);  // e^{-i theta}
+        for (int k = 0; k < n; ++k) {
+          cd gp = G[(size_t)k * n + p], gq = G[(size_t)k * n + q];
+          G[(size_t)k * n + p] = c * gp - s * e * gq;
+          G[(size_t)k * n + q] = s * gp + c * e * gq;
+          cd wp = W[(size_t)k * n + p], wq = W[(size_t)k * n + q];
+          W[(size_t)k * n + p] = c * wp - s * e * wq;
+          W[(size_t)k * n + q] = s * wp + c * e * wq;
+        }
+      }
+    }
+    if (off < 1e-16) break;
+  }
+  S.assign(n, 0.0);
+  for (int p = 0; p < n; ++p) {
+    double ss = 0;
+    for (int k = 0; k < n; ++k) ss += std::norm(G[(size_t)k * n + p]);
+    S[p] = std::sqrt(ss);
+  }
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return S[a] > S[b]; });
+  std::vector<cd> U2((size_t)n * n, cd(0)), W2((size_t)n * n, cd(0));
+  std::vector<double> S2(n);
+  std::vector<bool> have(n, false);
+  for (int j = 0; j < n; ++j) {
+    int p = order[j];
+    S2[j] = S[p];
+    for (int k = 0; k < n; ++k) W2[(size_t)k * n + j] = W[(size_t)k * n + p];
+    if (S[p] > 1e-300) {
+      for (int k = 0; k < n; ++k) U2[(size_t)k * n + j] = G[(size_t)k * n + p] / S[p];
+      have[j] = true;
+    }
+  }
+  // complete missing columns by Gram-Schmidt on unit vectors
+  for (int j = 0; j < n; ++j) {
+    if (have[j]) continue;
+    for (int e = 0; e < n; ++e) {
+      std::vector<cd> v(n, cd(0));
+      v[e] = 1.0;
+      for (int pass = 0; pass < 2; ++pass)
+        for (int o = 0; o < n; ++o) {
+          if (!have[o]) continue;
+          cd d = 0;
+          for (int k = 0; k < n; ++k) d += std::conj(U2[(size_t)k * n + o]) * v[k];
+          for (int k = 0; k < n; ++k) v[k] -= d * U2[(size_t)k * n + o];
+        }
+      double nv = 0;
+      for (int k = 0; k < n; ++k) nv += std::norm(v[k]);
+      nv = std::sqrt(nv);
+      if (nv > 0.5) {
+        for (int k = 0; k < n; ++k) U2[(size_t)k * n + j] = v[k] / nv;
+        have[j] = true;
+        break;
+      }
+    }
+  }
+  U.swap(U2);
+  W.swap(W2);
+  S.swap(S2);
+}
+
+// Householder QR of Z (m x n, m >= n, row-major): Z = Q R, Q m x m unitary.
+void householder_qr(int m, int n, const std::vector<cd>& Z, std::vector<cd>& Q, std::vector<cd>& R) {
+  R = Z;
+  Q.assign((size_t)m * m, cd(0));
+  for (int i = 0; i < m; ++i) Q[(size_t)i * m + i] = 1.0;
+  std::vector<cd> v(m);
+  for (int j = 0; j < n && j < m; ++j) {
+    double nx = 0;
+    for (int k = j; k < m; ++k) nx += std::norm(R[(size_t)k * n + j]);
+    nx = std::sqrt(nx);
+    if (nx == 0.0) continue;
+    cd x0 = R[(size_t)j * n + j];
+    cd ph = std::abs(x0) > 0 ? x0 / std::abs(x0) : cd(1.0);
+    cd alpha = -ph * nx;
+    double vn = 0;
+    for (int k = j; k < m; ++k) {
+      v[k] = R[(size_t)k * n + j];
+      if (k == j) v[k] -= alpha;
+      vn += std::norm(v[k]);
+    }
+    if (vn == 0.0) continue;
+    // R <- (I - 2 v v^H / vn) R on rows j..m-1
+    for (int c = j; c < n; ++c) {
+      cd d = 0;
+      for (int k = j; k < m; ++k) d += std::conj(v[k]) * R[(size_t)k * n + c];
+      d *= 2.0 / vn;
+      for (int k = j; k < m; ++k) R[(size_t)k * n + c] -= d * v[k];
+    }
+    // Q <- Q (I - 2 v v^H / vn) on columns j..m-1
+    for (int r = 0; r < m; ++r) {
+      cd d = 0;
+      for (int k = j; k < m; ++k) d += Q[(size_t)r * m + k] * v[k];
+      d *= 2.0 / vn;
+      for (int k = j; k < m; ++k) Q[(size_t)r * m + k] -= d * std::conj(v[k]);
+    }
+  }
+}
+
+}  // namespace
+
+void triangle_order(int b, std::vector<int>& l) {
+  l.clear();
+  for (int r = 0; r < b - 1; ++r)
+    for (int col = b - 1; col > r; --col) l.push_back(col - 1);
+}
+
+void triangle_decompose(int b, const cd* X, std::vector<Givens>& rots, std::vector<cd>& diag) {
+  std::vector<cd> M(X, X + (size_t)b * b);
+  rots.clear();
+  for (int r = 0; r < b - 1; ++r) {
+    for (int col = b - 1; col > r; --col) {
+      cd a = M[(size_t)r * b + col - 1], bb = M[(size_t)r * b + col];
+      double aa = std::abs(a), rho = std::hypot(aa, std::abs(bb));
+      double c = 1.0;
+      cd s = 0.0;
+      if (rho > 0.0) {
+        cd ph = aa > 0 ? a / aa : cd(1.0);
+        c = aa / rho;
+        s = bb * std::conj(ph) / rho;
+      }
+      for (int row = 0; row < b; ++row) {
+        cd x = M[(size_t)row * b + col - 1], y = M[(size_t)row * b + col];
+        M[(size_t)row * b + col - 1] = c * x + std::conj(s) * y;
+        M[(size_t)row * b + col] = -s * x + c * y;
+      }
+      rots.push_back({c, s});
+    }
+  }
+  diag.resize(b);
+  for (int i = 0; i < b; ++i) diag[i] = M[(size_t)i * b + i];
+}
+
+bool csd(int n, int h, const cd* Vp, std::vector<cd>& A1, std::vector<cd>& A2,
+         std::vector<double>& cosv, std::vector<double>& sinv, std::vector<cd>& B1,
+         std::vector<cd>& B2, double tol, double* err) {
+  const int q = n - h;
+  if (h < 1 || q < h) return false;
+  std::vector<cd> V(Vp, Vp + (size_t)n * n);
+  std::vector<cd> V11((size_t)h * h), V12((size_t)h * q), V21((size_t)q * h), V22((size_t)q * q);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      cd v = V[(size_t)r * n + c];
+      if (r < h && c < h) V11[(size_t)r * h + c] = v;
+      else if (r < h) V12[(size_t)r * q + (c - h)] = v;
+      else if (c < h) V21[(size_t)(r - h) * h + c] = v;
+      else V22[(size_t)(r - h) * q + (c - h)] = v;
+    }
+  std::vector<cd> U1, W1;
+  std::vector<double> cs;
+  svd_jacobi(h, V11, U1, cs, W1);
+  // Z = V21 W1 (q x h)
+  std::vector<cd> Z((size_t)q * h, cd(0));
+  for (int r = 0; r < q; ++r)
+    for (int c = 0; c < h; ++c) {
+      cd acc = 0;
+      for (int k = 0; k < h; ++k) acc += V21[(size_t)r * h + k] * W1[(size_t)k * h + c];
+      Z[(size_t)r * h + c] = acc;
+    }
+  std::vector<cd> Q, R;
+  householder_qr(q, h, Z, Q, R);
+  std::vector<cd> U2 = Q;
+  std::vector<double> sn(h);
+  for (int i = 0; i < h; ++i) {
+    cd rii = R[(size_t)i * h + i];
+    double ar = std::abs(rii);
+    cd ph = ar > 0 ? rii / ar : cd(1.0);
+    sn[i] = ar;
+    for (int k = 0; k < q; ++k) U2[(size_t)k * q + i] *= ph;
+  }
+  cosv.resize(h);
+  sinv.resize(h);
+  for (int i = 0; i < h; ++i) {
+    double th = std::atan2(sn[i], std::min(1.0, std::max(0.0, cs[i])));
+    cosv[i] = std::cos(th);
+    sinv[i] = std::sin(th);
+  }
+  // W2^H: rows i<h: c_i (U2^H V22)_i - s_i (U1^H V12)_i ; rows i>=h: (U2^H V22)_i
+  std::vector<cd> P((size_t)q * q, cd(0)), K((size_t)h * q, cd(0));
+  for (int r = 0; r < q; ++r)
+    for (int c = 0; c < q; ++c) {
+      cd acc = 0;
+      for (int k = 0; k < q; ++k) acc += std::conj(U2[(size_t)k * q + r]) * V22[(size_t)k * q + c];
+      P[(size_t)r * q + c] = acc;
+    }
+  for (int r = 0; r < h; ++r)
+    for (int c = 0; c < q; ++c) {
+      cd acc = 0;
+      for (int k = 0; k < h; ++k) acc += std::conj(U1[(size_t)k * h + r]) * V12[(size_t)k * q + c];
+      K[(size_t)r * q + c] = acc;
+    }
+  B2.assign((size_t)q * q, cd(0));
+  for (int r = 0; r < q; ++r)
+    for (int c = 0; c < q; ++c)
+      B2[(size_t)r * q + c] = r < h ? cosv[r] * P[(size_t)r * q + c] - sinv[r] * K[(size_t)r * q + c]
+                                    : P[(size_t)r * q + c];
+  B1.assign((size_t)h * h, cd(0));
+  for (int r = 0; r < h; ++r)
+    for (int c = 0; c < h; ++c) B1[(size_t)r * h + c] = std::conj(W1[(size_t)c * h + r]);
+  A1 = U1;
+  A2 = U2;
+  // reconstruction check
+  std::vector<cd> CSB((size_t)n * n, cd(0));  // CS * diag(B1, B2)
+  auto Bfull = [&](int r, int c) -> cd {
+    if (r < h && c < h) return B1[(size_t)r * h + c];
+    if (r >= h && c >= h) return B2[(size_t)(r - h) * q + (c - h)];
+    return 0.0;
+  };
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      cd acc;
+      if (r < h) acc = cosv[r] * Bfull(r, c) - sinv[r] * Bfull(h + r, c);
+      else if (r < 2 * h) acc = sinv[r - h] * Bfull(r - h, c) + cosv[r - h] * Bfull(r, c);
+      else acc = Bfull(r, c);
+      CSB[(size_t)r * n + c] = acc;
+    }
+  double e = 0;
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      cd acc = 0;
+      if (r < h)
+        for (int k = 0; k < h; ++k) acc += A1[(size_t)r * h + k] * CSB[(size_t)k * n + c];
+      else
+        for (int k = 0; k < q; ++k) acc += A2[(size_t)(r - h) * q + k] * CSB[(size_t)(h + k) * n + c];
+      e = std::max(e, std::abs(acc - V[(size_t)r * n + c]));
+    }
+  if (err) *err = e;
+  return e <= tol;
+}
+
+namespace {
+// multiply out a triangle network + diag into a b x b matrix (for checks)
+std::vector<cd> triangle_matrix(int b, const std::vector<Givens>& rots, const std::vector<cd>& diag) {
+  std::vector<int> l;
+  triangle_order(b, l);
+  std::vector<cd> M((size_t)b * b, cd(0));
+  for (int i = 0; i < b; ++i) M[(size_t)i * b + i] = 1.0;
+  // M = G_M ... G_1 : left-multiply successively
+  for (size_t k = 0; k < rots.size(); ++k) {
+    int a = l[k];
+    double c = rots[k].c;
+    cd s = rots[k].s;
+    for (int col = 0; col < b; ++col) {
+      cd x = M[(size_t)a * b + col], y = M[(size_t)(a + 1) * b + col];
+      M[(size_t)a * b + col] = c * x + s * y;
+      M[(size_t)(a + 1) * b + col] = -std::conj(s) * x + c * y;
+    }
+  }
+  for (int r = 0; r < b; ++r)
+    for (int col = 0; col < b; ++col) M[(size_t)r * b + col] *= diag[r];
+  return M;
+}
+}  // namespace
+
+bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
+  plan = SectorPlan();
+  plan.norb = norb;
+  if (norb == 0) {
+    plan.kind = PLAN_IDENTITY;
+    return true;
+  }
+  if (!want_csd || norb > 16) {
+    plan.kind = PLAN_TRIANGLE;
+    triangle_decompose(norb, V, plan.tri, plan.diag);
+    triangle_order(norb, plan.tri_l);
+    std::vector<cd> M = triangle_matrix(norb, plan.tri, plan.diag);
+    double e = 0;
+    for (size_t i = 0; i < M.size(); ++i) e = std::max(e, std::abs(M[i] - V[i]));
+    plan.max_err = e;
+    return true;
+  }
+  if (norb <= 8) {
+    plan.kind = PLAN_FULL;
+    plan.h = norb;
+    triangle_decompose(norb, V, plan.tri, plan.diag);
+    triangle_order(norb, plan.tri_l);
+    std::vector<cd> M = triangle_matrix(norb, plan.tri, plan.diag);
+    double e = 0;
+    for (size_t i = 0; i < M.size(); ++i) e = std::max(e, std::abs(M[i] - V[i]));
+    plan.max_err = e;
+    return true;
+  }
+  const int h = norb / 2, q = norb - h;
+  std::vector<cd> A1, A2, B1, B2;
+  std::vector<double> cv, sv;
+  double err = 0;
+  if (!csd(norb, h, V, A1, A2, cv, sv, B1, B2, 1e-11, &err)) {
+    // fall back to the generic network
+    return plan_sector(norb, V, false, plan);
+  }
+  plan.kind = PLAN_CSD;
+  plan.h = h;
+  std::vector<cd> dB1, dB2, dA1, dA2;
+  triangle_decompose(h, B1.data(), plan.b1, dB1);
+  triangle_decompose(q, B2.data(), plan.b2, dB2);
+  std::vector<cd> dB(dB1);
+  dB.insert(dB.end(), dB2.begin(), dB2.end());
+  plan.cs.clear();
+  for (int i = 0; i < h; ++i) {
+    int j = h + i;
+    Pair2 p;
+    p.i = i;
+    p.j = j;
+    p.g00 = cv[i];
+    p.g01 = std::conj(dB[i]) * (-sv[i]) * dB[j];
+    p.g10 = std::conj(dB[j]) * sv[i] * dB[i];
+    p.g11 = cv[i];
+    plan.cs.push_back(p);
+  }
+  // A' = A diag(dB)
+  for (int r = 0; r < h; ++r)
+    for (int c = 0; c < h; ++c) A1[(size_t)r * h + c] *= dB1[c];
+  for (int r = 0; r < q; ++r)
+    for (int c = 0; c < q; ++c) A2[(size_t)r * q + c] *= dB2[c];
+  triangle_decompose(h, A1.data(), plan.a1, dA1);
+  triangle_decompose(q, A2.data(), plan.a2, dA2);
+  plan.diag = dA1;
+  plan.diag.insert(plan.diag.end(), dA2.begin(), dA2.end());
+  // multiply the plan back out to measure its error
+  std::vector<cd> TB1 = triangle_matrix(h, plan.b1, std::vector<cd>(h, cd(1)));
+  std::vector<cd> TB2 = triangle_matrix(q, plan.b2, std::vector<cd>(q, cd(1)));
+  std::vector<cd> TA1 = triangle_matrix(h, plan.a1, dA1);
+  std::vector<cd> TA2 = triangle_matrix(q, plan.a2, dA2);
+  auto blk = [&](const std::vector<cd>& X1, const std::vector<cd>& X2) {
+    std::vector<cd> M((size_t)norb * norb, cd(0));
+    for (int r = 0; r < h; ++r)
+      for (int c = 0; c < h; ++c) M[(size_t)r * norb + c] = X1[(size_t)r * h + c];
+    for (int r = 0; r < q; ++r)
+      for (int c = 0; c < q; ++c) M[(size_t)(h + r) * norb + h + c] = X2[(size_t)r * q + c];
+    return M;
+  };
+  std::vector<cd> MB = blk(TB1, TB2), MA = blk(TA1, TA2);
+  std::vector<cd> MC((size_t)norb * norb, cd(0));
+  for (int i = 0; i < norb; ++i) MC[(size_t)i * norb + i] = 1.0;
+  for (const Pair2& p : plan.cs) {
+    MC[(size_t)p.i * norb + p.i] = p.g00;
+    MC[(size_t)p.i * norb + p.j] = p.g01;
+    MC[(size_t)p.j * norb + p.i] = p.g10;
+    MC[(size_t)p.j * norb + p.j] = p.g11;
+  }
+  auto mm = [&](const std::vector<cd>& X, const std::vector<cd>& Y) {
+    std::vector<cd> Out((size_t)norb * norb, cd(0));
+    for (int r = 0; r < norb; ++r)
+      for (int k = 0; k < norb; ++k) {
+        cd x = X[(size_t)r * norb + k];
+        if (x == cd(0)) continue;
+        for (int c = 0; c < norb; ++c) Out[(size_t)r * norb + c] += x * Y[(size_t)k * norb + c];
+      }
+    return Out;
+  };
+  std::vector<cd> full = mm(MA, mm(MC, MB));
+  double e = 0;
+  for (size_t i = 0; i < full.size(); ++i) e = std::max(e, std::abs(full[i] - V[i]));
+  plan.max_err = e;
+  if (e > 1e-10) return plan_sector(norb, V, false, plan);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Reference Givens decomposition, restated (src/linalg/givens.rs:20-149)
+// ---------------------------------------------------------------------------
+namespace {
+void zrotg_safe(cd a, cd b, double tol, double* c, cd* s) {
+  double aa = std::abs(a), ab = std::abs(b);
+  if (ab <= tol) {
+    *c = 1.0;
+    *s = 0.0;
+    return;
+  }
+  if (aa <= tol) {
+    *c = 0.0;
+    *s = 1.0;
+    return;
+  }
+  double r = std::hypot(aa, ab);
+  *c = std::min(1.0, std::max(-1.0, aa / r));
+  *s = (a / aa) * std::conj(b) / r;
+}
+}  // namespace
+
+bool reference_givens_decomposition(int n, const cd* mat, double tol, std::vector<RefGivens>& rots,
+                                    std::vector<cd>& diag) {
+  std::vector<cd> m(mat, mat + (size_t)n * n);
+  std::vector<RefGivens> left;
+  rots.clear();
+  auto rot_cols = [&](int x, int y, double c, cd s) {
+    for (int r = 0; r < n; ++r) {
+      cd xo = m[(size_t)r * n + x], yo = m[(size_t)r * n + y];
+      m[(size_t)r * n + x] = c * xo + s * yo;
+      m[(size_t)r * n + y] = c * yo - std::conj(s) * xo;
+    }
+  };
+  auto rot_rows = [&](int x, int y, double c, cd s) {
+    for (int col = 0; col < n; ++col) {
+      cd xo = m[(size_t)x * n + col], yo = m[(size_t)y * n + col];
+      m[(size_t)x * n + col] = c * xo + s * yo;
+      m[(size_t)y * n + col] = c * yo - std::conj(s) * xo;
+    }
+  };
+  for (int i = 0; i + 1 < n; ++i) {
+    for (int j = 0; j <= i; ++j) {
+      if (i % 2 == 0) {
+        int t = i - j, row = n - j - 1;
+        if (std::abs(m[(size_t)row * n + t]) > tol) {
+          double c;
+          cd s;
+          zrotg_safe(m[(size_t)row * n + t + 1], m[(size_t)row * n + t], tol, &c, &s);
+          rots.push_back({c, s, t + 1, t});
+          rot_cols(t + 1, t, c, s);
+        }
+      } else {
+        int t = n - i + j - 1, col = j;
+        if (std::abs(m[(size_t)t * n + col]) > tol) {
+          double c;
+          cd s;
+          zrotg_safe(m[(size_t)(t - 1) * n + col], m[(size_t)t * n + col], tol, &c, &s);
+          left.push_back({c, s, t - 1, t});
+          rot_rows(t - 1, t, c, s);
+        }
+      }
+    }
+  }
+  for (auto it = left.rbegin(); it != left.rend(); ++it) {
+    int i = it->i, j = it->j;
+    double c;
+    cd s;
+    zrotg_safe(it->c * m[(size_t)j * n + j], std::conj(it->s) * m[(size_t)i * n + i], tol, &c, &s);
+    rots.push_back({c, -std::conj(s), i, j});
+    cd di = m[(size_t)i * n + i], dj = m[(size_t)j * n + j];
+    cd g00 = c * di, g01 = -s * dj, g10 = std::conj(s) * di, g11 = c * dj;
+    double cn;
+    cd sn;
+    zrotg_safe(g11, g10, tol, &cn, &sn);
+    m[(size_t)i * n + i] = g00 * cn + g01 * (-std::conj(sn));
+    m[(size_t)j * n + j] = g10 * sn + g11 * cn;
+  }
+  diag.resize(n);
+  for (int i = 0; i < n; ++i) diag[i] = m[(size_t)i * n + i];
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Hermitian eigendecomposition by cyclic complex Jacobi rotations
+// ---------------------------------------------------------------------------
+void hermitian_eigh(int n, const cd* Ap, std::vector<double>& w, std::vector<cd>& vecs) {
+  std::vector<cd> A(Ap, Ap + (size_t)n * n);
+  for (int r = 0; r < n; ++r) {  // symmetrize
+    A[(size_t)r * n + r] = A[(size_t)r * n + r].real();
+    for (int c = r + 1; c < n; ++c) {
+      cd v = 0.5 * (A[(size_t)r * n + c] + std::conj(A[(size_t)c * n + r]));
+      A[(size_t)r * n + c] = v;
+      A[(size_t)c * n + r] = std::conj(v);
+    }
+  }
+  vecs.assign((size_t)n * n, cd(0));
+  for (int i = 0; i < n; ++i) vecs[(size_t)i * n + i] = 1.0;
+  double scale = 0;
+  for (auto& x : A) scale = std::max(scale, std::abs(x));
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off = std::max(off, std::abs(A[(size_t)p * n + q]));
+    if (off <= 1e-16 * std::max(scale, 1e-300)) break;
+    for (int p = 0; p < n; ++p) {
+      for (int q = p + 1; q < n; ++q) {
+        cd apq = A[(size_t)p * n + q];
+        double a = std::abs(apq);
+        if (a <= 1e-300) continue;
+        cd e = apq / a;  // e^{i phi}
+        double app = A[(size_t)p * n + p].real(), aqq = A[(size_t)q * n + q].real();
+        double tau = (aqq - app) / (2.0 * a);
+        double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+        double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
+        // J = [[c, s], [-s conj(e), c conj(e)]] on columns (p, q): A <- J^H A J
+        cd j00 = c, j01 = s, j10 = -s * std::conj(e), j11 = c * std::conj(e);
+        for (int k = 0; k < n; ++k) {  // A <- A J
+          cd x = A[(size_t)k * n + p], y = A[(size_t)k * n + q];
+          A[(size_t)k * n + p] = x * j00 + y * j10;
+          A[(size_t)k * n + q] = x * j01 + y * j11;
+        }
+        for (int k = 0; k < n; ++k) {  // A <- J^H A
+          cd x = A[(size_t)p * n + k], y = A[(size_t)q * n + k];
+          A[(size_t)p * n + k] = std::conj(j00) * x + std::conj(j10) * y;
+          A[(size_t)q * n + k] = std::conj(j01) * x + std::conj(j11) * y;
+        }
+        A[(size_t)p * n + q] = 0.0;
+        A[(size_t)q * n + p] = 0.0;
+        for (int k = 0; k < n; ++k) {
+          cd x = vecs[(size_t)k * n + p], y = vecs[(size_t)k * n + q];
+          vecs[(size_t)k * n + p] = x * j00 + y * j10;
+          vecs[(size_t)k * n + q] = x * j01 + y * j11;
+        }
+      }
+    }
+  }
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<double> d(n);
+  for (int i = 0; i < n; ++i) d[i] = A[(size_t)i * n + i].real();
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return d[a] < d[b]; });
+  w.resize(n);
+  std::vector<cd> v2((size_t)n * n);
+  for (int j = 0; j < n; ++j) {
+    w[j] = d[order[j]];
+    for (int k = 0; k < n; ++k) v2[(size_t)k * n + j] = vecs[(size_t)k * n + order[j]];
+  }
+  vecs.swap(v2);
+}
+
+}  // namespace ffgb

@@ -1,0 +1,79 @@
+// Host-side planning of orbital rotations for the sector kernels.
+//
+// An orbital rotation V (norb x norb unitary) acts on one spin sector as
+// W(V), the representation a^dag_k -> sum_l V_lk a^dag_l.  W is a group
+// homomorphism, so any exact factorization of V into simple unitaries gives
+// W(V) as the product of their actions.  Two factorizations are planned:
+//
+//  * TRIANGLE: V = D * G_M ... G_1, adjacent Givens rotations G_k on (l, l+1)
+//    in a fixed order (see triangle_decompose), applied one per shared-memory
+//    sweep.  Used for complex128 and as the generic path.
+//  * CSD (complex64, 9 <= norb <= 16): V = D * (T_A1 + T_A2) * CS' * (T_B1 + T_B2),
+//    a cosine-sine decomposition over the halves [0,h) and [h,norb); each
+//    half-block is a fixed triangle of window Givens applied in registers,
+//    CS' is h commuting rotations on orbital pairs (i, h+i).
+//    For norb <= 8 the whole sector is one window ("FULL").
+#pragma once
+
+#include <complex>
+#include <vector>
+
+namespace ffgb {
+
+using cd = std::complex<double>;
+
+struct Givens {  // 2x2 block [[c, s], [-conj(s), c]] on orbitals (l, l+1)
+  double c;
+  cd s;
+};
+
+struct Pair2 {  // general 2x2 unitary block on orbitals (i, j), i < j
+  int i, j;
+  cd g00, g01, g10, g11;
+};
+
+enum PlanKind { PLAN_IDENTITY = 0, PLAN_TRIANGLE = 1, PLAN_FULL = 2, PLAN_CSD = 3 };
+
+struct SectorPlan {
+  int kind = PLAN_IDENTITY;
+  int norb = 0;
+  int h = 0;  // split point for CSD; norb for FULL
+  std::vector<Givens> tri;   // TRIANGLE / FULL network (norb(norb-1)/2)
+  std::vector<int> tri_l;    // TRIANGLE: lower orbital of each rotation
+  std::vector<Givens> b1, b2, a1, a2;  // CSD window networks
+  std::vector<Pair2> cs;     // CSD middle rotations (i, h+i)
+  std::vector<cd> diag;      // final per-orbital phases (norb)
+  double max_err = 0.0;      // reconstruction error of the factorization
+};
+
+// Fixed triangular network: X (b x b unitary, row-major) = D * G_M ... G_1.
+// Rotation k acts on local orbitals (l_k, l_k+1), l_k from triangle_order().
+void triangle_decompose(int b, const cd* X, std::vector<Givens>& rots, std::vector<cd>& diag);
+void triangle_order(int b, std::vector<int>& l);
+
+// Cosine-sine decomposition of V (n x n) at split h (h <= n-h <= h+1):
+// V = diag(A1, A2) * CS * diag(B1, B2); returns false if it fails to
+// reconstruct V within tol.
+bool csd(int n, int h, const cd* V, std::vector<cd>& A1, std::vector<cd>& A2,
+         std::vector<double>& cosv, std::vector<double>& sinv, std::vector<cd>& B1,
+         std::vector<cd>& B2, double tol, double* err);
+
+// Build the plan for W(V) on a sector with nocc electrons in norb orbitals.
+// want_csd selects the register-window factorization when norb allows it.
+bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan);
+
+// Restatement of the reference Givens decomposition (src/linalg/givens.rs:68-149):
+// U = D * G_L^* ... G_1^*, rotations (c, s, i, j).
+struct RefGivens {
+  double c;
+  cd s;
+  int i, j;
+};
+bool reference_givens_decomposition(int n, const cd* mat, double tol, std::vector<RefGivens>& rots,
+                                    std::vector<cd>& diag);
+
+// Hermitian eigendecomposition (cyclic complex Jacobi), ascending eigenvalues,
+// eigenvectors as columns of vecs (row-major n x n).
+void hermitian_eigh(int n, const cd* A, std::vector<double>& w, std::vector<cd>& vecs);
+
+}  // namespace ffgb

@@ -1,0 +1,58 @@
+"""Fused LUCJ energy: the UCJ circuit applied to a state (Hartree-Fock by
+default) followed by the double-factorized Hamiltonian expectation, with the
+circuit's last orbital rotation merged into every Hamiltonian term.
+
+Equals ``np.vdot(psi, H @ psi).real`` with ``psi = apply_unitary(hf, ucj)``
+(tests/python/variational/ucj_spin_balanced_test.py:152-158 in the reference).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from ffsim_gb300 import _lib
+from ffsim_gb300._state import dim, scratch
+from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian
+from ffsim_gb300.variational import UCJOpSpinBalanced
+
+
+class LUCJEnergy:
+    """Reusable LUCJ energy evaluator holding its device buffers."""
+
+    def __init__(self, norb: int, nelec: tuple[int, int], *, dtype=torch.complex64, device="cuda"):
+        self.norb = norb
+        self.nelec = tuple(nelec)
+        self.dtype = dtype
+        self.code = _lib.FFGB_C64 if dtype == torch.complex64 else _lib.FFGB_C128
+        self.work = torch.empty(dim(norb, nelec), dtype=dtype, device=device)
+        self.buf, self.nbytes = scratch(self.work, 2, norb, *self.nelec)
+        self.stream = None
+
+    def __call__(self, ucj: UCJOpSpinBalanced, ham: DoubleFactorizedHamiltonian, vec=None) -> float:
+        n_alpha, n_beta = self.nelec
+        dcm = _lib.rmat(ucj.diag_coulomb_mats)
+        rots = _lib.cmat(ucj.orbital_rotations)
+        final = _lib.cmat(ucj.final_orbital_rotation)
+        if ham.z_representation:
+            ham = ham.to_number_representation()
+        one_body, hdcm, hrots = ham._arrays()
+        e = np.zeros(1)
+        vin = None
+        if vec is not None:
+            vin = vec.contiguous()
+            if vin.dtype != self.dtype:
+                raise TypeError("vec dtype must match the evaluator dtype")
+        stream = torch.cuda.current_stream(self.work.device).cuda_stream
+        _lib.call("ffgb_lucj_energy", None if vin is None else vin.data_ptr(), self.work.data_ptr(),
+                  self.code, self.norb, n_alpha, n_beta, ucj.n_reps, _lib.dptr(dcm),
+                  rots.ctypes.data_as(_lib._dp), _lib.dptr(final), _lib.dptr(one_body), hdcm.shape[0],
+                  _lib.dptr(hdcm), hrots.ctypes.data_as(_lib._dp), float(ham.constant), _lib.dptr(e),
+                  self.buf.data_ptr(), self.nbytes, stream)
+        return float(e[0])
+
+
+def lucj_energy(ucj: UCJOpSpinBalanced, ham: DoubleFactorizedHamiltonian, norb: int,
+                nelec: tuple[int, int], *, dtype=torch.complex64, vec=None) -> float:
+    """One LUCJ energy evaluation (allocates its buffers; use LUCJEnergy to reuse them)."""
+    return LUCJEnergy(norb, nelec, dtype=dtype)(ucj, ham, vec)

@@ -1,0 +1,88 @@
+"""Protocol dispatch and the GPU linear-operator type.
+
+``apply_unitary`` and ``linear_operator`` dispatch on the duck-typed
+``_apply_unitary_`` / ``_linear_operator_`` methods exactly like
+python/ffsim/protocols/apply_unitary_protocol.py:48-88 and
+python/ffsim/protocols/linear_operator_protocol.py:40-60.
+"""
+
+from __future__ import annotations
+
+from typing import Any, Callable
+
+import numpy as np
+import torch
+
+
+def apply_unitary(vec, obj: Any, norb: int, nelec, copy: bool = True):
+    """Apply the unitary effect of ``obj`` to ``vec``."""
+    method = getattr(obj, "_apply_unitary_", None)
+    if method is not None:
+        result = method(vec, norb=norb, nelec=nelec, copy=copy)
+        if result is not NotImplemented:
+            return result
+    raise TypeError(
+        "ffsim_gb300.apply_unitary failed. Object doesn't have a unitary effect.\n"
+        f"type: {type(obj)}\nobject: {obj!r}\n"
+        "The object did not have an _apply_unitary_ method that returned a value besides "
+        "NotImplemented."
+    )
+
+
+def linear_operator(obj: Any, norb: int, nelec):
+    """Return the GPU linear operator of ``obj``."""
+    method = getattr(obj, "_linear_operator_", None)
+    if method is not None:
+        result = method(norb=norb, nelec=nelec)
+        if result is not NotImplemented:
+            return result
+    raise TypeError(f"Object of type {type(obj)} has no _linear_operator_ method.")
+
+
+class LinearOperator:
+    """A (dim x dim) operator acting on CUDA state vectors.
+
+    ``matvec`` / ``rmatvec`` / ``@`` accept torch CUDA complex tensors (the
+    result has the same dtype) or numpy arrays (moved to the GPU; a numpy
+    array is returned).  Like the reference's SciPy operators, the shape is
+    ``(dim, dim)`` and ``dtype`` is complex.
+    """
+
+    def __init__(self, shape: tuple[int, int], matvec: Callable, rmatvec: Callable | None = None,
+                 expectation: Callable | None = None, dtype=complex):
+        self.shape = shape
+        self.dtype = np.dtype(dtype)
+        self._matvec = matvec
+        self._rmatvec = rmatvec or matvec
+        self._expectation = expectation
+
+    def _run(self, fn, vec):
+        if isinstance(vec, torch.Tensor):
+            return fn(vec)
+        arr = np.asarray(vec)
+        if arr.ndim == 2 and arr.shape[1] == 1:
+            arr = arr[:, 0]
+        if not np.iscomplexobj(arr):
+            arr = arr.astype(np.complex128)
+        t = torch.from_numpy(np.ascontiguousarray(arr)).to("cuda")
+        return fn(t).cpu().numpy()
+
+    def matvec(self, vec):
+        return self._run(self._matvec, vec)
+
+    def rmatvec(self, vec):
+        return self._run(self._rmatvec, vec)
+
+    def __matmul__(self, vec):
+        return self.matvec(vec)
+
+    def expectation(self, vec) -> float:
+        """Real part of <vec|A|vec> in FP64 (fused when the operator supports it)."""
+        if self._expectation is not None:
+            if not isinstance(vec, torch.Tensor):
+                vec = torch.from_numpy(np.ascontiguousarray(np.asarray(vec, dtype=complex))).to("cuda")
+            return float(self._expectation(vec))
+        from ffsim_gb300.states import vdot
+
+        v = vec if isinstance(vec, torch.Tensor) else torch.from_numpy(np.asarray(vec, dtype=complex)).to("cuda")
+        return float(vdot(v, self._matvec(v)).real)

@@ -1,0 +1,217 @@
+/*
+ * ffsim_gb300 -- C ABI of the GB300 (sm_103a) statevector gate path.
+ *
+ * Every entry point takes plain pointers and sizes, never throws, and
+ * returns an ffgb_status.  Device pointers are owned by the caller; kernels
+ * run asynchronously on the given CUDA stream (cudaStream_t passed as void*,
+ * NULL = legacy default stream).  Complex arrays are interleaved
+ * (re, im) pairs.  Host matrices are row-major complex128 (norb*norb*2
+ * doubles) unless stated otherwise.
+ *
+ * State layout (identical to ffsim): a spinful state is a C-contiguous
+ * (dim_a, dim_b) array; row = alpha string address, column = beta string
+ * address; the address of an occupation bitstring is its rank in ascending
+ * integer order among bitstrings with the same number of set bits.
+ *
+ * Scratch: entry points that need device scratch take (scratch,
+ * scratch_bytes); ffgb_scratch_bytes() returns the required size.  The
+ * library keeps only small per-device lookup tables (occupation strings),
+ * created on first use for each (norb, nocc) with a synchronous copy; make
+ * the first call for a shape outside stream capture.
+ *
+ * Reference interfaces replaced (paths inside the ffsim project):
+ *   python/ffsim/_lib.pyi:36-123 and src/lib.rs:20-68 (PyO3 module ffsim._lib)
+ */
+#ifndef FFSIM_GB300_H
+#define FFSIM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  FFGB_OK = 0,
+  FFGB_ERR_ARG = 1,         /* invalid argument (maps to ValueError) */
+  FFGB_ERR_DTYPE = 2,       /* unsupported dtype (TypeError) */
+  FFGB_ERR_OOM = 3,         /* scratch too small / allocation failed (MemoryError) */
+  FFGB_ERR_CUDA = 4,        /* CUDA runtime error (RuntimeError) */
+  FFGB_ERR_TIMEOUT = 5,     /* bounded wait expired (TimeoutError) */
+  FFGB_ERR_UNSUPPORTED = 6, /* shape not supported (NotImplementedError) */
+  FFGB_ERR_NUMERIC = 7      /* host factorization failed (ArithmeticError) */
+} ffgb_status;
+
+typedef enum { FFGB_C64 = 0, FFGB_C128 = 1 } ffgb_dtype;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int ffgb_version(void);
+/* Message of the last error raised on the calling thread ("" if none). */
+const char* ffgb_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* Host-side linear algebra                                             */
+/* ------------------------------------------------------------------ */
+
+/* Givens decomposition U = D G_L^* ... G_1^* of a square unitary.
+ * Replaces givens_decomposition (src/linalg/givens.rs:68-149,
+ * python/ffsim/linalg/givens.py:59-156 exact path).
+ * rot_cs: [n(n-1)/2][3] = (c, Re s, Im s); rot_ij: [n(n-1)/2][2];
+ * *n_rot = number written; diag: [n][2]. */
+int ffgb_givens_decomposition(const double* mat, int n, double tol, double* rot_cs, int* rot_ij,
+                              int* n_rot, double* diag);
+
+/* Hermitian eigendecomposition (ascending eigenvalues; eigenvectors in the
+ * columns of vecs, row-major complex).  Host replacement of the
+ * scipy.linalg.eigh call in double_factorized_hamiltonian.py:250. */
+int ffgb_eigh(const double* mat, int n, double* eigvals, double* vecs);
+
+/* Plan of W(mat) on one spin sector, serialized for inspection/tests:
+ * out[0]=kind, out[1]=h, out[2]=max reconstruction error, then the plan
+ * coefficients.  Returns the number of doubles written in *len. */
+int ffgb_debug_plan(const double* mat, int norb, int use_windows, double* out, int cap, int* len);
+
+/* Scratch bytes needed by the functions below for a state of the given
+ * shape (op: 0 = orbital rotation / evolutions, 1 = linear operator matvec,
+ * 2 = expectation / energy). */
+size_t ffgb_scratch_bytes(int op, int dtype, int norb, int n_alpha, int n_beta);
+
+/* ------------------------------------------------------------------ */
+/* Gates (in place on vec)                                              */
+/* ------------------------------------------------------------------ */
+
+/* One adjacent Givens rotation on one spin sector (spin 0 = alpha rows,
+ * 1 = beta columns): for every string pair x (i occupied, j empty) / y:
+ * x <- c x + s y, y <- c y - conj(s) x.  Replaces
+ * apply_givens_rotation_in_place (src/gates/orbital_rotation.rs:18-104)
+ * with pair slices computed on the device.  |i - j| must be 1. */
+int ffgb_apply_givens_rotation(void* vec, int dtype, int norb, int n_alpha, int n_beta, int spin,
+                               double c, double s_re, double s_im, int i, int j, void* stream);
+
+/* Multiply every string with orbital orb occupied in one spin sector by
+ * phase.  Replaces apply_phase_shift_in_place (src/gates/phase_shift.rs:17-30). */
+int ffgb_apply_phase_shift(void* vec, int dtype, int norb, int n_alpha, int n_beta, int spin,
+                           double phase_re, double phase_im, int orb, void* stream);
+
+/* Orbital rotation W(mat_a) (x) W(mat_b); either matrix may be NULL (no
+ * action on that sector).  Replaces the Python driver
+ * python/ffsim/gates/orbital_rotation.py:117-199 and the per-Givens kernels.
+ * Spinless systems: n_beta = -1 and mat_b ignored (vec has C(norb, n_alpha)
+ * entries). */
+int ffgb_apply_orbital_rotation(void* vec, int dtype, int norb, int n_alpha, int n_beta,
+                                const double* mat_a, const double* mat_b, void* scratch,
+                                size_t scratch_bytes, void* stream);
+
+/* exp(-i t sum J^{st}_ij n_is n_jt / 2) (number representation) or the Z
+ * representation, optionally conjugated by orbital rotations (rot_a, rot_b:
+ * NULL = none).  mat_aa/mat_ab/mat_bb: real norb*norb row-major, NULL = no
+ * interaction of that type.  Replaces
+ * apply_diag_coulomb_evolution_in_place_{num,z}_rep
+ * (src/gates/diag_coulomb.rs:19-190) and the driver
+ * python/ffsim/gates/diag_coulomb.py:68-275.  Spinless: n_beta = -1. */
+int ffgb_apply_diag_coulomb_evolution(void* vec, int dtype, int norb, int n_alpha, int n_beta,
+                                      const double* mat_aa, const double* mat_ab,
+                                      const double* mat_bb, double time, int z_representation,
+                                      const double* rot_a, const double* rot_b, void* scratch,
+                                      size_t scratch_bytes, void* stream);
+
+/* exp(-i t sum_i lambda_i n_is), coeffs_a/coeffs_b real norb (NULL = none),
+ * optionally conjugated by orbital rotations.  Replaces
+ * apply_num_op_sum_evolution_in_place (src/gates/num_op_sum.rs:18-36) and
+ * python/ffsim/gates/num_op_sum.py:62-236.  Spinless: n_beta = -1. */
+int ffgb_apply_num_op_sum_evolution(void* vec, int dtype, int norb, int n_alpha, int n_beta,
+                                    const double* coeffs_a, const double* coeffs_b, double time,
+                                    const double* rot_a, const double* rot_b, void* scratch,
+                                    size_t scratch_bytes, void* stream);
+
+/* UCJ spin-balanced unitary: for each rep k, W(U_k^dag U_{k-1}) then the
+ * diag-Coulomb evolution with (J_aa, J_ab, J_aa) at time -1, then the final
+ * rotation W(U_final U_L) (U_final = I when final_rotation is NULL).
+ * diag_coulomb_mats: [n_reps][2][norb][norb] real; orbital_rotations:
+ * [n_reps][norb][norb] complex.  Replaces UCJOpSpinBalanced._apply_unitary_
+ * (python/ffsim/variational/ucj_spin_balanced.py:657-696). */
+int ffgb_ucj_spin_balanced_apply(void* vec, int dtype, int norb, int n_alpha, int n_beta,
+                                 int n_reps, const double* diag_coulomb_mats,
+                                 const double* orbital_rotations, const double* final_rotation,
+                                 void* scratch, size_t scratch_bytes, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Contractions and linear operators                                    */
+/* ------------------------------------------------------------------ */
+
+/* out (+)= Z vec with Z the diagonal Coulomb operator
+ * sum J^{st}_ij n_is n_jt / 2 (number rep.) or its Z representation.
+ * Replaces contract_diag_coulomb_into_buffer_{num,z}_rep
+ * (src/contract/diag_coulomb.rs:22-174) and
+ * python/ffsim/contract/diag_coulomb.py:41-192. */
+int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, int n_alpha,
+                               int n_beta, const double* mat_aa, const double* mat_ab,
+                               const double* mat_bb, int z_representation, int accumulate,
+                               void* stream);
+
+/* out (+)= sum_i lambda_i (n_ia + n_ib) vec.  Replaces
+ * contract_num_op_sum_spin_into_buffer (src/contract/num_op_sum.rs:20-39)
+ * and python/ffsim/contract/num_op_sum.py:27-72. */
+int ffgb_contract_num_op_sum(const void* vec, void* out, int dtype, int norb, int n_alpha,
+                             int n_beta, const double* coeffs, int accumulate, void* stream);
+
+/* out (+)= W(rot) Z W(rot)^dag vec, Z = diagonal operator given by
+ * (one_body[norb] on n_ia + n_ib) + (mat, z_representation) two-body part
+ * (mat may be NULL).  rot may be NULL.  This is one matvec of
+ * diag_coulomb_linop / num_op_sum_linop
+ * (python/ffsim/contract/diag_coulomb.py:195-272,
+ * python/ffsim/contract/num_op_sum.py:75-131). */
+int ffgb_rotated_diag_matvec(const void* vec, void* out, int dtype, int norb, int n_alpha,
+                             int n_beta, const double* one_body, const double* mat,
+                             int z_representation, const double* rot, int accumulate,
+                             void* scratch, size_t scratch_bytes, void* stream);
+
+/* Double-factorized Hamiltonian matvec out = H vec with
+ * H = sum_pq kappa_pq a^dag a + 1/2 sum_t sum J^(t) n^(t) n^(t) + constant
+ * (one_body_tensor complex norb*norb; diag_coulomb_mats [n_terms][norb][norb]
+ * real; orbital_rotations [n_terms][norb][norb] complex).  Replaces
+ * DoubleFactorizedHamiltonian._linear_operator_ matvec
+ * (python/ffsim/hamiltonians/double_factorized_hamiltonian.py:244-275). */
+int ffgb_df_matvec(const void* vec, void* out, int dtype, int norb, int n_alpha, int n_beta,
+                   const double* one_body_tensor, int n_terms, const double* diag_coulomb_mats,
+                   const double* orbital_rotations, double constant, int z_representation,
+                   void* scratch, size_t scratch_bytes, void* stream);
+
+/* Energy <vec|H|vec> of the same Hamiltonian, fused: each term rotates the
+ * state into its basis and reduces sum_z z |phi|^2 in FP64 without forming
+ * H vec.  pre_rotation (NULL = none) is applied to vec before every term
+ * (used to merge a circuit's final orbital rotation).  *energy_out is a
+ * host double; the call synchronizes the stream.  Matches
+ * np.vdot(vec, H @ vec).real (tests/python/variational/ucj_spin_balanced_test.py:152-158). */
+int ffgb_df_expectation(const void* vec, int dtype, int norb, int n_alpha, int n_beta,
+                        const double* one_body_tensor, int n_terms,
+                        const double* diag_coulomb_mats, const double* orbital_rotations,
+                        double constant, int z_representation, const double* pre_rotation,
+                        double* energy_out, void* scratch, size_t scratch_bytes, void* stream);
+
+/* LUCJ energy from the Hartree-Fock state (or from vec_in when not NULL):
+ * applies the UCJ circuit without its last rotation, merges that rotation
+ * into every Hamiltonian term and returns <psi|H|psi>.  work_state must hold
+ * one state (dim_a*dim_b complex of dtype).  Synchronizes the stream. */
+int ffgb_lucj_energy(const void* vec_in, void* work_state, int dtype, int norb, int n_alpha,
+                     int n_beta, int n_reps, const double* ucj_diag_coulomb_mats,
+                     const double* ucj_orbital_rotations, const double* ucj_final_rotation,
+                     const double* one_body_tensor, int n_terms, const double* diag_coulomb_mats,
+                     const double* orbital_rotations, double constant, double* energy_out,
+                     void* scratch, size_t scratch_bytes, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Reductions and helpers                                               */
+/* ------------------------------------------------------------------ */
+
+/* out[0..1] = sum conj(x) y in FP64 (host pointer; synchronizes). */
+int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out, void* stream);
+
+/* vec <- one-hot at address 0 (Hartree-Fock state, states/slater.py:122-138). */
+int ffgb_hartree_fock(void* vec, int dtype, long long n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFSIM_GB300_H */

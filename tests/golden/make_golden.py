@@ -1,0 +1,356 @@
+"""Generate golden vectors by running the reference's own Python code.
+
+Run in a container that has the ffsim source tree (read-only) at
+``FFSIM_REF`` (default ``/root/reference``)::
+
+    python tests/golden/make_golden.py
+
+The reference package cannot be imported whole here: its Rust extension
+``ffsim._lib`` is not built (no Rust toolchain) and ``pyscf`` / ``jax`` are not
+installed.  This script therefore loads the individual reference modules on
+the hot path from their source files and satisfies their imports with:
+
+* ``ffsim._lib`` -> the reference's own pure-Python kernel restatements in
+  ``python/ffsim/_slow/`` (which the reference's tests assert equal to the
+  Rust kernels), plus a one-line phase shift (``src/gates/phase_shift.rs``)
+  and the oracle's restatement of ``givens_decomposition`` (Rust-only in the
+  reference; pinned separately by reconstruction and determinant checks);
+* ``pyscf.fci.cistring`` -> ``make_strings`` / ``gen_occslst`` restated from
+  their combinatorial definition (subsets of the orbital list in colexicographic
+  order of positions, which gives ascending integers for ``range(norb)``);
+* ``jax`` / ``opt_einsum`` / ``pyscf.ci`` -> inert placeholders (only used off
+  the path).
+
+Everything above the kernels -- reshapes, transposes, the ``s.conjugate()``
+convention, pair slices, diagonal halving, ``None`` handling, linear operator
+composition, UCJ rotation merging -- is the reference's own code.  The
+outputs are written to ``tests/golden/golden.npz``.
+"""
+
+from __future__ import annotations
+
+import importlib.util
+import itertools
+import math
+import os
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+import scipy.linalg
+
+REF = Path(os.environ.get("FFSIM_REF", "/root/reference"))
+PKG = REF / "python" / "ffsim"
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from oracle import ffsim_oracle as orc  # noqa: E402  (givens restatement only)
+
+
+def _module(name: str, attrs: dict | None = None, is_pkg: bool = False):
+    mod = types.ModuleType(name)
+    if is_pkg:
+        mod.__path__ = []
+    for k, v in (attrs or {}).items():
+        setattr(mod, k, v)
+    sys.modules[name] = mod
+    parent, _, child = name.rpartition(".")
+    if parent and parent in sys.modules:
+        setattr(sys.modules[parent], child, mod)
+    return mod
+
+
+def _load(name: str, relpath: str):
+    spec = importlib.util.spec_from_file_location(name, PKG / relpath)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    parent, _, child = name.rpartition(".")
+    if parent in sys.modules:
+        setattr(sys.modules[parent], child, mod)
+    return mod
+
+
+# ---- pyscf.fci.cistring (combinatorial definition) -------------------------
+
+
+def _make_strings(orb_list, nocc):
+    orb_list = list(orb_list)
+    m = len(orb_list)
+    if nocc == 0:
+        return np.asarray([0], dtype=np.int64)
+    if nocc > m:
+        return np.asarray([], dtype=np.int64)
+    subsets = sorted(
+        itertools.combinations(range(m), nocc), key=lambda c: sum(1 << p for p in c)
+    )
+    return np.asarray(
+        [sum(1 << int(orb_list[p]) for p in c) for c in subsets], dtype=np.int64
+    )
+
+
+def _gen_occslst(orb_list, nocc):
+    strings = _make_strings(orb_list, nocc)
+    occ = [[i for i in range(64) if (int(s) >> i) & 1] for s in strings]
+    return np.asarray(occ, dtype=np.int32).reshape(len(strings), nocc)
+
+
+def install_stubs():
+    _module("pyscf", is_pkg=True)
+    _module("pyscf.fci", is_pkg=True)
+    _module("pyscf.fci.cistring", {"make_strings": _make_strings, "gen_occslst": _gen_occslst})
+    _module("pyscf.ci", is_pkg=True)
+    jax = _module("jax", {"config": types.SimpleNamespace(update=lambda *a, **k: None)})
+    jax.numpy = _module("jax.numpy")
+    if importlib.util.find_spec("opt_einsum") is None:
+        _module("opt_einsum", {"contract": np.einsum})
+
+    ffsim = _module("ffsim", is_pkg=True)
+    ffsim.__path__ = [str(PKG)]
+    # _slow kernels (reference's own restatements of the Rust kernels)
+    _module("ffsim.gates", is_pkg=True)
+    _module("ffsim.gates.basic_gates", {"_apply_phase_shift": None})
+    slow_orb = _load("ffsim_slow_orb", "_slow/gates/orbital_rotation.py")
+    slow_dc = _load("ffsim_slow_dc", "_slow/gates/diag_coulomb.py")
+    slow_nos = _load("ffsim_slow_nos", "_slow/gates/num_op_sum.py")
+    slow_cdc = _load("ffsim_slow_cdc", "_slow/contract/diag_coulomb.py")
+    slow_cnos = _load("ffsim_slow_cnos", "_slow/contract/num_op_sum.py")
+
+    def apply_phase_shift_in_place(vec, phase, indices):
+        vec[indices] *= phase
+
+    lib = _module(
+        "ffsim._lib",
+        {
+            "apply_givens_rotation_in_place": slow_orb.apply_givens_rotation_in_place_slow,
+            "apply_phase_shift_in_place": apply_phase_shift_in_place,
+            "apply_num_op_sum_evolution_in_place": slow_nos.apply_num_op_sum_evolution_in_place_slow,
+            "apply_diag_coulomb_evolution_in_place_num_rep": slow_dc.apply_diag_coulomb_evolution_in_place_num_rep_slow,
+            "apply_diag_coulomb_evolution_in_place_z_rep": slow_dc.apply_diag_coulomb_evolution_in_place_z_rep_slow,
+            "contract_diag_coulomb_into_buffer_num_rep": slow_cdc.contract_diag_coulomb_into_buffer_num_rep_slow,
+            "contract_diag_coulomb_into_buffer_z_rep": slow_cdc.contract_diag_coulomb_into_buffer_z_rep_slow,
+            "contract_num_op_sum_spin_into_buffer": slow_cnos.contract_num_op_sum_spin_into_buffer_slow,
+            "givens_decomposition": lambda mat, tol=1e-12: orc.givens_decomposition(mat, tol),
+        },
+    )
+    _module("ffsim.linalg", is_pkg=True)
+    givens = types.SimpleNamespace()
+    sys.modules["ffsim.linalg"].givens_decomposition = lambda mat, tol=1e-12: lib.givens_decomposition(
+        np.asarray(mat, dtype=complex), tol
+    )
+    del givens
+    _load("ffsim._cistring", "_cistring.py")
+    _load("ffsim.states_dimensions", "states/dimensions.py")
+    gor = _load("ffsim.gates.orbital_rotation", "gates/orbital_rotation.py")
+    gdc = _load("ffsim.gates.diag_coulomb", "gates/diag_coulomb.py")
+    gnos = _load("ffsim.gates.num_op_sum", "gates/num_op_sum.py")
+    sys.modules["ffsim.gates"].apply_orbital_rotation = gor.apply_orbital_rotation
+    sys.modules["ffsim.gates"].apply_diag_coulomb_evolution = gdc.apply_diag_coulomb_evolution
+    sys.modules["ffsim.gates"].apply_num_op_sum_evolution = gnos.apply_num_op_sum_evolution
+    _module("ffsim.contract", is_pkg=True)
+    cdc = _load("ffsim.contract.diag_coulomb", "contract/diag_coulomb.py")
+    cnos = _load("ffsim.contract.num_op_sum", "contract/num_op_sum.py")
+    _load("ffsim.linalg.util", "linalg/util.py")
+    pred = _load("ffsim.linalg.predicates", "linalg/predicates.py")
+    sys.modules["ffsim.linalg"].is_real_symmetric = pred.is_real_symmetric
+    sys.modules["ffsim.linalg"].is_unitary = pred.is_unitary
+    _module("ffsim.variational", is_pkg=True)
+    _load("ffsim.variational.util", "variational/util.py")
+    proto = _module("ffsim.protocols", is_pkg=True)
+    proto.SupportsApplyUnitary = type("SupportsApplyUnitary", (), {})
+    proto.SupportsApproximateEquality = type("SupportsApproximateEquality", (), {})
+    ffsim.gates = sys.modules["ffsim.gates"]
+    ffsim.linalg = sys.modules["ffsim.linalg"]
+    ffsim.protocols = proto
+    ucj = _load("ffsim.variational.ucj_spin_balanced", "variational/ucj_spin_balanced.py")
+    return types.SimpleNamespace(
+        apply_orbital_rotation=gor.apply_orbital_rotation,
+        apply_diag_coulomb_evolution=gdc.apply_diag_coulomb_evolution,
+        apply_num_op_sum_evolution=gnos.apply_num_op_sum_evolution,
+        contract_diag_coulomb=cdc.contract_diag_coulomb,
+        diag_coulomb_linop=cdc.diag_coulomb_linop,
+        contract_num_op_sum=cnos.contract_num_op_sum,
+        num_op_sum_linop=cnos.num_op_sum_linop,
+        zero_one_subspace_indices=gor._zero_one_subspace_indices,
+        one_subspace_indices=gor._one_subspace_indices,
+        UCJOpSpinBalanced=ucj.UCJOpSpinBalanced,
+    )
+
+
+def df_matvec(ref, one_body, dcm, rots, constant, norb, nelec, z_rep):
+    """Body of DoubleFactorizedHamiltonian._linear_operator_
+    (hamiltonians/double_factorized_hamiltonian.py:244-275) over the
+    reference's own linear operators."""
+    eigs, vecs = scipy.linalg.eigh(one_body)
+    num_linop = ref.num_op_sum_linop(eigs, norb, nelec, orbital_rotation=vecs)
+    linops = [
+        ref.diag_coulomb_linop(m, norb, nelec, orbital_rotation=u, z_representation=z_rep)
+        for m, u in zip(dcm, rots)
+    ]
+
+    def matvec(vec):
+        vec = vec.astype(complex, copy=False)
+        result = constant * vec
+        result += num_linop @ vec
+        for linop in linops:
+            result += linop @ vec
+        return result
+
+    return matvec
+
+
+def main():
+    ref = install_stubs()
+    rng = np.random.default_rng(20260603)
+    out: dict[str, np.ndarray] = {}
+
+    # pair / occupied index subsets
+    for norb, nocc, orbs in [(5, 2, (1, 2)), (5, 3, (3, 2)), (6, 3, (0, 1)), (4, 2, (2, 3))]:
+        key = f"zero_one_{norb}_{nocc}_{orbs[0]}{orbs[1]}"
+        out[key] = np.asarray(ref.zero_one_subspace_indices(norb, nocc, orbs), dtype=np.int64)
+    for norb, nocc, i in [(5, 2, 0), (5, 3, 4), (6, 3, 2)]:
+        out[f"one_{norb}_{nocc}_{i}"] = np.asarray(
+            ref.one_subspace_indices(norb, nocc, (i,)), dtype=np.int64
+        )
+
+    # orbital rotations
+    cases = [(5, (3, 2)), (5, (2, 3)), (6, (3, 3)), (4, (3, 2)), (3, (2, 1)), (2, (1, 1)),
+             (1, (1, 0)), (1, (0, 1)), (2, (2, 2)), (7, (3, 4))]
+    for idx, (norb, nelec) in enumerate(cases):
+        d = orc.dim(norb, nelec)
+        vec = orc.random_state_vector(d, seed=rng)
+        ua = orc.random_unitary(norb, seed=rng)
+        ub = orc.random_unitary(norb, seed=rng)
+        out[f"rot{idx}_in"] = vec
+        out[f"rot{idx}_ua"] = ua
+        out[f"rot{idx}_ub"] = ub
+        out[f"rot{idx}_same"] = ref.apply_orbital_rotation(vec, ua, norb, nelec)
+        out[f"rot{idx}_pair"] = ref.apply_orbital_rotation(vec, (ua, ub), norb, nelec)
+        out[f"rot{idx}_aonly"] = ref.apply_orbital_rotation(vec, (ua, None), norb, nelec)
+        out[f"rot{idx}_bonly"] = ref.apply_orbital_rotation(vec, (None, ub), norb, nelec)
+    out["rot_cases"] = np.asarray([[n, a, b] for n, (a, b) in cases])
+
+    # spinless rotation
+    vec = orc.random_state_vector(math.comb(6, 2), seed=rng)
+    u = orc.random_unitary(6, seed=rng)
+    out["rotsl_in"], out["rotsl_u"] = vec, u
+    out["rotsl_out"] = ref.apply_orbital_rotation(vec, u, 6, 2)
+
+    # diag-Coulomb evolution, number and Z representations, with rotations
+    dc_cases = [(5, (3, 2)), (4, (2, 2)), (6, (3, 2)), (3, (1, 2))]
+    for idx, (norb, nelec) in enumerate(dc_cases):
+        d = orc.dim(norb, nelec)
+        vec = orc.random_state_vector(d, seed=rng)
+        jaa = orc.random_symmetric_normal(norb, scale=0.7, seed=rng)
+        jab = rng.standard_normal((norb, norb))
+        jbb = orc.random_symmetric_normal(norb, scale=0.7, seed=rng)
+        t = float(rng.uniform(-2, 2))
+        u = orc.random_unitary(norb, seed=rng)
+        out[f"dc{idx}_in"], out[f"dc{idx}_jaa"], out[f"dc{idx}_jab"] = vec, jaa, jab
+        out[f"dc{idx}_jbb"], out[f"dc{idx}_t"], out[f"dc{idx}_u"] = jbb, np.asarray(t), u
+        out[f"dc{idx}_num"] = ref.apply_diag_coulomb_evolution(vec, (jaa, jab, jbb), t, norb, nelec)
+        out[f"dc{idx}_z"] = ref.apply_diag_coulomb_evolution(
+            vec, (jaa, jab, jbb), t, norb, nelec, z_representation=True
+        )
+        out[f"dc{idx}_single"] = ref.apply_diag_coulomb_evolution(vec, jaa, t, norb, nelec)
+        out[f"dc{idx}_none"] = ref.apply_diag_coulomb_evolution(vec, (None, jab, None), t, norb, nelec)
+        out[f"dc{idx}_rot"] = ref.apply_diag_coulomb_evolution(
+            vec, (jaa, jab, jbb), t, norb, nelec, orbital_rotation=u
+        )
+        out[f"dc{idx}_zrot"] = ref.apply_diag_coulomb_evolution(
+            vec, jaa, t, norb, nelec, orbital_rotation=u, z_representation=True
+        )
+        # contractions
+        out[f"dc{idx}_cnum"] = ref.contract_diag_coulomb(vec, (jaa, jab, jbb), norb, nelec)
+        out[f"dc{idx}_cz"] = ref.contract_diag_coulomb(
+            vec, (jaa, jab, jbb), norb, nelec, z_representation=True
+        )
+        out[f"dc{idx}_csingle"] = ref.contract_diag_coulomb(vec, jaa, norb, nelec)
+        out[f"dc{idx}_linop"] = ref.diag_coulomb_linop(jaa, norb, nelec, orbital_rotation=u) @ vec
+    out["dc_cases"] = np.asarray([[n, a, b] for n, (a, b) in dc_cases])
+
+    # spinless diag-Coulomb
+    vec = orc.random_state_vector(math.comb(5, 2), seed=rng)
+    j = orc.random_symmetric_normal(5, seed=rng)
+    out["dcsl_in"], out["dcsl_j"] = vec, j
+    out["dcsl_out"] = ref.apply_diag_coulomb_evolution(vec, j, 0.3, 5, 2)
+
+    # num-op-sum evolution and contraction
+    for idx, (norb, nelec) in enumerate([(5, (3, 2)), (4, (1, 3))]):
+        d = orc.dim(norb, nelec)
+        vec = orc.random_state_vector(d, seed=rng)
+        ca = rng.standard_normal(norb)
+        cb = rng.standard_normal(norb)
+        u = orc.random_unitary(norb, seed=rng)
+        t = float(rng.uniform(-2, 2))
+        out[f"nos{idx}_in"], out[f"nos{idx}_ca"], out[f"nos{idx}_cb"] = vec, ca, cb
+        out[f"nos{idx}_u"], out[f"nos{idx}_t"] = u, np.asarray(t)
+        out[f"nos{idx}_pair"] = ref.apply_num_op_sum_evolution(vec, (ca, cb), t, norb, nelec)
+        out[f"nos{idx}_rot"] = ref.apply_num_op_sum_evolution(vec, ca, t, norb, nelec, orbital_rotation=u)
+        out[f"nos{idx}_bonly"] = ref.apply_num_op_sum_evolution(vec, (None, cb), t, norb, nelec)
+        out[f"nos{idx}_contract"] = ref.contract_num_op_sum(vec, ca, norb, nelec)
+        out[f"nos{idx}_linop"] = ref.num_op_sum_linop(ca, norb, nelec, orbital_rotation=u) @ vec
+
+    # double-factorized Hamiltonian matvec and energy
+    for idx, (norb, nelec, n_terms, z_rep) in enumerate([(4, (2, 2), 3, False), (5, (3, 2), 2, False),
+                                                         (4, (2, 1), 2, True)]):
+        d = orc.dim(norb, nelec)
+        vec = orc.random_state_vector(d, seed=rng)
+        g = rng.standard_normal((norb, norb)) + 1j * rng.standard_normal((norb, norb))
+        one_body = (g + g.conj().T) / 2
+        dcm = np.stack([orc.random_symmetric_normal(norb, seed=rng) for _ in range(n_terms)])
+        rots = np.stack([orc.random_unitary(norb, seed=rng) for _ in range(n_terms)])
+        const = float(rng.standard_normal())
+        mv = df_matvec(ref, one_body, dcm, rots, const, norb, nelec, z_rep)
+        hv = mv(vec)
+        out[f"df{idx}_in"], out[f"df{idx}_h1"], out[f"df{idx}_dcm"] = vec, one_body, dcm
+        out[f"df{idx}_rots"], out[f"df{idx}_const"] = rots, np.asarray(const)
+        out[f"df{idx}_z"] = np.asarray(z_rep)
+        out[f"df{idx}_hv"] = hv
+        out[f"df{idx}_energy"] = np.asarray(np.vdot(vec, hv).real)
+    out["df_cases"] = np.asarray([[4, 2, 2, 3], [5, 3, 2, 2], [4, 2, 1, 2]])
+
+    # UCJ spin-balanced apply_unitary (reference dataclass method)
+    for idx, (norb, nelec, n_reps, final) in enumerate([(4, (2, 2), 2, False), (5, (3, 2), 1, True),
+                                                        (6, (3, 3), 3, False)]):
+        d = orc.dim(norb, nelec)
+        n_params = n_reps * (norb * (norb + 1) + norb**2) + (norb**2 if final else 0)
+        params = rng.uniform(-1, 1, size=n_params)
+        op = ref.UCJOpSpinBalanced.from_parameters(
+            params, norb=norb, n_reps=n_reps, with_final_orbital_rotation=final
+        )
+        vec = orc.random_state_vector(d, seed=rng)
+        hf = orc.hartree_fock_state(norb, nelec)
+        out[f"ucj{idx}_params"] = params
+        out[f"ucj{idx}_dcm"] = op.diag_coulomb_mats
+        out[f"ucj{idx}_rots"] = op.orbital_rotations
+        out[f"ucj{idx}_final"] = (
+            op.final_orbital_rotation if final else np.zeros((0, 0), dtype=complex)
+        )
+        out[f"ucj{idx}_in"] = vec
+        out[f"ucj{idx}_out"] = op._apply_unitary_(vec, norb, nelec, copy=True)
+        out[f"ucj{idx}_hf_out"] = op._apply_unitary_(hf, norb, nelec, copy=True)
+    out["ucj_cases"] = np.asarray([[4, 2, 2, 2, 0], [5, 3, 2, 1, 1], [6, 3, 3, 3, 0]])
+
+    # synthetic configuration 0: norb=8, (4,4), rotation then diag-Coulomb t=0.7
+    r0 = np.random.default_rng(0)
+    vec = orc.random_state_vector(4900, seed=r0)
+    u = orc.random_unitary(8, seed=r0)
+    j = orc.random_symmetric_normal(8, scale=0.5, seed=r0)
+    mid = ref.apply_orbital_rotation(vec, u, 8, (4, 4))
+    out["cfg0_in"], out["cfg0_u"], out["cfg0_j"] = vec, u, j
+    out["cfg0_out"] = ref.apply_diag_coulomb_evolution(mid, j, 0.7, 8, (4, 4))
+
+    # reference fixture: tests/python/test_data/orbital_rotation-0.npy on HF (8, (5, 5))
+    mat = np.load(REF / "tests" / "python" / "test_data" / "orbital_rotation-0.npy")
+    hf = orc.hartree_fock_state(8, (5, 5))
+    out["fix_mat"] = mat
+    out["fix_out"] = ref.apply_orbital_rotation(hf, mat, 8, (5, 5))
+
+    np.savez_compressed(HERE / "golden.npz", **out)
+    print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+"""Host-side checks that need no GPU: the C ABI library loads and exports
+every declared symbol, and the host planning code (Givens decomposition,
+eigendecomposition, cosine-sine plans with the kernel's addressing) matches
+the oracle."""
+
+from __future__ import annotations
+
+import math
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import plan_emulator as pe
+from oracle import ffsim_oracle as o
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "ffsim_gb300.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(ffgb_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    from ffsim_gb300 import _lib
+
+    lib = _lib.load()
+    names = _declared_symbols()
+    assert len(names) >= 20
+    for name in names:
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, name
+    assert lib.ffgb_version() >= 100
+
+
+def test_givens_decomposition_matches_oracle():
+    import ffsim_gb300 as f
+
+    rng = np.random.default_rng(11)
+    for n in range(1, 13):
+        u = o.random_unitary(n, seed=rng)
+        got, gd = f.linalg.givens_decomposition(u)
+        ref, rd = o.givens_decomposition(u)
+        assert len(got) == len(ref)
+        for (c1, s1, i1, j1), (c2, s2, i2, j2) in zip(got, ref):
+            assert (i1, j1) == (i2, j2)
+            assert abs(c1 - c2) < 1e-12 and abs(s1 - s2) < 1e-12
+        np.testing.assert_allclose(gd, rd, atol=1e-12)
+    with pytest.raises(ValueError):
+        f.linalg.givens_decomposition(np.zeros((2, 3)))
+
+
+def test_givens_tolerance_skips_identity():
+    import ffsim_gb300 as f
+
+    rots, diag = f.linalg.givens_decomposition(np.eye(5))
+    assert rots == []
+    np.testing.assert_allclose(diag, np.ones(5))
+
+
+def test_eigh():
+    import ffsim_gb300 as f
+
+    rng = np.random.default_rng(3)
+    for n in (1, 4, 9, 16):
+        g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        h = (g + g.conj().T) / 2
+        w, v = f.linalg.eigh(h)
+        np.testing.assert_allclose(w, np.linalg.eigvalsh(h), atol=1e-12)
+        np.testing.assert_allclose(v @ np.diag(w) @ v.conj().T, h, atol=1e-12)
+
+
+def _plan(u, use_windows):
+    from ffsim_gb300 import _lib
+
+    m = _lib.cmat(u)
+    out = np.zeros(20000)
+    n = np.zeros(1, dtype=np.int32)
+    _lib.call("ffgb_debug_plan", _lib.dptr(m), u.shape[0], int(use_windows), _lib.dptr(out), len(out),
+              n.ctypes.data_as(_lib._ip))
+    return pe.parse(out[: n[0]])
+
+
+@pytest.mark.parametrize("norb, nocc", [(1, 1), (2, 1), (4, 2), (5, 3), (7, 3), (8, 4), (9, 4), (9, 5),
+                                         (10, 5), (11, 4), (12, 6), (13, 6)])
+@pytest.mark.parametrize("use_windows", [True, False])
+def test_plan_addressing_matches_oracle(norb, nocc, use_windows):
+    """The serialized plan applied with the kernel's addressing equals W(U)."""
+    rng = np.random.default_rng(norb * 31 + nocc)
+    u = o.random_unitary(norb, seed=rng)
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=rng)
+    plan = _plan(u, use_windows)
+    expect_kind = (2 if norb <= 8 else 3) if use_windows else 1
+    assert plan["kind"] == expect_kind
+    assert plan["err"] < 1e-12
+    got = pe.apply_plan(plan, vec, norb, nocc)
+    np.testing.assert_allclose(got, o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-12)
+
+
+def test_plan_special_matrices():
+    """Identity, permutations and block-diagonal unitaries (degenerate cosine-sine cases)."""
+    for norb, nocc in [(10, 5), (12, 5), (16, 8)]:
+        mats = [np.eye(norb), np.eye(norb)[::-1].copy(), np.roll(np.eye(norb), 3, axis=0)]
+        blk = np.zeros((norb, norb), dtype=complex)
+        h = norb // 2
+        blk[:h, :h] = o.random_unitary(h, seed=1)
+        blk[h:, h:] = o.random_unitary(norb - h, seed=2)
+        mats.append(blk)
+        for u in mats:
+            plan = _plan(u.astype(complex), True)
+            assert plan["err"] < 1e-12
+            if norb <= 12:
+                vec = o.random_state_vector(math.comb(norb, nocc), seed=3)
+                np.testing.assert_allclose(pe.apply_plan(plan, vec, norb, nocc),
+                                           o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-12)
+
+
+def test_scratch_sizes():
+    from ffsim_gb300 import _lib
+
+    lib = _lib.load()
+    s64 = lib.ffgb_scratch_bytes(0, 0, 16, 8, 8)
+    s128 = lib.ffgb_scratch_bytes(0, 1, 16, 8, 8)
+    assert s64 >= 12870**2 * 8 and s128 >= 12870**2 * 16
+    assert lib.ffgb_scratch_bytes(1, 0, 16, 8, 8) >= 2 * 12870**2 * 8
+
+
+def test_argument_errors_map_to_python_exceptions():
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _lib
+
+    with pytest.raises(TypeError):
+        _lib.call("ffgb_apply_orbital_rotation", None, 7, 4, 2, 2, None, None, None, 0, None)
+    with pytest.raises(ValueError):
+        _lib.call("ffgb_apply_orbital_rotation", None, 0, 4, 5, 2, None, None, None, 0, None)
+    with pytest.raises(NotImplementedError):
+        _lib.call("ffgb_apply_orbital_rotation", None, 0, 40, 2, 2, None, None, None, 0, None)
+    assert f.dim(16, (8, 8)) == 12870**2
