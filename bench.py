@@ -1,0 +1,373 @@
+"""LUCJ energy throughput on one GB300 (or N independent replicas).
+
+Workload (the metric's configuration): norb=16, nelec=(8,8) (dim_a = dim_b =
+12870, 1.656e8 amplitudes), spin-balanced UCJ with n_reps=2 applied to the
+Hartree-Fock state (Haar orbital rotations, diag-Coulomb entries N(0,0.1)),
+then <psi|H|psi> for a synthetic double-factorized Hamiltonian (Hermitian
+one-body N(0,1)/16, rank 32, Haar term rotations, J_t entries N(0,0.05),
+constant -100).  Inputs are seeded synthetic data (the reference publishes no
+dataset).  A step is one energy evaluation.
+
+Reported:
+* value      complex64 evaluations/s, device time (CUDA events on the
+             launching stream), inputs resident; max over ranks, summed over
+             ranks (replicas).
+* e2e        the same through the public API ``ffsim_gb300.lucj_energy`` with
+             host (numpy) inputs and the energy read back every step.
+* complex128 the plain complex128 GPU path on the same GPU (fewer steps).
+* roofline   the dominant kernel (two-pass orbital rotation, 4 S algorithmic
+             bytes per rotation with S the state size) against the measured
+             copy bandwidth in MEASURED_PEAKS.json.
+* cpu_baseline the C/OpenMP restatement of the reference CPU algorithm on a
+             bounded sample (one orbital rotation + one diag-Coulomb evolution
+             at norb=16, complex128), extrapolated to one evaluation.
+
+``--impl reference`` times that CPU restatement alone as the reference arm.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+NORB, NELEC, N_REPS, RANK = 16, (8, 8), 2, 32
+METRIC = "LUCJ energy evals/s norb=16 (8,8) c64 vs c128 at |dE|<=1e-6 Ha; p50/p99 ms"
+WORKLOAD = "LUCJ n_reps=2 from HF + DF Hamiltonian rank 32 energy, norb=16, nelec=(8,8)"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs(seed: int = 2026):
+    import ffsim_gb300 as f
+
+    ucj = f.random.random_ucj_op_spin_balanced(NORB, n_reps=N_REPS, diag_coulomb_normal=True,
+                                               diag_coulomb_scale=0.1, seed=seed)
+    ham = f.random.random_df_hamiltonian_normal(NORB, rank=RANK, seed=seed + 1)
+    return ucj, ham
+
+
+def time_energy(dtype, steps, warmup, ucj, ham, stream):
+    """Per-step CUDA-event times (ms) of LUCJ energy evaluations on `stream`."""
+    import torch
+
+    import ffsim_gb300 as f
+
+    ev = f.LUCJEnergy(NORB, NELEC, dtype=dtype)
+    energies = []
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            energies.append(ev(ucj, ham))
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for k in range(steps):
+            starts[k].record(stream)
+            energies.append(ev(ucj, ham))
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    del ev
+    torch.cuda.empty_cache()
+    return times, energies
+
+
+def time_e2e(steps, ucj, ham):
+    """Wall time per evaluation through the public API with host inputs."""
+    import torch
+
+    import ffsim_gb300 as f
+
+    ev = f.LUCJEnergy(NORB, NELEC, dtype=torch.complex64)
+    ev(ucj, ham)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ev(ucj, ham)  # numpy inputs -> planning -> kernels -> energy read back (synchronizes)
+    t1 = time.perf_counter()
+    del ev
+    torch.cuda.empty_cache()
+    return (t1 - t0) / steps
+
+
+def rotation_roofline(stream, reps: int = 6):
+    """Average time of one complex64 orbital rotation (two transposing passes of
+    the sector kernel) on a resident norb=16 state, and its algorithmic GB/s."""
+    import numpy as np
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _lib
+    from ffsim_gb300._state import scratch
+
+    d = f.dim(NORB, NELEC)
+    S = d * 8
+    u = f.random.random_unitary(NORB, seed=99)
+    with torch.cuda.stream(stream):
+        v = torch.randn(d, dtype=torch.complex64, device="cuda")
+        buf, nbytes = scratch(v, 0, NORB, *NELEC)
+        m = _lib.cmat(u)
+        sptr = stream.cuda_stream
+
+        def rot():
+            _lib.call("ffgb_apply_orbital_rotation", v.data_ptr(), _lib.FFGB_C64, NORB, NELEC[0], NELEC[1],
+                      _lib.dptr(m), _lib.dptr(m), buf.data_ptr(), nbytes, sptr)
+
+        for _ in range(2):
+            rot()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            rot()
+        b.record(stream)
+        torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    del v, buf
+    torch.cuda.empty_cache()
+    return ms, 4 * S / (ms * 1e-3) / 1e9, S, np
+
+
+def cpu_reference_sample(threads: int | None = None):
+    """Time the C restatement of the reference on one orbital rotation and one
+    diag-Coulomb evolution at norb=16 (complex128) and extrapolate one LUCJ
+    energy evaluation: (L+1) rotations + L evolutions + (R+1) DF terms, each term
+    2 rotations + 1 contraction (about one evolution's cost)."""
+    import numpy as np
+
+    from oracle import cpu_ref, ffsim_oracle as o
+
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    cpu_ref.lib()
+    cpu_ref.init_cache(NORB, NELEC)
+    d = o.dim(NORB, NELEC)
+    rng = np.random.default_rng(5)
+    vec = (rng.standard_normal(d) + 1j * rng.standard_normal(d)) / math.sqrt(2 * d)
+    u = o.random_unitary(NORB, seed=rng)
+    j = o.random_symmetric_normal(NORB, scale=0.1, seed=rng)
+    t0 = time.perf_counter()
+    w = cpu_ref.apply_orbital_rotation(vec, u, NORB, NELEC)
+    t1 = time.perf_counter()
+    cpu_ref.apply_diag_coulomb_evolution(w, j, -1.0, NORB, NELEC)
+    t2 = time.perf_counter()
+    t_rot, t_dc = t1 - t0, t2 - t1
+    t_eval = (N_REPS + 1) * t_rot + N_REPS * t_dc + (RANK + 1) * (2 * t_rot + t_dc)
+    return t_eval, t_rot, t_dc
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    samples = []
+    t_rot = t_dc = None
+    for k in range(args.warmup + args.steps):
+        t_eval, t_rot, t_dc = cpu_reference_sample(cores)
+        if k >= args.warmup:
+            samples.append(t_eval)
+    t = statistics.median(samples)
+    val = 1.0 / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "evals/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "norb": NORB, "nelec": list(NELEC), "n_reps": N_REPS,
+                   "df_rank": RANK, "l2": "state (2.65 GB) larger than L2"},
+        "cpu_baseline": {"value": val, "unit": "evals/s", "cores": cores, "kind": "port",
+                         "sample": f"one orbital rotation ({t_rot:.2f} s) + one diag-Coulomb evolution "
+                                   f"({t_dc:.2f} s) at norb=16 complex128 per step, extrapolated to "
+                                   f"{N_REPS + 1} rotations + {N_REPS} evolutions + {RANK + 1} DF terms"},
+        "e2e": {"value": val, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--c128-steps", type=int, default=2)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    from ffsim_gb300 import _lib
+
+    lib = _lib.load()
+    ucj, ham = make_inputs(2026 + rank)
+    stream = torch.cuda.Stream()
+
+    # complex64: the headline
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    n0 = lib.ffgb_launch_count()
+    t_wall0 = time.perf_counter()
+    times64, energies64 = time_energy(torch.complex64, args.steps, args.warmup, ucj, ham, stream)
+    t_wall1 = time.perf_counter()
+    launches = (lib.ffgb_launch_count() - n0) // (args.steps + args.warmup)
+    clk = clocks.stop()
+    barrier()
+    total_ms = sum(times64)
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms * 1e-3)
+
+    # complex128 on the same GPU (fewer steps: FP64 bound)
+    times128, energies128 = time_energy(torch.complex128, args.c128_steps, 1, ucj, ham, stream)
+    e64, e128 = energies64[-1], energies128[-1]
+
+    # end to end through the public API (host inputs, energy read back each step)
+    e2e_s = time_e2e(max(2, min(args.steps, 5)), ucj, ham)
+    h2d = sum(np.asarray(x).nbytes for x in (ucj.diag_coulomb_mats, ucj.orbital_rotations,
+                                              ham.one_body_tensor, ham.diag_coulomb_mats, ham.orbital_rotations))
+
+    # dominant kernel roofline
+    rot_ms, gbs, S, _ = rotation_roofline(stream)
+    peak, peak_kind = _peaks()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            t_eval, t_rot, t_dc = cpu_reference_sample(os.cpu_count())
+            cpu = {"value": 1.0 / t_eval, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"C/OpenMP restatement of the reference kernels: one orbital rotation "
+                             f"({t_rot:.2f} s) + one diag-Coulomb evolution ({t_dc:.2f} s) at norb=16 "
+                             f"complex128, extrapolated to one evaluation "
+                             f"({N_REPS + 1} rotations + {N_REPS} evolutions + {RANK + 1} DF terms)"}
+        except Exception as exc:  # noqa: BLE001
+            cpu = {"value": None, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {exc!r}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "norb": NORB, "nelec": list(NELEC), "n_reps": N_REPS,
+                       "df_rank": RANK, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (state 1.32 GB c64)"},
+            "p50_ms": statistics.median(times64),
+            "p99_ms": float(np.percentile(times64, 99)),
+            "energy_c64": e64, "energy_c128": e128, "abs_dE_c64_vs_c128": abs(e64 - e128),
+            "c128": {"value": 1e3 / statistics.mean(times128), "unit": "evals/s",
+                     "ms_per_step": statistics.mean(times128), "steps": len(times128)},
+            "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": 8 * (RANK + 2)},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                         "frac": gbs / peak, "traffic": None,
+                         "kernel": "sector_kernel<float,16> (two transposing passes = one orbital rotation)",
+                         "bytes_per_launch": 2 * S, "ms_per_rotation": rot_ms, "peak_kind": peak_kind},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches),
+            "wall_s_c64": t_wall1 - t_wall0,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

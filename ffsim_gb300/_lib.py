@@ -41,6 +41,7 @@ _ip = ctypes.POINTER(ctypes.c_int)
 SIGNATURES = {
     "ffgb_version": [],
     "ffgb_last_error": [],
+    "ffgb_launch_count": [],
     "ffgb_givens_decomposition": [_dp, _c_int, _c_double, _dp, _ip, _ip, _dp],
     "ffgb_eigh": [_dp, _c_int, _dp, _dp],
     "ffgb_debug_plan": [_dp, _c_int, _c_int, _dp, _c_int, _ip],
@@ -96,6 +97,7 @@ def load() -> ctypes.CDLL:
             fn.restype = _c_int
         lib.ffgb_last_error.restype = ctypes.c_char_p
         lib.ffgb_scratch_bytes.restype = _c_size_t
+        lib.ffgb_launch_count.restype = _c_ll
         _lib = lib
         return lib
 

@@ -13,6 +13,9 @@ namespace ffgb {
 // Record an error message for ffgb_last_error() and return `code`.
 int fail(int code, const std::string& msg);
 
+// Count one kernel launch (reported by ffgb_launch_count()).
+void count_launch();
+
 #define FFGB_CUDA(call)                                                              \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \

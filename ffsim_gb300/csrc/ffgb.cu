@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -27,6 +28,9 @@ int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static long long binom_h(int n, int k) {
   if (k < 0 || n < 0 || k > n) return 0;
@@ -223,6 +227,12 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
   if (norb > FFGB_MAXN) return fail(FFGB_ERR_UNSUPPORTED, "norb > 18 is not supported");
   const long long dim_ll = binom_h(norb, A.rot_nocc);
   if (dim_ll <= 0 || A.n_rows <= 0) return FFGB_OK;
+  // scratch taken by this pass (column table) is free again once it is queued
+  struct Restore {
+    Scratch& s;
+    size_t off;
+    ~Restore() { s.off = off; }
+  } restore{scr, scr.off};
   const int dim = (int)dim_ll;
   auto P = std::make_unique<SectorParams<T>>();
   std::memset(P.get(), 0, sizeof(SectorParams<T>));
@@ -317,6 +327,7 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
                                 cudaMemcpyHostToDevice, st));
       col_table_kernel<T><<<(dim + 255) / 256, 256, 0, st>>>(P->col_strings, dim, norb, P->zrep,
                                                              diag_mode, same, tab);
+      count_launch();
       FFGB_CUDA(cudaGetLastError());
       P->col_table = tab;
     }
@@ -324,7 +335,7 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
   // rows per CTA
   const int block = nw > 0 ? 192 : 256;
   const size_t row_bytes = (size_t)dim * sizeof(C);
-  const Layout L0 = make_layout(sizeof(T), 0, dim, norb, P->chunk_bits, P->has_dphase, diag_mode);
+  const Layout L0 = make_layout(sizeof(T), 0, dim, norb, P->chunk_bits, P->has_dphase, diag_mode, P->kind);
   const long long budget = 110 * 1024;
   long long rmax = (budget - L0.total) / (long long)row_bytes;
   if (rmax < 1) {
@@ -336,7 +347,7 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
   int R = (int)std::min<long long>(std::min<long long>(rmax, want), 4096);
   if (R < 1) R = 1;
   P->rows_per_cta = R;
-  const Layout L = make_layout(sizeof(T), R, dim, norb, P->chunk_bits, P->has_dphase, diag_mode);
+  const Layout L = make_layout(sizeof(T), R, dim, norb, P->chunk_bits, P->has_dphase, diag_mode, P->kind);
   const long long grid = (A.n_rows + R - 1) / R;
   if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "grid too large");
   if (A.out_op == OUT_EXPECT) {
@@ -619,6 +630,7 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
   B.n_ctas = &nct;
   FFGB_TRY(run_pass<T>(B, scr, st));
   reduce_partials_kernel<<<1, 256, 0, st>>>(partials, nct, dslot, 0);
+  count_launch();
   FFGB_CUDA(cudaGetLastError());
   scr.off = mark;
   return FFGB_OK;
@@ -685,6 +697,7 @@ static int givens_impl(void* vec, int norb, int na, int nb, int spin, double c, 
   const int blocks = (int)std::min<long long>((total + 255) / 256, 8192);
   givens_sector_kernel<T><<<blocks, 256, 0, st>>>((typename CT<T>::type*)vec, norb, nocc, dim_other,
                                                   nb < 0 ? 1 : spin, l, (T)c, (T)s_re, (T)s_im);
+  count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }
@@ -722,6 +735,8 @@ extern "C" {
 int ffgb_version(void) { return 100; }
 
 const char* ffgb_last_error(void) { return ffgb::g_err.c_str(); }
+
+long long ffgb_launch_count(void) { return g_launches.load(); }
 
 int ffgb_givens_decomposition(const double* mat, int n, double tol, double* rot_cs, int* rot_ij,
                               int* n_rot, double* diag) {
@@ -838,8 +853,10 @@ int ffgb_apply_phase_shift(void* vec, int dtype, int norb, int na, int nb, int s
   const int blocks = (int)std::max<long long>(1, std::min<long long>((da * db + 255) / 256, 8192));
   if (dtype == FFGB_C64)
     phase_shift_kernel<float><<<blocks, 256, 0, st>>>((float2*)vec, strs, da, db, sp, orb, (float)pr, (float)pi);
+    count_launch();
   else
     phase_shift_kernel<double><<<blocks, 256, 0, st>>>((double2*)vec, strs, da, db, sp, orb, pr, pi);
+    count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }
@@ -991,8 +1008,10 @@ int ffgb_df_matvec(const void* vec, void* out, int dtype, int norb, int na, int 
   const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
   if (dtype == FFGB_C64)
     scale_copy_kernel<float><<<blocks, 256, 0, st>>>((const float2*)vec, (float2*)out, n, (float)constant, 0.f);
+    count_launch();
   else
     scale_copy_kernel<double><<<blocks, 256, 0, st>>>((const double2*)vec, (double2*)out, n, constant, 0.0);
+    count_launch();
   FFGB_CUDA(cudaGetLastError());
   for (const Term& t : terms) {
     const size_t mark = scr.off;
@@ -1040,8 +1059,10 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
     const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
     if (dtype == FFGB_C64)
       one_hot_kernel<float><<<blocks, 256, 0, st>>>((float2*)work, n);
+      count_launch();
     else
       one_hot_kernel<double><<<blocks, 256, 0, st>>>((double2*)work, n);
+      count_launch();
     FFGB_CUDA(cudaGetLastError());
   }
   Scratch scr(scratch, scratch_bytes);
@@ -1078,8 +1099,10 @@ int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out,
   FFGB_CUDA(cudaMallocAsync(&part, sizeof(double) * (2 * blocks + 2), st));
   if (dtype == FFGB_C64)
     vdot_kernel<float><<<blocks, 256, 0, st>>>((const float2*)x, (const float2*)y, n, part);
+    count_launch();
   else if (dtype == FFGB_C128)
     vdot_kernel<double><<<blocks, 256, 0, st>>>((const double2*)x, (const double2*)y, n, part);
+    count_launch();
   else
     return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
   FFGB_CUDA(cudaGetLastError());
@@ -1103,8 +1126,10 @@ int ffgb_hartree_fock(void* vec, int dtype, long long n, void* stream) {
   const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096));
   if (dtype == FFGB_C64)
     one_hot_kernel<float><<<blocks, 256, 0, st>>>((float2*)vec, n);
+    count_launch();
   else
     one_hot_kernel<double><<<blocks, 256, 0, st>>>((double2*)vec, n);
+    count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }

@@ -80,13 +80,15 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
 // Shared-memory layout; identical on host and device.
 __host__ __device__ inline Layout make_layout(int tsize, int R, int dim, int col_norb,
-                                              int chunk_bits, int has_dphase, int diag_mode) {
+                                              int chunk_bits, int has_dphase, int diag_mode,
+                                              int kind) {
   Layout L;
   int off = 0;
   L.binom = off;
   off += align16(FFGB_BST * FFGB_BST * 4);
   L.plan = off;
-  off += align16((FFGB_MAXTRI * 3 + 4 * 28 * 3 + 64 + 2 * FFGB_MAXN) * tsize);
+  if (kind == KIND_TRIANGLE) off += align16(FFGB_MAXTRI * 3 * tsize);
+  if (kind == KIND_FULL || kind == KIND_CSD) off += align16((4 * 28 * 3 + 64) * tsize);
   L.tab = off;
   off += align16(256 * 2 + 256 * 4 + 16 * 4);
   L.chunk_bits = chunk_bits;
@@ -94,7 +96,7 @@ __host__ __device__ inline Layout make_layout(int tsize, int R, int dim, int col
   if (L.nch < 1) L.nch = 1;
   const int nent = L.nch << chunk_bits;
   L.dt = off;
-  if (has_dphase) off += align16(nent * 2 * tsize);
+  if (has_dphase && diag_mode != DIAG_PHASE) off += align16(nent * 2 * tsize);
   L.xt = off;
   if (diag_mode == DIAG_PHASE) off += align16(nent * 2 * tsize + 2 * FFGB_MAXN * 8 + 16);
   if (diag_mode == DIAG_COEF) off += align16(nent * tsize + 2 * FFGB_MAXN * 8 + 16);
@@ -236,7 +238,9 @@ __global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
   using C = typename CT<T>::type;
   extern __shared__ __align__(16) unsigned char smem[];
   const Layout L = make_layout((int)sizeof(T), P.rows_per_cta, P.dim, P.norb, P.chunk_bits,
-                               P.has_dphase, P.diag_mode);
+                               P.has_dphase, P.diag_mode, P.kind);
+  // final orbital phases are folded into the per-row phase tables when both are present
+  const bool sep_dphase = P.has_dphase && P.diag_mode != DIAG_PHASE;
   int* sB = (int*)(smem + L.binom);
   T* sPlan = (T*)(smem + L.plan);
   unsigned short* sS2 = (unsigned short*)(smem + L.tab);
@@ -397,7 +401,7 @@ __global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
   const int cb = L.chunk_bits, nch = L.nch, nent = nch << cb;
   const unsigned cmask = (1u << cb) - 1u;
   C* sDT = (C*)(smem + L.dt);
-  if (P.has_dphase) {
+  if (sep_dphase) {
     for (int e = tid; e < nent; e += nth) {
       const int c = e >> cb;
       unsigned x = (unsigned)(e & cmask);
@@ -475,7 +479,22 @@ __global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
           if (orb < norb) f += wsc * sM[orb];
         }
         if (P.diag_mode == DIAG_PHASE) {
-          sXP[e] = phase_of(f, (C*)nullptr);
+          C ph = phase_of(f, (C*)nullptr);
+          if (P.has_dphase) {
+            unsigned y = (unsigned)(e & cmask);
+            while (y) {
+              const int b = __ffs(y) - 1;
+              y &= y - 1;
+              const int orb = c * cb + b;
+              if (orb < norb) {
+                C d;
+                d.x = P.dphase[orb][0];
+                d.y = P.dphase[orb][1];
+                ph = cmul(ph, d);
+              }
+            }
+          }
+          sXP[e] = ph;
         } else {
           sXC[e] = (T)f;
         }
@@ -488,7 +507,7 @@ __global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
       C v = vr[j];
       unsigned s = 0;
       if (P.has_dphase || P.diag_mode != DIAG_NONE) s = P.col_strings[j];
-      if (P.has_dphase) {
+      if (sep_dphase) {
         for (int c = 0; c < nch; ++c) v = cmul(v, sDT[(c << cb) + ((s >> (c * cb)) & cmask)]);
       }
       T z = (T)1;

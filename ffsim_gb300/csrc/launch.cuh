@@ -14,6 +14,7 @@ int launch_sector(const SectorParams<T>& P, int grid, int block, int smem, cudaS
     attr_set = true;
   }
   sector_kernel<T, NW><<<grid, block, smem, st>>>(P);
+  count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }

@@ -48,6 +48,8 @@ typedef enum { FFGB_C64 = 0, FFGB_C128 = 1 } ffgb_dtype;
 int ffgb_version(void);
 /* Message of the last error raised on the calling thread ("" if none). */
 const char* ffgb_last_error(void);
+/* Number of CUDA kernels this library has launched in the process. */
+long long ffgb_launch_count(void);
 
 /* ------------------------------------------------------------------ */
 /* Host-side linear algebra                                             */
