@@ -853,10 +853,9 @@ int ffgb_apply_phase_shift(void* vec, int dtype, int norb, int na, int nb, int s
   const int blocks = (int)std::max<long long>(1, std::min<long long>((da * db + 255) / 256, 8192));
   if (dtype == FFGB_C64)
     phase_shift_kernel<float><<<blocks, 256, 0, st>>>((float2*)vec, strs, da, db, sp, orb, (float)pr, (float)pi);
-    count_launch();
   else
     phase_shift_kernel<double><<<blocks, 256, 0, st>>>((double2*)vec, strs, da, db, sp, orb, pr, pi);
-    count_launch();
+  count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }
@@ -1008,10 +1007,9 @@ int ffgb_df_matvec(const void* vec, void* out, int dtype, int norb, int na, int 
   const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
   if (dtype == FFGB_C64)
     scale_copy_kernel<float><<<blocks, 256, 0, st>>>((const float2*)vec, (float2*)out, n, (float)constant, 0.f);
-    count_launch();
   else
     scale_copy_kernel<double><<<blocks, 256, 0, st>>>((const double2*)vec, (double2*)out, n, constant, 0.0);
-    count_launch();
+  count_launch();
   FFGB_CUDA(cudaGetLastError());
   for (const Term& t : terms) {
     const size_t mark = scr.off;
@@ -1059,10 +1057,9 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
     const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
     if (dtype == FFGB_C64)
       one_hot_kernel<float><<<blocks, 256, 0, st>>>((float2*)work, n);
-      count_launch();
     else
       one_hot_kernel<double><<<blocks, 256, 0, st>>>((double2*)work, n);
-      count_launch();
+    count_launch();
     FFGB_CUDA(cudaGetLastError());
   }
   Scratch scr(scratch, scratch_bytes);
@@ -1095,16 +1092,15 @@ int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out,
   g_err.clear();
   cudaStream_t st = (cudaStream_t)stream;
   const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 1024));
+  if (dtype != FFGB_C64 && dtype != FFGB_C128)
+    return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
   double* part = nullptr;
   FFGB_CUDA(cudaMallocAsync(&part, sizeof(double) * (2 * blocks + 2), st));
   if (dtype == FFGB_C64)
     vdot_kernel<float><<<blocks, 256, 0, st>>>((const float2*)x, (const float2*)y, n, part);
-    count_launch();
-  else if (dtype == FFGB_C128)
-    vdot_kernel<double><<<blocks, 256, 0, st>>>((const double2*)x, (const double2*)y, n, part);
-    count_launch();
   else
-    return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
+    vdot_kernel<double><<<blocks, 256, 0, st>>>((const double2*)x, (const double2*)y, n, part);
+  count_launch();
   FFGB_CUDA(cudaGetLastError());
   std::vector<double> h(2 * blocks);
   FFGB_CUDA(cudaMemcpyAsync(h.data(), part, sizeof(double) * 2 * blocks, cudaMemcpyDeviceToHost, st));
@@ -1126,10 +1122,9 @@ int ffgb_hartree_fock(void* vec, int dtype, long long n, void* stream) {
   const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096));
   if (dtype == FFGB_C64)
     one_hot_kernel<float><<<blocks, 256, 0, st>>>((float2*)vec, n);
-    count_launch();
   else
     one_hot_kernel<double><<<blocks, 256, 0, st>>>((double2*)vec, n);
-    count_launch();
+  count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }
