@@ -47,7 +47,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
     nvcc = _nvcc()
     inc = ["-I", str(BUILD), "-I", str(CSRC)]
     flags = NVFLAGS + (extra_flags or [])
-    units = [("ffgb.cu", "ffgb.o"), ("plan.cpp", "plan.o")] + [
+    units = [("ffgb.cu", "ffgb.o"), ("plan.cpp", "plan.o"), ("stages.cu", "stages.o")] + [
         (f"inst_{i}.cu", f"inst_{i}.o") for i in range(5)]
     cmds = [[nvcc, *ARCH, *flags, *inc, "-c", str(CSRC / src), "-o", str(BUILD / obj)]
             for src, obj in units]

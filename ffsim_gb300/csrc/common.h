@@ -29,8 +29,32 @@ void count_launch();
     if (s_ != FFGB_OK) return s_; \
   } while (0)
 
-// Launch sector_kernel<T, NW>; instantiated in the inst_*.cu units.
+// Launch sector_kernel<T, NW> with a persistent grid of at most n_chunks CTAs
+// (as many as fit on the device); the grid used is returned in *grid_out.
+// Instantiated in the inst_*.cu units.
 template <typename T, int NW>
-int launch_sector(const SectorParams<T>& P, int grid, int block, int smem, cudaStream_t st);
+int launch_sector(const SectorParams<T>& P, long long n_chunks, int block, int smem, cudaStream_t st,
+                  int* grid_out);
+
+struct SectorPlan;
+
+// Stage-major complex64 rotation of the sector whose strings index the rows
+// of a row-major array (ld elements per row, ncols columns processed):
+// in -> out (in == out allowed).  ph_in / ph_out: optional per-row phase
+// tables (complex64, one per string) multiplied in before / after the
+// network; the plan's own orbital phases go in as ph_out.
+int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long ld, long long ncols,
+                      const SectorPlan& plan, bool comp, const void* ph_in, const void* ph_out,
+                      cudaStream_t st);
+template <typename T>
+int launch_transpose(const void* in, void* out, long long rows, long long cols, const void* row_ph,
+                     const void* col_ph, cudaStream_t st);
+template <typename T>
+int launch_string_phases(const unsigned* strings, long long dim, int norb, const double* d_host, void* out,
+                         cudaStream_t st);
+template <typename T>
+int launch_row_scale(void* x, long long rows, long long ld, const void* ph, cudaStream_t st);
+template <typename T>
+int launch_axpy(const void* x, void* y, long long n, double a, cudaStream_t st);
 
 }  // namespace ffgb

@@ -102,10 +102,12 @@ struct Scratch {
   }
 };
 
+// column table (16 B/string), partial sums (8 B/row) and up to four
+// string-phase tables (8 B/string) of the stage path, plus alignment slack
 static size_t extras_bytes(int norb, int na, int nb) {
   long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;
   long long m = std::max<long long>(std::max(da, db), 1);
-  return (size_t)m * 16 + (size_t)m * 8 + 4096 + 2048;
+  return (size_t)m * 16 + (size_t)m * 8 + (size_t)m * 32 + 16384;
 }
 
 // ---------------------------------------------------------------------------
@@ -187,34 +189,35 @@ struct PassArgs {
   double alpha = 1.0;
   const DiagSpec* diag = nullptr;
   bool apply_dphase = true;
+  bool comp = false;           // compensated window coefficients (complex64)
   double* partials = nullptr;  // EXPECT
   int* n_ctas = nullptr;
 };
 
 template <typename T>
-static int dispatch_sector(int nw, const SectorParams<T>& P, int grid, int block, int smem,
-                           cudaStream_t st) {
+static int dispatch_sector(int nw, const SectorParams<T>& P, long long grid, int block, int smem,
+                           cudaStream_t st, int* grid_out) {
   if constexpr (sizeof(T) == 8) {
-    return launch_sector<T, 0>(P, grid, block, smem, st);
+    return launch_sector<T, 0>(P, grid, block, smem, st, grid_out);
   } else {
     switch (nw) {
-      case 0: return launch_sector<T, 0>(P, grid, block, smem, st);
-      case 1: return launch_sector<T, 1>(P, grid, block, smem, st);
-      case 2: return launch_sector<T, 2>(P, grid, block, smem, st);
-      case 3: return launch_sector<T, 3>(P, grid, block, smem, st);
-      case 4: return launch_sector<T, 4>(P, grid, block, smem, st);
-      case 5: return launch_sector<T, 5>(P, grid, block, smem, st);
-      case 6: return launch_sector<T, 6>(P, grid, block, smem, st);
-      case 7: return launch_sector<T, 7>(P, grid, block, smem, st);
-      case 8: return launch_sector<T, 8>(P, grid, block, smem, st);
-      case 9: return launch_sector<T, 9>(P, grid, block, smem, st);
-      case 10: return launch_sector<T, 10>(P, grid, block, smem, st);
-      case 11: return launch_sector<T, 11>(P, grid, block, smem, st);
-      case 12: return launch_sector<T, 12>(P, grid, block, smem, st);
-      case 13: return launch_sector<T, 13>(P, grid, block, smem, st);
-      case 14: return launch_sector<T, 14>(P, grid, block, smem, st);
-      case 15: return launch_sector<T, 15>(P, grid, block, smem, st);
-      case 16: return launch_sector<T, 16>(P, grid, block, smem, st);
+      case 0: return launch_sector<T, 0>(P, grid, block, smem, st, grid_out);
+      case 1: return launch_sector<T, 1>(P, grid, block, smem, st, grid_out);
+      case 2: return launch_sector<T, 2>(P, grid, block, smem, st, grid_out);
+      case 3: return launch_sector<T, 3>(P, grid, block, smem, st, grid_out);
+      case 4: return launch_sector<T, 4>(P, grid, block, smem, st, grid_out);
+      case 5: return launch_sector<T, 5>(P, grid, block, smem, st, grid_out);
+      case 6: return launch_sector<T, 6>(P, grid, block, smem, st, grid_out);
+      case 7: return launch_sector<T, 7>(P, grid, block, smem, st, grid_out);
+      case 8: return launch_sector<T, 8>(P, grid, block, smem, st, grid_out);
+      case 9: return launch_sector<T, 9>(P, grid, block, smem, st, grid_out);
+      case 10: return launch_sector<T, 10>(P, grid, block, smem, st, grid_out);
+      case 11: return launch_sector<T, 11>(P, grid, block, smem, st, grid_out);
+      case 12: return launch_sector<T, 12>(P, grid, block, smem, st, grid_out);
+      case 13: return launch_sector<T, 13>(P, grid, block, smem, st, grid_out);
+      case 14: return launch_sector<T, 14>(P, grid, block, smem, st, grid_out);
+      case 15: return launch_sector<T, 15>(P, grid, block, smem, st, grid_out);
+      case 16: return launch_sector<T, 16>(P, grid, block, smem, st, grid_out);
       default: return fail(FFGB_ERR_UNSUPPORTED, "no window kernel for this norb");
     }
   }
@@ -254,11 +257,16 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
         P->tri_l[g] = (signed char)pl.tri_l[g];
       }
     } else {
+      P->comp = A.comp ? 1 : 0;
+      auto lo = [](double x) { return (T)(x - (double)(T)x); };
       auto put = [&](int w, const std::vector<Givens>& v) {
         for (size_t g = 0; g < v.size(); ++g) {
           P->win[w][3 * g] = (T)v[g].c;
           P->win[w][3 * g + 1] = (T)v[g].s.real();
           P->win[w][3 * g + 2] = (T)v[g].s.imag();
+          P->win_lo[w][3 * g] = lo(v[g].c);
+          P->win_lo[w][3 * g + 1] = lo(v[g].s.real());
+          P->win_lo[w][3 * g + 2] = lo(v[g].s.imag());
         }
       };
       if (pl.kind == PLAN_FULL) {
@@ -271,10 +279,13 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
         for (size_t i = 0; i < pl.cs.size(); ++i) {
           const Pair2& p = pl.cs[i];
           T* c = P->cs[i];
-          c[0] = (T)p.g00.real(); c[1] = (T)p.g00.imag();
-          c[2] = (T)p.g01.real(); c[3] = (T)p.g01.imag();
-          c[4] = (T)p.g10.real(); c[5] = (T)p.g10.imag();
-          c[6] = (T)p.g11.real(); c[7] = (T)p.g11.imag();
+          T* cl = P->cs_lo[i];
+          const double vals[8] = {p.g00.real(), p.g00.imag(), p.g01.real(), p.g01.imag(),
+                                  p.g10.real(), p.g10.imag(), p.g11.real(), p.g11.imag()};
+          for (int q = 0; q < 8; ++q) {
+            c[q] = (T)vals[q];
+            cl[q] = lo(vals[q]);
+          }
         }
       }
       nw = norb;
@@ -299,7 +310,7 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
   P->alpha_re = (T)A.alpha;
   P->alpha_im = (T)0;
   P->diag_mode = diag_mode;
-  P->chunk_bits = norb > 8 ? 8 : 4;
+  P->chunk_bits = (diag_mode == DIAG_COEF && norb > 8) ? 8 : 4;
   const bool need_col = P->has_dphase || diag_mode != DIAG_NONE;
   if (need_col) {
     const unsigned* cs = nullptr;
@@ -333,9 +344,9 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
     }
   }
   // rows per CTA
-  const int block = nw > 0 ? 192 : 256;
+  const int block = sector_threads(nw);
   const size_t row_bytes = (size_t)dim * sizeof(C);
-  const Layout L0 = make_layout(sizeof(T), 0, dim, norb, P->chunk_bits, P->has_dphase, diag_mode, P->kind);
+  const Layout L0 = make_layout(sizeof(T), 0, dim, norb, P->chunk_bits, P->has_dphase, diag_mode, P->kind, P->comp);
   const long long budget = 110 * 1024;
   long long rmax = (budget - L0.total) / (long long)row_bytes;
   if (rmax < 1) {
@@ -347,15 +358,16 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
   int R = (int)std::min<long long>(std::min<long long>(rmax, want), 4096);
   if (R < 1) R = 1;
   P->rows_per_cta = R;
-  const Layout L = make_layout(sizeof(T), R, dim, norb, P->chunk_bits, P->has_dphase, diag_mode, P->kind);
-  const long long grid = (A.n_rows + R - 1) / R;
-  if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "grid too large");
+  const Layout L = make_layout(sizeof(T), R, dim, norb, P->chunk_bits, P->has_dphase, diag_mode, P->kind, P->comp);
+  const long long n_chunks = (A.n_rows + R - 1) / R;
   if (A.out_op == OUT_EXPECT) {
     if (!A.partials) return fail(FFGB_ERR_ARG, "missing partials buffer");
     P->partials = A.partials;
   }
-  if (A.n_ctas) *A.n_ctas = (int)grid;
-  return dispatch_sector<T>(nw, *P, (int)grid, block, L.total, st);
+  int grid = 0;
+  FFGB_TRY(dispatch_sector<T>(nw, *P, n_chunks, block, L.total, st, &grid));
+  if (A.n_ctas) *A.n_ctas = grid;
+  return FFGB_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -395,13 +407,93 @@ static int make_plan(int norb, const std::vector<cd>& V, SectorPlan& plan) {
   return FFGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// stage-major complex64 path (cosine-sine plans, 9 <= norb <= 16)
+// ---------------------------------------------------------------------------
+template <typename T>
+static bool staged(const SectorPlan* a, const SectorPlan* b) {
+  if (sizeof(T) != 4 || (!a && !b)) return false;
+  if (a && a->kind != PLAN_CSD) return false;
+  if (b && b->kind != PLAN_CSD) return false;
+  return true;
+}
+
+// Per-string table of a plan's final orbital phases (nullptr when they are all 1).
+static int phase_table(const SectorPlan* p, int norb, int nocc, Scratch& scr, cudaStream_t st,
+                       const void** out) {
+  *out = nullptr;
+  if (!p) return FFGB_OK;
+  std::vector<double> d(2 * norb);
+  bool trivial = true;
+  for (int i = 0; i < norb; ++i) {
+    d[2 * i] = p->diag[i].real();
+    d[2 * i + 1] = p->diag[i].imag();
+    if (std::abs(p->diag[i] - cd(1.0)) > 1e-15) trivial = false;
+  }
+  if (trivial) return FFGB_OK;
+  const unsigned* strs = nullptr;
+  FFGB_TRY(device_strings(norb, nocc, &strs));
+  const long long dim = binom_h(norb, nocc);
+  void* t = scr.take((size_t)dim * sizeof(float2));
+  if (!t) return fail(FFGB_ERR_OOM, "scratch too small for a string-phase table");
+  FFGB_TRY(launch_string_phases<float>(strs, dim, norb, d.data(), t, st));
+  *out = t;
+  return FFGB_OK;
+}
+
+// W(pa) (x) W(pb) of the state `in` (alpha rows), through `x` (same shape) and
+// `tmp` (beta rows).  keep_t = false: the result is in x with alpha rows;
+// keep_t = true: the result is in tmp with beta rows.  phases = false leaves
+// out the plans' final orbital phases (they do not change |amplitude|^2).
+static int staged_rotate(const void* in, void* x, void* tmp, int norb, int na, int nb,
+                         const SectorPlan* pa, const SectorPlan* pb, bool phases, bool comp, bool keep_t,
+                         Scratch& scr, cudaStream_t st) {
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  const void *fa = nullptr, *fb = nullptr;
+  if (phases) {
+    FFGB_TRY(phase_table(pa, norb, na, scr, st, &fa));
+    FFGB_TRY(phase_table(pb, norb, nb, scr, st, &fb));
+  }
+  if (pa) FFGB_TRY(stage_rotate_rows(in, x, norb, na, db, db, *pa, comp, nullptr, fa, st));
+  if (!pb && !keep_t) {
+    if (!pa && in != x) FFGB_CUDA(cudaMemcpyAsync(x, in, (size_t)(da * db) * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    return FFGB_OK;
+  }
+  FFGB_TRY(launch_transpose<float>(pa ? x : in, tmp, da, db, nullptr, nullptr, st));
+  if (pb) FFGB_TRY(stage_rotate_rows(tmp, tmp, norb, nb, da, da, *pb, comp, nullptr, fb, st));
+  if (!keep_t) FFGB_TRY(launch_transpose<float>(tmp, x, db, da, nullptr, nullptr, st));
+  return FFGB_OK;
+}
+
+// Diagonal operator on a state held with beta rows (db rows of da columns):
+// in place (PHASE / COEF) or reduced into partial sums (EXPECT).  `spec` is
+// written with alpha rows.
+template <typename T>
+static int diag_pass_t(void* t, int norb, int na, int nb, const DiagSpec& spec, int out_op, double* partials,
+                       int* n_ctas, Scratch& scr, cudaStream_t st) {
+  DiagSpec dt = spec.transposed();
+  PassArgs<T> A;
+  A.norb = norb;
+  A.rot_nocc = na;
+  A.row_nocc = nb;
+  A.n_rows = binom_h(norb, nb);
+  A.in = t;
+  A.out = out_op == OUT_EXPECT ? nullptr : t;
+  A.out_op = out_op;
+  A.layout = LAYOUT_SAME;
+  A.diag = &dt;
+  A.partials = partials;
+  A.n_ctas = n_ctas;
+  return run_pass<T>(A, scr, st);
+}
+
 // Both sectors rotated, state (dim_a, dim_b) in `vec`; the result lands in
 // `vec` (two transposing passes through `tmp`).  Optional diagonal operator
 // applied in the second pass (rows = beta).
 template <typename T>
 static int rotate_both(void* vec, void* tmp, int norb, int na, int nb, const SectorPlan* pa,
                        const SectorPlan* pb, const DiagSpec* diag_ab, Scratch& scr,
-                       cudaStream_t st) {
+                       cudaStream_t st, bool comp = false) {
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
   PassArgs<T> A;
   A.plan = pb;
@@ -412,6 +504,7 @@ static int rotate_both(void* vec, void* tmp, int norb, int na, int nb, const Sec
   A.in = vec;
   A.out = tmp;
   A.layout = LAYOUT_T;
+  A.comp = comp;
   FFGB_TRY(run_pass<T>(A, scr, st));
   DiagSpec dt;
   PassArgs<T> B;
@@ -423,6 +516,7 @@ static int rotate_both(void* vec, void* tmp, int norb, int na, int nb, const Sec
   B.in = tmp;
   B.out = vec;
   B.layout = LAYOUT_T;
+  B.comp = comp;
   if (diag_ab) {
     dt = diag_ab->transposed();
     B.diag = &dt;
@@ -466,6 +560,8 @@ static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const doub
   const size_t S = (size_t)binom_h(norb, na) * binom_h(norb, nb) * sizeof(C);
   void* tmp = scr.take(S);
   if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  if (staged<T>(&pa, mb ? &pb : nullptr))
+    return staged_rotate(vec, vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, true, false, false, scr, st);
   return rotate_both<T>(vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, nullptr, scr, st);
 }
 
@@ -530,6 +626,20 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
   const size_t S = (size_t)da * binom_h(norb, nb) * sizeof(C);
   void* tmp = scr.take(S);
   if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  const SectorPlan *sad = rot_a ? &pad : nullptr, *sbd = rot_b ? &pbd : nullptr;
+  if (staged<T>(sad, sbd)) {
+    // W(U) D W(U)^dag: rotate into the beta-row layout, diagonal, beta back, alpha back
+    FFGB_TRY(staged_rotate(vec, vec, tmp, norb, na, nb, sad, sbd, true, false, true, scr, st));
+    FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
+    const long long db = binom_h(norb, nb);
+    const void *fa = nullptr, *fb = nullptr;
+    FFGB_TRY(phase_table(rot_a ? &pau : nullptr, norb, na, scr, st, &fa));
+    FFGB_TRY(phase_table(rot_b ? &pbu : nullptr, norb, nb, scr, st, &fb));
+    if (rot_b) FFGB_TRY(stage_rotate_rows(tmp, tmp, norb, nb, da, da, pbu, false, nullptr, fb, st));
+    FFGB_TRY(launch_transpose<float>(tmp, vec, db, da, nullptr, nullptr, st));
+    if (rot_a) FFGB_TRY(stage_rotate_rows(vec, vec, norb, na, db, db, pau, false, nullptr, fa, st));
+    return FFGB_OK;
+  }
   FFGB_TRY(rotate_both<T>(vec, tmp, norb, na, nb, rot_a ? &pad : nullptr, rot_b ? &pbd : nullptr,
                           &spec, scr, st));
   return rotate_both<T>(vec, tmp, norb, na, nb, rot_a ? &pau : nullptr, rot_b ? &pbu : nullptr,
@@ -562,6 +672,18 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
   void* t1 = scr.take(S);
   void* t2 = scr.take(S);
   if (!t1 || !t2) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
+  if (staged<T>(&pd, &pu)) {
+    FFGB_TRY(staged_rotate(vec, t1, t2, norb, na, nb, &pd, &pd, true, false, true, scr, st));
+    FFGB_TRY(diag_pass_t<T>(t2, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
+    const void *fa = nullptr, *fb = nullptr;
+    FFGB_TRY(phase_table(&pu, norb, na, scr, st, &fa));
+    FFGB_TRY(phase_table(&pu, norb, nb, scr, st, &fb));
+    FFGB_TRY(stage_rotate_rows(t2, t2, norb, nb, da, da, pu, false, nullptr, fb, st));
+    FFGB_TRY(launch_transpose<float>(t2, t1, db, da, nullptr, nullptr, st));
+    if (!accumulate) return stage_rotate_rows(t1, out, norb, na, db, db, pu, false, nullptr, fa, st);
+    FFGB_TRY(stage_rotate_rows(t1, t1, norb, na, db, db, pu, false, nullptr, fa, st));
+    return launch_axpy<float>(t1, out, da * db, 1.0, st);
+  }
   PassArgs<T> A;
   A.norb = norb;
   A.layout = LAYOUT_T;
@@ -597,12 +719,25 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
 // <vec| W(V)^dag... : sum z |W(V) vec|^2 into dslot (device double)
 template <typename T>
 static int expectation_term(const void* vec, int norb, int na, int nb, const DiagSpec& spec,
-                            const std::vector<cd>& V, void* tmp, double* dslot, Scratch& scr,
+                            const std::vector<cd>& V, void* tmp, void* tmp2, double* dslot, Scratch& scr,
                             cudaStream_t st) {
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
   SectorPlan pv;
   FFGB_TRY(make_plan<T>(norb, V, pv));
   const size_t mark = scr.off;
+  if (tmp2 && staged<T>(&pv, &pv)) {
+    // coherent coefficient rounding would bias every term: compensated coefficients
+    FFGB_TRY(staged_rotate(vec, tmp, tmp2, norb, na, nb, &pv, &pv, false, true, true, scr, st));
+    double* partials = (double*)scr.take(sizeof(double) * (size_t)std::max<long long>(db, 1));
+    if (!partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
+    int nct = 0;
+    FFGB_TRY(diag_pass_t<T>(tmp2, norb, na, nb, spec, OUT_EXPECT, partials, &nct, scr, st));
+    reduce_partials_kernel<<<1, 256, 0, st>>>(partials, nct, dslot, 0);
+    count_launch();
+    FFGB_CUDA(cudaGetLastError());
+    scr.off = mark;
+    return FFGB_OK;
+  }
   PassArgs<T> A;
   A.norb = norb;
   A.layout = LAYOUT_T;
@@ -613,6 +748,7 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
   A.in = vec;
   A.out = tmp;
   A.apply_dphase = false;  // |phi|^2 does not see the final orbital phases
+  A.comp = true;           // coherent coefficient rounding would bias every term
   FFGB_TRY(run_pass<T>(A, scr, st));
   double* partials = (double*)scr.take(sizeof(double) * (size_t)std::max<long long>(db, 1));
   if (!partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
@@ -634,6 +770,25 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
   FFGB_CUDA(cudaGetLastError());
   scr.off = mark;
   return FFGB_OK;
+}
+
+// One UCJ layer on x: both sectors rotated by the plan p, then the diagonal
+// phase operator `spec` (none for the final rotation).  Compensated
+// coefficients in complex64.
+template <typename T>
+static int ucj_layer(void* x, void* tmp, int norb, int na, int nb, const SectorPlan& p, const DiagSpec* spec,
+                     Scratch& scr, cudaStream_t st) {
+  if (staged<T>(&p, &p)) {
+    const size_t mark = scr.off;
+    FFGB_TRY(staged_rotate(x, x, tmp, norb, na, nb, &p, &p, true, true, spec != nullptr, scr, st));
+    if (spec) {
+      FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, *spec, OUT_STORE, nullptr, nullptr, scr, st));
+      FFGB_TRY(launch_transpose<float>(tmp, x, binom_h(norb, nb), binom_h(norb, na), nullptr, nullptr, st));
+    }
+    scr.off = mark;
+    return FFGB_OK;
+  }
+  return rotate_both<T>(x, tmp, norb, na, nb, &p, &p, spec, scr, st, sizeof(T) == 4);
 }
 
 // DF Hamiltonian terms as (Z spec, rotation V = term basis)
@@ -709,12 +864,13 @@ static int df_expectation_impl(const void* vec, int norb, int na, int nb, const 
   using C = typename CT<T>::type;
   const size_t S = (size_t)binom_h(norb, na) * binom_h(norb, nb) * sizeof(C);
   void* tmp = scr.take(S);
+  void* tmp2 = sizeof(T) == 4 ? scr.take(S) : nullptr;
   double* slots = (double*)scr.take(sizeof(double) * (terms.size() + 1));
-  if (!tmp || !slots) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+  if (!tmp || !slots || (sizeof(T) == 4 && !tmp2)) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
   for (size_t k = 0; k < terms.size(); ++k) {
     std::vector<cd> V = dagger(terms[k].rot, norb);
     if (pre) V = matmul(V, *pre, norb);
-    FFGB_TRY(expectation_term<T>(vec, norb, na, nb, terms[k].spec, V, tmp, slots + k, scr, st));
+    FFGB_TRY(expectation_term<T>(vec, norb, na, nb, terms[k].spec, V, tmp, tmp2, slots + k, scr, st));
   }
   std::vector<double> h(terms.size() + 1, 0.0);
   if (!terms.empty())
@@ -821,7 +977,7 @@ size_t ffgb_scratch_bytes(int op, int dtype, int norb, int na, int nb) {
   const long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;
   const size_t S = (size_t)da * db * el;
   const size_t ex = extras_bytes(norb, na, nb) + 4096;
-  if (op == 1) return 2 * S + ex;
+  if (op == 1 || op == 2) return 2 * S + ex;
   return S + ex;
 }
 
@@ -921,8 +1077,8 @@ int ffgb_ucj_spin_balanced_apply(void* vec, int dtype, int norb, int na, int nb,
     SectorPlan p;
     int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
     if (s) return s;
-    s = dtype == FFGB_C64 ? rotate_both<float>(vec, tmp, norb, na, nb, &p, &p, &spec, scr, st)
-                          : rotate_both<double>(vec, tmp, norb, na, nb, &p, &p, &spec, scr, st);
+    s = dtype == FFGB_C64 ? ucj_layer<float>(vec, tmp, norb, na, nb, p, &spec, scr, st)
+                          : ucj_layer<double>(vec, tmp, norb, na, nb, p, &spec, scr, st);
     if (s) return s;
     current = U;
   }
@@ -930,8 +1086,8 @@ int ffgb_ucj_spin_balanced_apply(void* vec, int dtype, int norb, int na, int nb,
   SectorPlan p;
   int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
   if (s) return s;
-  return dtype == FFGB_C64 ? rotate_both<float>(vec, tmp, norb, na, nb, &p, &p, nullptr, scr, st)
-                           : rotate_both<double>(vec, tmp, norb, na, nb, &p, &p, nullptr, scr, st);
+  return dtype == FFGB_C64 ? ucj_layer<float>(vec, tmp, norb, na, nb, p, nullptr, scr, st)
+                           : ucj_layer<double>(vec, tmp, norb, na, nb, p, nullptr, scr, st);
 }
 
 int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, int na, int nb,
@@ -1074,8 +1230,8 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
     SectorPlan p;
     int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
     if (s) return s;
-    s = dtype == FFGB_C64 ? rotate_both<float>(work, tmp, norb, na, nb, &p, &p, &spec, scr, st)
-                          : rotate_both<double>(work, tmp, norb, na, nb, &p, &p, &spec, scr, st);
+    s = dtype == FFGB_C64 ? ucj_layer<float>(work, tmp, norb, na, nb, p, &spec, scr, st)
+                          : ucj_layer<double>(work, tmp, norb, na, nb, p, &spec, scr, st);
     if (s) return s;
     current = U;
   }

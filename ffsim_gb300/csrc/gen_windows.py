@@ -15,10 +15,13 @@ For each (B, K) this script writes:
   applied to the member array ``v``; ``gp`` holds ``(c, Re s, Im s)`` per
   rotation in network order.  The network is: for r in 0..B-2, for col from
   B-1 down to r+1, rotate local orbitals (col-1, col).
-* ``cs_site_H_K(i, ...)`` -- for the cross-half rotation on orbitals
-  (i, H + i): the members of a K-family of the low half that have bit i set,
-  their partner index in the (K-1)-family with bit i cleared, and the parity
-  of the occupied low-half orbitals above i (the fermionic sign).
+* ``win_group_B_K(s, off, ...)`` -- loads the members ``s[off[j]]`` into
+  registers, applies the network and stores them back; ``WinDispatch<B>``
+  selects the function for a runtime K.
+* ``win_rows_B_K(si, so, ld, off, ...)`` -- the same on members that are rows
+  ``off[j]`` of a row-major array (one column per thread), with optional
+  per-row phases multiplied in after the loads (``ph_in``) and before the
+  stores (``ph_out``).
 
 The output is a pure function of the window sizes, so it is regenerated at
 build time and is not stored in the repository.
@@ -49,80 +52,86 @@ def triangle(b: int) -> list[int]:
 
 
 def emit_givens(b: int, k: int) -> str:
+    """Triangle network as a runtime loop over its rows r with the rotations of
+    each row unrolled: rotation (col-1, col) runs when col > r.  Only b-1
+    distinct orbital pairs exist, so the code holds b-1 pair patterns instead of
+    b(b-1)/2 (keeps the instruction footprint small)."""
     ms = members(b, k)
     index = {w: j for j, w in enumerate(ms)}
     n = len(ms)
     lines = [
-        f"__device__ __forceinline__ void win_givens_{b}_{k}(float2 (&v)[{max(n, 1)}], const float* __restrict__ gp) {{"
+        "template <bool COMP>",
+        f"__device__ __forceinline__ void win_givens_{b}_{k}(float2 (&v)[{max(n, 1)}], const float* __restrict__ gp,"
+        " const float* __restrict__ gl) {",
     ]
-    for g, l in enumerate(triangle(b)):
+    if b < 2:
+        lines.append("}")
+        return "\n".join(lines)
+    lines.append("  int g = 0;")
+    lines.append("#pragma unroll 1")
+    lines.append(f"  for (int r = 0; r < {b - 1}; ++r) {{")
+    for col in range(b - 1, 0, -1):
+        l = col - 1
         pairs = []
         for w in ms:
             if (w >> l) & 1 and not (w >> (l + 1)) & 1:
                 pairs.append((index[w], index[w ^ (3 << l)]))
-        if not pairs:
-            continue
-        lines.append(f"  {{ const float c = gp[{3 * g}], sr = gp[{3 * g + 1}], si = gp[{3 * g + 2}];")
-        for x, y in pairs:
-            lines.append(f"    rot_pair(v[{x}], v[{y}], c, sr, si);")
-        lines.append("  }")
+        lines.append(f"    if ({col} > r) {{")
+        if pairs:
+            lines.append("      const float c = gp[3 * g], sr = gp[3 * g + 1], si = gp[3 * g + 2];")
+            lines.append("      const float cl = COMP ? gl[3 * g] : 0.f, srl = COMP ? gl[3 * g + 1] : 0.f,"
+                         " sil = COMP ? gl[3 * g + 2] : 0.f;")
+            for x, y in pairs:
+                lines.append(f"      rot_pair<COMP>(v[{x}], v[{y}], c, sr, si, cl, srl, sil);")
+        lines.append("      ++g;")
+        lines.append("    }")
+    lines.append("  }")
     lines.append("}")
     return "\n".join(lines)
 
 
-def emit_cs(h: int, k: int) -> str:
-    """Pairs of the cross-half rotation at low-half site i (K-family -> (K-1)-family)."""
-    ms = members(h, k)
-    prev = {w: j for j, w in enumerate(members(h, k - 1))} if k >= 1 else {}
-    lines = [
-        f"template <class F> __device__ __forceinline__ void cs_site_{h}_{k}(int i, F&& f) {{",
-        "  switch (i) {",
-    ]
-    for i in range(h):
-        lines.append(f"  case {i}:")
-        for j, w in enumerate(ms):
-            if (w >> i) & 1:
-                par = bin(w >> (i + 1)).count("1") & 1
-                lines.append(f"    f({j}, {prev[w ^ (1 << i)]}, {par});")
-        lines.append("    break;")
-    lines.append("  default: break;\n  }\n}")
-    return "\n".join(lines)
-
-
 def emit_groups(b: int) -> str:
-    """Group load/compute/store functions and the per-window dispatch struct."""
+    """One group function per (b, k): members at s[off[j]] (off is the identity for
+    groups that are contiguous runs), so the low- and high-half stages share code."""
     lines = []
     for k in range(0, b + 1):
         m = math.comb(b, k)
         lines.append(
-            f"static __device__ __noinline__ void win_contig_{b}_{k}(float2* __restrict__ s, const float* __restrict__ gp) {{\n"
-            f"  float2 v[{m}];\n"
-            f"#pragma unroll\n  for (int j = 0; j < {m}; ++j) v[j] = s[j];\n"
-            f"  win_givens_{b}_{k}(v, gp);\n"
-            f"#pragma unroll\n  for (int j = 0; j < {m}; ++j) s[j] = v[j];\n}}"
-        )
-        lines.append(
-            f"static __device__ __noinline__ void win_table_{b}_{k}(float2* __restrict__ s, const int* __restrict__ off, const float* __restrict__ gp) {{\n"
+            f"template <bool COMP> static __device__ __noinline__ void win_group_{b}_{k}(float2* __restrict__ s,"
+            f" const int* __restrict__ off, const float* __restrict__ gp, const float* __restrict__ gl) {{\n"
             f"  float2 v[{m}];\n"
             f"#pragma unroll\n  for (int j = 0; j < {m}; ++j) v[j] = s[off[j]];\n"
-            f"  win_givens_{b}_{k}(v, gp);\n"
+            f"  win_givens_{b}_{k}<COMP>(v, gp, gl);\n"
             f"#pragma unroll\n  for (int j = 0; j < {m}; ++j) s[off[j]] = v[j];\n}}"
         )
+    for k in range(0, b + 1):
+        m = math.comb(b, k)
+        lines.append(
+            f"template <bool COMP> static __device__ __noinline__ void win_rows_{b}_{k}(const float2* __restrict__ si,"
+            f" float2* __restrict__ so, long long ld, const int* __restrict__ off, const float* __restrict__ gp,"
+            f" const float* __restrict__ gl, const float2* __restrict__ ph_in, const float2* __restrict__ ph_out) {{\n"
+            f"  float2 v[{m}];\n"
+            f"#pragma unroll\n  for (int j = 0; j < {m}; ++j) v[j] = si[(long long)off[j] * ld];\n"
+            f"  if (ph_in) {{\n"
+            f"#pragma unroll\n    for (int j = 0; j < {m}; ++j) v[j] = cmulf2(v[j], ph_in[off[j]]);\n  }}\n"
+            f"  win_givens_{b}_{k}<COMP>(v, gp, gl);\n"
+            f"  if (ph_out) {{\n"
+            f"#pragma unroll\n    for (int j = 0; j < {m}; ++j) v[j] = cmulf2(v[j], ph_out[off[j]]);\n  }}\n"
+            f"#pragma unroll\n  for (int j = 0; j < {m}; ++j) so[(long long)off[j] * ld] = v[j];\n}}"
+        )
     lines.append(f"template <> struct WinDispatch<{b}> {{")
-    lines.append("  static __device__ __forceinline__ void contig(int k, float2* s, const float* gp) {")
+    lines.append("  template <bool COMP> static __device__ __forceinline__ void rows(int k, const float2* si, float2* so,"
+                 " long long ld, const int* off, const float* gp, const float* gl, const float2* ph_in,"
+                 " const float2* ph_out) {")
     lines.append("    switch (k) {")
     for k in range(0, b + 1):
-        lines.append(f"      case {k}: win_contig_{b}_{k}(s, gp); break;")
+        lines.append(f"      case {k}: win_rows_{b}_{k}<COMP>(si, so, ld, off, gp, gl, ph_in, ph_out); break;")
     lines.append("      default: break;\n    }\n  }")
-    lines.append("  static __device__ __forceinline__ void table(int k, float2* s, const int* off, const float* gp) {")
+    lines.append("  template <bool COMP> static __device__ __forceinline__ void group(int k, float2* s, const int* off,"
+                 " const float* gp, const float* gl) {")
     lines.append("    switch (k) {")
     for k in range(0, b + 1):
-        lines.append(f"      case {k}: win_table_{b}_{k}(s, off, gp); break;")
-    lines.append("      default: break;\n    }\n  }")
-    lines.append("  template <class F> static __device__ __forceinline__ void cs(int k, int i, F&& f) {")
-    lines.append("    switch (k) {")
-    for k in range(1, b + 1):
-        lines.append(f"      case {k}: cs_site_{b}_{k}(i, f); break;")
+        lines.append(f"      case {k}: win_group_{b}_{k}<COMP>(s, off, gp, gl); break;")
     lines.append("      default: break;\n    }\n  }")
     lines.append("};")
     return "\n".join(lines)
@@ -137,13 +146,13 @@ def main(out_path: str) -> None:
         "  return (k < 0 || k > b) ? 0 : (k == 0 || k == b) ? 1 : win_members(b - 1, k - 1) + win_members(b - 1, k);",
         "}",
         "template <int B> struct WinDispatch;",
+        "__device__ __forceinline__ float2 cmulf2(float2 a, float2 b) {",
+        "  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);",
+        "}",
     ]
     for b in range(1, MAX_B + 1):
         for k in range(0, b + 1):
             parts.append(emit_givens(b, k))
-    for h in range(1, MAX_B + 1):
-        for k in range(1, h + 1):
-            parts.append(emit_cs(h, k))
     for b in range(1, MAX_B + 1):
         parts.append(emit_groups(b))
     Path(out_path).write_text("\n".join(parts) + "\n")

@@ -2,5 +2,5 @@
 #include "launch.cuh"
 
 namespace ffgb {
-template int launch_sector<float, 15>(const SectorParams<float>&, int, int, int, cudaStream_t);
+template int launch_sector<float, 15>(const SectorParams<float>&, long long, int, int, cudaStream_t, int*);
 }  // namespace ffgb

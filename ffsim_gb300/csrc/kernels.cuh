@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #define FFGB_MAXN 18
 #define FFGB_MAXTRI (FFGB_MAXN * (FFGB_MAXN - 1) / 2)
 #define FFGB_BST (FFGB_MAXN + 2)  // stride of the binomial table
@@ -49,6 +51,9 @@ struct SectorParams {
   signed char tri_l[FFGB_MAXTRI];
   T win[4][28 * 3];
   T cs[8][8];
+  int comp;              // apply the FP32 rounding residuals of the window/CS coefficients
+  T win_lo[4][28 * 3];
+  T cs_lo[8][8];
   int has_dphase;
   T dphase[FFGB_MAXN][2];
   // rows
@@ -73,7 +78,7 @@ struct SectorParams {
 
 struct Layout {
   int binom, plan, tab, dt, xt, red, rows, total;
-  int nch, chunk_bits;
+  int nch, chunk_bits, dch;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
@@ -81,22 +86,28 @@ __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 // Shared-memory layout; identical on host and device.
 __host__ __device__ inline Layout make_layout(int tsize, int R, int dim, int col_norb,
                                               int chunk_bits, int has_dphase, int diag_mode,
-                                              int kind) {
+                                              int kind, int comp) {
   Layout L;
   int off = 0;
   L.binom = off;
   off += align16(FFGB_BST * FFGB_BST * 4);
   L.plan = off;
   if (kind == KIND_TRIANGLE) off += align16(FFGB_MAXTRI * 3 * tsize);
-  if (kind == KIND_FULL || kind == KIND_CSD) off += align16((4 * 28 * 3 + 64) * tsize);
+  if (kind == KIND_FULL || kind == KIND_CSD) off += align16((comp ? 2 : 1) * (4 * 28 * 3 + 64) * tsize);
   L.tab = off;
   off += align16(256 * 2 + 256 * 4 + 16 * 4);
+  // cross-half pair table: (k, i) -> packed (j, jp, parity) entries and offsets
+  if (kind == KIND_CSD) off += align16(1024 * 2 + 9 * 8 * 2 + 16);
+  if (kind == KIND_CSD || kind == KIND_FULL) off += align16(72 * 4);  // identity member offsets
   L.chunk_bits = chunk_bits;
   L.nch = (col_norb + chunk_bits - 1) / chunk_bits;
   if (L.nch < 1) L.nch = 1;
   const int nent = L.nch << chunk_bits;
+  // final orbital phases: 4-bit chunks (small table, a few more multiplies)
+  L.dch = (col_norb + 3) / 4;
+  if (L.dch < 1) L.dch = 1;
   L.dt = off;
-  if (has_dphase && diag_mode != DIAG_PHASE) off += align16(nent * 2 * tsize);
+  if (has_dphase && diag_mode != DIAG_PHASE) off += align16((L.dch << 4) * 2 * tsize);
   L.xt = off;
   if (diag_mode == DIAG_PHASE) off += align16(nent * 2 * tsize + 2 * FFGB_MAXN * 8 + 16);
   if (diag_mode == DIAG_COEF) off += align16(nent * tsize + 2 * FFGB_MAXN * 8 + 16);
@@ -190,13 +201,34 @@ __device__ __forceinline__ int rank_shifted(unsigned s, int base_orb, int m0, co
 }
 
 // rotation of a complex64 pair by [[c, s], [-conj(s), c]]:
-// x <- c x + s y, y <- -conj(s) x + c y
-__device__ __forceinline__ void rot_pair(float2& x, float2& y, float c, float sr, float si) {
+// x <- c x + s y, y <- -conj(s) x + c y, on packed FP32x2 (re, im) lanes.
+// With COMP the coefficients are (c + cl, s + sl): the FP32 rounding residuals
+// of the FP64 plan are applied first, so the rotation angle is exact to ~1e-14
+// instead of ~6e-8.
+template <bool COMP>
+__device__ __forceinline__ void rot_pair(float2& x, float2& y, float c, float sr, float si, float cl,
+                                         float srl, float sil) {
+  const float2 xs = make_float2(x.y, x.x), ys = make_float2(y.y, y.x);
+  const float2 i2 = make_float2(-si, si);
   float2 nx, ny;
-  nx.x = fmaf(c, x.x, fmaf(sr, y.x, -si * y.y));
-  nx.y = fmaf(c, x.y, fmaf(sr, y.y, si * y.x));
-  ny.x = fmaf(c, y.x, fmaf(-sr, x.x, -si * x.y));
-  ny.y = fmaf(c, y.y, fmaf(-sr, x.y, si * x.x));
+  if constexpr (!COMP) {
+    nx = __fmul2_rn(make_float2(c, c), x);
+    ny = __fmul2_rn(make_float2(c, c), y);
+  } else {
+    const float2 il = make_float2(-sil, sil);
+    nx = __fmul2_rn(make_float2(cl, cl), x);
+    nx = __ffma2_rn(make_float2(srl, srl), y, nx);
+    nx = __ffma2_rn(il, ys, nx);
+    ny = __fmul2_rn(make_float2(cl, cl), y);
+    ny = __ffma2_rn(make_float2(-srl, -srl), x, ny);
+    ny = __ffma2_rn(il, xs, ny);
+    nx = __ffma2_rn(make_float2(c, c), x, nx);
+    ny = __ffma2_rn(make_float2(c, c), y, ny);
+  }
+  nx = __ffma2_rn(make_float2(sr, sr), y, nx);
+  nx = __ffma2_rn(i2, ys, nx);
+  ny = __ffma2_rn(make_float2(-sr, -sr), x, ny);
+  ny = __ffma2_rn(i2, xs, ny);
   x = nx;
   y = ny;
 }
@@ -210,12 +242,17 @@ namespace ffgb {
 namespace ffgb {
 
 // Distribute work items to warps so that each warp handles 32 items of one
-// class k (the register-array shape depends on k).
+// class k (the register-array shape depends on k).  Classes run from the
+// middle of [kbeg, kend] outwards (largest groups first) and consecutive
+// tasks go to consecutive warps, so few distinct code paths are live at once.
 template <class CountF, class Body>
 __device__ __forceinline__ void warp_tasks(int kbeg, int kend, CountF count, Body body) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int kmid = (kbeg + kend) >> 1;
   int t0 = 0;
-  for (int k = kbeg; k <= kend; ++k) {
+  for (int step = 0; step <= kend - kbeg; ++step) {
+    const int k = (step & 1) ? kmid + ((step + 1) >> 1) : kmid - (step >> 1);
+    if (k < kbeg || k > kend) continue;
     const int n = count(k);
     const int nt = (n + 31) >> 5;
     int first = warp - (t0 % nw);
@@ -232,13 +269,47 @@ __device__ __forceinline__ void warp_tasks(int kbeg, int kend, CountF count, Bod
 // the sector kernel
 // ---------------------------------------------------------------------------
 
+__device__ __forceinline__ void cp_async8(void* s, const void* g) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* s, const void* g) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Copy `bytes` (a multiple of 8) from global to shared memory with the
+// asynchronous copy unit; 16-byte copies when both sides allow it.
+__device__ __forceinline__ void stage_rows(void* dst, const void* src, long long bytes) {
+  const int tid = threadIdx.x, nth = blockDim.x;
+  if ((((uintptr_t)dst | (uintptr_t)src) & 15) == 0 && (bytes & 15) == 0) {
+    const long long n = bytes >> 4;
+    for (long long i = tid; i < n; i += nth)
+      cp_async16((char*)dst + (i << 4), (const char*)src + (i << 4));
+  } else {
+    const long long n = bytes >> 3;
+    for (long long i = tid; i < n; i += nth) cp_async8((char*)dst + (i << 3), (const char*)src + (i << 3));
+  }
+  cp_async_wait_all();
+}
+
+// Persistent CTAs: each CTA builds its tables once and then processes the row
+// chunks blockIdx.x, blockIdx.x + gridDim.x, ...
+// Threads per CTA of the sector kernel: windows of 8 orbitals hold 70
+// complex64 members per thread, so those kernels run 128 threads with the
+// full register file share of 2 CTAs per SM.
+__host__ __device__ constexpr int sector_threads(int nw) {
+  return nw == 0 ? 256 : ((nw == 8 || nw >= 15) ? 128 : 192);
+}
+
 template <typename T, int NW>
-__global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
+__global__ void __launch_bounds__(sector_threads(NW), NW > 0 ? 2 : 1)
     sector_kernel(const __grid_constant__ SectorParams<T> P) {
   using C = typename CT<T>::type;
   extern __shared__ __align__(16) unsigned char smem[];
   const Layout L = make_layout((int)sizeof(T), P.rows_per_cta, P.dim, P.norb, P.chunk_bits,
-                               P.has_dphase, P.diag_mode, P.kind);
+                               P.has_dphase, P.diag_mode, P.kind, P.comp);
   // final orbital phases are folded into the per-row phase tables when both are present
   const bool sep_dphase = P.has_dphase && P.diag_mode != DIAG_PHASE;
   int* sB = (int*)(smem + L.binom);
@@ -250,166 +321,93 @@ __global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
   double* sRed = (double*)(smem + L.red);
 
   const int tid = threadIdx.x, nth = blockDim.x;
-  const long long row0 = (long long)blockIdx.x * P.rows_per_cta;
-  long long rem = P.n_rows - row0;
-  const int R = (int)(rem < P.rows_per_cta ? rem : P.rows_per_cta);
   const int dim = P.dim, norb = P.norb, nocc = P.nocc;
+  const long long n_chunks = (P.n_rows + P.rows_per_cta - 1) / P.rows_per_cta;
 
-  // binomial table
+  // ------------------------------------------------------------ per-CTA setup
   for (int idx = tid; idx < FFGB_BST * FFGB_BST; idx += nth) {
-    int a = idx / FFGB_BST, b = idx % FFGB_BST;
+    const int a = idx / FFGB_BST, b = idx % FFGB_BST;
     int v = 0;
     if (b <= a) {
-      long long r = 1;
-      for (int i = 1; i <= b; ++i) r = r * (a - b + i) / i;
-      v = (int)r;
+      int r = 1;
+      for (int i = 1; i <= b; ++i) r = r * (a - b + i) / i;  // exact: r * (a-b+i) is divisible by i
+      v = r;
     }
     sB[idx] = v;
   }
-  // plan coefficients
   if (P.kind == KIND_TRIANGLE) {
     for (int idx = tid; idx < P.n_tri * 3; idx += nth) sPlan[idx] = P.tri[idx];
   } else if (P.kind == KIND_FULL || P.kind == KIND_CSD) {
     for (int idx = tid; idx < 4 * 28 * 3; idx += nth) sPlan[idx] = (&P.win[0][0])[idx];
     for (int idx = tid; idx < 64; idx += nth) sPlan[4 * 28 * 3 + idx] = (&P.cs[0][0])[idx];
+    int* sId = (int*)(smem + L.tab + (P.kind == KIND_CSD ? align16(1600 + 1024 * 2 + 9 * 8 * 2 + 16) : 1600));
+    for (int idx = tid; idx < 72; idx += nth) sId[idx] = idx;
+    if (P.comp) {
+      for (int idx = tid; idx < 4 * 28 * 3; idx += nth) sPlan[400 + idx] = (&P.win_lo[0][0])[idx];
+      for (int idx = tid; idx < 64; idx += nth) sPlan[400 + 4 * 28 * 3 + idx] = (&P.cs_lo[0][0])[idx];
+    }
   }
-  // rows: contiguous block [row0, row0 + R) of the input
-  {
-    const C* src = (const C*)P.in + row0 * (long long)dim;
-    const int n = R * dim;
-    for (int idx = tid; idx < n; idx += nth) srow[idx] = src[idx];
-  }
-  __syncthreads();
-
-  // --------------------------------------------------------------- stages
-  if constexpr (NW == 0) {
-    if (P.kind == KIND_TRIANGLE && nocc >= 1 && nocc <= norb - 1) {
-      const int npairs = bn(sB, norb - 2, nocc - 1);
-      const int items = R * npairs;
-      for (int g = 0; g < P.n_tri; ++g) {
-        const int l = P.tri_l[g];
-        const T c = sPlan[3 * g], sr = sPlan[3 * g + 1], si = sPlan[3 * g + 2];
-        const unsigned lowmask = (1u << l) - 1u;
-        for (int item = tid; item < items; item += nth) {
-          const int rho = item / npairs, t = item - rho * npairs;
-          const unsigned p = unrank_colex(t, norb - 2, nocc - 1, sB);
-          const unsigned x = (p & lowmask) | (1u << l) | ((p >> l) << (l + 2));
-          const int rx = rank_colex(x, sB);
-          const int ry = rx + bn(sB, l, __popc(p & lowmask));
-          C* base = srow + (long long)rho * dim;
-          C a = base[rx], b = base[ry];
-          C na, nb;
-          na.x = c * a.x + sr * b.x - si * b.y;
-          na.y = c * a.y + sr * b.y + si * b.x;
-          nb.x = c * b.x - sr * a.x - si * a.y;
-          nb.y = c * b.y - sr * a.y + si * a.x;
-          base[rx] = na;
-          base[ry] = nb;
+  constexpr int H = (NW <= 8) ? NW : NW / 2;
+  constexpr int Q = NW - H;
+  if constexpr (NW > 8) {
+    __syncthreads();
+    if (tid <= Q) {
+      int o = 0;
+      for (int m = 0; m < tid; ++m) o += bn(sB, Q, m);
+      sMoff[tid] = o;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < (1 << Q); idx += nth) {
+      int m = 0;
+      while (m < Q && idx >= sMoff[m + 1]) ++m;
+      const int g = idx - sMoff[m];
+      const unsigned s2 = unrank_colex(g, Q, m, sB);
+      sS2[idx] = (unsigned short)s2;
+      const int m0 = nocc - m;
+      sRT[idx] = (m0 >= 0 && m0 <= H) ? rank_shifted(s2, H, m0, sB) : 0;
+    }
+    // pair table of the cross-half rotations: for k electrons in the low half
+    // and site i, every member j (colex index) of the k-family with bit i set,
+    // the index jp of its partner (bit i cleared) in the (k-1)-family and the
+    // parity of the low-half orbitals occupied above i.
+    unsigned short* sCS = (unsigned short*)(smem + L.tab + 1600);
+    unsigned short* sCSo = sCS + 1024;  // [k][i] offsets, k in 1..H
+    if (tid == 0) {
+      int o = 0;
+      for (int k = 1; k <= H; ++k)
+        for (int i = 0; i < H; ++i) {
+          sCSo[(k - 1) * 8 + i] = (unsigned short)o;
+          o += bn(sB, H - 1, k - 1);
         }
-        __syncthreads();
-      }
     }
-  } else {
-    static_assert(NW == 0 || sizeof(T) == 4, "window kernels are complex64 only");
-    constexpr int H = (NW <= 8) ? NW : NW / 2;
-    constexpr int Q = NW - H;
-    const float* wp = (const float*)sPlan;
-    if constexpr (NW <= 8) {
-      // the whole sector is one window
-      for (int rho = tid; rho < R; rho += nth) WinDispatch<H>::contig(nocc, srow + (long long)rho * dim, wp);
-      __syncthreads();
-    } else {
-      // tables over subsets of the high half (Q bits)
-      if (tid <= Q) {
-        int o = 0;
-        for (int m = 0; m < tid; ++m) o += bn(sB, Q, m);
-        sMoff[tid] = o;
+    __syncthreads();
+    if (tid < H * H) {  // one thread per (k, i) fills its list
+      const int k = tid / H + 1, i = tid % H;
+      unsigned short* dst = sCS + sCSo[(k - 1) * 8 + i];
+      const int nk = bn(sB, H, k);
+      int pos = 0;
+      for (int j = 0; j < nk; ++j) {
+        const unsigned w = unrank_colex(j, H, k, sB);
+        if (!((w >> i) & 1u)) continue;
+        const int jp = rank_colex(w ^ (1u << i), sB);
+        const int par = __popc(w >> (i + 1)) & 1;
+        dst[pos++] = (unsigned short)(j | (jp << 7) | (par << 14));
       }
-      __syncthreads();
-      for (int idx = tid; idx < (1 << Q); idx += nth) {
-        int m = 0;
-        while (m < Q && idx >= sMoff[m + 1]) ++m;
-        const int g = idx - sMoff[m];
-        const unsigned s2 = unrank_colex(g, Q, m, sB);
-        sS2[idx] = (unsigned short)s2;
-        const int m0 = nocc - m;
-        sRT[idx] = (m0 >= 0 && m0 <= H) ? rank_shifted(s2, H, m0, sB) : 0;
-      }
-      __syncthreads();
-      const int klo_low = max(0, nocc - Q), khi_low = min(H, nocc);
-      const int klo_high = max(0, nocc - H), khi_high = min(Q, nocc);
-      auto low_stage = [&](const float* gp) {
-        warp_tasks(
-            klo_low, khi_low, [&](int k) { return R * bn(sB, Q, nocc - k); },
-            [&](int k, int item) {
-              const int G = bn(sB, Q, nocc - k);
-              const int rho = item / G, g = item - rho * G;
-              const int base = rho * dim + sRT[sMoff[nocc - k] + g];
-              WinDispatch<H>::contig(k, srow + base, gp);
-            });
-        __syncthreads();
-      };
-      auto high_stage = [&](const float* gp) {
-        warp_tasks(
-            klo_high, khi_high, [&](int k) { return R * bn(sB, H, nocc - k); },
-            [&](int k, int item) {
-              const int G = bn(sB, H, nocc - k);
-              const int rho = item / G, g = item - rho * G;
-              WinDispatch<Q>::table(k, srow + rho * dim + g, sRT + sMoff[k], gp);
-            });
-        __syncthreads();
-      };
-      low_stage(wp + 0 * 84);
-      high_stage(wp + 1 * 84);
-      // cross-half rotations (i, H + i)
-      const float* csp = wp + 4 * 84;
-      for (int i = 0; i < H; ++i) {
-        const float g00r = csp[8 * i + 0], g00i = csp[8 * i + 1], g01r = csp[8 * i + 2],
-                    g01i = csp[8 * i + 3], g10r = csp[8 * i + 4], g10i = csp[8 * i + 5],
-                    g11r = csp[8 * i + 6], g11i = csp[8 * i + 7];
-        warp_tasks(
-            max(1, klo_low), khi_low, [&](int k) { return R * bn(sB, Q, nocc - k); },
-            [&](int k, int item) {
-              const int m = nocc - k;
-              const int G = bn(sB, Q, m);
-              const int rho = item / G, g = item - rho * G;
-              const unsigned s2 = sS2[sMoff[m] + g];
-              if ((s2 >> i) & 1u) return;
-              float2* bx = srow + rho * dim + sRT[sMoff[m] + g];
-              float2* by = srow + rho * dim + rank_shifted(s2 | (1u << i), H, k - 1, sB);
-              const int sg0 = __popc(s2 & ((1u << i) - 1u)) & 1;
-              WinDispatch<H>::cs(k, i, [&](int j, int jp, int par) {
-                const float sgn = ((par ^ sg0) & 1) ? -1.f : 1.f;
-                const float2 x = bx[j], y = by[jp];
-                float2 nx, ny;
-                nx.x = g00r * x.x - g00i * x.y + sgn * (g01r * y.x - g01i * y.y);
-                nx.y = g00r * x.y + g00i * x.x + sgn * (g01r * y.y + g01i * y.x);
-                ny.x = sgn * (g10r * x.x - g10i * x.y) + g11r * y.x - g11i * y.y;
-                ny.y = sgn * (g10r * x.y + g10i * x.x) + g11r * y.y + g11i * y.x;
-                bx[j] = nx;
-                by[jp] = ny;
-              });
-            });
-        __syncthreads();
-      }
-      low_stage(wp + 2 * 84);
-      high_stage(wp + 3 * 84);
     }
   }
-
-  // --------------------------------------------------------------- epilogue
   const int cb = L.chunk_bits, nch = L.nch, nent = nch << cb;
   const unsigned cmask = (1u << cb) - 1u;
   C* sDT = (C*)(smem + L.dt);
+  const int dch = L.dch;
   if (sep_dphase) {
-    for (int e = tid; e < nent; e += nth) {
-      const int c = e >> cb;
-      unsigned x = (unsigned)(e & cmask);
+    for (int e = tid; e < (dch << 4); e += nth) {
+      const int c = e >> 4;
+      unsigned x = (unsigned)(e & 15);
       C ph = cmake<C>(1.0, 0.0);
       while (x) {
         const int b = __ffs(x) - 1;
         x &= x - 1;
-        const int orb = c * cb + b;
+        const int orb = c * 4 + b;
         if (orb < norb) {
           C d;
           d.x = P.dphase[orb][0];
@@ -431,126 +429,302 @@ __global__ void __launch_bounds__(NW > 0 ? 192 : 256, NW > 0 ? 2 : 1)
   float acc_f = 0.f, comp_f = 0.f;
   __syncthreads();
 
-  for (int rho = 0; rho < R; ++rho) {
-    const long long r = row0 + rho;
-    T rowconst = 0;
-    if (P.diag_mode != DIAG_NONE) {
-      const unsigned rs = P.row_strings[r];
-      const int rn = P.row_norb;
-      // m[l] = sum_i cross[i][l] g_i(r); sM[0..norb) = weights, sM[MAXN] = row constant
-      if (tid < norb) {
-        double m = 0.0;
-        for (int i = 0; i < rn; ++i) {
-          const double gi = P.zrep ? ((rs >> i) & 1u ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
-          m += P.cross[i][tid] * gi;
-        }
-        sM[tid] = m;
-      }
-      if (tid == 32 || (nth <= 32 && tid == 0)) {
-        double f = 0.0;
-        for (int i = 0; i < rn; ++i) {
-          const double gi = P.zrep ? ((rs >> i) & 1u ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
-          if (gi == 0.0) continue;
-          for (int i2 = i; i2 < rn; ++i2) {
-            const double gj = P.zrep ? ((rs >> i2) & 1u ? -1.0 : 1.0) : (double)((rs >> i2) & 1u);
-            f += P.rsame[i][i2] * gi * gj;
+  for (long long chunk = blockIdx.x; chunk < n_chunks; chunk += gridDim.x) {
+    const long long row0 = chunk * P.rows_per_cta;
+    const long long rem = P.n_rows - row0;
+    const int R = (int)(rem < P.rows_per_cta ? rem : P.rows_per_cta);
+
+    // rows [row0, row0 + R) are contiguous in the input
+    stage_rows(srow, (const C*)P.in + row0 * (long long)dim, (long long)R * dim * (long long)sizeof(C));
+    __syncthreads();
+
+    // ------------------------------------------------------------- stages
+    if constexpr (NW == 0) {
+      if (P.kind == KIND_TRIANGLE && nocc >= 1 && nocc <= norb - 1) {
+        const int npairs = bn(sB, norb - 2, nocc - 1);
+        const int items = R * npairs;
+        for (int g = 0; g < P.n_tri; ++g) {
+          const int l = P.tri_l[g];
+          const T c = sPlan[3 * g], sr = sPlan[3 * g + 1], si = sPlan[3 * g + 2];
+          const unsigned lowmask = (1u << l) - 1u;
+          for (int item = tid; item < items; item += nth) {
+            const int rho = item / npairs, t = item - rho * npairs;
+            const unsigned p = unrank_colex(t, norb - 2, nocc - 1, sB);
+            const unsigned x = (p & lowmask) | (1u << l) | ((p >> l) << (l + 2));
+            const int rx = rank_colex(x, sB);
+            const int ry = rx + bn(sB, l, __popc(p & lowmask));
+            C* base = srow + (long long)rho * dim;
+            const C a = base[rx], b = base[ry];
+            C na, nb;
+            na.x = c * a.x + sr * b.x - si * b.y;
+            na.y = c * a.y + sr * b.y + si * b.x;
+            nb.x = c * b.x - sr * a.x - si * a.y;
+            nb.y = c * b.y - sr * a.y + si * a.x;
+            base[rx] = na;
+            base[ry] = nb;
           }
+          __syncthreads();
         }
-        sM[FFGB_MAXN] = f;
       }
-      __syncthreads();
-      if (tid == 0) {
-        double f = sM[FFGB_MAXN];
-        if (P.zrep)
-          for (int l = 0; l < norb; ++l) f += sM[l];
-        sM[FFGB_MAXN + 1] = f;
-      }
-      __syncthreads();
-      const double wsc = P.zrep ? -2.0 : 1.0;
-      const double rc = sM[FFGB_MAXN + 1];
-      for (int e = tid; e < nent; e += nth) {
-        const int c = e >> cb;
-        unsigned x = (unsigned)(e & cmask);
-        double f = (c == 0) ? rc : 0.0;
-        while (x) {
-          const int b = __ffs(x) - 1;
-          x &= x - 1;
-          const int orb = c * cb + b;
-          if (orb < norb) f += wsc * sM[orb];
+    } else {
+      static_assert(NW == 0 || sizeof(T) == 4, "window kernels are complex64 only");
+      const float* wp = (const float*)sPlan;
+      const int* sId = (const int*)(smem + L.tab + (NW > 8 ? align16(1600 + 1024 * 2 + 9 * 8 * 2 + 16) : 1600));
+      if constexpr (NW <= 8) {
+        // the whole sector is one window
+        for (int rho = tid; rho < R; rho += nth) {
+          if (P.comp)
+            WinDispatch<H>::template group<true>(nocc, srow + (long long)rho * dim, sId, wp, wp + 400);
+          else
+            WinDispatch<H>::template group<false>(nocc, srow + (long long)rho * dim, sId, wp, wp);
         }
-        if (P.diag_mode == DIAG_PHASE) {
-          C ph = phase_of(f, (C*)nullptr);
-          if (P.has_dphase) {
-            unsigned y = (unsigned)(e & cmask);
-            while (y) {
-              const int b = __ffs(y) - 1;
-              y &= y - 1;
-              const int orb = c * cb + b;
-              if (orb < norb) {
-                C d;
-                d.x = P.dphase[orb][0];
-                d.y = P.dphase[orb][1];
-                ph = cmul(ph, d);
-              }
+        __syncthreads();
+      } else {
+        const int klo_low = max(0, nocc - Q), khi_low = min(H, nocc);
+        const int klo_high = max(0, nocc - H), khi_high = min(Q, nocc);
+        auto low_stage = [&](const float* gp) {
+          warp_tasks(
+              klo_low, khi_low, [&](int k) { return R * bn(sB, Q, nocc - k); },
+              [&](int k, int item) {
+                const int G = bn(sB, Q, nocc - k);
+                const int rho = item / G, g = item - rho * G;
+                const int base = rho * dim + sRT[sMoff[nocc - k] + g];
+                if (P.comp)
+                  WinDispatch<H>::template group<true>(k, srow + base, sId, gp, gp + 400);
+                else
+                  WinDispatch<H>::template group<false>(k, srow + base, sId, gp, gp);
+              });
+          __syncthreads();
+        };
+        auto high_stage = [&](const float* gp) {
+          warp_tasks(
+              klo_high, khi_high, [&](int k) { return R * bn(sB, H, nocc - k); },
+              [&](int k, int item) {
+                const int G = bn(sB, H, nocc - k);
+                const int rho = item / G, g = item - rho * G;
+                if (P.comp)
+                  WinDispatch<Q>::template group<true>(k, srow + rho * dim + g, sRT + sMoff[k], gp, gp + 400);
+                else
+                  WinDispatch<Q>::template group<false>(k, srow + rho * dim + g, sRT + sMoff[k], gp, gp);
+              });
+          __syncthreads();
+        };
+        low_stage(wp + 0 * 84);
+        high_stage(wp + 1 * 84);
+        // cross-half rotations (i, H + i): for each site, the groups of the
+        // low-half window whose high part lacks bit i (s2 enumerated over the
+        // other Q-1 high orbitals), each pair read from the shared table.
+        const float* csp = wp + 4 * 84;
+        const unsigned short* sCS = (const unsigned short*)(smem + L.tab + 1600);
+        const unsigned short* sCSo = sCS + 1024;
+        for (int i = 0; i < H; ++i) {
+          const float g00r = csp[8 * i + 0], g00i = csp[8 * i + 1], g01r = csp[8 * i + 2],
+                      g01i = csp[8 * i + 3], g10r = csp[8 * i + 4], g10i = csp[8 * i + 5],
+                      g11r = csp[8 * i + 6], g11i = csp[8 * i + 7];
+          const float* csl = csp + 400;
+          const bool comp = P.comp != 0;
+          const float l00r = comp ? csl[8 * i + 0] : 0.f, l00i = comp ? csl[8 * i + 1] : 0.f,
+                      l01r = comp ? csl[8 * i + 2] : 0.f, l01i = comp ? csl[8 * i + 3] : 0.f,
+                      l10r = comp ? csl[8 * i + 4] : 0.f, l10i = comp ? csl[8 * i + 5] : 0.f,
+                      l11r = comp ? csl[8 * i + 6] : 0.f, l11i = comp ? csl[8 * i + 7] : 0.f;
+          const unsigned lowm = (1u << i) - 1u;
+          warp_tasks(
+              max(1, klo_low), min(khi_low, nocc), [&](int k) { return R * bn(sB, Q - 1, nocc - k); },
+              [&](int k, int item) {
+                const int m = nocc - k;
+                const int G = bn(sB, Q - 1, m);
+                const int rho = item / G, g = item - rho * G;
+                const unsigned s2r = unrank_colex(g, Q - 1, m, sB);
+                const unsigned s2 = (s2r & lowm) | ((s2r >> i) << (i + 1));
+                float2* bx = srow + rho * dim + rank_shifted(s2, H, k, sB);
+                float2* by = srow + rho * dim + rank_shifted(s2 | (1u << i), H, k - 1, sB);
+                const int sg0 = __popc(s2 & lowm) & 1;
+                const unsigned short* tab = sCS + sCSo[(k - 1) * 8 + i];
+                const int cnt = bn(sB, H - 1, k - 1);
+                auto run = [&](auto comp_tag) {
+                  constexpr bool CP = decltype(comp_tag)::value;
+#pragma unroll 2
+                  for (int t = 0; t < cnt; ++t) {
+                    const unsigned e = tab[t];
+                    const int j = e & 127, jp = (e >> 7) & 127;
+                    const float sgn = (((e >> 14) ^ sg0) & 1) ? -1.f : 1.f;
+                    const float2 x = bx[j], y = by[jp];
+                    float ax = 0.f, ay = 0.f, bxr = 0.f, byi = 0.f;
+                    if constexpr (CP) {  // FP32 rounding residuals of the coefficients first
+                      ax = l00r * x.x - l00i * x.y + sgn * (l01r * y.x - l01i * y.y);
+                      ay = l00r * x.y + l00i * x.x + sgn * (l01r * y.y + l01i * y.x);
+                      bxr = sgn * (l10r * x.x - l10i * x.y) + l11r * y.x - l11i * y.y;
+                      byi = sgn * (l10r * x.y + l10i * x.x) + l11r * y.y + l11i * y.x;
+                    }
+                    float2 nx, ny;
+                    nx.x = g00r * x.x - g00i * x.y + sgn * (g01r * y.x - g01i * y.y) + ax;
+                    nx.y = g00r * x.y + g00i * x.x + sgn * (g01r * y.y + g01i * y.x) + ay;
+                    ny.x = sgn * (g10r * x.x - g10i * x.y) + g11r * y.x - g11i * y.y + bxr;
+                    ny.y = sgn * (g10r * x.y + g10i * x.x) + g11r * y.y + g11i * y.x + byi;
+                    bx[j] = nx;
+                    by[jp] = ny;
+                  }
+                };
+                if (comp)
+                  run(std::true_type{});
+                else
+                  run(std::false_type{});
+              });
+          __syncthreads();
+        }
+        low_stage(wp + 2 * 84);
+        high_stage(wp + 3 * 84);
+      }
+    }
+
+    // ----------------------------------------------------------- epilogue
+    for (int rho = 0; rho < R; ++rho) {
+      const long long r = row0 + rho;
+      if (P.diag_mode != DIAG_NONE) {
+        const unsigned rs = P.row_strings[r];
+        const int rn = P.row_norb;
+        // m[l] = sum_i cross[i][l] g_i(r); sM[0..norb) = weights, sM[MAXN] = row part
+        if (tid < norb) {
+          double m = 0.0;
+          for (int i = 0; i < rn; ++i) {
+            const double gi = P.zrep ? ((rs >> i) & 1u ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
+            m += P.cross[i][tid] * gi;
+          }
+          sM[tid] = m;
+        }
+        if (tid == 32) {
+          double f = 0.0;
+          for (int i = 0; i < rn; ++i) {
+            const double gi = P.zrep ? ((rs >> i) & 1u ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
+            if (gi == 0.0) continue;
+            for (int i2 = i; i2 < rn; ++i2) {
+              const double gj = P.zrep ? ((rs >> i2) & 1u ? -1.0 : 1.0) : (double)((rs >> i2) & 1u);
+              f += P.rsame[i][i2] * gi * gj;
             }
           }
-          sXP[e] = ph;
-        } else {
-          sXC[e] = (T)f;
+          sM[FFGB_MAXN] = f;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          double f = sM[FFGB_MAXN];
+          if (P.zrep)
+            for (int l = 0; l < norb; ++l) f += sM[l];
+          sM[FFGB_MAXN + 1] = f;
+        }
+        __syncthreads();
+        const double wsc = P.zrep ? -2.0 : 1.0;
+        const double rc = sM[FFGB_MAXN + 1];
+        for (int e = tid; e < nent; e += nth) {
+          const int c = e >> cb;
+          unsigned x = (unsigned)(e & cmask);
+          double f = (c == 0) ? rc : 0.0;
+          while (x) {
+            const int b = __ffs(x) - 1;
+            x &= x - 1;
+            const int orb = c * cb + b;
+            if (orb < norb) f += wsc * sM[orb];
+          }
+          if (P.diag_mode == DIAG_PHASE) {
+            C ph = phase_of(f, (C*)nullptr);
+            if (P.has_dphase) {
+              unsigned y = (unsigned)(e & cmask);
+              while (y) {
+                const int b = __ffs(y) - 1;
+                y &= y - 1;
+                const int orb = c * cb + b;
+                if (orb < norb) {
+                  C d;
+                  d.x = P.dphase[orb][0];
+                  d.y = P.dphase[orb][1];
+                  ph = cmul(ph, d);
+                }
+              }
+            }
+            sXP[e] = ph;
+          } else {
+            sXC[e] = (T)f;
+          }
+        }
+        __syncthreads();
+      }
+      const C* vr = srow + (long long)rho * dim;
+      const bool need_s = P.has_dphase || P.diag_mode != DIAG_NONE;
+      const unsigned* __restrict__ cstr = P.col_strings;
+      constexpr int U = 4;  // elements per thread per step: their global loads overlap
+      for (int j0 = tid; j0 < dim; j0 += U * nth) {
+        unsigned sv[U];
+        C cp[U];
+        T cz[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int j = j0 + u * nth;
+          sv[u] = 0;
+          cz[u] = (T)0;
+          cp[u] = cmake<C>(1.0, 0.0);
+          if (j < dim) {
+            if (need_s) sv[u] = __ldg(cstr + j);
+            if (P.diag_mode == DIAG_PHASE && colP) cp[u] = colP[j];
+            if (P.diag_mode == DIAG_COEF && colZ) cz[u] = colZ[j];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int j = j0 + u * nth;
+          if (j >= dim) break;
+          C v = vr[j];
+          const unsigned s = sv[u];
+          if (sep_dphase) {
+            for (int c = 0; c < dch; ++c) v = cmul(v, sDT[(c << 4) + ((s >> (c * 4)) & 15u)]);
+          }
+          T z = (T)1;
+          if (P.diag_mode == DIAG_PHASE) {
+            C f = cp[u];
+            for (int c = 0; c < nch; ++c) f = cmul(f, sXP[(c << cb) + ((s >> (c * cb)) & cmask)]);
+            v = cmul(v, f);
+          } else if (P.diag_mode == DIAG_COEF) {
+            z = cz[u];
+            for (int c = 0; c < nch; ++c) z += sXC[(c << cb) + ((s >> (c * cb)) & cmask)];
+            if (P.out_op != OUT_EXPECT) {
+              v.x *= z;
+              v.y *= z;
+            }
+          }
+          if (P.out_op == OUT_EXPECT) {
+            const T w = (v.x * v.x + v.y * v.y) * z;
+            if constexpr (sizeof(T) == 4) {
+              const float y = (float)w - comp_f;
+              const float t = acc_f + y;
+              comp_f = (t - acc_f) - y;
+              acc_f = t;
+            } else {
+              acc_d += (double)w;
+            }
+          } else if (P.out_op != OUT_NONE) {
+            const long long o = (P.layout == LAYOUT_SAME) ? r * (long long)dim + j : (long long)j * P.n_rows + r;
+            if (P.out_op == OUT_STORE) {
+              out[o] = v;
+            } else {
+              C a = out[o];
+              a.x += P.alpha_re * v.x - P.alpha_im * v.y;
+              a.y += P.alpha_re * v.y + P.alpha_im * v.x;
+              out[o] = a;
+            }
+          }
         }
       }
-      __syncthreads();
-      rowconst = 0;
+      if (P.diag_mode != DIAG_NONE) __syncthreads();
     }
-    const C* vr = srow + (long long)rho * dim;
-    for (int j = tid; j < dim; j += nth) {
-      C v = vr[j];
-      unsigned s = 0;
-      if (P.has_dphase || P.diag_mode != DIAG_NONE) s = P.col_strings[j];
-      if (sep_dphase) {
-        for (int c = 0; c < nch; ++c) v = cmul(v, sDT[(c << cb) + ((s >> (c * cb)) & cmask)]);
-      }
-      T z = (T)1;
-      if (P.diag_mode == DIAG_PHASE) {
-        C f = colP ? colP[j] : cmake<C>(1.0, 0.0);
-        for (int c = 0; c < nch; ++c) f = cmul(f, sXP[(c << cb) + ((s >> (c * cb)) & cmask)]);
-        v = cmul(v, f);
-      } else if (P.diag_mode == DIAG_COEF) {
-        z = colZ ? colZ[j] : (T)0;
-        for (int c = 0; c < nch; ++c) z += sXC[(c << cb) + ((s >> (c * cb)) & cmask)];
-        z += rowconst;
-        if (P.out_op != OUT_EXPECT) {
-          v.x *= z;
-          v.y *= z;
-        }
-      }
-      if (P.out_op == OUT_EXPECT) {
-        const T w = (v.x * v.x + v.y * v.y) * z;
-        if constexpr (sizeof(T) == 4) {
-          const float y = (float)w - comp_f;
-          const float t = acc_f + y;
-          comp_f = (t - acc_f) - y;
-          acc_f = t;
-        } else {
-          acc_d += (double)w;
-        }
-      } else if (P.out_op != OUT_NONE) {
-        const long long o = (P.layout == LAYOUT_SAME) ? r * (long long)dim + j : (long long)j * P.n_rows + r;
-        if (P.out_op == OUT_STORE) {
-          out[o] = v;
-        } else {
-          C a = out[o];
-          a.x += P.alpha_re * v.x - P.alpha_im * v.y;
-          a.y += P.alpha_re * v.y + P.alpha_im * v.x;
-          out[o] = a;
-        }
-      }
+    if constexpr (sizeof(T) == 4) {
+      // fold the FP32 partial into FP64 once per chunk
+      acc_d += (double)acc_f - (double)comp_f;
+      acc_f = 0.f;
+      comp_f = 0.f;
     }
-    if (P.diag_mode != DIAG_NONE) __syncthreads();
+    __syncthreads();  // the next chunk overwrites the staged rows
   }
 
   if (P.out_op == OUT_EXPECT) {
-    double a = (sizeof(T) == 4) ? (double)acc_f - (double)comp_f : acc_d;
+    double a = acc_d;
     for (int off = 16; off > 0; off >>= 1) a += __shfl_down_sync(0xffffffffu, a, off);
     if ((tid & 31) == 0) sRed[tid >> 5] = a;
     __syncthreads();
