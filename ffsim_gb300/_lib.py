@@ -61,6 +61,8 @@ SIGNATURES = {
                                      _dp, _c_void_p, _c_size_t, _c_void_p],
     "ffgb_contract_diag_coulomb": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _dp,
                                    _dp, _c_int, _c_int, _c_void_p],
+    "ffgb_contract_diag_coulomb_static": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp,
+                                          _dp, _dp, _c_int, _c_int, _c_void_p],
     "ffgb_contract_num_op_sum": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _c_int,
                                  _c_void_p],
     "ffgb_rotated_diag_matvec": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _dp,

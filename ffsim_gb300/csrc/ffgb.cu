@@ -192,6 +192,9 @@ struct PassArgs {
   bool comp = false;           // compensated window coefficients (complex64)
   double* partials = nullptr;  // EXPECT
   int* n_ctas = nullptr;
+  // occupation strings supplied by the caller (null: the shared per-shape cache)
+  const unsigned* col_strings = nullptr;
+  const unsigned* row_strings = nullptr;
 };
 
 template <typename T>
@@ -313,13 +316,13 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
   P->chunk_bits = (diag_mode == DIAG_COEF && norb > 8) ? 8 : 4;
   const bool need_col = P->has_dphase || diag_mode != DIAG_NONE;
   if (need_col) {
-    const unsigned* cs = nullptr;
-    FFGB_TRY(device_strings(norb, A.rot_nocc, &cs));
+    const unsigned* cs = A.col_strings;
+    if (!cs) FFGB_TRY(device_strings(norb, A.rot_nocc, &cs));
     P->col_strings = cs;
   }
   if (diag_mode != DIAG_NONE) {
-    const unsigned* rs = nullptr;
-    FFGB_TRY(device_strings(norb, A.row_nocc, &rs));
+    const unsigned* rs = A.row_strings;
+    if (!rs) FFGB_TRY(device_strings(norb, A.row_nocc, &rs));
     P->row_strings = rs;
     P->row_norb = norb;
     P->row_nocc = A.row_nocc;
@@ -882,6 +885,89 @@ static int df_expectation_impl(const void* vec, int norb, int na, int nb, const 
   return FFGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// allocation-free contraction: scratch in a fixed device array
+// ---------------------------------------------------------------------------
+// Every byte read from this array is written earlier in the same call, so it
+// never needs clearing.  One array per device: calls that overlap in time on
+// one device (other streams, other host threads) share it and race.
+static __device__ __align__(256) unsigned char g_static_scratch[FFGB_STATIC_SCRATCH_BYTES];
+
+// Occupation string of every colex rank (ascending bit patterns with nocc bits).
+static __global__ void colex_strings_kernel(unsigned* __restrict__ out, int dim, int norb, int nocc) {
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t0 >= dim) return;
+  int t = t0, k = nocc;
+  unsigned s = 0;
+  for (int p = norb - 1; p >= 0 && k > 0; --p) {
+    long long c = 1;  // C(p, k)
+    if (k > p) {
+      c = 0;
+    } else {
+      for (int i = 1; i <= k; ++i) c = c * (p - k + i) / i;
+    }
+    if (t >= c) {
+      s |= 1u << p;
+      t -= (int)c;
+      --k;
+    }
+  }
+  out[t0] = s;
+}
+
+static std::mutex g_static_mu;
+static void* g_static_ptr[64] = {};
+
+// Device address of g_static_scratch on the current device, looked up once per device.
+static int static_scratch(void** out) {
+  int dev = 0;
+  FFGB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(FFGB_ERR_UNSUPPORTED, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_ptr[dev]) FFGB_CUDA(cudaGetSymbolAddress(&g_static_ptr[dev], g_static_scratch));
+  *out = g_static_ptr[dev];
+  return FFGB_OK;
+}
+
+static size_t round256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+template <typename T>
+static int contract_static_impl(const void* vec, void* out, int norb, int na, int nb, const DiagSpec& spec,
+                                int accumulate, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  const size_t need = round256((size_t)da * 4) + round256((size_t)db * 4) + round256((size_t)db * sizeof(C)) +
+                      round256(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
+  if (need > FFGB_STATIC_SCRATCH_BYTES)
+    return fail(FFGB_ERR_ARG, "this shape needs " + std::to_string(need) + " bytes of scratch; the fixed scratch of "
+                                  "ffgb_contract_diag_coulomb_static holds " +
+                                  std::to_string((size_t)FFGB_STATIC_SCRATCH_BYTES) +
+                                  " (use ffgb_contract_diag_coulomb)");
+  if (da <= 0 || db <= 0) return FFGB_OK;
+  void* base = nullptr;
+  FFGB_TRY(static_scratch(&base));
+  Scratch scr(base, FFGB_STATIC_SCRATCH_BYTES);
+  unsigned* sa = (unsigned*)scr.take((size_t)da * 4);
+  unsigned* sb = (unsigned*)scr.take((size_t)db * 4);
+  colex_strings_kernel<<<(unsigned)((da + 255) / 256), 256, 0, st>>>(sa, (int)da, norb, na);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  colex_strings_kernel<<<(unsigned)((db + 255) / 256), 256, 0, st>>>(sb, (int)db, norb, nb);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  PassArgs<T> A;
+  A.norb = norb;
+  A.rot_nocc = nb;
+  A.row_nocc = na;
+  A.n_rows = da;
+  A.in = vec;
+  A.out = out;
+  A.out_op = accumulate ? OUT_ACCUM : OUT_STORE;
+  A.diag = &spec;
+  A.col_strings = sb;
+  A.row_strings = sa;
+  return run_pass<T>(A, scr, st);
+}
 
 // ===========================================================================
 // C ABI
@@ -1110,6 +1196,18 @@ int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, 
                         rotated_matvec_impl<double>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st));
   cudaFreeAsync(tmp, st);
   return s;
+}
+
+int ffgb_contract_diag_coulomb_static(const void* vec, void* out, int dtype, int norb, int na, int nb,
+                                      const double* aa, const double* ab, const double* bb, int zrep,
+                                      int accumulate, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "contraction needs a spinful system");
+  DiagSpec spec = diag_coulomb_spec(norb, aa, ab, bb, zrep, 1.0, DIAG_COEF);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype, contract_static_impl<float>(vec, out, norb, na, nb, spec, accumulate, st),
+                       contract_static_impl<double>(vec, out, norb, na, nb, spec, accumulate, st));
 }
 
 int ffgb_contract_num_op_sum(const void* vec, void* out, int dtype, int norb, int na, int nb,

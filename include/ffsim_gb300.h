@@ -151,6 +151,27 @@ int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, 
                                const double* mat_bb, int z_representation, int accumulate,
                                void* stream);
 
+/* Size of the fixed device scratch of ffgb_contract_diag_coulomb_static. */
+#define FFGB_STATIC_SCRATCH_BYTES (1u << 20)
+
+/* ffgb_contract_diag_coulomb without any device allocation.  No counterpart
+ * in the reference: it exists for callers that cannot allocate device memory
+ * (all of it is held by another allocator, or cudaMalloc/cudaFree would stall
+ * a latency-bound loop).  Same arguments and results as
+ * ffgb_contract_diag_coulomb.  Its scratch (occupation strings and a column
+ * table, 4*dim_a + (4 + element size)*dim_b bytes plus 3 KB, each part rounded
+ * up to 256 bytes) lives in one FFGB_STATIC_SCRATCH_BYTES array per device;
+ * larger shapes return FFGB_ERR_ARG with the byte counts.  Nothing in that
+ * array has to start at zero: the call writes every byte it reads.  Calls on
+ * one device that overlap in time (different streams or host threads) share
+ * the array and race: issue them on one stream or one at a time.  The first
+ * call on each device looks up the array's address (cudaGetSymbolAddress),
+ * so make it before any stream capture. */
+int ffgb_contract_diag_coulomb_static(const void* vec, void* out, int dtype, int norb, int n_alpha,
+                                      int n_beta, const double* mat_aa, const double* mat_ab,
+                                      const double* mat_bb, int z_representation, int accumulate,
+                                      void* stream);
+
 /* out (+)= sum_i lambda_i (n_ia + n_ib) vec.  Replaces
  * contract_num_op_sum_spin_into_buffer (src/contract/num_op_sum.rs:20-39)
  * and python/ffsim/contract/num_op_sum.py:27-72. */
