@@ -48,7 +48,8 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
     inc = ["-I", str(BUILD), "-I", str(CSRC)]
     flags = NVFLAGS + (extra_flags or [])
     units = [("ffgb.cu", "ffgb.o"), ("plan.cpp", "plan.o"), ("stages.cu", "stages.o")] + [
-        (f"inst_{i}.cu", f"inst_{i}.o") for i in range(5)]
+        (f"inst_{i}.cu", f"inst_{i}.o") for i in range(5)] + [
+        (f"stage_b{b}.cu", f"stage_b{b}.o") for b in range(4, 9)]
     cmds = [[nvcc, *ARCH, *flags, *inc, "-c", str(CSRC / src), "-o", str(BUILD / obj)]
             for src, obj in units]
     with ThreadPoolExecutor(max_workers=len(cmds)) as ex:

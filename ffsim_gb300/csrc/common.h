@@ -38,14 +38,37 @@ int launch_sector(const SectorParams<T>& P, long long n_chunks, int block, int s
 
 struct SectorPlan;
 
+// Fused expectation on the last stage of a stage-major rotation (see
+// StageExpect in stages.cuh): sum z(row, col) |psi|^2 into one FP64 partial
+// per CTA.  X[i][l] couples row orbital i with column orbital l.
+struct StageExpectArgs {
+  const float* zrow = nullptr;
+  const float* zcol = nullptr;
+  const unsigned* row_str = nullptr;
+  const unsigned* col_str = nullptr;
+  double* partials = nullptr;
+  long long partial_cap = 0;
+  float X[FFGB_MAXN][FFGB_MAXN] = {};
+  int zrep = 0;
+};
+
+struct StageOpts {
+  int mode = 2;             // window coefficients: 0 plain FP32, 1 compensated, 2 dithered
+  unsigned salt = 0;        // decorrelates the dithering of different rotations
+  const void* ph_in = nullptr;   // per-row phases before the network (complex64 per string)
+  const void* ph_out = nullptr;  // per-row phases after the network (the plan's orbital phases)
+  const StageExpectArgs* expect = nullptr;  // last stage reduces instead of storing
+  int* expect_ctas = nullptr;               // partials written by the fused expectation
+};
+
 // Stage-major complex64 rotation of the sector whose strings index the rows
 // of a row-major array (ld elements per row, ncols columns processed):
-// in -> out (in == out allowed).  ph_in / ph_out: optional per-row phase
-// tables (complex64, one per string) multiplied in before / after the
-// network; the plan's own orbital phases go in as ph_out.
+// in -> out (in == out allowed).
 int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long ld, long long ncols,
-                      const SectorPlan& plan, bool comp, const void* ph_in, const void* ph_out,
-                      cudaStream_t st);
+                      const SectorPlan& plan, const StageOpts& o, cudaStream_t st);
+
+// Upper bound of the partial sums written by a fused expectation over ncols columns.
+long long stage_expect_partials(int norb, long long ncols);
 template <typename T>
 int launch_transpose(const void* in, void* out, long long rows, long long cols, const void* row_ph,
                      const void* col_ph, cudaStream_t st);

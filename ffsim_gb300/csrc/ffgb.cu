@@ -107,7 +107,8 @@ struct Scratch {
 static size_t extras_bytes(int norb, int na, int nb) {
   long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;
   long long m = std::max<long long>(std::max(da, db), 1);
-  return (size_t)m * 16 + (size_t)m * 8 + (size_t)m * 32 + 16384;
+  return (size_t)m * 16 + (size_t)m * 8 + (size_t)m * 32 + (size_t)m * 8 +
+         (size_t)stage_expect_partials(norb, m) * 8 + 65536;
 }
 
 // ---------------------------------------------------------------------------
@@ -444,12 +445,31 @@ static int phase_table(const SectorPlan* p, int norb, int nocc, Scratch& scr, cu
   return FFGB_OK;
 }
 
+// Window-coefficient mode of the stage path: dithered FP32 rounding (unbiased
+// per column; see win_coef).
+constexpr int STAGE_MODE = 2;
+
+// One sector's stage-major rotation with its final orbital phases (ph_out) and
+// an optional fused expectation on the last stage.
+static int stage_sector(const void* in, void* out, int norb, int nocc, long long ld, long long ncols,
+                        const SectorPlan& p, const void* ph_out, unsigned salt, cudaStream_t st,
+                        const StageExpectArgs* ex = nullptr, int* ex_ctas = nullptr) {
+  StageOpts o;
+  o.mode = STAGE_MODE;
+  o.salt = salt;
+  o.ph_out = ph_out;
+  o.expect = ex;
+  o.expect_ctas = ex_ctas;
+  return stage_rotate_rows(in, out, norb, nocc, ld, ncols, p, o, st);
+}
+
 // W(pa) (x) W(pb) of the state `in` (alpha rows), through `x` (same shape) and
 // `tmp` (beta rows).  keep_t = false: the result is in x with alpha rows;
 // keep_t = true: the result is in tmp with beta rows.  phases = false leaves
 // out the plans' final orbital phases (they do not change |amplitude|^2).
+// `salt` decorrelates the coefficient dithering of different rotations.
 static int staged_rotate(const void* in, void* x, void* tmp, int norb, int na, int nb,
-                         const SectorPlan* pa, const SectorPlan* pb, bool phases, bool comp, bool keep_t,
+                         const SectorPlan* pa, const SectorPlan* pb, bool phases, bool keep_t, unsigned salt,
                          Scratch& scr, cudaStream_t st) {
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
   const void *fa = nullptr, *fb = nullptr;
@@ -457,13 +477,13 @@ static int staged_rotate(const void* in, void* x, void* tmp, int norb, int na, i
     FFGB_TRY(phase_table(pa, norb, na, scr, st, &fa));
     FFGB_TRY(phase_table(pb, norb, nb, scr, st, &fb));
   }
-  if (pa) FFGB_TRY(stage_rotate_rows(in, x, norb, na, db, db, *pa, comp, nullptr, fa, st));
+  if (pa) FFGB_TRY(stage_sector(in, x, norb, na, db, db, *pa, fa, 2 * salt, st));
   if (!pb && !keep_t) {
     if (!pa && in != x) FFGB_CUDA(cudaMemcpyAsync(x, in, (size_t)(da * db) * sizeof(float2), cudaMemcpyDeviceToDevice, st));
     return FFGB_OK;
   }
   FFGB_TRY(launch_transpose<float>(pa ? x : in, tmp, da, db, nullptr, nullptr, st));
-  if (pb) FFGB_TRY(stage_rotate_rows(tmp, tmp, norb, nb, da, da, *pb, comp, nullptr, fb, st));
+  if (pb) FFGB_TRY(stage_sector(tmp, tmp, norb, nb, da, da, *pb, fb, 2 * salt + 1, st));
   if (!keep_t) FFGB_TRY(launch_transpose<float>(tmp, x, db, da, nullptr, nullptr, st));
   return FFGB_OK;
 }
@@ -564,7 +584,7 @@ static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const doub
   void* tmp = scr.take(S);
   if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
   if (staged<T>(&pa, mb ? &pb : nullptr))
-    return staged_rotate(vec, vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, true, false, false, scr, st);
+    return staged_rotate(vec, vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, true, false, 1, scr, st);
   return rotate_both<T>(vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, nullptr, scr, st);
 }
 
@@ -632,15 +652,15 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
   const SectorPlan *sad = rot_a ? &pad : nullptr, *sbd = rot_b ? &pbd : nullptr;
   if (staged<T>(sad, sbd)) {
     // W(U) D W(U)^dag: rotate into the beta-row layout, diagonal, beta back, alpha back
-    FFGB_TRY(staged_rotate(vec, vec, tmp, norb, na, nb, sad, sbd, true, false, true, scr, st));
+    FFGB_TRY(staged_rotate(vec, vec, tmp, norb, na, nb, sad, sbd, true, true, 2, scr, st));
     FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
     const long long db = binom_h(norb, nb);
     const void *fa = nullptr, *fb = nullptr;
     FFGB_TRY(phase_table(rot_a ? &pau : nullptr, norb, na, scr, st, &fa));
     FFGB_TRY(phase_table(rot_b ? &pbu : nullptr, norb, nb, scr, st, &fb));
-    if (rot_b) FFGB_TRY(stage_rotate_rows(tmp, tmp, norb, nb, da, da, pbu, false, nullptr, fb, st));
+    if (rot_b) FFGB_TRY(stage_sector(tmp, tmp, norb, nb, da, da, pbu, fb, 7, st));
     FFGB_TRY(launch_transpose<float>(tmp, vec, db, da, nullptr, nullptr, st));
-    if (rot_a) FFGB_TRY(stage_rotate_rows(vec, vec, norb, na, db, db, pau, false, nullptr, fa, st));
+    if (rot_a) FFGB_TRY(stage_sector(vec, vec, norb, na, db, db, pau, fa, 6, st));
     return FFGB_OK;
   }
   FFGB_TRY(rotate_both<T>(vec, tmp, norb, na, nb, rot_a ? &pad : nullptr, rot_b ? &pbd : nullptr,
@@ -676,15 +696,15 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
   void* t2 = scr.take(S);
   if (!t1 || !t2) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
   if (staged<T>(&pd, &pu)) {
-    FFGB_TRY(staged_rotate(vec, t1, t2, norb, na, nb, &pd, &pd, true, false, true, scr, st));
+    FFGB_TRY(staged_rotate(vec, t1, t2, norb, na, nb, &pd, &pd, true, true, 4, scr, st));
     FFGB_TRY(diag_pass_t<T>(t2, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
     const void *fa = nullptr, *fb = nullptr;
     FFGB_TRY(phase_table(&pu, norb, na, scr, st, &fa));
     FFGB_TRY(phase_table(&pu, norb, nb, scr, st, &fb));
-    FFGB_TRY(stage_rotate_rows(t2, t2, norb, nb, da, da, pu, false, nullptr, fb, st));
+    FFGB_TRY(stage_sector(t2, t2, norb, nb, da, da, pu, fb, 11, st));
     FFGB_TRY(launch_transpose<float>(t2, t1, db, da, nullptr, nullptr, st));
-    if (!accumulate) return stage_rotate_rows(t1, out, norb, na, db, db, pu, false, nullptr, fa, st);
-    FFGB_TRY(stage_rotate_rows(t1, t1, norb, na, db, db, pu, false, nullptr, fa, st));
+    if (!accumulate) return stage_sector(t1, out, norb, na, db, db, pu, fa, 10, st);
+    FFGB_TRY(stage_sector(t1, t1, norb, na, db, db, pu, fa, 10, st));
     return launch_axpy<float>(t1, out, da * db, 1.0, st);
   }
   PassArgs<T> A;
@@ -719,23 +739,62 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
   return run_pass<T>(B, scr, st);
 }
 
+// Tables of the fused expectation for a state held with beta rows (rows =
+// beta strings, columns = alpha strings); `spec` is written with alpha rows.
+static int expect_tables(int norb, int na, int nb, const DiagSpec& spec, Scratch& scr, cudaStream_t st,
+                         StageExpectArgs& ex) {
+  const DiagSpec dt = spec.transposed();
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  const unsigned *sa = nullptr, *sb = nullptr;
+  FFGB_TRY(device_strings(norb, na, &sa));
+  FFGB_TRY(device_strings(norb, nb, &sb));
+  float* zrow = (float*)scr.take(sizeof(float) * (size_t)db);
+  float* zcol = (float*)scr.take(sizeof(float) * (size_t)da);
+  double* same = (double*)scr.take(2 * sizeof(double) * FFGB_MAXN * FFGB_MAXN);
+  if (!zrow || !zcol || !same) return fail(FFGB_ERR_OOM, "scratch too small for the expectation tables");
+  FFGB_CUDA(cudaMemcpyAsync(same, dt.row_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN, cudaMemcpyHostToDevice, st));
+  FFGB_CUDA(cudaMemcpyAsync(same + FFGB_MAXN * FFGB_MAXN, dt.col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN,
+                            cudaMemcpyHostToDevice, st));
+  col_table_kernel<float><<<(unsigned)((db + 255) / 256), 256, 0, st>>>(sb, (int)db, norb, dt.zrep, DIAG_COEF,
+                                                                         same, zrow);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  col_table_kernel<float><<<(unsigned)((da + 255) / 256), 256, 0, st>>>(
+      sa, (int)da, norb, dt.zrep, DIAG_COEF, same + FFGB_MAXN * FFGB_MAXN, zcol);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  ex.zrow = zrow;
+  ex.zcol = zcol;
+  ex.row_str = sb;
+  ex.col_str = sa;
+  ex.zrep = dt.zrep;
+  for (int i = 0; i < FFGB_MAXN; ++i)
+    for (int l = 0; l < FFGB_MAXN; ++l) ex.X[i][l] = (float)dt.cross[i][l];
+  return FFGB_OK;
+}
+
 // <vec| W(V)^dag... : sum z |W(V) vec|^2 into dslot (device double)
 template <typename T>
 static int expectation_term(const void* vec, int norb, int na, int nb, const DiagSpec& spec,
-                            const std::vector<cd>& V, void* tmp, void* tmp2, double* dslot, Scratch& scr,
-                            cudaStream_t st) {
+                            const std::vector<cd>& V, void* tmp, void* tmp2, double* dslot, unsigned salt,
+                            Scratch& scr, cudaStream_t st) {
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
   SectorPlan pv;
   FFGB_TRY(make_plan<T>(norb, V, pv));
   const size_t mark = scr.off;
   if (tmp2 && staged<T>(&pv, &pv)) {
-    // coherent coefficient rounding would bias every term: compensated coefficients
-    FFGB_TRY(staged_rotate(vec, tmp, tmp2, norb, na, nb, &pv, &pv, false, true, true, scr, st));
-    double* partials = (double*)scr.take(sizeof(double) * (size_t)std::max<long long>(db, 1));
-    if (!partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
+    // alpha stages into tmp, transpose to beta rows, beta stages with the
+    // expectation fused into the last one (no phases: |psi|^2 does not see them)
+    FFGB_TRY(stage_sector(vec, tmp, norb, na, db, db, pv, nullptr, 2 * salt, st));
+    FFGB_TRY(launch_transpose<float>(tmp, tmp2, da, db, nullptr, nullptr, st));
+    StageExpectArgs ex;
+    FFGB_TRY(expect_tables(norb, na, nb, spec, scr, st, ex));
+    ex.partial_cap = stage_expect_partials(norb, da);
+    ex.partials = (double*)scr.take(sizeof(double) * (size_t)ex.partial_cap);
+    if (!ex.partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
     int nct = 0;
-    FFGB_TRY(diag_pass_t<T>(tmp2, norb, na, nb, spec, OUT_EXPECT, partials, &nct, scr, st));
-    reduce_partials_kernel<<<1, 256, 0, st>>>(partials, nct, dslot, 0);
+    FFGB_TRY(stage_sector(tmp2, tmp2, norb, nb, da, da, pv, nullptr, 2 * salt + 1, st, &ex, &nct));
+    reduce_partials_kernel<<<1, 256, 0, st>>>(ex.partials, nct, dslot, 0);
     count_launch();
     FFGB_CUDA(cudaGetLastError());
     scr.off = mark;
@@ -780,10 +839,10 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
 // coefficients in complex64.
 template <typename T>
 static int ucj_layer(void* x, void* tmp, int norb, int na, int nb, const SectorPlan& p, const DiagSpec* spec,
-                     Scratch& scr, cudaStream_t st) {
+                     unsigned salt, Scratch& scr, cudaStream_t st) {
   if (staged<T>(&p, &p)) {
     const size_t mark = scr.off;
-    FFGB_TRY(staged_rotate(x, x, tmp, norb, na, nb, &p, &p, true, true, spec != nullptr, scr, st));
+    FFGB_TRY(staged_rotate(x, x, tmp, norb, na, nb, &p, &p, true, spec != nullptr, salt, scr, st));
     if (spec) {
       FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, *spec, OUT_STORE, nullptr, nullptr, scr, st));
       FFGB_TRY(launch_transpose<float>(tmp, x, binom_h(norb, nb), binom_h(norb, na), nullptr, nullptr, st));
@@ -873,7 +932,8 @@ static int df_expectation_impl(const void* vec, int norb, int na, int nb, const 
   for (size_t k = 0; k < terms.size(); ++k) {
     std::vector<cd> V = dagger(terms[k].rot, norb);
     if (pre) V = matmul(V, *pre, norb);
-    FFGB_TRY(expectation_term<T>(vec, norb, na, nb, terms[k].spec, V, tmp, tmp2, slots + k, scr, st));
+    FFGB_TRY(expectation_term<T>(vec, norb, na, nb, terms[k].spec, V, tmp, tmp2, slots + k,
+                                 100u + (unsigned)k, scr, st));
   }
   std::vector<double> h(terms.size() + 1, 0.0);
   if (!terms.empty())
@@ -1163,8 +1223,8 @@ int ffgb_ucj_spin_balanced_apply(void* vec, int dtype, int norb, int na, int nb,
     SectorPlan p;
     int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
     if (s) return s;
-    s = dtype == FFGB_C64 ? ucj_layer<float>(vec, tmp, norb, na, nb, p, &spec, scr, st)
-                          : ucj_layer<double>(vec, tmp, norb, na, nb, p, &spec, scr, st);
+    s = dtype == FFGB_C64 ? ucj_layer<float>(vec, tmp, norb, na, nb, p, &spec, 20u + (unsigned)k, scr, st)
+                          : ucj_layer<double>(vec, tmp, norb, na, nb, p, &spec, 0, scr, st);
     if (s) return s;
     current = U;
   }
@@ -1172,8 +1232,8 @@ int ffgb_ucj_spin_balanced_apply(void* vec, int dtype, int norb, int na, int nb,
   SectorPlan p;
   int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
   if (s) return s;
-  return dtype == FFGB_C64 ? ucj_layer<float>(vec, tmp, norb, na, nb, p, nullptr, scr, st)
-                           : ucj_layer<double>(vec, tmp, norb, na, nb, p, nullptr, scr, st);
+  return dtype == FFGB_C64 ? ucj_layer<float>(vec, tmp, norb, na, nb, p, nullptr, 19u, scr, st)
+                           : ucj_layer<double>(vec, tmp, norb, na, nb, p, nullptr, 0, scr, st);
 }
 
 int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, int na, int nb,
@@ -1328,8 +1388,8 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
     SectorPlan p;
     int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
     if (s) return s;
-    s = dtype == FFGB_C64 ? ucj_layer<float>(work, tmp, norb, na, nb, p, &spec, scr, st)
-                          : ucj_layer<double>(work, tmp, norb, na, nb, p, &spec, scr, st);
+    s = dtype == FFGB_C64 ? ucj_layer<float>(work, tmp, norb, na, nb, p, &spec, 20u + (unsigned)k, scr, st)
+                          : ucj_layer<double>(work, tmp, norb, na, nb, p, &spec, 0, scr, st);
     if (s) return s;
     current = U;
   }

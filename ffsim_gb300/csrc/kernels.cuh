@@ -233,6 +233,52 @@ __device__ __forceinline__ void rot_pair(float2& x, float2& y, float c, float sr
   y = ny;
 }
 
+// Coefficients (c, Re s, Im s) of rotation g of a window network.
+//   MODE 0: FP32 values gp.
+//   MODE 1: FP32 values gp plus FP32 residuals gl (compensated, see rot_pair).
+//   MODE 2: dithered rounding.  gp / gl hold the two FP32 neighbours below /
+//           above each FP64 coefficient and gt the probability of the upper
+//           one as a 32-bit threshold.  Every thread draws its own choice from
+//           its generator `rng`, so each column sees an unbiased rounding of
+//           the plan and the rounding errors of different columns are
+//           independent instead of identical.
+template <int MODE>
+__device__ __forceinline__ void win_coef(const float* __restrict__ gp, const float* __restrict__ gl,
+                                         const unsigned* __restrict__ gt, int g, unsigned& rng, float& c,
+                                         float& sr, float& si, float& cl, float& srl, float& sil) {
+  if constexpr (MODE == 2) {
+    float v[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      rng = rng * 1664525u + 1013904223u;
+      v[q] = rng < gt[3 * g + q] ? gl[3 * g + q] : gp[3 * g + q];
+    }
+    c = v[0];
+    sr = v[1];
+    si = v[2];
+    cl = srl = sil = 0.f;
+  } else {
+    c = gp[3 * g];
+    sr = gp[3 * g + 1];
+    si = gp[3 * g + 2];
+    cl = MODE == 1 ? gl[3 * g] : 0.f;
+    srl = MODE == 1 ? gl[3 * g + 1] : 0.f;
+    sil = MODE == 1 ? gl[3 * g + 2] : 0.f;
+  }
+}
+
+// Start of a thread's generator for dithered coefficients (a hash of the
+// column and the stage's salt).
+__device__ __forceinline__ unsigned dither_seed(unsigned long long col, unsigned salt) {
+  unsigned x = (unsigned)col * 0x9E3779B9u ^ (unsigned)(col >> 32) ^ salt;
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
 }  // namespace ffgb
 
 namespace ffgb {

@@ -1,0 +1,6 @@
+// Window stage kernels for 6-orbital windows (split for parallel builds).
+#include "stage_launch.cuh"
+
+namespace ffgb {
+template int launch_win_stage<6>(const WinStageParams&, int, int, bool, cudaStream_t);
+}  // namespace ffgb

@@ -1,5 +1,6 @@
 // Host side of the stage-major complex64 path (see stages.cuh).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -12,6 +13,9 @@
 #include "stages.cuh"
 
 namespace ffgb {
+
+template <int B>
+int launch_win_stage(const WinStageParams& P, int grid, int mode, bool expect, cudaStream_t st);
 
 namespace {
 
@@ -51,6 +55,12 @@ long long rank_shifted(unsigned s, int base, int m0) {
   return r;
 }
 
+int popcount(unsigned x) {
+  int c = 0;
+  for (; x; x &= x - 1) ++c;
+  return c;
+}
+
 // Half-sector rank tables of a sector (norb, nocc) split at h: for every
 // subset s2 of the q = norb - h high orbitals with m bits (colex index g),
 // rt[moff[m] + g] = rank contribution of s2 above a low part of nocc - m electrons.
@@ -74,79 +84,165 @@ HalfTables half_tables(int norb, int nocc, int h) {
   return t;
 }
 
-struct CsTables {
-  std::vector<int*> pairs;  // device, per site
-  std::vector<int> counts;
+// Coefficient tables of one rotation list for win_coef<mode>.
+void put_coefs(const double* v, int n, int mode, float* gp, float* gl, unsigned* gt) {
+  for (int i = 0; i < n; ++i) {
+    const double x = v[i];
+    if (mode == 2) {
+      float dn = (float)x;
+      if ((double)dn > x) dn = std::nextafter(dn, -INFINITY);
+      const float up = std::nextafter(dn, INFINITY);
+      const double p = (x - (double)dn) / ((double)up - (double)dn);
+      gp[i] = dn;
+      gl[i] = up;
+      gt[i] = (unsigned)std::min(4294967295.0, std::max(0.0, std::floor(p * 4294967296.0 + 0.5)));
+    } else {
+      gp[i] = (float)x;
+      gl[i] = (float)(x - (double)(float)x);
+      gt[i] = 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fused cross-half tables
+// ---------------------------------------------------------------------------
+struct CsPass {
+  int* tab = nullptr;  // device
+  int n_classes = 0;
+  int cls_m[5] = {}, cls_groups[5] = {}, cls_base[5] = {};
 };
 
 std::mutex g_cs_mu;
-std::map<std::tuple<int, int, int, int>, CsTables> g_cs;
+std::map<std::tuple<int, int, int, int, int, int>, CsPass> g_cs;
 
-// Pair tables of the cross-half rotations (i, h + i) of a sector: every string
-// with i occupied and h + i empty, its partner, and the parity of the occupied
-// orbitals strictly between i and h + i.
-int cs_tables(int norb, int nocc, int h, const CsTables** out) {
+// Groups of the sector (norb, nocc) under the cross-half sites [s0, s1).
+int cs_pass_tables(int norb, int nocc, int h, int s0, int s1, const CsPass** out) {
   int dev = 0;
   FFGB_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_cs_mu);
-  auto key = std::make_tuple(dev, norb, nocc, h);
+  auto key = std::make_tuple(dev, norb, nocc, h, s0, s1);
   auto it = g_cs.find(key);
   if (it != g_cs.end()) {
     *out = &it->second;
     return FFGB_OK;
   }
-  CsTables t;
   const long long dim = C(norb, nocc);
-  for (int i = 0; i < h; ++i) {
-    const int j = h + i;
-    const unsigned between = ((1u << j) - 1u) & ~((1u << (i + 1)) - 1u);
-    std::vector<int> host;
-    for (long long a = 0; a < dim; ++a) {
-      const unsigned s = unrank(a, norb, nocc);
-      if (!((s >> i) & 1u) || ((s >> j) & 1u)) continue;
-      const unsigned y = s ^ (1u << i) ^ (1u << j);
-      const int sign = __builtin_popcount(s & between) & 1;
-      host.push_back((int)a | (sign ? (int)0x80000000u : 0));
-      host.push_back((int)rank(y));
+  std::vector<std::vector<int>> per_m(5);
+  std::vector<int> counts(5, 0);
+  for (long long a = 0; a < dim; ++a) {
+    const unsigned s = unrank(a, norb, nocc);
+    int act[4], m = 0;
+    bool canonical = true;
+    for (int i = s0; i < s1; ++i) {
+      const bool lo = (s >> i) & 1u, hi = (s >> (h + i)) & 1u;
+      if (lo != hi) {
+        act[m++] = i;
+        if (hi) canonical = false;  // the group is emitted from its all-low member
+      }
     }
-    int* d = nullptr;
-    const size_t bytes = std::max<size_t>(host.size(), 2) * sizeof(int);
-    FFGB_CUDA(cudaMalloc(&d, bytes));
-    if (!host.empty()) FFGB_CUDA(cudaMemcpy(d, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice));
-    t.pairs.push_back(d);
-    t.counts.push_back((int)(host.size() / 2));
+    if (m == 0 || !canonical) continue;
+    std::vector<int>& T = per_m[m];
+    int header = 0;
+    for (int t = 0; t < m; ++t) header |= act[t] << (3 * t);
+    T.push_back(header);
+    for (int j = 0; j < (1 << m); ++j) {
+      unsigned mem = s;
+      for (int t = 0; t < m; ++t)
+        if ((j >> t) & 1) mem ^= (1u << act[t]) | (1u << (h + act[t]));
+      int sign = 0;
+      for (int t = 0; t < m; ++t) {
+        if ((j >> t) & 1) continue;
+        const int i = act[t], jj = h + act[t];
+        const unsigned between = ((1u << jj) - 1u) & ~((1u << (i + 1)) - 1u);
+        if (popcount(mem & between) & 1) sign |= 1 << t;
+      }
+      const long long r = rank(mem);
+      if (r >= (1 << 24)) return fail(FFGB_ERR_UNSUPPORTED, "sector too large for the cross-half tables");
+      T.push_back((int)r | (sign << 24));
+    }
+    ++counts[m];
   }
-  g_cs[key] = t;
+  CsPass P;
+  std::vector<int> host;
+  for (int m = 4; m >= 1; --m) {
+    if (counts[m] == 0) continue;
+    P.cls_m[P.n_classes] = m;
+    P.cls_groups[P.n_classes] = counts[m];
+    P.cls_base[P.n_classes] = (int)host.size();
+    host.insert(host.end(), per_m[m].begin(), per_m[m].end());
+    ++P.n_classes;
+  }
+  const size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(int);
+  FFGB_CUDA(cudaMalloc(&P.tab, bytes));
+  if (!host.empty()) FFGB_CUDA(cudaMemcpy(P.tab, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice));
+  g_cs[key] = P;
   *out = &g_cs[key];
   return FFGB_OK;
 }
 
-template <int B>
-int launch_win(const WinStageParams& P, int grid, cudaStream_t st) {
-  win_stage_kernel<B><<<grid, STAGE_THREADS, 0, st>>>(P);
-  count_launch();
-  FFGB_CUDA(cudaGetLastError());
+int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h, const std::vector<Pair2>& cs,
+             int mode, unsigned salt, cudaStream_t st) {
+  for (int s0 = 0; s0 < h; s0 += 4) {
+    const int s1 = std::min(h, s0 + 4);
+    const CsPass* T = nullptr;
+    FFGB_TRY(cs_pass_tables(norb, nocc, h, s0, s1, &T));
+    if (T->n_classes == 0) continue;
+    CsStageParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.x = x;
+    P.ld = ld;
+    P.ncols = ncols;
+    P.tab = T->tab;
+    P.n_classes = T->n_classes;
+    P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
+    P.salt = salt * 0x9E3779B9u + 0x51ED270Bu * (unsigned)(s0 + 1);
+    long long cta = 0;
+    for (int c = 0; c < T->n_classes; ++c) {
+      P.cls_m[c] = T->cls_m[c];
+      P.cls_base[c] = T->cls_base[c];
+      P.cls_cta0[c] = (int)cta;
+      cta += (long long)T->cls_groups[c] * P.tiles;
+    }
+    P.cls_cta0[T->n_classes] = (int)cta;
+    if (cta > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
+    double v[24] = {};
+    for (int i = 0; i < h && i < 8; ++i) {
+      v[3 * i] = cs[i].g00.real();
+      v[3 * i + 1] = cs[i].g01.real();
+      v[3 * i + 2] = cs[i].g01.imag();
+    }
+    put_coefs(v, 24, mode, P.gp, P.gl, P.gt);
+    if (cta == 0) continue;
+    if (mode == 0)
+      cs_stage_kernel<0><<<(unsigned)cta, STAGE_THREADS, 0, st>>>(P);
+    else if (mode == 1)
+      cs_stage_kernel<1><<<(unsigned)cta, STAGE_THREADS, 0, st>>>(P);
+    else
+      cs_stage_kernel<2><<<(unsigned)cta, STAGE_THREADS, 0, st>>>(P);
+    count_launch();
+    FFGB_CUDA(cudaGetLastError());
+  }
   return FFGB_OK;
 }
 
-int launch_win_b(int b, const WinStageParams& P, int grid, cudaStream_t st) {
+int launch_win_b(int b, const WinStageParams& P, int grid, int mode, bool expect, cudaStream_t st) {
   switch (b) {
-    case 4: return launch_win<4>(P, grid, st);
-    case 5: return launch_win<5>(P, grid, st);
-    case 6: return launch_win<6>(P, grid, st);
-    case 7: return launch_win<7>(P, grid, st);
-    case 8: return launch_win<8>(P, grid, st);
+    case 4: return launch_win_stage<4>(P, grid, mode, expect, st);
+    case 5: return launch_win_stage<5>(P, grid, mode, expect, st);
+    case 6: return launch_win_stage<6>(P, grid, mode, expect, st);
+    case 7: return launch_win_stage<7>(P, grid, mode, expect, st);
+    case 8: return launch_win_stage<8>(P, grid, mode, expect, st);
     default: return fail(FFGB_ERR_UNSUPPORTED, "window size outside [4, 8]");
   }
 }
 
-float lo32(double x) { return (float)(x - (double)(float)x); }
-
 // One window stage.  low: window [0, h) with groups = high-half patterns;
 // otherwise window [h, norb) with groups = low-half patterns.
 int window_stage(const float2* in, float2* out, long long ld, long long ncols, int norb, int nocc,
-                 const HalfTables& T, bool low, const std::vector<Givens>& net, bool comp,
-                 const float2* ph_in, const float2* ph_out, cudaStream_t st) {
+                 const HalfTables& T, bool low, const std::vector<Givens>& net, int mode, unsigned salt,
+                 const float2* ph_in, const float2* ph_out, const StageExpectArgs* ex, int* ex_ctas,
+                 cudaStream_t st) {
   const int h = T.h, q = T.q;
   const int b = low ? h : q;
   auto P = std::make_unique<WinStageParams>();
@@ -156,18 +252,19 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
   P->ld = ld;
   P->ncols = ncols;
   P->low = low ? 1 : 0;
-  P->comp = comp ? 1 : 0;
+  P->norb = norb;
+  P->lo = low ? 0 : h;
+  P->salt = salt;
   P->ph_in = ph_in;
   P->ph_out = ph_out;
-  for (int j = 0; j < 72; ++j) P->ident[j] = j;
+  std::vector<double> v(3 * net.size());
   for (size_t g = 0; g < net.size(); ++g) {
-    P->gp[3 * g] = (float)net[g].c;
-    P->gp[3 * g + 1] = (float)net[g].s.real();
-    P->gp[3 * g + 2] = (float)net[g].s.imag();
-    P->gl[3 * g] = lo32(net[g].c);
-    P->gl[3 * g + 1] = lo32(net[g].s.real());
-    P->gl[3 * g + 2] = lo32(net[g].s.imag());
+    v[3 * g] = net[g].c;
+    v[3 * g + 1] = net[g].s.real();
+    v[3 * g + 2] = net[g].s.imag();
   }
+  if (v.size() > 84) return fail(FFGB_ERR_UNSUPPORTED, "window network too long");
+  put_coefs(v.data(), (int)v.size(), mode, P->gp, P->gl, P->gt);
   P->tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
   // classes: k electrons inside the window
   const int kbeg = low ? std::max(0, nocc - q) : std::max(0, nocc - h);
@@ -175,79 +272,77 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
   std::vector<int> ks;
   for (int k = kbeg; k <= kend; ++k) ks.push_back(k);
   std::stable_sort(ks.begin(), ks.end(), [&](int a, int c) { return C(b, a) > C(b, c); });
-  int cta = 0, toff = 0;
+  long long cta = 0;
+  int toff = 0;
   P->n_classes = (int)ks.size();
   for (size_t ci = 0; ci < ks.size(); ++ci) {
     const int k = ks[ci];
     P->cls_k[ci] = k;
-    P->cls_cta0[ci] = cta;
+    P->cls_cta0[ci] = (int)cta;
     P->cls_off[ci] = toff;
     long long groups;
     if (low) {  // groups: high-half patterns with nocc - k electrons, base row = rt
       const int m = nocc - k;
       groups = C(q, m);
+      if (toff + groups > 256) return fail(FFGB_ERR_UNSUPPORTED, "window table overflow");
       for (long long g = 0; g < groups; ++g) P->tab[toff + g] = T.rt[T.moff[m] + g];
       toff += (int)groups;
     } else {  // groups: low-half patterns (row = colex rank), members at rt offsets
       groups = C(h, nocc - k);
+      if (toff + C(q, k) > 256) return fail(FFGB_ERR_UNSUPPORTED, "window table overflow");
       for (long long j = 0; j < C(q, k); ++j) P->tab[toff + j] = T.rt[T.moff[k] + j];
       toff += (int)C(q, k);
     }
-    if (toff > 256) return fail(FFGB_ERR_UNSUPPORTED, "window table overflow");
-    cta += (int)(groups * P->tiles);
+    cta += groups * P->tiles;
   }
-  P->cls_cta0[ks.size()] = cta;
+  P->cls_cta0[ks.size()] = (int)cta;
+  if (cta > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "window stage grid too large");
+  if (ex) {
+    if (cta > ex->partial_cap) return fail(FFGB_ERR_OOM, "partial-sum buffer too small");
+    StageExpect& E = P->ex;
+    E.zrow = ex->zrow;
+    E.zcol = ex->zcol;
+    E.row_str = ex->row_str;
+    E.col_str = ex->col_str;
+    E.partials = ex->partials;
+    E.zrep = ex->zrep;
+    for (int i = 0; i < FFGB_MAXN; ++i)
+      for (int l = 0; l < FFGB_MAXN; ++l) {
+        E.X[i][l] = ex->X[i][l];
+        E.Xsum[l] += ex->X[i][l];
+      }
+    if (ex_ctas) *ex_ctas = (int)cta;
+  }
   if (cta == 0) return FFGB_OK;
-  return launch_win_b(b, *P, cta, st);
-}
-
-int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h,
-             const std::vector<Pair2>& cs, bool comp, cudaStream_t st) {
-  const CsTables* T = nullptr;
-  FFGB_TRY(cs_tables(norb, nocc, h, &T));
-  for (size_t i = 0; i < cs.size(); ++i) {
-    const int n = T->counts[i];
-    if (n == 0) continue;
-    CsSiteParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.x = x;
-    P.ld = ld;
-    P.ncols = ncols;
-    P.pairs = T->pairs[i];
-    P.n_pairs = n;
-    P.ppc = 8;
-    P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
-    P.comp = comp ? 1 : 0;
-    const double v[8] = {cs[i].g00.real(), cs[i].g00.imag(), cs[i].g01.real(), cs[i].g01.imag(),
-                         cs[i].g10.real(), cs[i].g10.imag(), cs[i].g11.real(), cs[i].g11.imag()};
-    for (int q = 0; q < 8; ++q) {
-      P.g[q] = (float)v[q];
-      P.gl[q] = lo32(v[q]);
-    }
-    const long long grid = (long long)P.tiles * ((n + P.ppc - 1) / P.ppc);
-    cs_site_kernel<<<(int)grid, STAGE_THREADS, 0, st>>>(P);
-    count_launch();
-    FFGB_CUDA(cudaGetLastError());
-  }
-  return FFGB_OK;
+  return launch_win_b(b, *P, (int)cta, mode, ex != nullptr, st);
 }
 
 }  // namespace
 
+long long stage_expect_partials(int norb, long long ncols) {
+  const int h = norb / 2;
+  const long long groups = 1LL << std::max(h, norb - h);
+  return groups * ((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
+}
+
 int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long ld, long long ncols,
-                      const SectorPlan& plan, bool comp, const void* ph_in, const void* ph_out,
-                      cudaStream_t st) {
+                      const SectorPlan& plan, const StageOpts& o, cudaStream_t st) {
   if (plan.kind != PLAN_CSD) return fail(FFGB_ERR_ARG, "stage path needs a cosine-sine plan");
   if (plan.h < 4 || plan.h > 8 || norb - plan.h < 4 || norb - plan.h > 8)
     return fail(FFGB_ERR_UNSUPPORTED, "stage path needs half windows of 4 to 8 orbitals");
   const HalfTables T = half_tables(norb, nocc, plan.h);
   const float2* src = (const float2*)in;
   float2* dst = (float2*)out;
-  FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, comp, (const float2*)ph_in, nullptr, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.b2, comp, nullptr, nullptr, st));
-  FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, plan.h, plan.cs, comp, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, true, plan.a1, comp, nullptr, nullptr, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.a2, comp, nullptr, (const float2*)ph_out, st));
+  const unsigned s = o.salt * 0x2545F491u;
+  FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, o.mode, s + 1, (const float2*)o.ph_in,
+                        nullptr, nullptr, nullptr, st));
+  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.b2, o.mode, s + 2, nullptr, nullptr,
+                        nullptr, nullptr, st));
+  FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, plan.h, plan.cs, o.mode, s + 3, st));
+  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, true, plan.a1, o.mode, s + 4, nullptr, nullptr,
+                        nullptr, nullptr, st));
+  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.a2, o.mode, s + 5, nullptr,
+                        (const float2*)o.ph_out, o.expect, o.expect_ctas, st));
   return FFGB_OK;
 }
 
