@@ -40,6 +40,12 @@ def _run(cmd: list[str], verbose: bool) -> None:
         print(res.stdout + res.stderr, flush=True)
 
 
+# window-stage kernels: (window size, first class, last class) per translation
+# unit; the large classes of 7- and 8-orbital windows get units of their own
+STAGE_UNITS = [(4, 0, 4), (5, 0, 5), (6, 0, 6), (7, 0, 2), (7, 3, 3), (7, 4, 4), (7, 5, 7),
+               (8, 0, 2), (8, 3, 3), (8, 4, 4), (8, 5, 5), (8, 6, 8)]
+
+
 def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
     BUILD.mkdir(exist_ok=True)
     subprocess.run([sys.executable, str(CSRC / "gen_windows.py"), str(BUILD / "windows_gen.cuh")],
@@ -47,15 +53,16 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
     nvcc = _nvcc()
     inc = ["-I", str(BUILD), "-I", str(CSRC)]
     flags = NVFLAGS + (extra_flags or [])
-    units = [("ffgb.cu", "ffgb.o"), ("plan.cpp", "plan.o"), ("stages.cu", "stages.o")] + [
-        (f"inst_{i}.cu", f"inst_{i}.o") for i in range(5)] + [
-        (f"stage_b{b}.cu", f"stage_b{b}.o") for b in range(4, 9)]
-    cmds = [[nvcc, *ARCH, *flags, *inc, "-c", str(CSRC / src), "-o", str(BUILD / obj)]
-            for src, obj in units]
+    units = [("ffgb.cu", "ffgb.o", []), ("plan.cpp", "plan.o", []), ("stages.cu", "stages.o", [])] + [
+        (f"inst_{i}.cu", f"inst_{i}.o", []) for i in range(5)] + [
+        ("stage_inst.cu", f"stage_b{b}_k{k0}.o", [f"-DWIN_B={b}", f"-DWIN_K0={k0}", f"-DWIN_K1={k1}"])
+        for b, k0, k1 in STAGE_UNITS]
+    cmds = [[nvcc, *ARCH, *flags, *defs, *inc, "-c", str(CSRC / src), "-o", str(BUILD / obj)]
+            for src, obj, defs in units]
     with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
         list(ex.map(lambda c: _run(c, verbose), cmds))
     tmp = BUILD / "libffgb.so.tmp"
-    _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(BUILD / o) for _, o in units],
+    _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *[str(BUILD / o) for _, o, _ in units],
           "-lcudart"], verbose)
     os.replace(tmp, LIB)
     return LIB

@@ -55,8 +55,6 @@ struct StageExpectArgs {
 struct StageOpts {
   int mode = 2;             // window coefficients: 0 plain FP32, 1 compensated, 2 dithered
   unsigned salt = 0;        // decorrelates the dithering of different rotations
-  const void* ph_in = nullptr;   // per-row phases before the network (complex64 per string)
-  const void* ph_out = nullptr;  // per-row phases after the network (the plan's orbital phases)
   const StageExpectArgs* expect = nullptr;  // last stage reduces instead of storing
   int* expect_ctas = nullptr;               // partials written by the fused expectation
 };

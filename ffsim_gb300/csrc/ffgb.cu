@@ -449,15 +449,14 @@ static int phase_table(const SectorPlan* p, int norb, int nocc, Scratch& scr, cu
 // per column; see win_coef).
 constexpr int STAGE_MODE = 2;
 
-// One sector's stage-major rotation with its final orbital phases (ph_out) and
-// an optional fused expectation on the last stage.
+// One sector's stage-major rotation (without the plan's final orbital phases)
+// with an optional fused expectation on the last stage.
 static int stage_sector(const void* in, void* out, int norb, int nocc, long long ld, long long ncols,
-                        const SectorPlan& p, const void* ph_out, unsigned salt, cudaStream_t st,
-                        const StageExpectArgs* ex = nullptr, int* ex_ctas = nullptr) {
+                        const SectorPlan& p, unsigned salt, cudaStream_t st, const StageExpectArgs* ex = nullptr,
+                        int* ex_ctas = nullptr) {
   StageOpts o;
   o.mode = STAGE_MODE;
   o.salt = salt;
-  o.ph_out = ph_out;
   o.expect = ex;
   o.expect_ctas = ex_ctas;
   return stage_rotate_rows(in, out, norb, nocc, ld, ncols, p, o, st);
@@ -465,27 +464,44 @@ static int stage_sector(const void* in, void* out, int norb, int nocc, long long
 
 // W(pa) (x) W(pb) of the state `in` (alpha rows), through `x` (same shape) and
 // `tmp` (beta rows).  keep_t = false: the result is in x with alpha rows;
-// keep_t = true: the result is in tmp with beta rows.  phases = false leaves
-// out the plans' final orbital phases (they do not change |amplitude|^2).
-// `salt` decorrelates the coefficient dithering of different rotations.
+// keep_t = true: the result is in tmp with beta rows.  The plans' final
+// orbital phases ride on the transposes (rows of the source are the sector
+// just rotated).  With keep_t the beta phases are returned in *fb_pending for
+// the caller to apply (null: applied here); phases = false leaves them out
+// (they do not change |amplitude|^2).  `salt` decorrelates the coefficient
+// dithering of different rotations.
 static int staged_rotate(const void* in, void* x, void* tmp, int norb, int na, int nb,
                          const SectorPlan* pa, const SectorPlan* pb, bool phases, bool keep_t, unsigned salt,
-                         Scratch& scr, cudaStream_t st) {
+                         Scratch& scr, cudaStream_t st, const void** fb_pending = nullptr) {
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
   const void *fa = nullptr, *fb = nullptr;
   if (phases) {
     FFGB_TRY(phase_table(pa, norb, na, scr, st, &fa));
     FFGB_TRY(phase_table(pb, norb, nb, scr, st, &fb));
   }
-  if (pa) FFGB_TRY(stage_sector(in, x, norb, na, db, db, *pa, fa, 2 * salt, st));
+  if (fb_pending) *fb_pending = nullptr;
+  if (pa) FFGB_TRY(stage_sector(in, x, norb, na, db, db, *pa, 2 * salt, st));
   if (!pb && !keep_t) {
     if (!pa && in != x) FFGB_CUDA(cudaMemcpyAsync(x, in, (size_t)(da * db) * sizeof(float2), cudaMemcpyDeviceToDevice, st));
+    if (fa) FFGB_TRY(launch_row_scale<float>(x, da, db, fa, st));
     return FFGB_OK;
   }
-  FFGB_TRY(launch_transpose<float>(pa ? x : in, tmp, da, db, nullptr, nullptr, st));
-  if (pb) FFGB_TRY(stage_sector(tmp, tmp, norb, nb, da, da, *pb, fb, 2 * salt + 1, st));
-  if (!keep_t) FFGB_TRY(launch_transpose<float>(tmp, x, db, da, nullptr, nullptr, st));
-  return FFGB_OK;
+  FFGB_TRY(launch_transpose<float>(pa ? x : in, tmp, da, db, fa, nullptr, st));
+  if (pb) FFGB_TRY(stage_sector(tmp, tmp, norb, nb, da, da, *pb, 2 * salt + 1, st));
+  if (keep_t) {
+    if (fb_pending)
+      *fb_pending = fb;
+    else if (fb)
+      FFGB_TRY(launch_row_scale<float>(tmp, db, da, fb, st));
+    return FFGB_OK;
+  }
+  return launch_transpose<float>(tmp, x, db, da, fb, nullptr, st);
+}
+
+// Number-representation diagonal operators absorb orbital phases d_i of the
+// column (beta) sector: exp(i arg(d_i) n_i) = d_i^(n_i).
+static void fold_col_phases(DiagSpec& spec, const SectorPlan& p, int norb) {
+  for (int i = 0; i < norb; ++i) spec.col_same[i][i] += std::arg(p.diag[i]);
 }
 
 // Diagonal operator on a state held with beta rows (db rows of da columns):
@@ -652,15 +668,24 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
   const SectorPlan *sad = rot_a ? &pad : nullptr, *sbd = rot_b ? &pbd : nullptr;
   if (staged<T>(sad, sbd)) {
     // W(U) D W(U)^dag: rotate into the beta-row layout, diagonal, beta back, alpha back
-    FFGB_TRY(staged_rotate(vec, vec, tmp, norb, na, nb, sad, sbd, true, true, 2, scr, st));
-    FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
+    const void* fbp = nullptr;
+    FFGB_TRY(staged_rotate(vec, vec, tmp, norb, na, nb, sad, sbd, true, true, 2, scr, st, &fbp));
     const long long db = binom_h(norb, nb);
+    if (fbp && !spec.zrep) {
+      DiagSpec s2 = spec;
+      fold_col_phases(s2, pbd, norb);
+      FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, s2, OUT_STORE, nullptr, nullptr, scr, st));
+    } else {
+      if (fbp) FFGB_TRY(launch_row_scale<float>(tmp, db, da, fbp, st));
+      FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
+    }
     const void *fa = nullptr, *fb = nullptr;
     FFGB_TRY(phase_table(rot_a ? &pau : nullptr, norb, na, scr, st, &fa));
     FFGB_TRY(phase_table(rot_b ? &pbu : nullptr, norb, nb, scr, st, &fb));
-    if (rot_b) FFGB_TRY(stage_sector(tmp, tmp, norb, nb, da, da, pbu, fb, 7, st));
-    FFGB_TRY(launch_transpose<float>(tmp, vec, db, da, nullptr, nullptr, st));
-    if (rot_a) FFGB_TRY(stage_sector(vec, vec, norb, na, db, db, pau, fa, 6, st));
+    if (rot_b) FFGB_TRY(stage_sector(tmp, tmp, norb, nb, da, da, pbu, 7, st));
+    FFGB_TRY(launch_transpose<float>(tmp, vec, db, da, fb, nullptr, st));
+    if (rot_a) FFGB_TRY(stage_sector(vec, vec, norb, na, db, db, pau, 6, st));
+    if (fa) FFGB_TRY(launch_row_scale<float>(vec, da, db, fa, st));
     return FFGB_OK;
   }
   FFGB_TRY(rotate_both<T>(vec, tmp, norb, na, nb, rot_a ? &pad : nullptr, rot_b ? &pbd : nullptr,
@@ -696,15 +721,21 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
   void* t2 = scr.take(S);
   if (!t1 || !t2) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
   if (staged<T>(&pd, &pu)) {
-    FFGB_TRY(staged_rotate(vec, t1, t2, norb, na, nb, &pd, &pd, true, true, 4, scr, st));
+    const void* fbp = nullptr;
+    FFGB_TRY(staged_rotate(vec, t1, t2, norb, na, nb, &pd, &pd, true, true, 4, scr, st, &fbp));
+    if (fbp) FFGB_TRY(launch_row_scale<float>(t2, db, da, fbp, st));
     FFGB_TRY(diag_pass_t<T>(t2, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
     const void *fa = nullptr, *fb = nullptr;
     FFGB_TRY(phase_table(&pu, norb, na, scr, st, &fa));
     FFGB_TRY(phase_table(&pu, norb, nb, scr, st, &fb));
-    FFGB_TRY(stage_sector(t2, t2, norb, nb, da, da, pu, fb, 11, st));
-    FFGB_TRY(launch_transpose<float>(t2, t1, db, da, nullptr, nullptr, st));
-    if (!accumulate) return stage_sector(t1, out, norb, na, db, db, pu, fa, 10, st);
-    FFGB_TRY(stage_sector(t1, t1, norb, na, db, db, pu, fa, 10, st));
+    FFGB_TRY(stage_sector(t2, t2, norb, nb, da, da, pu, 11, st));
+    FFGB_TRY(launch_transpose<float>(t2, t1, db, da, fb, nullptr, st));
+    if (!accumulate) {
+      FFGB_TRY(stage_sector(t1, out, norb, na, db, db, pu, 10, st));
+      return fa ? launch_row_scale<float>(out, da, db, fa, st) : FFGB_OK;
+    }
+    FFGB_TRY(stage_sector(t1, t1, norb, na, db, db, pu, 10, st));
+    if (fa) FFGB_TRY(launch_row_scale<float>(t1, da, db, fa, st));
     return launch_axpy<float>(t1, out, da * db, 1.0, st);
   }
   PassArgs<T> A;
@@ -785,7 +816,7 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
   if (tmp2 && staged<T>(&pv, &pv)) {
     // alpha stages into tmp, transpose to beta rows, beta stages with the
     // expectation fused into the last one (no phases: |psi|^2 does not see them)
-    FFGB_TRY(stage_sector(vec, tmp, norb, na, db, db, pv, nullptr, 2 * salt, st));
+    FFGB_TRY(stage_sector(vec, tmp, norb, na, db, db, pv, 2 * salt, st));
     FFGB_TRY(launch_transpose<float>(tmp, tmp2, da, db, nullptr, nullptr, st));
     StageExpectArgs ex;
     FFGB_TRY(expect_tables(norb, na, nb, spec, scr, st, ex));
@@ -793,7 +824,7 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
     ex.partials = (double*)scr.take(sizeof(double) * (size_t)ex.partial_cap);
     if (!ex.partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
     int nct = 0;
-    FFGB_TRY(stage_sector(tmp2, tmp2, norb, nb, da, da, pv, nullptr, 2 * salt + 1, st, &ex, &nct));
+    FFGB_TRY(stage_sector(tmp2, tmp2, norb, nb, da, da, pv, 2 * salt + 1, st, &ex, &nct));
     reduce_partials_kernel<<<1, 256, 0, st>>>(ex.partials, nct, dslot, 0);
     count_launch();
     FFGB_CUDA(cudaGetLastError());
@@ -842,9 +873,17 @@ static int ucj_layer(void* x, void* tmp, int norb, int na, int nb, const SectorP
                      unsigned salt, Scratch& scr, cudaStream_t st) {
   if (staged<T>(&p, &p)) {
     const size_t mark = scr.off;
-    FFGB_TRY(staged_rotate(x, x, tmp, norb, na, nb, &p, &p, true, spec != nullptr, salt, scr, st));
+    const void* fbp = nullptr;
+    FFGB_TRY(staged_rotate(x, x, tmp, norb, na, nb, &p, &p, true, spec != nullptr, salt, scr, st, &fbp));
     if (spec) {
-      FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, *spec, OUT_STORE, nullptr, nullptr, scr, st));
+      DiagSpec s2 = *spec;
+      if (fbp) {
+        if (s2.zrep)
+          FFGB_TRY(launch_row_scale<float>(tmp, binom_h(norb, nb), binom_h(norb, na), fbp, st));
+        else
+          fold_col_phases(s2, p, norb);
+      }
+      FFGB_TRY(diag_pass_t<T>(tmp, norb, na, nb, s2, OUT_STORE, nullptr, nullptr, scr, st));
       FFGB_TRY(launch_transpose<float>(tmp, x, binom_h(norb, nb), binom_h(norb, na), nullptr, nullptr, st));
     }
     scr.off = mark;

@@ -21,6 +21,9 @@ For each (B, K) this script writes:
 * ``win_group_B_K(s, off, ...)`` -- loads the members ``s[off[j]]`` into
   registers, applies the network and stores them back; ``WinDispatch<B>``
   selects the function for a runtime K (shared-memory sector kernel).
+* ``win_pair_B_K`` / ``win_self_B_K`` and ``WinPack<B, K>`` -- the same
+  network on complement-packed members (see the section below), checked
+  against the plain network by a model run at generation time.
 
 The output is a pure function of the window sizes, so it is regenerated at
 build time and is not stored in the repository.
@@ -89,6 +92,34 @@ def emit_givens(b: int, k: int) -> str:
     return "\n".join(lines)
 
 
+def emit_givens_unrolled(b: int, k: int) -> str:
+    """The same network as straight-line code (stage kernels: one class per
+    kernel, so the larger code does not compete with other classes)."""
+    ms = members(b, k)
+    index = {w: j for j, w in enumerate(ms)}
+    n = len(ms)
+    lines = [
+        "template <int MODE>",
+        f"__device__ __forceinline__ void win_givens_u_{b}_{k}(float2 (&v)[{max(n, 1)}], const float* __restrict__ gp,"
+        " const float* __restrict__ gl, const unsigned* __restrict__ gt, unsigned& rng) {",
+    ]
+    g = 0
+    for r in range(b - 1):
+        for col in range(b - 1, r, -1):
+            l = col - 1
+            pairs = [(index[w], index[w ^ (3 << l)]) for w in ms if (w >> l) & 1 and not (w >> (l + 1)) & 1]
+            if pairs:
+                lines.append("  {")
+                lines.append("    float c, sr, si, cl, srl, sil;")
+                lines.append(f"    win_coef<MODE>(gp, gl, gt, {g}, rng, c, sr, si, cl, srl, sil);")
+                for x, y in pairs:
+                    lines.append(f"    rot_pair<MODE == 1>(v[{x}], v[{y}], c, sr, si, cl, srl, sil);")
+                lines.append("  }")
+            g += 1
+    lines.append("}")
+    return "\n".join(lines)
+
+
 def emit_groups(b: int) -> str:
     """Per (b, k): ``WinNet<b, k>`` (member count and network) and, for the
     shared-memory sector kernel, a group function on members at s[off[j]]."""
@@ -100,7 +131,7 @@ def emit_groups(b: int) -> str:
             f"  static constexpr int M = {m};\n"
             f"  template <int MODE> static __device__ __forceinline__ void apply(float2 (&v)[{m}], const float* gp,"
             f" const float* gl, const unsigned* gt, unsigned& rng) {{\n"
-            f"    win_givens_{b}_{k}<MODE>(v, gp, gl, gt, rng);\n  }}\n}};"
+            f"    win_givens_u_{b}_{k}<MODE>(v, gp, gl, gt, rng);\n  }}\n}};"
         )
         lines.append(
             f"template <bool COMP> static __device__ __noinline__ void win_group_{b}_{k}(float2* __restrict__ s,"
@@ -122,6 +153,192 @@ def emit_groups(b: int) -> str:
     return "\n".join(lines)
 
 
+# ---------------------------------------------------------------------------
+# complement-packed networks
+# ---------------------------------------------------------------------------
+# A pack holds two members whose window patterns are complements, in split
+# form: R = (re0, re1), I = (im0, im1) as two FP32x2 registers.  An adjacent
+# rotation (l, l+1) maps complement pairs to complement pairs, and the two
+# lanes of a pack always play opposite roles (one holds the lower orbital,
+# the other the upper one), so one rotation of two packs is 12 packed FMAs with
+# no lane swaps (complex rotations on (re, im) pairs need two swaps each).
+#   pair: lane 0 = member j of a group with K electrons in the window, lane 1 =
+#         the complement member of a group with B - K electrons (K < B - K).
+#   self: K = B/2; the members with window bit 0 clear take lane 0.  Only
+#         rotation (0, 1) then pairs lane 0 with lane 1 of the partner pack,
+#         which costs lane swaps (it occurs once per network).
+
+
+def comp_index(b: int, k: int) -> list[int]:
+    """For member j of class k: index of its complement in class b - k."""
+    full = (1 << b) - 1
+    other = {w: j for j, w in enumerate(members(b, b - k))}
+    return [other[full ^ w] for w in members(b, k)]
+
+
+def pack_lanes(b: int, k: int, kind: str) -> list[tuple[int, int]]:
+    """Window patterns (lane 0, lane 1) of every pack."""
+    full = (1 << b) - 1
+    if kind == "pair":
+        return [(w, full ^ w) for w in members(b, k)]
+    return [(w, full ^ w) for w in members(b, k) if not w & 1]
+
+
+def pack_schedule(b: int, k: int, kind: str) -> list[list[tuple[int, int, bool, bool, bool]]]:
+    """Per rotation pattern col (b-1 down to 1; pair (col-1, col)): the ops
+    (p, q, swap, vp_a, vq_a).  swap: lane 0 of p partners lane 1 of q.
+    vp_a: lane 0 of p holds the lower orbital (coefficients (s, -conj s)),
+    otherwise (-conj s, s); likewise vq_a for q."""
+    lanes = pack_lanes(b, k, kind)
+    where = {}
+    for p, (w0, w1) in enumerate(lanes):
+        where[w0] = (p, 0)
+        where[w1] = (p, 1)
+    out = []
+    for col in range(b - 1, 0, -1):
+        l = col - 1
+        m = 3 << l
+        ops, seen = [], set()
+        for p, (w0, _) in enumerate(lanes):
+            if ((w0 >> l) & 1) == ((w0 >> (l + 1)) & 1) or p in seen:
+                continue
+            q, lam = where[w0 ^ m]
+            seen.add(p)
+            seen.add(q)
+            vp_a = bool((w0 >> l) & 1)
+            swap = lam == 1
+            q0 = lanes[q][0]
+            vq_a = bool((q0 >> l) & 1)
+            ops.append((p, q, swap, vp_a, vq_a))
+        out.append(ops)
+    return out
+
+
+def _model_check(b: int, k: int, kind: str) -> None:
+    """Packed schedule == plain network on random data (complex128 model)."""
+    import random
+
+    rnd = random.Random(1000 * b + k)
+    nrot = b * (b - 1) // 2
+    coefs = []
+    for _ in range(nrot):
+        c = rnd.uniform(-1, 1)
+        ph = rnd.uniform(0, 6.283)
+        r = (1 - c * c) ** 0.5
+        coefs.append((c, complex(r * __import__("math").cos(ph), r * __import__("math").sin(ph))))
+
+    def plain(bb, kk, v):
+        ms = members(bb, kk)
+        idx = {w: j for j, w in enumerate(ms)}
+        v = list(v)
+        g = 0
+        for r in range(bb - 1):
+            for col in range(bb - 1, r, -1):
+                l = col - 1
+                c, s = coefs[g]
+                for w in ms:
+                    if (w >> l) & 1 and not (w >> (l + 1)) & 1:
+                        x, y = idx[w], idx[w ^ (3 << l)]
+                        v[x], v[y] = c * v[x] + s * v[y], -s.conjugate() * v[x] + c * v[y]
+                g += 1
+        return v
+
+    lanes = pack_lanes(b, k, kind)
+    sched = pack_schedule(b, k, kind)
+    if kind == "pair":
+        va = [complex(rnd.gauss(0, 1), rnd.gauss(0, 1)) for _ in members(b, k)]
+        vb = [complex(rnd.gauss(0, 1), rnd.gauss(0, 1)) for _ in members(b, b - k)]
+        ia = {w: j for j, w in enumerate(members(b, k))}
+        ib = {w: j for j, w in enumerate(members(b, b - k))}
+        P = [[va[ia[w0]], vb[ib[w1]]] for w0, w1 in lanes]
+        want_a, want_b = plain(b, k, va), plain(b, b - k, vb)
+    else:
+        v = [complex(rnd.gauss(0, 1), rnd.gauss(0, 1)) for _ in members(b, k)]
+        iv = {w: j for j, w in enumerate(members(b, k))}
+        P = [[v[iv[w0]], v[iv[w1]]] for w0, w1 in lanes]
+        want = plain(b, k, v)
+    g = 0
+    for r in range(b - 1):
+        for ci, col in enumerate(range(b - 1, 0, -1)):
+            if not col > r:
+                continue
+            c, s = coefs[g]
+            A, Bv = (s, -s.conjugate()), (-s.conjugate(), s)
+            for p, q, swap, vp_a, vq_a in sched[ci]:
+                Pp, Qq = P[p], P[q]
+                Qx = [Qq[1], Qq[0]] if swap else Qq
+                Px = [Pp[1], Pp[0]] if swap else Pp
+                vp, vq = (A if vp_a else Bv), (A if vq_a else Bv)
+                P[p] = [c * Pp[t] + vp[t] * Qx[t] for t in range(2)]
+                P[q] = [c * Qq[t] + vq[t] * Px[t] for t in range(2)]
+            g += 1
+    if kind == "pair":
+        for pi, (w0, w1) in enumerate(lanes):
+            assert abs(P[pi][0] - want_a[ia[w0]]) < 1e-9 and abs(P[pi][1] - want_b[ib[w1]]) < 1e-9, (b, k)
+    else:
+        for pi, (w0, w1) in enumerate(lanes):
+            assert abs(P[pi][0] - want[iv[w0]]) < 1e-9 and abs(P[pi][1] - want[iv[w1]]) < 1e-9, (b, k)
+
+
+def pack_kind(b: int, k: int) -> str | None:
+    if 2 * k == b:
+        return "self"
+    if 2 * k < b and math.comb(b, k) <= 35:
+        return "pair"
+    return None
+
+
+def emit_packed(b: int, k: int, kind: str) -> str:
+    lanes = pack_lanes(b, k, kind)
+    sched = pack_schedule(b, k, kind)
+    n = len(lanes)
+    name = f"win_{kind}_{b}_{k}"
+    # Straight-line network: a runtime loop with conditional rotation blocks
+    # makes the compiler copy every updated pack back into loop-invariant
+    # registers (one MOV per register pair per rotation).
+    lines = [
+        "template <int MODE>",
+        f"__device__ __forceinline__ void {name}(float2 (&R)[{n}], float2 (&I)[{n}], const float* __restrict__ gp,"
+        " const float* __restrict__ gl, const unsigned* __restrict__ gt, unsigned& rng) {",
+    ]
+    g = 0
+    for r in range(b - 1):
+        for ci, col in enumerate(range(b - 1, 0, -1)):
+            if not col > r:
+                continue
+            if sched[ci]:
+                lines.append("  {")
+                lines.append("    PackCoef pc;")
+                lines.append(f"    pack_coef<MODE>(gp, gl, gt, {g}, rng, pc);")
+                for p, q, swap, vp_a, vq_a in sched[ci]:
+                    fn = "rot_pack_x" if swap else "rot_pack"
+                    lines.append(f"    {fn}<{str(vp_a).lower()}, {str(vq_a).lower()}>(R[{p}], I[{p}], R[{q}], I[{q}], pc);")
+                lines.append("  }")
+            g += 1
+    lines.append("}")
+    # lane tables: member index (class K, and class B-K for lane 1 of pairs)
+    ia = {w: j for j, w in enumerate(members(b, k))}
+    ib = {w: j for j, w in enumerate(members(b, b - k))}
+    l0 = ", ".join(str(ia[w0]) for w0, _ in lanes)
+    l1 = ", ".join(str((ib if kind == "pair" else ia)[w1]) for _, w1 in lanes)
+    p0 = ", ".join(str(w0) for w0, _ in lanes)
+    p1 = ", ".join(str(w1) for _, w1 in lanes)
+    lines.append(
+        f"template <> struct WinPack<{b}, {k}> {{\n"
+        f"  static constexpr int NP = {n};\n"
+        f"  static constexpr bool PAIR = {'true' if kind == 'pair' else 'false'};\n"
+        f"  // member index of lane 0 / lane 1 (lane 1 indexes class B - K for pairs) and window patterns\n"
+        f"  static __host__ __device__ constexpr int lane0(int q) {{ constexpr int t[{n}] = {{{l0}}}; return t[q]; }}\n"
+        f"  static __host__ __device__ constexpr int lane1(int q) {{ constexpr int t[{n}] = {{{l1}}}; return t[q]; }}\n"
+        f"  static __host__ __device__ constexpr unsigned pat0(int q) {{ constexpr unsigned t[{n}] = {{{p0}}}; return t[q]; }}\n"
+        f"  static __host__ __device__ constexpr unsigned pat1(int q) {{ constexpr unsigned t[{n}] = {{{p1}}}; return t[q]; }}\n"
+        f"  template <int MODE> static __device__ __forceinline__ void apply(float2 (&R)[{n}], float2 (&I)[{n}],"
+        f" const float* gp, const float* gl, const unsigned* gt, unsigned& rng) {{\n"
+        f"    {name}<MODE>(R, I, gp, gl, gt, rng);\n  }}\n}};"
+    )
+    return "\n".join(lines)
+
+
 def main(out_path: str) -> None:
     parts = [
         "// Generated by gen_windows.py -- do not edit.",
@@ -136,8 +353,16 @@ def main(out_path: str) -> None:
     for b in range(1, MAX_B + 1):
         for k in range(0, b + 1):
             parts.append(emit_givens(b, k))
+            parts.append(emit_givens_unrolled(b, k))
     for b in range(1, MAX_B + 1):
         parts.append(emit_groups(b))
+    parts.append("template <int B, int K> struct WinPack { static constexpr int NP = 0; };")
+    for b in range(2, MAX_B + 1):
+        for k in range(0, b + 1):
+            kind = pack_kind(b, k)
+            if kind:
+                _model_check(b, k, kind)
+                parts.append(emit_packed(b, k, kind))
     Path(out_path).write_text("\n".join(parts) + "\n")
 
 

@@ -267,6 +267,69 @@ __device__ __forceinline__ void win_coef(const float* __restrict__ gp, const flo
   }
 }
 
+// Coefficients of one rotation for complement-packed members (split
+// re / im lanes): c2 = (c, c), sa = (sr, -sr), sb = (-sr, sr),
+// sip = (si, si), sim = (-si, -si).
+struct PackCoef {
+  float2 c2, sa, sb, sip, sim;
+};
+
+template <int MODE>
+__device__ __forceinline__ void pack_coef(const float* __restrict__ gp, const float* __restrict__ gl,
+                                          const unsigned* __restrict__ gt, int g, unsigned& rng, PackCoef& k) {
+  float c, sr, si, cl, srl, sil;
+  win_coef<MODE == 1 ? 0 : MODE>(gp, gl, gt, g, rng, c, sr, si, cl, srl, sil);
+  k.c2 = make_float2(c, c);
+  k.sa = make_float2(sr, -sr);
+  k.sb = make_float2(-sr, sr);
+  k.sip = make_float2(si, si);
+  k.sim = make_float2(-si, -si);
+}
+
+// One rotation on two packs P, Q whose lanes are partners lane by lane:
+// P <- c P + vp (.) Q, Q <- c Q + vq (.) P, with vp, vq = (s, -conj s) when
+// VP_A / VQ_A, else (-conj s, s); complex lane products in split form.
+template <bool VP_A, bool VQ_A>
+__device__ __forceinline__ void rot_pack(float2& PR, float2& PI, float2& QR, float2& QI, const PackCoef& k) {
+  const float2 rp = VP_A ? k.sa : k.sb, rq = VQ_A ? k.sa : k.sb;
+  float2 pr = __fmul2_rn(k.c2, PR), pi = __fmul2_rn(k.c2, PI);
+  float2 qr = __fmul2_rn(k.c2, QR), qi = __fmul2_rn(k.c2, QI);
+  pr = __ffma2_rn(rp, QR, pr);
+  pr = __ffma2_rn(k.sim, QI, pr);
+  pi = __ffma2_rn(rp, QI, pi);
+  pi = __ffma2_rn(k.sip, QR, pi);
+  qr = __ffma2_rn(rq, PR, qr);
+  qr = __ffma2_rn(k.sim, PI, qr);
+  qi = __ffma2_rn(rq, PI, qi);
+  qi = __ffma2_rn(k.sip, PR, qi);
+  PR = pr;
+  PI = pi;
+  QR = qr;
+  QI = qi;
+}
+
+// The same with lane 0 of P partnering lane 1 of Q (and lane 1 of P lane 0 of Q).
+template <bool VP_A, bool VQ_A>
+__device__ __forceinline__ void rot_pack_x(float2& PR, float2& PI, float2& QR, float2& QI, const PackCoef& k) {
+  const float2 rp = VP_A ? k.sa : k.sb, rq = VQ_A ? k.sa : k.sb;
+  const float2 QRs = make_float2(QR.y, QR.x), QIs = make_float2(QI.y, QI.x);
+  const float2 PRs = make_float2(PR.y, PR.x), PIs = make_float2(PI.y, PI.x);
+  float2 pr = __fmul2_rn(k.c2, PR), pi = __fmul2_rn(k.c2, PI);
+  float2 qr = __fmul2_rn(k.c2, QR), qi = __fmul2_rn(k.c2, QI);
+  pr = __ffma2_rn(rp, QRs, pr);
+  pr = __ffma2_rn(k.sim, QIs, pr);
+  pi = __ffma2_rn(rp, QIs, pi);
+  pi = __ffma2_rn(k.sip, QRs, pi);
+  qr = __ffma2_rn(rq, PRs, qr);
+  qr = __ffma2_rn(k.sim, PIs, qr);
+  qi = __ffma2_rn(rq, PIs, qi);
+  qi = __ffma2_rn(k.sip, PRs, qi);
+  PR = pr;
+  PI = pi;
+  QR = qr;
+  QI = qi;
+}
+
 // Start of a thread's generator for dithered coefficients (a hash of the
 // column and the stage's salt).
 __device__ __forceinline__ unsigned dither_seed(unsigned long long col, unsigned salt) {

@@ -1,4 +1,5 @@
-// Launch of one window stage; instantiated per window size in stage_b*.cu.
+// Launch of one window-stage job.  launch_win_bk<B, K> is instantiated by
+// stage_inst.cu, compiled once per (B, range of K) for parallel builds.
 #pragma once
 
 #include "common.h"
@@ -6,26 +7,32 @@
 
 namespace ffgb {
 
-template <int B>
-int launch_win_stage(const WinStageParams& P, int grid, int mode, bool expect, cudaStream_t st) {
-  if (expect) {
-    if (mode == 1)
-      win_stage_kernel<B, 1, true><<<grid, STAGE_THREADS, 0, st>>>(P);
-    else if (mode == 2)
-      win_stage_kernel<B, 2, true><<<grid, STAGE_THREADS, 0, st>>>(P);
-    else
-      return fail(FFGB_ERR_ARG, "fused expectation needs compensated or dithered coefficients");
+template <int B, int K, int KIND>
+int launch_win_job_k(const WinJob& P, bool low, int epi, int grid, cudaStream_t st) {
+  if (low) {
+    if (epi != EPI_STORE) return fail(FFGB_ERR_ARG, "the expectation runs on the upper window");
+    win_class_kernel<B, K, KIND, true, EPI_STORE><<<grid, STAGE_THREADS, 0, st>>>(P);
+  } else if (epi == EPI_STORE) {
+    win_class_kernel<B, K, KIND, false, EPI_STORE><<<grid, STAGE_THREADS, 0, st>>>(P);
   } else {
-    if (mode == 0)
-      win_stage_kernel<B, 0, false><<<grid, STAGE_THREADS, 0, st>>>(P);
-    else if (mode == 1)
-      win_stage_kernel<B, 1, false><<<grid, STAGE_THREADS, 0, st>>>(P);
-    else
-      win_stage_kernel<B, 2, false><<<grid, STAGE_THREADS, 0, st>>>(P);
+    win_class_kernel<B, K, KIND, false, EPI_EXPECT><<<grid, STAGE_THREADS, 0, st>>>(P);
   }
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
+}
+
+// kind 0: plain members; 1: K = B/2 complement-packed; 2: classes K and B - K packed together
+template <int B, int K>
+int launch_win_bk(const WinJob& P, int kind, bool low, int epi, int grid, cudaStream_t st) {
+  if (kind == 0) return launch_win_job_k<B, K, 0>(P, low, epi, grid, st);
+  if constexpr (2 * K == B) {
+    if (kind == 1) return launch_win_job_k<B, K, 1>(P, low, epi, grid, st);
+  }
+  if constexpr (2 * K < B && win_members(B, K) <= 35) {
+    if (kind == 2) return launch_win_job_k<B, K, 2>(P, low, epi, grid, st);
+  }
+  return fail(FFGB_ERR_ARG, "no packed kernel for this window class");
 }
 
 }  // namespace ffgb

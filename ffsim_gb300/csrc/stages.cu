@@ -14,8 +14,8 @@
 
 namespace ffgb {
 
-template <int B>
-int launch_win_stage(const WinStageParams& P, int grid, int mode, bool expect, cudaStream_t st);
+template <int B, int K>
+int launch_win_bk(const WinJob& P, int kind, bool low, int epi, int grid, cudaStream_t st);
 
 namespace {
 
@@ -197,12 +197,14 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h
     P.n_classes = T->n_classes;
     P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
     P.salt = salt * 0x9E3779B9u + 0x51ED270Bu * (unsigned)(s0 + 1);
+    P.gpc = CS_MAX_GPC;
     long long cta = 0;
     for (int c = 0; c < T->n_classes; ++c) {
       P.cls_m[c] = T->cls_m[c];
       P.cls_base[c] = T->cls_base[c];
+      P.cls_groups[c] = T->cls_groups[c];
       P.cls_cta0[c] = (int)cta;
-      cta += (long long)T->cls_groups[c] * P.tiles;
+      cta += (long long)((T->cls_groups[c] + P.gpc - 1) / P.gpc) * P.tiles;
     }
     P.cls_cta0[T->n_classes] = (int)cta;
     if (cta > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
@@ -226,37 +228,48 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h
   return FFGB_OK;
 }
 
-int launch_win_b(int b, const WinStageParams& P, int grid, int mode, bool expect, cudaStream_t st) {
+template <int B, int K = 0>
+int launch_job_k(int k, const WinJob& P, int kind, bool low, int epi, int grid, cudaStream_t st) {
+  if constexpr (K <= B) {
+    if (k == K) return launch_win_bk<B, K>(P, kind, low, epi, grid, st);
+    return launch_job_k<B, K + 1>(k, P, kind, low, epi, grid, st);
+  } else {
+    return fail(FFGB_ERR_ARG, "window class out of range");
+  }
+}
+
+int launch_job_b(int b, const WinJob& P, int k, int kind, bool low, int epi, int grid, cudaStream_t st) {
   switch (b) {
-    case 4: return launch_win_stage<4>(P, grid, mode, expect, st);
-    case 5: return launch_win_stage<5>(P, grid, mode, expect, st);
-    case 6: return launch_win_stage<6>(P, grid, mode, expect, st);
-    case 7: return launch_win_stage<7>(P, grid, mode, expect, st);
-    case 8: return launch_win_stage<8>(P, grid, mode, expect, st);
+    case 4: return launch_job_k<4>(k, P, kind, low, epi, grid, st);
+    case 5: return launch_job_k<5>(k, P, kind, low, epi, grid, st);
+    case 6: return launch_job_k<6>(k, P, kind, low, epi, grid, st);
+    case 7: return launch_job_k<7>(k, P, kind, low, epi, grid, st);
+    case 8: return launch_job_k<8>(k, P, kind, low, epi, grid, st);
     default: return fail(FFGB_ERR_UNSUPPORTED, "window size outside [4, 8]");
   }
 }
 
-// One window stage.  low: window [0, h) with groups = high-half patterns;
-// otherwise window [h, norb) with groups = low-half patterns.
+// One window stage.  low: window [0, h), groups = high-half patterns (members
+// are consecutive rows after a base row); otherwise window [h, norb), groups =
+// low-half patterns (row = colex rank of the pattern, members at offsets).
+// Every electron-count class k is one launch; classes k and B - k are
+// processed together (complement-packed) where their registers fit.
 int window_stage(const float2* in, float2* out, long long ld, long long ncols, int norb, int nocc,
-                 const HalfTables& T, bool low, const std::vector<Givens>& net, int mode, unsigned salt,
-                 const float2* ph_in, const float2* ph_out, const StageExpectArgs* ex, int* ex_ctas,
-                 cudaStream_t st) {
+                 const HalfTables& T, bool low, const std::vector<Givens>& net, unsigned salt,
+                 const StageExpectArgs* ex, int* ex_ctas, cudaStream_t st) {
   const int h = T.h, q = T.q;
   const int b = low ? h : q;
-  auto P = std::make_unique<WinStageParams>();
-  std::memset(P.get(), 0, sizeof(WinStageParams));
-  P->in = in;
-  P->out = out;
-  P->ld = ld;
-  P->ncols = ncols;
-  P->low = low ? 1 : 0;
-  P->norb = norb;
-  P->lo = low ? 0 : h;
-  P->salt = salt;
-  P->ph_in = ph_in;
-  P->ph_out = ph_out;
+  auto base = std::make_unique<WinJob>();
+  std::memset(base.get(), 0, sizeof(WinJob));
+  base->in = in;
+  base->out = out;
+  base->ld = ld;
+  base->ncols = ncols;
+  base->tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
+  base->norb = norb;
+  base->lo = low ? 0 : h;
+  base->salt = salt;
+  const int epi = ex ? EPI_EXPECT : EPI_STORE;
   std::vector<double> v(3 * net.size());
   for (size_t g = 0; g < net.size(); ++g) {
     v[3 * g] = net[g].c;
@@ -264,57 +277,79 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
     v[3 * g + 2] = net[g].s.imag();
   }
   if (v.size() > 84) return fail(FFGB_ERR_UNSUPPORTED, "window network too long");
-  put_coefs(v.data(), (int)v.size(), mode, P->gp, P->gl, P->gt);
-  P->tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
-  // classes: k electrons inside the window
-  const int kbeg = low ? std::max(0, nocc - q) : std::max(0, nocc - h);
-  const int kend = low ? std::min(h, nocc) : std::min(q, nocc);
-  std::vector<int> ks;
-  for (int k = kbeg; k <= kend; ++k) ks.push_back(k);
-  std::stable_sort(ks.begin(), ks.end(), [&](int a, int c) { return C(b, a) > C(b, c); });
-  long long cta = 0;
-  int toff = 0;
-  P->n_classes = (int)ks.size();
-  for (size_t ci = 0; ci < ks.size(); ++ci) {
-    const int k = ks[ci];
-    P->cls_k[ci] = k;
-    P->cls_cta0[ci] = (int)cta;
-    P->cls_off[ci] = toff;
-    long long groups;
-    if (low) {  // groups: high-half patterns with nocc - k electrons, base row = rt
-      const int m = nocc - k;
-      groups = C(q, m);
-      if (toff + groups > 256) return fail(FFGB_ERR_UNSUPPORTED, "window table overflow");
-      for (long long g = 0; g < groups; ++g) P->tab[toff + g] = T.rt[T.moff[m] + g];
-      toff += (int)groups;
-    } else {  // groups: low-half patterns (row = colex rank), members at rt offsets
-      groups = C(h, nocc - k);
-      if (toff + C(q, k) > 256) return fail(FFGB_ERR_UNSUPPORTED, "window table overflow");
-      for (long long j = 0; j < C(q, k); ++j) P->tab[toff + j] = T.rt[T.moff[k] + j];
-      toff += (int)C(q, k);
-    }
-    cta += groups * P->tiles;
-  }
-  P->cls_cta0[ks.size()] = (int)cta;
-  if (cta > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "window stage grid too large");
+  put_coefs(v.data(), (int)v.size(), 2, base->gp, base->gl, base->gt);
   if (ex) {
-    if (cta > ex->partial_cap) return fail(FFGB_ERR_OOM, "partial-sum buffer too small");
-    StageExpect& E = P->ex;
+    StageExpect& E = base->ex;
     E.zrow = ex->zrow;
     E.zcol = ex->zcol;
     E.row_str = ex->row_str;
     E.col_str = ex->col_str;
-    E.partials = ex->partials;
     E.zrep = ex->zrep;
     for (int i = 0; i < FFGB_MAXN; ++i)
       for (int l = 0; l < FFGB_MAXN; ++l) {
         E.X[i][l] = ex->X[i][l];
         E.Xsum[l] += ex->X[i][l];
       }
-    if (ex_ctas) *ex_ctas = (int)cta;
   }
-  if (cta == 0) return FFGB_OK;
-  return launch_win_b(b, *P, (int)cta, mode, ex != nullptr, st);
+  // classes: k electrons inside the window
+  const int kbeg = low ? std::max(0, nocc - q) : std::max(0, nocc - h);
+  const int kend = low ? std::min(h, nocc) : std::min(q, nocc);
+  auto in_range = [&](int k) { return k >= kbeg && k <= kend; };
+  auto count = [&](int k) { return low ? C(q, nocc - k) : C(h, nocc - k); };
+  struct Job {
+    int k, kind, kb;
+    long long n, start, work;
+  };
+  std::vector<Job> jobs;
+  for (int k = kbeg; k <= kend; ++k) {
+    const int kp = b - k;
+    const bool pairable = 2 * k < b && in_range(kp) && C(b, k) <= 35;
+    const bool partner_pairs = 2 * k > b && in_range(kp) && C(b, kp) <= 35;
+    if (partner_pairs) continue;
+    if (2 * k == b) {
+      // complement-packed within the group on the lower window; on the upper
+      // window its member-offset table pushes the packed kernel into spills
+      jobs.push_back({k, low ? 1 : 0, k, count(k), 0, count(k) * C(b, k)});
+    } else if (pairable) {
+      const long long np = std::min(count(k), count(kp));
+      if (np > 0) jobs.push_back({k, 2, kp, np, 0, 2 * np * C(b, k)});
+      if (count(k) > np) jobs.push_back({k, 0, k, count(k) - np, np, (count(k) - np) * C(b, k)});
+      if (count(kp) > np) jobs.push_back({kp, 0, kp, count(kp) - np, np, (count(kp) - np) * C(b, kp)});
+    } else {
+      jobs.push_back({k, 0, k, count(k), 0, count(k) * C(b, k)});
+    }
+  }
+  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& c) { return a.work > c.work; });
+  auto fill = [&](int k, long long start, long long n, int* bases, int* offs, int* g0) -> int {
+    if (low) {
+      const int m = nocc - k;
+      if (n > 72) return fail(FFGB_ERR_UNSUPPORTED, "window group table overflow");
+      for (long long g = 0; g < n; ++g) bases[g] = T.rt[T.moff[m] + start + g];
+    } else {
+      if (C(q, k) > 72) return fail(FFGB_ERR_UNSUPPORTED, "window member table overflow");
+      for (long long j = 0; j < C(q, k); ++j) offs[j] = T.rt[T.moff[k] + j];
+      *g0 = (int)start;
+    }
+    return FFGB_OK;
+  };
+  long long pbase = 0;
+  WinJob P;
+  for (const Job& jb : jobs) {
+    std::memcpy(&P, base.get(), sizeof(WinJob));
+    FFGB_TRY(fill(jb.k, jb.start, jb.n, P.base_a, P.off_a, &P.ga0));
+    if (jb.kind == 2) FFGB_TRY(fill(jb.kb, 0, jb.n, P.base_b, P.off_b, &P.gb0));
+    const long long grid = jb.n * base->tiles;
+    if (grid <= 0) continue;
+    if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "window stage grid too large");
+    if (ex) {
+      if (pbase + grid > ex->partial_cap) return fail(FFGB_ERR_OOM, "partial-sum buffer too small");
+      P.ex.partials = ex->partials + pbase;
+    }
+    FFGB_TRY(launch_job_b(b, P, jb.k, jb.kind, low, epi, (int)grid, st));
+    pbase += grid;
+  }
+  if (ex_ctas) *ex_ctas = (int)pbase;
+  return FFGB_OK;
 }
 
 }  // namespace
@@ -333,16 +368,13 @@ int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long l
   const HalfTables T = half_tables(norb, nocc, plan.h);
   const float2* src = (const float2*)in;
   float2* dst = (float2*)out;
+  if (o.mode != 2) return fail(FFGB_ERR_ARG, "stage kernels use dithered coefficients");
   const unsigned s = o.salt * 0x2545F491u;
-  FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, o.mode, s + 1, (const float2*)o.ph_in,
-                        nullptr, nullptr, nullptr, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.b2, o.mode, s + 2, nullptr, nullptr,
-                        nullptr, nullptr, st));
+  FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, s + 1, nullptr, nullptr, st));
+  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.b2, s + 2, nullptr, nullptr, st));
   FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, plan.h, plan.cs, o.mode, s + 3, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, true, plan.a1, o.mode, s + 4, nullptr, nullptr,
-                        nullptr, nullptr, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.a2, o.mode, s + 5, nullptr,
-                        (const float2*)o.ph_out, o.expect, o.expect_ctas, st));
+  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, true, plan.a1, s + 4, nullptr, nullptr, st));
+  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.a2, s + 5, o.expect, o.expect_ctas, st));
   return FFGB_OK;
 }
 

@@ -30,33 +30,24 @@ struct StageExpect {
   int zrep;
 };
 
-struct WinStageParams {
+// One launch of a window stage: the groups of one electron-count class K
+// (KIND 0: plain members; KIND 1: K = B/2, complement-packed within the
+// group), or pairs of groups of classes K and B - K (KIND 2, complement-packed
+// across the two groups).
+struct WinJob {
   const float2* in;
-  float2* out;      // unused by the fused expectation
+  float2* out;
   long long ld;     // row stride (elements)
   long long ncols;  // columns processed
-  int n_classes;
-  int cls_k[9];     // electrons inside the window, per class (largest classes first)
-  int cls_cta0[10]; // first CTA of each class
-  int cls_off[9];   // offset of the class's group bases (LOW) / member offsets (HIGH) in tab
   int tiles;        // column tiles per group
-  int low;          // 1: window [0, h), members are consecutive rows after a per-group base row
   int norb, lo;     // orbitals; first orbital of the window
-  int tab[256];
-  float gp[84], gl[84];  // window network coefficients (see win_coef)
+  int ga0, gb0;     // window [h, norb): first group (= its low-half rank) of class K / B - K
+  int base_a[72], base_b[72];  // window [0, h): base rows of the groups
+  int off_a[72], off_b[72];    // window [h, norb): member row offsets of class K / B - K
+  float gp[84], gl[84];        // window network coefficients (see win_coef)
   unsigned gt[84];
   unsigned salt;
-  const float2* ph_in;   // optional per-row phases applied before the network
-  const float2* ph_out;  // optional per-row phases applied after the network
-  StageExpect ex;
-};
-
-// Per-thread part of the fused expectation: the window orbitals' weights and
-// the constant part of z for this (group, column).
-struct ZCtx {
-  float w[8];
-  float base, scale;
-  const float* zrow;
+  StageExpect ex;        // partials of this launch start at ex.partials
 };
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
@@ -77,88 +68,56 @@ __host__ __device__ constexpr unsigned win_member(int b, int k, int j) {
   return m;
 }
 
-template <int B, int K, int MODE, bool LOW>
-static __device__ __noinline__ void win_rows(const float2* __restrict__ si, float2* __restrict__ so,
-                                             long long ld, const int* __restrict__ off,
-                                             const float* __restrict__ gp, const float* __restrict__ gl,
-                                             const unsigned* __restrict__ gt, unsigned rng,
-                                             const float2* __restrict__ ph_in,
-                                             const float2* __restrict__ ph_out) {
-  constexpr int M = WinNet<B, K>::M;
-  float2 v[M];
-#pragma unroll
-  for (int j = 0; j < M; ++j) v[j] = si[(long long)(LOW ? j : off[j]) * ld];
-  if (ph_in) {
-#pragma unroll
-    for (int j = 0; j < M; ++j) v[j] = cmulf(v[j], ph_in[LOW ? j : off[j]]);
-  }
-  WinNet<B, K>::template apply<MODE>(v, gp, gl, gt, rng);
-  if (ph_out) {
-#pragma unroll
-    for (int j = 0; j < M; ++j) v[j] = cmulf(v[j], ph_out[LOW ? j : off[j]]);
-  }
-#pragma unroll
-  for (int j = 0; j < M; ++j) so[(long long)(LOW ? j : off[j]) * ld] = v[j];
+// Registers: the members of one thread are 2 * C(B, K) floats (twice that for
+// KIND 2); addressing, coefficients and scheduling slack take about
+// 30 + 0.55 * data more (measured with -Xptxas -v), the fused expectation ~16.
+__host__ __device__ constexpr int win_min_blocks(int b, int k, int kind, int epi) {
+  const int data = 2 * win_members(b, k) * (kind == 2 ? 2 : 1);
+  const int need = 30 + (155 * data) / 100 + (epi == 2 ? 16 : 0);
+  return need <= 64 ? 8 : need <= 80 ? 6 : need <= 96 ? 5 : need <= 128 ? 4 : need <= 168 ? 3 : 2;
 }
 
-// Last stage fused with the expectation: returns sum_j z_j |v_j|^2 (FP32
-// Kahan inside, FP64 out); nothing is stored.
-template <int B, int K, int MODE, bool LOW>
-static __device__ __noinline__ double win_rows_expect(const float2* __restrict__ si, long long ld,
-                                                      const int* __restrict__ off, const float* __restrict__ gp,
-                                                      const float* __restrict__ gl,
-                                                      const unsigned* __restrict__ gt, unsigned rng, ZCtx z) {
-  constexpr int M = WinNet<B, K>::M;
-  float2 v[M];
-#pragma unroll
-  for (int j = 0; j < M; ++j) v[j] = si[(long long)(LOW ? j : off[j]) * ld];
-  WinNet<B, K>::template apply<MODE>(v, gp, gl, gt, rng);
-  float acc = 0.f, cmp = 0.f;
-#pragma unroll
-  for (int j = 0; j < M; ++j) {
-    const unsigned mem = win_member(B, K, j);
-    float wsum = 0.f;
-#pragma unroll
-    for (int t = 0; t < B; ++t)
-      if ((mem >> t) & 1u) wsum += z.w[t];
-    const float zj = __ldg(z.zrow + (LOW ? j : off[j])) + z.base + z.scale * wsum;
-    const float y = zj * (v[j].x * v[j].x + v[j].y * v[j].y) - cmp;
-    const float t2 = acc + y;
-    cmp = (t2 - acc) - y;
-    acc = t2;
-  }
-  return (double)acc - (double)cmp;
-}
+// Per-thread part of the fused expectation: weights of the window orbitals
+// (sum_l X[lo + t][l] g_l(col)) and the constant part of z for one group.
+struct ZCtx {
+  float w[8];
+  float base, scale;
+};
 
-template <int B, int MODE, int K = 0>
-__device__ __forceinline__ void win_rows_k(int k, bool low, const float2* si, float2* so, long long ld,
-                                           const int* off, const float* gp, const float* gl, const unsigned* gt,
-                                           unsigned rng, const float2* ph_in, const float2* ph_out) {
-  if constexpr (K <= B) {
-    if (k == K) {
-      if (low)
-        win_rows<B, K, MODE, true>(si, so, ld, off, gp, gl, gt, rng, ph_in, ph_out);
-      else
-        win_rows<B, K, MODE, false>(si, so, ld, off, gp, gl, gt, rng, ph_in, ph_out);
-    } else {
-      win_rows_k<B, MODE, K + 1>(k, low, si, so, ld, off, gp, gl, gt, rng, ph_in, ph_out);
-    }
+template <int B>
+__device__ __forceinline__ void zctx_make(const StageExpect& E, int norb, int lo, unsigned cstr, unsigned outside_a,
+                                          unsigned outside_b, ZCtx& za, ZCtx& zb, float zc) {
+  float sa = 0.f, sb = 0.f, wall = 0.f;
+#pragma unroll
+  for (int t = 0; t < B; ++t) za.w[t] = 0.f;
+  for (int l = 0; l < norb; ++l) {
+    const float gcol = E.zrep ? (((cstr >> l) & 1u) ? -1.f : 1.f) : (float)((cstr >> l) & 1u);
+#pragma unroll
+    for (int t = 0; t < B; ++t) za.w[t] += E.X[lo + t][l] * gcol;
+    for (unsigned o = outside_a; o; o &= o - 1) sa += E.X[__ffs(o) - 1][l] * gcol;
+    for (unsigned o = outside_b; o; o &= o - 1) sb += E.X[__ffs(o) - 1][l] * gcol;
+    wall += E.Xsum[l] * gcol;
   }
-}
-
-template <int B, int MODE, int K = 0>
-__device__ __forceinline__ double win_expect_k(int k, bool low, const float2* si, long long ld, const int* off,
-                                               const float* gp, const float* gl, const unsigned* gt, unsigned rng,
-                                               const ZCtx& z) {
-  if constexpr (K <= B) {
-    if (k == K) {
-      return low ? win_rows_expect<B, K, MODE, true>(si, ld, off, gp, gl, gt, rng, z)
-                 : win_rows_expect<B, K, MODE, false>(si, ld, off, gp, gl, gt, rng, z);
-    }
-    return win_expect_k<B, MODE, K + 1>(k, low, si, ld, off, gp, gl, gt, rng, z);
+#pragma unroll
+  for (int t = 0; t < B; ++t) zb.w[t] = za.w[t];
+  if (E.zrep) {
+    za.base = zc + wall - 2.f * sa;
+    zb.base = zc + wall - 2.f * sb;
+    za.scale = zb.scale = -2.f;
   } else {
-    return 0.0;
+    za.base = zc + sa;
+    zb.base = zc + sb;
+    za.scale = zb.scale = 1.f;
   }
+}
+
+template <int B>
+__device__ __forceinline__ float zpat(const ZCtx& z, unsigned pat, float zrow) {
+  float ws = 0.f;
+#pragma unroll
+  for (int t = 0; t < B; ++t)
+    if ((pat >> t) & 1u) ws += z.w[t];
+  return zrow + z.base + z.scale * ws;
 }
 
 // Sum over the CTA's 128 threads; the result is valid in thread 0.
@@ -172,65 +131,115 @@ __device__ __forceinline__ double block_sum_128(double a, double* sh) {
   return s;
 }
 
-template <int B, int MODE, bool EXPECT>
-__global__ void __launch_bounds__(STAGE_THREADS, 2) win_stage_kernel(const __grid_constant__ WinStageParams P) {
-  const int cta = blockIdx.x;
-  int ci = 0;
-  while (ci + 1 < P.n_classes && cta >= P.cls_cta0[ci + 1]) ++ci;
-  const int k = P.cls_k[ci];
-  const int local = cta - P.cls_cta0[ci];
-  const int g = local / P.tiles, tile = local - g * P.tiles;
+// Kahan step in FP32.
+__device__ __forceinline__ void kahan_add(float& acc, float& cmp, float v) {
+  const float y = v - cmp;
+  const float t = acc + y;
+  cmp = (t - acc) - y;
+  acc = t;
+}
+
+// Epilogues of a window stage: store, or the fused expectation (nothing stored).
+enum { EPI_STORE = 0, EPI_EXPECT = 2 };
+
+template <int B, int K, int KIND, bool LOW, int EPI>
+__global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI))
+    win_class_kernel(const __grid_constant__ WinJob P) {
+  constexpr int MODE = 2;
+  constexpr bool EXPECT = EPI == EPI_EXPECT;
+  const int g = blockIdx.x / P.tiles, tile = blockIdx.x - g * P.tiles;
   const long long col = (long long)tile * STAGE_THREADS + threadIdx.x;
   const bool active = col < P.ncols;
   if (!EXPECT && !active) return;
-  const bool low = P.low != 0;
-  long long row0;
-  const int* off;
-  if (low) {
-    row0 = P.tab[P.cls_off[ci] + g];
-    off = nullptr;
-  } else {
-    row0 = g;
-    off = P.tab + P.cls_off[ci];
-  }
-  const unsigned rng = dither_seed((unsigned long long)col, P.salt);
-  if constexpr (!EXPECT) {
-    const float2* si = P.in + row0 * P.ld + col;
-    float2* so = P.out + row0 * P.ld + col;
-    win_rows_k<B, MODE>(k, low, si, so, P.ld, off, P.gp, P.gl, P.gt, rng, P.ph_in ? P.ph_in + row0 : nullptr,
-                        P.ph_out ? P.ph_out + row0 : nullptr);
-  } else {
-    __shared__ double sh[STAGE_THREADS / 32];
-    double part = 0.0;
-    if (active) {
-      const StageExpect& E = P.ex;
-      const unsigned cstr = E.col_str[col];
-      // the orbitals outside the window are the same for every member: read member 0
-      const unsigned r0str = E.row_str[row0 + (low ? 0 : off[0])];
-      const unsigned wmask = ((1u << B) - 1u) << P.lo;
-      const unsigned outside = r0str & ~wmask;
-      ZCtx z;
-      float s_out = 0.f, w_all = 0.f;
+  const long long ra = LOW ? (long long)P.base_a[g] : (long long)(P.ga0 + g);
+  const long long rb = LOW ? (long long)P.base_b[g] : (long long)(P.gb0 + g);
+  unsigned rng = dither_seed((unsigned long long)col, P.salt);
+  const long long ld = P.ld;
+  // member j of group A (class K) / group B (class B - K): row offset from the group's base
+#define ROW_A(j) (LOW ? (long long)(j) : (long long)P.off_a[(j)])
+#define ROW_B(j) (LOW ? (long long)(j) : (long long)P.off_b[(j)])
+  double part = 0.0;
+  if (active) {
+    const float2* sa = P.in + ra * ld + col;
+    const float2* sb = P.in + rb * ld + col;
+    if constexpr (KIND == 0) {
+      constexpr int M = WinNet<B, K>::M;
+      float2 v[M];
 #pragma unroll
-      for (int t = 0; t < B; ++t) z.w[t] = 0.f;
-      for (int l = 0; l < P.norb; ++l) {
-        const float gcol = E.zrep ? (((cstr >> l) & 1u) ? -1.f : 1.f) : (float)((cstr >> l) & 1u);
+      for (int j = 0; j < M; ++j) v[j] = sa[ROW_A(j) * ld];
+      WinNet<B, K>::template apply<MODE>(v, P.gp, P.gl, P.gt, rng);
+      if constexpr (!EXPECT) {
+        // fresh copies: keeps the compiler from holding every member's offset
+        // live from the loads to the stores
+        float2* da = P.out + ra * ld + col;
+        long long ls = ld;
+        asm volatile("" : "+l"(da), "+l"(ls));
 #pragma unroll
-        for (int t = 0; t < B; ++t) z.w[t] += E.X[P.lo + t][l] * gcol;
-        for (unsigned o = outside; o; o &= o - 1) s_out += E.X[__ffs(o) - 1][l] * gcol;
-        w_all += E.Xsum[l] * gcol;
-      }
-      const float zc = E.zcol[col];
-      if (E.zrep) {
-        z.base = zc + w_all - 2.f * s_out;
-        z.scale = -2.f;
+        for (int j = 0; j < M; ++j) da[ROW_A(j) * ls] = v[j];
       } else {
-        z.base = zc + s_out;
-        z.scale = 1.f;
+        const StageExpect& E = P.ex;
+        const unsigned outside = E.row_str[ra + ROW_A(0)] & ~(((1u << B) - 1u) << P.lo);
+        ZCtx za, zb;
+        zctx_make<B>(E, P.norb, P.lo, E.col_str[col], outside, 0u, za, zb, E.zcol[col]);
+        float acc = 0.f, cmp = 0.f;
+#pragma unroll
+        for (int j = 0; j < M; ++j) {
+          const float z = zpat<B>(za, win_member(B, K, j), __ldg(E.zrow + ra + ROW_A(j)));
+          kahan_add(acc, cmp, z * (v[j].x * v[j].x + v[j].y * v[j].y));
+        }
+        part = (double)acc - (double)cmp;
       }
-      z.zrow = E.zrow + row0;
-      part = win_expect_k<B, MODE>(k, low, P.in + row0 * P.ld + col, P.ld, off, P.gp, P.gl, P.gt, rng, z);
+    } else {
+      using PK = WinPack<B, K>;
+      constexpr int NP = PK::NP;
+      constexpr bool PAIR = KIND == 2;
+      const float2* s1 = PAIR ? sb : sa;
+      const long long r1 = PAIR ? rb : ra;
+      float2 R[NP], I[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const float2 a = sa[ROW_A(PK::lane0(q)) * ld];
+        const float2 b = s1[(PAIR ? ROW_B(PK::lane1(q)) : ROW_A(PK::lane1(q))) * ld];
+        R[q] = make_float2(a.x, b.x);
+        I[q] = make_float2(a.y, b.y);
+      }
+      PK::template apply<MODE>(R, I, P.gp, P.gl, P.gt, rng);
+      if constexpr (!EXPECT) {
+        float2* da = P.out + ra * ld + col;
+        float2* db = P.out + r1 * ld + col;
+        long long ls = ld;
+        asm volatile("" : "+l"(da), "+l"(db), "+l"(ls));
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+          const long long o0 = ROW_A(PK::lane0(q)), o1 = PAIR ? ROW_B(PK::lane1(q)) : ROW_A(PK::lane1(q));
+          da[o0 * ls] = make_float2(R[q].x, I[q].x);
+          db[o1 * ls] = make_float2(R[q].y, I[q].y);
+        }
+      } else {
+        const StageExpect& E = P.ex;
+        const unsigned wmask = ((1u << B) - 1u) << P.lo;
+        const unsigned out_a = E.row_str[ra + ROW_A(0)] & ~wmask;
+        const unsigned out_b = PAIR ? (E.row_str[rb + ROW_B(0)] & ~wmask) : out_a;
+        ZCtx za, zb;
+        zctx_make<B>(E, P.norb, P.lo, E.col_str[col], out_a, out_b, za, zb, E.zcol[col]);
+        float acc = 0.f, cmp = 0.f;
+#pragma unroll
+        for (int q = 0; q < NP; ++q) {
+          const float z0 = zpat<B>(za, PK::pat0(q), __ldg(E.zrow + ra + ROW_A(PK::lane0(q))));
+          const float z1 = zpat<B>(PAIR ? zb : za, PK::pat1(q),
+                                   __ldg(E.zrow + r1 + (PAIR ? ROW_B(PK::lane1(q)) : ROW_A(PK::lane1(q)))));
+          const float2 m2 = __ffma2_rn(R[q], R[q], __fmul2_rn(I[q], I[q]));
+          kahan_add(acc, cmp, z0 * m2.x);
+          kahan_add(acc, cmp, z1 * m2.y);
+        }
+        part = (double)acc - (double)cmp;
+      }
     }
+  }
+#undef ROW_A
+#undef ROW_B
+  if constexpr (EXPECT) {
+    __shared__ double sh[STAGE_THREADS / 32];
     const double s = block_sum_128(part, sh);
     if (threadIdx.x == 0) P.ex.partials[blockIdx.x] = s;
   }
@@ -245,6 +254,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, 2) win_stage_kernel(const __gri
 // orbitals of active site t, read on the member whose lower orbital is
 // occupied.  Pairs with both or neither orbital occupied are left alone: the
 // 2x2 blocks of the plan have determinant 1.
+constexpr int CS_MAX_GPC = 8;  // groups per CTA of the cross-half stage (at most)
+
 struct CsStageParams {
   float2* x;
   long long ld, ncols;
@@ -252,8 +263,10 @@ struct CsStageParams {
   int n_classes;
   int cls_m[5];
   int cls_cta0[6];
-  int cls_base[5];  // first int of the class's groups in tab
+  int cls_base[5];    // first int of the class's groups in tab
+  int cls_groups[5];  // groups of the class
   int tiles;
+  int gpc;            // groups per CTA (one column tile each)
   float gp[24], gl[24];  // per site (c, Re t, Im t), see win_coef
   unsigned gt[24];
   unsigned salt;
@@ -295,18 +308,28 @@ __global__ void __launch_bounds__(STAGE_THREADS, 2) cs_stage_kernel(const __grid
   while (ci + 1 < P.n_classes && cta >= P.cls_cta0[ci + 1]) ++ci;
   const int m = P.cls_m[ci];
   const int local = cta - P.cls_cta0[ci];
-  const int g = local / P.tiles, tile = local - g * P.tiles;
+  const int chunk = local / P.tiles, tile = local - chunk * P.tiles;
   const long long col = (long long)tile * STAGE_THREADS + threadIdx.x;
+  const int g0 = chunk * P.gpc, g1 = min(g0 + P.gpc, P.cls_groups[ci]);
+  // this CTA's group tables, staged once in shared memory
+  __shared__ int sent[CS_MAX_GPC * 17];
+  const int stride = 1 + (1 << m);
+  const int n_ent = (g1 - g0) * stride;
+  const int* src = P.tab + P.cls_base[ci] + (long long)g0 * stride;
+  for (int i = threadIdx.x; i < n_ent; i += STAGE_THREADS) sent[i] = src[i];
+  __syncthreads();
   if (col >= P.ncols) return;
-  const int* ent = P.tab + P.cls_base[ci] + (long long)g * (1 + (1 << m));
   const unsigned rng = dither_seed((unsigned long long)col, P.salt);
   float2* xc = P.x + col;
-  switch (m) {
-    case 1: cs_group<1, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-    case 2: cs_group<2, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-    case 3: cs_group<3, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-    case 4: cs_group<4, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-    default: break;
+  for (int g = g0; g < g1; ++g) {
+    const int* ent = sent + (g - g0) * stride;
+    switch (m) {
+      case 1: cs_group<1, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
+      case 2: cs_group<2, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
+      case 3: cs_group<3, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
+      case 4: cs_group<4, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
+      default: break;
+    }
   }
 }
 
