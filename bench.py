@@ -15,9 +15,12 @@ Reported:
 * e2e        the same through the public API ``ffsim_gb300.lucj_energy`` with
              host (numpy) inputs and the energy read back every step.
 * complex128 the plain complex128 GPU path on the same GPU (fewer steps).
-* roofline   the dominant kernel (two-pass orbital rotation, 4 S algorithmic
-             bytes per rotation with S the state size) against the measured
-             copy bandwidth in MEASURED_PEAKS.json.
+* roofline   the dominant kernel (one window stage of the stage-major
+             rotation: 2 S algorithmic bytes, S the state size, timed with
+             CUDA events through ffgb_debug_stage) against the measured copy
+             bandwidth in MEASURED_PEAKS.json; the cross-half pass, a full
+             orbital rotation (4 S) and the whole evaluation (S (6 L + 3 (R+1)),
+             the final UCJ rotation merged into every term) beside it.
 * cpu_baseline the C/OpenMP restatement of the reference CPU algorithm on a
              bounded sample (one orbital rotation + one diag-Coulomb evolution
              at norb=16, complex128), extrapolated to one evaluation.
@@ -163,10 +166,18 @@ def time_e2e(steps, ucj, ham):
     return (t1 - t0) / steps
 
 
-def rotation_roofline(stream, reps: int = 6):
-    """Average time of one complex64 orbital rotation (two transposing passes of
-    the sector kernel) on a resident norb=16 state, and its algorithmic GB/s."""
-    import numpy as np
+# DRAM bytes (read + write) of one 8-orbital window stage at norb=16 (8,8)
+# complex64, summed over its class launches, from the ncu launch list in
+# profiles/window_stage_norb16_c64.md.
+WINDOW_STAGE_TRAFFIC = 2.386e9
+
+
+def stage_rooflines(stream, reps: int = 8):
+    """CUDA-event times of single stages and of a full orbital rotation on a
+    resident norb=16 complex64 state, with their algorithmic bytes:
+    a window stage or the cross-half pass reads and writes the state once
+    (2 S); a two-sector orbital rotation is 4 S (one read and one write per
+    sector)."""
     import torch
 
     import ffsim_gb300 as f
@@ -175,30 +186,109 @@ def rotation_roofline(stream, reps: int = 6):
 
     d = f.dim(NORB, NELEC)
     S = d * 8
-    u = f.random.random_unitary(NORB, seed=99)
+    u = _lib.cmat(f.random.random_unitary(NORB, seed=99))
+    out = {}
     with torch.cuda.stream(stream):
         v = torch.randn(d, dtype=torch.complex64, device="cuda")
+        v /= torch.linalg.vector_norm(v)
         buf, nbytes = scratch(v, 0, NORB, *NELEC)
-        m = _lib.cmat(u)
         sptr = stream.cuda_stream
+
+        def timed(fn):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / reps
+
+        def stage(k):
+            return lambda: _lib.call("ffgb_debug_stage", v.data_ptr(), _lib.FFGB_C64, NORB, NELEC[0], NELEC[1],
+                                     _lib.dptr(u), k, sptr)
 
         def rot():
             _lib.call("ffgb_apply_orbital_rotation", v.data_ptr(), _lib.FFGB_C64, NORB, NELEC[0], NELEC[1],
-                      _lib.dptr(m), _lib.dptr(m), buf.data_ptr(), nbytes, sptr)
+                      _lib.dptr(u), _lib.dptr(u), buf.data_ptr(), nbytes, sptr)
 
+        out["window_stage_ms"] = timed(stage(0))
+        out["cross_half_pass_ms"] = timed(stage(2)) / 2  # the stage is two passes of four sites
+        out["rotation_ms"] = timed(rot)
+    del v, buf
+    torch.cuda.empty_cache()
+    out["S"] = S
+    return out
+
+
+def run_ops(args) -> None:
+    """Per-operation GB/s on a resident state (--ops): one JSON line per op,
+    each against its algorithmic bytes (S = state bytes)."""
+    import numpy as np
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _lib
+    from ffsim_gb300._state import scratch
+
+    norb = args.norb
+    nelec = (norb // 2, norb - norb // 2)
+    d = f.dim(norb, nelec)
+    dtype = torch.complex64 if args.dtype == "c64" else torch.complex128
+    code = _lib.FFGB_C64 if args.dtype == "c64" else _lib.FFGB_C128
+    el = 8 if args.dtype == "c64" else 16
+    S = d * el
+    peak, peak_kind = _peaks()
+    rng = np.random.default_rng(7)
+    u = _lib.cmat(f.random.random_unitary(norb, seed=rng))
+    jm = np.asarray(f.random.random_symmetric_matrix_normal(norb, scale=0.1, seed=rng), dtype=np.float64)
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        v = torch.randn(d, dtype=dtype, device="cuda")
+        v /= torch.linalg.vector_norm(v)
+        out = torch.empty_like(v)
+        buf, nbytes = scratch(v, 1, norb, *nelec)
+
+    def timed(fn):
         for _ in range(2):
-            rot()
+            fn()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for _ in range(reps):
-            rot()
+        for _ in range(args.reps):
+            fn()
         b.record(stream)
         torch.cuda.synchronize()
-    ms = a.elapsed_time(b) / reps
-    del v, buf
-    torch.cuda.empty_cache()
-    return ms, 4 * S / (ms * 1e-3) / 1e9, S, np
+        return a.elapsed_time(b) / args.reps
+
+    ops = {
+        "window_stage": (2 * S, lambda: _lib.call("ffgb_debug_stage", v.data_ptr(), code, norb, nelec[0], nelec[1],
+                                                  _lib.dptr(u), 0, sptr)),
+        "cross_half_stage": (2 * S, lambda: _lib.call("ffgb_debug_stage", v.data_ptr(), code, norb, nelec[0],
+                                                      nelec[1], _lib.dptr(u), 2, sptr)),
+        "orbital_rotation": (4 * S, lambda: _lib.call("ffgb_apply_orbital_rotation", v.data_ptr(), code, norb,
+                                                      nelec[0], nelec[1], _lib.dptr(u), _lib.dptr(u),
+                                                      buf.data_ptr(), nbytes, sptr)),
+        "diag_coulomb_evolution": (2 * S, lambda: _lib.call(
+            "ffgb_apply_diag_coulomb_evolution", v.data_ptr(), code, norb, nelec[0], nelec[1], _lib.dptr(jm),
+            _lib.dptr(jm), _lib.dptr(jm), 1.0, 0, None, None, buf.data_ptr(), nbytes, sptr)),
+        "rotated_diag_matvec": (9 * S, lambda: _lib.call(
+            "ffgb_rotated_diag_matvec", v.data_ptr(), out.data_ptr(), code, norb, nelec[0], nelec[1], None,
+            _lib.dptr(jm), 0, _lib.dptr(u), 1, buf.data_ptr(), nbytes, sptr)),
+    }
+    for name, (nb, fn) in ops.items():
+        try:
+            ms = timed(fn)
+            gbs = nb / (ms * 1e-3) / 1e9
+            line = {"op": name, "norb": norb, "nelec": list(nelec), "dtype": args.dtype, "ms": ms,
+                    "algorithmic_bytes": nb, "GB/s": gbs, "frac": gbs / peak, "peak": peak,
+                    "peak_kind": peak_kind}
+        except Exception as exc:  # noqa: BLE001
+            line = {"op": name, "norb": norb, "dtype": args.dtype, "unsupported": str(exc)}
+        print(json.dumps(line), flush=True)
 
 
 def cpu_reference_sample(threads: int | None = None):
@@ -264,8 +354,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--c128-steps", type=int, default=2)
+    ap.add_argument("--ops", action="store_true", help="per-operation GB/s lines instead of the energy metric")
+    ap.add_argument("--norb", type=int, default=NORB, help="--ops: orbitals (half filling)")
+    ap.add_argument("--dtype", default="c64", choices=["c64", "c128"], help="--ops: state dtype")
+    ap.add_argument("--reps", type=int, default=5, help="--ops: timed repetitions per op")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.ops:
+        run_ops(args)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -324,8 +421,11 @@ def main():
                                               ham.one_body_tensor, ham.diag_coulomb_mats, ham.orbital_rotations))
 
     # dominant kernel roofline
-    rot_ms, gbs, S, _ = rotation_roofline(stream)
+    st = stage_rooflines(stream)
+    S = st["S"]
     peak, peak_kind = _peaks()
+    gbs = 2 * S / (st["window_stage_ms"] * 1e-3) / 1e9
+    eval_bytes = (6 * N_REPS + 3 * (RANK + 1)) * S
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -356,9 +456,19 @@ def main():
             "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": 8 * (RANK + 2)},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
-                         "frac": gbs / peak, "traffic": None,
-                         "kernel": "sector_kernel<float,16> (two transposing passes = one orbital rotation)",
-                         "bytes_per_launch": 2 * S, "ms_per_rotation": rot_ms, "peak_kind": peak_kind},
+                         "frac": gbs / peak, "traffic": WINDOW_STAGE_TRAFFIC,
+                         "kernel": "win_class_kernel: one 8-orbital window stage (one launch per electron-count "
+                                   "class), 2 S algorithmic bytes",
+                         "algorithmic_bytes": 2 * S, "ms": st["window_stage_ms"],
+                         "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                         "others": {
+                             "cross_half_pass": {"ms": st["cross_half_pass_ms"],
+                                                 "GB/s": 2 * S / (st["cross_half_pass_ms"] * 1e-3) / 1e9},
+                             "orbital_rotation": {"ms": st["rotation_ms"], "algorithmic_bytes": 4 * S,
+                                                  "GB/s": 4 * S / (st["rotation_ms"] * 1e-3) / 1e9},
+                             "energy_eval": {"ms": total_ms / args.steps, "algorithmic_bytes": eval_bytes,
+                                             "GB/s": eval_bytes / (total_ms / args.steps * 1e-3) / 1e9,
+                                             "frac": eval_bytes / (total_ms / args.steps * 1e-3) / 1e9 / peak}}},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),

@@ -45,6 +45,7 @@ SIGNATURES = {
     "ffgb_givens_decomposition": [_dp, _c_int, _c_double, _dp, _ip, _ip, _dp],
     "ffgb_eigh": [_dp, _c_int, _dp, _dp],
     "ffgb_debug_plan": [_dp, _c_int, _c_int, _dp, _c_int, _ip],
+    "ffgb_debug_stage": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _c_int, _c_void_p],
     "ffgb_scratch_bytes": [_c_int, _c_int, _c_int, _c_int, _c_int],
     "ffgb_apply_givens_rotation": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_double,
                                    _c_double, _c_double, _c_int, _c_int, _c_void_p],

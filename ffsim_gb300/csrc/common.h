@@ -57,6 +57,7 @@ struct StageOpts {
   unsigned salt = 0;        // decorrelates the dithering of different rotations
   const StageExpectArgs* expect = nullptr;  // last stage reduces instead of storing
   int* expect_ctas = nullptr;               // partials written by the fused expectation
+  int only_stage = -1;  // >= 0: run only this stage (0 B1, 1 B2, 2 cross-half, 3 A1, 4 A2), in place
 };
 
 // Stage-major complex64 rotation of the sector whose strings index the rows

@@ -1157,6 +1157,22 @@ int ffgb_debug_plan(const double* mat, int norb, int use_windows, double* out, i
   return FFGB_OK;
 }
 
+int ffgb_debug_stage(void* vec, int dtype, int norb, int na, int nb, const double* mat, int stage,
+                     void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (dtype != FFGB_C64 || nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "stage kernels run on spinful complex64 states");
+  if (!mat) return fail(FFGB_ERR_ARG, "mat must not be NULL");
+  SectorPlan p;
+  FFGB_TRY(make_plan<float>(norb, load_mat(mat, norb), p));
+  if (p.kind != PLAN_CSD) return fail(FFGB_ERR_UNSUPPORTED, "no cosine-sine plan for this norb");
+  StageOpts o;
+  o.mode = STAGE_MODE;
+  o.only_stage = stage;
+  const long long db = binom_h(norb, nb);
+  return stage_rotate_rows(vec, vec, norb, na, db, db, p, o, (cudaStream_t)stream);
+}
+
 size_t ffgb_scratch_bytes(int op, int dtype, int norb, int na, int nb) {
   const size_t el = dtype == FFGB_C128 ? 16 : 8;
   const long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;

@@ -181,33 +181,33 @@ int cs_pass_tables(int norb, int nocc, int h, int s0, int s1, const CsPass** out
   return FFGB_OK;
 }
 
+template <int M>
+int launch_cs(const CsStageParams& P, int grid, int mode, cudaStream_t st) {
+  if (mode == 0)
+    cs_stage_kernel<M, 0><<<grid, STAGE_THREADS, 0, st>>>(P);
+  else if (mode == 1)
+    cs_stage_kernel<M, 1><<<grid, STAGE_THREADS, 0, st>>>(P);
+  else
+    cs_stage_kernel<M, 2><<<grid, STAGE_THREADS, 0, st>>>(P);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+
 int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h, const std::vector<Pair2>& cs,
              int mode, unsigned salt, cudaStream_t st) {
   for (int s0 = 0; s0 < h; s0 += 4) {
     const int s1 = std::min(h, s0 + 4);
     const CsPass* T = nullptr;
     FFGB_TRY(cs_pass_tables(norb, nocc, h, s0, s1, &T));
-    if (T->n_classes == 0) continue;
     CsStageParams P;
     std::memset(&P, 0, sizeof(P));
     P.x = x;
     P.ld = ld;
     P.ncols = ncols;
-    P.tab = T->tab;
-    P.n_classes = T->n_classes;
     P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
     P.salt = salt * 0x9E3779B9u + 0x51ED270Bu * (unsigned)(s0 + 1);
     P.gpc = CS_MAX_GPC;
-    long long cta = 0;
-    for (int c = 0; c < T->n_classes; ++c) {
-      P.cls_m[c] = T->cls_m[c];
-      P.cls_base[c] = T->cls_base[c];
-      P.cls_groups[c] = T->cls_groups[c];
-      P.cls_cta0[c] = (int)cta;
-      cta += (long long)((T->cls_groups[c] + P.gpc - 1) / P.gpc) * P.tiles;
-    }
-    P.cls_cta0[T->n_classes] = (int)cta;
-    if (cta > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
     double v[24] = {};
     for (int i = 0; i < h && i < 8; ++i) {
       v[3 * i] = cs[i].g00.real();
@@ -215,15 +215,20 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h
       v[3 * i + 2] = cs[i].g01.imag();
     }
     put_coefs(v, 24, mode, P.gp, P.gl, P.gt);
-    if (cta == 0) continue;
-    if (mode == 0)
-      cs_stage_kernel<0><<<(unsigned)cta, STAGE_THREADS, 0, st>>>(P);
-    else if (mode == 1)
-      cs_stage_kernel<1><<<(unsigned)cta, STAGE_THREADS, 0, st>>>(P);
-    else
-      cs_stage_kernel<2><<<(unsigned)cta, STAGE_THREADS, 0, st>>>(P);
-    count_launch();
-    FFGB_CUDA(cudaGetLastError());
+    for (int c = 0; c < T->n_classes; ++c) {
+      P.tab = T->tab + T->cls_base[c];
+      P.n_groups = T->cls_groups[c];
+      const long long grid = (long long)((P.n_groups + P.gpc - 1) / P.gpc) * P.tiles;
+      if (grid <= 0) continue;
+      if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
+      switch (T->cls_m[c]) {
+        case 1: FFGB_TRY(launch_cs<1>(P, (int)grid, mode, st)); break;
+        case 2: FFGB_TRY(launch_cs<2>(P, (int)grid, mode, st)); break;
+        case 3: FFGB_TRY(launch_cs<3>(P, (int)grid, mode, st)); break;
+        case 4: FFGB_TRY(launch_cs<4>(P, (int)grid, mode, st)); break;
+        default: return fail(FFGB_ERR_ARG, "bad cross-half class");
+      }
+    }
   }
   return FFGB_OK;
 }
@@ -370,6 +375,17 @@ int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long l
   float2* dst = (float2*)out;
   if (o.mode != 2) return fail(FFGB_ERR_ARG, "stage kernels use dithered coefficients");
   const unsigned s = o.salt * 0x2545F491u;
+  switch (o.only_stage) {
+    case -1: break;
+    case 0: return window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, s + 1, nullptr, nullptr, st);
+    case 1: return window_stage(src, dst, ld, ncols, norb, nocc, T, false, plan.b2, s + 2, nullptr, nullptr, st);
+    case 2:
+      if (in != out) return fail(FFGB_ERR_ARG, "the cross-half stage runs in place");
+      return cs_stage(dst, ld, ncols, norb, nocc, plan.h, plan.cs, o.mode, s + 3, st);
+    case 3: return window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.a1, s + 4, nullptr, nullptr, st);
+    case 4: return window_stage(src, dst, ld, ncols, norb, nocc, T, false, plan.a2, s + 5, nullptr, nullptr, st);
+    default: return fail(FFGB_ERR_ARG, "stage must be in [0, 4]");
+  }
   FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, s + 1, nullptr, nullptr, st));
   FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.b2, s + 2, nullptr, nullptr, st));
   FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, plan.h, plan.cs, o.mode, s + 3, st));

@@ -259,32 +259,21 @@ constexpr int CS_MAX_GPC = 8;  // groups per CTA of the cross-half stage (at mos
 struct CsStageParams {
   float2* x;
   long long ld, ncols;
-  const int* tab;
-  int n_classes;
-  int cls_m[5];
-  int cls_cta0[6];
-  int cls_base[5];    // first int of the class's groups in tab
-  int cls_groups[5];  // groups of the class
+  const int* tab;  // this class's groups, (1 + 2^M) ints each
+  int n_groups;
   int tiles;
-  int gpc;            // groups per CTA (one column tile each)
+  int gpc;  // groups per CTA (one column tile each), an even number <= CS_MAX_GPC
   float gp[24], gl[24];  // per site (c, Re t, Im t), see win_coef
   unsigned gt[24];
   unsigned salt;
 };
 
+// One group's cross-half rotations on registers; e[j] = row | sign bits.
 template <int M, int MODE>
-static __device__ __noinline__ void cs_group(float2* __restrict__ xc, long long ld, const int* __restrict__ ent,
-                                             const float* __restrict__ gp, const float* __restrict__ gl,
-                                             const unsigned* __restrict__ gt, unsigned rng) {
+__device__ __forceinline__ void cs_rotate(float2 (&v)[1 << M], const int (&e)[1 << M], int sites,
+                                          const float* __restrict__ gp, const float* __restrict__ gl,
+                                          const unsigned* __restrict__ gt, unsigned rng) {
   constexpr int NM = 1 << M;
-  const int sites = ent[0];
-  int e[NM];
-  float2 v[NM];
-#pragma unroll
-  for (int j = 0; j < NM; ++j) {
-    e[j] = ent[1 + j];
-    v[j] = xc[(long long)(e[j] & 0xffffff) * ld];
-  }
 #pragma unroll
   for (int t = 0; t < M; ++t) {
     const int site = (sites >> (3 * t)) & 7;
@@ -297,38 +286,51 @@ static __device__ __noinline__ void cs_group(float2* __restrict__ xc, long long 
       rot_pair<MODE == 1>(v[j], v[j | (1 << t)], c, sg * sr, sg * si, cl, sg * srl, sg * sil);
     }
   }
-#pragma unroll
-  for (int j = 0; j < NM; ++j) xc[(long long)(e[j] & 0xffffff) * ld] = v[j];
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(STAGE_THREADS, 2) cs_stage_kernel(const __grid_constant__ CsStageParams P) {
-  const int cta = blockIdx.x;
-  int ci = 0;
-  while (ci + 1 < P.n_classes && cta >= P.cls_cta0[ci + 1]) ++ci;
-  const int m = P.cls_m[ci];
-  const int local = cta - P.cls_cta0[ci];
-  const int chunk = local / P.tiles, tile = local - chunk * P.tiles;
+// Groups with M active sites; each thread takes two groups at a time so that
+// both groups' loads are in flight together.
+template <int M, int MODE>
+__global__ void __launch_bounds__(STAGE_THREADS, M >= 4 ? 4 : 6) cs_stage_kernel(const __grid_constant__ CsStageParams P) {
+  constexpr int NM = 1 << M;
+  constexpr int STRIDE = 1 + NM;
+  const int chunk = blockIdx.x / P.tiles, tile = blockIdx.x - chunk * P.tiles;
   const long long col = (long long)tile * STAGE_THREADS + threadIdx.x;
-  const int g0 = chunk * P.gpc, g1 = min(g0 + P.gpc, P.cls_groups[ci]);
+  const int g0 = chunk * P.gpc, g1 = min(g0 + P.gpc, P.n_groups);
   // this CTA's group tables, staged once in shared memory
   __shared__ int sent[CS_MAX_GPC * 17];
-  const int stride = 1 + (1 << m);
-  const int n_ent = (g1 - g0) * stride;
-  const int* src = P.tab + P.cls_base[ci] + (long long)g0 * stride;
+  const int n_ent = (g1 - g0) * STRIDE;
+  const int* src = P.tab + (long long)g0 * STRIDE;
   for (int i = threadIdx.x; i < n_ent; i += STAGE_THREADS) sent[i] = src[i];
   __syncthreads();
   if (col >= P.ncols) return;
   const unsigned rng = dither_seed((unsigned long long)col, P.salt);
   float2* xc = P.x + col;
-  for (int g = g0; g < g1; ++g) {
-    const int* ent = sent + (g - g0) * stride;
-    switch (m) {
-      case 1: cs_group<1, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-      case 2: cs_group<2, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-      case 3: cs_group<3, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-      case 4: cs_group<4, MODE>(xc, P.ld, ent, P.gp, P.gl, P.gt, rng); break;
-      default: break;
+  const long long ld = P.ld;
+  for (int g = g0; g < g1; g += 2) {
+    const bool two = g + 1 < g1;
+    const int* ea = sent + (g - g0) * STRIDE;
+    const int* eb = two ? ea + STRIDE : ea;
+    int e0[NM], e1[NM];
+    float2 v0[NM], v1[NM];
+#pragma unroll
+    for (int j = 0; j < NM; ++j) {
+      e0[j] = ea[1 + j];
+      e1[j] = eb[1 + j];
+    }
+#pragma unroll
+    for (int j = 0; j < NM; ++j) v0[j] = xc[(long long)(e0[j] & 0xffffff) * ld];
+    if (two) {
+#pragma unroll
+      for (int j = 0; j < NM; ++j) v1[j] = xc[(long long)(e1[j] & 0xffffff) * ld];
+    }
+    cs_rotate<M, MODE>(v0, e0, ea[0], P.gp, P.gl, P.gt, rng);
+#pragma unroll
+    for (int j = 0; j < NM; ++j) xc[(long long)(e0[j] & 0xffffff) * ld] = v0[j];
+    if (two) {
+      cs_rotate<M, MODE>(v1, e1, eb[0], P.gp, P.gl, P.gt, rng);
+#pragma unroll
+      for (int j = 0; j < NM; ++j) xc[(long long)(e1[j] & 0xffffff) * ld] = v1[j];
     }
   }
 }

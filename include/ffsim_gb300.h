@@ -73,6 +73,14 @@ int ffgb_eigh(const double* mat, int n, double* eigvals, double* vecs);
  * coefficients.  Returns the number of doubles written in *len. */
 int ffgb_debug_plan(const double* mat, int norb, int use_windows, double* out, int cap, int* len);
 
+/* One stage of the complex64 cosine-sine plan of W(mat) on the alpha sector of
+ * vec, in place (stage 0/1: first lower/upper window, 2: cross-half pass,
+ * 3/4: second lower/upper window).  A diagnostic for timing a single kernel
+ * stage; the result alone is not a meaningful state.  No counterpart in the
+ * reference. */
+int ffgb_debug_stage(void* vec, int dtype, int norb, int n_alpha, int n_beta, const double* mat, int stage,
+                     void* stream);
+
 /* Scratch bytes needed by the functions below for a state of the given
  * shape (op: 0 = orbital rotation / evolutions, 1 = linear operator matvec,
  * 2 = expectation / energy). */
