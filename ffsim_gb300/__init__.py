@@ -10,6 +10,7 @@ hand-written sm_103a kernels through the C ABI in ``include/ffsim_gb300.h``.
 from ffsim_gb300 import contract, linalg, random, states
 from ffsim_gb300._state import dim, dims
 from ffsim_gb300.energy import LUCJEnergy, lucj_energy
+from ffsim_gb300.gradient import LUCJGradient, lucj_energy_autograd
 from ffsim_gb300.gates import (
     apply_diag_coulomb_evolution,
     apply_givens_rotation_in_place,
@@ -23,6 +24,8 @@ from ffsim_gb300.states import hartree_fock_state, vdot
 from ffsim_gb300.variational import UCJOpSpinBalanced
 
 __all__ = [
+    "LUCJGradient",
+    "lucj_energy_autograd",
     "DoubleFactorizedHamiltonian",
     "LUCJEnergy",
     "LinearOperator",

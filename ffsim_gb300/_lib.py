@@ -74,6 +74,10 @@ SIGNATURES = {
                             _c_double, _c_int, _dp, _dp, _c_void_p, _c_size_t, _c_void_p],
     "ffgb_lucj_energy": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _dp, _dp, _dp,
                          _dp, _c_int, _dp, _dp, _c_double, _dp, _c_void_p, _c_size_t, _c_void_p],
+    "ffgb_transition_rdm1": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _c_void_p, _c_size_t,
+                             _c_void_p],
+    "ffgb_pair_density": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _c_void_p, _c_size_t,
+                          _c_void_p],
     "ffgb_vdot": [_c_void_p, _c_void_p, _c_int, _c_ll, _dp, _c_void_p],
     "ffgb_hartree_fock": [_c_void_p, _c_int, _c_ll, _c_void_p],
 }

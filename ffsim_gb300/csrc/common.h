@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/ffsim_gb300.h"
 #include "kernels.cuh"
@@ -68,6 +69,16 @@ int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long l
 
 // Upper bound of the partial sums written by a fused expectation over ncols columns.
 long long stage_expect_partials(int norb, long long ncols);
+
+// Densities between two states (grad.cu); results summed on the host in FP64.
+template <typename T>
+int rdm1_rows(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
+              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st);
+template <typename T>
+int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
+              int norb, void* partial_buf, size_t partial_bytes, std::vector<double>& rr, std::vector<double>& rc,
+              cudaStream_t st);
+size_t density_partial_bytes(int norb, long long rows);
 template <typename T>
 int launch_transpose(const void* in, void* out, long long rows, long long cols, const void* row_ph,
                      const void* col_ph, cudaStream_t st);

@@ -1068,6 +1068,41 @@ static int contract_static_impl(const void* vec, void* out, int norb, int na, in
   return run_pass<T>(A, scr, st);
 }
 
+// Densities between two states: the beta sector runs on transposed copies.
+template <typename T>
+static int densities(const void* x, const void* y, int norb, int na, int nb, bool pair, double* out,
+                     Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  const unsigned *sa = nullptr, *sb = nullptr;
+  FFGB_TRY(device_strings(norb, na, &sa));
+  FFGB_TRY(device_strings(norb, nb, &sb));
+  const size_t S = (size_t)(da * db) * sizeof(C);
+  void* tx = scr.take(S);
+  void* ty = scr.take(S);
+  const size_t pbytes = std::max(density_partial_bytes(norb, da), density_partial_bytes(norb, db));
+  void* part = scr.take(pbytes);
+  if (!tx || !ty || !part) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
+  FFGB_TRY(launch_transpose<T>(x, tx, da, db, nullptr, nullptr, st));
+  FFGB_TRY(launch_transpose<T>(y, ty, da, db, nullptr, nullptr, st));
+  const size_t n2 = 2 * (size_t)norb * norb;
+  if (!pair) {
+    std::vector<double> ga, gb;
+    FFGB_TRY(rdm1_rows<T>(x, y, sa, (int)da, (int)db, norb, part, pbytes, ga, st));
+    FFGB_TRY(rdm1_rows<T>(tx, ty, sb, (int)db, (int)da, norb, part, pbytes, gb, st));
+    std::memcpy(out, ga.data(), n2 * sizeof(double));
+    std::memcpy(out + n2, gb.data(), n2 * sizeof(double));
+  } else {
+    std::vector<double> aa, ab, bb, ba;
+    FFGB_TRY(pair_rows<T>(x, y, sa, sb, (int)da, (int)db, norb, part, pbytes, aa, ab, st));
+    FFGB_TRY(pair_rows<T>(tx, ty, sb, sa, (int)db, (int)da, norb, part, pbytes, bb, ba, st));
+    std::memcpy(out, aa.data(), n2 * sizeof(double));
+    std::memcpy(out + n2, ab.data(), n2 * sizeof(double));
+    std::memcpy(out + 2 * n2, bb.data(), n2 * sizeof(double));
+  }
+  return FFGB_OK;
+}
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
@@ -1179,6 +1214,10 @@ size_t ffgb_scratch_bytes(int op, int dtype, int norb, int na, int nb) {
   const size_t S = (size_t)da * db * el;
   const size_t ex = extras_bytes(norb, na, nb) + 4096;
   if (op == 1 || op == 2) return 2 * S + ex;
+  if (op == 3) {
+    const long long m = std::max<long long>(std::max(da, db), 1);
+    return 2 * S + density_partial_bytes(norb, m) + ex;
+  }
   return S + ex;
 }
 
@@ -1455,6 +1494,30 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
   return FFGB_DISPATCH(dtype,
                        df_expectation_impl<float>(work, norb, na, nb, terms, &final_basis, constant, energy_out, scr, st),
                        df_expectation_impl<double>(work, norb, na, nb, terms, &final_basis, constant, energy_out, scr, st));
+}
+
+int ffgb_transition_rdm1(const void* x, const void* y, int dtype, int norb, int na, int nb, double* out,
+                         void* scratch, size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "densities need a spinful system");
+  if (!out) return fail(FFGB_ERR_ARG, "out must not be NULL");
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype, densities<float>(x, y, norb, na, nb, false, out, scr, st),
+                       densities<double>(x, y, norb, na, nb, false, out, scr, st));
+}
+
+int ffgb_pair_density(const void* x, const void* y, int dtype, int norb, int na, int nb, double* out,
+                      void* scratch, size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "densities need a spinful system");
+  if (!out) return fail(FFGB_ERR_ARG, "out must not be NULL");
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype, densities<float>(x, y, norb, na, nb, true, out, scr, st),
+                       densities<double>(x, y, norb, na, nb, true, out, scr, st));
 }
 
 int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out, void* stream) {

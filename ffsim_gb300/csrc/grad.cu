@@ -1,0 +1,236 @@
+// Reduced densities between two states, for the adjoint gradient of the LUCJ
+// energy:
+//   transition one-body density  G^s_pq = <x| a+_{p s} a_{q s} |y>
+//   diagonal pair density        P^{st}_ij = <x| n_{i s} n_{j t} |y>
+// Both are accumulated in FP64 from complex64 or complex128 states, per CTA,
+// and the partial sums are reduced on the host in a fixed order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.h"
+
+namespace ffgb {
+
+namespace {
+
+constexpr int DTHREADS = 256;
+constexpr int RDM_ROWS = 16;  // rows of the rotated sector per CTA
+
+template <typename C>
+__device__ __forceinline__ double2 cdot_acc(double2 acc, C a, C b) {  // acc += conj(a) * b
+  acc.x += (double)a.x * (double)b.x + (double)a.y * (double)b.y;
+  acc.y += (double)a.x * (double)b.y - (double)a.y * (double)b.x;
+  return acc;
+}
+
+__device__ __forceinline__ double2 block_sum2(double2 v, double2* sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+  }
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double2 s = make_double2(0.0, 0.0);
+  if (threadIdx.x == 0)
+    for (int w = 0; w < DTHREADS / 32; ++w) {
+      s.x += sh[w].x;
+      s.y += sh[w].y;
+    }
+  __syncthreads();
+  return s;
+}
+
+// One (p, q) pair (blockIdx.y) over a chunk of rows (blockIdx.x) of the rotated
+// sector, whose strings index the rows; columns = the other sector.
+template <typename T>
+__global__ void __launch_bounds__(DTHREADS) rdm1_kernel(const typename CT<T>::type* __restrict__ x,
+                                                        const typename CT<T>::type* __restrict__ y,
+                                                        const unsigned* __restrict__ strings, int rows, int cols,
+                                                        int norb, double2* __restrict__ partial) {
+  __shared__ int sB[FFGB_BST * FFGB_BST];
+  __shared__ double2 sh[DTHREADS / 32];
+  for (int idx = threadIdx.x; idx < FFGB_BST * FFGB_BST; idx += DTHREADS) {
+    const int a = idx / FFGB_BST, b = idx % FFGB_BST;
+    long long r = 0;
+    if (b <= a) {
+      r = 1;
+      for (int i = 1; i <= b; ++i) r = r * (a - b + i) / i;
+    }
+    sB[idx] = (int)r;
+  }
+  __syncthreads();
+  const int pair = blockIdx.y, p = pair / norb, q = pair - p * norb;
+  const int a0 = blockIdx.x * RDM_ROWS, a1 = min(a0 + RDM_ROWS, rows);
+  double2 acc = make_double2(0.0, 0.0);
+  for (int a = a0; a < a1; ++a) {
+    const unsigned s = strings[a];
+    if (!((s >> q) & 1u)) continue;
+    unsigned t = s;
+    int sign = 0;
+    if (p != q) {
+      if ((s >> p) & 1u) continue;
+      const unsigned r1 = s & ~(1u << q);
+      sign = (__popc(s & ((1u << q) - 1u)) + __popc(r1 & ((1u << p) - 1u))) & 1;
+      t = r1 | (1u << p);
+    }
+    const long long ap = rank_colex(t, sB);
+    const auto* xr = x + ap * cols;
+    const auto* yr = y + (long long)a * cols;
+    double2 d = make_double2(0.0, 0.0);
+    for (int c = threadIdx.x; c < cols; c += DTHREADS) d = cdot_acc(d, xr[c], yr[c]);
+    if (sign) {
+      d.x = -d.x;
+      d.y = -d.y;
+    }
+    acc.x += d.x;
+    acc.y += d.y;
+  }
+  const double2 s = block_sum2(acc, sh);
+  if (threadIdx.x == 0) partial[(long long)pair * gridDim.x + blockIdx.x] = s;
+}
+
+// Pair densities within the row sector (P^rr_ij, rows i, j) and between the
+// row and column sectors (P^rc_ij) over a chunk of rows.
+template <typename T>
+__global__ void __launch_bounds__(DTHREADS) pair_density_kernel(const typename CT<T>::type* __restrict__ x,
+                                                                const typename CT<T>::type* __restrict__ y,
+                                                                const unsigned* __restrict__ rstr,
+                                                                const unsigned* __restrict__ cstr, int rows,
+                                                                int cols, int norb, double2* __restrict__ partial) {
+  __shared__ double2 sh[DTHREADS / 32];
+  __shared__ double2 acc_rr[FFGB_MAXN * FFGB_MAXN], acc_rc[FFGB_MAXN * FFGB_MAXN];
+  __shared__ double2 red[FFGB_MAXN + 1];
+  for (int i = threadIdx.x; i < FFGB_MAXN * FFGB_MAXN; i += DTHREADS) {
+    acc_rr[i] = make_double2(0.0, 0.0);
+    acc_rc[i] = make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const int a0 = blockIdx.x * RDM_ROWS, a1 = min(a0 + RDM_ROWS, rows);
+  for (int a = a0; a < a1; ++a) {
+    const auto* xr = x + (long long)a * cols;
+    const auto* yr = y + (long long)a * cols;
+    double2 r = make_double2(0.0, 0.0);
+    double2 cj[FFGB_MAXN];
+#pragma unroll
+    for (int j = 0; j < FFGB_MAXN; ++j) cj[j] = make_double2(0.0, 0.0);
+    for (int c = threadIdx.x; c < cols; c += DTHREADS) {
+      const double2 w = cdot_acc(make_double2(0.0, 0.0), xr[c], yr[c]);
+      r.x += w.x;
+      r.y += w.y;
+      const unsigned sc = cstr[c];
+#pragma unroll
+      for (int j = 0; j < FFGB_MAXN; ++j)
+        if ((sc >> j) & 1u) {
+          cj[j].x += w.x;
+          cj[j].y += w.y;
+        }
+    }
+    const double2 rs = block_sum2(r, sh);
+    if (threadIdx.x == 0) red[FFGB_MAXN] = rs;
+#pragma unroll
+    for (int j = 0; j < FFGB_MAXN; ++j) {
+      if (j < norb) {  // uniform: every thread takes the same branch
+        const double2 v = block_sum2(cj[j], sh);
+        if (threadIdx.x == 0) red[j] = v;
+      }
+    }
+    __syncthreads();
+    const unsigned sr = rstr[a];
+    for (int idx = threadIdx.x; idx < norb * norb; idx += DTHREADS) {
+      const int i = idx / norb, j = idx - i * norb;
+      if (!((sr >> i) & 1u)) continue;
+      const double2 c = red[j];
+      acc_rc[i * FFGB_MAXN + j].x += c.x;
+      acc_rc[i * FFGB_MAXN + j].y += c.y;
+      if ((sr >> j) & 1u) {
+        acc_rr[i * FFGB_MAXN + j].x += red[FFGB_MAXN].x;
+        acc_rr[i * FFGB_MAXN + j].y += red[FFGB_MAXN].y;
+      }
+    }
+    __syncthreads();
+  }
+  double2* out = partial + (long long)blockIdx.x * 2 * norb * norb;
+  for (int idx = threadIdx.x; idx < norb * norb; idx += DTHREADS) {
+    const int i = idx / norb, j = idx - i * norb;
+    out[idx] = acc_rr[i * FFGB_MAXN + j];
+    out[norb * norb + idx] = acc_rc[i * FFGB_MAXN + j];
+  }
+}
+
+}  // namespace
+
+// Transition one-body density of the sector on the rows of x, y (rows x cols).
+template <typename T>
+int rdm1_rows(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
+              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st) {
+  const int chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
+  const size_t need = sizeof(double2) * (size_t)chunks * norb * norb;
+  if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
+  if (rows > 0 && cols > 0 && norb > 0) {
+    dim3 grid((unsigned)chunks, (unsigned)(norb * norb));
+    rdm1_kernel<T><<<grid, DTHREADS, 0, st>>>((const typename CT<T>::type*)x, (const typename CT<T>::type*)y,
+                                              strings, rows, cols, norb, (double2*)partial_buf);
+    count_launch();
+    FFGB_CUDA(cudaGetLastError());
+  }
+  std::vector<double> h(2 * (size_t)chunks * norb * norb, 0.0);
+  if (!h.empty()) FFGB_CUDA(cudaMemcpyAsync(h.data(), partial_buf, need, cudaMemcpyDeviceToHost, st));
+  FFGB_CUDA(cudaStreamSynchronize(st));
+  out.assign(2 * (size_t)norb * norb, 0.0);
+  for (int pq = 0; pq < norb * norb; ++pq)
+    for (int c = 0; c < chunks; ++c) {
+      out[2 * pq] += h[2 * ((size_t)pq * chunks + c)];
+      out[2 * pq + 1] += h[2 * ((size_t)pq * chunks + c) + 1];
+    }
+  return FFGB_OK;
+}
+
+// Pair densities (row-row and row-column) of x, y with rows indexed by rstr.
+template <typename T>
+int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
+              int norb, void* partial_buf, size_t partial_bytes, std::vector<double>& rr, std::vector<double>& rc,
+              cudaStream_t st) {
+  const int chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
+  const size_t per = (size_t)2 * norb * norb;
+  const size_t need = sizeof(double2) * (size_t)chunks * per;
+  if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
+  if (rows > 0 && cols > 0 && norb > 0) {
+    pair_density_kernel<T><<<chunks, DTHREADS, 0, st>>>((const typename CT<T>::type*)x,
+                                                       (const typename CT<T>::type*)y, rstr, cstr, rows, cols,
+                                                       norb, (double2*)partial_buf);
+    count_launch();
+    FFGB_CUDA(cudaGetLastError());
+  }
+  std::vector<double> h(2 * (size_t)chunks * per, 0.0);
+  if (!h.empty()) FFGB_CUDA(cudaMemcpyAsync(h.data(), partial_buf, need, cudaMemcpyDeviceToHost, st));
+  FFGB_CUDA(cudaStreamSynchronize(st));
+  rr.assign(2 * (size_t)norb * norb, 0.0);
+  rc.assign(2 * (size_t)norb * norb, 0.0);
+  for (int c = 0; c < chunks; ++c)
+    for (size_t k = 0; k < (size_t)norb * norb; ++k) {
+      rr[2 * k] += h[2 * (c * per + k)];
+      rr[2 * k + 1] += h[2 * (c * per + k) + 1];
+      rc[2 * k] += h[2 * (c * per + norb * norb + k)];
+      rc[2 * k + 1] += h[2 * (c * per + norb * norb + k) + 1];
+    }
+  return FFGB_OK;
+}
+
+template int rdm1_rows<float>(const void*, const void*, const unsigned*, int, int, int, void*, size_t,
+                              std::vector<double>&, cudaStream_t);
+template int rdm1_rows<double>(const void*, const void*, const unsigned*, int, int, int, void*, size_t,
+                               std::vector<double>&, cudaStream_t);
+template int pair_rows<float>(const void*, const void*, const unsigned*, const unsigned*, int, int, int, void*,
+                              size_t, std::vector<double>&, std::vector<double>&, cudaStream_t);
+template int pair_rows<double>(const void*, const void*, const unsigned*, const unsigned*, int, int, int, void*,
+                               size_t, std::vector<double>&, std::vector<double>&, cudaStream_t);
+
+// Partial-sum bytes the density kernels need for a sector of `rows` strings.
+size_t density_partial_bytes(int norb, long long rows) {
+  const long long chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
+  return sizeof(double2) * (size_t)chunks * 2 * norb * norb + 256;
+}
+
+}  // namespace ffgb

@@ -1,0 +1,219 @@
+"""Adjoint gradient of the LUCJ energy with respect to the parameters of a
+spin-balanced UCJ operator (``UCJOpSpinBalanced.from_parameters`` layout).
+
+With the UCJ rotations merged as in ``_apply_unitary_``
+(python/ffsim/variational/ucj_spin_balanced.py:657-696 in the reference)::
+
+    psi = W(V_{L+1}) D_L W(V_L) ... D_1 W(V_1) |HF>,
+    V_1 = U_1^dag, V_k = U_k^dag U_{k-1}, V_{L+1} = U_final U_L,
+    D_k = exp(i f_k),  f_k = sum_{i<=j} w_ij J^aa_ij (n_ia n_ja + n_ib n_jb) + sum_ij J^ab_ij n_ia n_jb
+
+the energy E = <psi|H|psi> is differentiated by reverse accumulation: with
+lambda = H psi, the gates are undone one by one on both psi and lambda (the
+circuit is uncomputed, nothing is stored), and at each gate
+
+* an orbital rotation W(V) perturbed as V exp(t G) contributes
+  2 Re sum_pq G_pq <lambda| a+_p a_q |phi> (phi, lambda taken just below the
+  gate): the transition one-body density, ffgb_transition_rdm1;
+* a diagonal phase exp(i f) contributes -2 Im <lambda| df |phi>: the diagonal
+  pair densities, ffgb_pair_density.
+
+The generator gradients are mapped to the antihermitian parameters of each
+U_k = exp(K_k) (python/ffsim/linalg/util.py:93-124) through the derivative of
+the matrix exponential in the eigenbasis of K_k, in FP64 on the host.  The
+states run in complex64 or complex128 on the GPU.  The reference has no
+gradient; the result is checked against central finite differences of the
+energy.
+"""
+
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+import torch
+
+from ffsim_gb300 import _lib
+from ffsim_gb300._state import dim, scratch
+from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian
+from ffsim_gb300.linalg import antihermitians_from_parameters
+from ffsim_gb300.variational import UCJOpSpinBalanced
+
+
+def _antihermitian_basis(norb: int) -> np.ndarray:
+    """dK/dtheta for every one of the norb**2 rotation parameters."""
+    eye = np.eye(norb * norb)
+    return antihermitians_from_parameters(eye.reshape(-1), norb, norb * norb)
+
+
+def _dexp(K: np.ndarray, dK: np.ndarray) -> np.ndarray:
+    """d exp(K)[dK] for antihermitian K and a batch dK (n, norb, norb)."""
+    w, W = np.linalg.eigh(-1j * K)  # K = W diag(i w) W^dag
+    e = np.exp(1j * w)
+    diff = 1j * (w[:, None] - w[None, :])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        phi = (e[:, None] - e[None, :]) / diff
+    close = np.abs(diff) < 1e-12
+    phi[close] = np.broadcast_to(e[:, None], phi.shape)[close]
+    M = np.einsum("ia,nij,jb->nab", W.conj(), dK, W)
+    return np.einsum("ia,nab,jb->nij", W, M * phi[None], W.conj())
+
+
+class LUCJGradient:
+    """Energy and gradient of the LUCJ ansatz for one (norb, nelec) shape,
+    holding its device buffers (two states and scratch)."""
+
+    def __init__(self, norb: int, nelec: tuple[int, int], *, dtype=torch.complex64, device="cuda"):
+        self.norb = norb
+        self.nelec = tuple(nelec)
+        self.dtype = dtype
+        self.code = _lib.FFGB_C64 if dtype == torch.complex64 else _lib.FFGB_C128
+        d = dim(norb, nelec)
+        self.cur = torch.empty(d, dtype=dtype, device=device)
+        self.lam = torch.empty(d, dtype=dtype, device=device)
+        need = max(_lib.load().ffgb_scratch_bytes(op, self.code, norb, *self.nelec) for op in (0, 1, 3))
+        self.buf = torch.empty(need, dtype=torch.uint8, device=device)
+        self.nbytes = need
+        self.basis = _antihermitian_basis(norb)
+
+    # -- device helpers ----------------------------------------------------
+    def _stream(self):
+        return torch.cuda.current_stream(self.cur.device).cuda_stream
+
+    def _rotate(self, vec: torch.Tensor, mat: np.ndarray) -> None:
+        m = _lib.cmat(mat)
+        na, nb = self.nelec
+        _lib.call("ffgb_apply_orbital_rotation", vec.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(m),
+                  _lib.dptr(m), self.buf.data_ptr(), self.nbytes, self._stream())
+
+    def _phase(self, vec: torch.Tensor, jaa: np.ndarray, jab: np.ndarray, time: float) -> None:
+        aa, ab = _lib.rmat(jaa), _lib.rmat(jab)
+        na, nb = self.nelec
+        _lib.call("ffgb_apply_diag_coulomb_evolution", vec.data_ptr(), self.code, self.norb, na, nb,
+                  _lib.dptr(aa), _lib.dptr(ab), _lib.dptr(aa), float(time), 0, None, None, self.buf.data_ptr(),
+                  self.nbytes, self._stream())
+
+    def _density(self, name: str, x: torch.Tensor, y: torch.Tensor, blocks: int) -> np.ndarray:
+        out = np.zeros(2 * blocks * self.norb * self.norb)
+        na, nb = self.nelec
+        _lib.call(name, x.data_ptr(), y.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(out),
+                  self.buf.data_ptr(), self.nbytes, self._stream())
+        return out.view(np.complex128).reshape(blocks, self.norb, self.norb)
+
+    # -- energy and gradient -------------------------------------------------
+    def value_and_grad(self, params: np.ndarray, n_reps: int, ham: DoubleFactorizedHamiltonian, *,
+                       with_final_orbital_rotation: bool = False) -> tuple[float, np.ndarray]:
+        norb = self.norb
+        na, nb = self.nelec
+        params = np.asarray(params, dtype=float)
+        ucj = UCJOpSpinBalanced.from_parameters(params, norb=norb, n_reps=n_reps,
+                                                with_final_orbital_rotation=with_final_orbital_rotation)
+        L = n_reps
+        U = [np.eye(norb, dtype=complex)] + [np.asarray(u) for u in ucj.orbital_rotations]
+        Uf = (np.asarray(ucj.final_orbital_rotation) if ucj.final_orbital_rotation is not None
+              else np.eye(norb, dtype=complex))
+        V = [None] + [U[k].conj().T @ U[k - 1] for k in range(1, L + 1)] + [Uf @ U[L]]
+        jaa = [None] + [ucj.diag_coulomb_mats[k, 0] for k in range(L)]
+        jab = [None] + [ucj.diag_coulomb_mats[k, 1] for k in range(L)]
+
+        # forward: psi from the Hartree-Fock state
+        _lib.call("ffgb_hartree_fock", self.cur.data_ptr(), self.code, self.cur.numel(), self._stream())
+        for k in range(1, L + 1):
+            self._rotate(self.cur, V[k])
+            self._phase(self.cur, jaa[k], jab[k], -1.0)
+        self._rotate(self.cur, V[L + 1])
+
+        # lambda = (H - c) psi: the constant c changes neither the gradient (the
+        # gates keep the norm) nor needs the states' precision, so it is added
+        # to the energy exactly: E = c + <psi|lambda>
+        if ham.z_representation:
+            ham = ham.to_number_representation()
+        one_body, hdcm, hrots = ham._arrays()
+        _lib.call("ffgb_df_matvec", self.cur.data_ptr(), self.lam.data_ptr(), self.code, norb, na, nb,
+                  _lib.dptr(one_body), hdcm.shape[0], _lib.dptr(hdcm), hrots.ctypes.data_as(_lib._dp),
+                  0.0, 0, self.buf.data_ptr(), self.nbytes, self._stream())
+        e = np.zeros(2)
+        _lib.call("ffgb_vdot", self.cur.data_ptr(), self.lam.data_ptr(), self.code, self.cur.numel(),
+                  _lib.dptr(e), self._stream())
+        energy = float(ham.constant) + float(e[0])
+
+        # backward: undo the gates on psi and lambda
+        gamma = [None] * (L + 2)  # generator gradients of V_j
+        pdens = [None] * (L + 1)  # pair densities at D_k
+        for j in range(L + 1, 0, -1):
+            vd = V[j].conj().T
+            self._rotate(self.cur, vd)
+            self._rotate(self.lam, vd)
+            g = self._density("ffgb_transition_rdm1", self.lam, self.cur, 2)
+            gamma[j] = g[0] + g[1]
+            if j > 1:
+                k = j - 1
+                pdens[k] = self._density("ffgb_pair_density", self.lam, self.cur, 3)
+                self._phase(self.cur, jaa[k], jab[k], 1.0)
+                self._phase(self.lam, jaa[k], jab[k], 1.0)
+
+        # chain rule to the parameters
+        grad = np.zeros_like(params)
+        triu = list(itertools.combinations_with_replacement(range(norb), 2))
+        n_triu = len(triu)
+        index = 0
+        for k in range(1, L + 1):
+            Kk = antihermitians_from_parameters(params[index: index + norb * norb], norb, 1)[0]
+            dU = _dexp(Kk, self.basis)  # (norb**2, norb, norb)
+            # V_k = U_k^dag U_{k-1}:  G = U_{k-1}^dag U_k dU_k^dag U_{k-1}
+            Gk = np.einsum("ij,jk,nlk,lm->nim", U[k - 1].conj().T, U[k], dU.conj(), U[k - 1])
+            # V_{k+1} = U_{k+1}^dag U_k (or U_final U_L):  G = U_k^dag dU_k
+            Gk1 = np.einsum("ji,njk->nik", U[k].conj(), dU)
+            grad[index: index + norb * norb] = 2 * (
+                np.einsum("nij,ij->n", Gk, gamma[k]).real + np.einsum("nij,ij->n", Gk1, gamma[k + 1]).real)
+            index += norb * norb
+            P = pdens[k]
+            for t, (i, j) in enumerate(triu):
+                if i == j:
+                    daa = 0.5 * (P[0, i, i] + P[2, i, i])
+                    dab = P[1, i, i]
+                else:
+                    daa = P[0, i, j] + P[2, i, j]
+                    dab = P[1, i, j] + P[1, j, i]
+                grad[index + t] = -2 * daa.imag
+                grad[index + n_triu + t] = -2 * dab.imag
+            index += 2 * n_triu
+        if with_final_orbital_rotation:
+            Kf = antihermitians_from_parameters(params[index:], norb, 1)[0]
+            dUf = _dexp(Kf, self.basis)
+            # V_{L+1} = U_final U_L:  G = U_L^dag U_final^dag dU_final U_L
+            Gf = np.einsum("ij,jk,nkl,lm->nim", U[L].conj().T, Uf.conj().T, dUf, U[L])
+            grad[index:] = 2 * np.einsum("nij,ij->n", Gf, gamma[L + 1]).real
+        return energy, grad
+
+
+class LUCJEnergyFunction(torch.autograd.Function):
+    """E(params) with the adjoint gradient as its backward.  params: float64
+    tensor of shape (n_params,) or (batch, n_params); returns E of shape () or
+    (batch,)."""
+
+    @staticmethod
+    def forward(ctx, params, evaluator: LUCJGradient, n_reps: int, ham: DoubleFactorizedHamiltonian,
+                with_final_orbital_rotation: bool = False):
+        p = params.detach().cpu().numpy().astype(float)
+        batch = p.reshape(-1, p.shape[-1])
+        es, gs = [], []
+        for row in batch:
+            e, g = evaluator.value_and_grad(row, n_reps, ham, with_final_orbital_rotation=with_final_orbital_rotation)
+            es.append(e)
+            gs.append(g)
+        grad = torch.as_tensor(np.array(gs).reshape(p.shape), dtype=params.dtype, device=params.device)
+        ctx.save_for_backward(grad)
+        out = torch.as_tensor(np.array(es), dtype=params.dtype, device=params.device)
+        return out.reshape(p.shape[:-1])
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (grad,) = ctx.saved_tensors
+        return grad_out.unsqueeze(-1) * grad, None, None, None, None
+
+
+def lucj_energy_autograd(params: torch.Tensor, evaluator: LUCJGradient, n_reps: int,
+                         ham: DoubleFactorizedHamiltonian, *, with_final_orbital_rotation: bool = False):
+    """LUCJ energy as a differentiable function of the parameter tensor."""
+    return LUCJEnergyFunction.apply(params, evaluator, n_reps, ham, with_final_orbital_rotation)

@@ -83,7 +83,7 @@ int ffgb_debug_stage(void* vec, int dtype, int norb, int n_alpha, int n_beta, co
 
 /* Scratch bytes needed by the functions below for a state of the given
  * shape (op: 0 = orbital rotation / evolutions, 1 = linear operator matvec,
- * 2 = expectation / energy). */
+ * 2 = expectation / energy, 3 = densities). */
 size_t ffgb_scratch_bytes(int op, int dtype, int norb, int n_alpha, int n_beta);
 
 /* ------------------------------------------------------------------ */
@@ -234,6 +234,23 @@ int ffgb_lucj_energy(const void* vec_in, void* work_state, int dtype, int norb, 
 /* ------------------------------------------------------------------ */
 /* Reductions and helpers                                               */
 /* ------------------------------------------------------------------ */
+
+/* Transition one-body density out[s][p][q] = <x| a+_{p s} a_{q s} |y> for
+ * s = alpha, beta (complex, interleaved re/im; 2*norb*norb complex values; host
+ * pointer; synchronizes).  The gradient of the LUCJ energy with respect to an
+ * orbital-rotation generator.  Scratch: ffgb_scratch_bytes(3, ...).  The
+ * reference computes this on the CPU (python/ffsim/states/rdm.py:73-274 via
+ * pyscf's trans_rdm1s); no counterpart on its kernel path. */
+int ffgb_transition_rdm1(const void* x, const void* y, int dtype, int norb, int n_alpha, int n_beta,
+                         double* out, void* scratch, size_t scratch_bytes, void* stream);
+
+/* Diagonal pair densities <x| n_{i s} n_{j t} |y> for (s, t) = (alpha, alpha),
+ * (alpha, beta), (beta, beta): 3*norb*norb complex values (host pointer;
+ * synchronizes).  The gradient of the LUCJ energy with respect to the
+ * diagonal Coulomb matrices.  Scratch: ffgb_scratch_bytes(3, ...).  No
+ * counterpart in the reference. */
+int ffgb_pair_density(const void* x, const void* y, int dtype, int norb, int n_alpha, int n_beta, double* out,
+                      void* scratch, size_t scratch_bytes, void* stream);
 
 /* out[0..1] = sum conj(x) y in FP64 (host pointer; synchronizes). */
 int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out, void* stream);

@@ -1,0 +1,109 @@
+"""Adjoint gradient of the LUCJ energy against central finite differences of
+the complex128 energy (h = 1e-5, FP64)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+
+def test_dexp_matches_finite_differences():
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    from ffsim_gb300.gradient import _antihermitian_basis, _dexp
+    from ffsim_gb300.linalg import antihermitians_from_parameters
+
+    rng = np.random.default_rng(3)
+    norb = 5
+    K = antihermitians_from_parameters(rng.normal(scale=0.7, size=norb * norb), norb, 1)[0]
+    basis = _antihermitian_basis(norb)
+    got = _dexp(K, basis)
+    h = 1e-6
+    for n in range(0, norb * norb, 3):
+        fd = (scipy_linalg.expm(K + h * basis[n]) - scipy_linalg.expm(K - h * basis[n])) / (2 * h)
+        np.testing.assert_allclose(got[n], fd, atol=1e-8)
+
+
+def _setup(norb, n_reps, rank, seed, with_final):
+    import ffsim_gb300 as f
+
+    rng = np.random.default_rng(seed)
+    n = f.UCJOpSpinBalanced.n_params(norb, n_reps, with_final_orbital_rotation=with_final)
+    params = rng.normal(scale=0.4, size=n)
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=rank, seed=seed + 1)
+    return params, ham
+
+
+def _energy(params, norb, nelec, n_reps, ham, with_final, dtype):
+    import ffsim_gb300 as f
+
+    op = f.UCJOpSpinBalanced.from_parameters(params, norb=norb, n_reps=n_reps,
+                                             with_final_orbital_rotation=with_final)
+    return f.lucj_energy(op, ham, norb, nelec, dtype=dtype)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("with_final", [False, True])
+def test_gradient_small_full(cuda, with_final):
+    import torch
+
+    from ffsim_gb300.gradient import LUCJGradient
+
+    norb, nelec, n_reps = 6, (3, 3), 2
+    params, ham = _setup(norb, n_reps, 4, 11, with_final)
+    h = 1e-5
+    fd = np.array([
+        (_energy(params + h * e, norb, nelec, n_reps, ham, with_final, torch.complex128)
+         - _energy(params - h * e, norb, nelec, n_reps, ham, with_final, torch.complex128)) / (2 * h)
+        for e in np.eye(len(params))])
+    e128 = _energy(params, norb, nelec, n_reps, ham, with_final, torch.complex128)
+    for dtype, tol in [(torch.complex128, 1e-6), (torch.complex64, 1e-4)]:
+        ev = LUCJGradient(norb, nelec, dtype=dtype)
+        e, g = ev.value_and_grad(params, n_reps, ham, with_final_orbital_rotation=with_final)
+        assert abs(e - e128) < (1e-10 if dtype == torch.complex128 else 1e-5)
+        rel = np.linalg.norm(g - fd) / np.linalg.norm(fd)
+        assert rel < tol, (dtype, rel)
+
+
+@pytest.mark.gpu
+def test_gradient_norb12_directional(cuda):
+    """norb=12, (6,6), three repetitions, rank 24: directional derivatives of
+    two parameter vectors along random directions."""
+    import torch
+
+    from ffsim_gb300.gradient import LUCJGradient
+
+    norb, nelec, n_reps = 12, (6, 6), 3
+    params0, ham = _setup(norb, n_reps, 24, 21, False)
+    rng = np.random.default_rng(5)
+    ev = LUCJGradient(norb, nelec, dtype=torch.complex64)
+    h = 1e-5
+    for b in range(2):
+        params = params0 + 0.1 * b * rng.normal(size=len(params0))
+        _, g = ev.value_and_grad(params, n_reps, ham)
+        for _ in range(2):
+            d = rng.normal(size=len(params))
+            d /= np.linalg.norm(d)
+            fd = (_energy(params + h * d, norb, nelec, n_reps, ham, False, torch.complex128)
+                  - _energy(params - h * d, norb, nelec, n_reps, ham, False, torch.complex128)) / (2 * h)
+            assert abs(g @ d - fd) <= 1e-4 * max(abs(fd), 1e-3 * np.linalg.norm(g)), (g @ d, fd)
+
+
+@pytest.mark.gpu
+def test_autograd_function_batch(cuda):
+    import torch
+
+    from ffsim_gb300.gradient import LUCJGradient, lucj_energy_autograd
+
+    norb, nelec, n_reps = 6, (3, 3), 1
+    params, ham = _setup(norb, n_reps, 3, 31, False)
+    batch = torch.tensor(np.stack([params, params * 0.5, params * -0.3]), dtype=torch.float64,
+                         requires_grad=True)
+    ev = LUCJGradient(norb, nelec, dtype=torch.complex128)
+    energies = lucj_energy_autograd(batch, ev, n_reps, ham)
+    assert energies.shape == (3,)
+    energies.sum().backward()
+    energies = energies.detach()
+    for row in range(3):
+        e, g = ev.value_and_grad(batch[row].detach().numpy(), n_reps, ham)
+        assert abs(energies[row].item() - e) < 1e-12
+        np.testing.assert_allclose(batch.grad[row].numpy(), g, atol=1e-12)
