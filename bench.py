@@ -291,6 +291,95 @@ def run_ops(args) -> None:
         print(json.dumps(line), flush=True)
 
 
+def run_grad(args) -> None:
+    """Gradient workload: norb=12 (6,6), UCJ n_reps=3, DF rank 24, a batch of
+    parameter vectors; energies and adjoint gradients per second, with the
+    directional derivative of one vector checked against central finite
+    differences of the complex128 energy (h = 1e-5)."""
+    import numpy as np
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300.gradient import LUCJGradient
+    from ffsim_gb300.serving import LUCJServer, Request
+
+    norb, nelec, L, R, B = 12, (6, 6), 3, 24, args.batch
+    rng = np.random.default_rng(2026)
+    n = f.UCJOpSpinBalanced.n_params(norb, L)
+    base = f.random.random_ucj_op_spin_balanced(norb, n_reps=L, diag_coulomb_normal=True,
+                                                diag_coulomb_scale=0.1, seed=2026).to_parameters()
+    batch = base[None, :] + 0.05 * rng.normal(size=(B, n))
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=R, seed=2027)
+    ev = LUCJGradient(norb, nelec, dtype=torch.complex64)
+    for row in batch[:2]:
+        ev.value_and_grad(row, L, ham)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grads = [ev.value_and_grad(row, L, ham)[1] for row in batch]
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    # the same batch through the serving loop (concurrent streams)
+    srv = LUCJServer(workers=args.workers)
+    reqs = [Request(i, "gradient", norb, nelec, L, row, ham) for i, row in enumerate(batch)]
+    t0 = time.perf_counter()
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(B)
+    t_srv = time.perf_counter() - t0
+    srv.close()
+    same = max(float(np.max(np.abs(r.grad - g))) for r, g in zip(res, grads))
+    # accuracy: directional derivative against FD of the complex128 energy
+    d = rng.normal(size=n)
+    d /= np.linalg.norm(d)
+    h = 1e-5
+
+    def e128(p):
+        op = f.UCJOpSpinBalanced.from_parameters(p, norb=norb, n_reps=L)
+        return f.lucj_energy(op, ham, norb, nelec, dtype=torch.complex128)
+
+    fd = (e128(batch[0] + h * d) - e128(batch[0] - h * d)) / (2 * h)
+    rel = abs(grads[0] @ d - fd) / abs(fd)
+    print(json.dumps({
+        "metric": "LUCJ energy+gradient evals/s norb=12 (6,6) n_reps=3 rank 24 (complex64, FP64 reductions)",
+        "value": B / t_srv, "unit": "evals/s", "batch": B, "n_params": n, "dtype": "c64",
+        "sequential_evals_per_s": B / t_seq, "concurrent_workers": args.workers,
+        "max_abs_diff_concurrent_vs_sequential": same,
+        "fd_check": {"h": h, "directional_rel_err": rel, "bar": 1e-4},
+        "data": "synthetic (seeded UCJ parameters near a random operator; Haar term rotations)"}), flush=True)
+
+
+def run_serve(args) -> None:
+    """Serving workload: Poisson arrivals of LUCJ energy (80%) and gradient
+    (20%) requests, norb uniform over {8,10,12,14,16} at half filling,
+    n_reps in {1,2,3}, DF rank 2*norb; p50/p99 latency and throughput."""
+    import torch
+
+    from ffsim_gb300.serving import LUCJServer, latency_stats, replay, synthetic_stream
+
+    offsets, reqs = synthetic_stream(args.requests, rate=args.rate, seed=2026)
+    # warm the shapes (plans, string tables, kernels) outside the measurement
+    warm = LUCJServer(workers=1)
+    _, wreqs = synthetic_stream(10, rate=1e6, seed=7)
+    for r in wreqs:
+        warm.submit(r)
+    warm.drain(len(wreqs))
+    warm.close()
+    torch.cuda.synchronize()
+    srv = LUCJServer(workers=args.workers)
+    res = replay(srv, offsets, reqs)
+    srv.close()
+    st = latency_stats(res)
+    n_grad = sum(r.kind == "gradient" for r in reqs)
+    print(json.dumps({
+        "metric": "LUCJ serving evals/s, mixed norb {8..16} half filling, n_reps {1,2,3}, 80% energy / 20% "
+                  "gradient, Poisson arrivals; p50/p99 ms",
+        "value": st["evals_per_s"], "unit": "evals/s", "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+        "requests": len(reqs), "gradients": n_grad, "arrival_rate_per_s": args.rate,
+        "workers": args.workers, "max_concurrent": srv.max_concurrent, "span_s": st["span_s"],
+        "dtype": "c64", "sample": f"{len(reqs)} requests of the 10,000-request stream (seed 2026)",
+        "data": "synthetic"}), flush=True)
+
+
 def cpu_reference_sample(threads: int | None = None):
     """Time the C restatement of the reference on one orbital rotation and one
     diag-Coulomb evolution at norb=16 (complex128) and extrapolate one LUCJ
@@ -358,10 +447,22 @@ def main():
     ap.add_argument("--norb", type=int, default=NORB, help="--ops: orbitals (half filling)")
     ap.add_argument("--dtype", default="c64", choices=["c64", "c128"], help="--ops: state dtype")
     ap.add_argument("--reps", type=int, default=5, help="--ops: timed repetitions per op")
+    ap.add_argument("--grad", action="store_true", help="gradient workload (norb=12, batch of parameters)")
+    ap.add_argument("--batch", type=int, default=64, help="--grad: parameter vectors")
+    ap.add_argument("--serve", action="store_true", help="serving workload (mixed requests, Poisson arrivals)")
+    ap.add_argument("--requests", type=int, default=300, help="--serve: requests")
+    ap.add_argument("--rate", type=float, default=4.0, help="--serve: mean arrivals per second")
+    ap.add_argument("--workers", type=int, default=6, help="--serve/--grad: concurrent requests")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.ops:
         run_ops(args)
+        return
+    if args.grad:
+        run_grad(args)
+        return
+    if args.serve:
+        run_serve(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))

@@ -55,8 +55,9 @@ def _dexp(K: np.ndarray, dK: np.ndarray) -> np.ndarray:
         phi = (e[:, None] - e[None, :]) / diff
     close = np.abs(diff) < 1e-12
     phi[close] = np.broadcast_to(e[:, None], phi.shape)[close]
-    M = np.einsum("ia,nij,jb->nab", W.conj(), dK, W)
-    return np.einsum("ia,nab,jb->nij", W, M * phi[None], W.conj())
+    Wd = W.conj().T
+    M = Wd @ dK @ W
+    return W @ (M * phi[None]) @ Wd
 
 
 class LUCJGradient:
@@ -161,11 +162,11 @@ class LUCJGradient:
             Kk = antihermitians_from_parameters(params[index: index + norb * norb], norb, 1)[0]
             dU = _dexp(Kk, self.basis)  # (norb**2, norb, norb)
             # V_k = U_k^dag U_{k-1}:  G = U_{k-1}^dag U_k dU_k^dag U_{k-1}
-            Gk = np.einsum("ij,jk,nlk,lm->nim", U[k - 1].conj().T, U[k], dU.conj(), U[k - 1])
+            Gk = (U[k - 1].conj().T @ U[k]) @ dU.conj().transpose(0, 2, 1) @ U[k - 1]
             # V_{k+1} = U_{k+1}^dag U_k (or U_final U_L):  G = U_k^dag dU_k
-            Gk1 = np.einsum("ji,njk->nik", U[k].conj(), dU)
+            Gk1 = U[k].conj().T @ dU
             grad[index: index + norb * norb] = 2 * (
-                np.einsum("nij,ij->n", Gk, gamma[k]).real + np.einsum("nij,ij->n", Gk1, gamma[k + 1]).real)
+                (Gk * gamma[k]).sum(axis=(1, 2)).real + (Gk1 * gamma[k + 1]).sum(axis=(1, 2)).real)
             index += norb * norb
             P = pdens[k]
             for t, (i, j) in enumerate(triu):
@@ -182,8 +183,8 @@ class LUCJGradient:
             Kf = antihermitians_from_parameters(params[index:], norb, 1)[0]
             dUf = _dexp(Kf, self.basis)
             # V_{L+1} = U_final U_L:  G = U_L^dag U_final^dag dU_final U_L
-            Gf = np.einsum("ij,jk,nkl,lm->nim", U[L].conj().T, Uf.conj().T, dUf, U[L])
-            grad[index:] = 2 * np.einsum("nij,ij->n", Gf, gamma[L + 1]).real
+            Gf = (U[L].conj().T @ Uf.conj().T) @ dUf @ U[L]
+            grad[index:] = 2 * (Gf * gamma[L + 1]).sum(axis=(1, 2)).real
         return energy, grad
 
 
