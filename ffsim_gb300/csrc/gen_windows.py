@@ -10,12 +10,13 @@ the window's Givens rotations without touching shared memory in between.
 
 For each (B, K) this script writes:
 
-* ``win_givens_B_K<MODE>(v, gp, gl, gt, rng)`` -- the fixed triangular Givens
-  network of a ``B x B`` window unitary (host side: ``triangle_decompose`` in
-  plan.cpp) applied to the member array ``v``; the coefficients
+* ``win_givens_B_K<MODE>(v, gp, gl, gt, rng)`` -- the rectangular ("brick")
+  Givens network of a ``B x B`` window unitary (host side: ``brick_decompose``
+  in plan.cpp) applied to the member array ``v``; the coefficients
   ``(c, Re s, Im s)`` of each rotation, in network order, are read by
-  ``win_coef<MODE>``.  The network is: for r in 0..B-2, for col from B-1 down
-  to r+1, rotate local orbitals (col-1, col).
+  ``win_coef<MODE>``.  The network is B layers alternating the rotations
+  (0,1),(2,3),... and (1,2),(3,4),..., emitted as a loop over layer pairs whose
+  body has no conditionals.
 * ``WinNet<B, K>`` -- the member count and the network as a template, for the
   stage kernels of stages.cuh.
 * ``win_group_B_K(s, off, ...)`` -- loads the members ``s[off[j]]`` into
@@ -44,78 +45,62 @@ def members(b: int, k: int) -> list[int]:
     return sorted(out)
 
 
-def triangle(b: int) -> list[int]:
-    """Local lower index l of each rotation (l, l+1) in network order."""
-    seq = []
-    for r in range(b - 1):
-        for col in range(b - 1, r, -1):
-            seq.append(col - 1)
-    return seq
+def layer_pairs(b: int, parity: int) -> list[int]:
+    """Lower orbital l of the rotations (l, l+1) of one brick layer."""
+    return list(range(parity, b - 1, 2))
+
+
+def brick(b: int) -> list[int]:
+    """Local lower index l of each rotation in network order (b layers,
+    alternating even and odd pairs; plan.cpp brick_order)."""
+    return [l for t in range(b) for l in layer_pairs(b, t % 2)]
+
+
+def _rolled(b: int, layer_code) -> list[str]:
+    """Brick network as a loop over (even, odd) layer pairs with one trailing
+    even layer for odd b: the loop body has no conditionals, so the members
+    stay in the same registers across iterations."""
+    ne, no = len(layer_pairs(b, 0)), len(layer_pairs(b, 1))
+    lines = []
+    if b < 2:
+        return lines
+    lines.append("  int g = 0;")
+    lines.append("#pragma unroll 1")
+    lines.append(f"  for (int t = 0; t < {b // 2}; ++t) {{")
+    lines += ["  " + x for x in layer_code(0, "g")]
+    lines += ["  " + x for x in layer_code(1, f"g + {ne}")]
+    lines.append(f"    g += {ne + no};")
+    lines.append("  }")
+    if b % 2:
+        lines += layer_code(0, "g")
+    return lines
 
 
 def emit_givens(b: int, k: int) -> str:
-    """Triangle network as a runtime loop over its rows r with the rotations of
-    each row unrolled: rotation (col-1, col) runs when col > r.  Only b-1
-    distinct orbital pairs exist, so the code holds b-1 pair patterns instead of
-    b(b-1)/2 (keeps the instruction footprint small).  MODE selects how the
-    coefficients are read (see ``win_coef`` in kernels.cuh)."""
     ms = members(b, k)
     index = {w: j for j, w in enumerate(ms)}
     n = len(ms)
+
+    def layer(parity, g0):
+        out = []
+        for i, l in enumerate(layer_pairs(b, parity)):
+            pairs = [(index[w], index[w ^ (3 << l)]) for w in ms if (w >> l) & 1 and not (w >> (l + 1)) & 1]
+            if not pairs:
+                continue
+            out.append("  {")
+            out.append("    float c, sr, si, cl, srl, sil;")
+            out.append(f"    win_coef<MODE>(gp, gl, gt, {g0} + {i}, rng, c, sr, si, cl, srl, sil);")
+            for x, y in pairs:
+                out.append(f"    rot_pair<MODE == 1>(v[{x}], v[{y}], c, sr, si, cl, srl, sil);")
+            out.append("  }")
+        return out
+
     lines = [
         "template <int MODE>",
         f"__device__ __forceinline__ void win_givens_{b}_{k}(float2 (&v)[{max(n, 1)}], const float* __restrict__ gp,"
         " const float* __restrict__ gl, const unsigned* __restrict__ gt, unsigned& rng) {",
     ]
-    if b < 2:
-        lines.append("}")
-        return "\n".join(lines)
-    lines.append("  int g = 0;")
-    lines.append("#pragma unroll 1")
-    lines.append(f"  for (int r = 0; r < {b - 1}; ++r) {{")
-    for col in range(b - 1, 0, -1):
-        l = col - 1
-        pairs = []
-        for w in ms:
-            if (w >> l) & 1 and not (w >> (l + 1)) & 1:
-                pairs.append((index[w], index[w ^ (3 << l)]))
-        lines.append(f"    if ({col} > r) {{")
-        if pairs:
-            lines.append("      float c, sr, si, cl, srl, sil;")
-            lines.append("      win_coef<MODE>(gp, gl, gt, g, rng, c, sr, si, cl, srl, sil);")
-            for x, y in pairs:
-                lines.append(f"      rot_pair<MODE == 1>(v[{x}], v[{y}], c, sr, si, cl, srl, sil);")
-        lines.append("      ++g;")
-        lines.append("    }")
-    lines.append("  }")
-    lines.append("}")
-    return "\n".join(lines)
-
-
-def emit_givens_unrolled(b: int, k: int) -> str:
-    """The same network as straight-line code (stage kernels: one class per
-    kernel, so the larger code does not compete with other classes)."""
-    ms = members(b, k)
-    index = {w: j for j, w in enumerate(ms)}
-    n = len(ms)
-    lines = [
-        "template <int MODE>",
-        f"__device__ __forceinline__ void win_givens_u_{b}_{k}(float2 (&v)[{max(n, 1)}], const float* __restrict__ gp,"
-        " const float* __restrict__ gl, const unsigned* __restrict__ gt, unsigned& rng) {",
-    ]
-    g = 0
-    for r in range(b - 1):
-        for col in range(b - 1, r, -1):
-            l = col - 1
-            pairs = [(index[w], index[w ^ (3 << l)]) for w in ms if (w >> l) & 1 and not (w >> (l + 1)) & 1]
-            if pairs:
-                lines.append("  {")
-                lines.append("    float c, sr, si, cl, srl, sil;")
-                lines.append(f"    win_coef<MODE>(gp, gl, gt, {g}, rng, c, sr, si, cl, srl, sil);")
-                for x, y in pairs:
-                    lines.append(f"    rot_pair<MODE == 1>(v[{x}], v[{y}], c, sr, si, cl, srl, sil);")
-                lines.append("  }")
-            g += 1
+    lines += _rolled(b, layer)
     lines.append("}")
     return "\n".join(lines)
 
@@ -131,7 +116,7 @@ def emit_groups(b: int) -> str:
             f"  static constexpr int M = {m};\n"
             f"  template <int MODE> static __device__ __forceinline__ void apply(float2 (&v)[{m}], const float* gp,"
             f" const float* gl, const unsigned* gt, unsigned& rng) {{\n"
-            f"    win_givens_u_{b}_{k}<MODE>(v, gp, gl, gt, rng);\n  }}\n}};"
+            f"    win_givens_{b}_{k}<MODE>(v, gp, gl, gt, rng);\n  }}\n}};"
         )
         lines.append(
             f"template <bool COMP> static __device__ __noinline__ void win_group_{b}_{k}(float2* __restrict__ s,"
@@ -231,16 +216,12 @@ def _model_check(b: int, k: int, kind: str) -> None:
         ms = members(bb, kk)
         idx = {w: j for j, w in enumerate(ms)}
         v = list(v)
-        g = 0
-        for r in range(bb - 1):
-            for col in range(bb - 1, r, -1):
-                l = col - 1
-                c, s = coefs[g]
-                for w in ms:
-                    if (w >> l) & 1 and not (w >> (l + 1)) & 1:
-                        x, y = idx[w], idx[w ^ (3 << l)]
-                        v[x], v[y] = c * v[x] + s * v[y], -s.conjugate() * v[x] + c * v[y]
-                g += 1
+        for g, l in enumerate(brick(bb)):
+            c, s = coefs[g]
+            for w in ms:
+                if (w >> l) & 1 and not (w >> (l + 1)) & 1:
+                    x, y = idx[w], idx[w ^ (3 << l)]
+                    v[x], v[y] = c * v[x] + s * v[y], -s.conjugate() * v[x] + c * v[y]
         return v
 
     lanes = pack_lanes(b, k, kind)
@@ -257,11 +238,9 @@ def _model_check(b: int, k: int, kind: str) -> None:
         iv = {w: j for j, w in enumerate(members(b, k))}
         P = [[v[iv[w0]], v[iv[w1]]] for w0, w1 in lanes]
         want = plain(b, k, v)
-    g = 0
-    for r in range(b - 1):
-        for ci, col in enumerate(range(b - 1, 0, -1)):
-            if not col > r:
-                continue
+    for g, l in enumerate(brick(b)):
+        ci = b - 1 - (l + 1)
+        if True:
             c, s = coefs[g]
             A, Bv = (s, -s.conjugate()), (-s.conjugate(), s)
             for p, q, swap, vp_a, vq_a in sched[ci]:
@@ -271,7 +250,6 @@ def _model_check(b: int, k: int, kind: str) -> None:
                 vp, vq = (A if vp_a else Bv), (A if vq_a else Bv)
                 P[p] = [c * Pp[t] + vp[t] * Qx[t] for t in range(2)]
                 P[q] = [c * Qq[t] + vq[t] * Px[t] for t in range(2)]
-            g += 1
     if kind == "pair":
         for pi, (w0, w1) in enumerate(lanes):
             assert abs(P[pi][0] - want_a[ia[w0]]) < 1e-9 and abs(P[pi][1] - want_b[ib[w1]]) < 1e-9, (b, k)
@@ -290,31 +268,31 @@ def pack_kind(b: int, k: int) -> str | None:
 
 def emit_packed(b: int, k: int, kind: str) -> str:
     lanes = pack_lanes(b, k, kind)
-    sched = pack_schedule(b, k, kind)
+    sched = pack_schedule(b, k, kind)  # indexed by col = l + 1 from b - 1 down to 1
     n = len(lanes)
     name = f"win_{kind}_{b}_{k}"
-    # Straight-line network: a runtime loop with conditional rotation blocks
-    # makes the compiler copy every updated pack back into loop-invariant
-    # registers (one MOV per register pair per rotation).
+
+    def layer(parity, g0):
+        out = []
+        for i, l in enumerate(layer_pairs(b, parity)):
+            ops = sched[b - 1 - (l + 1)]
+            if not ops:
+                continue
+            out.append("  {")
+            out.append("    PackCoef pc;")
+            out.append(f"    pack_coef<MODE>(gp, gl, gt, {g0} + {i}, rng, pc);")
+            for p, q, swap, vp_a, vq_a in ops:
+                fn = "rot_pack_x" if swap else "rot_pack"
+                out.append(f"    {fn}<{str(vp_a).lower()}, {str(vq_a).lower()}>(R[{p}], I[{p}], R[{q}], I[{q}], pc);")
+            out.append("  }")
+        return out
+
     lines = [
         "template <int MODE>",
         f"__device__ __forceinline__ void {name}(float2 (&R)[{n}], float2 (&I)[{n}], const float* __restrict__ gp,"
         " const float* __restrict__ gl, const unsigned* __restrict__ gt, unsigned& rng) {",
     ]
-    g = 0
-    for r in range(b - 1):
-        for ci, col in enumerate(range(b - 1, 0, -1)):
-            if not col > r:
-                continue
-            if sched[ci]:
-                lines.append("  {")
-                lines.append("    PackCoef pc;")
-                lines.append(f"    pack_coef<MODE>(gp, gl, gt, {g}, rng, pc);")
-                for p, q, swap, vp_a, vq_a in sched[ci]:
-                    fn = "rot_pack_x" if swap else "rot_pack"
-                    lines.append(f"    {fn}<{str(vp_a).lower()}, {str(vq_a).lower()}>(R[{p}], I[{p}], R[{q}], I[{q}], pc);")
-                lines.append("  }")
-            g += 1
+    lines += _rolled(b, layer)
     lines.append("}")
     # lane tables: member index (class K, and class B-K for lane 1 of pairs)
     ia = {w: j for j, w in enumerate(members(b, k))}
@@ -353,7 +331,6 @@ def main(out_path: str) -> None:
     for b in range(1, MAX_B + 1):
         for k in range(0, b + 1):
             parts.append(emit_givens(b, k))
-            parts.append(emit_givens_unrolled(b, k))
     for b in range(1, MAX_B + 1):
         parts.append(emit_groups(b))
     parts.append("template <int B, int K> struct WinPack { static constexpr int NP = 0; };")

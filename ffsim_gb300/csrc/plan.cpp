@@ -171,6 +171,108 @@ void triangle_decompose(int b, const cd* X, std::vector<Givens>& rots, std::vect
   for (int i = 0; i < b; ++i) diag[i] = M[(size_t)i * b + i];
 }
 
+void brick_order(int b, std::vector<int>& l) {
+  l.clear();
+  for (int t = 0; t < b; ++t)
+    for (int a = t % 2; a + 1 < b; a += 2) l.push_back(a);
+}
+
+// Rectangular ("brick") network: b layers alternating the pairs (0,1),(2,3),...
+// and (1,2),(3,4),...  Built by nulling the entries of X alternately with
+// column operations from the right and row operations from the left, then
+// moving the left operations through the resulting diagonal (Clements et al.,
+// Optica 3, 1460 (2016)), for the rotation form [[c, s], [-conj(s), c]].
+bool brick_decompose(int b, const cd* X, std::vector<Givens>& rots, std::vector<cd>& diag) {
+  std::vector<cd> U(X, X + (size_t)b * b);
+  struct Op {
+    int a;
+    double c;
+    cd s;
+  };
+  std::vector<Op> right, left;
+  for (int i = 1; i < b; ++i) {
+    if (i % 2 == 1) {
+      for (int j = 0; j < i; ++j) {
+        const int r = b - 1 - j, a = i - 1 - j;
+        // column operation G^dag on (a, a+1): col_a <- c col_a + conj(s) col_{a+1}, zeroing U[r][a]
+        const cd ua = U[(size_t)r * b + a], ub = U[(size_t)r * b + a + 1];
+        const double rho = std::hypot(std::abs(ua), std::abs(ub));
+        double c = 1.0;
+        cd s = 0.0;
+        if (rho > 0.0) {
+          if (std::abs(ub) == 0.0) {
+            c = 0.0;
+            s = std::conj(-ua / std::abs(ua));
+          } else {
+            c = std::abs(ub) / rho;
+            s = std::conj(-c * ua / ub);
+          }
+        }
+        for (int row = 0; row < b; ++row) {
+          const cd x = U[(size_t)row * b + a], y = U[(size_t)row * b + a + 1];
+          U[(size_t)row * b + a] = c * x + std::conj(s) * y;
+          U[(size_t)row * b + a + 1] = -s * x + c * y;
+        }
+        right.push_back({a, c, s});
+      }
+    } else {
+      for (int j = 1; j <= i; ++j) {
+        const int a = b + j - i - 2, col = j - 1;
+        // row operation G on (a, a+1): row_{a+1} <- -conj(s) row_a + c row_{a+1}, zeroing U[a+1][col]
+        const cd ua = U[(size_t)a * b + col], ub = U[(size_t)(a + 1) * b + col];
+        const double rho = std::hypot(std::abs(ua), std::abs(ub));
+        double c = 1.0;
+        cd s = 0.0;
+        if (rho > 0.0) {
+          if (std::abs(ua) == 0.0) {
+            c = 0.0;
+            s = std::conj(ub / std::abs(ub));
+          } else {
+            c = std::abs(ua) / rho;
+            s = std::conj(c * ub / ua);
+          }
+        }
+        for (int cc = 0; cc < b; ++cc) {
+          const cd x = U[(size_t)a * b + cc], y = U[(size_t)(a + 1) * b + cc];
+          U[(size_t)a * b + cc] = c * x + s * y;
+          U[(size_t)(a + 1) * b + cc] = -std::conj(s) * x + c * y;
+        }
+        left.push_back({a, c, s});
+      }
+    }
+  }
+  diag.resize(b);
+  for (int i = 0; i < b; ++i) diag[i] = U[(size_t)i * b + i];
+  // X = D * (left ops, inverted and moved through D) * (right ops, inverted), applied right to left
+  std::vector<Op> seq(right.begin(), right.end());
+  for (auto it = left.rbegin(); it != left.rend(); ++it) {
+    const cd d1 = diag[it->a], d2 = diag[it->a + 1];
+    seq.push_back({it->a, it->c, -it->s * d2 / d1});
+  }
+  // layer of every rotation (as early as its orbitals allow), then layer order
+  std::vector<int> last(b, -1), layer(seq.size());
+  for (size_t k = 0; k < seq.size(); ++k) {
+    const int t = std::max(last[seq[k].a], last[seq[k].a + 1]) + 1;
+    last[seq[k].a] = last[seq[k].a + 1] = t;
+    layer[k] = t;
+  }
+  std::vector<size_t> idx(seq.size());
+  for (size_t k = 0; k < idx.size(); ++k) idx[k] = k;
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) {
+    return layer[x] != layer[y] ? layer[x] < layer[y] : seq[x].a < seq[y].a;
+  });
+  std::vector<int> want;
+  brick_order(b, want);
+  if (want.size() != seq.size()) return false;
+  rots.clear();
+  for (size_t k = 0; k < idx.size(); ++k) {
+    const Op& o = seq[idx[k]];
+    if (o.a != want[k]) return false;
+    rots.push_back({o.c, o.s});
+  }
+  return true;
+}
+
 bool csd(int n, int h, const cd* Vp, std::vector<cd>& A1, std::vector<cd>& A2,
          std::vector<double>& cosv, std::vector<double>& sinv, std::vector<cd>& B1,
          std::vector<cd>& B2, double tol, double* err) {
@@ -270,12 +372,11 @@ bool csd(int n, int h, const cd* Vp, std::vector<cd>& A1, std::vector<cd>& A2,
 
 namespace {
 // multiply out a triangle network + diag into a b x b matrix (for checks)
-std::vector<cd> triangle_matrix(int b, const std::vector<Givens>& rots, const std::vector<cd>& diag) {
-  std::vector<int> l;
-  triangle_order(b, l);
+// D * G_M ... G_1 for rotations G_k on (l_k, l_k + 1)
+std::vector<cd> network_matrix(int b, const std::vector<Givens>& rots, const std::vector<int>& l,
+                               const std::vector<cd>& diag) {
   std::vector<cd> M((size_t)b * b, cd(0));
   for (int i = 0; i < b; ++i) M[(size_t)i * b + i] = 1.0;
-  // M = G_M ... G_1 : left-multiply successively
   for (size_t k = 0; k < rots.size(); ++k) {
     int a = l[k];
     double c = rots[k].c;
@@ -289,6 +390,18 @@ std::vector<cd> triangle_matrix(int b, const std::vector<Givens>& rots, const st
   for (int r = 0; r < b; ++r)
     for (int col = 0; col < b; ++col) M[(size_t)r * b + col] *= diag[r];
   return M;
+}
+
+std::vector<cd> triangle_matrix(int b, const std::vector<Givens>& rots, const std::vector<cd>& diag) {
+  std::vector<int> l;
+  triangle_order(b, l);
+  return network_matrix(b, rots, l, diag);
+}
+
+std::vector<cd> brick_matrix(int b, const std::vector<Givens>& rots, const std::vector<cd>& diag) {
+  std::vector<int> l;
+  brick_order(b, l);
+  return network_matrix(b, rots, l, diag);
 }
 }  // namespace
 
@@ -312,9 +425,9 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
   if (norb <= 8) {
     plan.kind = PLAN_FULL;
     plan.h = norb;
-    triangle_decompose(norb, V, plan.tri, plan.diag);
-    triangle_order(norb, plan.tri_l);
-    std::vector<cd> M = triangle_matrix(norb, plan.tri, plan.diag);
+    if (!brick_decompose(norb, V, plan.tri, plan.diag)) return plan_sector(norb, V, false, plan);
+    brick_order(norb, plan.tri_l);
+    std::vector<cd> M = brick_matrix(norb, plan.tri, plan.diag);
     double e = 0;
     for (size_t i = 0; i < M.size(); ++i) e = std::max(e, std::abs(M[i] - V[i]));
     plan.max_err = e;
@@ -331,8 +444,8 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
   plan.kind = PLAN_CSD;
   plan.h = h;
   std::vector<cd> dB1, dB2, dA1, dA2;
-  triangle_decompose(h, B1.data(), plan.b1, dB1);
-  triangle_decompose(q, B2.data(), plan.b2, dB2);
+  if (!brick_decompose(h, B1.data(), plan.b1, dB1) || !brick_decompose(q, B2.data(), plan.b2, dB2))
+    return plan_sector(norb, V, false, plan);
   std::vector<cd> dB(dB1);
   dB.insert(dB.end(), dB2.begin(), dB2.end());
   plan.cs.clear();
@@ -352,15 +465,15 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
     for (int c = 0; c < h; ++c) A1[(size_t)r * h + c] *= dB1[c];
   for (int r = 0; r < q; ++r)
     for (int c = 0; c < q; ++c) A2[(size_t)r * q + c] *= dB2[c];
-  triangle_decompose(h, A1.data(), plan.a1, dA1);
-  triangle_decompose(q, A2.data(), plan.a2, dA2);
+  if (!brick_decompose(h, A1.data(), plan.a1, dA1) || !brick_decompose(q, A2.data(), plan.a2, dA2))
+    return plan_sector(norb, V, false, plan);
   plan.diag = dA1;
   plan.diag.insert(plan.diag.end(), dA2.begin(), dA2.end());
   // multiply the plan back out to measure its error
-  std::vector<cd> TB1 = triangle_matrix(h, plan.b1, std::vector<cd>(h, cd(1)));
-  std::vector<cd> TB2 = triangle_matrix(q, plan.b2, std::vector<cd>(q, cd(1)));
-  std::vector<cd> TA1 = triangle_matrix(h, plan.a1, dA1);
-  std::vector<cd> TA2 = triangle_matrix(q, plan.a2, dA2);
+  std::vector<cd> TB1 = brick_matrix(h, plan.b1, std::vector<cd>(h, cd(1)));
+  std::vector<cd> TB2 = brick_matrix(q, plan.b2, std::vector<cd>(q, cd(1)));
+  std::vector<cd> TA1 = brick_matrix(h, plan.a1, dA1);
+  std::vector<cd> TA2 = brick_matrix(q, plan.a2, dA2);
   auto blk = [&](const std::vector<cd>& X1, const std::vector<cd>& X2) {
     std::vector<cd> M((size_t)norb * norb, cd(0));
     for (int r = 0; r < h; ++r)

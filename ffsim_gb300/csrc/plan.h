@@ -50,6 +50,12 @@ struct SectorPlan {
 // Rotation k acts on local orbitals (l_k, l_k+1), l_k from triangle_order().
 void triangle_decompose(int b, const cd* X, std::vector<Givens>& rots, std::vector<cd>& diag);
 void triangle_order(int b, std::vector<int>& l);
+// Rectangular network of b layers alternating the pairs (0,1),(2,3),... and
+// (1,2),(3,4),...: X = D * (rotations in brick_order, applied first to last).
+// Window networks use it (a loop of identical layer pairs).  False if the
+// construction does not give the rectangular shape.
+bool brick_decompose(int b, const cd* X, std::vector<Givens>& rots, std::vector<cd>& diag);
+void brick_order(int b, std::vector<int>& l);
 
 // Cosine-sine decomposition of V (n x n) at split h (h <= n-h <= h+1):
 // V = diag(A1, A2) * CS * diag(B1, B2); returns false if it fails to

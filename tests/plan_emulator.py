@@ -22,6 +22,11 @@ def _triangle(b):
     return [col - 1 for r in range(b - 1) for col in range(b - 1, r, -1)]
 
 
+def _brick(b):
+    """Window networks: b layers alternating the pairs (0,1),(2,3),... and (1,2),(3,4),..."""
+    return [l for t in range(b) for l in range(t % 2, b - 1, 2)]
+
+
 def _rank_shifted(s, base, m0):
     r, t = 0, m0
     p = 0
@@ -73,7 +78,7 @@ def apply_plan(plan, vec, norb, nocc):
     strings = sorted(sum(1 << i for i in c) for c in itertools.combinations(range(norb), nocc))
     addr = {s: a for a, s in enumerate(strings)}
     if kind in (1, 2):  # TRIANGLE or FULL: adjacent rotations over the whole sector
-        for (c, s), l in zip(plan["tri"], _triangle(norb)):
+        for (c, s), l in zip(plan["tri"], _triangle(norb) if kind == 1 else _brick(norb)):
             for st in strings:
                 if (st >> l) & 1 and not (st >> (l + 1)) & 1:
                     _rot(v, addr[st], addr[st ^ (3 << l)], c, s)
@@ -90,7 +95,7 @@ def apply_plan(plan, vec, norb, nocc):
                     idx = [base + j for j in range(len(mem))]
                     grp = v[idx].copy()
                     local = {w: j for j, w in enumerate(mem)}
-                    for (c, s), l in zip(gp, _triangle(H)):
+                    for (c, s), l in zip(gp, _brick(H)):
                         for w in mem:
                             if (w >> l) & 1 and not (w >> (l + 1)) & 1:
                                 _rot(grp, local[w], local[w ^ (3 << l)], c, s)
@@ -104,7 +109,7 @@ def apply_plan(plan, vec, norb, nocc):
                     idx = [g + o for o in offs]
                     grp = v[idx].copy()
                     local = {w: j for j, w in enumerate(mem)}
-                    for (c, s), l in zip(gp, _triangle(Q)):
+                    for (c, s), l in zip(gp, _brick(Q)):
                         for w in mem:
                             if (w >> l) & 1 and not (w >> (l + 1)) & 1:
                                 _rot(grp, local[w], local[w ^ (3 << l)], c, s)
