@@ -71,8 +71,9 @@ int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long l
 // the last check (synchronizes the stream).
 int stage_check_timeout(cudaStream_t st);
 
-// Upper bound of the partial sums written by a fused expectation over ncols columns.
-long long stage_expect_partials(int norb, long long ncols);
+// Upper bound of the partial sums written by a fused expectation on a state
+// of `rows` rows (the rotated sector's strings) and ncols columns.
+long long stage_expect_partials(long long rows, long long ncols);
 
 // Densities between two states (grad.cu); results summed on the host in FP64.
 template <typename T>

@@ -1,0 +1,120 @@
+// Diagonal operators streamed row by row: no shared-memory copy of a row, so
+// every sector size fits.  For a state whose rows are strings of one sector
+// and whose columns are strings of the other,
+//   f(r, c) = F_R(r) + F_C(c) + sum_{i,l} X[i][l] g_i(r) g_l(c),
+// g = n (number representation) or 1 - 2n (Z representation).  Per row the
+// FP64 row term and the weights m_l(r) = sum_i X[i][l] g_i(r) are formed once;
+// per element the column term comes from a table (exp(i F_C) for phases, F_C
+// for coefficients) and the cross term is a short FP32 sum of m_l over the
+// column string's occupied orbitals.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace ffgb {
+
+constexpr int DIAG_THREADS = 256;
+constexpr int DIAG_ROWS_PER_CTA = 4;
+
+template <typename T>
+struct DiagRowsArgs {
+  using C = typename CT<T>::type;
+  const C* in;
+  C* out;
+  long long rows, cols;
+  const unsigned* rstr;
+  const unsigned* cstr;
+  const void* col_table;  // PHASE: C exp(i F_C); COEF: T F_C
+  double rsame[FFGB_MAXN][FFGB_MAXN];
+  double cross[FFGB_MAXN][FFGB_MAXN];
+  int norb, zrep, mode, accumulate;
+};
+
+template <typename T>
+__device__ __forceinline__ typename CT<T>::type phase_small(T f) {
+  using C = typename CT<T>::type;
+  T s, c;
+  if constexpr (sizeof(T) == 4) {
+    sincosf(f, &s, &c);
+  } else {
+    sincos(f, &s, &c);
+  }
+  C r;
+  r.x = c;
+  r.y = s;
+  return r;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_constant__ DiagRowsArgs<T> A) {
+  using C = typename CT<T>::type;
+  __shared__ T sm[FFGB_MAXN];
+  __shared__ double sF;
+  const int tid = threadIdx.x;
+  const long long r0 = (long long)blockIdx.x * DIAG_ROWS_PER_CTA;
+  const long long r1 = min(r0 + DIAG_ROWS_PER_CTA, A.rows);
+  for (long long r = r0; r < r1; ++r) {
+    const unsigned rs = A.rstr[r];
+    if (tid < A.norb) {
+      double m = 0.0;
+      for (int i = 0; i < A.norb; ++i) {
+        const double gi = A.zrep ? (((rs >> i) & 1u) ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
+        m += A.cross[i][tid] * gi;
+      }
+      sm[tid] = (T)m;
+    }
+    if (tid == 32) {
+      double f = 0.0;
+      for (int i = 0; i < A.norb; ++i) {
+        const double gi = A.zrep ? (((rs >> i) & 1u) ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
+        if (gi == 0.0) continue;
+        for (int i2 = i; i2 < A.norb; ++i2) {
+          const double gj = A.zrep ? (((rs >> i2) & 1u) ? -1.0 : 1.0) : (double)((rs >> i2) & 1u);
+          f += A.rsame[i][i2] * gi * gj;
+        }
+      }
+      if (A.zrep)  // g_l(c) = 1 - 2 n_l(c): the constant part of the cross term
+        for (int l = 0; l < A.norb; ++l) {
+          double m = 0.0;
+          for (int i = 0; i < A.norb; ++i) m += A.cross[i][l] * (((rs >> i) & 1u) ? -1.0 : 1.0);
+          f += m;
+        }
+      sF = f;
+    }
+    __syncthreads();
+    const double F = sF;
+    const T wsc = A.zrep ? (T)-2 : (T)1;
+    C rowph;
+    if (A.mode == DIAG_PHASE) rowph = phase_of(F, (C*)nullptr);
+    const C* xin = A.in + r * A.cols;
+    C* xout = A.out + r * A.cols;
+    for (long long c = tid; c < A.cols; c += DIAG_THREADS) {
+      unsigned s = A.cstr[c];
+      T fx = (T)0;
+      while (s) {
+        fx += sm[__ffs(s) - 1];
+        s &= s - 1;
+      }
+      fx *= wsc;
+      C v = xin[c];
+      if (A.mode == DIAG_PHASE) {
+        const C ph = cmul(cmul(rowph, ((const C*)A.col_table)[c]), phase_small<T>(fx));
+        v = cmul(v, ph);
+      } else {
+        const T z = (T)F + ((const T*)A.col_table)[c] + fx;
+        v.x *= z;
+        v.y *= z;
+      }
+      if (A.accumulate) {
+        C o = xout[c];
+        o.x += v.x;
+        o.y += v.y;
+        v = o;
+      }
+      xout[c] = v;
+    }
+    __syncthreads();  // the next row overwrites sm, sF
+  }
+}
+
+}  // namespace ffgb

@@ -16,6 +16,7 @@
 #include "../../include/ffsim_gb300.h"
 #include "common.h"
 #include "plan.h"
+#include "diag.cuh"
 
 namespace ffgb {
 
@@ -107,7 +108,7 @@ static size_t extras_bytes(int norb, int na, int nb) {
   long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;
   long long m = std::max<long long>(std::max(da, db), 1);
   return (size_t)m * 16 + (size_t)m * 8 + (size_t)m * 32 + (size_t)m * 8 +
-         (size_t)stage_expect_partials(norb, m) * 8 + 65536;
+         (size_t)stage_expect_partials(m, m) * 8 + 65536;
 }
 
 // ---------------------------------------------------------------------------
@@ -249,6 +250,8 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
   int nw = 0;
   if (A.plan && A.plan->kind != PLAN_IDENTITY) {
     const SectorPlan& pl = *A.plan;
+    if (pl.kind == PLAN_CSD && pl.b1.empty())
+      return fail(FFGB_ERR_UNSUPPORTED, "nested cosine-sine plans run on the stage kernels only");
     P->kind = pl.kind;
     P->h = pl.h;
     if (pl.kind == PLAN_TRIANGLE) {
@@ -404,7 +407,7 @@ static std::vector<cd> eye(int n) {
 
 template <typename T>
 static int make_plan(int norb, const std::vector<cd>& V, SectorPlan& plan) {
-  const bool windows = sizeof(T) == 4 && norb <= 16;
+  const bool windows = sizeof(T) == 4 && norb <= FFGB_MAXN;
   if (!plan_sector(norb, V.data(), windows, plan)) return fail(FFGB_ERR_NUMERIC, "plan failed");
   if (plan.max_err > 1e-9) return fail(FFGB_ERR_NUMERIC, "orbital rotation is not unitary");
   return FFGB_OK;
@@ -503,6 +506,51 @@ static void fold_col_phases(DiagSpec& spec, const SectorPlan& p, int norb) {
   for (int i = 0; i < norb; ++i) spec.col_same[i][i] += std::arg(p.diag[i]);
 }
 
+// out (+)= D in for a diagonal operator D (PHASE: exp(i f), COEF: f) on a
+// state whose rows are the strings with row_nocc electrons; `spec` is written
+// with these rows.  Streams rows (any sector size).
+template <typename T>
+static int diag_rows(const void* in, void* out, int norb, int row_nocc, int col_nocc, const DiagSpec& spec,
+                     bool accumulate, Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const long long rows = binom_h(norb, row_nocc), cols = binom_h(norb, col_nocc);
+  if (rows <= 0 || cols <= 0) return FFGB_OK;
+  if (spec.mode != DIAG_PHASE && spec.mode != DIAG_COEF) return fail(FFGB_ERR_ARG, "diagonal mode");
+  const size_t mark = scr.off;
+  const unsigned *rs = nullptr, *cs = nullptr;
+  FFGB_TRY(device_strings(norb, row_nocc, &rs));
+  FFGB_TRY(device_strings(norb, col_nocc, &cs));
+  void* tab = scr.take((size_t)cols * (spec.mode == DIAG_PHASE ? sizeof(C) : sizeof(T)));
+  double* same = (double*)scr.take(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
+  if (!tab || !same) return fail(FFGB_ERR_OOM, "scratch too small for the column table");
+  FFGB_CUDA(cudaMemcpyAsync(same, spec.col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN, cudaMemcpyHostToDevice, st));
+  col_table_kernel<T><<<(unsigned)((cols + 255) / 256), 256, 0, st>>>(cs, (int)cols, norb, spec.zrep, spec.mode,
+                                                                      same, tab);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  auto A = std::make_unique<DiagRowsArgs<T>>();
+  std::memset(A.get(), 0, sizeof(DiagRowsArgs<T>));
+  A->in = (const C*)in;
+  A->out = (C*)out;
+  A->rows = rows;
+  A->cols = cols;
+  A->rstr = rs;
+  A->cstr = cs;
+  A->col_table = tab;
+  std::memcpy(A->rsame, spec.row_same, sizeof(A->rsame));
+  std::memcpy(A->cross, spec.cross, sizeof(A->cross));
+  A->norb = norb;
+  A->zrep = spec.zrep;
+  A->mode = spec.mode;
+  A->accumulate = accumulate ? 1 : 0;
+  const long long grid = (rows + DIAG_ROWS_PER_CTA - 1) / DIAG_ROWS_PER_CTA;
+  diag_rows_kernel<T><<<(unsigned)grid, DIAG_THREADS, 0, st>>>(*A);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  scr.off = mark;
+  return FFGB_OK;
+}
+
 // Diagonal operator on a state held with beta rows (db rows of da columns):
 // in place (PHASE / COEF) or reduced into partial sums (EXPECT).  `spec` is
 // written with alpha rows.
@@ -510,6 +558,7 @@ template <typename T>
 static int diag_pass_t(void* t, int norb, int na, int nb, const DiagSpec& spec, int out_op, double* partials,
                        int* n_ctas, Scratch& scr, cudaStream_t st) {
   DiagSpec dt = spec.transposed();
+  if (sizeof(T) == 4 && out_op == OUT_STORE) return diag_rows<T>(t, t, norb, nb, na, dt, false, scr, st);
   PassArgs<T> A;
   A.norb = norb;
   A.rot_nocc = na;
@@ -640,6 +689,7 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
   }
   const long long da = binom_h(norb, na);
   if (!rot_a && !rot_b) {
+    if (sizeof(T) == 4) return diag_rows<T>(vec, vec, norb, na, nb, spec, false, scr, st);
     PassArgs<T> A;
     A.norb = norb;
     A.rot_nocc = nb;
@@ -701,6 +751,7 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
   using C = typename CT<T>::type;
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
   if (!rot) {
+    if (sizeof(T) == 4) return diag_rows<T>(vec, out, norb, na, nb, spec, accumulate != 0, scr, st);
     PassArgs<T> A;
     A.norb = norb;
     A.rot_nocc = nb;
@@ -819,7 +870,7 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
     FFGB_TRY(launch_transpose<float>(tmp, tmp2, da, db, nullptr, nullptr, st));
     StageExpectArgs ex;
     FFGB_TRY(expect_tables(norb, na, nb, spec, scr, st, ex));
-    ex.partial_cap = stage_expect_partials(norb, da);
+    ex.partial_cap = stage_expect_partials(db, da);
     ex.partials = (double*)scr.take(sizeof(double) * (size_t)ex.partial_cap);
     if (!ex.partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
     int nct = 0;

@@ -405,6 +405,83 @@ std::vector<cd> brick_matrix(int b, const std::vector<Givens>& rots, const std::
 }
 }  // namespace
 
+// X (n x n, unitary) on orbitals [lo, lo + n) = diag(d) * (ops appended here,
+// applied first to last).  Blocks of at most 8 orbitals are one window; larger
+// blocks are split by a cosine-sine decomposition whose right blocks' phases
+// are pushed through the cross-half rotations into the left blocks.
+bool block_ops(int n, const cd* X, int lo, std::vector<StageOp>& ops, std::vector<cd>& d) {
+  if (n <= 8) {
+    StageOp w;
+    w.type = 0;
+    w.lo = lo;
+    w.b = n;
+    if (!brick_decompose(n, X, w.net, d)) return false;
+    ops.push_back(std::move(w));
+    return true;
+  }
+  const int h = n / 2, q = n - h;
+  std::vector<cd> A1, A2, B1, B2;
+  std::vector<double> cv, sv;
+  double err = 0;
+  if (!csd(n, h, X, A1, A2, cv, sv, B1, B2, 1e-11, &err)) return false;
+  std::vector<cd> dB1, dB2, dA1, dA2;
+  if (!block_ops(h, B1.data(), lo, ops, dB1) || !block_ops(q, B2.data(), lo + h, ops, dB2)) return false;
+  std::vector<cd> dB(dB1);
+  dB.insert(dB.end(), dB2.begin(), dB2.end());
+  StageOp c;
+  c.type = 1;
+  c.lo = lo;
+  c.b = h;
+  for (int i = 0; i < h; ++i) {
+    const int j = h + i;
+    Pair2 p;
+    p.i = lo + i;
+    p.j = lo + j;
+    p.g00 = cv[i];
+    p.g01 = std::conj(dB[i]) * (-sv[i]) * dB[j];
+    p.g10 = std::conj(dB[j]) * sv[i] * dB[i];
+    p.g11 = cv[i];
+    c.pairs.push_back(p);
+  }
+  ops.push_back(std::move(c));
+  for (int r = 0; r < h; ++r)
+    for (int cc = 0; cc < h; ++cc) A1[(size_t)r * h + cc] *= dB1[cc];
+  for (int r = 0; r < q; ++r)
+    for (int cc = 0; cc < q; ++cc) A2[(size_t)r * q + cc] *= dB2[cc];
+  if (!block_ops(h, A1.data(), lo, ops, dA1) || !block_ops(q, A2.data(), lo + h, ops, dA2)) return false;
+  d = dA1;
+  d.insert(d.end(), dA2.begin(), dA2.end());
+  return true;
+}
+
+// diag(D) * (ops applied in order) as an n x n matrix.
+std::vector<cd> ops_matrix(int n, const std::vector<StageOp>& ops, const std::vector<cd>& D) {
+  std::vector<cd> M((size_t)n * n, cd(0));
+  for (int i = 0; i < n; ++i) M[(size_t)i * n + i] = 1.0;
+  auto rot = [&](int a, int b2, cd g00, cd g01, cd g10, cd g11) {
+    for (int col = 0; col < n; ++col) {
+      const cd x = M[(size_t)a * n + col], y = M[(size_t)b2 * n + col];
+      M[(size_t)a * n + col] = g00 * x + g01 * y;
+      M[(size_t)b2 * n + col] = g10 * x + g11 * y;
+    }
+  };
+  for (const StageOp& op : ops) {
+    if (op.type == 0) {
+      std::vector<int> l;
+      brick_order(op.b, l);
+      for (size_t k = 0; k < op.net.size(); ++k) {
+        const Givens& g = op.net[k];
+        rot(op.lo + l[k], op.lo + l[k] + 1, g.c, g.s, -std::conj(g.s), g.c);
+      }
+    } else {
+      for (const Pair2& p : op.pairs) rot(p.i, p.j, p.g00, p.g01, p.g10, p.g11);
+    }
+  }
+  for (int r = 0; r < n; ++r)
+    for (int col = 0; col < n; ++col) M[(size_t)r * n + col] *= D[r];
+  return M;
+}
+
 bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
   plan = SectorPlan();
   plan.norb = norb;
@@ -412,7 +489,7 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
     plan.kind = PLAN_IDENTITY;
     return true;
   }
-  if (!want_csd || norb > 16) {
+  if (!want_csd || norb > 18) {
     plan.kind = PLAN_TRIANGLE;
     triangle_decompose(norb, V, plan.tri, plan.diag);
     triangle_order(norb, plan.tri_l);
@@ -434,6 +511,17 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
     return true;
   }
   const int h = norb / 2, q = norb - h;
+  if (q > 8) {  // nested blocks: the stage sequence only
+    plan.kind = PLAN_CSD;
+    plan.h = h;
+    if (!block_ops(norb, V, 0, plan.ops, plan.diag)) return plan_sector(norb, V, false, plan);
+    std::vector<cd> M = ops_matrix(norb, plan.ops, plan.diag);
+    double e = 0;
+    for (size_t i = 0; i < M.size(); ++i) e = std::max(e, std::abs(M[i] - V[i]));
+    plan.max_err = e;
+    if (e > 1e-10) return plan_sector(norb, V, false, plan);
+    return true;
+  }
   std::vector<cd> A1, A2, B1, B2;
   std::vector<double> cv, sv;
   double err = 0;
@@ -506,6 +594,20 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
   for (size_t i = 0; i < full.size(); ++i) e = std::max(e, std::abs(full[i] - V[i]));
   plan.max_err = e;
   if (e > 1e-10) return plan_sector(norb, V, false, plan);
+  auto window = [](int lo, int b, const std::vector<Givens>& net) {
+    StageOp w;
+    w.type = 0;
+    w.lo = lo;
+    w.b = b;
+    w.net = net;
+    return w;
+  };
+  StageOp c;
+  c.type = 1;
+  c.lo = 0;
+  c.b = h;
+  c.pairs = plan.cs;
+  plan.ops = {window(0, h, plan.b1), window(h, q, plan.b2), c, window(0, h, plan.a1), window(h, q, plan.a2)};
   return true;
 }
 

@@ -8,10 +8,11 @@
 //  * TRIANGLE: V = D * G_M ... G_1, adjacent Givens rotations G_k on (l, l+1)
 //    in a fixed order (see triangle_decompose), applied one per shared-memory
 //    sweep.  Used for complex128 and as the generic path.
-//  * CSD (complex64, 9 <= norb <= 16): V = D * (T_A1 + T_A2) * CS' * (T_B1 + T_B2),
+//  * CSD (complex64, 9 <= norb <= 18): V = D * (T_A1 + T_A2) * CS' * (T_B1 + T_B2),
 //    a cosine-sine decomposition over the halves [0,h) and [h,norb); each
-//    half-block is a fixed triangle of window Givens applied in registers,
-//    CS' is h commuting rotations on orbital pairs (i, h+i).
+//    half-block of at most 8 orbitals is a window network (brick_decompose)
+//    applied in registers, a larger one is split again the same way; CS' is
+//    h commuting rotations on orbital pairs (i, h+i).  `ops` lists the stages.
 //    For norb <= 8 the whole sector is one window ("FULL").
 #pragma once
 
@@ -34,14 +35,24 @@ struct Pair2 {  // general 2x2 unitary block on orbitals (i, j), i < j
 
 enum PlanKind { PLAN_IDENTITY = 0, PLAN_TRIANGLE = 1, PLAN_FULL = 2, PLAN_CSD = 3 };
 
+// One stage of a cosine-sine plan, in application order.
+struct StageOp {
+  int type = 0;  // 0: window network on orbitals [lo, lo + b); 1: cross-half rotations
+  int lo = 0;    // first orbital
+  int b = 0;     // window size, or the half width hh of the sites (lo + i, lo + hh + i), i < hh
+  std::vector<Givens> net;   // window: brick network (brick_order)
+  std::vector<Pair2> pairs;  // cross-half: pairs[i] on (lo + i, lo + hh + i)
+};
+
 struct SectorPlan {
   int kind = PLAN_IDENTITY;
   int norb = 0;
   int h = 0;  // split point for CSD; norb for FULL
   std::vector<Givens> tri;   // TRIANGLE / FULL network (norb(norb-1)/2)
   std::vector<int> tri_l;    // TRIANGLE: lower orbital of each rotation
-  std::vector<Givens> b1, b2, a1, a2;  // CSD window networks
-  std::vector<Pair2> cs;     // CSD middle rotations (i, h+i)
+  std::vector<Givens> b1, b2, a1, a2;  // CSD window networks (norb <= 16)
+  std::vector<Pair2> cs;     // CSD middle rotations (i, h+i) (norb <= 16)
+  std::vector<StageOp> ops;  // CSD: the stage sequence (every norb; blocks above 8 orbitals nested)
   std::vector<cd> diag;      // final per-orbital phases (norb)
   double max_err = 0.0;      // reconstruction error of the factorization
 };

@@ -63,29 +63,6 @@ int popcount(unsigned x) {
   return c;
 }
 
-// Half-sector rank tables of a sector (norb, nocc) split at h: for every
-// subset s2 of the q = norb - h high orbitals with m bits (colex index g),
-// rt[moff[m] + g] = rank contribution of s2 above a low part of nocc - m electrons.
-struct HalfTables {
-  int h, q;
-  std::vector<int> moff, rt;
-};
-
-HalfTables half_tables(int norb, int nocc, int h) {
-  HalfTables t;
-  t.h = h;
-  t.q = norb - h;
-  t.moff.assign(t.q + 2, 0);
-  for (int m = 0; m <= t.q; ++m) t.moff[m + 1] = t.moff[m] + (int)C(t.q, m);
-  t.rt.assign(t.moff[t.q + 1], 0);
-  for (int m = 0; m <= t.q; ++m)
-    for (long long g = 0; g < C(t.q, m); ++g) {
-      const int m0 = nocc - m;
-      t.rt[t.moff[m] + g] = (m0 >= 0 && m0 <= h) ? (int)rank_shifted(unrank(g, t.q, m), h, m0) : 0;
-    }
-  return t;
-}
-
 // Coefficient tables of one rotation list for win_coef<mode>.
 void put_coefs(const double* v, int n, int mode, float* gp, float* gl, unsigned* gt) {
   for (int i = 0; i < n; ++i) {
@@ -116,14 +93,15 @@ struct CsPass {
 };
 
 std::mutex g_cs_mu;
-std::map<std::tuple<int, int, int, int, int, int>, CsPass> g_cs;
+std::map<std::tuple<int, int, int, int, int, int, int>, CsPass> g_cs;
 
-// Groups of the sector (norb, nocc) under the cross-half sites [s0, s1).
-int cs_pass_tables(int norb, int nocc, int h, int s0, int s1, const CsPass** out) {
+// Groups of the sector (norb, nocc) under the cross-half sites i in [s0, s1),
+// site i rotating orbitals (lo + i, lo + hh + i).
+int cs_pass_tables(int norb, int nocc, int lo, int hh, int s0, int s1, const CsPass** out) {
   int dev = 0;
   FFGB_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_cs_mu);
-  auto key = std::make_tuple(dev, norb, nocc, h, s0, s1);
+  auto key = std::make_tuple(dev, norb, nocc, lo, hh, s0, s1);
   auto it = g_cs.find(key);
   if (it != g_cs.end()) {
     *out = &it->second;
@@ -137,25 +115,25 @@ int cs_pass_tables(int norb, int nocc, int h, int s0, int s1, const CsPass** out
     int act[4], m = 0;
     bool canonical = true;
     for (int i = s0; i < s1; ++i) {
-      const bool lo = (s >> i) & 1u, hi = (s >> (h + i)) & 1u;
-      if (lo != hi) {
+      const bool o_lo = (s >> (lo + i)) & 1u, o_hi = (s >> (lo + hh + i)) & 1u;
+      if (o_lo != o_hi) {
         act[m++] = i;
-        if (hi) canonical = false;  // the group is emitted from its all-low member
+        if (o_hi) canonical = false;  // the group is emitted from its all-low member
       }
     }
     if (m == 0 || !canonical) continue;
     std::vector<int>& T = per_m[m];
     int header = 0;
-    for (int t = 0; t < m; ++t) header |= act[t] << (3 * t);
+    for (int t = 0; t < m; ++t) header |= act[t] << (4 * t);
     T.push_back(header);
     for (int j = 0; j < (1 << m); ++j) {
       unsigned mem = s;
       for (int t = 0; t < m; ++t)
-        if ((j >> t) & 1) mem ^= (1u << act[t]) | (1u << (h + act[t]));
+        if ((j >> t) & 1) mem ^= (1u << (lo + act[t])) | (1u << (lo + hh + act[t]));
       int sign = 0;
       for (int t = 0; t < m; ++t) {
         if ((j >> t) & 1) continue;
-        const int i = act[t], jj = h + act[t];
+        const int i = lo + act[t], jj = lo + hh + act[t];
         const unsigned between = ((1u << jj) - 1u) & ~((1u << (i + 1)) - 1u);
         if (popcount(mem & between) & 1) sign |= 1 << t;
       }
@@ -196,12 +174,13 @@ int launch_cs(const CsStageParams& P, int grid, int mode, cudaStream_t st) {
   return FFGB_OK;
 }
 
-int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h, const std::vector<Pair2>& cs,
-             int mode, unsigned salt, cudaStream_t st) {
-  for (int s0 = 0; s0 < h; s0 += 4) {
-    const int s1 = std::min(h, s0 + 4);
+int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int lo, int hh,
+             const std::vector<Pair2>& cs, int mode, unsigned salt, cudaStream_t st) {
+  if (hh > CS_MAX_SITES) return fail(FFGB_ERR_UNSUPPORTED, "too many cross-half sites");
+  for (int s0 = 0; s0 < hh; s0 += 4) {
+    const int s1 = std::min(hh, s0 + 4);
     const CsPass* T = nullptr;
-    FFGB_TRY(cs_pass_tables(norb, nocc, h, s0, s1, &T));
+    FFGB_TRY(cs_pass_tables(norb, nocc, lo, hh, s0, s1, &T));
     CsStageParams P;
     std::memset(&P, 0, sizeof(P));
     P.x = x;
@@ -210,13 +189,13 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int h
     P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
     P.salt = salt * 0x9E3779B9u + 0x51ED270Bu * (unsigned)(s0 + 1);
     P.gpc = CS_MAX_GPC;
-    double v[24] = {};
-    for (int i = 0; i < h && i < 8; ++i) {
+    double v[3 * CS_MAX_SITES] = {};
+    for (int i = 0; i < hh; ++i) {
       v[3 * i] = cs[i].g00.real();
       v[3 * i + 1] = cs[i].g01.real();
       v[3 * i + 2] = cs[i].g01.imag();
     }
-    put_coefs(v, 24, mode, P.gp, P.gl, P.gt);
+    put_coefs(v, 3 * CS_MAX_SITES, mode, P.gp, P.gl, P.gt);
     for (int c = 0; c < T->n_classes; ++c) {
       P.tab = T->tab + T->cls_base[c];
       P.n_groups = T->cls_groups[c];
@@ -277,16 +256,77 @@ int stage_err_flag(int** out) {
   return FFGB_OK;
 }
 
-// One window stage.  low: window [0, h), groups = high-half patterns (members
-// are consecutive rows after a base row); otherwise window [h, norb), groups =
-// low-half patterns (row = colex rank of the pattern, members at offsets).
-// Every electron-count class k is one launch; classes k and B - k are
-// processed together (complement-packed) where their registers fit.
-int window_stage(const float2* in, float2* out, long long ld, long long ncols, int norb, int nocc,
-                 const HalfTables& T, bool low, const std::vector<Givens>& net, unsigned salt,
-                 const StageExpectArgs* ex, int* ex_ctas, cudaStream_t st) {
-  const int h = T.h, q = T.q;
-  const int b = low ? h : q;
+// Layout of a window [lo, lo + B) of the sector (norb, nocc): one class per
+// (k electrons inside, m0 electrons below lo).  A group of a class fixes the
+// occupation outside the window; its member j (colex order of the window
+// pattern w_j) sits at row base[g] + off[j] with
+//   base[g] = rank(below) + rank_shifted(above, lo + B, m0 + k),
+//   off[j]  = rank_shifted(w_j, lo, m0).
+struct WinClass {
+  int k, m0;
+  long long groups;
+  long long base_off;  // first entry of this class in the device base table
+  std::vector<int> off;
+};
+struct WinLayout {
+  std::vector<WinClass> cls;
+  int* dev_base = nullptr;
+};
+
+std::mutex g_win_mu;
+std::map<std::tuple<int, int, int, int, int>, WinLayout> g_win;
+
+int win_layout(int norb, int nocc, int lo, int B, const WinLayout** out) {
+  int dev = 0;
+  FFGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_win_mu);
+  auto key = std::make_tuple(dev, norb, nocc, lo, B);
+  auto it = g_win.find(key);
+  if (it != g_win.end()) {
+    *out = &it->second;
+    return FFGB_OK;
+  }
+  const int above = norb - lo - B;
+  WinLayout W;
+  std::vector<int> host;
+  for (int k = std::max(0, nocc - lo - above); k <= std::min(B, nocc); ++k)
+    for (int m0 = std::max(0, nocc - k - above); m0 <= std::min(lo, nocc - k); ++m0) {
+      WinClass c;
+      c.k = k;
+      c.m0 = m0;
+      const int ma = nocc - k - m0;
+      c.base_off = (long long)host.size();
+      for (long long ib = 0; ib < C(lo, m0); ++ib) {
+        const long long rb = rank(unrank(ib, lo, m0));
+        for (long long ia = 0; ia < C(above, ma); ++ia) {
+          const long long r = rb + rank_shifted(unrank(ia, above, ma), lo + B, m0 + k);
+          if (r >= (1LL << 31)) return fail(FFGB_ERR_UNSUPPORTED, "sector too large");
+          host.push_back((int)r);
+        }
+      }
+      c.groups = (long long)host.size() - c.base_off;
+      for (long long j = 0; j < C(B, k); ++j) c.off.push_back((int)rank_shifted(unrank(j, B, k), lo, m0));
+      if (c.groups > 0) W.cls.push_back(std::move(c));
+    }
+  const size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(int);
+  FFGB_CUDA(cudaMalloc(&W.dev_base, bytes));
+  if (!host.empty())
+    FFGB_CUDA(cudaMemcpy(W.dev_base, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice));
+  g_win[key] = std::move(W);
+  *out = &g_win[key];
+  return FFGB_OK;
+}
+
+// One window stage on [lo, lo + B).  Every class is one launch; classes k and
+// B - k with the same m0 are processed together (complement-packed) where
+// their registers fit, and k = B/2 is packed within its groups.
+int window_stage(const float2* in, float2* out, long long ld, long long ncols, int norb, int nocc, int lo, int B,
+                 const std::vector<Givens>& net, unsigned salt, const StageExpectArgs* ex, int* ex_ctas,
+                 cudaStream_t st) {
+  if (B < 4 || B > 8) return fail(FFGB_ERR_UNSUPPORTED, "window size outside [4, 8]");
+  const WinLayout* L = nullptr;
+  FFGB_TRY(win_layout(norb, nocc, lo, B, &L));
+  const bool low = lo == 0;  // members are consecutive rows
   auto base = std::make_unique<WinJob>();
   std::memset(base.get(), 0, sizeof(WinJob));
   base->in = in;
@@ -295,7 +335,7 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
   base->ncols = ncols;
   base->tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
   base->norb = norb;
-  base->lo = low ? 0 : h;
+  base->lo = lo;
   base->salt = salt;
   FFGB_TRY(stage_err_flag(&base->err));
   const int epi = ex ? EPI_EXPECT : EPI_STORE;
@@ -322,53 +362,49 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
         E.Xsum[l] += ex->X[i][l];
       }
   }
-  // classes: k electrons inside the window
-  const int kbeg = low ? std::max(0, nocc - q) : std::max(0, nocc - h);
-  const int kend = low ? std::min(h, nocc) : std::min(q, nocc);
-  auto in_range = [&](int k) { return k >= kbeg && k <= kend; };
-  auto count = [&](int k) { return low ? C(q, nocc - k) : C(h, nocc - k); };
   struct Job {
-    int k, kind, kb;
+    const WinClass *a, *b;
+    int kind;
     long long n, start, work;
   };
+  auto find = [&](int k, int m0) -> const WinClass* {
+    for (const WinClass& c : L->cls)
+      if (c.k == k && c.m0 == m0) return &c;
+    return nullptr;
+  };
   std::vector<Job> jobs;
-  for (int k = kbeg; k <= kend; ++k) {
-    const int kp = b - k;
-    const bool pairable = 2 * k < b && in_range(kp) && C(b, k) <= 35;
-    const bool partner_pairs = 2 * k > b && in_range(kp) && C(b, kp) <= 35;
-    if (partner_pairs) continue;
-    if (2 * k == b) {
-      // complement-packed within the group on the lower window; on the upper
-      // window its member-offset table pushes the packed kernel into spills
-      jobs.push_back({k, low ? 1 : 0, k, count(k), 0, count(k) * C(b, k)});
-    } else if (pairable) {
-      const long long np = std::min(count(k), count(kp));
-      if (np > 0) jobs.push_back({k, 2, kp, np, 0, 2 * np * C(b, k)});
-      if (count(k) > np) jobs.push_back({k, 0, k, count(k) - np, np, (count(k) - np) * C(b, k)});
-      if (count(kp) > np) jobs.push_back({kp, 0, kp, count(kp) - np, np, (count(kp) - np) * C(b, kp)});
+  for (const WinClass& c : L->cls) {
+    const int kp = B - c.k;
+    const WinClass* partner = find(kp, c.m0);
+    const bool packable = 2 * c.k < B && C(B, c.k) <= 35;
+    const bool partner_packs = 2 * c.k > B && C(B, kp) <= 35 && partner;
+    if (partner_packs) continue;  // taken with its partner
+    if (2 * c.k == B) {
+      // packed within the group on windows starting at orbital 0; elsewhere the
+      // member-offset table pushes the packed kernel into spills
+      jobs.push_back({&c, nullptr, low ? 1 : 0, c.groups, 0, c.groups * C(B, c.k)});
+    } else if (packable && partner) {
+      const long long np = std::min(c.groups, partner->groups);
+      jobs.push_back({&c, partner, 2, np, 0, 2 * np * C(B, c.k)});
+      if (c.groups > np) jobs.push_back({&c, nullptr, 0, c.groups - np, np, (c.groups - np) * C(B, c.k)});
+      if (partner->groups > np)
+        jobs.push_back({partner, nullptr, 0, partner->groups - np, np, (partner->groups - np) * C(B, kp)});
     } else {
-      jobs.push_back({k, 0, k, count(k), 0, count(k) * C(b, k)});
+      jobs.push_back({&c, nullptr, 0, c.groups, 0, c.groups * C(B, c.k)});
     }
   }
-  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& a, const Job& c) { return a.work > c.work; });
-  auto fill = [&](int k, long long start, long long n, int* bases, int* offs, int* g0) -> int {
-    if (low) {
-      const int m = nocc - k;
-      if (n > 72) return fail(FFGB_ERR_UNSUPPORTED, "window group table overflow");
-      for (long long g = 0; g < n; ++g) bases[g] = T.rt[T.moff[m] + start + g];
-    } else {
-      if (C(q, k) > 72) return fail(FFGB_ERR_UNSUPPORTED, "window member table overflow");
-      for (long long j = 0; j < C(q, k); ++j) offs[j] = T.rt[T.moff[k] + j];
-      *g0 = (int)start;
-    }
-    return FFGB_OK;
-  };
+  std::stable_sort(jobs.begin(), jobs.end(), [](const Job& x, const Job& y) { return x.work > y.work; });
   long long pbase = 0;
   WinJob P;
   for (const Job& jb : jobs) {
     std::memcpy(&P, base.get(), sizeof(WinJob));
-    FFGB_TRY(fill(jb.k, jb.start, jb.n, P.base_a, P.off_a, &P.ga0));
-    if (jb.kind == 2) FFGB_TRY(fill(jb.kb, 0, jb.n, P.base_b, P.off_b, &P.gb0));
+    if (jb.a->off.size() > 72) return fail(FFGB_ERR_UNSUPPORTED, "window member table overflow");
+    P.gbase_a = L->dev_base + jb.a->base_off + jb.start;
+    for (size_t j = 0; j < jb.a->off.size(); ++j) P.off_a[j] = jb.a->off[j];
+    if (jb.b) {
+      P.gbase_b = L->dev_base + jb.b->base_off;
+      for (size_t j = 0; j < jb.b->off.size(); ++j) P.off_b[j] = jb.b->off[j];
+    }
     P.n_groups = (int)jb.n;
     const long long items = jb.n * base->tiles;
     if (items <= 0) continue;
@@ -378,7 +414,7 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
       P.ex.partials = ex->partials + pbase;
     }
     int used = 0;
-    FFGB_TRY(launch_job_b(b, P, jb.k, jb.kind, low, epi, tma, items, st, &used));
+    FFGB_TRY(launch_job_b(B, P, jb.a->k, jb.kind, low, epi, tma, items, st, &used));
     pbase += used;
   }
   if (ex_ctas) *ex_ctas = (int)pbase;
@@ -400,38 +436,36 @@ int stage_check_timeout(cudaStream_t st) {
   return FFGB_OK;
 }
 
-long long stage_expect_partials(int norb, long long ncols) {
-  const int h = norb / 2;
-  const long long groups = 1LL << std::max(h, norb - h);
-  return groups * ((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
+long long stage_expect_partials(long long rows, long long ncols) {
+  return std::max<long long>(rows, 1) * ((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
 }
 
 int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long ld, long long ncols,
                       const SectorPlan& plan, const StageOpts& o, cudaStream_t st) {
-  if (plan.kind != PLAN_CSD) return fail(FFGB_ERR_ARG, "stage path needs a cosine-sine plan");
-  if (plan.h < 4 || plan.h > 8 || norb - plan.h < 4 || norb - plan.h > 8)
-    return fail(FFGB_ERR_UNSUPPORTED, "stage path needs half windows of 4 to 8 orbitals");
-  const HalfTables T = half_tables(norb, nocc, plan.h);
-  const float2* src = (const float2*)in;
-  float2* dst = (float2*)out;
+  if (plan.kind != PLAN_CSD || plan.ops.empty()) return fail(FFGB_ERR_ARG, "stage path needs a cosine-sine plan");
   if (o.mode != 2) return fail(FFGB_ERR_ARG, "stage kernels use dithered coefficients");
+  const int n_ops = (int)plan.ops.size();
+  if (plan.ops[0].type != 0 || plan.ops[n_ops - 1].type != 0)
+    return fail(FFGB_ERR_ARG, "a cosine-sine plan starts and ends with window stages");
   const unsigned s = o.salt * 0x2545F491u;
-  switch (o.only_stage) {
-    case -1: break;
-    case 0: return window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, s + 1, nullptr, nullptr, st);
-    case 1: return window_stage(src, dst, ld, ncols, norb, nocc, T, false, plan.b2, s + 2, nullptr, nullptr, st);
-    case 2:
-      if (in != out) return fail(FFGB_ERR_ARG, "the cross-half stage runs in place");
-      return cs_stage(dst, ld, ncols, norb, nocc, plan.h, plan.cs, o.mode, s + 3, st);
-    case 3: return window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.a1, s + 4, nullptr, nullptr, st);
-    case 4: return window_stage(src, dst, ld, ncols, norb, nocc, T, false, plan.a2, s + 5, nullptr, nullptr, st);
-    default: return fail(FFGB_ERR_ARG, "stage must be in [0, 4]");
+  int first = 0, last = n_ops - 1;
+  if (o.only_stage >= 0) {
+    if (o.only_stage >= n_ops) return fail(FFGB_ERR_ARG, "stage index out of range");
+    if (plan.ops[o.only_stage].type == 1 && in != out) return fail(FFGB_ERR_ARG, "the cross-half stage runs in place");
+    first = last = o.only_stage;
   }
-  FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, T, true, plan.b1, s + 1, nullptr, nullptr, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.b2, s + 2, nullptr, nullptr, st));
-  FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, plan.h, plan.cs, o.mode, s + 3, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, true, plan.a1, s + 4, nullptr, nullptr, st));
-  FFGB_TRY(window_stage(dst, dst, ld, ncols, norb, nocc, T, false, plan.a2, s + 5, o.expect, o.expect_ctas, st));
+  for (int i = first; i <= last; ++i) {
+    const StageOp& op = plan.ops[i];
+    const float2* src = (const float2*)(i == first ? in : out);
+    float2* dst = (float2*)out;
+    if (op.type == 0) {
+      const bool fused = o.expect && i == n_ops - 1 && o.only_stage < 0;
+      FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, op.lo, op.b, op.net, s + 1 + i,
+                            fused ? o.expect : nullptr, fused ? o.expect_ctas : nullptr, st));
+    } else {
+      FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, op.lo, op.b, op.pairs, o.mode, s + 1 + i, st));
+    }
+  }
   return FFGB_OK;
 }
 

@@ -41,9 +41,9 @@ struct WinJob {
   long long ncols;  // columns processed
   int tiles;        // column tiles per group
   int norb, lo;     // orbitals; first orbital of the window
-  int ga0, gb0;     // window [h, norb): first group (= its low-half rank) of class K / B - K
-  int base_a[72], base_b[72];  // window [0, h): base rows of the groups
-  int off_a[72], off_b[72];    // window [h, norb): member row offsets of class K / B - K
+  const int* gbase_a;  // base row of every group of class K (device table)
+  const int* gbase_b;  // and of the paired class B - K (packed launches)
+  int off_a[72], off_b[72];    // member row offsets from the base row (windows not starting at orbital 0)
   float gp[84], gl[84];        // window network coefficients (see win_coef)
   unsigned gt[84];
   unsigned salt;
@@ -153,8 +153,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
   const long long col = (long long)tile * STAGE_THREADS + threadIdx.x;
   const bool active = col < P.ncols;
   if (!EXPECT && !active) return;
-  const long long ra = LOW ? (long long)P.base_a[g] : (long long)(P.ga0 + g);
-  const long long rb = LOW ? (long long)P.base_b[g] : (long long)(P.gb0 + g);
+  const long long ra = P.gbase_a[g];
+  const long long rb = P.gbase_b ? (long long)P.gbase_b[g] : ra;
   unsigned rng = dither_seed((unsigned long long)col, P.salt);
   const long long ld = P.ld;
   // member j of group A (class K) / group B (class B - K): row offset from the group's base
@@ -334,8 +334,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
   auto group_rows = [&](long long it, long long& ra, long long& rb, long long& col0) {
     const int g = (int)(it / P.tiles);
     col0 = (it - (long long)g * P.tiles) * STAGE_THREADS;
-    ra = LOW ? (long long)P.base_a[g] : (long long)(P.ga0 + g);
-    rb = LOW ? (long long)P.base_b[g] : (long long)(P.gb0 + g);
+    ra = P.gbase_a[g];
+    rb = P.gbase_b ? (long long)P.gbase_b[g] : ra;
   };
   auto issue = [&](long long it) {  // one thread: the bulk copies of item `it`
     long long ra, rb, col0;
@@ -458,16 +458,17 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
   }
 }
 
-// Cross-half rotations (i, h + i) of up to four sites in one pass.  A group is
-// the set of strings that agree everywhere except in which orbital of each
-// "active" pair (exactly one of i, h + i occupied) is occupied: 2^M members
+// Cross-half rotations (lo + i, lo + hh + i) of up to four sites in one pass.  A
+// group is the set of strings that agree everywhere except in which orbital of
+// each "active" pair (exactly one of the two occupied) is occupied: 2^M members
 // for M active sites.  Table entry per group: a header with the active sites
-// (3 bits each, ascending), then per member its row | (sign bits << 24); bit
+// (4 bits each, ascending), then per member its row | (sign bits << 24); bit
 // 24 + t is the parity of the occupied orbitals strictly between the two
 // orbitals of active site t, read on the member whose lower orbital is
 // occupied.  Pairs with both or neither orbital occupied are left alone: the
 // 2x2 blocks of the plan have determinant 1.
-constexpr int CS_MAX_GPC = 8;  // groups per CTA of the cross-half stage (at most)
+constexpr int CS_MAX_GPC = 8;     // groups per CTA of the cross-half stage (at most)
+constexpr int CS_MAX_SITES = 12;  // cross-half sites of one stage (at most)
 
 struct CsStageParams {
   float2* x;
@@ -476,8 +477,8 @@ struct CsStageParams {
   int n_groups;
   int tiles;
   int gpc;  // groups per CTA (one column tile each), an even number <= CS_MAX_GPC
-  float gp[24], gl[24];  // per site (c, Re t, Im t), see win_coef
-  unsigned gt[24];
+  float gp[3 * CS_MAX_SITES], gl[3 * CS_MAX_SITES];  // per site (c, Re t, Im t), see win_coef
+  unsigned gt[3 * CS_MAX_SITES];
   unsigned salt;
 };
 
@@ -489,7 +490,7 @@ __device__ __forceinline__ void cs_rotate(float2 (&v)[1 << M], const int (&e)[1 
   constexpr int NM = 1 << M;
 #pragma unroll
   for (int t = 0; t < M; ++t) {
-    const int site = (sites >> (3 * t)) & 7;
+    const int site = (sites >> (4 * t)) & 15;
     float c, sr, si, cl, srl, sil;
     win_coef<MODE>(gp, gl, gt, site, rng, c, sr, si, cl, srl, sil);
 #pragma unroll

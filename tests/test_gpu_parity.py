@@ -278,3 +278,36 @@ def test_lucj_energy_matches_oracle(cuda):
     e64 = f.lucj_energy(ucj, ham, norb, nelec, dtype=torch.complex64)
     assert abs(e128 - e_ref) < 1e-10
     assert abs(e64 - e_ref) < 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("norb, nelec", [(17, (3, 4)), (18, (3, 2)), (18, (4, 4))])
+def test_nested_cosine_sine_plans(cuda, norb, nelec):
+    """norb 17 and 18: 9-orbital halves split again (4 + 5) on the complex64
+    stage path, against the complex128 path (shared-memory kernel with the
+    adjacent-Givens network) on the same inputs."""
+    import torch
+
+    import ffsim_gb300 as f
+
+    rng = np.random.default_rng(norb * 10 + nelec[0])
+    d = f.dim(norb, nelec)
+    v = rng.standard_normal(d) + 1j * rng.standard_normal(d)
+    v /= np.linalg.norm(v)
+    u = f.random.random_unitary(norb, seed=rng)
+    j = f.random.random_symmetric_matrix_normal(norb, scale=0.1, seed=rng)
+    for op in ("rot", "dc"):
+        outs = {}
+        for dtype in (torch.complex64, torch.complex128):
+            t = torch.tensor(v, dtype=dtype, device=cuda)
+            if op == "rot":
+                t = f.apply_orbital_rotation(t, u, norb, nelec)
+            else:
+                t = f.apply_diag_coulomb_evolution(t, j, 0.7, norb, nelec, orbital_rotation=u)
+            outs[dtype] = t.cpu().numpy().astype(np.complex128)
+        assert np.linalg.norm(outs[torch.complex64] - outs[torch.complex128]) < 2e-5, op
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=3, seed=5)
+    ucj = f.random.random_ucj_op_spin_balanced(norb, n_reps=1, seed=6)
+    e64 = f.lucj_energy(ucj, ham, norb, nelec, dtype=torch.complex64)
+    e128 = f.lucj_energy(ucj, ham, norb, nelec, dtype=torch.complex128)
+    assert abs(e64 - e128) < 1e-5
