@@ -244,13 +244,16 @@ def run_ops(args) -> None:
     rng = np.random.default_rng(7)
     u = _lib.cmat(f.random.random_unitary(norb, seed=rng))
     jm = np.asarray(f.random.random_symmetric_matrix_normal(norb, scale=0.1, seed=rng), dtype=np.float64)
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=norb, seed=11)
+    ob, dcm, hrots = ham._arrays()
+    eout = np.zeros(1)
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
     with torch.cuda.stream(stream):
         v = torch.randn(d, dtype=dtype, device="cuda")
         v /= torch.linalg.vector_norm(v)
         out = torch.empty_like(v)
-        buf, nbytes = scratch(v, 1, norb, *nelec)
+        buf, nbytes = scratch(v, 2, norb, *nelec)
 
     def timed(fn):
         for _ in range(2):
@@ -278,6 +281,11 @@ def run_ops(args) -> None:
         "rotated_diag_matvec": (9 * S, lambda: _lib.call(
             "ffgb_rotated_diag_matvec", v.data_ptr(), out.data_ptr(), code, norb, nelec[0], nelec[1], None,
             _lib.dptr(jm), 0, _lib.dptr(u), 1, buf.data_ptr(), nbytes, sptr)),
+        # energy of a rank-norb double-factorized Hamiltonian: R + 1 terms, 3 S each
+        f"df_energy_rank{norb}": (3 * S * (norb + 1), lambda: _lib.call(
+            "ffgb_df_expectation", v.data_ptr(), code, norb, nelec[0], nelec[1], _lib.dptr(ob), dcm.shape[0],
+            _lib.dptr(dcm), hrots.ctypes.data_as(_lib._dp), float(ham.constant), 0, None, _lib.dptr(eout),
+            buf.data_ptr(), nbytes, sptr)),
     }
     for name, (nb, fn) in ops.items():
         try:
