@@ -267,11 +267,15 @@ def run_ops(args) -> None:
         torch.cuda.synchronize()
         return a.elapsed_time(b) / args.reps
 
+    # stage sequences: three 8-orbital windows up to norb 12; windows on the
+    # halves around the cross-half stage (index 2) up to 16; for 17 and 18 one
+    # window and three overlapping windows on each side of it (index 4)
+    cs_index = None if norb <= 12 else (2 if norb <= 16 else 4)
     ops = {
         "window_stage": (2 * S, lambda: _lib.call("ffgb_debug_stage", v.data_ptr(), code, norb, nelec[0], nelec[1],
                                                   _lib.dptr(u), 0, sptr)),
         "cross_half_stage": (2 * S, lambda: _lib.call("ffgb_debug_stage", v.data_ptr(), code, norb, nelec[0],
-                                                      nelec[1], _lib.dptr(u), 2, sptr)),
+                                                      nelec[1], _lib.dptr(u), cs_index, sptr)),
         "orbital_rotation": (4 * S, lambda: _lib.call("ffgb_apply_orbital_rotation", v.data_ptr(), code, norb,
                                                       nelec[0], nelec[1], _lib.dptr(u), _lib.dptr(u),
                                                       buf.data_ptr(), nbytes, sptr)),
@@ -287,6 +291,8 @@ def run_ops(args) -> None:
             _lib.dptr(dcm), hrots.ctypes.data_as(_lib._dp), float(ham.constant), 0, None, _lib.dptr(eout),
             buf.data_ptr(), nbytes, sptr)),
     }
+    if cs_index is None:
+        del ops["cross_half_stage"]
     for name, (nb, fn) in ops.items():
         try:
             ms = timed(fn)

@@ -299,9 +299,10 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
     if (A.apply_dphase) {
       bool trivial = true;
       for (int i = 0; i < norb; ++i) {
-        P->dphase[i][0] = (T)pl.diag[i].real();
-        P->dphase[i][1] = (T)pl.diag[i].imag();
-        if (std::abs(pl.diag[i] - cd(1.0)) > 1e-15) trivial = false;
+        const cd di = pl.kind == PLAN_CSD ? pl.csd_diag[i] : pl.diag[i];
+        P->dphase[i][0] = (T)di.real();
+        P->dphase[i][1] = (T)di.imag();
+        if (std::abs(di - cd(1.0)) > 1e-15) trivial = false;
       }
       P->has_dphase = trivial ? 0 : 1;
     }
@@ -1230,6 +1231,29 @@ int ffgb_debug_plan(const double* mat, int norb, int use_windows, double* out, i
     for (cd z : {c.g00, c.g01, c.g10, c.g11}) {
       o.push_back(z.real());
       o.push_back(z.imag());
+    }
+  }
+  // the five-stage form's phases, then the stage sequence with its phases
+  const std::vector<cd>& d5 = p.kind == PLAN_CSD ? p.csd_diag : p.diag;
+  o.push_back((double)d5.size());
+  for (cd z : d5) {
+    o.push_back(z.real());
+    o.push_back(z.imag());
+  }
+  o.push_back((double)p.ops.size());
+  for (const StageOp& op : p.ops) {
+    o.push_back(op.type);
+    o.push_back(op.lo);
+    o.push_back(op.b);
+    put_g(op.net);
+    o.push_back((double)op.pairs.size());
+    for (auto& c : op.pairs) {
+      o.push_back(c.i);
+      o.push_back(c.j);
+      for (cd z : {c.g00, c.g01, c.g10, c.g11}) {
+        o.push_back(z.real());
+        o.push_back(z.imag());
+      }
     }
   }
   o.push_back((double)p.diag.size());

@@ -405,10 +405,82 @@ std::vector<cd> brick_matrix(int b, const std::vector<Givens>& rots, const std::
 }
 }  // namespace
 
+// X (n x n, 8 < n <= 12) on orbitals [lo, lo + n) as three overlapping
+// windows of 8: X = diag(1, A) * diag(B, 1) * diag(1, C), A and C on the last
+// eight orbitals, B on the first eight (the last stage then never starts at
+// orbital 0).  With t = n - 8 head orbitals: A^dag maps the last-eight-row part
+// of the t head columns into the rows [t, 2t) (a QR factorization), which lie
+// inside B's window when t <= 4; B^dag then maps the head columns onto unit
+// vectors, so B^dag A^dag X = diag(1, C).  Each window's phases are pushed into
+// the next window (the ones outside a window commute with it); d gets the rest.
+bool three_windows(int n, const cd* X, int lo, std::vector<StageOp>& ops, std::vector<cd>& d) {
+  const int t = n - 8;
+  if (t < 1 || t > 4) return false;
+  std::vector<cd> Y(X, X + (size_t)n * n);
+  auto left_apply_dag = [&](const std::vector<cd>& U, int r0) {  // rows [r0, r0 + 8) of Y <- U^dag rows
+    std::vector<cd> tmp((size_t)8 * n, cd(0));
+    for (int r = 0; r < 8; ++r)
+      for (int k = 0; k < 8; ++k) {
+        const cd u = std::conj(U[(size_t)k * 8 + r]);
+        if (u == cd(0)) continue;
+        for (int c = 0; c < n; ++c) tmp[(size_t)r * n + c] += u * Y[(size_t)(r0 + k) * n + c];
+      }
+    std::copy(tmp.begin(), tmp.end(), Y.begin() + (size_t)r0 * n);
+  };
+  // A: Q^dag Z = R, nonzero in its first t rows
+  std::vector<cd> Z((size_t)8 * t), A, R;
+  for (int r = 0; r < 8; ++r)
+    for (int c = 0; c < t; ++c) Z[(size_t)r * t + c] = Y[(size_t)(t + r) * n + c];
+  householder_qr(8, t, Z, A, R);
+  left_apply_dag(A, t);
+  // B = [W | complement of W], W = rows [0, 8) of the head columns (orthonormal)
+  std::vector<cd> Wm((size_t)8 * t), Q2, R2;
+  for (int r = 0; r < 8; ++r)
+    for (int c = 0; c < t; ++c) Wm[(size_t)r * t + c] = Y[(size_t)r * n + c];
+  householder_qr(8, t, Wm, Q2, R2);
+  std::vector<cd> B((size_t)64);
+  for (int r = 0; r < 8; ++r) {
+    for (int c = 0; c < t; ++c) B[(size_t)r * 8 + c] = Wm[(size_t)r * t + c];
+    for (int c = t; c < 8; ++c) B[(size_t)r * 8 + c] = Q2[(size_t)r * 8 + c];
+  }
+  left_apply_dag(B, 0);
+  // Y = diag(1, C) now
+  double off = 0;
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c)
+      if (r < t || c < t) off = std::max(off, std::abs(Y[(size_t)r * n + c] - (r == c ? cd(1) : cd(0))));
+  if (off > 1e-10) return false;
+  std::vector<cd> C((size_t)64);
+  for (int r = 0; r < 8; ++r)
+    for (int c = 0; c < 8; ++c) C[(size_t)r * 8 + c] = Y[(size_t)(t + r) * n + t + c];
+  StageOp wc, wb, wa;
+  wc.type = wb.type = wa.type = 0;
+  wc.b = wb.b = wa.b = 8;
+  wc.lo = wa.lo = lo + t;
+  wb.lo = lo;
+  std::vector<cd> dC, dB, dA;
+  if (!brick_decompose(8, C.data(), wc.net, dC)) return false;
+  for (int r = 0; r < 8; ++r)  // C's phases on orbitals [t, 8) into B's columns
+    for (int c = t; c < 8; ++c) B[(size_t)r * 8 + c] *= dC[c - t];
+  if (!brick_decompose(8, B.data(), wb.net, dB)) return false;
+  for (int r = 0; r < 8; ++r)  // B's phases on [t, 8) and C's on [8, n) into A's columns
+    for (int c = 0; c < 8; ++c) A[(size_t)r * 8 + c] *= t + c < 8 ? dB[t + c] : dC[c];
+  if (!brick_decompose(8, A.data(), wa.net, dA)) return false;
+  d.assign(n, cd(1));
+  for (int i = 0; i < t; ++i) d[i] = dB[i];
+  for (int i = t; i < n; ++i) d[i] = dA[i - t];
+  ops.push_back(std::move(wc));
+  ops.push_back(std::move(wb));
+  ops.push_back(std::move(wa));
+  return true;
+}
+
 // X (n x n, unitary) on orbitals [lo, lo + n) = diag(d) * (ops appended here,
-// applied first to last).  Blocks of at most 8 orbitals are one window; larger
-// blocks are split by a cosine-sine decomposition whose right blocks' phases
-// are pushed through the cross-half rotations into the left blocks.
+// applied first to last).  Blocks of at most 8 orbitals are one window, of 9 to
+// 12 orbitals three overlapping windows; larger blocks are split by a
+// cosine-sine decomposition (halves of at most 8 orbitals up to 16, else 8
+// plus the rest) whose right blocks' phases are pushed through the cross-half
+// rotations into the left blocks.
 bool block_ops(int n, const cd* X, int lo, std::vector<StageOp>& ops, std::vector<cd>& d) {
   if (n <= 8) {
     StageOp w;
@@ -419,7 +491,12 @@ bool block_ops(int n, const cd* X, int lo, std::vector<StageOp>& ops, std::vecto
     ops.push_back(std::move(w));
     return true;
   }
-  const int h = n / 2, q = n - h;
+  if (n <= 12) {
+    const size_t mark = ops.size();
+    if (three_windows(n, X, lo, ops, d)) return true;
+    ops.resize(mark);
+  }
+  const int h = n <= 16 ? n / 2 : 8, q = n - h;
   std::vector<cd> A1, A2, B1, B2;
   std::vector<double> cv, sv;
   double err = 0;
@@ -513,7 +590,7 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
   const int h = norb / 2, q = norb - h;
   if (q > 8) {  // nested blocks: the stage sequence only
     plan.kind = PLAN_CSD;
-    plan.h = h;
+    plan.h = 8;
     if (!block_ops(norb, V, 0, plan.ops, plan.diag)) return plan_sector(norb, V, false, plan);
     std::vector<cd> M = ops_matrix(norb, plan.ops, plan.diag);
     double e = 0;
@@ -608,6 +685,21 @@ bool plan_sector(int norb, const cd* V, bool want_csd, SectorPlan& plan) {
   c.b = h;
   c.pairs = plan.cs;
   plan.ops = {window(0, h, plan.b1), window(h, q, plan.b2), c, window(0, h, plan.a1), window(h, q, plan.a2)};
+  plan.csd_diag = plan.diag;
+  if (norb <= 12) {  // three windows instead of five stages
+    std::vector<StageOp> ops3;
+    std::vector<cd> d3;
+    if (three_windows(norb, V, 0, ops3, d3)) {
+      std::vector<cd> M = ops_matrix(norb, ops3, d3);
+      double e3 = 0;
+      for (size_t i = 0; i < M.size(); ++i) e3 = std::max(e3, std::abs(M[i] - V[i]));
+      if (e3 <= 1e-10) {
+        plan.ops = std::move(ops3);
+        plan.diag = std::move(d3);
+        plan.max_err = std::max(plan.max_err, e3);
+      }
+    }
+  }
   return true;
 }
 

@@ -11,8 +11,12 @@
 //  * CSD (complex64, 9 <= norb <= 18): V = D * (T_A1 + T_A2) * CS' * (T_B1 + T_B2),
 //    a cosine-sine decomposition over the halves [0,h) and [h,norb); each
 //    half-block of at most 8 orbitals is a window network (brick_decompose)
-//    applied in registers, a larger one is split again the same way; CS' is
-//    h commuting rotations on orbital pairs (i, h+i).  `ops` lists the stages.
+//    applied in registers, one of 9 to 12 orbitals three overlapping windows
+//    (three_windows); CS' is h commuting rotations on orbital pairs (i, h+i).
+//    `ops` lists the stages of the stage kernels: three windows for
+//    norb <= 12, five stages up to 16, nine for 17 and 18 (h = 8).  For
+//    norb <= 16 the fields b1 .. a2, cs keep the five-stage form for the
+//    sector kernel, with its phases in csd_diag.
 //    For norb <= 8 the whole sector is one window ("FULL").
 #pragma once
 
@@ -53,7 +57,8 @@ struct SectorPlan {
   std::vector<Givens> b1, b2, a1, a2;  // CSD window networks (norb <= 16)
   std::vector<Pair2> cs;     // CSD middle rotations (i, h+i) (norb <= 16)
   std::vector<StageOp> ops;  // CSD: the stage sequence (every norb; blocks above 8 orbitals nested)
-  std::vector<cd> diag;      // final per-orbital phases (norb)
+  std::vector<cd> diag;      // final per-orbital phases (norb); of `ops` for CSD plans
+  std::vector<cd> csd_diag;  // CSD, norb <= 16: the phases of the five-stage form (b1 .. a2, cs)
   double max_err = 0.0;      // reconstruction error of the factorization
 };
 
@@ -74,6 +79,12 @@ void brick_order(int b, std::vector<int>& l);
 bool csd(int n, int h, const cd* V, std::vector<cd>& A1, std::vector<cd>& A2,
          std::vector<double>& cosv, std::vector<double>& sinv, std::vector<cd>& B1,
          std::vector<cd>& B2, double tol, double* err);
+
+// X (n x n, 8 < n <= 12) on orbitals [lo, lo + n) = diag(d) * three windows of
+// eight orbitals (appended to ops, applied first to last).
+bool three_windows(int n, const cd* X, int lo, std::vector<StageOp>& ops, std::vector<cd>& d);
+// diag(D) * (ops applied in order) as an n x n matrix.
+std::vector<cd> ops_matrix(int n, const std::vector<StageOp>& ops, const std::vector<cd>& D);
 
 // Build the plan for W(V) on a sector with nocc electrons in norb orbitals.
 // want_csd selects the register-window factorization when norb allows it.

@@ -70,7 +70,9 @@ int ffgb_eigh(const double* mat, int n, double* eigvals, double* vecs);
 
 /* Plan of W(mat) on one spin sector, serialized for inspection/tests:
  * out[0]=kind, out[1]=h, out[2]=max reconstruction error, then the plan
- * coefficients.  Returns the number of doubles written in *len. */
+ * coefficients: the sector-kernel networks and phases, then the stage
+ * sequence of the stage kernels (windows and cross-half rotations) with its
+ * phases.  Returns the number of doubles written in *len. */
 int ffgb_debug_plan(const double* mat, int norb, int use_windows, double* out, int cap, int* len);
 
 /* One stage of the complex64 cosine-sine plan of W(mat) on the alpha sector of

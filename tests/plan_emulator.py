@@ -58,7 +58,54 @@ def parse(buf):
         cs.append((i, j, g))
     nd = int(next(it))
     diag = np.array([complex(next(it), next(it)) for _ in range(nd)])
-    return dict(kind=kind, h=h, err=err, tri=tri, b1=b1, b2=b2, a1=a1, a2=a2, cs=cs, diag=diag)
+    ops = []
+    for _ in range(int(next(it))):
+        typ, lo, b = int(next(it)), int(next(it)), int(next(it))
+        net = giv()
+        pairs = []
+        for _ in range(int(next(it))):
+            i, j = int(next(it)), int(next(it))
+            pairs.append((i, j, [complex(next(it), next(it)) for _ in range(4)]))
+        ops.append(dict(type=typ, lo=lo, b=b, net=net, pairs=pairs))
+    nd = int(next(it))
+    ops_diag = np.array([complex(next(it), next(it)) for _ in range(nd)])
+    return dict(kind=kind, h=h, err=err, tri=tri, b1=b1, b2=b2, a1=a1, a2=a2, cs=cs, diag=diag, ops=ops,
+                ops_diag=ops_diag)
+
+
+def apply_ops(plan, vec, norb, nocc):
+    """The stage sequence of a cosine-sine plan applied string by string:
+    window networks on orbitals (lo + l, lo + l + 1) and cross-half rotations
+    on (i, j) with the fermionic sign of the occupied orbitals between them,
+    then the final orbital phases."""
+    v = np.array(vec, dtype=complex)
+    strings = sorted(sum(1 << i for i in c) for c in itertools.combinations(range(norb), nocc))
+    addr = {s: a for a, s in enumerate(strings)}
+    for op in plan["ops"]:
+        if op["type"] == 0:
+            for (c, s), l in zip(op["net"], _brick(op["b"])):
+                a = op["lo"] + l
+                for st in strings:
+                    if (st >> a) & 1 and not (st >> (a + 1)) & 1:
+                        _rot(v, addr[st], addr[st ^ (3 << a)], c, s)
+        else:
+            for pi, pj, g in op["pairs"]:
+                between = ((1 << pj) - 1) & ~((1 << (pi + 1)) - 1)
+                for st in strings:
+                    if (st >> pi) & 1 and not (st >> pj) & 1:
+                        x, y = addr[st], addr[st ^ (1 << pi) ^ (1 << pj)]
+                        sgn = -1.0 if bin(st & between).count("1") & 1 else 1.0
+                        vx, vy = v[x], v[y]
+                        v[x] = g[0] * vx + g[1] * sgn * vy
+                        v[y] = g[2] * sgn * vx + g[3] * vy
+    d = plan["ops_diag"]
+    for a, st in enumerate(strings):
+        ph = 1.0 + 0j
+        for i in range(norb):
+            if (st >> i) & 1:
+                ph *= d[i]
+        v[a] *= ph
+    return v
 
 
 def _rot(v, x, y, c, s):

@@ -99,6 +99,41 @@ def test_plan_addressing_matches_oracle(norb, nocc, use_windows):
     np.testing.assert_allclose(got, o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-12)
 
 
+@pytest.mark.parametrize("norb, nocc, n_stages", [(9, 1, 3), (9, 4, 3), (10, 3, 3), (11, 5, 3), (12, 3, 3),
+                                                   (13, 2, 5), (16, 2, 5), (17, 2, 9), (17, 3, 9), (18, 2, 9),
+                                                   (18, 3, 9)])
+def test_stage_sequence_matches_oracle(norb, nocc, n_stages):
+    """The stage kernels' sequence (three overlapping windows up to 12
+    orbitals, cosine-sine stages above) applied string by string equals W(U)."""
+    rng = np.random.default_rng(norb * 7 + nocc)
+    u = o.random_unitary(norb, seed=rng)
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=rng)
+    plan = _plan(u, True)
+    assert plan["kind"] == 3 and plan["err"] < 1e-10
+    assert len(plan["ops"]) == n_stages
+    assert all(op["b"] <= 8 for op in plan["ops"] if op["type"] == 0)
+    got = pe.apply_ops(plan, vec, norb, nocc)
+    np.testing.assert_allclose(got, o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-11)
+
+
+def test_stage_sequence_special_matrices():
+    """Block-diagonal, permutation and identity unitaries: the three-window form,
+    or the generic network where the cosine-sine form degenerates."""
+    for norb, nocc in [(9, 3), (10, 4), (12, 2)]:
+        blk = np.zeros((norb, norb), dtype=complex)
+        blk[:8, :8] = o.random_unitary(8, seed=4)
+        blk[8:, 8:] = o.random_unitary(norb - 8, seed=5)
+        for u in [np.eye(norb, dtype=complex), np.eye(norb)[::-1].astype(complex),
+                  np.roll(np.eye(norb), 5, axis=0).astype(complex), blk]:
+            plan = _plan(u, True)
+            assert plan["err"] < 1e-10
+            vec = o.random_state_vector(math.comb(norb, nocc), seed=6)
+            apply = pe.apply_ops if plan["kind"] == 3 else pe.apply_plan
+            assert plan["kind"] == 1 or len(plan["ops"]) == 3
+            np.testing.assert_allclose(apply(plan, vec, norb, nocc),
+                                       o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-11)
+
+
 def test_plan_special_matrices():
     """Identity, permutations and block-diagonal unitaries (degenerate cosine-sine cases)."""
     for norb, nocc in [(10, 5), (12, 5), (16, 8)]:
