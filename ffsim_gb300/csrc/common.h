@@ -67,10 +67,6 @@ struct StageOpts {
 int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long ld, long long ncols,
                       const SectorPlan& plan, const StageOpts& o, cudaStream_t st);
 
-// FFGB_ERR_TIMEOUT if a bounded wait of a pipelined window stage gave up since
-// the last check (synchronizes the stream).
-int stage_check_timeout(cudaStream_t st);
-
 // Upper bound of the partial sums written by a fused expectation on a state
 // of `rows` rows (the rotated sector's strings) and ncols columns.
 long long stage_expect_partials(long long rows, long long ncols);

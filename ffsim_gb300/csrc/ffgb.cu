@@ -1029,7 +1029,6 @@ static int df_expectation_impl(const void* vec, int norb, int na, int nb, const 
   if (!terms.empty())
     FFGB_CUDA(cudaMemcpyAsync(h.data(), slots, sizeof(double) * terms.size(), cudaMemcpyDeviceToHost, st));
   FFGB_CUDA(cudaStreamSynchronize(st));
-  if (sizeof(T) == 4) FFGB_TRY(stage_check_timeout(st));
   double e = constant;
   for (size_t k = 0; k < terms.size(); ++k) e += h[k];
   *energy = e;

@@ -5,7 +5,7 @@
 namespace ffgb {
 
 #define FFGB_WIN_INST(K)                                                                              \
-  template int launch_win_bk<WIN_B, K>(const WinJob&, int, bool, int, bool, long long, cudaStream_t, int*);
+  template int launch_win_bk<WIN_B, K>(const WinJob&, int, bool, int, long long, cudaStream_t, int*);
 
 #if WIN_K0 <= 0 && 0 <= WIN_K1
 FFGB_WIN_INST(0)

@@ -16,7 +16,7 @@
 namespace ffgb {
 
 template <int B, int K>
-int launch_win_bk(const WinJob& P, int kind, bool low, int epi, bool tma, long long items, cudaStream_t st,
+int launch_win_bk(const WinJob& P, int kind, bool low, int epi, long long items, cudaStream_t st,
                   int* grid_used);
 
 namespace {
@@ -215,45 +215,26 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int l
 }
 
 template <int B, int K = 0>
-int launch_job_k(int k, const WinJob& P, int kind, bool low, int epi, bool tma, long long items, cudaStream_t st,
+int launch_job_k(int k, const WinJob& P, int kind, bool low, int epi, long long items, cudaStream_t st,
                  int* grid_used) {
   if constexpr (K <= B) {
-    if (k == K) return launch_win_bk<B, K>(P, kind, low, epi, tma, items, st, grid_used);
-    return launch_job_k<B, K + 1>(k, P, kind, low, epi, tma, items, st, grid_used);
+    if (k == K) return launch_win_bk<B, K>(P, kind, low, epi, items, st, grid_used);
+    return launch_job_k<B, K + 1>(k, P, kind, low, epi, items, st, grid_used);
   } else {
     return fail(FFGB_ERR_ARG, "window class out of range");
   }
 }
 
-int launch_job_b(int b, const WinJob& P, int k, int kind, bool low, int epi, bool tma, long long items,
+int launch_job_b(int b, const WinJob& P, int k, int kind, bool low, int epi, long long items,
                  cudaStream_t st, int* grid_used) {
   switch (b) {
-    case 4: return launch_job_k<4>(k, P, kind, low, epi, tma, items, st, grid_used);
-    case 5: return launch_job_k<5>(k, P, kind, low, epi, tma, items, st, grid_used);
-    case 6: return launch_job_k<6>(k, P, kind, low, epi, tma, items, st, grid_used);
-    case 7: return launch_job_k<7>(k, P, kind, low, epi, tma, items, st, grid_used);
-    case 8: return launch_job_k<8>(k, P, kind, low, epi, tma, items, st, grid_used);
+    case 4: return launch_job_k<4>(k, P, kind, low, epi, items, st, grid_used);
+    case 5: return launch_job_k<5>(k, P, kind, low, epi, items, st, grid_used);
+    case 6: return launch_job_k<6>(k, P, kind, low, epi, items, st, grid_used);
+    case 7: return launch_job_k<7>(k, P, kind, low, epi, items, st, grid_used);
+    case 8: return launch_job_k<8>(k, P, kind, low, epi, items, st, grid_used);
     default: return fail(FFGB_ERR_UNSUPPORTED, "window size outside [4, 8]");
   }
-}
-
-std::mutex g_err_mu;
-std::map<int, int*> g_err_flag;
-
-// Per-device flag that a bounded wait of the pipelined kernel gave up.
-int stage_err_flag(int** out) {
-  int dev = 0;
-  FFGB_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(g_err_mu);
-  auto it = g_err_flag.find(dev);
-  if (it == g_err_flag.end()) {
-    int* f = nullptr;
-    FFGB_CUDA(cudaMalloc(&f, sizeof(int)));
-    FFGB_CUDA(cudaMemset(f, 0, sizeof(int)));
-    it = g_err_flag.emplace(dev, f).first;
-  }
-  *out = it->second;
-  return FFGB_OK;
 }
 
 // Layout of a window [lo, lo + B) of the sector (norb, nocc): one class per
@@ -337,10 +318,7 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
   base->norb = norb;
   base->lo = lo;
   base->salt = salt;
-  FFGB_TRY(stage_err_flag(&base->err));
   const int epi = ex ? EPI_EXPECT : EPI_STORE;
-  // bulk copies need 16-byte aligned rows and an even number of columns
-  const bool tma = ((uintptr_t)in % 16 == 0) && (ld % 2 == 0) && (ncols % 2 == 0);
   std::vector<double> v(3 * net.size());
   for (size_t g = 0; g < net.size(); ++g) {
     v[3 * g] = net[g].c;
@@ -414,7 +392,7 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
       P.ex.partials = ex->partials + pbase;
     }
     int used = 0;
-    FFGB_TRY(launch_job_b(B, P, jb.a->k, jb.kind, low, epi, tma, items, st, &used));
+    FFGB_TRY(launch_job_b(B, P, jb.a->k, jb.kind, low, epi, items, st, &used));
     pbase += used;
   }
   if (ex_ctas) *ex_ctas = (int)pbase;
@@ -422,19 +400,6 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
 }
 
 }  // namespace
-
-int stage_check_timeout(cudaStream_t st) {
-  int* f = nullptr;
-  FFGB_TRY(stage_err_flag(&f));
-  int h = 0;
-  FFGB_CUDA(cudaMemcpyAsync(&h, f, sizeof(int), cudaMemcpyDeviceToHost, st));
-  FFGB_CUDA(cudaStreamSynchronize(st));
-  if (h) {
-    FFGB_CUDA(cudaMemsetAsync(f, 0, sizeof(int), st));
-    return fail(FFGB_ERR_TIMEOUT, "a window stage gave up waiting for its bulk copies");
-  }
-  return FFGB_OK;
-}
 
 long long stage_expect_partials(long long rows, long long ncols) {
   return std::max<long long>(rows, 1) * ((ncols + STAGE_THREADS - 1) / STAGE_THREADS);

@@ -49,7 +49,6 @@ struct WinJob {
   unsigned salt;
   StageExpect ex;        // partials of this launch start at ex.partials
   int n_groups;          // groups (or group pairs) of this launch
-  int* err;              // set to 1 when a bounded wait of the pipelined kernel gives up
 };
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
@@ -244,217 +243,6 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
     __shared__ double sh[STAGE_THREADS / 32];
     const double s = block_sum_128(part, sh);
     if (threadIdx.x == 0) P.ex.partials[blockIdx.x] = s;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Pipelined window stage: bulk asynchronous copies (TMA) of the next item into
-// shared memory while the current item is rotated in registers.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_init_fence() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
-  asm volatile(
-      "{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
-      "r"(bytes)
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-// orders this thread's shared-memory reads before later asynchronous (TMA) writes
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-constexpr unsigned WIN_WAIT_LIMIT = 1u << 22;  // try_wait polls before a wait gives up (seconds)
-
-template <int B, int K, int KIND>
-__host__ __device__ constexpr int win_slots() {
-  if constexpr (KIND == 0) {
-    return WinNet<B, K>::M;
-  } else {
-    return 2 * WinPack<B, K>::NP;
-  }
-}
-
-// Row offset (from the group's base row) of buffer slot s.  KIND 0: member s;
-// packed kinds: slot 2q / 2q+1 = lane 0 / lane 1 of pack q.
-template <int B, int K, int KIND, bool LOW>
-__device__ __forceinline__ long long win_slot_row(const WinJob& P, int s, long long ra, long long rb) {
-#define ROW_A(j) (LOW ? (long long)(j) : (long long)P.off_a[(j)])
-#define ROW_B(j) (LOW ? (long long)(j) : (long long)P.off_b[(j)])
-  if constexpr (KIND == 0) {
-    return ra + ROW_A(s);
-  } else {
-    using PK = WinPack<B, K>;
-    const int q = s >> 1;
-    if ((s & 1) == 0) return ra + ROW_A(PK::lane0(q));
-    return KIND == 2 ? rb + ROW_B(PK::lane1(q)) : ra + ROW_A(PK::lane1(q));
-  }
-#undef ROW_A
-#undef ROW_B
-}
-
-template <int B, int K, int KIND, bool LOW, int EPI>
-__global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI))
-    win_tma_kernel(const __grid_constant__ WinJob P) {
-  constexpr bool EXPECT = EPI == EPI_EXPECT;
-  constexpr int NS = win_slots<B, K, KIND>();
-  extern __shared__ __align__(128) float2 sbuf[];  // [NS][STAGE_THREADS]
-  __shared__ __align__(8) unsigned long long mbar;
-  __shared__ double sh[STAGE_THREADS / 32];
-  // the item's dithered coefficients (double-buffered across items)
-  __shared__ float scoef[2][84];
-  const int tid = threadIdx.x;
-  constexpr int NCOEF = 3 * (B * (B - 1) / 2);
-  const long long items = (long long)P.n_groups * P.tiles;
-  if (tid == 0) {
-    mbar_init(&mbar, 1);
-    mbar_init_fence();
-  }
-  __syncthreads();
-  auto group_rows = [&](long long it, long long& ra, long long& rb, long long& col0) {
-    const int g = (int)(it / P.tiles);
-    col0 = (it - (long long)g * P.tiles) * STAGE_THREADS;
-    ra = P.gbase_a[g];
-    rb = P.gbase_b ? (long long)P.gbase_b[g] : ra;
-  };
-  auto issue = [&](long long it) {  // one thread: the bulk copies of item `it`
-    long long ra, rb, col0;
-    group_rows(it, ra, rb, col0);
-    const long long nc = min((long long)STAGE_THREADS, P.ncols - col0);
-    const unsigned bytes = (unsigned)(nc * (long long)sizeof(float2));
-    mbar_expect_tx(&mbar, bytes * NS);
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-      bulk_g2s(sbuf + s * STAGE_THREADS, P.in + win_slot_row<B, K, KIND, LOW>(P, s, ra, rb) * P.ld + col0, bytes,
-               &mbar);
-  };
-  long long item = blockIdx.x;
-  if (tid == 0 && item < items) issue(item);
-  unsigned parity = 0;
-  double part = 0.0;
-  for (; item < items; item += gridDim.x) {
-    bool ok = true;
-    for (unsigned n = 0; !mbar_try_wait(&mbar, parity);)
-      if (++n > WIN_WAIT_LIMIT) {
-        ok = false;
-        break;
-      }
-    if (__syncthreads_or(!ok)) {  // uniform: every thread leaves together
-      if (tid == 0) *P.err = 1;
-      break;
-    }
-    parity ^= 1;
-    long long ra, rb, col0;
-    group_rows(item, ra, rb, col0);
-    const long long col = col0 + tid;
-    const bool active = col < P.ncols;
-    // dithered rounding drawn per item: unbiased, independent across items
-    float* coef = scoef[(int)(((item - blockIdx.x) / gridDim.x) & 1)];
-    if (tid < NCOEF) {
-      const unsigned u = dither_seed((unsigned long long)item * NCOEF + tid, P.salt);
-      coef[tid] = u < P.gt[tid] ? P.gl[tid] : P.gp[tid];
-    }
-    unsigned rng = 0;
-    if constexpr (KIND == 0) {
-      constexpr int M = WinNet<B, K>::M;
-      float2 v[M];
-#pragma unroll
-      for (int j = 0; j < M; ++j) v[j] = sbuf[j * STAGE_THREADS + tid];
-      fence_proxy_async();
-      __syncthreads();
-      if (tid == 0 && item + gridDim.x < items) issue(item + gridDim.x);
-      WinNet<B, K>::template apply<0>(v, coef, nullptr, nullptr, rng);
-      if (active) {
-        if constexpr (!EXPECT) {
-          float2* da = P.out + col;
-          long long ls = P.ld;
-          asm volatile("" : "+l"(da), "+l"(ls));
-#pragma unroll
-          for (int j = 0; j < M; ++j) da[win_slot_row<B, K, 0, LOW>(P, j, ra, rb) * ls] = v[j];
-        } else {
-          const StageExpect& E = P.ex;
-          const unsigned outside = E.row_str[win_slot_row<B, K, 0, LOW>(P, 0, ra, rb)] & ~(((1u << B) - 1u) << P.lo);
-          ZCtx za, zb;
-          zctx_make<B>(E, P.norb, P.lo, E.col_str[col], outside, 0u, za, zb, E.zcol[col]);
-          float acc = 0.f, cmp = 0.f;
-#pragma unroll
-          for (int j = 0; j < M; ++j) {
-            const float z = zpat<B>(za, win_member(B, K, j), __ldg(E.zrow + win_slot_row<B, K, 0, LOW>(P, j, ra, rb)));
-            kahan_add(acc, cmp, z * (v[j].x * v[j].x + v[j].y * v[j].y));
-          }
-          part += (double)acc - (double)cmp;
-        }
-      }
-    } else {
-      using PK = WinPack<B, K>;
-      constexpr int NP = PK::NP;
-      float2 R[NP], I[NP];
-#pragma unroll
-      for (int q = 0; q < NP; ++q) {
-        const float2 a = sbuf[(2 * q) * STAGE_THREADS + tid];
-        const float2 b = sbuf[(2 * q + 1) * STAGE_THREADS + tid];
-        R[q] = make_float2(a.x, b.x);
-        I[q] = make_float2(a.y, b.y);
-      }
-      fence_proxy_async();
-      __syncthreads();
-      if (tid == 0 && item + gridDim.x < items) issue(item + gridDim.x);
-      PK::template apply<0>(R, I, coef, nullptr, nullptr, rng);
-      if (active) {
-        if constexpr (!EXPECT) {
-          float2* dst = P.out + col;
-          long long ls = P.ld;
-          asm volatile("" : "+l"(dst), "+l"(ls));
-#pragma unroll
-          for (int q = 0; q < NP; ++q) {
-            dst[win_slot_row<B, K, KIND, LOW>(P, 2 * q, ra, rb) * ls] = make_float2(R[q].x, I[q].x);
-            dst[win_slot_row<B, K, KIND, LOW>(P, 2 * q + 1, ra, rb) * ls] = make_float2(R[q].y, I[q].y);
-          }
-        } else {
-          const StageExpect& E = P.ex;
-          const unsigned wmask = ((1u << B) - 1u) << P.lo;
-          const unsigned out_a = E.row_str[win_slot_row<B, K, KIND, LOW>(P, 0, ra, rb)] & ~wmask;
-          const unsigned out_b = E.row_str[win_slot_row<B, K, KIND, LOW>(P, 1, ra, rb)] & ~wmask;
-          ZCtx za, zb;
-          zctx_make<B>(E, P.norb, P.lo, E.col_str[col], out_a, KIND == 2 ? out_b : out_a, za, zb, E.zcol[col]);
-          float acc = 0.f, cmp = 0.f;
-#pragma unroll
-          for (int q = 0; q < NP; ++q) {
-            const float z0 = zpat<B>(za, PK::pat0(q), __ldg(E.zrow + win_slot_row<B, K, KIND, LOW>(P, 2 * q, ra, rb)));
-            const float z1 =
-                zpat<B>(KIND == 2 ? zb : za, PK::pat1(q), __ldg(E.zrow + win_slot_row<B, K, KIND, LOW>(P, 2 * q + 1, ra, rb)));
-            const float2 m2 = __ffma2_rn(R[q], R[q], __fmul2_rn(I[q], I[q]));
-            kahan_add(acc, cmp, z0 * m2.x);
-            kahan_add(acc, cmp, z1 * m2.y);
-          }
-          part += (double)acc - (double)cmp;
-        }
-      }
-    }
-  }
-  if constexpr (EXPECT) {
-    const double s2 = block_sum_128(part, sh);
-    if (tid == 0) P.ex.partials[blockIdx.x] = s2;
   }
 }
 

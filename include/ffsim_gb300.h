@@ -37,7 +37,7 @@ typedef enum {
   FFGB_ERR_DTYPE = 2,       /* unsupported dtype (TypeError) */
   FFGB_ERR_OOM = 3,         /* scratch too small / allocation failed (MemoryError) */
   FFGB_ERR_CUDA = 4,        /* CUDA runtime error (RuntimeError) */
-  FFGB_ERR_TIMEOUT = 5,     /* bounded wait expired (TimeoutError) */
+  FFGB_ERR_TIMEOUT = 5,     /* reserved for bounded device waits (TimeoutError); no kernel waits now */
   FFGB_ERR_UNSUPPORTED = 6, /* shape not supported (NotImplementedError) */
   FFGB_ERR_NUMERIC = 7      /* host factorization failed (ArithmeticError) */
 } ffgb_status;
