@@ -169,7 +169,7 @@ def time_e2e(steps, ucj, ham):
 # DRAM bytes (read + write) of one 8-orbital window stage at norb=16 (8,8)
 # complex64, summed over its class launches, from the ncu launch list in
 # profiles/window_stage_norb16_c64.md.
-WINDOW_STAGE_TRAFFIC = 2.386e9
+WINDOW_STAGE_TRAFFIC = 2.389e9
 
 
 def stage_rooflines(stream, reps: int = 8):
