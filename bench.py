@@ -256,7 +256,7 @@ def run_ops(args) -> None:
         buf, nbytes = scratch(v, 2, norb, *nelec)
 
     def timed(fn):
-        for _ in range(2):
+        for _ in range(min(args.warmup, 2)):
             fn()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -291,8 +291,10 @@ def run_ops(args) -> None:
             _lib.dptr(dcm), hrots.ctypes.data_as(_lib._dp), float(ham.constant), 0, None, _lib.dptr(eout),
             buf.data_ptr(), nbytes, sptr)),
     }
-    if cs_index is None:
+    if cs_index is None or args.dtype != "c64":
         del ops["cross_half_stage"]
+    if args.dtype != "c64":  # the stage kernels are complex64
+        del ops["window_stage"]
     for name, (nb, fn) in ops.items():
         try:
             ms = timed(fn)

@@ -28,6 +28,7 @@ struct DiagRowsArgs {
   double rsame[FFGB_MAXN][FFGB_MAXN];
   double cross[FFGB_MAXN][FFGB_MAXN];
   int norb, zrep, mode, accumulate;
+  double* partials;  // COEF only: when set, sum f |in|^2 per CTA here instead of writing out
 };
 
 template <typename T>
@@ -50,7 +51,9 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
   using C = typename CT<T>::type;
   __shared__ T sm[FFGB_MAXN];
   __shared__ double sF;
+  __shared__ double sred[DIAG_THREADS / 32];
   const int tid = threadIdx.x;
+  double part = 0.0;
   const long long r0 = (long long)blockIdx.x * DIAG_ROWS_PER_CTA;
   const long long r1 = min(r0 + DIAG_ROWS_PER_CTA, A.rows);
   for (long long r = r0; r < r1; ++r) {
@@ -97,6 +100,11 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
       }
       fx *= wsc;
       C v = xin[c];
+      if (A.partials) {
+        const T z = (T)F + ((const T*)A.col_table)[c] + fx;
+        part += (double)(z * (v.x * v.x + v.y * v.y));
+        continue;
+      }
       if (A.mode == DIAG_PHASE) {
         const C ph = cmul(cmul(rowph, ((const C*)A.col_table)[c]), phase_small<T>(fx));
         v = cmul(v, ph);
@@ -114,6 +122,31 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
       xout[c] = v;
     }
     __syncthreads();  // the next row overwrites sm, sF
+  }
+  if (A.partials) {  // fixed-order block reduction
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) sred[tid >> 5] = part;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < DIAG_THREADS / 32; ++w) t += sred[w];
+      A.partials[blockIdx.x] = t;
+    }
+  }
+}
+
+// x[r][c] *= row_ph[r] * col_ph[c] (either table optional).
+template <typename C>
+__global__ void __launch_bounds__(256) outer_scale_kernel(C* __restrict__ x, long long rows, long long cols,
+                                                           const C* __restrict__ row_ph,
+                                                           const C* __restrict__ col_ph) {
+  const long long n = rows * cols;
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n; i += (long long)gridDim.x * 256) {
+    const long long r = i / cols, c = i - r * cols;
+    C v = x[i];
+    if (row_ph) v = cmul(v, row_ph[r]);
+    if (col_ph) v = cmul(v, col_ph[c]);
+    x[i] = v;
   }
 }
 

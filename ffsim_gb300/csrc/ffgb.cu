@@ -425,7 +425,9 @@ static bool staged(const SectorPlan* a, const SectorPlan* b) {
   return true;
 }
 
-// Per-string table of a plan's final orbital phases (nullptr when they are all 1).
+// Per-string table of a plan's final orbital phases (nullptr when they are all 1),
+// complex of T.
+template <typename T = float>
 static int phase_table(const SectorPlan* p, int norb, int nocc, Scratch& scr, cudaStream_t st,
                        const void** out) {
   *out = nullptr;
@@ -441,9 +443,9 @@ static int phase_table(const SectorPlan* p, int norb, int nocc, Scratch& scr, cu
   const unsigned* strs = nullptr;
   FFGB_TRY(device_strings(norb, nocc, &strs));
   const long long dim = binom_h(norb, nocc);
-  void* t = scr.take((size_t)dim * sizeof(float2));
+  void* t = scr.take((size_t)dim * sizeof(typename CT<T>::type));
   if (!t) return fail(FFGB_ERR_OOM, "scratch too small for a string-phase table");
-  FFGB_TRY(launch_string_phases<float>(strs, dim, norb, d.data(), t, st));
+  FFGB_TRY(launch_string_phases<T>(strs, dim, norb, d.data(), t, st));
   *out = t;
   return FFGB_OK;
 }
@@ -552,6 +554,101 @@ static int diag_rows(const void* in, void* out, int norb, int row_nocc, int col_
   return FFGB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// complex128 states whose sector rows exceed shared memory (norb 17-18 near
+// half filling): the generic network, one adjacent Givens rotation per launch
+// on the whole state, then one pass with both sectors' final phases; diagonal
+// operators stream rows.  FP64 CUDA-core work bounds these passes on GB300.
+// ---------------------------------------------------------------------------
+template <typename T>
+static bool big_rows(int norb, int na, int nb) {
+  if (sizeof(T) != 8) return false;
+  const double lim = 215.0 * 1024.0;  // a row of the sector kernel, with its tables
+  return (double)binom_h(norb, na) * 16.0 > lim || (nb >= 0 && (double)binom_h(norb, nb) * 16.0 > lim);
+}
+
+template <typename T>
+static int big_rotate(void* vec, int norb, int na, int nb, const SectorPlan* pa, const SectorPlan* pb, bool phases,
+                      Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const long long da = binom_h(norb, na), db = nb < 0 ? 1 : binom_h(norb, nb);
+  auto sweep = [&](const SectorPlan* p, int spin, int nocc, long long dim_other) -> int {
+    if (!p || p->kind == PLAN_IDENTITY) return FFGB_OK;
+    if (p->kind != PLAN_TRIANGLE) return fail(FFGB_ERR_ARG, "generic network expected");
+    if (nocc < 1 || nocc > norb - 1) return FFGB_OK;
+    const long long total = binom_h(norb - 2, nocc - 1) * dim_other;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 4 * 152 * 8);
+    for (size_t k = 0; k < p->tri.size(); ++k) {
+      const Givens& g = p->tri[k];
+      givens_sector_kernel<T><<<blocks, 256, 0, st>>>((C*)vec, norb, nocc, dim_other, spin, p->tri_l[k], (T)g.c,
+                                                      (T)g.s.real(), (T)g.s.imag());
+      count_launch();
+      FFGB_CUDA(cudaGetLastError());
+    }
+    return FFGB_OK;
+  };
+  FFGB_TRY(sweep(pa, 0, na, db));
+  if (nb >= 0) FFGB_TRY(sweep(pb, 1, nb, da));
+  if (!phases) return FFGB_OK;
+  const size_t mark = scr.off;
+  const void *fa = nullptr, *fb = nullptr;
+  FFGB_TRY(phase_table<T>(pa, norb, na, scr, st, &fa));
+  if (nb >= 0) FFGB_TRY(phase_table<T>(pb, norb, nb, scr, st, &fb));
+  if (fa || fb) {
+    const long long n = da * db;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4 * 152 * 8);
+    outer_scale_kernel<C><<<blocks, 256, 0, st>>>((C*)vec, da, db, (const C*)fa, (const C*)fb);
+    count_launch();
+    FFGB_CUDA(cudaGetLastError());
+  }
+  scr.off = mark;
+  return FFGB_OK;
+}
+
+// sum f |x|^2 of a COEF diagonal into dslot (device double).
+template <typename T>
+static int big_expect(const void* x, int norb, int na, int nb, const DiagSpec& spec, double* dslot, Scratch& scr,
+                      cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const size_t mark = scr.off;
+  const long long rows = binom_h(norb, na), cols = binom_h(norb, nb);
+  const unsigned *rs = nullptr, *cs = nullptr;
+  FFGB_TRY(device_strings(norb, na, &rs));
+  FFGB_TRY(device_strings(norb, nb, &cs));
+  const long long grid = (rows + DIAG_ROWS_PER_CTA - 1) / DIAG_ROWS_PER_CTA;
+  void* tab = scr.take((size_t)cols * sizeof(T));
+  double* same = (double*)scr.take(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
+  double* partials = (double*)scr.take(sizeof(double) * (size_t)grid);
+  if (!tab || !same || !partials) return fail(FFGB_ERR_OOM, "scratch too small for the expectation tables");
+  FFGB_CUDA(cudaMemcpyAsync(same, spec.col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN, cudaMemcpyHostToDevice, st));
+  col_table_kernel<T><<<(unsigned)((cols + 255) / 256), 256, 0, st>>>(cs, (int)cols, norb, spec.zrep, DIAG_COEF,
+                                                                      same, tab);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  auto A = std::make_unique<DiagRowsArgs<T>>();
+  std::memset(A.get(), 0, sizeof(DiagRowsArgs<T>));
+  A->in = (const C*)x;
+  A->rows = rows;
+  A->cols = cols;
+  A->rstr = rs;
+  A->cstr = cs;
+  A->col_table = tab;
+  std::memcpy(A->rsame, spec.row_same, sizeof(A->rsame));
+  std::memcpy(A->cross, spec.cross, sizeof(A->cross));
+  A->norb = norb;
+  A->zrep = spec.zrep;
+  A->mode = DIAG_COEF;
+  A->partials = partials;
+  diag_rows_kernel<T><<<(unsigned)grid, DIAG_THREADS, 0, st>>>(*A);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  reduce_partials_kernel<<<1, 256, 0, st>>>(partials, (int)grid, dslot, 0);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  scr.off = mark;
+  return FFGB_OK;
+}
+
 // Diagonal operator on a state held with beta rows (db rows of da columns):
 // in place (PHASE / COEF) or reduced into partial sums (EXPECT).  `spec` is
 // written with alpha rows.
@@ -616,6 +713,12 @@ template <typename T>
 static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const double* ma,
                                  const double* mb, Scratch& scr, cudaStream_t st) {
   using C = typename CT<T>::type;
+  if (big_rows<T>(norb, na, nb)) {
+    SectorPlan pa, pb;
+    if (ma) FFGB_TRY(make_plan<T>(norb, load_mat(ma, norb), pa));
+    if (mb && nb >= 0) FFGB_TRY(make_plan<T>(norb, load_mat(mb, norb), pb));
+    return big_rotate<T>(vec, norb, na, nb, ma ? &pa : nullptr, mb && nb >= 0 ? &pb : nullptr, true, scr, st);
+  }
   if (nb < 0) {  // spinless
     if (!ma) return FFGB_OK;
     SectorPlan p;
@@ -659,6 +762,31 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
                                const double* rot_a, const double* rot_b, Scratch& scr,
                                cudaStream_t st) {
   using C = typename CT<T>::type;
+  if (big_rows<T>(norb, na, nb)) {
+    const bool rb = rot_b && nb >= 0;
+    SectorPlan pad, pbd, pau, pbu;
+    if (rot_a) {
+      auto U = load_mat(rot_a, norb);
+      FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pad));
+      FFGB_TRY(make_plan<T>(norb, U, pau));
+    }
+    if (rb) {
+      auto U = load_mat(rot_b, norb);
+      FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pbd));
+      FFGB_TRY(make_plan<T>(norb, U, pbu));
+    }
+    FFGB_TRY(big_rotate<T>(vec, norb, na, nb, rot_a ? &pad : nullptr, rb ? &pbd : nullptr, true, scr, st));
+    if (nb < 0) {  // spinless: one row whose columns are the strings
+      DiagSpec d = spec;
+      std::memcpy(d.col_same, spec.row_same, sizeof(d.col_same));
+      std::memset(d.row_same, 0, sizeof(d.row_same));
+      std::memset(d.cross, 0, sizeof(d.cross));
+      FFGB_TRY(diag_rows<T>(vec, vec, norb, 0, na, d, false, scr, st));
+    } else {
+      FFGB_TRY(diag_rows<T>(vec, vec, norb, na, nb, spec, false, scr, st));
+    }
+    return big_rotate<T>(vec, norb, na, nb, rot_a ? &pau : nullptr, rb ? &pbu : nullptr, true, scr, st);
+  }
   if (nb < 0) {  // spinless: one row
     SectorPlan pu, pd;
     if (rot_a) {
@@ -751,6 +879,22 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
                                Scratch& scr, cudaStream_t st) {
   using C = typename CT<T>::type;
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  if (big_rows<T>(norb, na, nb)) {
+    if (!rot) return diag_rows<T>(vec, out, norb, na, nb, spec, accumulate != 0, scr, st);
+    SectorPlan pd, pu;
+    FFGB_TRY(make_plan<T>(norb, dagger(*rot, norb), pd));
+    FFGB_TRY(make_plan<T>(norb, *rot, pu));
+    const size_t S = (size_t)da * db * sizeof(C);
+    void* t1 = scr.take(S);
+    if (!t1) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+    FFGB_CUDA(cudaMemcpyAsync(t1, vec, S, cudaMemcpyDeviceToDevice, st));
+    FFGB_TRY(big_rotate<T>(t1, norb, na, nb, &pd, &pd, true, scr, st));
+    FFGB_TRY(diag_rows<T>(t1, t1, norb, na, nb, spec, false, scr, st));
+    FFGB_TRY(big_rotate<T>(t1, norb, na, nb, &pu, &pu, true, scr, st));
+    if (accumulate) return launch_axpy<T>(t1, out, da * db, 1.0, st);
+    FFGB_CUDA(cudaMemcpyAsync(out, t1, S, cudaMemcpyDeviceToDevice, st));
+    return FFGB_OK;
+  }
   if (!rot) {
     if (sizeof(T) == 4) return diag_rows<T>(vec, out, norb, na, nb, spec, accumulate != 0, scr, st);
     PassArgs<T> A;
@@ -864,6 +1008,14 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
   SectorPlan pv;
   FFGB_TRY(make_plan<T>(norb, V, pv));
   const size_t mark = scr.off;
+  if (big_rows<T>(norb, na, nb)) {  // |phi|^2 does not see the final orbital phases
+    FFGB_CUDA(cudaMemcpyAsync(tmp, vec, (size_t)(da * db) * sizeof(typename CT<T>::type), cudaMemcpyDeviceToDevice,
+                              st));
+    FFGB_TRY(big_rotate<T>(tmp, norb, na, nb, &pv, &pv, false, scr, st));
+    FFGB_TRY(big_expect<T>(tmp, norb, na, nb, spec, dslot, scr, st));
+    scr.off = mark;
+    return FFGB_OK;
+  }
   if (tmp2 && staged<T>(&pv, &pv)) {
     // alpha stages into tmp, transpose to beta rows, beta stages with the
     // expectation fused into the last one (no phases: |psi|^2 does not see them)
@@ -922,6 +1074,10 @@ static int expectation_term(const void* vec, int norb, int na, int nb, const Dia
 template <typename T>
 static int ucj_layer(void* x, void* tmp, int norb, int na, int nb, const SectorPlan& p, const DiagSpec* spec,
                      unsigned salt, Scratch& scr, cudaStream_t st) {
+  if (big_rows<T>(norb, na, nb)) {
+    FFGB_TRY(big_rotate<T>(x, norb, na, nb, &p, &p, true, scr, st));
+    return spec ? diag_rows<T>(x, x, norb, na, nb, *spec, false, scr, st) : FFGB_OK;
+  }
   if (staged<T>(&p, &p)) {
     const size_t mark = scr.off;
     const void* fbp = nullptr;
