@@ -503,6 +503,22 @@ static int staged_rotate(const void* in, void* x, void* tmp, int norb, int na, i
   return launch_transpose<float>(tmp, x, db, da, fb, nullptr, st);
 }
 
+// complex64 plans that exist only as a stage sequence (norb 17-18) cannot
+// run on the shared-memory sector kernel; a single sector vector (spinless)
+// then runs the stage kernels as a one-column matrix.
+static bool ops_only(const SectorPlan& p) { return p.kind == PLAN_CSD && p.b1.empty(); }
+
+static int stage_spinless(void* vec, int norb, int nocc, const SectorPlan& p, unsigned salt, Scratch& scr,
+                          cudaStream_t st) {
+  const size_t mark = scr.off;
+  FFGB_TRY(stage_sector(vec, vec, norb, nocc, 1, 1, p, salt, st));
+  const void* f = nullptr;
+  FFGB_TRY(phase_table(&p, norb, nocc, scr, st, &f));
+  if (f) FFGB_TRY(launch_row_scale<float>(vec, binom_h(norb, nocc), 1, f, st));
+  scr.off = mark;
+  return FFGB_OK;
+}
+
 // Number-representation diagonal operators absorb orbital phases d_i of the
 // column (beta) sector: exp(i arg(d_i) n_i) = d_i^(n_i).
 static void fold_col_phases(DiagSpec& spec, const SectorPlan& p, int norb) {
@@ -723,6 +739,7 @@ static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const doub
     if (!ma) return FFGB_OK;
     SectorPlan p;
     FFGB_TRY(make_plan<T>(norb, load_mat(ma, norb), p));
+    if (sizeof(T) == 4 && ops_only(p)) return stage_spinless(vec, norb, na, p, 1, scr, st);
     PassArgs<T> A;
     A.plan = &p;
     A.norb = norb;
@@ -738,6 +755,12 @@ static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const doub
   if (mb) FFGB_TRY(make_plan<T>(norb, load_mat(mb, norb), pb));
   if (!ma && !mb) return FFGB_OK;
   if (!ma) {  // beta only: rows are alpha strings, in place
+    if (sizeof(T) == 4 && ops_only(pb)) {
+      const size_t S = (size_t)binom_h(norb, na) * binom_h(norb, nb) * sizeof(C);
+      void* tmp = scr.take(S);
+      if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+      return staged_rotate(vec, vec, tmp, norb, na, nb, nullptr, &pb, true, false, 1, scr, st);
+    }
     PassArgs<T> A;
     A.plan = &pb;
     A.norb = norb;
@@ -798,6 +821,12 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
     std::memcpy(d.col_same, spec.row_same, sizeof(d.col_same));
     std::memset(d.row_same, 0, sizeof(d.row_same));
     std::memset(d.cross, 0, sizeof(d.cross));
+    if (sizeof(T) == 4 && rot_a && ops_only(pd)) {
+      FFGB_TRY(stage_spinless(vec, norb, na, pd, 2, scr, st));
+      FFGB_TRY(diag_rows<T>(vec, vec, norb, 0, na, d, false, scr, st));
+      return stage_spinless(vec, norb, na, pu, 3, scr, st);
+    }
+    if (sizeof(T) == 4 && !rot_a) return diag_rows<T>(vec, vec, norb, 0, na, d, false, scr, st);
     PassArgs<T> A;
     A.plan = rot_a ? &pd : nullptr;
     A.norb = norb;

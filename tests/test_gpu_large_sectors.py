@@ -1,7 +1,8 @@
-"""complex128 states whose sector rows exceed shared memory (norb 17):
-rotations as one adjacent Givens rotation per pass and row-streamed
-diagonals, against the FP64 oracle.  One sector is at half filling (24,310
-strings, 389 KB per row); the other holds one electron so the oracle stays fast."""
+"""Sectors too large for the shared-memory sector kernel (norb 17, 24,310
+strings at half filling), against the FP64 oracle.  complex128: one adjacent
+Givens rotation per pass and row-streamed diagonals.  complex64: the stage
+kernels, also for one spin sector alone and for spinless vectors.  The other
+sector holds one electron so the oracle stays fast."""
 
 from __future__ import annotations
 
@@ -90,3 +91,38 @@ def test_spinless_rotation(cuda):
     u = o.random_unitary(NORB, seed=rng)
     got = _n(f.apply_orbital_rotation(_t(vec), u, NORB, 8))
     np.testing.assert_allclose(got, o.apply_orbital_rotation(vec, u, NORB, 8), atol=TOL)
+
+
+TOL64 = 2e-5
+
+
+@pytest.mark.parametrize("nelec", CASES)
+def test_complex64_one_sector_and_spinless(cuda, nelec):
+    import ffsim_gb300 as f
+
+    vec, u, j = _inputs(nelec, 53 + nelec[0])
+
+    def c64(x):
+        return torch.from_numpy(np.ascontiguousarray(x)).to("cuda").to(torch.complex64)
+
+    for mat in (u, (None, u), (u, None)):
+        got = _n(f.apply_orbital_rotation(c64(vec), mat, NORB, nelec))
+        np.testing.assert_allclose(got, o.apply_orbital_rotation(vec, mat, NORB, nelec), atol=TOL64)
+    got = _n(f.apply_diag_coulomb_evolution(c64(vec), j, 0.7, NORB, nelec, orbital_rotation=u))
+    exp = o.apply_diag_coulomb_evolution(vec, j, 0.7, NORB, nelec, orbital_rotation=u)
+    np.testing.assert_allclose(got, exp, atol=TOL64)
+
+
+def test_complex64_spinless(cuda):
+    import ffsim_gb300 as f
+
+    rng = np.random.default_rng(61)
+    vec = o.random_state_vector(math.comb(NORB, 8), seed=rng)
+    u = o.random_unitary(NORB, seed=rng)
+    t = torch.from_numpy(vec).to("cuda").to(torch.complex64)
+    got = _n(f.apply_orbital_rotation(t, u, NORB, 8))
+    np.testing.assert_allclose(got, o.apply_orbital_rotation(vec, u, NORB, 8), atol=TOL64)
+    coeffs = rng.standard_normal(NORB)
+    got = _n(f.apply_num_op_sum_evolution(t, coeffs, 0.4, NORB, 8, orbital_rotation=u))
+    exp = o.apply_num_op_sum_evolution(vec, coeffs, 0.4, NORB, 8, orbital_rotation=u)
+    np.testing.assert_allclose(got, exp, atol=TOL64)
