@@ -86,54 +86,55 @@ void put_coefs(const double* v, int n, int mode, float* gp, float* gl, unsigned*
 // ---------------------------------------------------------------------------
 // fused cross-half tables
 // ---------------------------------------------------------------------------
+// One launch of the cross-half stage: groups with m active sites, their
+// tables at `base` (1 + 2^m ints per group).
+struct CsClass {
+  int m = 0, groups = 0;
+  long long base = 0;
+};
+
 struct CsPass {
   int* tab = nullptr;  // device
-  int n_classes = 0;
-  int cls_m[5] = {}, cls_groups[5] = {}, cls_base[5] = {};
+  std::vector<CsClass> cls;  // in launch order
 };
 
 std::mutex g_cs_mu;
-std::map<std::tuple<int, int, int, int, int, int, int>, CsPass> g_cs;
+std::map<std::tuple<int, int, int, int, int>, CsPass> g_cs;
 
-// Groups of the sector (norb, nocc) under the cross-half sites i in [s0, s1),
-// site i rotating orbitals (lo + i, lo + hh + i).
-int cs_pass_tables(int norb, int nocc, int lo, int hh, int s0, int s1, const CsPass** out) {
+// Groups of the sector (norb, nocc) under all cross-half sites i < hh, site i
+// rotating orbitals (lo + i, lo + hh + i), for one pass over the state.  Groups
+// with at most CS_MAX_M active sites are one class each; a larger group (rare:
+// 2% of the rows at norb 16) runs as two sub-passes, first over its first four
+// active sites (one sub-group per setting of the others), then over the rest,
+// and these classes come last in this order.
+int cs_pass_tables(int norb, int nocc, int lo, int hh, const CsPass** out) {
   int dev = 0;
   FFGB_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(g_cs_mu);
-  auto key = std::make_tuple(dev, norb, nocc, lo, hh, s0, s1);
+  auto key = std::make_tuple(dev, norb, nocc, lo, hh);
   auto it = g_cs.find(key);
   if (it != g_cs.end()) {
     *out = &it->second;
     return FFGB_OK;
   }
   const long long dim = C(norb, nocc);
-  std::vector<std::vector<int>> per_m(5);
-  std::vector<int> counts(5, 0);
-  for (long long a = 0; a < dim; ++a) {
-    const unsigned s = unrank(a, norb, nocc);
-    int act[4], m = 0;
-    bool canonical = true;
-    for (int i = s0; i < s1; ++i) {
-      const bool o_lo = (s >> (lo + i)) & 1u, o_hi = (s >> (lo + hh + i)) & 1u;
-      if (o_lo != o_hi) {
-        act[m++] = i;
-        if (o_hi) canonical = false;  // the group is emitted from its all-low member
-      }
-    }
-    if (m == 0 || !canonical) continue;
-    std::vector<int>& T = per_m[m];
+  // per class: direct m = 1..CS_MAX_M, then sub-pass A (4 sites), then sub-pass B (m - 4 = 1..4 sites)
+  std::vector<std::vector<int>> direct(CS_MAX_M + 1), sub_a(1), sub_b(5);
+  std::vector<int> n_direct(CS_MAX_M + 1, 0), n_sub_b(5, 0);
+  int n_sub_a = 0;
+  // one (sub-)group: base string, its sites (indices into act) and the table entries
+  auto emit = [&](std::vector<int>& T, unsigned base, const int* sites, int m) -> int {
     int header = 0;
-    for (int t = 0; t < m; ++t) header |= act[t] << (4 * t);
+    for (int t = 0; t < m; ++t) header |= sites[t] << (4 * t);
     T.push_back(header);
     for (int j = 0; j < (1 << m); ++j) {
-      unsigned mem = s;
+      unsigned mem = base;
       for (int t = 0; t < m; ++t)
-        if ((j >> t) & 1) mem ^= (1u << (lo + act[t])) | (1u << (lo + hh + act[t]));
+        if ((j >> t) & 1) mem ^= (1u << (lo + sites[t])) | (1u << (lo + hh + sites[t]));
       int sign = 0;
       for (int t = 0; t < m; ++t) {
         if ((j >> t) & 1) continue;
-        const int i = lo + act[t], jj = lo + hh + act[t];
+        const int i = lo + sites[t], jj = lo + hh + sites[t];
         const unsigned between = ((1u << jj) - 1u) & ~((1u << (i + 1)) - 1u);
         if (popcount(mem & between) & 1) sign |= 1 << t;
       }
@@ -141,22 +142,61 @@ int cs_pass_tables(int norb, int nocc, int lo, int hh, int s0, int s1, const CsP
       if (r >= (1 << 24)) return fail(FFGB_ERR_UNSUPPORTED, "sector too large for the cross-half tables");
       T.push_back((int)r | (sign << 24));
     }
-    ++counts[m];
+    return FFGB_OK;
+  };
+  for (long long a = 0; a < dim; ++a) {
+    const unsigned s = unrank(a, norb, nocc);
+    int act[CS_MAX_SITES], m = 0;
+    bool canonical = true;
+    for (int i = 0; i < hh; ++i) {
+      const bool o_lo = (s >> (lo + i)) & 1u, o_hi = (s >> (lo + hh + i)) & 1u;
+      if (o_lo != o_hi) {
+        act[m++] = i;
+        if (o_hi) canonical = false;  // the group is emitted from its all-low member
+      }
+    }
+    if (m == 0 || !canonical) continue;
+    if (m <= CS_MAX_M) {
+      FFGB_TRY(emit(direct[m], s, act, m));
+      ++n_direct[m];
+      continue;
+    }
+    if (m > 8) return fail(FFGB_ERR_UNSUPPORTED, "too many active cross-half sites");
+    const int mb = m - 4;
+    auto flip = [&](unsigned x, int t) { return x ^ ((1u << (lo + act[t])) | (1u << (lo + hh + act[t]))); };
+    for (int b = 0; b < (1 << mb); ++b) {  // sub-pass A: sites act[0..4), act[4..m) set by b
+      unsigned base = s;
+      for (int t = 0; t < mb; ++t)
+        if ((b >> t) & 1) base = flip(base, 4 + t);
+      FFGB_TRY(emit(sub_a[0], base, act, 4));
+      ++n_sub_a;
+    }
+    for (int b = 0; b < 16; ++b) {  // sub-pass B: sites act[4..m), act[0..4) set by b
+      unsigned base = s;
+      for (int t = 0; t < 4; ++t)
+        if ((b >> t) & 1) base = flip(base, t);
+      FFGB_TRY(emit(sub_b[mb], base, act + 4, mb));
+      ++n_sub_b[mb];
+    }
   }
   CsPass P;
   std::vector<int> host;
-  for (int m = 4; m >= 1; --m) {
-    if (counts[m] == 0) continue;
-    P.cls_m[P.n_classes] = m;
-    P.cls_groups[P.n_classes] = counts[m];
-    P.cls_base[P.n_classes] = (int)host.size();
-    host.insert(host.end(), per_m[m].begin(), per_m[m].end());
-    ++P.n_classes;
-  }
+  auto add = [&](int m, int groups, const std::vector<int>& T) {
+    if (groups == 0) return;
+    CsClass c;
+    c.m = m;
+    c.groups = groups;
+    c.base = (long long)host.size();
+    host.insert(host.end(), T.begin(), T.end());
+    P.cls.push_back(c);
+  };
+  for (int m = CS_MAX_M; m >= 1; --m) add(m, n_direct[m], direct[m]);
+  add(4, n_sub_a, sub_a[0]);
+  for (int m = 4; m >= 1; --m) add(m, n_sub_b[m], sub_b[m]);
   const size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(int);
   FFGB_CUDA(cudaMalloc(&P.tab, bytes));
   if (!host.empty()) FFGB_CUDA(cudaMemcpy(P.tab, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice));
-  g_cs[key] = P;
+  g_cs[key] = std::move(P);
   *out = &g_cs[key];
   return FFGB_OK;
 }
@@ -177,38 +217,39 @@ int launch_cs(const CsStageParams& P, int grid, int mode, cudaStream_t st) {
 int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int lo, int hh,
              const std::vector<Pair2>& cs, int mode, unsigned salt, cudaStream_t st) {
   if (hh > CS_MAX_SITES) return fail(FFGB_ERR_UNSUPPORTED, "too many cross-half sites");
-  for (int s0 = 0; s0 < hh; s0 += 4) {
-    const int s1 = std::min(hh, s0 + 4);
-    const CsPass* T = nullptr;
-    FFGB_TRY(cs_pass_tables(norb, nocc, lo, hh, s0, s1, &T));
-    CsStageParams P;
-    std::memset(&P, 0, sizeof(P));
-    P.x = x;
-    P.ld = ld;
-    P.ncols = ncols;
-    P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
-    P.salt = salt * 0x9E3779B9u + 0x51ED270Bu * (unsigned)(s0 + 1);
-    P.gpc = CS_MAX_GPC;
-    double v[3 * CS_MAX_SITES] = {};
-    for (int i = 0; i < hh; ++i) {
-      v[3 * i] = cs[i].g00.real();
-      v[3 * i + 1] = cs[i].g01.real();
-      v[3 * i + 2] = cs[i].g01.imag();
-    }
-    put_coefs(v, 3 * CS_MAX_SITES, mode, P.gp, P.gl, P.gt);
-    for (int c = 0; c < T->n_classes; ++c) {
-      P.tab = T->tab + T->cls_base[c];
-      P.n_groups = T->cls_groups[c];
-      const long long grid = (long long)((P.n_groups + P.gpc - 1) / P.gpc) * P.tiles;
-      if (grid <= 0) continue;
-      if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
-      switch (T->cls_m[c]) {
-        case 1: FFGB_TRY(launch_cs<1>(P, (int)grid, mode, st)); break;
-        case 2: FFGB_TRY(launch_cs<2>(P, (int)grid, mode, st)); break;
-        case 3: FFGB_TRY(launch_cs<3>(P, (int)grid, mode, st)); break;
-        case 4: FFGB_TRY(launch_cs<4>(P, (int)grid, mode, st)); break;
-        default: return fail(FFGB_ERR_ARG, "bad cross-half class");
-      }
+  const CsPass* T = nullptr;
+  FFGB_TRY(cs_pass_tables(norb, nocc, lo, hh, &T));
+  CsStageParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.x = x;
+  P.ld = ld;
+  P.ncols = ncols;
+  P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
+  double v[3 * CS_MAX_SITES] = {};
+  for (int i = 0; i < hh; ++i) {
+    v[3 * i] = cs[i].g00.real();
+    v[3 * i + 1] = cs[i].g01.real();
+    v[3 * i + 2] = cs[i].g01.imag();
+  }
+  put_coefs(v, 3 * CS_MAX_SITES, mode, P.gp, P.gl, P.gt);
+  for (size_t c = 0; c < T->cls.size(); ++c) {
+    const CsClass& k = T->cls[c];
+    P.tab = T->tab + k.base;
+    P.n_groups = k.groups;
+    P.gpc = k.m >= 5 ? CS_MAX_GPC / 2 : CS_MAX_GPC;
+    // every launch draws its own dithered coefficients
+    P.salt = salt * 0x9E3779B9u + 0x51ED270Bu * (unsigned)(c + 1);
+    const long long grid = (long long)((P.n_groups + P.gpc - 1) / P.gpc) * P.tiles;
+    if (grid <= 0) continue;
+    if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
+    switch (k.m) {
+      case 1: FFGB_TRY(launch_cs<1>(P, (int)grid, mode, st)); break;
+      case 2: FFGB_TRY(launch_cs<2>(P, (int)grid, mode, st)); break;
+      case 3: FFGB_TRY(launch_cs<3>(P, (int)grid, mode, st)); break;
+      case 4: FFGB_TRY(launch_cs<4>(P, (int)grid, mode, st)); break;
+      case 5: FFGB_TRY(launch_cs<5>(P, (int)grid, mode, st)); break;
+      case 6: FFGB_TRY(launch_cs<6>(P, (int)grid, mode, st)); break;
+      default: return fail(FFGB_ERR_ARG, "bad cross-half class");
     }
   }
   return FFGB_OK;

@@ -246,10 +246,10 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
   }
 }
 
-// Cross-half rotations (lo + i, lo + hh + i) of up to four sites in one pass.  A
+// Cross-half rotations (lo + i, lo + hh + i) of all sites in one pass.  A
 // group is the set of strings that agree everywhere except in which orbital of
 // each "active" pair (exactly one of the two occupied) is occupied: 2^M members
-// for M active sites.  Table entry per group: a header with the active sites
+// for M active sites, held in registers for M <= CS_MAX_M.  Table entry per group: a header with the active sites
 // (4 bits each, ascending), then per member its row | (sign bits << 24); bit
 // 24 + t is the parity of the occupied orbitals strictly between the two
 // orbitals of active site t, read on the member whose lower orbital is
@@ -257,6 +257,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
 // 2x2 blocks of the plan have determinant 1.
 constexpr int CS_MAX_GPC = 8;     // groups per CTA of the cross-half stage (at most)
 constexpr int CS_MAX_SITES = 12;  // cross-half sites of one stage (at most)
+constexpr int CS_MAX_M = 6;       // active sites of a group kept in registers
 
 struct CsStageParams {
   float2* x;
@@ -264,7 +265,7 @@ struct CsStageParams {
   const int* tab;  // this class's groups, (1 + 2^M) ints each
   int n_groups;
   int tiles;
-  int gpc;  // groups per CTA (one column tile each), an even number <= CS_MAX_GPC
+  int gpc;  // groups per CTA (one column tile each): an even number <= CS_MAX_GPC, at most half that for M >= 5
   float gp[3 * CS_MAX_SITES], gl[3 * CS_MAX_SITES];  // per site (c, Re t, Im t), see win_coef
   unsigned gt[3 * CS_MAX_SITES];
   unsigned salt;
@@ -272,7 +273,7 @@ struct CsStageParams {
 
 // One group's cross-half rotations on registers; e[j] = row | sign bits.
 template <int M, int MODE>
-__device__ __forceinline__ void cs_rotate(float2 (&v)[1 << M], const int (&e)[1 << M], int sites,
+__device__ __forceinline__ void cs_rotate(float2 (&v)[1 << M], const int* e, int sites,
                                           const float* __restrict__ gp, const float* __restrict__ gl,
                                           const unsigned* __restrict__ gt, unsigned rng) {
   constexpr int NM = 1 << M;
@@ -290,17 +291,21 @@ __device__ __forceinline__ void cs_rotate(float2 (&v)[1 << M], const int (&e)[1 
   }
 }
 
-// Groups with M active sites; each thread takes two groups at a time so that
-// both groups' loads are in flight together.
+// Groups with M active sites.  For M <= 4 each thread takes two groups at a
+// time so that both groups' loads are in flight together; larger groups (up to
+// 64 members) go one at a time.  The member tables stay in shared memory.
 template <int M, int MODE>
-__global__ void __launch_bounds__(STAGE_THREADS, M >= 4 ? 4 : 6) cs_stage_kernel(const __grid_constant__ CsStageParams P) {
+__global__ void __launch_bounds__(STAGE_THREADS, M >= 6 ? 2 : (M >= 5 ? 3 : (M >= 4 ? 4 : 6)))
+    cs_stage_kernel(const __grid_constant__ CsStageParams P) {
   constexpr int NM = 1 << M;
   constexpr int STRIDE = 1 + NM;
+  constexpr bool TWO = M <= 4;
+  constexpr int GPC = TWO ? CS_MAX_GPC : CS_MAX_GPC / 2;
   const int chunk = blockIdx.x / P.tiles, tile = blockIdx.x - chunk * P.tiles;
   const long long col = (long long)tile * STAGE_THREADS + threadIdx.x;
   const int g0 = chunk * P.gpc, g1 = min(g0 + P.gpc, P.n_groups);
   // this CTA's group tables, staged once in shared memory
-  __shared__ int sent[CS_MAX_GPC * 17];
+  __shared__ int sent[GPC * STRIDE];
   const int n_ent = (g1 - g0) * STRIDE;
   const int* src = P.tab + (long long)g0 * STRIDE;
   for (int i = threadIdx.x; i < n_ent; i += STAGE_THREADS) sent[i] = src[i];
@@ -309,30 +314,31 @@ __global__ void __launch_bounds__(STAGE_THREADS, M >= 4 ? 4 : 6) cs_stage_kernel
   const unsigned rng = dither_seed((unsigned long long)col, P.salt);
   float2* xc = P.x + col;
   const long long ld = P.ld;
-  for (int g = g0; g < g1; g += 2) {
-    const bool two = g + 1 < g1;
+  for (int g = g0; g < g1; g += TWO ? 2 : 1) {
+    const bool two = TWO && g + 1 < g1;
     const int* ea = sent + (g - g0) * STRIDE;
     const int* eb = two ? ea + STRIDE : ea;
-    int e0[NM], e1[NM];
-    float2 v0[NM], v1[NM];
+    float2 v0[NM], v1[TWO ? NM : 1];
 #pragma unroll
-    for (int j = 0; j < NM; ++j) {
-      e0[j] = ea[1 + j];
-      e1[j] = eb[1 + j];
+    for (int j = 0; j < NM; ++j) v0[j] = xc[(long long)(ea[1 + j] & 0xffffff) * ld];
+    if constexpr (TWO) {
+      if (two) {
+#pragma unroll
+        for (int j = 0; j < NM; ++j) v1[j] = xc[(long long)(eb[1 + j] & 0xffffff) * ld];
+      }
     }
+    cs_rotate<M, MODE>(v0, ea + 1, ea[0], P.gp, P.gl, P.gt, rng);
+    // re-read the rows from shared memory for the stores instead of keeping
+    // 2^M addresses live across the rotations
+    asm volatile("" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < NM; ++j) v0[j] = xc[(long long)(e0[j] & 0xffffff) * ld];
-    if (two) {
+    for (int j = 0; j < NM; ++j) xc[(long long)(ea[1 + j] & 0xffffff) * ld] = v0[j];
+    if constexpr (TWO) {
+      if (two) {
+        cs_rotate<M, MODE>(v1, eb + 1, eb[0], P.gp, P.gl, P.gt, rng);
 #pragma unroll
-      for (int j = 0; j < NM; ++j) v1[j] = xc[(long long)(e1[j] & 0xffffff) * ld];
-    }
-    cs_rotate<M, MODE>(v0, e0, ea[0], P.gp, P.gl, P.gt, rng);
-#pragma unroll
-    for (int j = 0; j < NM; ++j) xc[(long long)(e0[j] & 0xffffff) * ld] = v0[j];
-    if (two) {
-      cs_rotate<M, MODE>(v1, e1, eb[0], P.gp, P.gl, P.gt, rng);
-#pragma unroll
-      for (int j = 0; j < NM; ++j) xc[(long long)(e1[j] & 0xffffff) * ld] = v1[j];
+        for (int j = 0; j < NM; ++j) xc[(long long)(eb[1 + j] & 0xffffff) * ld] = v1[j];
+      }
     }
   }
 }
