@@ -3,10 +3,9 @@
 // and whose columns are strings of the other,
 //   f(r, c) = F_R(r) + F_C(c) + sum_{i,l} X[i][l] g_i(r) g_l(c),
 // g = n (number representation) or 1 - 2n (Z representation).  Per row the
-// FP64 row term and the weights m_l(r) = sum_i X[i][l] g_i(r) are formed once;
-// per element the column term comes from a table (exp(i F_C) for phases, F_C
-// for coefficients) and the cross term is a short FP32 sum of m_l over the
-// column string's occupied orbitals.
+// FP64 row term and the weights m_l(r) = sum_i X[i][l] g_i(r) are formed once
+// and tabulated over the halves of the column string (below); per element the
+// column term comes from a table (exp(i F_C) for phases, F_C for coefficients).
 #pragma once
 
 #include "kernels.cuh"
@@ -31,28 +30,27 @@ struct DiagRowsArgs {
   double* partials;  // COEF only: when set, sum f |in|^2 per CTA here instead of writing out
 };
 
-template <typename T>
-__device__ __forceinline__ typename CT<T>::type phase_small(T f) {
-  using C = typename CT<T>::type;
-  T s, c;
-  if constexpr (sizeof(T) == 4) {
-    sincosf(f, &s, &c);
-  } else {
-    sincos(f, &s, &c);
-  }
-  C r;
-  r.x = c;
-  r.y = s;
-  return r;
-}
+// Per row, the row term and the cross term are tabulated over the two halves
+// of the column string's bits: with h = norb / 2,
+//   F(r) + sum_{l in occ(c)} w m_l(r) = L_r[c & (2^h - 1)] + H_r[c >> h]
+// (w = -2 in the Z representation, else 1), each entry summed in FP64.  PHASE
+// tables hold exp(i L), exp(i H); COEF tables the real sums.  An element then
+// costs two shared-memory reads and two or three complex products instead of
+// a loop over its occupied orbitals and a sine/cosine.
+constexpr int DIAG_HALF = 1 << ((FFGB_MAXN + 1) / 2);
 
 template <typename T>
 __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_constant__ DiagRowsArgs<T> A) {
   using C = typename CT<T>::type;
-  __shared__ T sm[FFGB_MAXN];
+  __shared__ double sm[FFGB_MAXN];
   __shared__ double sF;
+  __shared__ C tl[DIAG_HALF], th[DIAG_HALF];  // PHASE tables
+  __shared__ T ul[DIAG_HALF], uh[DIAG_HALF];  // COEF tables
   __shared__ double sred[DIAG_THREADS / 32];
   const int tid = threadIdx.x;
+  const int h = A.norb / 2, nl = 1 << h, nh = 1 << (A.norb - h);
+  const unsigned lmask = (unsigned)nl - 1u;
+  const bool phase = A.mode == DIAG_PHASE;
   double part = 0.0;
   const long long r0 = (long long)blockIdx.x * DIAG_ROWS_PER_CTA;
   const long long r1 = min(r0 + DIAG_ROWS_PER_CTA, A.rows);
@@ -64,7 +62,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
         const double gi = A.zrep ? (((rs >> i) & 1u) ? -1.0 : 1.0) : (double)((rs >> i) & 1u);
         m += A.cross[i][tid] * gi;
       }
-      sm[tid] = (T)m;
+      sm[tid] = A.zrep ? -2.0 * m : m;
     }
     if (tid == 32) {
       double f = 0.0;
@@ -85,33 +83,35 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
       sF = f;
     }
     __syncthreads();
-    const double F = sF;
-    const T wsc = A.zrep ? (T)-2 : (T)1;
-    C rowph;
-    if (A.mode == DIAG_PHASE) rowph = phase_of(F, (C*)nullptr);
+    for (int e = tid; e < nl + nh; e += DIAG_THREADS) {
+      const bool low = e < nl;
+      const unsigned bits = low ? (unsigned)e : (unsigned)(e - nl);
+      const int off = low ? 0 : h;
+      double a = low ? sF : 0.0;
+      for (unsigned b = bits; b; b &= b - 1) a += sm[off + __ffs(b) - 1];
+      if (phase) {
+        const C z = phase_of(a, (C*)nullptr);
+        if (low) tl[e] = z; else th[e - nl] = z;
+      } else {
+        if (low) ul[e] = (T)a; else uh[e - nl] = (T)a;
+      }
+    }
+    __syncthreads();
     const C* xin = A.in + r * A.cols;
     C* xout = A.out + r * A.cols;
     for (long long c = tid; c < A.cols; c += DIAG_THREADS) {
-      unsigned s = A.cstr[c];
-      T fx = (T)0;
-      while (s) {
-        fx += sm[__ffs(s) - 1];
-        s &= s - 1;
-      }
-      fx *= wsc;
+      const unsigned s = A.cstr[c];
       C v = xin[c];
-      if (A.partials) {
-        const T z = (T)F + ((const T*)A.col_table)[c] + fx;
-        part += (double)(z * (v.x * v.x + v.y * v.y));
-        continue;
-      }
-      if (A.mode == DIAG_PHASE) {
-        const C ph = cmul(cmul(rowph, ((const C*)A.col_table)[c]), phase_small<T>(fx));
-        v = cmul(v, ph);
-      } else {
-        const T z = (T)F + ((const T*)A.col_table)[c] + fx;
+      if (!phase) {
+        const T z = ul[s & lmask] + uh[s >> h] + ((const T*)A.col_table)[c];
+        if (A.partials) {
+          part += (double)(z * (v.x * v.x + v.y * v.y));
+          continue;
+        }
         v.x *= z;
         v.y *= z;
+      } else {
+        v = cmul(cmul(v, ((const C*)A.col_table)[c]), cmul(tl[s & lmask], th[s >> h]));
       }
       if (A.accumulate) {
         C o = xout[c];
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
       }
       xout[c] = v;
     }
-    __syncthreads();  // the next row overwrites sm, sF
+    __syncthreads();  // the next row overwrites the tables
   }
   if (A.partials) {  // fixed-order block reduction
     for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);

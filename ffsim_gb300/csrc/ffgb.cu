@@ -846,18 +846,7 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
     return FFGB_OK;
   }
   const long long da = binom_h(norb, na);
-  if (!rot_a && !rot_b) {
-    if (sizeof(T) == 4) return diag_rows<T>(vec, vec, norb, na, nb, spec, false, scr, st);
-    PassArgs<T> A;
-    A.norb = norb;
-    A.rot_nocc = nb;
-    A.row_nocc = na;
-    A.n_rows = da;
-    A.in = vec;
-    A.out = vec;
-    A.diag = &spec;
-    return run_pass<T>(A, scr, st);
-  }
+  if (!rot_a && !rot_b) return diag_rows<T>(vec, vec, norb, na, nb, spec, false, scr, st);
   SectorPlan pad, pbd, pau, pbu;
   if (rot_a) {
     auto U = load_mat(rot_a, norb);
@@ -924,19 +913,7 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
     FFGB_CUDA(cudaMemcpyAsync(out, t1, S, cudaMemcpyDeviceToDevice, st));
     return FFGB_OK;
   }
-  if (!rot) {
-    if (sizeof(T) == 4) return diag_rows<T>(vec, out, norb, na, nb, spec, accumulate != 0, scr, st);
-    PassArgs<T> A;
-    A.norb = norb;
-    A.rot_nocc = nb;
-    A.row_nocc = na;
-    A.n_rows = da;
-    A.in = vec;
-    A.out = out;
-    A.out_op = accumulate ? OUT_ACCUM : OUT_STORE;
-    A.diag = &spec;
-    return run_pass<T>(A, scr, st);
-  }
+  if (!rot) return diag_rows<T>(vec, out, norb, na, nb, spec, accumulate != 0, scr, st);
   SectorPlan pd, pu;
   FFGB_TRY(make_plan<T>(norb, dagger(*rot, norb), pd));
   FFGB_TRY(make_plan<T>(norb, *rot, pu));
