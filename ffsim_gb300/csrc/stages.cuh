@@ -55,20 +55,6 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// colex-ordered member j of a window with k of b orbitals occupied
-__host__ __device__ constexpr unsigned win_member(int b, int k, int j) {
-  unsigned m = 0;
-  int count = 0;
-  for (unsigned w = 0; w < (1u << b); ++w) {
-    int pc = 0;
-    for (unsigned x = w; x; x &= x - 1) ++pc;
-    if (pc != k) continue;
-    if (count == j) m = w;
-    ++count;
-  }
-  return m;
-}
-
 // Registers: the members of one thread are 2 * C(B, K) floats (twice that for
 // KIND 2); addressing, coefficients and scheduling slack take about
 // 30 + 0.55 * data more (measured with -Xptxas -v), the fused expectation ~16.
@@ -85,23 +71,26 @@ struct ZCtx {
   float base, scale;
 };
 
+// xw[t][l] = X[lo + t][l] (rows of FFGB_MAXN), xs[l] = sum_i X[i][l], and
+// ya[l], yb[l] = sum over the group's electrons outside the window of X[i][l]:
+// per-CTA tables in shared memory.
 template <int B>
-__device__ __forceinline__ void zctx_make(const StageExpect& E, int norb, int lo, unsigned cstr, unsigned outside_a,
-                                          unsigned outside_b, ZCtx& za, ZCtx& zb, float zc) {
+__device__ __forceinline__ void zctx_make(const float* xw, const float* xs, const float* ya, const float* yb, int norb,
+                                          int zrep, unsigned cstr, ZCtx& za, ZCtx& zb, float zc) {
   float sa = 0.f, sb = 0.f, wall = 0.f;
 #pragma unroll
   for (int t = 0; t < B; ++t) za.w[t] = 0.f;
   for (int l = 0; l < norb; ++l) {
-    const float gcol = E.zrep ? (((cstr >> l) & 1u) ? -1.f : 1.f) : (float)((cstr >> l) & 1u);
+    const float gcol = zrep ? (((cstr >> l) & 1u) ? -1.f : 1.f) : (float)((cstr >> l) & 1u);
 #pragma unroll
-    for (int t = 0; t < B; ++t) za.w[t] += E.X[lo + t][l] * gcol;
-    for (unsigned o = outside_a; o; o &= o - 1) sa += E.X[__ffs(o) - 1][l] * gcol;
-    for (unsigned o = outside_b; o; o &= o - 1) sb += E.X[__ffs(o) - 1][l] * gcol;
-    wall += E.Xsum[l] * gcol;
+    for (int t = 0; t < B; ++t) za.w[t] += xw[t * FFGB_MAXN + l] * gcol;
+    sa += ya[l] * gcol;
+    sb += yb[l] * gcol;
+    wall += xs[l] * gcol;
   }
 #pragma unroll
   for (int t = 0; t < B; ++t) zb.w[t] = za.w[t];
-  if (E.zrep) {
+  if (zrep) {
     za.base = zc + wall - 2.f * sa;
     zb.base = zc + wall - 2.f * sb;
     za.scale = zb.scale = -2.f;
@@ -160,6 +149,30 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
 #define ROW_A(j) (LOW ? (long long)(j) : (long long)P.off_a[(j)])
 #define ROW_B(j) (LOW ? (long long)(j) : (long long)P.off_b[(j)])
   double part = 0.0;
+  // fused expectation: the operator's weights for this CTA's group(s), once per CTA
+  constexpr int XS = EXPECT ? FFGB_MAXN : 1;
+  __shared__ float sxw[EXPECT ? B * FFGB_MAXN : 1], sxs[XS], sya[XS], syb[XS];
+  if constexpr (EXPECT) {
+    const unsigned wmask = ((1u << B) - 1u) << P.lo;
+    const unsigned out_a = P.ex.row_str[ra + ROW_A(0)] & ~wmask;
+    const unsigned out_b = KIND == 2 ? (P.ex.row_str[rb + ROW_B(0)] & ~wmask) : out_a;
+    const int n = P.norb;
+    for (int e = threadIdx.x; e < (B + 3) * n; e += STAGE_THREADS) {
+      const int row = e / n, l = e - row * n;
+      if (row < B) {
+        sxw[row * FFGB_MAXN + l] = P.ex.X[P.lo + row][l];
+      } else if (row == B) {
+        sxs[l] = P.ex.Xsum[l];
+      } else {
+        const unsigned o = row == B + 1 ? out_a : out_b;
+        float y = 0.f;
+        for (int i = 0; i < n; ++i)
+          if ((o >> i) & 1u) y += P.ex.X[i][l];
+        (row == B + 1 ? sya : syb)[l] = y;
+      }
+    }
+    __syncthreads();
+  }
   if (active) {
     const float2* sa = P.in + ra * ld + col;
     const float2* sb = P.in + rb * ld + col;
@@ -179,14 +192,20 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
         for (int j = 0; j < M; ++j) da[ROW_A(j) * ls] = v[j];
       } else {
         const StageExpect& E = P.ex;
-        const unsigned outside = E.row_str[ra + ROW_A(0)] & ~(((1u << B) - 1u) << P.lo);
         ZCtx za, zb;
-        zctx_make<B>(E, P.norb, P.lo, E.col_str[col], outside, 0u, za, zb, E.zcol[col]);
+        zctx_make<B>(sxw, sxs, sya, sya, P.norb, E.zrep, E.col_str[col], za, zb, E.zcol[col]);
         float acc = 0.f, cmp = 0.f;
+        // member patterns in colex order = ascending integers with K bits set,
+        // stepped with the next-same-popcount recurrence (folds to constants)
+        unsigned pat = (1u << K) - 1u;
 #pragma unroll
         for (int j = 0; j < M; ++j) {
-          const float z = zpat<B>(za, win_member(B, K, j), __ldg(E.zrow + ra + ROW_A(j)));
+          const float z = zpat<B>(za, pat, __ldg(E.zrow + ra + ROW_A(j)));
           kahan_add(acc, cmp, z * (v[j].x * v[j].x + v[j].y * v[j].y));
+          if (j + 1 < M) {
+            const unsigned low = pat & (0u - pat), r = pat + low;
+            pat = (((r ^ pat) >> 2) / low) | r;
+          }
         }
         part = (double)acc - (double)cmp;
       }
@@ -218,11 +237,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
         }
       } else {
         const StageExpect& E = P.ex;
-        const unsigned wmask = ((1u << B) - 1u) << P.lo;
-        const unsigned out_a = E.row_str[ra + ROW_A(0)] & ~wmask;
-        const unsigned out_b = PAIR ? (E.row_str[rb + ROW_B(0)] & ~wmask) : out_a;
         ZCtx za, zb;
-        zctx_make<B>(E, P.norb, P.lo, E.col_str[col], out_a, out_b, za, zb, E.zcol[col]);
+        zctx_make<B>(sxw, sxs, sya, syb, P.norb, E.zrep, E.col_str[col], za, zb, E.zcol[col]);
         float acc = 0.f, cmp = 0.f;
 #pragma unroll
         for (int q = 0; q < NP; ++q) {
