@@ -311,7 +311,7 @@ __device__ __forceinline__ void cs_rotate(float2 (&v)[1 << M], const int* e, int
 // time so that both groups' loads are in flight together; larger groups (up to
 // 64 members) go one at a time.  The member tables stay in shared memory.
 template <int M, int MODE>
-__global__ void __launch_bounds__(STAGE_THREADS, M >= 6 ? 2 : (M >= 5 ? 3 : (M >= 4 ? 4 : 6)))
+__global__ void __launch_bounds__(STAGE_THREADS, M >= 5 ? 3 : (M >= 4 ? 4 : 6))
     cs_stage_kernel(const __grid_constant__ CsStageParams P) {
   constexpr int NM = 1 << M;
   constexpr int STRIDE = 1 + NM;
