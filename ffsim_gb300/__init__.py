@@ -2,8 +2,9 @@
 
 Drop-in counterparts of ``ffsim.apply_orbital_rotation``,
 ``ffsim.apply_diag_coulomb_evolution``, ``ffsim.apply_num_op_sum_evolution``,
-``ffsim.apply_unitary`` for ``UCJOpSpinBalanced`` and
-``ffsim.linear_operator`` for ``DoubleFactorizedHamiltonian``, running
+``ffsim.apply_unitary`` for ``UCJOpSpinBalanced``,
+``ffsim.linear_operator`` for ``DoubleFactorizedHamiltonian`` and
+``ffsim.simulate_trotter_double_factorized``, running
 hand-written sm_103a kernels through the C ABI in ``include/ffsim_gb300.h``.
 """
 
@@ -21,6 +22,7 @@ from ffsim_gb300.gates import (
 from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian
 from ffsim_gb300.protocols import LinearOperator, apply_unitary, linear_operator
 from ffsim_gb300.states import hartree_fock_state, vdot
+from ffsim_gb300.trotter import simulate_trotter_double_factorized
 from ffsim_gb300.variational import UCJOpSpinBalanced
 
 __all__ = [
@@ -36,6 +38,7 @@ __all__ = [
     "apply_orbital_rotation",
     "apply_phase_shift_in_place",
     "apply_unitary",
+    "simulate_trotter_double_factorized",
     "contract",
     "dim",
     "dims",

@@ -600,6 +600,57 @@ def df_energy(vec, one_body_tensor, diag_coulomb_mats, orbital_rotations, consta
 
 
 # ---------------------------------------------------------------------------
+# Trotter-Suzuki evolution of a double-factorized Hamiltonian
+# (trotter/double_factorized.py:25-127, trotter/_util.py:18-60)
+# ---------------------------------------------------------------------------
+
+
+def trotter_step_terms(n_terms, time, order=0):
+    """(term index, time) sequence of one Trotter step (trotter/_util.py:18-60):
+    order 0 is the plain product; order k >= 1 is Suzuki's symmetric fractal
+    (J. Math. Phys. 32, 400 (1991)): order 1 sweeps the terms at half time up
+    to the last one at full time and back, and order k nests five order-(k-1)
+    steps with times p, p, 1 - 4p, p, p, p = 1 / (4 - 4^(1/(2k-1)))."""
+    if order == 0:
+        return [(i, time) for i in range(n_terms)]
+    if order == 1:
+        seq = [(i, time / 2) for i in range(n_terms - 1)] + [(n_terms - 1, time)]
+        return seq + [(i, time / 2) for i in reversed(range(n_terms - 1))]
+    p = time / (4 - 4 ** (1 / (2 * order - 1)))
+    inner = trotter_step_terms(n_terms, p, order - 1)
+    return inner * 2 + trotter_step_terms(n_terms, time - 4 * p, order - 1) + inner * 2
+
+
+def simulate_trotter_double_factorized(vec, one_body_tensor, diag_coulomb_mats, orbital_rotations, constant,
+                                       time, norb, nelec, n_steps=1, order=0, z_representation=False):
+    """double_factorized.py:25-127: term 0 (one-body) multiplies the running
+    orbital basis by exp(-i t h); term k >= 1 rotates the state into
+    U_k's basis and applies exp(-i t J_k n n); the last basis and the global
+    phase exp(-i T constant) close the evolution."""
+    if order < 0 or n_steps < 0:
+        raise ValueError("order and n_steps must be non-negative")
+    vec = np.array(vec, dtype=complex, copy=True)
+    if n_steps == 0:
+        return vec
+    step = time / n_steps
+    basis = np.eye(norb, dtype=complex)
+    for _ in range(n_steps):
+        for k, t in trotter_step_terms(1 + len(diag_coulomb_mats), step, order):
+            if k == 0:
+                basis = scipy.linalg.expm(-1j * t * one_body_tensor) @ basis
+            else:
+                u = orbital_rotations[k - 1]
+                vec = apply_orbital_rotation(vec, u.T.conj() @ basis, norb, nelec, copy=False)
+                vec = apply_diag_coulomb_evolution(vec, diag_coulomb_mats[k - 1], t, norb, nelec,
+                                                   z_representation=z_representation, copy=False)
+                basis = u
+    vec = apply_orbital_rotation(vec, basis, norb, nelec, copy=False)
+    if constant:
+        vec = vec * np.exp(-1j * time * constant)
+    return vec
+
+
+# ---------------------------------------------------------------------------
 # UCJ (variational/ucj_spin_balanced.py:657-696) and parameter maps
 # ---------------------------------------------------------------------------
 

@@ -164,7 +164,14 @@ def install_stubs():
     ffsim.linalg = sys.modules["ffsim.linalg"]
     ffsim.protocols = proto
     ucj = _load("ffsim.variational.ucj_spin_balanced", "variational/ucj_spin_balanced.py")
+    # Trotter: the reference's step iterator and double-factorized evolution
+    # (the Hamiltonian class is only a type annotation there)
+    _module("ffsim.hamiltonians", {"DoubleFactorizedHamiltonian": types.SimpleNamespace})
+    _module("ffsim.trotter", is_pkg=True)
+    _load("ffsim.trotter._util", "trotter/_util.py")
+    tdf = _load("ffsim.trotter.double_factorized", "trotter/double_factorized.py")
     return types.SimpleNamespace(
+        simulate_trotter_double_factorized=tdf.simulate_trotter_double_factorized,
         apply_orbital_rotation=gor.apply_orbital_rotation,
         apply_diag_coulomb_evolution=gdc.apply_diag_coulomb_evolution,
         apply_num_op_sum_evolution=gnos.apply_num_op_sum_evolution,
@@ -347,6 +354,27 @@ def main():
     hf = orc.hartree_fock_state(8, (5, 5))
     out["fix_mat"] = mat
     out["fix_out"] = ref.apply_orbital_rotation(hf, mat, 8, (5, 5))
+
+    # double-factorized Trotter evolution (trotter/double_factorized.py:25-127)
+    rt = np.random.default_rng(20261204)
+    trotter_cases = [(4, (2, 2), 0.3, 2, 0, False), (4, (2, 1), 0.2, 1, 2, True), (5, (3, 2), 0.25, 3, 1, False),
+                     (3, (1, 1), 0.1, 2, 1, True)]
+    for idx, (norb, nelec, t, n_steps, order, z_rep) in enumerate(trotter_cases):
+        d = orc.dim(norb, nelec)
+        vec = orc.random_state_vector(d, seed=rt)
+        g = rt.standard_normal((norb, norb)) + 1j * rt.standard_normal((norb, norb))
+        one_body = (g + g.conj().T) / 2
+        n_terms = norb
+        dcm = np.stack([orc.random_symmetric_normal(norb, seed=rt) for _ in range(n_terms)])
+        rots = np.stack([orc.random_unitary(norb, seed=rt) for _ in range(n_terms)])
+        const = float(rt.standard_normal())
+        ham = types.SimpleNamespace(one_body_tensor=one_body, diag_coulomb_mats=dcm, orbital_rotations=rots,
+                                    constant=const, z_representation=z_rep)
+        out[f"trot{idx}_in"], out[f"trot{idx}_h1"], out[f"trot{idx}_dcm"] = vec, one_body, dcm
+        out[f"trot{idx}_rots"], out[f"trot{idx}_const"] = rots, np.asarray(const)
+        out[f"trot{idx}_out"] = ref.simulate_trotter_double_factorized(
+            vec, ham, t, norb=norb, nelec=nelec, n_steps=n_steps, order=order)
+    out["trot_cases"] = np.asarray([[n, a, b, t, s, o, int(z)] for n, (a, b), t, s, o, z in trotter_cases])
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")

@@ -153,3 +153,40 @@ def test_diag_coulomb_eigenphase_kat(norb, nelec):
                                       (0, 1): mat_ab[i, j], (1, 0): mat_ab[j, i]}[(s, t)]
             res = o.apply_diag_coulomb_evolution(state, (mat_aa, mat_ab, mat_bb), time, norb, nelec)
             np.testing.assert_allclose(res, np.exp(-1j * eig * time) * state, atol=1e-12)
+
+
+def _trotter_case(golden, idx, row):
+    n, a, b, t, steps, order, z = row
+    g = lambda s: golden[f"trot{idx}_{s}"]  # noqa: E731
+    return (int(n), (int(a), int(b)), float(t), int(steps), int(order), bool(z), g)
+
+
+def test_trotter_double_factorized(golden):
+    """Trotter-Suzuki evolution (orders 0-2) against the reference's own
+    trotter/double_factorized.py run over its kernels."""
+    for idx, row in enumerate(golden["trot_cases"]):
+        n, ne, t, steps, order, z, g = _trotter_case(golden, idx, row)
+        got = o.simulate_trotter_double_factorized(g("in"), g("h1"), g("dcm"), g("rots"), float(g("const")), t,
+                                                   n, ne, n_steps=steps, order=order, z_representation=z)
+        np.testing.assert_allclose(got, g("out"), atol=TOL)
+
+
+def test_trotter_converges_to_exact_evolution():
+    """Higher order and more steps approach exp(-i t H) psi (the reference's own
+    accuracy test, trotter/double_factorized_test.py:23-85, on the oracle)."""
+    scipy_sparse_linalg = pytest.importorskip("scipy.sparse.linalg")
+    rng = np.random.default_rng(11)
+    norb, nelec, t = 4, (2, 2), 0.4
+    d = o.dim(norb, nelec)
+    g = rng.standard_normal((norb, norb)) + 1j * rng.standard_normal((norb, norb))
+    h1 = (g + g.conj().T) / 4
+    dcm = np.stack([o.random_symmetric_normal(norb, scale=0.5, seed=rng) for _ in range(3)])
+    rots = np.stack([o.random_unitary(norb, seed=rng) for _ in range(3)])
+    vec = o.random_state_vector(d, seed=rng)
+    mv = o.df_hamiltonian_matvec(h1, dcm, rots, 0.3, norb, nelec)
+    op = scipy_sparse_linalg.LinearOperator((d, d), matvec=mv, rmatvec=mv, dtype=complex)
+    exact = scipy_sparse_linalg.expm_multiply(-1j * t * op, vec, traceA=-1j * t)
+    errs = [np.linalg.norm(o.simulate_trotter_double_factorized(vec, h1, dcm, rots, 0.3, t, norb, nelec,
+                                                                 n_steps=s, order=k) - exact)
+            for s, k in [(2, 0), (8, 0), (4, 1), (4, 2)]]
+    assert errs[1] < errs[0] and errs[2] < errs[1] and errs[3] < errs[2] and errs[3] < 1e-4, errs
