@@ -21,6 +21,7 @@ from ffsim_gb300.gates import (
 )
 from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian
 from ffsim_gb300.protocols import LinearOperator, apply_unitary, linear_operator
+from ffsim_gb300.rdm import rdms
 from ffsim_gb300.states import hartree_fock_state, vdot
 from ffsim_gb300.trotter import simulate_trotter_double_factorized
 from ffsim_gb300.variational import UCJOpSpinBalanced
@@ -38,6 +39,7 @@ __all__ = [
     "apply_orbital_rotation",
     "apply_phase_shift_in_place",
     "apply_unitary",
+    "rdms",
     "simulate_trotter_double_factorized",
     "contract",
     "dim",

@@ -1,5 +1,5 @@
 """Contractions and linear operators: the GPU counterparts of
-python/ffsim/contract/{diag_coulomb,num_op_sum}.py."""
+python/ffsim/contract/{diag_coulomb,num_op_sum,one_body}.py."""
 
 from __future__ import annotations
 
@@ -10,6 +10,7 @@ from ffsim_gb300 import _lib
 from ffsim_gb300._state import dim as _dim
 from ffsim_gb300._state import prepare, scratch, stream_ptr
 from ffsim_gb300.gates import _dagger, _split_pair, apply_orbital_rotation
+from ffsim_gb300.linalg import eigh
 from ffsim_gb300.protocols import LinearOperator
 
 
@@ -93,3 +94,35 @@ def num_op_sum_linop(coeffs, norb: int, nelec: tuple[int, int], *, orbital_rotat
         return _rotated_matvec(vec, norb, nelec, coeffs, None, False, orbital_rotation)
 
     return LinearOperator((d, d), matvec)
+
+
+def _hermitian_parts(mat):
+    """M = A + i B with A = (M + M^H) / 2, B = (M - M^H) / (2i), both Hermitian."""
+    m = np.asarray(mat, dtype=complex)
+    return (m + m.conj().T) / 2, (m - m.conj().T) / 2j
+
+
+def contract_one_body(vec, mat, norb: int, nelec: tuple[int, int]):
+    r""":math:`\sum_{pq} M_{pq} a^\dagger_{p\sigma} a_{q\sigma}` applied to ``vec``
+    (python/ffsim/contract/one_body.py:24-58) for any complex matrix M.
+
+    Each Hermitian part of M is diagonal in its eigenbasis, so its action is one
+    rotated number-operator matvec ``W(V) (sum_i w_i n_i) W(V)^dag``
+    (``ffgb_rotated_diag_matvec``); the anti-Hermitian part adds a second one.
+    """
+    a, b = _hermitian_parts(mat)
+    wa, va = eigh(a)
+    out = num_op_sum_linop(wa, norb, nelec, orbital_rotation=va) @ vec
+    if np.abs(b).max() > 0.0:
+        wb, vb = eigh(b)
+        out = out + 1j * (num_op_sum_linop(wb, norb, nelec, orbital_rotation=vb) @ vec)
+    return out
+
+
+def one_body_linop(mat, norb: int, nelec: tuple[int, int]) -> LinearOperator:
+    """Linear operator of a one-body tensor (python/ffsim/contract/one_body.py:61-90);
+    rmatvec applies M^H."""
+    d = _dim(norb, nelec)
+    m = np.asarray(mat, dtype=complex)
+    return LinearOperator((d, d), lambda v: contract_one_body(v, m, norb, nelec),
+                          lambda v: contract_one_body(v, m.conj().T, norb, nelec))

@@ -600,6 +600,69 @@ def df_energy(vec, one_body_tensor, diag_coulomb_mats, orbital_rotations, consta
 
 
 # ---------------------------------------------------------------------------
+# One-body operators and 1-RDMs from their definition (contract/one_body.py:24-90,
+# states/rdm.py:73-170; the reference's tests/python/states/rdm_test.py:147-176
+# evaluate <a+_p a_q> the same way)
+# ---------------------------------------------------------------------------
+
+
+def _excitation_lists(norb, nocc, p, q):
+    """Source and target addresses and signs of a+_p a_q on one sector's
+    strings (colex addresses, Jordan-Wigner order within the sector)."""
+    strings = make_strings(norb, nocc)
+    addr = {int(s): i for i, s in enumerate(strings)}
+    src, dst, sgn = [], [], []
+    for i, s in enumerate(strings):
+        s = int(s)
+        if not (s >> q) & 1:
+            continue
+        t = s & ~(1 << q)
+        if p != q and (t >> p) & 1:
+            continue
+        sign = (-1) ** (bin(s & ((1 << q) - 1)).count("1") + bin(t & ((1 << p) - 1)).count("1"))
+        src.append(i)
+        dst.append(addr[t | (1 << p)])
+        sgn.append(sign)
+    return np.array(src, dtype=np.int64), np.array(dst, dtype=np.int64), np.array(sgn, dtype=float)
+
+
+def _apply_excitation(v2, norb, nelec, p, q, spin):
+    na, nb = nelec
+    out = np.zeros_like(v2)
+    src, dst, sgn = _excitation_lists(norb, na if spin == 0 else nb, p, q)
+    if spin == 0:
+        np.add.at(out, dst, sgn[:, None] * v2[src])
+    else:
+        np.add.at(out.T, dst, sgn[:, None] * v2.T[src])
+    return out
+
+
+def one_body_action(vec, mat, norb, nelec):
+    """sum_{pq} M_pq (a+_{p alpha} a_{q alpha} + a+_{p beta} a_{q beta}) vec."""
+    na, nb = nelec
+    v2 = np.asarray(vec, dtype=complex).reshape(math.comb(norb, na), math.comb(norb, nb))
+    out = np.zeros_like(v2)
+    for p in range(norb):
+        for q in range(norb):
+            if mat[p, q] != 0:
+                for spin in (0, 1):
+                    out += mat[p, q] * _apply_excitation(v2, norb, nelec, p, q, spin)
+    return out.reshape(-1)
+
+
+def rdm1s(vec, norb, nelec):
+    """[alpha, beta] 1-RDMs, rdm[p, q] = <vec| a+_p a_q |vec>."""
+    na, nb = nelec
+    v2 = np.asarray(vec, dtype=complex).reshape(math.comb(norb, na), math.comb(norb, nb))
+    out = np.zeros((2, norb, norb), dtype=complex)
+    for spin in (0, 1):
+        for p in range(norb):
+            for q in range(norb):
+                out[spin, p, q] = np.vdot(v2, _apply_excitation(v2, norb, nelec, p, q, spin))
+    return out
+
+
+# ---------------------------------------------------------------------------
 # Trotter-Suzuki evolution of a double-factorized Hamiltonian
 # (trotter/double_factorized.py:25-127, trotter/_util.py:18-60)
 # ---------------------------------------------------------------------------
