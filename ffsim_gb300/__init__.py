@@ -24,15 +24,18 @@ from ffsim_gb300.protocols import LinearOperator, apply_unitary, linear_operator
 from ffsim_gb300.rdm import rdms
 from ffsim_gb300.states import hartree_fock_state, vdot
 from ffsim_gb300.trotter import simulate_trotter_double_factorized
-from ffsim_gb300.variational import UCJOpSpinBalanced
+from ffsim_gb300.variational import GivensAnsatzOp, UCJOpSpinBalanced, UCJOpSpinless, UCJOpSpinUnbalanced
 
 __all__ = [
     "LUCJGradient",
     "lucj_energy_autograd",
     "DoubleFactorizedHamiltonian",
+    "GivensAnsatzOp",
     "LUCJEnergy",
     "LinearOperator",
     "UCJOpSpinBalanced",
+    "UCJOpSpinUnbalanced",
+    "UCJOpSpinless",
     "apply_diag_coulomb_evolution",
     "apply_givens_rotation_in_place",
     "apply_num_op_sum_evolution",

@@ -140,3 +140,360 @@ class UCJOpSpinBalanced:
             return bool(np.allclose(self.final_orbital_rotation, other.final_orbital_rotation,
                                     rtol=rtol, atol=atol))
         return True
+
+
+def _check_params(params, n: int) -> np.ndarray:
+    params = np.asarray(params, dtype=float)
+    if len(params) != n:
+        raise ValueError(
+            "The number of parameters passed did not match the number expected based on the "
+            f"function inputs. Expected {n} but got {len(params)}.")
+    return params
+
+
+def _allclose_or_none(a, b, rtol, atol) -> bool:
+    if (a is None) != (b is None):
+        return False
+    return a is None or bool(np.allclose(a, b, rtol=rtol, atol=atol))
+
+
+@dataclass(frozen=True)
+class UCJOpSpinUnbalanced:
+    r"""Spin-unbalanced UCJ operator: per repetition an orbital rotation for each
+    spin and diagonal Coulomb matrices [aa, ab, bb] (ucj_spin_unbalanced.py:28-141).
+    ``_apply_unitary_`` composes the GPU gates as the reference does
+    (ucj_spin_unbalanced.py:705-745)."""
+
+    diag_coulomb_mats: np.ndarray  # (n_reps, 3, norb, norb): [aa, ab, bb]
+    orbital_rotations: np.ndarray  # (n_reps, 2, norb, norb): [alpha, beta]
+    final_orbital_rotation: np.ndarray | None = None  # (2, norb, norb)
+    validate: InitVar[bool] = True
+    rtol: InitVar[float] = 1e-5
+    atol: InitVar[float] = 1e-8
+
+    def __post_init__(self, validate: bool, rtol: float, atol: float):
+        if not validate:
+            return
+        if self.diag_coulomb_mats.ndim != 4 or self.diag_coulomb_mats.shape[1] != 3:
+            raise ValueError(
+                "diag_coulomb_mats should have shape (n_reps, 3, norb, norb). "
+                f"Got shape {self.diag_coulomb_mats.shape}.")
+        if self.orbital_rotations.ndim != 4 or self.orbital_rotations.shape[1] != 2:
+            raise ValueError(
+                "orbital_rotations should have shape (n_reps, 2, norb, norb). "
+                f"Got shape {self.orbital_rotations.shape}.")
+        if self.final_orbital_rotation is not None and self.final_orbital_rotation.ndim != 3:
+            raise ValueError(
+                "final_orbital_rotation should have shape (2, norb, norb). "
+                f"Got shape {self.final_orbital_rotation.shape}.")
+        if self.diag_coulomb_mats.shape[0] != self.orbital_rotations.shape[0]:
+            raise ValueError(
+                "diag_coulomb_mats and orbital_rotations should have the same first dimension. "
+                f"Got {self.diag_coulomb_mats.shape[0]} and {self.orbital_rotations.shape[0]}.")
+        if not all(linalg.is_real_symmetric(m[0], rtol=rtol, atol=atol)
+                   and linalg.is_real_symmetric(m[2], rtol=rtol, atol=atol) for m in self.diag_coulomb_mats):
+            raise ValueError("alpha-alpha and beta-beta diagonal Coulomb matrices were not all real symmetric.")
+        if not all(linalg.is_unitary(u[0], rtol=rtol, atol=atol) and linalg.is_unitary(u[1], rtol=rtol, atol=atol)
+                   for u in self.orbital_rotations):
+            raise ValueError("Orbital rotations were not all unitary.")
+        if self.final_orbital_rotation is not None and not (
+                linalg.is_unitary(self.final_orbital_rotation[0], rtol=rtol, atol=atol)
+                and linalg.is_unitary(self.final_orbital_rotation[1], rtol=rtol, atol=atol)):
+            raise ValueError("Final orbital rotation was not unitary.")
+
+    @property
+    def norb(self) -> int:
+        return self.diag_coulomb_mats.shape[-1]
+
+    @property
+    def n_reps(self) -> int:
+        return self.diag_coulomb_mats.shape[0]
+
+    @staticmethod
+    def n_params(norb: int, n_reps: int, *, with_final_orbital_rotation: bool = False) -> int:
+        """ucj_spin_unbalanced.py:146-206 without interaction pairs."""
+        n_triu = norb * (norb + 1) // 2
+        return n_reps * (2 * n_triu + norb**2 + 2 * norb**2) + with_final_orbital_rotation * 2 * norb**2
+
+    @staticmethod
+    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int,
+                        with_final_orbital_rotation: bool = False) -> "UCJOpSpinUnbalanced":
+        """ucj_spin_unbalanced.py:208-329 without interaction pairs: per rep the
+        alpha and beta rotations (norb**2 each), the aa upper triangle, the ab
+        matrix (row-major) and the bb upper triangle; then the final rotations."""
+        params = _check_params(params, UCJOpSpinUnbalanced.n_params(
+            norb, n_reps, with_final_orbital_rotation=with_final_orbital_rotation))
+        triu = tuple(zip(*itertools.combinations_with_replacement(range(norb), 2)))
+        dcm = np.zeros((n_reps, 3, norb, norb))
+        rots = np.zeros((n_reps, 2, norb, norb), dtype=complex)
+        i = 0
+        for r in range(n_reps):
+            for s in range(2):
+                rots[r, s] = linalg.unitary_from_parameters(params[i: i + norb**2], norb)
+                i += norb**2
+            for t in (0, 1, 2):
+                if t == 1:
+                    dcm[r, 1] = params[i: i + norb**2].reshape(norb, norb)
+                    i += norb**2
+                else:
+                    vals = params[i: i + len(triu[0])]
+                    dcm[r, t][triu[1], triu[0]] = vals
+                    dcm[r, t][triu] = vals
+                    i += len(triu[0])
+        final = None
+        if with_final_orbital_rotation:
+            final = np.stack([linalg.unitary_from_parameters(params[i + s * norb**2: i + (s + 1) * norb**2], norb)
+                              for s in range(2)])
+        return UCJOpSpinUnbalanced(dcm, rots, final)
+
+    def to_parameters(self) -> np.ndarray:
+        """ucj_spin_unbalanced.py:331-432 without interaction pairs."""
+        norb = self.norb
+        triu = tuple(zip(*itertools.combinations_with_replacement(range(norb), 2)))
+        out = []
+        for u, mats in zip(self.orbital_rotations, self.diag_coulomb_mats):
+            out += [linalg.unitary_to_parameters(u[0]), linalg.unitary_to_parameters(u[1])]
+            out += [mats[0][triu], mats[1].reshape(-1), mats[2][triu]]
+        if self.final_orbital_rotation is not None:
+            out += [linalg.unitary_to_parameters(u) for u in self.final_orbital_rotation]
+        return np.concatenate(out)
+
+    def _apply_unitary_(self, vec, norb: int, nelec, copy: bool):
+        from ffsim_gb300.gates import apply_diag_coulomb_evolution, apply_orbital_rotation
+
+        if isinstance(nelec, (int, np.integer)):
+            return NotImplemented
+        p = prepare(vec, norb, nelec, copy=copy)
+        state = p.tensor.reshape(-1)
+        eye = np.eye(norb, dtype=complex)
+        basis = (eye, eye)
+        for mats, rot in zip(self.diag_coulomb_mats, self.orbital_rotations):
+            state = apply_orbital_rotation(state, (rot[0].conj().T @ basis[0], rot[1].conj().T @ basis[1]), norb,
+                                           nelec, copy=False)
+            state = apply_diag_coulomb_evolution(state, (mats[0], mats[1], mats[2]), -1.0, norb, nelec, copy=False)
+            basis = (rot[0], rot[1])
+        if self.final_orbital_rotation is not None:
+            basis = (self.final_orbital_rotation[0] @ basis[0], self.final_orbital_rotation[1] @ basis[1])
+        state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
+        if state.data_ptr() != p.tensor.data_ptr():
+            p.tensor.reshape(-1).copy_(state)
+        return p.finish()
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, UCJOpSpinUnbalanced):
+            return NotImplemented
+        return (bool(np.allclose(self.diag_coulomb_mats, other.diag_coulomb_mats, rtol=rtol, atol=atol))
+                and bool(np.allclose(self.orbital_rotations, other.orbital_rotations, rtol=rtol, atol=atol))
+                and _allclose_or_none(self.final_orbital_rotation, other.final_orbital_rotation, rtol, atol))
+
+
+@dataclass(frozen=True)
+class UCJOpSpinless:
+    r"""Spinless UCJ operator: per repetition one orbital rotation and one
+    diagonal Coulomb matrix (ucj_spinless.py:28-120).  On spinful states the
+    matrix acts within each spin, (J, 0, J) (ucj_spinless.py:456-515)."""
+
+    diag_coulomb_mats: np.ndarray  # (n_reps, norb, norb)
+    orbital_rotations: np.ndarray  # (n_reps, norb, norb)
+    final_orbital_rotation: np.ndarray | None = None  # (norb, norb)
+    validate: InitVar[bool] = True
+    rtol: InitVar[float] = 1e-5
+    atol: InitVar[float] = 1e-8
+
+    def __post_init__(self, validate: bool, rtol: float, atol: float):
+        if not validate:
+            return
+        if self.diag_coulomb_mats.ndim != 3:
+            raise ValueError(
+                "diag_coulomb_mats should have shape (n_reps, norb, norb). "
+                f"Got shape {self.diag_coulomb_mats.shape}.")
+        if self.orbital_rotations.ndim != 3:
+            raise ValueError(
+                "orbital_rotations should have shape (n_reps, norb, norb). "
+                f"Got shape {self.orbital_rotations.shape}.")
+        if self.final_orbital_rotation is not None and self.final_orbital_rotation.ndim != 2:
+            raise ValueError(
+                "final_orbital_rotation should have shape (norb, norb). "
+                f"Got shape {self.final_orbital_rotation.shape}.")
+        if self.diag_coulomb_mats.shape[0] != self.orbital_rotations.shape[0]:
+            raise ValueError(
+                "diag_coulomb_mats and orbital_rotations should have the same first dimension. "
+                f"Got {self.diag_coulomb_mats.shape[0]} and {self.orbital_rotations.shape[0]}.")
+        if not all(linalg.is_real_symmetric(m, rtol=rtol, atol=atol) for m in self.diag_coulomb_mats):
+            raise ValueError("Diagonal Coulomb matrices were not all real symmetric.")
+        if not all(linalg.is_unitary(u, rtol=rtol, atol=atol) for u in self.orbital_rotations):
+            raise ValueError("Orbital rotations were not all unitary.")
+        if self.final_orbital_rotation is not None and not linalg.is_unitary(
+                self.final_orbital_rotation, rtol=rtol, atol=atol):
+            raise ValueError("Final orbital rotation was not unitary.")
+
+    @property
+    def norb(self) -> int:
+        return self.diag_coulomb_mats.shape[-1]
+
+    @property
+    def n_reps(self) -> int:
+        return self.diag_coulomb_mats.shape[0]
+
+    @staticmethod
+    def n_params(norb: int, n_reps: int, *, with_final_orbital_rotation: bool = False) -> int:
+        """ucj_spinless.py:133-172 without interaction pairs."""
+        return n_reps * (norb * (norb + 1) // 2 + norb**2) + with_final_orbital_rotation * norb**2
+
+    @staticmethod
+    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int,
+                        with_final_orbital_rotation: bool = False) -> "UCJOpSpinless":
+        """ucj_spinless.py:174-262 without interaction pairs: per rep the
+        rotation's norb**2 parameters, then the upper triangle."""
+        params = _check_params(params, UCJOpSpinless.n_params(
+            norb, n_reps, with_final_orbital_rotation=with_final_orbital_rotation))
+        triu = tuple(zip(*itertools.combinations_with_replacement(range(norb), 2)))
+        dcm = np.zeros((n_reps, norb, norb))
+        rots = np.zeros((n_reps, norb, norb), dtype=complex)
+        i = 0
+        for r in range(n_reps):
+            rots[r] = linalg.unitary_from_parameters(params[i: i + norb**2], norb)
+            i += norb**2
+            vals = params[i: i + len(triu[0])]
+            dcm[r][triu[1], triu[0]] = vals
+            dcm[r][triu] = vals
+            i += len(triu[0])
+        final = linalg.unitary_from_parameters(params[i:], norb) if with_final_orbital_rotation else None
+        return UCJOpSpinless(dcm, rots, final)
+
+    def to_parameters(self) -> np.ndarray:
+        """ucj_spinless.py:264-324 without interaction pairs."""
+        triu = tuple(zip(*itertools.combinations_with_replacement(range(self.norb), 2)))
+        out = []
+        for u, m in zip(self.orbital_rotations, self.diag_coulomb_mats):
+            out += [linalg.unitary_to_parameters(u), m[triu]]
+        if self.final_orbital_rotation is not None:
+            out.append(linalg.unitary_to_parameters(self.final_orbital_rotation))
+        return np.concatenate(out)
+
+    def _apply_unitary_(self, vec, norb: int, nelec, copy: bool):
+        from ffsim_gb300.gates import apply_diag_coulomb_evolution, apply_orbital_rotation
+
+        p = prepare(vec, norb, nelec, copy=copy)
+        state = p.tensor.reshape(-1)
+        spinless = isinstance(nelec, (int, np.integer))
+        zero = np.zeros((norb, norb))
+        basis = np.eye(norb, dtype=complex)
+        for mat, rot in zip(self.diag_coulomb_mats, self.orbital_rotations):
+            state = apply_orbital_rotation(state, rot.conj().T @ basis, norb, nelec, copy=False)
+            state = apply_diag_coulomb_evolution(state, mat if spinless else (mat, zero, mat), -1.0, norb, nelec,
+                                                 copy=False)
+            basis = rot
+        if self.final_orbital_rotation is not None:
+            basis = self.final_orbital_rotation @ basis
+        state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
+        if state.data_ptr() != p.tensor.data_ptr():
+            p.tensor.reshape(-1).copy_(state)
+        return p.finish()
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, UCJOpSpinless):
+            return NotImplemented
+        return (bool(np.allclose(self.diag_coulomb_mats, other.diag_coulomb_mats, rtol=rtol, atol=atol))
+                and bool(np.allclose(self.orbital_rotations, other.orbital_rotations, rtol=rtol, atol=atol))
+                and _allclose_or_none(self.final_orbital_rotation, other.final_orbital_rotation, rtol, atol))
+
+
+def _brickwork(pairs, thetas, phis, norb):
+    """Place a Givens sequence in a full brickwork of adjacent rotations
+    (python/ffsim/variational/givens.py:229-300): ceil(norb/2) layers on the
+    pairs (0,1),(2,3),... alternate with floor(norb/2) layers on (1,2),(3,4),...;
+    each rotation goes in the earliest layer of its kind after every earlier
+    rotation on its orbitals (an odd-layer slot k follows even layer k); unused
+    slots keep angle 0."""
+    q, r = divmod(norb, 2)
+    even = [[((i, i + 1), 0.0, 0.0) for i in range(0, norb - 1, 2)] for _ in range(q + r)]
+    odd = [[((i, i + 1), 0.0, 0.0) for i in range(1, norb - 1, 2)] for _ in range(q)]
+    last_even, last_odd = [-1] * norb, [-1] * norb
+    for (i, j), theta, phi in zip(pairs, thetas, phis):
+        if i > j:
+            i, j, theta, phi = j, i, -theta, -phi
+        if i % 2 == 0:
+            k = max(last_even[i], last_even[j], last_odd[i], last_odd[j]) + 1
+            even[k][i // 2] = ((i, j), theta, phi)
+            last_even[i] = last_even[j] = k
+        else:
+            k = max(last_odd[i] + 1, last_odd[j] + 1, last_even[i], last_even[j])
+            odd[k][i // 2] = ((i, j), theta, phi)
+            last_odd[i] = last_odd[j] = k
+    out = [g for e, o in itertools.zip_longest(even, odd, fillvalue=()) for g in (*e, *o)]
+    return [g[0] for g in out], [g[1] for g in out], [g[2] for g in out]
+
+
+@dataclass(frozen=True)
+class GivensAnsatzOp:
+    r"""Givens rotation ansatz (python/ffsim/variational/givens.py:29-227): a
+    product of Givens rotations on ``interaction_pairs`` with angles ``thetas``
+    and optional phases ``phis``, after an optional layer of orbital phases.
+    It is an orbital rotation, so ``_apply_unitary_`` is one
+    ``ffgb_apply_orbital_rotation``."""
+
+    norb: int
+    interaction_pairs: list
+    thetas: np.ndarray
+    phis: np.ndarray | None
+    phase_angles: np.ndarray | None
+
+    @staticmethod
+    def n_params(norb: int, interaction_pairs, with_phis: bool = True, with_phase_angles: bool = True) -> int:
+        return (1 + with_phis) * len(interaction_pairs) + with_phase_angles * norb
+
+    def to_parameters(self) -> np.ndarray:
+        parts = [self.thetas] + [x for x in (self.phis, self.phase_angles) if x is not None]
+        return np.concatenate(parts) if len(parts) > 1 else self.thetas
+
+    @staticmethod
+    def from_parameters(params: np.ndarray, norb: int, interaction_pairs, with_phis: bool = True,
+                        with_phase_angles: bool = True) -> "GivensAnsatzOp":
+        params = _check_params(params, GivensAnsatzOp.n_params(norb, interaction_pairs, with_phis,
+                                                               with_phase_angles))
+        n = len(interaction_pairs)
+        thetas = params[:n]
+        phis = params[n: 2 * n] if with_phis else None
+        phase_angles = params[(2 if with_phis else 1) * n:] if with_phase_angles else None
+        return GivensAnsatzOp(norb, interaction_pairs, thetas, phis, phase_angles)
+
+    @staticmethod
+    def from_orbital_rotation(orbital_rotation: np.ndarray) -> "GivensAnsatzOp":
+        """From the Givens decomposition of the rotation, laid out in a brickwork
+        (givens.py:154-178)."""
+        norb = orbital_rotation.shape[0]
+        rots, phases = linalg.givens_decomposition(orbital_rotation)
+        pairs = [(i, j) for _, _, i, j in rots]
+        thetas = [float(np.arctan2(abs(s), c)) for c, s, _, _ in rots]
+        phis = [float(np.angle(s)) for _, s, _, _ in rots]
+        pairs, thetas, phis = _brickwork(pairs, thetas, phis, norb)
+        return GivensAnsatzOp(norb, pairs, np.array(thetas), np.array(phis), np.angle(phases))
+
+    def to_orbital_rotation(self) -> np.ndarray:
+        """diag(exp(i phase_angles)) times the rotations, last pair first, each
+        on columns (j, i): col_j <- c col_j + s col_i, col_i <- c col_i - conj(s) col_j
+        with c = cos(theta), s = sin(theta) exp(-i phi) (givens.py:180-198)."""
+        phis = np.zeros(len(self.interaction_pairs)) if self.phis is None else self.phis
+        angles = np.zeros(self.norb) if self.phase_angles is None else self.phase_angles
+        mat = np.diag(np.exp(1j * np.asarray(angles, dtype=float)))
+        for (i, j), theta, phi in zip(self.interaction_pairs[::-1], self.thetas[::-1], phis[::-1]):
+            c, s = np.cos(theta), np.sin(theta) * np.exp(-1j * phi)
+            cj, ci = mat[:, j].copy(), mat[:, i].copy()
+            mat[:, j] = c * cj + s * ci
+            mat[:, i] = c * ci - np.conj(s) * cj
+        return mat
+
+    def _apply_unitary_(self, vec, norb: int, nelec, copy: bool):
+        from ffsim_gb300.gates import apply_orbital_rotation
+
+        return apply_orbital_rotation(vec, self.to_orbital_rotation(), norb, nelec, copy=copy)
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, GivensAnsatzOp):
+            return NotImplemented
+        if self.norb != other.norb or list(self.interaction_pairs) != list(other.interaction_pairs):
+            return False
+        return (bool(np.allclose(self.thetas, other.thetas, rtol=rtol, atol=atol))
+                and _allclose_or_none(self.phis, other.phis, rtol, atol)
+                and _allclose_or_none(self.phase_angles, other.phase_angles, rtol, atol))

@@ -734,6 +734,37 @@ def ucj_spin_balanced_apply(vec, diag_coulomb_mats, orbital_rotations, final_orb
     return vec
 
 
+def ucj_spin_unbalanced_apply(vec, diag_coulomb_mats, orbital_rotations, final_orbital_rotation, norb, nelec):
+    """ucj_spin_unbalanced.py:705-745: per rep the (alpha, beta) rotations
+    U_k^dag U_{k-1} and exp(+i J_k) with [aa, ab, bb], then the final rotation."""
+    vec = np.array(vec, dtype=complex, copy=True)
+    basis = [np.eye(norb), np.eye(norb)]
+    for mats, rot in zip(diag_coulomb_mats, orbital_rotations):
+        vec = apply_orbital_rotation(vec, (rot[0].T.conj() @ basis[0], rot[1].T.conj() @ basis[1]), norb, nelec,
+                                     copy=False)
+        vec = apply_diag_coulomb_evolution(vec, (mats[0], mats[1], mats[2]), -1.0, norb, nelec, copy=False)
+        basis = [rot[0], rot[1]]
+    if final_orbital_rotation is not None:
+        basis = [final_orbital_rotation[0] @ basis[0], final_orbital_rotation[1] @ basis[1]]
+    return apply_orbital_rotation(vec, tuple(basis), norb, nelec, copy=False)
+
+
+def ucj_spinless_apply(vec, diag_coulomb_mats, orbital_rotations, final_orbital_rotation, norb, nelec):
+    """ucj_spinless.py:456-515: one rotation and one matrix per rep; on spinful
+    states the matrix acts within each spin, (J, 0, J)."""
+    vec = np.array(vec, dtype=complex, copy=True)
+    basis = np.eye(norb)
+    zero = np.zeros((norb, norb))
+    for mat, rot in zip(diag_coulomb_mats, orbital_rotations):
+        vec = apply_orbital_rotation(vec, rot.T.conj() @ basis, norb, nelec, copy=False)
+        m = mat if isinstance(nelec, int) else (mat, zero, mat)
+        vec = apply_diag_coulomb_evolution(vec, m, -1.0, norb, nelec, copy=False)
+        basis = rot
+    if final_orbital_rotation is not None:
+        basis = final_orbital_rotation @ basis
+    return apply_orbital_rotation(vec, basis, norb, nelec, copy=False)
+
+
 def antihermitians_from_parameters(params, dim_, n_mats):
     """linalg/util.py:93-124 (complex case)."""
     per = dim_**2

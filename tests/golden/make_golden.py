@@ -164,6 +164,9 @@ def install_stubs():
     ffsim.linalg = sys.modules["ffsim.linalg"]
     ffsim.protocols = proto
     ucj = _load("ffsim.variational.ucj_spin_balanced", "variational/ucj_spin_balanced.py")
+    ucju = _load("ffsim.variational.ucj_spin_unbalanced", "variational/ucj_spin_unbalanced.py")
+    ucjs = _load("ffsim.variational.ucj_spinless", "variational/ucj_spinless.py")
+    giv = _load("ffsim.variational.givens", "variational/givens.py")
     # Trotter: the reference's step iterator and double-factorized evolution
     # (the Hamiltonian class is only a type annotation there)
     _module("ffsim.hamiltonians", {"DoubleFactorizedHamiltonian": types.SimpleNamespace})
@@ -182,6 +185,9 @@ def install_stubs():
         zero_one_subspace_indices=gor._zero_one_subspace_indices,
         one_subspace_indices=gor._one_subspace_indices,
         UCJOpSpinBalanced=ucj.UCJOpSpinBalanced,
+        UCJOpSpinUnbalanced=ucju.UCJOpSpinUnbalanced,
+        UCJOpSpinless=ucjs.UCJOpSpinless,
+        GivensAnsatzOp=giv.GivensAnsatzOp,
     )
 
 
@@ -375,6 +381,50 @@ def main():
         out[f"trot{idx}_out"] = ref.simulate_trotter_double_factorized(
             vec, ham, t, norb=norb, nelec=nelec, n_steps=n_steps, order=order)
     out["trot_cases"] = np.asarray([[n, a, b, t, s, o, int(z)] for n, (a, b), t, s, o, z in trotter_cases])
+
+    # spin-unbalanced and spinless UCJ operators (reference dataclass methods)
+    ru = np.random.default_rng(20261205)
+    other_cases = [("ucju", 4, (2, 1), 2, False), ("ucju", 5, (2, 2), 1, True), ("ucjs", 4, (2, 2), 2, True),
+                   ("ucjs", 5, 2, 2, False)]
+    for idx, (kind, norb, nelec, n_reps, final) in enumerate(other_cases):
+        cls = ref.UCJOpSpinUnbalanced if kind == "ucju" else ref.UCJOpSpinless
+        n_params = cls.n_params(norb, n_reps, with_final_orbital_rotation=final)
+        params = ru.uniform(-1, 1, size=n_params)
+        op = cls.from_parameters(params, norb=norb, n_reps=n_reps, with_final_orbital_rotation=final)
+        d = orc.dim(norb, nelec)
+        vec = orc.random_state_vector(d, seed=ru)
+        out[f"ucjx{idx}_params"] = params
+        out[f"ucjx{idx}_dcm"] = op.diag_coulomb_mats
+        out[f"ucjx{idx}_rots"] = op.orbital_rotations
+        out[f"ucjx{idx}_in"] = vec
+        out[f"ucjx{idx}_out"] = op._apply_unitary_(vec, norb, nelec, copy=True)
+    out["ucjx_cases"] = np.asarray([[0 if k == "ucju" else 1, n, *(ne if isinstance(ne, tuple) else (ne, -1)), r,
+                                     int(fi)] for k, n, ne, r, fi in other_cases])
+
+    # Givens rotation ansatz (variational/givens.py): from parameters and from a rotation
+    rg = np.random.default_rng(20261206)
+    giv_cases = [(4, (2, 1), [(0, 1), (2, 3), (1, 2), (0, 1)], True, True),
+                 (5, (2, 2), [(1, 2), (3, 4), (0, 1), (2, 3)], False, True),
+                 (4, (1, 2), [(2, 3), (1, 2)], True, False)]
+    for idx, (norb, nelec, pairs, with_phis, with_angles) in enumerate(giv_cases):
+        n = ref.GivensAnsatzOp.n_params(norb, pairs, with_phis=with_phis, with_phase_angles=with_angles)
+        params = rg.uniform(-np.pi, np.pi, size=n)
+        op = ref.GivensAnsatzOp.from_parameters(params, norb, pairs, with_phis=with_phis,
+                                                 with_phase_angles=with_angles)
+        vec = orc.random_state_vector(orc.dim(norb, nelec), seed=rg)
+        out[f"giv{idx}_params"], out[f"giv{idx}_pairs"] = params, np.asarray(pairs)
+        out[f"giv{idx}_rot"] = op.to_orbital_rotation()
+        out[f"giv{idx}_in"] = vec
+        out[f"giv{idx}_out"] = op._apply_unitary_(vec, norb, nelec, copy=True)
+    out["giv_cases"] = np.asarray([[n, a, b, int(p), int(q)] for n, (a, b), _, p, q in giv_cases])
+    for norb in (4, 5):
+        u = orc.random_unitary(norb, seed=rg)
+        op = ref.GivensAnsatzOp.from_orbital_rotation(u)
+        out[f"givu{norb}_u"] = u
+        out[f"givu{norb}_pairs"] = np.asarray(op.interaction_pairs)
+        out[f"givu{norb}_thetas"] = np.asarray(op.thetas)
+        out[f"givu{norb}_phis"] = np.asarray(op.phis)
+        out[f"givu{norb}_angles"] = np.asarray(op.phase_angles)
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
