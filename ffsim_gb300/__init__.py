@@ -19,7 +19,7 @@ from ffsim_gb300.gates import (
     apply_orbital_rotation,
     apply_phase_shift_in_place,
 )
-from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian
+from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian, MolecularHamiltonian
 from ffsim_gb300.protocols import LinearOperator, apply_unitary, linear_operator
 from ffsim_gb300.rdm import rdms
 from ffsim_gb300.states import hartree_fock_state, vdot
@@ -33,6 +33,7 @@ __all__ = [
     "GivensAnsatzOp",
     "LUCJEnergy",
     "LinearOperator",
+    "MolecularHamiltonian",
     "UCJOpSpinBalanced",
     "UCJOpSpinUnbalanced",
     "UCJOpSpinless",

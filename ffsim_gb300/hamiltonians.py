@@ -1,5 +1,5 @@
-"""Double-factorized Hamiltonian with a GPU linear operator
-(python/ffsim/hamiltonians/double_factorized_hamiltonian.py)."""
+"""Double-factorized and molecular Hamiltonians with GPU linear operators
+(python/ffsim/hamiltonians/double_factorized_hamiltonian.py, molecular_hamiltonian.py)."""
 
 from __future__ import annotations
 
@@ -99,3 +99,81 @@ def _df_z_representation(diag_coulomb_mats, orbital_rotations):
     )
     constant = 0.25 * np.einsum("ijj->", diag_coulomb_mats) - 0.5 * np.sum(diag_coulomb_mats)
     return one_body, float(constant)
+
+
+def _exact_double_factorization(one_body, two_body, tol: float = 1e-12):
+    r"""An exact double-factorized form of
+    :math:`\sum h_{pq} E_{pq} + \frac12 \sum h_{pqrs} a^\dagger_{p\sigma} a^\dagger_{r\tau} a_{s\tau} a_{q\sigma}`
+    (:math:`E_{pq} = \sum_\sigma a^\dagger_{p\sigma} a_{q\sigma}`), for two-body
+    tensors with the symmetries of molecular integrals, h_pqrs = h_rspq =
+    conj(h_qpsr).
+
+    Normal ordering gives sum_pqrs h_pqrs E_pq E_rs / 2 plus the one-body term
+    -sum_r h_prrq / 2.  The matrix A[(p, q), (s, r)] = h_pqrs is Hermitian, so
+    h_pqrs = sum_t lambda_t L_t[p, q] conj(L_t[s, r]) and
+    sum h_pqrs E_pq E_rs = sum_t lambda_t X_t X_t^dag with X_t = sum L_t[p, q] E_pq.
+    With L_t = H1 + i H2 (H1, H2 Hermitian) and A_k = sum (H_k)_pq E_pq,
+    X X^dag = A_1^2 + A_2^2 + i [A_2, A_1], the commutator a one-body operator
+    with matrix i [H2, H1].  Each A_k^2 is (sum_i mu_i n_i)^2 in the eigenbasis U
+    of H_k: a diagonal Coulomb term J = lambda mu mu^T with rotation U.
+    Returns (one-body tensor, J terms, rotations)."""
+    n = one_body.shape[0]
+    h = np.asarray(two_body, dtype=complex)
+    kappa = np.asarray(one_body, dtype=complex) - 0.5 * np.einsum("prrq->pq", h)
+    amat = h.transpose(0, 1, 3, 2).reshape(n * n, n * n)
+    amat = (amat + amat.conj().T) / 2
+    lam, vecs = np.linalg.eigh(amat)
+    scale = max(np.abs(lam).max(), 1.0) if lam.size else 1.0
+    mats, rots = [], []
+    for t in range(lam.size):
+        if abs(lam[t]) <= tol * scale:
+            continue
+        l_t = vecs[:, t].reshape(n, n)
+        h1 = (l_t + l_t.conj().T) / 2
+        h2 = (l_t - l_t.conj().T) / 2j
+        for hk in (h1, h2):
+            if np.abs(hk).max() <= tol:
+                continue
+            mu, u = np.linalg.eigh(hk)
+            mats.append(lam[t] * np.outer(mu, mu))
+            rots.append(u)
+        kappa = kappa + 0.5 * lam[t] * 1j * (h2 @ h1 - h1 @ h2)
+    if not mats:
+        return kappa, np.zeros((0, n, n)), np.zeros((0, n, n), dtype=complex)
+    return kappa, np.stack(mats), np.stack(rots)
+
+
+@dataclasses.dataclass(frozen=True)
+class MolecularHamiltonian:
+    r""":math:`H = \sum h_{pq} a^\dagger_{p\sigma} a_{q\sigma} + \frac12 \sum h_{pqrs}
+    a^\dagger_{p\sigma} a^\dagger_{r\tau} a_{s\tau} a_{q\sigma} + \text{constant}`
+    (python/ffsim/hamiltonians/molecular_hamiltonian.py:24-60).
+
+    The linear operator (matvec and a fused FP64 ``expectation``) runs the
+    exact double-factorized form of the Hamiltonian on the GPU: at most
+    2 norb^2 rotated diagonal Coulomb terms.  The reference contracts the
+    two-body tensor with double-excitation string links on the CPU
+    (contract/two_body.py); the operator is the same."""
+
+    one_body_tensor: np.ndarray
+    two_body_tensor: np.ndarray
+    constant: float = 0.0
+
+    @property
+    def norb(self) -> int:
+        return self.one_body_tensor.shape[0]
+
+    def to_double_factorized(self) -> DoubleFactorizedHamiltonian:
+        kappa, mats, rots = _exact_double_factorization(self.one_body_tensor, self.two_body_tensor)
+        return DoubleFactorizedHamiltonian(kappa, mats, rots, constant=float(self.constant))
+
+    def _linear_operator_(self, norb: int, nelec) -> LinearOperator:
+        assert isinstance(nelec, tuple)
+        return self.to_double_factorized()._linear_operator_(norb, nelec)
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, MolecularHamiltonian):
+            return NotImplemented
+        return (bool(np.isclose(self.constant, other.constant, rtol=rtol, atol=atol))
+                and bool(np.allclose(self.one_body_tensor, other.one_body_tensor, rtol=rtol, atol=atol))
+                and bool(np.allclose(self.two_body_tensor, other.two_body_tensor, rtol=rtol, atol=atol)))

@@ -650,6 +650,41 @@ def one_body_action(vec, mat, norb, nelec):
     return out.reshape(-1)
 
 
+def molecular_hamiltonian_action(vec, one_body_tensor, two_body_tensor, constant, norb, nelec):
+    """H vec for H = sum h_pq E_pq + 1/2 sum h_pqrs a+_ps a+_rt a_st a_qs + constant
+    (hamiltonians/molecular_hamiltonian.py:24-60) from the definition, with
+    a+_ps a+_rt a_st a_qs = E^s_pq E^t_rs - delta_qr delta_st E^s_ps."""
+    na, nb = nelec
+    v2 = np.asarray(vec, dtype=complex).reshape(math.comb(norb, na), math.comb(norb, nb))
+
+    def e(x, p, q):
+        return _apply_excitation(x, norb, nelec, p, q, 0) + _apply_excitation(x, norb, nelec, p, q, 1)
+
+    out = constant * v2
+    for p in range(norb):
+        for q in range(norb):
+            coef = one_body_tensor[p, q] - 0.5 * sum(two_body_tensor[p, r, r, q] for r in range(norb))
+            if coef != 0:
+                out = out + coef * e(v2, p, q)
+    for r in range(norb):
+        for s in range(norb):
+            phi = e(v2, r, s)
+            for p in range(norb):
+                for q in range(norb):
+                    if two_body_tensor[p, q, r, s] != 0:
+                        out = out + 0.5 * two_body_tensor[p, q, r, s] * e(phi, p, q)
+    return out.reshape(-1)
+
+
+def random_two_body_tensor(norb, *, seed=None):
+    """sum_k M_k (x) M_k over norb**2 random Hermitian M_k (random/random.py:211-237):
+    the symmetries of molecular integrals, h_pqrs = h_rspq = conj(h_qpsr)."""
+    rng = np.random.default_rng(seed)
+    m = rng.standard_normal((norb * norb, norb, norb)) + 1j * rng.standard_normal((norb * norb, norb, norb))
+    m = m + m.transpose(0, 2, 1).conj()
+    return np.tensordot(m, m, axes=(0, 0))
+
+
 def rdm1s(vec, norb, nelec):
     """[alpha, beta] 1-RDMs, rdm[p, q] = <vec| a+_p a_q |vec>."""
     na, nb = nelec
