@@ -12,6 +12,35 @@ from ffsim_gb300 import _lib, linalg
 from ffsim_gb300._state import prepare, scratch, split_nelec, stream_ptr
 
 
+def validate_interaction_pairs(interaction_pairs, ordered: bool) -> None:
+    """No duplicates; unordered (same-spin or spinless) pairs must be upper
+    triangular (python/ffsim/variational/util.py:19-35)."""
+    if interaction_pairs is None:
+        return
+    if len(set(interaction_pairs)) != len(interaction_pairs):
+        raise ValueError(f"Duplicate interaction pairs encountered: {interaction_pairs}.")
+    if not ordered:
+        for i, j in interaction_pairs:
+            if i > j:
+                raise ValueError(
+                    "When specifying spinless, alpha-alpha or beta-beta interaction pairs, you must provide "
+                    f"only upper triangular pairs. Got {(i, j)}, which is a lower triangular pair.")
+
+
+def _triu(norb: int) -> list:
+    return list(itertools.combinations_with_replacement(range(norb), 2))
+
+
+def _put(mat, pairs, vals, symmetric: bool) -> None:
+    """Write vals at the pairs (and their mirror when symmetric)."""
+    if not pairs:
+        return
+    rows, cols = zip(*pairs)
+    if symmetric:
+        mat[cols, rows] = vals
+    mat[rows, cols] = vals
+
+
 @dataclass(frozen=True)
 class UCJOpSpinBalanced:
     r""":math:`\prod_{k=1}^L \mathcal{U}_k e^{i \mathcal{J}_k} \mathcal{U}_k^\dagger`, optionally
@@ -63,24 +92,29 @@ class UCJOpSpinBalanced:
         return self.diag_coulomb_mats.shape[0]
 
     @staticmethod
-    def n_params(norb: int, n_reps: int, *, with_final_orbital_rotation: bool = False) -> int:
-        """ucj_spin_balanced.py:149-195 without interaction pairs."""
+    def n_params(norb: int, n_reps: int, *, interaction_pairs=None,
+                 with_final_orbital_rotation: bool = False) -> int:
+        """ucj_spin_balanced.py:149-195.  ``interaction_pairs`` = (aa pairs, ab
+        pairs), each upper triangular or None (all pairs)."""
+        pairs_aa, pairs_ab = interaction_pairs if interaction_pairs is not None else (None, None)
+        validate_interaction_pairs(pairs_aa, ordered=False)
+        validate_interaction_pairs(pairs_ab, ordered=False)
         n_triu = norb * (norb + 1) // 2
-        return n_reps * (2 * n_triu + norb**2) + with_final_orbital_rotation * norb**2
+        n_aa = n_triu if pairs_aa is None else len(pairs_aa)
+        n_ab = n_triu if pairs_ab is None else len(pairs_ab)
+        return n_reps * (n_aa + n_ab + norb**2) + with_final_orbital_rotation * norb**2
 
     @staticmethod
-    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int,
+    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int, interaction_pairs=None,
                         with_final_orbital_rotation: bool = False) -> "UCJOpSpinBalanced":
-        """ucj_spin_balanced.py:197-293 without interaction pairs: per rep, the
-        orbital rotation's norb**2 parameters, then the aa and ab upper triangles."""
-        params = np.asarray(params, dtype=float)
-        n = UCJOpSpinBalanced.n_params(norb, n_reps, with_final_orbital_rotation=with_final_orbital_rotation)
-        if len(params) != n:
-            raise ValueError(
-                "The number of parameters passed did not match the number expected based on the "
-                f"function inputs. Expected {n} but got {len(params)}.")
-        triu = list(itertools.combinations_with_replacement(range(norb), 2))
-        rows, cols = zip(*triu)
+        """ucj_spin_balanced.py:197-293: per rep, the orbital rotation's norb**2
+        parameters, then the aa and the ab entries at their pairs (both matrices
+        symmetric); then the final rotation."""
+        params = _check_params(params, UCJOpSpinBalanced.n_params(
+            norb, n_reps, interaction_pairs=interaction_pairs,
+            with_final_orbital_rotation=with_final_orbital_rotation))
+        pairs_aa, pairs_ab = interaction_pairs if interaction_pairs is not None else (None, None)
+        pairs = [_triu(norb) if pairs_aa is None else pairs_aa, _triu(norb) if pairs_ab is None else pairs_ab]
         dcm = np.zeros((n_reps, 2, norb, norb))
         rots = np.zeros((n_reps, norb, norb), dtype=complex)
         index = 0
@@ -88,25 +122,26 @@ class UCJOpSpinBalanced:
             rots[r] = linalg.unitary_from_parameters(params[index: index + norb**2], norb)
             index += norb**2
             for t in range(2):
-                vals = params[index: index + len(triu)]
-                dcm[r, t][cols, rows] = vals
-                dcm[r, t][rows, cols] = vals
-                index += len(triu)
+                _put(dcm[r, t], pairs[t], params[index: index + len(pairs[t])], True)
+                index += len(pairs[t])
         final = None
         if with_final_orbital_rotation:
             final = linalg.unitary_from_parameters(params[index:], norb)
         return UCJOpSpinBalanced(dcm, rots, final)
 
-    def to_parameters(self) -> np.ndarray:
-        """ucj_spin_balanced.py:295-374 without interaction pairs."""
-        n_reps, _, norb, _ = self.diag_coulomb_mats.shape
-        triu = list(itertools.combinations_with_replacement(range(norb), 2))
-        idx = tuple(zip(*triu))
+    def to_parameters(self, *, interaction_pairs=None) -> np.ndarray:
+        """ucj_spin_balanced.py:295-374."""
+        norb = self.norb
+        pairs_aa, pairs_ab = interaction_pairs if interaction_pairs is not None else (None, None)
+        validate_interaction_pairs(pairs_aa, ordered=False)
+        validate_interaction_pairs(pairs_ab, ordered=False)
+        pairs = [_triu(norb) if pairs_aa is None else pairs_aa, _triu(norb) if pairs_ab is None else pairs_ab]
         out = []
         for u, mats in zip(self.orbital_rotations, self.diag_coulomb_mats):
             out.append(linalg.unitary_to_parameters(u))
-            out.append(mats[0][idx])
-            out.append(mats[1][idx])
+            for t in range(2):
+                if pairs[t]:
+                    out.append(mats[t][tuple(zip(*pairs[t]))])
         if self.final_orbital_rotation is not None:
             out.append(linalg.unitary_to_parameters(self.final_orbital_rotation))
         return np.concatenate(out)
@@ -210,50 +245,56 @@ class UCJOpSpinUnbalanced:
         return self.diag_coulomb_mats.shape[0]
 
     @staticmethod
-    def n_params(norb: int, n_reps: int, *, with_final_orbital_rotation: bool = False) -> int:
-        """ucj_spin_unbalanced.py:146-206 without interaction pairs."""
-        n_triu = norb * (norb + 1) // 2
-        return n_reps * (2 * n_triu + norb**2 + 2 * norb**2) + with_final_orbital_rotation * 2 * norb**2
+    def _pairs(norb: int, interaction_pairs):
+        pairs_aa, pairs_ab, pairs_bb = interaction_pairs if interaction_pairs is not None else (None, None, None)
+        validate_interaction_pairs(pairs_aa, ordered=False)
+        validate_interaction_pairs(pairs_ab, ordered=True)
+        validate_interaction_pairs(pairs_bb, ordered=False)
+        full = list(itertools.product(range(norb), repeat=2))
+        return [_triu(norb) if pairs_aa is None else pairs_aa, full if pairs_ab is None else pairs_ab,
+                _triu(norb) if pairs_bb is None else pairs_bb]
 
     @staticmethod
-    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int,
+    def n_params(norb: int, n_reps: int, *, interaction_pairs=None,
+                 with_final_orbital_rotation: bool = False) -> int:
+        """ucj_spin_unbalanced.py:146-206.  ``interaction_pairs`` = (aa, ab, bb);
+        aa and bb upper triangular, ab ordered; None means all pairs."""
+        pairs = UCJOpSpinUnbalanced._pairs(norb, interaction_pairs)
+        return n_reps * (sum(len(x) for x in pairs) + 2 * norb**2) + with_final_orbital_rotation * 2 * norb**2
+
+    @staticmethod
+    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int, interaction_pairs=None,
                         with_final_orbital_rotation: bool = False) -> "UCJOpSpinUnbalanced":
-        """ucj_spin_unbalanced.py:208-329 without interaction pairs: per rep the
-        alpha and beta rotations (norb**2 each), the aa upper triangle, the ab
-        matrix (row-major) and the bb upper triangle; then the final rotations."""
+        """ucj_spin_unbalanced.py:208-329: per rep the alpha and beta rotations
+        (norb**2 each), then the aa, ab and bb entries at their pairs (aa, bb
+        symmetric); then the final rotations."""
         params = _check_params(params, UCJOpSpinUnbalanced.n_params(
-            norb, n_reps, with_final_orbital_rotation=with_final_orbital_rotation))
-        triu = tuple(zip(*itertools.combinations_with_replacement(range(norb), 2)))
+            norb, n_reps, interaction_pairs=interaction_pairs,
+            with_final_orbital_rotation=with_final_orbital_rotation))
+        pairs = UCJOpSpinUnbalanced._pairs(norb, interaction_pairs)
         dcm = np.zeros((n_reps, 3, norb, norb))
         rots = np.zeros((n_reps, 2, norb, norb), dtype=complex)
         i = 0
         for r in range(n_reps):
-            for s in range(2):
-                rots[r, s] = linalg.unitary_from_parameters(params[i: i + norb**2], norb)
+            for sp in range(2):
+                rots[r, sp] = linalg.unitary_from_parameters(params[i: i + norb**2], norb)
                 i += norb**2
-            for t in (0, 1, 2):
-                if t == 1:
-                    dcm[r, 1] = params[i: i + norb**2].reshape(norb, norb)
-                    i += norb**2
-                else:
-                    vals = params[i: i + len(triu[0])]
-                    dcm[r, t][triu[1], triu[0]] = vals
-                    dcm[r, t][triu] = vals
-                    i += len(triu[0])
+            for t in range(3):
+                _put(dcm[r, t], pairs[t], params[i: i + len(pairs[t])], t != 1)
+                i += len(pairs[t])
         final = None
         if with_final_orbital_rotation:
-            final = np.stack([linalg.unitary_from_parameters(params[i + s * norb**2: i + (s + 1) * norb**2], norb)
-                              for s in range(2)])
+            final = np.stack([linalg.unitary_from_parameters(params[i + sp * norb**2: i + (sp + 1) * norb**2], norb)
+                              for sp in range(2)])
         return UCJOpSpinUnbalanced(dcm, rots, final)
 
-    def to_parameters(self) -> np.ndarray:
-        """ucj_spin_unbalanced.py:331-432 without interaction pairs."""
-        norb = self.norb
-        triu = tuple(zip(*itertools.combinations_with_replacement(range(norb), 2)))
+    def to_parameters(self, interaction_pairs=None) -> np.ndarray:
+        """ucj_spin_unbalanced.py:331-432."""
+        pairs = UCJOpSpinUnbalanced._pairs(self.norb, interaction_pairs)
         out = []
         for u, mats in zip(self.orbital_rotations, self.diag_coulomb_mats):
             out += [linalg.unitary_to_parameters(u[0]), linalg.unitary_to_parameters(u[1])]
-            out += [mats[0][triu], mats[1].reshape(-1), mats[2][triu]]
+            out += [mats[t][tuple(zip(*pairs[t]))] for t in range(3) if pairs[t]]
         if self.final_orbital_rotation is not None:
             out += [linalg.unitary_to_parameters(u) for u in self.final_orbital_rotation]
         return np.concatenate(out)
@@ -336,37 +377,42 @@ class UCJOpSpinless:
         return self.diag_coulomb_mats.shape[0]
 
     @staticmethod
-    def n_params(norb: int, n_reps: int, *, with_final_orbital_rotation: bool = False) -> int:
-        """ucj_spinless.py:133-172 without interaction pairs."""
-        return n_reps * (norb * (norb + 1) // 2 + norb**2) + with_final_orbital_rotation * norb**2
+    def n_params(norb: int, n_reps: int, *, interaction_pairs=None,
+                 with_final_orbital_rotation: bool = False) -> int:
+        """ucj_spinless.py:133-172 (``interaction_pairs``: upper triangular, or None for all)."""
+        validate_interaction_pairs(interaction_pairs, ordered=False)
+        n_pairs = norb * (norb + 1) // 2 if interaction_pairs is None else len(interaction_pairs)
+        return n_reps * (n_pairs + norb**2) + with_final_orbital_rotation * norb**2
 
     @staticmethod
-    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int,
+    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int, interaction_pairs=None,
                         with_final_orbital_rotation: bool = False) -> "UCJOpSpinless":
-        """ucj_spinless.py:174-262 without interaction pairs: per rep the
-        rotation's norb**2 parameters, then the upper triangle."""
+        """ucj_spinless.py:174-262: per rep the rotation's norb**2 parameters,
+        then the (symmetric) matrix entries at the pairs."""
         params = _check_params(params, UCJOpSpinless.n_params(
-            norb, n_reps, with_final_orbital_rotation=with_final_orbital_rotation))
-        triu = tuple(zip(*itertools.combinations_with_replacement(range(norb), 2)))
+            norb, n_reps, interaction_pairs=interaction_pairs,
+            with_final_orbital_rotation=with_final_orbital_rotation))
+        pairs = _triu(norb) if interaction_pairs is None else interaction_pairs
         dcm = np.zeros((n_reps, norb, norb))
         rots = np.zeros((n_reps, norb, norb), dtype=complex)
         i = 0
         for r in range(n_reps):
             rots[r] = linalg.unitary_from_parameters(params[i: i + norb**2], norb)
             i += norb**2
-            vals = params[i: i + len(triu[0])]
-            dcm[r][triu[1], triu[0]] = vals
-            dcm[r][triu] = vals
-            i += len(triu[0])
+            _put(dcm[r], pairs, params[i: i + len(pairs)], True)
+            i += len(pairs)
         final = linalg.unitary_from_parameters(params[i:], norb) if with_final_orbital_rotation else None
         return UCJOpSpinless(dcm, rots, final)
 
-    def to_parameters(self) -> np.ndarray:
-        """ucj_spinless.py:264-324 without interaction pairs."""
-        triu = tuple(zip(*itertools.combinations_with_replacement(range(self.norb), 2)))
+    def to_parameters(self, *, interaction_pairs=None) -> np.ndarray:
+        """ucj_spinless.py:264-324."""
+        validate_interaction_pairs(interaction_pairs, ordered=False)
+        pairs = _triu(self.norb) if interaction_pairs is None else interaction_pairs
         out = []
         for u, m in zip(self.orbital_rotations, self.diag_coulomb_mats):
-            out += [linalg.unitary_to_parameters(u), m[triu]]
+            out.append(linalg.unitary_to_parameters(u))
+            if pairs:
+                out.append(m[tuple(zip(*pairs))])
         if self.final_orbital_rotation is not None:
             out.append(linalg.unitary_to_parameters(self.final_orbital_rotation))
         return np.concatenate(out)

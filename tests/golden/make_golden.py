@@ -426,6 +426,26 @@ def main():
         out[f"givu{norb}_phis"] = np.asarray(op.phis)
         out[f"givu{norb}_angles"] = np.asarray(op.phase_angles)
 
+    # UCJ parameter maps with restricted interaction pairs (local UCJ)
+    rp = np.random.default_rng(20261207)
+    pair_cases = [
+        ("bal", 4, 2, ([(0, 0), (1, 1), (0, 1), (2, 3)], [(0, 0), (1, 2), (3, 3)]), True),
+        ("bal", 5, 1, (None, [(p, p) for p in range(5)]), False),
+        ("unb", 4, 2, ([(0, 1), (2, 2)], [(1, 0), (0, 1), (3, 2)], None), True),
+        ("unb", 4, 1, ([], [(2, 2)], [(0, 3)]), False),
+        ("sl", 4, 2, [(0, 0), (1, 3), (2, 3)], True),
+    ]
+    for idx, (kind, norb, n_reps, pairs, final) in enumerate(pair_cases):
+        cls = {"bal": ref.UCJOpSpinBalanced, "unb": ref.UCJOpSpinUnbalanced, "sl": ref.UCJOpSpinless}[kind]
+        n = cls.n_params(norb, n_reps, interaction_pairs=pairs, with_final_orbital_rotation=final)
+        params = rp.uniform(-1, 1, size=n)
+        op = cls.from_parameters(params, norb=norb, n_reps=n_reps, interaction_pairs=pairs,
+                                 with_final_orbital_rotation=final)
+        out[f"pairs{idx}_params"] = params
+        out[f"pairs{idx}_dcm"] = op.diag_coulomb_mats
+        out[f"pairs{idx}_rots"] = op.orbital_rotations
+        out[f"pairs{idx}_to"] = op.to_parameters(interaction_pairs=pairs)
+
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
 

@@ -109,3 +109,35 @@ def test_givens_ansatz_apply(cuda, golden):
             v = torch.from_numpy(golden[f"giv{idx}_in"]).to("cuda").to(dtype)
             out = f.apply_unitary(v, op, norb, nelec)
             np.testing.assert_allclose(out.cpu().numpy().astype(complex), golden[f"giv{idx}_out"], atol=tol)
+
+
+def test_interaction_pairs(golden):
+    """Local-UCJ parameter maps with restricted interaction pairs, against the
+    reference's from_parameters / to_parameters of the three UCJ classes."""
+    import ffsim_gb300 as f
+
+    cases = [
+        (f.UCJOpSpinBalanced, 4, 2, ([(0, 0), (1, 1), (0, 1), (2, 3)], [(0, 0), (1, 2), (3, 3)]), True),
+        (f.UCJOpSpinBalanced, 5, 1, (None, [(p, p) for p in range(5)]), False),
+        (f.UCJOpSpinUnbalanced, 4, 2, ([(0, 1), (2, 2)], [(1, 0), (0, 1), (3, 2)], None), True),
+        (f.UCJOpSpinUnbalanced, 4, 1, ([], [(2, 2)], [(0, 3)]), False),
+        (f.UCJOpSpinless, 4, 2, [(0, 0), (1, 3), (2, 3)], True),
+    ]
+    for idx, (cls, norb, n_reps, pairs, final) in enumerate(cases):
+        params = golden[f"pairs{idx}_params"]
+        assert cls.n_params(norb, n_reps, interaction_pairs=pairs, with_final_orbital_rotation=final) == len(params)
+        op = cls.from_parameters(params, norb=norb, n_reps=n_reps, interaction_pairs=pairs,
+                                 with_final_orbital_rotation=final)
+        np.testing.assert_allclose(op.diag_coulomb_mats, golden[f"pairs{idx}_dcm"], atol=1e-15)
+        np.testing.assert_allclose(op.orbital_rotations, golden[f"pairs{idx}_rots"], atol=1e-12)
+        np.testing.assert_allclose(op.to_parameters(interaction_pairs=pairs), golden[f"pairs{idx}_to"], atol=1e-10)
+
+
+def test_interaction_pair_validation():
+    import ffsim_gb300 as f
+
+    with pytest.raises(ValueError):  # lower triangular same-spin pair
+        f.UCJOpSpinBalanced.n_params(4, 1, interaction_pairs=([(1, 0)], None))
+    with pytest.raises(ValueError):  # duplicates
+        f.UCJOpSpinUnbalanced.n_params(4, 1, interaction_pairs=(None, [(1, 0), (1, 0)], None))
+    assert f.UCJOpSpinUnbalanced.n_params(4, 1, interaction_pairs=(None, [(1, 0)], None)) == 10 + 1 + 10 + 32
