@@ -51,6 +51,8 @@ SIGNATURES = {
                                    _c_double, _c_double, _c_int, _c_int, _c_void_p],
     "ffgb_apply_phase_shift": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_double,
                                _c_double, _c_int, _c_void_p],
+    "ffgb_apply_excitation": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int,
+                              _c_void_p],
     "ffgb_apply_orbital_rotation": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _dp, _c_void_p,
                                     _c_size_t, _c_void_p],
     "ffgb_apply_diag_coulomb_evolution": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _dp, _dp,

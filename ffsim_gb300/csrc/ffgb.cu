@@ -1492,6 +1492,33 @@ int ffgb_apply_phase_shift(void* vec, int dtype, int norb, int na, int nb, int s
   return FFGB_OK;
 }
 
+int ffgb_apply_excitation(const void* vec, void* out, int dtype, int norb, int na, int nb, int spin, int p, int q,
+                          void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  if (!vec || !out || vec == out) return fail(FFGB_ERR_ARG, "vec and out must be distinct device buffers");
+  if (p < 0 || q < 0 || p >= norb || q >= norb) return fail(FFGB_ERR_ARG, "orbital index out of range");
+  if (spin != 0 && spin != 1) return fail(FFGB_ERR_ARG, "spin must be 0 (alpha) or 1 (beta)");
+  if (nb < 0 && spin != 0) return fail(FFGB_ERR_ARG, "spinless systems have one sector");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int sp = nb < 0 ? 0 : spin;
+  const int nocc = sp == 0 ? na : nb;
+  const long long da = binom_h(norb, na), db = nb < 0 ? 1 : binom_h(norb, nb);
+  const size_t el = dtype == FFGB_C64 ? sizeof(float2) : sizeof(double2);
+  FFGB_CUDA(cudaMemsetAsync(out, 0, (size_t)(da * db) * el, st));
+  if (nocc == 0 || da * db == 0) return FFGB_OK;
+  const unsigned* strs = nullptr;
+  FFGB_TRY(device_strings(norb, nocc, &strs));
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((da * db + 255) / 256, 8192));
+  if (dtype == FFGB_C64)
+    excitation_kernel<float><<<blocks, 256, 0, st>>>((const float2*)vec, (float2*)out, strs, da, db, sp, p, q);
+  else
+    excitation_kernel<double><<<blocks, 256, 0, st>>>((const double2*)vec, (double2*)out, strs, da, db, sp, p, q);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+
 int ffgb_apply_orbital_rotation(void* vec, int dtype, int norb, int na, int nb, const double* ma,
                                 const double* mb, void* scratch, size_t scratch_bytes, void* stream) {
   g_err.clear();

@@ -914,6 +914,48 @@ __global__ void phase_shift_kernel(typename CT<T>::type* __restrict__ vec, const
   }
 }
 
+// out = a+_{p spin} a_{q spin} in: each string with q occupied and p empty (or
+// p == q) moves to the string with q emptied and p filled, with the sign of the
+// occupied orbitals below q (annihilation) and below p after it (creation).
+// The map is injective for fixed (p, q), so every target is written once;
+// targets without a source keep the zeros the caller wrote.
+template <typename T>
+__global__ void excitation_kernel(const typename CT<T>::type* __restrict__ in, typename CT<T>::type* __restrict__ out,
+                                  const unsigned* __restrict__ strings, long long dim_a, long long dim_b, int spin,
+                                  int p, int q) {
+  using C = typename CT<T>::type;
+  __shared__ int sB[FFGB_BST * FFGB_BST];
+  for (int idx = threadIdx.x; idx < FFGB_BST * FFGB_BST; idx += blockDim.x) {
+    const int a = idx / FFGB_BST, b = idx % FFGB_BST;
+    long long r = 0;
+    if (b <= a) {
+      r = 1;
+      for (int i = 1; i <= b; ++i) r = r * (a - b + i) / i;
+    }
+    sB[idx] = (int)r;
+  }
+  __syncthreads();
+  const long long total = dim_a * dim_b;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long a = idx / dim_b, b = idx - a * dim_b;
+    const unsigned s = strings[spin == 0 ? a : b];
+    if (!((s >> q) & 1u)) continue;
+    const unsigned mid = s & ~(1u << q);
+    if (p != q && ((mid >> p) & 1u)) continue;
+    const unsigned t = mid | (1u << p);
+    const int parity = (__popc(s & ((1u << q) - 1u)) + __popc(mid & ((1u << p) - 1u))) & 1;
+    const long long r = rank_colex(t, sB);
+    const long long dst = spin == 0 ? r * dim_b + b : a * dim_b + r;
+    C v = in[idx];
+    if (parity) {
+      v.x = -v.x;
+      v.y = -v.y;
+    }
+    out[dst] = v;
+  }
+}
+
 // F_C(j) of the rotated sector: phase exp(i F) (mode 1) or coefficient F (mode 2)
 template <typename T>
 __global__ void col_table_kernel(const unsigned* __restrict__ strings, int dim, int norb, int zrep,

@@ -100,6 +100,13 @@ size_t ffgb_scratch_bytes(int op, int dtype, int norb, int n_alpha, int n_beta);
 int ffgb_apply_givens_rotation(void* vec, int dtype, int norb, int n_alpha, int n_beta, int spin,
                                double c, double s_re, double s_im, int i, int j, void* stream);
 
+/* out = a+_{p spin} a_{q spin} vec (a single excitation within one spin
+ * sector; out is zeroed first, vec and out must differ).  The building block of
+ * the rank-2 reduced density matrices, which the reference computes with pyscf
+ * (python/ffsim/states/rdm.py:181-274 via make_rdm12s / trans_rdm12s). */
+int ffgb_apply_excitation(const void* vec, void* out, int dtype, int norb, int n_alpha, int n_beta, int spin,
+                          int p, int q, void* stream);
+
 /* Multiply every string with orbital orb occupied in one spin sector by
  * phase.  Replaces apply_phase_shift_in_place (src/gates/phase_shift.rs:17-30). */
 int ffgb_apply_phase_shift(void* vec, int dtype, int norb, int n_alpha, int n_beta, int spin,

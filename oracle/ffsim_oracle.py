@@ -650,6 +650,26 @@ def one_body_action(vec, mat, norb, nelec):
     return out.reshape(-1)
 
 
+def rdm2s(vec, norb, nelec, reorder=True):
+    """[aa, ab, bb] 2-RDMs from the definition (states/rdm.py:73-120):
+    reorder=True: rdm2[p, q, r, s] = <a+_p a+_r a_s a_q>; reorder=False:
+    rdm2[p, q, r, s] = <a+_p a_q a+_r a_s>; first index pair on the first spin."""
+    na, nb = nelec
+    v2 = np.asarray(vec, dtype=complex).reshape(math.comb(norb, na), math.comb(norb, nb))
+    out = np.zeros((3, norb, norb, norb, norb), dtype=complex)
+    for blk, (t, sg) in enumerate([(0, 0), (0, 1), (1, 1)]):
+        for r in range(norb):
+            for s in range(norb):
+                phi = _apply_excitation(v2, norb, nelec, r, s, sg)
+                for p in range(norb):
+                    for q in range(norb):
+                        val = np.vdot(v2, _apply_excitation(phi, norb, nelec, p, q, t))
+                        if reorder and t == sg and q == r:
+                            val -= np.vdot(v2, _apply_excitation(v2, norb, nelec, p, s, t))
+                        out[blk, p, q, r, s] = val
+    return out
+
+
 def molecular_hamiltonian_action(vec, one_body_tensor, two_body_tensor, constant, norb, nelec):
     """H vec for H = sum h_pq E_pq + 1/2 sum h_pqrs a+_ps a+_rt a_st a_qs + constant
     (hamiltonians/molecular_hamiltonian.py:24-60) from the definition, with
