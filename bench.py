@@ -451,6 +451,24 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def replica_max_ms(local_ms: float, dist, device: str) -> float:
+    """The slowest replica's time: the job ends when every rank has finished
+    its K steps (a max all-reduce; the only collective, none on the data path)."""
+    if dist is None:
+        return float(local_ms)
+    import torch
+
+    t = torch.tensor([float(local_ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, steps: int, max_ms: float) -> float:
+    """Whole-job evaluations per second: every replica runs its own `steps`
+    evaluations (weak scaling), timed by the slowest one."""
+    return world * steps / (max_ms * 1e-3)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -521,12 +539,8 @@ def main():
     launches = (lib.ffgb_launch_count() - n0) // (args.steps + args.warmup)
     clk = clocks.stop()
     barrier()
-    total_ms = sum(times64)
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps / (total_ms * 1e-3)
+    total_ms = replica_max_ms(sum(times64), dist, "cuda")
+    value = replica_throughput(world, args.steps, total_ms)
 
     # complex128 on the same GPU (fewer steps: FP64 bound)
     times128, energies128 = time_energy(torch.complex128, args.c128_steps, 1, ucj, ham, stream)
