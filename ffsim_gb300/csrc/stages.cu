@@ -419,10 +419,16 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
     std::memcpy(&P, base.get(), sizeof(WinJob));
     if (jb.a->off.size() > 72) return fail(FFGB_ERR_UNSUPPORTED, "window member table overflow");
     P.gbase_a = L->dev_base + jb.a->base_off + jb.start;
-    for (size_t j = 0; j < jb.a->off.size(); ++j) P.off_a[j] = jb.a->off[j];
+    for (size_t j = 0; j < jb.a->off.size(); ++j) {
+      P.off_a[j] = jb.a->off[j];
+      P.eoff_a[j] = (long long)jb.a->off[j] * ld;
+    }
     if (jb.b) {
       P.gbase_b = L->dev_base + jb.b->base_off;
-      for (size_t j = 0; j < jb.b->off.size(); ++j) P.off_b[j] = jb.b->off[j];
+      for (size_t j = 0; j < jb.b->off.size(); ++j) {
+        P.off_b[j] = jb.b->off[j];
+        P.eoff_b[j] = (long long)jb.b->off[j] * ld;
+      }
     }
     P.n_groups = (int)jb.n;
     const long long items = jb.n * base->tiles;

@@ -44,6 +44,7 @@ struct WinJob {
   const int* gbase_a;  // base row of every group of class K (device table)
   const int* gbase_b;  // and of the paired class B - K (packed launches)
   int off_a[72], off_b[72];    // member row offsets from the base row (windows not starting at orbital 0)
+  long long eoff_a[72], eoff_b[72];  // the same times ld: element offsets, so an address is one add
   float gp[84], gl[84];        // window network coefficients (see win_coef)
   unsigned gt[84];
   unsigned salt;
@@ -148,6 +149,9 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
   // member j of group A (class K) / group B (class B - K): row offset from the group's base
 #define ROW_A(j) (LOW ? (long long)(j) : (long long)P.off_a[(j)])
 #define ROW_B(j) (LOW ? (long long)(j) : (long long)P.off_b[(j)])
+  // element offsets of member j for the leading dimension `l`
+#define EL_A(j, l) (LOW ? (long long)(j) * (l) : P.eoff_a[(j)])
+#define EL_B(j, l) (LOW ? (long long)(j) * (l) : P.eoff_b[(j)])
   double part = 0.0;
   // fused expectation: the operator's weights for this CTA's group(s), once per CTA
   constexpr int XS = EXPECT ? FFGB_MAXN : 1;
@@ -180,7 +184,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
       constexpr int M = WinNet<B, K>::M;
       float2 v[M];
 #pragma unroll
-      for (int j = 0; j < M; ++j) v[j] = sa[ROW_A(j) * ld];
+      for (int j = 0; j < M; ++j) v[j] = sa[EL_A(j, ld)];
       WinNet<B, K>::template apply<MODE>(v, P.gp, P.gl, P.gt, rng);
       if constexpr (!EXPECT) {
         // fresh copies: keeps the compiler from holding every member's offset
@@ -189,7 +193,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
         long long ls = ld;
         asm volatile("" : "+l"(da), "+l"(ls));
 #pragma unroll
-        for (int j = 0; j < M; ++j) da[ROW_A(j) * ls] = v[j];
+        for (int j = 0; j < M; ++j) da[EL_A(j, ls)] = v[j];
       } else {
         const StageExpect& E = P.ex;
         ZCtx za, zb;
@@ -218,8 +222,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
       float2 R[NP], I[NP];
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
-        const float2 a = sa[ROW_A(PK::lane0(q)) * ld];
-        const float2 b = s1[(PAIR ? ROW_B(PK::lane1(q)) : ROW_A(PK::lane1(q))) * ld];
+        const float2 a = sa[EL_A(PK::lane0(q), ld)];
+        const float2 b = s1[PAIR ? EL_B(PK::lane1(q), ld) : EL_A(PK::lane1(q), ld)];
         R[q] = make_float2(a.x, b.x);
         I[q] = make_float2(a.y, b.y);
       }
@@ -231,9 +235,9 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
         asm volatile("" : "+l"(da), "+l"(db), "+l"(ls));
 #pragma unroll
         for (int q = 0; q < NP; ++q) {
-          const long long o0 = ROW_A(PK::lane0(q)), o1 = PAIR ? ROW_B(PK::lane1(q)) : ROW_A(PK::lane1(q));
-          da[o0 * ls] = make_float2(R[q].x, I[q].x);
-          db[o1 * ls] = make_float2(R[q].y, I[q].y);
+          const long long o0 = EL_A(PK::lane0(q), ls), o1 = PAIR ? EL_B(PK::lane1(q), ls) : EL_A(PK::lane1(q), ls);
+          da[o0] = make_float2(R[q].x, I[q].x);
+          db[o1] = make_float2(R[q].y, I[q].y);
         }
       } else {
         const StageExpect& E = P.ex;
@@ -255,6 +259,8 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
   }
 #undef ROW_A
 #undef ROW_B
+#undef EL_A
+#undef EL_B
   if constexpr (EXPECT) {
     __shared__ double sh[STAGE_THREADS / 32];
     const double s = block_sum_128(part, sh);
