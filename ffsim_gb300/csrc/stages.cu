@@ -486,7 +486,7 @@ int launch_transpose(const void* in, void* out, long long rows, long long cols, 
                      const void* col_ph, cudaStream_t st) {
   using Cx = typename CT<T>::type;
   if (rows <= 0 || cols <= 0) return FFGB_OK;
-  const long long gy = (rows + 31) / 32;
+  const long long gy = (rows + 63) / 64;
   if (gy > 65535) return fail(FFGB_ERR_UNSUPPORTED, "transpose: too many rows");
   dim3 grid((unsigned)((cols + 31) / 32), (unsigned)gy);
   transpose_kernel<Cx><<<grid, 256, 0, st>>>((const Cx*)in, (Cx*)out, rows, cols, (const Cx*)row_ph,

@@ -365,16 +365,19 @@ __global__ void __launch_bounds__(STAGE_THREADS, M >= 5 ? 3 : (M >= 4 ? 4 : 6))
   }
 }
 
-// out[c][r] = in[r][c] * row_ph[r] * col_ph[c] (phase tables optional).
+// out[c][r] = in[r][c] * row_ph[r] * col_ph[c] (phase tables optional).  A CTA
+// moves a 64-row x 32-column tile through shared memory (padded rows: no bank
+// conflicts); each thread has eight loads in flight.
 template <typename C>
 __global__ void __launch_bounds__(256) transpose_kernel(const C* __restrict__ in, C* __restrict__ out,
                                                         long long rows, long long cols,
                                                         const C* __restrict__ row_ph,
                                                         const C* __restrict__ col_ph) {
-  __shared__ C tile[32][33];
-  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+  __shared__ C tile[64][33];
+  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 64;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int j = ty; j < 32; j += 8) {
+#pragma unroll
+  for (int j = ty; j < 64; j += 8) {
     const long long r = r0 + j, c = c0 + tx;
     if (r < rows && c < cols) {
       C v = in[r * cols + c];
@@ -384,9 +387,14 @@ __global__ void __launch_bounds__(256) transpose_kernel(const C* __restrict__ in
     }
   }
   __syncthreads();
+#pragma unroll
   for (int j = ty; j < 32; j += 8) {
-    const long long c = c0 + j, r = r0 + tx;
-    if (c < cols && r < rows) out[c * rows + r] = tile[tx][j];
+    const long long c = c0 + j;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long long r = r0 + tx + 32 * h;
+      if (c < cols && r < rows) out[c * rows + r] = tile[tx + 32 * h][j];
+    }
   }
 }
 
