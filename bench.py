@@ -295,6 +295,34 @@ def run_ops(args) -> None:
         del ops["cross_half_stage"]
     if args.dtype != "c64":  # the stage kernels are complex64
         del ops["window_stage"]
+
+    # compositions on the same entry points: Trotter evolution, the
+    # spin-unbalanced UCJ operator, 1-RDMs and a molecular Hamiltonian
+    def on_stream(fn):
+        def run():
+            with torch.cuda.stream(stream):
+                fn()
+        return run
+
+    ucju = f.UCJOpSpinUnbalanced.from_parameters(
+        rng.uniform(-0.5, 0.5, size=f.UCJOpSpinUnbalanced.n_params(norb, 2)), norb=norb, n_reps=2)
+    ops[f"trotter_step_rank{norb}"] = (norb * 6 * S + 4 * S, on_stream(
+        lambda: f.simulate_trotter_double_factorized(v, ham, 0.1, norb=norb, nelec=nelec, copy=False)))
+    ops["ucj_spin_unbalanced_apply_L2"] = (3 * 4 * S + 2 * 2 * S, on_stream(
+        lambda: f.apply_unitary(v, ucju, norb, nelec, copy=False)))
+    ops["rdm1"] = (S, on_stream(lambda: f.rdms(v, norb, nelec)))
+    if norb == NORB:
+        n12, ne12 = 12, (6, 6)
+        g = rng.standard_normal((n12, n12)) + 1j * rng.standard_normal((n12, n12))
+        mk = rng.standard_normal((n12 * n12, n12, n12)) + 1j * rng.standard_normal((n12 * n12, n12, n12))
+        mk = mk + mk.transpose(0, 2, 1).conj()
+        mol = f.MolecularHamiltonian((g + g.conj().T) / 2, np.tensordot(mk, mk, axes=(0, 0)) / n12**2, 0.5)
+        lin12 = f.linear_operator(mol, n12, ne12)
+        n_terms = mol.to_double_factorized().diag_coulomb_mats.shape[0] + 1
+        with torch.cuda.stream(stream):
+            v12 = torch.randn(f.dim(n12, ne12), dtype=dtype, device="cuda")
+        ops[f"molecular_matvec_norb12_{n_terms}terms"] = (n_terms * 9 * v12.numel() * el,
+                                                          on_stream(lambda: lin12 @ v12))
     for name, (nb, fn) in ops.items():
         try:
             ms = timed(fn)

@@ -2,8 +2,11 @@
 // energy:
 //   transition one-body density  G^s_pq = <x| a+_{p s} a_{q s} |y>
 //   diagonal pair density        P^{st}_ij = <x| n_{i s} n_{j t} |y>
-// Both are accumulated in FP64 from complex64 or complex128 states, per CTA,
-// and the partial sums are reduced on the host in a fixed order.
+// A thread sums its share of one row (a few dozen products) in the state's
+// precision -- FP32 for complex64, whose products are FP32 anyway, FP64 for
+// complex128 -- and everything above that (rows, CTAs) accumulates in FP64;
+// the CTAs' partial sums are reduced on the host in a fixed order.  (FP64
+// arithmetic per element ran at 3 GB/s on GB300, whose FP64 rate is low.)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,11 +21,17 @@ namespace {
 constexpr int DTHREADS = 256;
 constexpr int RDM_ROWS = 16;  // rows of the rotated sector per CTA
 
+// Row partials in the state's precision: float2 for complex64, double2 for complex128.
 template <typename C>
-__device__ __forceinline__ double2 cdot_acc(double2 acc, C a, C b) {  // acc += conj(a) * b
-  acc.x += (double)a.x * (double)b.x + (double)a.y * (double)b.y;
-  acc.y += (double)a.x * (double)b.y - (double)a.y * (double)b.x;
+__device__ __forceinline__ C cdot_row(C acc, C a, C b) {  // acc += conj(a) * b
+  acc.x = fma(a.x, b.x, fma(a.y, b.y, acc.x));
+  acc.y = fma(a.x, b.y, fma(-a.y, b.x, acc.y));
   return acc;
+}
+
+template <typename C>
+__device__ __forceinline__ double2 to_d2(C v) {
+  return make_double2((double)v.x, (double)v.y);
 }
 
 __device__ __forceinline__ double2 block_sum2(double2 v, double2* sh) {
@@ -78,8 +87,10 @@ __global__ void __launch_bounds__(DTHREADS) rdm1_kernel(const typename CT<T>::ty
     const long long ap = rank_colex(t, sB);
     const auto* xr = x + ap * cols;
     const auto* yr = y + (long long)a * cols;
-    double2 d = make_double2(0.0, 0.0);
-    for (int c = threadIdx.x; c < cols; c += DTHREADS) d = cdot_acc(d, xr[c], yr[c]);
+    typename CT<T>::type dr;
+    dr.x = dr.y = (T)0;
+    for (int c = threadIdx.x; c < cols; c += DTHREADS) dr = cdot_row(dr, xr[c], yr[c]);
+    double2 d = to_d2(dr);
     if (sign) {
       d.x = -d.x;
       d.y = -d.y;
@@ -111,12 +122,15 @@ __global__ void __launch_bounds__(DTHREADS) pair_density_kernel(const typename C
   for (int a = a0; a < a1; ++a) {
     const auto* xr = x + (long long)a * cols;
     const auto* yr = y + (long long)a * cols;
-    double2 r = make_double2(0.0, 0.0);
-    double2 cj[FFGB_MAXN];
+    using Cx = typename CT<T>::type;
+    Cx r, cj[FFGB_MAXN];
+    r.x = r.y = (T)0;
 #pragma unroll
-    for (int j = 0; j < FFGB_MAXN; ++j) cj[j] = make_double2(0.0, 0.0);
+    for (int j = 0; j < FFGB_MAXN; ++j) cj[j].x = cj[j].y = (T)0;
     for (int c = threadIdx.x; c < cols; c += DTHREADS) {
-      const double2 w = cdot_acc(make_double2(0.0, 0.0), xr[c], yr[c]);
+      Cx w;
+      w.x = w.y = (T)0;
+      w = cdot_row(w, xr[c], yr[c]);
       r.x += w.x;
       r.y += w.y;
       const unsigned sc = cstr[c];
@@ -127,12 +141,12 @@ __global__ void __launch_bounds__(DTHREADS) pair_density_kernel(const typename C
           cj[j].y += w.y;
         }
     }
-    const double2 rs = block_sum2(r, sh);
+    const double2 rs = block_sum2(to_d2(r), sh);
     if (threadIdx.x == 0) red[FFGB_MAXN] = rs;
 #pragma unroll
     for (int j = 0; j < FFGB_MAXN; ++j) {
       if (j < norb) {  // uniform: every thread takes the same branch
-        const double2 v = block_sum2(cj[j], sh);
+        const double2 v = block_sum2(to_d2(cj[j]), sh);
         if (threadIdx.x == 0) red[j] = v;
       }
     }
