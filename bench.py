@@ -311,6 +311,13 @@ def run_ops(args) -> None:
     ops["ucj_spin_unbalanced_apply_L2"] = (3 * 4 * S + 2 * 2 * S, on_stream(
         lambda: f.apply_unitary(v, ucju, norb, nelec, copy=False)))
     ops["rdm1"] = (S, on_stream(lambda: f.rdms(v, norb, nelec)))
+    # split-operator step of a Hubbard chain (hopping 1, U 4): two rotations
+    # (the running basis, then the identity that closes the evolution) and one
+    # diagonal evolution
+    hop = np.diag(-np.ones(norb - 1), 1)
+    hub = f.DiagonalCoulombHamiltonian(hop + hop.T, np.stack([np.zeros((norb, norb)), 4.0 * np.eye(norb)]))
+    ops[f"trotter_split_op_step_norb{norb}"] = (2 * 4 * S + 2 * S, on_stream(
+        lambda: f.simulate_trotter_diag_coulomb_split_op(v, hub, 0.1, norb=norb, nelec=nelec, copy=False)))
     if norb == NORB:
         n12, ne12 = 12, (6, 6)
         g = rng.standard_normal((n12, n12)) + 1j * rng.standard_normal((n12, n12))
@@ -324,6 +331,8 @@ def run_ops(args) -> None:
         ops[f"molecular_matvec_norb12_{n_terms}terms"] = (n_terms * 9 * v12.numel() * el,
                                                           on_stream(lambda: lin12 @ v12))
     for name, (nb, fn) in ops.items():
+        if args.op and args.op not in name:
+            continue
         try:
             ms = timed(fn)
             gbs = nb / (ms * 1e-3) / 1e9
@@ -509,6 +518,7 @@ def main():
     ap.add_argument("--norb", type=int, default=NORB, help="--ops: orbitals (half filling)")
     ap.add_argument("--dtype", default="c64", choices=["c64", "c128"], help="--ops: state dtype")
     ap.add_argument("--reps", type=int, default=5, help="--ops: timed repetitions per op")
+    ap.add_argument("--op", default="", help="--ops: only the ops whose name contains this text")
     ap.add_argument("--grad", action="store_true", help="gradient workload (norb=12, batch of parameters)")
     ap.add_argument("--batch", type=int, default=64, help="--grad: parameter vectors")
     ap.add_argument("--serve", action="store_true", help="serving workload (mixed requests, Poisson arrivals)")

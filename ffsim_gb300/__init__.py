@@ -19,16 +19,17 @@ from ffsim_gb300.gates import (
     apply_orbital_rotation,
     apply_phase_shift_in_place,
 )
-from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian, MolecularHamiltonian
-from ffsim_gb300.protocols import LinearOperator, apply_unitary, linear_operator
+from ffsim_gb300.hamiltonians import DiagonalCoulombHamiltonian, DoubleFactorizedHamiltonian, MolecularHamiltonian
+from ffsim_gb300.protocols import LinearOperator, apply_unitary, diag, linear_operator, trace
 from ffsim_gb300.rdm import rdms
 from ffsim_gb300.states import hartree_fock_state, vdot
-from ffsim_gb300.trotter import simulate_trotter_double_factorized
+from ffsim_gb300.trotter import simulate_trotter_diag_coulomb_split_op, simulate_trotter_double_factorized
 from ffsim_gb300.variational import GivensAnsatzOp, UCJOpSpinBalanced, UCJOpSpinless, UCJOpSpinUnbalanced
 
 __all__ = [
     "LUCJGradient",
     "lucj_energy_autograd",
+    "DiagonalCoulombHamiltonian",
     "DoubleFactorizedHamiltonian",
     "GivensAnsatzOp",
     "LUCJEnergy",
@@ -44,8 +45,10 @@ __all__ = [
     "apply_phase_shift_in_place",
     "apply_unitary",
     "rdms",
+    "simulate_trotter_diag_coulomb_split_op",
     "simulate_trotter_double_factorized",
     "contract",
+    "diag",
     "dim",
     "dims",
     "hartree_fock_state",
@@ -54,5 +57,6 @@ __all__ = [
     "lucj_energy",
     "random",
     "states",
+    "trace",
     "vdot",
 ]

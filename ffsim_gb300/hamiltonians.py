@@ -177,3 +177,72 @@ class MolecularHamiltonian:
         return (bool(np.isclose(self.constant, other.constant, rtol=rtol, atol=atol))
                 and bool(np.allclose(self.one_body_tensor, other.one_body_tensor, rtol=rtol, atol=atol))
                 and bool(np.allclose(self.two_body_tensor, other.two_body_tensor, rtol=rtol, atol=atol)))
+
+
+@dataclasses.dataclass(frozen=True)
+class DiagonalCoulombHamiltonian:
+    r""":math:`H = \sum h_{pq} a^\dagger_{p\sigma} a_{q\sigma} + \frac12 \sum
+    J^{\sigma\tau}_{pq} n_{p\sigma} n_{q\tau} + \text{constant}` with
+    :math:`J^{\alpha\alpha} = J^{\beta\beta}` = ``diag_coulomb_mats[0]`` and
+    :math:`J^{\alpha\beta} = J^{\beta\alpha}` = ``diag_coulomb_mats[1]``
+    (python/ffsim/hamiltonians/diagonal_coulomb_hamiltonian.py:27-66).
+
+    The linear operator is one rotated number-operator matvec in the eigenbasis
+    of h (``ffgb_rotated_diag_matvec``) plus one diagonal Coulomb contraction
+    in the occupation basis (``ffgb_contract_diag_coulomb``); the diagonal is
+    the same two contractions applied to the all-ones vector."""
+
+    one_body_tensor: np.ndarray
+    diag_coulomb_mats: np.ndarray
+    constant: float = 0.0
+
+    @property
+    def norb(self) -> int:
+        return self.one_body_tensor.shape[0]
+
+    def _coulomb_mats(self):
+        aa, ab = np.asarray(self.diag_coulomb_mats, dtype=float)
+        return aa, ab, aa
+
+    def _linear_operator_(self, norb: int, nelec) -> LinearOperator:
+        """GPU counterpart of diagonal_coulomb_hamiltonian.py:67-97 (matvec = rmatvec)."""
+        from ffsim_gb300.contract import contract_diag_coulomb, num_op_sum_linop
+        from ffsim_gb300.linalg import eigh
+
+        assert isinstance(nelec, tuple)
+        d = _dim(norb, nelec)
+        eigs, vecs = eigh(np.asarray(self.one_body_tensor, dtype=complex))
+        num_linop = num_op_sum_linop(eigs, norb, nelec, orbital_rotation=vecs)
+        mats = self._coulomb_mats()
+        constant = float(self.constant)
+
+        def matvec(vec: torch.Tensor) -> torch.Tensor:
+            t = vec.contiguous()
+            if t.dtype not in (torch.complex64, torch.complex128):
+                t = t.to(torch.complex128)
+            out = num_linop @ t
+            out += contract_diag_coulomb(t, mats, norb, nelec)
+            if constant:
+                out += constant * t
+            return out
+
+        return LinearOperator((d, d), matvec, matvec)
+
+    def _diag_(self, norb: int, nelec) -> np.ndarray:
+        """Diagonal entries (diagonal_coulomb_hamiltonian.py:208-238), as a host
+        FP64 array like the reference's."""
+        from ffsim_gb300.contract import contract_diag_coulomb, contract_num_op_sum
+
+        assert isinstance(nelec, tuple)
+        ones = torch.ones(_dim(norb, nelec), dtype=torch.complex128, device="cuda")
+        h = np.real(np.diag(np.asarray(self.one_body_tensor))).astype(float)
+        out = contract_num_op_sum(ones, h, norb, nelec)
+        out += contract_diag_coulomb(ones, self._coulomb_mats(), norb, nelec)
+        return out.real.cpu().numpy() + float(self.constant)
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, DiagonalCoulombHamiltonian):
+            return NotImplemented
+        return (bool(np.isclose(self.constant, other.constant, rtol=rtol, atol=atol))
+                and bool(np.allclose(self.one_body_tensor, other.one_body_tensor, rtol=rtol, atol=atol))
+                and bool(np.allclose(self.diag_coulomb_mats, other.diag_coulomb_mats, rtol=rtol, atol=atol)))

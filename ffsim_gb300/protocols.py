@@ -39,6 +39,29 @@ def linear_operator(obj: Any, norb: int, nelec):
     raise TypeError(f"Object of type {type(obj)} has no _linear_operator_ method.")
 
 
+def diag(obj: Any, norb: int, nelec) -> np.ndarray:
+    """Diagonal entries of ``obj``'s operator
+    (python/ffsim/protocols/diagonal_protocol.py:42-50)."""
+    method = getattr(obj, "_diag_", None)
+    if method is not None:
+        return method(norb=norb, nelec=nelec)
+    raise TypeError(
+        f"Could not compute diagonal entries of object of type {type(obj)}.\n"
+        "The object did not have a _diag_ method that returned its diagonal entries."
+    )
+
+
+def trace(obj: Any, norb: int, nelec) -> float:
+    """Trace of ``obj``'s operator: its own ``_trace_`` or the sum of its
+    diagonal (python/ffsim/protocols/trace_protocol.py)."""
+    method = getattr(obj, "_trace_", None)
+    if method is not None:
+        return method(norb=norb, nelec=nelec)
+    if getattr(obj, "_diag_", None) is not None:
+        return float(np.sum(diag(obj, norb, nelec)))
+    raise TypeError(f"Could not compute trace of object of type {type(obj)}.")
+
+
 class LinearOperator:
     """A (dim x dim) operator acting on CUDA state vectors.
 

@@ -8,6 +8,11 @@ a two-body term t rotates the state from the running basis into U_t's basis
 exp(-i t J_t n n) (``ffgb_apply_diag_coulomb_evolution``).  The last basis and
 the global phase exp(-i T constant) close the evolution, so a step costs one
 orbital rotation and one diagonal evolution per two-body term.
+
+``simulate_trotter_diag_coulomb_split_op`` is the split-operator counterpart
+for a diagonal Coulomb Hamiltonian
+(python/ffsim/trotter/diagonal_coulomb_split_op.py:25-122): two terms, the
+Coulomb one applied in the occupation basis.
 """
 
 from __future__ import annotations
@@ -89,6 +94,47 @@ def simulate_trotter_double_factorized(vec, hamiltonian, time: float, *, norb: i
                 state = apply_diag_coulomb_evolution(state, dcm[k - 1], t, norb, nelec,
                                                      z_representation=z_rep, copy=False)
                 basis = u
+    state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
+    if hamiltonian.constant:
+        state.mul_(cmath.exp(-1j * time * hamiltonian.constant))
+    if state.data_ptr() != p.tensor.data_ptr():
+        p.tensor.reshape(-1).copy_(state)
+    return p.finish()
+
+
+def simulate_trotter_diag_coulomb_split_op(vec, hamiltonian, time: float, *, norb: int, nelec: tuple[int, int],
+                                           n_steps: int = 1, order: int = 0, copy: bool = True):
+    """Evolve ``vec`` by exp(-i time H) for a ``DiagonalCoulombHamiltonian`` with
+    the split-operator method (``ffsim.simulate_trotter_diag_coulomb_split_op``,
+    python/ffsim/trotter/diagonal_coulomb_split_op.py:25-122).
+
+    The step sequence has two terms.  The one-body term multiplies the running
+    orbital basis by exp(-i t h) on the host; the Coulomb term rotates the
+    state by that basis (``ffgb_apply_orbital_rotation``), applies
+    exp(-i t J n n) with (J_aa, J_ab, J_aa) in the occupation basis
+    (``ffgb_apply_diag_coulomb_evolution``) and resets the basis to the identity.
+    """
+    if order < 0:
+        raise ValueError(f"order must be non-negative, got {order}.")
+    if n_steps < 0:
+        raise ValueError(f"n_steps must be non-negative, got {n_steps}.")
+    p = prepare(vec, norb, nelec, copy=copy)
+    if n_steps == 0:
+        return p.finish()
+    state = p.tensor.reshape(-1)
+    one_body = np.asarray(hamiltonian.one_body_tensor, dtype=complex)
+    aa, ab = np.asarray(hamiltonian.diag_coulomb_mats, dtype=float)
+    eye = np.eye(norb, dtype=complex)
+    step = time / n_steps
+    basis = eye
+    for _ in range(n_steps):
+        for k, t in simulate_trotter_step_iterator(2, step, order):
+            if k == 0:
+                basis = _expm_hermitian(one_body, t) @ basis
+            else:
+                state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
+                state = apply_diag_coulomb_evolution(state, (aa, ab, aa), t, norb, nelec, copy=False)
+                basis = eye
     state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
     if hamiltonian.constant:
         state.mul_(cmath.exp(-1j * time * hamiltonian.constant))

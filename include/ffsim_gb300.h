@@ -126,7 +126,7 @@ int ffgb_apply_orbital_rotation(void* vec, int dtype, int norb, int n_alpha, int
  * NULL = none).  mat_aa/mat_ab/mat_bb: real norb*norb row-major, NULL = no
  * interaction of that type.  Replaces
  * apply_diag_coulomb_evolution_in_place_{num,z}_rep
- * (src/gates/diag_coulomb.rs:19-190) and the driver
+ * (src/gates/diag_coulomb.rs:19-190) and the Python wrapper
  * python/ffsim/gates/diag_coulomb.py:68-275.  Spinless: n_beta = -1. */
 int ffgb_apply_diag_coulomb_evolution(void* vec, int dtype, int norb, int n_alpha, int n_beta,
                                       const double* mat_aa, const double* mat_ab,

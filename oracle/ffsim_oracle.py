@@ -769,6 +769,71 @@ def simulate_trotter_double_factorized(vec, one_body_tensor, diag_coulomb_mats, 
 
 
 # ---------------------------------------------------------------------------
+# Diagonal Coulomb Hamiltonian (hamiltonians/diagonal_coulomb_hamiltonian.py:27-252)
+# and its split-operator Trotter evolution (trotter/diagonal_coulomb_split_op.py:25-122)
+# ---------------------------------------------------------------------------
+
+
+def diag_coulomb_hamiltonian_action(vec, one_body_tensor, diag_coulomb_mats, constant, norb, nelec):
+    """H |vec> for H = sum h_pq a+_ps a_qs + 1/2 sum J^{st}_pq n_ps n_qt + constant,
+    J^{aa} = J^{bb} = mats[0], J^{ab} = J^{ba} = mats[1]
+    (diagonal_coulomb_hamiltonian.py:67-97): the one-body part in the
+    eigenbasis of h, the Coulomb part diagonal in the occupation basis."""
+    vec = np.asarray(vec, dtype=complex)
+    eigs, vecs = scipy.linalg.eigh(one_body_tensor)
+    aa, ab = diag_coulomb_mats
+    out = constant * vec
+    out = out + num_op_sum_linop_matvec(eigs, norb, nelec, orbital_rotation=vecs)(vec)
+    return out + contract_diag_coulomb(vec, (aa, ab, aa), norb, nelec)
+
+
+def diag_coulomb_hamiltonian_diag(one_body_tensor, diag_coulomb_mats, constant, norb, nelec):
+    """Diagonal of H in the occupation basis (diagonal_coulomb_hamiltonian.py:208-238):
+    the one-body diagonal summed over occupied orbitals plus the Coulomb
+    energy of each (alpha, beta) pair of strings."""
+    na, nb = nelec
+    occ_a = np.zeros((math.comb(norb, na), norb))
+    occ_b = np.zeros((math.comb(norb, nb), norb))
+    for k, occ in enumerate(gen_occslst(norb, na)):
+        occ_a[k, occ] = 1.0
+    for k, occ in enumerate(gen_occslst(norb, nb)):
+        occ_b[k, occ] = 1.0
+    aa, ab = (np.asarray(m, dtype=float) for m in diag_coulomb_mats)
+    h = np.diag(one_body_tensor).real
+    ea = occ_a @ h + 0.5 * np.einsum("ip,pq,iq->i", occ_a, aa, occ_a)
+    eb = occ_b @ h + 0.5 * np.einsum("ip,pq,iq->i", occ_b, aa, occ_b)
+    return (ea[:, None] + eb[None, :] + occ_a @ ab @ occ_b.T + constant).reshape(-1)
+
+
+def simulate_trotter_diag_coulomb_split_op(vec, one_body_tensor, diag_coulomb_mats, constant, time,
+                                           norb, nelec, n_steps=1, order=0):
+    """diagonal_coulomb_split_op.py:25-122: a two-term step sequence; term 0
+    multiplies the running basis by exp(-i t h), term 1 rotates the state by
+    the running basis, applies exp(-i t J n n) with (J_aa, J_ab, J_aa) and
+    resets the basis to the identity."""
+    if order < 0 or n_steps < 0:
+        raise ValueError("order and n_steps must be non-negative")
+    vec = np.array(vec, dtype=complex, copy=True)
+    if n_steps == 0:
+        return vec
+    aa, ab = diag_coulomb_mats
+    step = time / n_steps
+    basis = np.eye(norb, dtype=complex)
+    for _ in range(n_steps):
+        for k, t in trotter_step_terms(2, step, order):
+            if k == 0:
+                basis = scipy.linalg.expm(-1j * t * one_body_tensor) @ basis
+            else:
+                vec = apply_orbital_rotation(vec, basis, norb, nelec, copy=False)
+                vec = apply_diag_coulomb_evolution(vec, (aa, ab, aa), t, norb, nelec, copy=False)
+                basis = np.eye(norb, dtype=complex)
+    vec = apply_orbital_rotation(vec, basis, norb, nelec, copy=False)
+    if constant:
+        vec = vec * np.exp(-1j * time * constant)
+    return vec
+
+
+# ---------------------------------------------------------------------------
 # UCJ (variational/ucj_spin_balanced.py:657-696) and parameter maps
 # ---------------------------------------------------------------------------
 

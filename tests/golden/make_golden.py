@@ -169,12 +169,25 @@ def install_stubs():
     giv = _load("ffsim.variational.givens", "variational/givens.py")
     # Trotter: the reference's step iterator and double-factorized evolution
     # (the Hamiltonian class is only a type annotation there)
-    _module("ffsim.hamiltonians", {"DoubleFactorizedHamiltonian": types.SimpleNamespace})
+    _module("ffsim.hamiltonians", {"DoubleFactorizedHamiltonian": types.SimpleNamespace,
+                                   "DiagonalCoulombHamiltonian": types.SimpleNamespace})
     _module("ffsim.trotter", is_pkg=True)
     _load("ffsim.trotter._util", "trotter/_util.py")
     tdf = _load("ffsim.trotter.double_factorized", "trotter/double_factorized.py")
+    tsplit = _load("ffsim.trotter.diagonal_coulomb_split_op", "trotter/diagonal_coulomb_split_op.py")
+    # the diagonal Coulomb Hamiltonian dataclass itself: its FermionOperator
+    # methods (Rust-backed) are never called, so the operator names are inert
+    for name in ("SupportsDiagonal", "SupportsFermionOperator", "SupportsLinearOperator"):
+        setattr(proto, name, type(name, (), {}))
+    _module("ffsim.operators", {k: None for k in ("FermionOperator", "cre_a", "cre_b", "des_a", "des_b")})
+    if "ffsim.states" not in sys.modules:
+        _module("ffsim.states", is_pkg=True)
+    _load("ffsim.states.dimensions", "states/dimensions.py")
+    dch = _load("ffsim.hamiltonians.diagonal_coulomb_hamiltonian", "hamiltonians/diagonal_coulomb_hamiltonian.py")
     return types.SimpleNamespace(
         simulate_trotter_double_factorized=tdf.simulate_trotter_double_factorized,
+        simulate_trotter_diag_coulomb_split_op=tsplit.simulate_trotter_diag_coulomb_split_op,
+        DiagonalCoulombHamiltonian=dch.DiagonalCoulombHamiltonian,
         apply_orbital_rotation=gor.apply_orbital_rotation,
         apply_diag_coulomb_evolution=gdc.apply_diag_coulomb_evolution,
         apply_num_op_sum_evolution=gnos.apply_num_op_sum_evolution,
@@ -445,6 +458,51 @@ def main():
         out[f"pairs{idx}_dcm"] = op.diag_coulomb_mats
         out[f"pairs{idx}_rots"] = op.orbital_rotations
         out[f"pairs{idx}_to"] = op.to_parameters(interaction_pairs=pairs)
+
+    # diagonal Coulomb Hamiltonian: linear operator and diagonal
+    # (hamiltonians/diagonal_coulomb_hamiltonian.py:67-97,208-238), and its
+    # split-operator Trotter evolution (trotter/diagonal_coulomb_split_op.py:25-122).
+    # Case 0 of the evolution is a 1-D Fermi-Hubbard chain with hopping 1,
+    # interaction 4, chemical potential 0.5 and nearest-neighbour repulsion 0.3.
+    rd = np.random.default_rng(20261208)
+    dch_cases = [(4, (2, 2)), (5, (3, 1)), (6, (2, 3)), (3, (0, 2))]
+    for idx, (norb, nelec) in enumerate(dch_cases):
+        g = rd.standard_normal((norb, norb)) + 1j * rd.standard_normal((norb, norb))
+        one_body = (g + g.conj().T) / 2
+        dcm = np.stack([orc.random_symmetric_normal(norb, seed=rd), orc.random_symmetric_normal(norb, seed=rd)])
+        const = float(rd.standard_normal())
+        ham = ref.DiagonalCoulombHamiltonian(one_body, dcm, constant=const)
+        vec = orc.random_state_vector(orc.dim(norb, nelec), seed=rd)
+        out[f"dch{idx}_h1"], out[f"dch{idx}_dcm"], out[f"dch{idx}_const"] = one_body, dcm, np.asarray(const)
+        out[f"dch{idx}_in"] = vec
+        out[f"dch{idx}_matvec"] = ham._linear_operator_(norb, nelec) @ vec
+        out[f"dch{idx}_diag"] = ham._diag_(norb, nelec)
+    out["dch_cases"] = np.asarray([[n, a, b] for n, (a, b) in dch_cases])
+
+    split_cases = [(4, (2, 2), 0.5, 3, 0), (4, (2, 1), 0.3, 2, 1), (5, (2, 2), 0.4, 1, 2), (3, (1, 2), 0.2, 2, 0)]
+    for idx, (norb, nelec, t, n_steps, order) in enumerate(split_cases):
+        if idx == 0:
+            one_body = np.zeros((norb, norb), dtype=complex)
+            for p in range(norb - 1):
+                one_body[p, p + 1] = one_body[p + 1, p] = -1.0
+            one_body -= 0.5 * np.eye(norb)
+            aa = np.zeros((norb, norb))
+            for p in range(norb - 1):
+                aa[p, p + 1] = aa[p + 1, p] = 0.3
+            ab = 4.0 * np.eye(norb) + aa
+            dcm, const = np.stack([aa, ab]), 0.0
+        else:
+            g = rd.standard_normal((norb, norb)) + 1j * rd.standard_normal((norb, norb))
+            one_body = (g + g.conj().T) / 2
+            dcm = np.stack([orc.random_symmetric_normal(norb, seed=rd), orc.random_symmetric_normal(norb, seed=rd)])
+            const = float(rd.standard_normal())
+        ham = ref.DiagonalCoulombHamiltonian(one_body, dcm, constant=const)
+        vec = orc.random_state_vector(orc.dim(norb, nelec), seed=rd)
+        out[f"split{idx}_h1"], out[f"split{idx}_dcm"], out[f"split{idx}_const"] = one_body, dcm, np.asarray(const)
+        out[f"split{idx}_in"] = vec
+        out[f"split{idx}_out"] = ref.simulate_trotter_diag_coulomb_split_op(
+            vec, ham, t, norb=norb, nelec=nelec, n_steps=n_steps, order=order)
+    out["split_cases"] = np.asarray([[n, a, b, t, s, o] for n, (a, b), t, s, o in split_cases])
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
