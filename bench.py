@@ -311,12 +311,12 @@ def run_ops(args) -> None:
     ops["ucj_spin_unbalanced_apply_L2"] = (3 * 4 * S + 2 * 2 * S, on_stream(
         lambda: f.apply_unitary(v, ucju, norb, nelec, copy=False)))
     ops["rdm1"] = (S, on_stream(lambda: f.rdms(v, norb, nelec)))
-    # split-operator step of a Hubbard chain (hopping 1, U 4): two rotations
-    # (the running basis, then the identity that closes the evolution) and one
-    # diagonal evolution
+    # split-operator step of a Hubbard chain (hopping 1, U 4): one rotation by
+    # the banded near-identity exp(-i 0.1 h) and one diagonal evolution (the
+    # closing rotation by the identity is skipped)
     hop = np.diag(-np.ones(norb - 1), 1)
     hub = f.DiagonalCoulombHamiltonian(hop + hop.T, np.stack([np.zeros((norb, norb)), 4.0 * np.eye(norb)]))
-    ops[f"trotter_split_op_step_norb{norb}"] = (2 * 4 * S + 2 * S, on_stream(
+    ops[f"trotter_split_op_step_norb{norb}"] = (4 * S + 2 * S, on_stream(
         lambda: f.simulate_trotter_diag_coulomb_split_op(v, hub, 0.1, norb=norb, nelec=nelec, copy=False)))
     if norb == NORB:
         n12, ne12 = 12, (6, 6)

@@ -11,21 +11,19 @@ namespace {
 
 inline cd at(const std::vector<cd>& m, int n, int r, int c) { return m[(size_t)r * n + c]; }
 
-// One-sided (Hestenes) Jacobi SVD of a square n x n matrix A (row-major):
-// A = U diag(S) W^H, S descending.  Columns of U belonging to zero singular
-// values are completed to an orthonormal basis.
-void svd_jacobi(int n, const std::vector<cd>& A, std::vector<cd>& U, std::vector<double>& S,
-                std::vector<cd>& W) {
-  std::vector<cd> G = A;
-  W.assign((size_t)n * n, cd(0));
-  for (int i = 0; i < n; ++i) W[(size_t)i * n + i] = 1.0;
+// One-sided (Hestenes) Jacobi sweeps on the columns of G (m x n, row-major):
+// rotates column pairs until they are mutually orthogonal, accumulating the
+// rotations into Y (n x n, G_out = G_in Y when Y starts as the identity).
+// Accuracy is relative to each column's norm, so singular values spanning
+// many orders of magnitude are all resolved.
+void jacobi_columns(int m, int n, std::vector<cd>& G, std::vector<cd>& Y) {
   for (int sweep = 0; sweep < 80; ++sweep) {
     double off = 0.0;
     for (int p = 0; p < n; ++p) {
       for (int q = p + 1; q < n; ++q) {
         double alpha = 0, beta = 0;
         cd gamma = 0;
-        for (int k = 0; k < n; ++k) {
+        for (int k = 0; k < m; ++k) {
           cd gp = G[(size_t)k * n + p], gq = G[(size_t)k * n + q];
           alpha += std::norm(gp);
           beta += std::norm(gq);
@@ -38,18 +36,31 @@ void svd_jacobi(int n, const std::vector<cd>& A, std::vector<cd>& U, std::vector
         double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
         double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
         cd e = std::conj(gamma / ag);  // e^{-i theta}
-        for (int k = 0; k < n; ++k) {
+        for (int k = 0; k < m; ++k) {
           cd gp = G[(size_t)k * n + p], gq = G[(size_t)k * n + q];
           G[(size_t)k * n + p] = c * gp - s * e * gq;
           G[(size_t)k * n + q] = s * gp + c * e * gq;
-          cd wp = W[(size_t)k * n + p], wq = W[(size_t)k * n + q];
-          W[(size_t)k * n + p] = c * wp - s * e * wq;
-          W[(size_t)k * n + q] = s * wp + c * e * wq;
+        }
+        for (int k = 0; k < n; ++k) {
+          cd wp = Y[(size_t)k * n + p], wq = Y[(size_t)k * n + q];
+          Y[(size_t)k * n + p] = c * wp - s * e * wq;
+          Y[(size_t)k * n + q] = s * wp + c * e * wq;
         }
       }
     }
     if (off < 1e-16) break;
   }
+}
+
+// One-sided (Hestenes) Jacobi SVD of a square n x n matrix A (row-major):
+// A = U diag(S) W^H, S descending.  Columns of U belonging to zero singular
+// values are completed to an orthonormal basis.
+void svd_jacobi(int n, const std::vector<cd>& A, std::vector<cd>& U, std::vector<double>& S,
+                std::vector<cd>& W) {
+  std::vector<cd> G = A;
+  W.assign((size_t)n * n, cd(0));
+  for (int i = 0; i < n; ++i) W[(size_t)i * n + i] = 1.0;
+  jacobi_columns(n, n, G, W);
   S.assign(n, 0.0);
   for (int p = 0; p < n; ++p) {
     double ss = 0;
@@ -291,6 +302,59 @@ bool csd(int n, int h, const cd* Vp, std::vector<cd>& A1, std::vector<cd>& A2,
   std::vector<cd> U1, W1;
   std::vector<double> cs;
   svd_jacobi(h, V11, U1, cs, W1);
+  // Cosines within rounding of 1 hide their sines (c = 1 - s^2/2), so V11's
+  // right singular vectors are arbitrary inside that cluster; banded unitaries
+  // (short-time evolutions, lattice hoppings) have many such sines between
+  // 1e-16 and 1e-2.  For the columns with c > 1/sqrt(2) the right vectors are
+  // re-resolved from V21 (Jacobi on V21 W_L, whose column norms are the sines)
+  // and U1, c recomputed from V11 W_L, whose columns are then orthogonal.
+  int nl = 0;
+  while (nl < h && cs[nl] > 0.70710678118654752) ++nl;  // cs is descending
+  if (nl > 1) {
+    std::vector<cd> ZL((size_t)q * nl, cd(0)), Y((size_t)nl * nl, cd(0));
+    for (int r = 0; r < q; ++r)
+      for (int c = 0; c < nl; ++c) {
+        cd acc = 0;
+        for (int k = 0; k < h; ++k) acc += V21[(size_t)r * h + k] * W1[(size_t)k * h + c];
+        ZL[(size_t)r * nl + c] = acc;
+      }
+    for (int i = 0; i < nl; ++i) Y[(size_t)i * nl + i] = 1.0;
+    jacobi_columns(q, nl, ZL, Y);
+    std::vector<cd> WL((size_t)h * nl, cd(0));
+    for (int r = 0; r < h; ++r)
+      for (int c = 0; c < nl; ++c) {
+        cd acc = 0;
+        for (int k = 0; k < nl; ++k) acc += W1[(size_t)r * h + k] * Y[(size_t)k * nl + c];
+        WL[(size_t)r * nl + c] = acc;
+      }
+    for (int r = 0; r < h; ++r)
+      for (int c = 0; c < nl; ++c) W1[(size_t)r * h + c] = WL[(size_t)r * nl + c];
+    for (int c = 0; c < nl; ++c) {
+      std::vector<cd> x(h, cd(0));
+      for (int r = 0; r < h; ++r)
+        for (int k = 0; k < h; ++k) x[r] += V11[(size_t)r * h + k] * W1[(size_t)k * h + c];
+      double nx = 0;
+      for (int r = 0; r < h; ++r) nx += std::norm(x[r]);
+      nx = std::sqrt(nx);
+      cs[c] = nx;
+      for (int r = 0; r < h; ++r) U1[(size_t)r * h + c] = x[r] / nx;
+    }
+    // two Gram-Schmidt passes keep U1 unitary to rounding (the columns are
+    // orthogonal in exact arithmetic, and their norms are at least 1/sqrt(2))
+    for (int pass = 0; pass < 2; ++pass)
+      for (int c = 0; c < nl; ++c) {
+        for (int o = 0; o < h; ++o) {
+          if (o == c || (o < nl && o > c)) continue;
+          cd d = 0;
+          for (int r = 0; r < h; ++r) d += std::conj(U1[(size_t)r * h + o]) * U1[(size_t)r * h + c];
+          for (int r = 0; r < h; ++r) U1[(size_t)r * h + c] -= d * U1[(size_t)r * h + o];
+        }
+        double nu = 0;
+        for (int r = 0; r < h; ++r) nu += std::norm(U1[(size_t)r * h + c]);
+        nu = std::sqrt(nu);
+        for (int r = 0; r < h; ++r) U1[(size_t)r * h + c] /= nu;
+      }
+  }
   // Z = V21 W1 (q x h)
   std::vector<cd> Z((size_t)q * h, cd(0));
   for (int r = 0; r < q; ++r)
@@ -299,6 +363,30 @@ bool csd(int n, int h, const cd* Vp, std::vector<cd>& A1, std::vector<cd>& A2,
       for (int k = 0; k < h; ++k) acc += V21[(size_t)r * h + k] * W1[(size_t)k * h + c];
       Z[(size_t)r * h + c] = acc;
     }
+  // QR in order of descending column norm (the sines): a column whose norm is
+  // at rounding level has an arbitrary direction, and taken early its
+  // reflection would move part of a larger later column off the diagonal of R.
+  // The pairs (i, h + i) are independent, so permuting the index i of U1, W1
+  // and the cosines together leaves the factorization intact.
+  {
+    std::vector<double> zn(h, 0.0);
+    for (int c = 0; c < h; ++c)
+      for (int r = 0; r < q; ++r) zn[c] += std::norm(Z[(size_t)r * h + c]);
+    std::vector<int> order(h);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return zn[a] > zn[b]; });
+    auto permute_cols = [&](std::vector<cd>& M, int rows) {
+      std::vector<cd> T(M);
+      for (int r = 0; r < rows; ++r)
+        for (int c = 0; c < h; ++c) M[(size_t)r * h + c] = T[(size_t)r * h + order[c]];
+    };
+    permute_cols(Z, q);
+    permute_cols(W1, h);
+    permute_cols(U1, h);
+    std::vector<double> cs2(h);
+    for (int c = 0; c < h; ++c) cs2[c] = cs[order[c]];
+    cs.swap(cs2);
+  }
   std::vector<cd> Q, R;
   householder_qr(q, h, Z, Q, R);
   std::vector<cd> U2 = Q;

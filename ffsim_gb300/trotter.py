@@ -124,18 +124,20 @@ def simulate_trotter_diag_coulomb_split_op(vec, hamiltonian, time: float, *, nor
     state = p.tensor.reshape(-1)
     one_body = np.asarray(hamiltonian.one_body_tensor, dtype=complex)
     aa, ab = np.asarray(hamiltonian.diag_coulomb_mats, dtype=float)
-    eye = np.eye(norb, dtype=complex)
     step = time / n_steps
-    basis = eye
+    basis = None  # the identity: a rotation by it is skipped (it changes no amplitude)
     for _ in range(n_steps):
         for k, t in simulate_trotter_step_iterator(2, step, order):
             if k == 0:
-                basis = _expm_hermitian(one_body, t) @ basis
+                u = _expm_hermitian(one_body, t)
+                basis = u if basis is None else u @ basis
             else:
-                state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
+                if basis is not None:
+                    state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
                 state = apply_diag_coulomb_evolution(state, (aa, ab, aa), t, norb, nelec, copy=False)
-                basis = eye
-    state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
+                basis = None
+    if basis is not None:
+        state = apply_orbital_rotation(state, basis, norb, nelec, copy=False)
     if hamiltonian.constant:
         state.mul_(cmath.exp(-1j * time * hamiltonian.constant))
     if state.data_ptr() != p.tensor.data_ptr():

@@ -160,3 +160,39 @@ def test_gpu_split_op_stage_path(cuda):
     # the evolution nearly conserves the energy (the oracle's drift is 6.7e-5)
     lin = f.linear_operator(ham, norb, nelec)
     assert abs(lin.expectation(outs[torch.complex128]) - lin.expectation(v)) < 1e-3
+
+
+def test_split_op_host_sequence(golden, monkeypatch):
+    """The host-side step logic of the GPU evolution (basis products, skipped
+    identity rotations, the closing phase) with the two gate entry points
+    replaced by the oracle's, against the reference's golden vectors."""
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _state
+    from ffsim_gb300 import trotter as tr
+
+    def rot(state, mat, norb, nelec, copy=False):
+        return torch.from_numpy(o.apply_orbital_rotation(state.numpy(), mat, norb, nelec))
+
+    def evo(state, mat, t, norb, nelec, copy=False):
+        return torch.from_numpy(o.apply_diag_coulomb_evolution(state.numpy(), mat, t, norb, nelec))
+
+    def prep(vec, norb, nelec, *, copy):
+        arr = np.array(vec, dtype=complex)
+        return _state.Prepared(torch.from_numpy(arr), arr.shape, True)
+
+    calls = []
+    monkeypatch.setattr(tr, "apply_orbital_rotation", lambda *a, **k: calls.append("rot") or rot(*a, **k))
+    monkeypatch.setattr(tr, "apply_diag_coulomb_evolution", evo)
+    monkeypatch.setattr(tr, "prepare", prep)
+    for idx, (n, a, b, t, steps, order) in enumerate(golden["split_cases"]):
+        n, ne = int(n), (int(a), int(b))
+        h1, dcm, c = _dch(golden, "split", idx)
+        ham = f.DiagonalCoulombHamiltonian(h1, dcm, constant=c)
+        calls.clear()
+        out = tr.simulate_trotter_diag_coulomb_split_op(golden[f"split{idx}_in"], ham, float(t), norb=n, nelec=ne,
+                                                        n_steps=int(steps), order=int(order))
+        np.testing.assert_allclose(np.asarray(out).reshape(-1), golden[f"split{idx}_out"], atol=1e-12)
+        if int(order) == 0:  # one rotation per step; the closing identity is skipped
+            assert len(calls) == int(steps)

@@ -311,3 +311,26 @@ def test_nested_cosine_sine_plans(cuda, norb, nelec):
     e64 = f.lucj_energy(ucj, ham, norb, nelec, dtype=torch.complex64)
     e128 = f.lucj_energy(ucj, ham, norb, nelec, dtype=torch.complex128)
     assert abs(e64 - e128) < 1e-5
+
+
+@pytest.mark.parametrize("norb, nelec", [(10, (3, 4)), (13, (3, 3)), (16, (3, 2)), (17, (2, 3)), (18, (2, 2))])
+def test_banded_and_near_identity_rotations(cuda, norb, nelec):
+    """Short-time hopping evolutions exp(-i t h) (banded, near the identity) and
+    a permutation: the cosine-sine plans resolve their small sines, on the
+    complex64 stage kernels and the complex128 path, against the oracle."""
+    import scipy.linalg
+
+    import ffsim_gb300 as f
+
+    rng = np.random.default_rng(norb * 3 + 1)
+    d = math.comb(norb, nelec[0]) * math.comb(norb, nelec[1])
+    vec = o.random_state_vector(d, seed=rng)
+    hop = np.diag(-np.ones(norb - 1), 1)
+    mats = [scipy.linalg.expm(-1j * t * (hop + hop.T)) for t in (1e-3, 0.1, 1.0)]
+    mats.append(np.roll(np.eye(norb), 5, axis=0).astype(complex))
+    for u in mats:
+        ref = o.apply_orbital_rotation(vec, (u, u.conj()), norb, nelec)
+        out = f.apply_orbital_rotation(_t(vec, torch.complex64), (u, u.conj()), norb, nelec)
+        np.testing.assert_allclose(_n(out), ref, atol=TOL64)
+        out = f.apply_orbital_rotation(_t(vec, torch.complex128), (u, u.conj()), norb, nelec)
+        np.testing.assert_allclose(_n(out), ref, atol=TOL128)

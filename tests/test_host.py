@@ -117,8 +117,7 @@ def test_stage_sequence_matches_oracle(norb, nocc, n_stages):
 
 
 def test_stage_sequence_special_matrices():
-    """Block-diagonal, permutation and identity unitaries: the three-window form,
-    or the generic network where the cosine-sine form degenerates."""
+    """Block-diagonal, permutation and identity unitaries take the three-window form."""
     for norb, nocc in [(9, 3), (10, 4), (12, 2)]:
         blk = np.zeros((norb, norb), dtype=complex)
         blk[:8, :8] = o.random_unitary(8, seed=4)
@@ -128,9 +127,8 @@ def test_stage_sequence_special_matrices():
             plan = _plan(u, True)
             assert plan["err"] < 1e-10
             vec = o.random_state_vector(math.comb(norb, nocc), seed=6)
-            apply = pe.apply_ops if plan["kind"] == 3 else pe.apply_plan
-            assert plan["kind"] == 1 or len(plan["ops"]) == 3
-            np.testing.assert_allclose(apply(plan, vec, norb, nocc),
+            assert plan["kind"] == 3 and len(plan["ops"]) == 3
+            np.testing.assert_allclose(pe.apply_ops(plan, vec, norb, nocc),
                                        o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-11)
 
 
@@ -150,6 +148,31 @@ def test_plan_special_matrices():
                 vec = o.random_state_vector(math.comb(norb, nocc), seed=3)
                 np.testing.assert_allclose(pe.apply_plan(plan, vec, norb, nocc),
                                            o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-12)
+
+
+def _hopping_evolution(norb, t, band, seed):
+    """exp(-i t h) for a random Hermitian h with the given bandwidth: a banded,
+    near-identity unitary for small t (short-time evolutions, lattice models)."""
+    import scipy.linalg
+
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((norb, norb)) + 1j * rng.standard_normal((norb, norb))
+    h = np.triu(np.tril(g + g.conj().T, band), -band)
+    return scipy.linalg.expm(-1j * t * h)
+
+
+@pytest.mark.parametrize("norb, nocc", [(9, 3), (12, 4), (13, 3), (16, 2), (17, 2), (18, 2)])
+@pytest.mark.parametrize("t, band", [(1e-6, 1), (0.01, 1), (0.1, 1), (1.0, 1), (0.3, 2), (1e-3, 17)])
+def test_stage_sequence_banded_and_near_identity(norb, nocc, t, band):
+    """Banded and near-identity unitaries stay on the stage sequence: cosines
+    within rounding of 1 hide their sines from the diagonal block, so the
+    cosine-sine split resolves them from the off-diagonal block."""
+    u = _hopping_evolution(norb, t, band, seed=norb * 100 + band)
+    plan = _plan(u, True)
+    assert plan["kind"] == 3 and plan["err"] < 1e-10
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=9)
+    np.testing.assert_allclose(pe.apply_ops(plan, vec, norb, nocc),
+                               o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-11)
 
 
 def test_scratch_sizes():
