@@ -28,8 +28,17 @@ and lines it follows (paths are relative to the ffsim project root):
 * linear operators       python/ffsim/contract/diag_coulomb.py:195-272,
                          python/ffsim/contract/num_op_sum.py:75-131,
                          python/ffsim/hamiltonians/double_factorized_hamiltonian.py:244-275
-* UCJ apply_unitary      python/ffsim/variational/ucj_spin_balanced.py:657-696
+* UCJ apply_unitary      python/ffsim/variational/ucj_spin_balanced.py:657-696,
+                         ucj_spin_unbalanced.py, ucj_spinless.py
 * parameter maps         python/ffsim/linalg/util.py:93-124,212-232
+* one-body operators,    python/ffsim/contract/one_body.py:24-90,
+  1- and 2-RDMs          python/ffsim/states/rdm.py:73-274
+* molecular Hamiltonian  python/ffsim/hamiltonians/molecular_hamiltonian.py:24-173
+* Trotter evolution      python/ffsim/trotter/double_factorized.py:25-127,
+                         python/ffsim/trotter/_util.py:18-60,
+                         python/ffsim/trotter/diagonal_coulomb_split_op.py:25-122
+* diagonal Coulomb       python/ffsim/hamiltonians/diagonal_coulomb_hamiltonian.py:67-97,208-238
+  Hamiltonian
 * random inputs          python/ffsim/random/random.py:24-47,84-106,549-560,563-665
 
 Parity pins: tests/golden/make_golden.py runs the reference's own Python
