@@ -54,6 +54,47 @@ class DoubleFactorizedHamiltonian:
         return DoubleFactorizedHamiltonian(self.one_body_tensor - ob, self.diag_coulomb_mats,
                                            self.orbital_rotations, self.constant - c, False)
 
+    @staticmethod
+    def from_molecular_hamiltonian(hamiltonian: "MolecularHamiltonian", *, z_representation: bool = False,
+                                   tol: float = 1e-8, max_vecs: int | None = None, optimize: bool = False,
+                                   method: str = "L-BFGS-B", callback=None, options: dict | None = None,
+                                   diag_coulomb_indices=None, cholesky: bool = True) -> "DoubleFactorizedHamiltonian":
+        """Double-factorize a molecular Hamiltonian (double_factorized_hamiltonian.py:140-222):
+        normal ordering moves -1/2 sum_r h_prrq into the one-body tensor, and
+        the two-body tensor is factored by ``linalg.double_factorized``."""
+        from ffsim_gb300.linalg import double_factorized
+
+        one_body = hamiltonian.one_body_tensor - 0.5 * np.einsum("prrq", hamiltonian.two_body_tensor)
+        mats, rots = double_factorized(hamiltonian.two_body_tensor, tol=tol, max_vecs=max_vecs, optimize=optimize,
+                                       method=method, callback=callback, options=options,
+                                       diag_coulomb_indices=diag_coulomb_indices, cholesky=cholesky)
+        df = DoubleFactorizedHamiltonian(one_body, mats, rots, constant=hamiltonian.constant)
+        return df.to_z_representation() if z_representation else df
+
+    def to_molecular_hamiltonian(self) -> "MolecularHamiltonian":
+        """The molecular Hamiltonian with the same operator
+        (double_factorized_hamiltonian.py:224-242)."""
+        df = self.to_number_representation()
+        u = np.asarray(df.orbital_rotations)
+        two_body = np.einsum("kij,kpi,kqi,krj,ksj->pqrs", df.diag_coulomb_mats, u, u.conj(), u, u.conj(),
+                             optimize=True)
+        one_body = df.one_body_tensor + 0.5 * np.einsum("prrq", two_body)
+        return MolecularHamiltonian(one_body, two_body, constant=df.constant)
+
+    def _diag_(self, norb: int, nelec) -> np.ndarray:
+        """Diagonal entries, through the molecular form (double_factorized_hamiltonian.py:277-280)."""
+        return self.to_molecular_hamiltonian()._diag_(norb, nelec)
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, DoubleFactorizedHamiltonian):
+            return NotImplemented
+        return (self.z_representation == other.z_representation
+                and bool(np.isclose(self.constant, other.constant, rtol=rtol, atol=atol))
+                and all(bool(np.allclose(a, b, rtol=rtol, atol=atol)) for a, b in [
+                    (self.one_body_tensor, other.one_body_tensor),
+                    (self.diag_coulomb_mats, other.diag_coulomb_mats),
+                    (self.orbital_rotations, other.orbital_rotations)]))
+
     def _linear_operator_(self, norb: int, nelec) -> LinearOperator:
         """GPU counterpart of double_factorized_hamiltonian.py:244-275 (matvec = rmatvec),
         with a fused FP64 ``expectation``."""
@@ -170,6 +211,30 @@ class MolecularHamiltonian:
     def _linear_operator_(self, norb: int, nelec) -> LinearOperator:
         assert isinstance(nelec, tuple)
         return self.to_double_factorized()._linear_operator_(norb, nelec)
+
+    def rotated(self, orbital_rotation: np.ndarray) -> "MolecularHamiltonian":
+        """U H U^dag as a molecular Hamiltonian (molecular_hamiltonian.py:119-144)."""
+        from ffsim_gb300.linalg import rotate_one_body_tensor, rotate_two_body_tensor
+
+        return MolecularHamiltonian(rotate_one_body_tensor(self.one_body_tensor, orbital_rotation),
+                                    rotate_two_body_tensor(self.two_body_tensor, orbital_rotation, orbital_rotation),
+                                    constant=self.constant)
+
+    def _diag_(self, norb: int, nelec) -> np.ndarray:
+        """Diagonal entries for real tensors (molecular_hamiltonian.py:175-188).
+
+        In the occupation basis only the Coulomb integrals J_pr = h_pprr and,
+        within a spin, the exchange integrals K_pr = h_prrp survive, so the
+        diagonal is that of the diagonal Coulomb Hamiltonian with
+        J^aa = J - K and J^ab = J, computed on the GPU."""
+        if np.iscomplexobj(self.two_body_tensor) or np.iscomplexobj(self.one_body_tensor):
+            raise NotImplementedError("Computing diagonal of complex molecular Hamiltonian is not yet supported.")
+        h = np.asarray(self.two_body_tensor, dtype=float)
+        coulomb = np.einsum("pprr->pr", h)
+        exchange = np.einsum("prrp->pr", h)
+        dch = DiagonalCoulombHamiltonian(self.one_body_tensor, np.stack([coulomb - exchange, coulomb]),
+                                         constant=self.constant)
+        return dch._diag_(norb, nelec)
 
     def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
         if not isinstance(other, MolecularHamiltonian):

@@ -1,5 +1,6 @@
 """Host linear algebra on the path (FP64): Givens decomposition, Hermitian
-eigendecomposition and the UCJ parameter maps."""
+eigendecomposition, the UCJ parameter maps, the double factorization of a
+two-body tensor and tensor rotations."""
 
 from __future__ import annotations
 
@@ -91,3 +92,102 @@ def is_unitary(mat: np.ndarray, *, rtol: float = 1e-5, atol: float = 1e-8) -> bo
 def is_real_symmetric(mat: np.ndarray, *, rtol: float = 1e-5, atol: float = 1e-8) -> bool:
     mat = np.asarray(mat)
     return bool(np.all(np.isreal(mat)) and np.allclose(mat, mat.T, rtol=rtol, atol=atol))
+
+
+def modified_cholesky(mat: np.ndarray, *, tol: float = 1e-8, max_vecs: int | None = None) -> np.ndarray:
+    r"""Pivoted ("modified") Cholesky factorization :math:`M \approx \sum_i v_i v_i^\dagger`
+    of a positive semidefinite matrix (python/ffsim/linalg/double_factorized_decomposition.py:70-131;
+    Motta and Zhang, arXiv:1711.02242).
+
+    Each step pivots on the largest remaining diagonal error, takes that column
+    of M minus the part the earlier vectors already explain, and scales it by
+    the error's square root.  It stops when the largest error falls below
+    ``tol`` or after ``max_vecs`` vectors; the vectors are the returned columns.
+    """
+    mat = np.asarray(mat)
+    n = mat.shape[0]
+    if not n:
+        return np.empty((0, 0))
+    if max_vecs is None:
+        max_vecs = n
+    vecs = np.zeros((n, max_vecs), dtype=mat.dtype)
+    err = np.real(np.diagonal(mat)).copy()
+    k = 0
+    while k < max_vecs:
+        piv = int(np.argmax(err))
+        e = err[piv]
+        if e < tol:
+            break
+        col = mat[:, piv].copy()
+        if k:
+            col -= vecs[:, :k] @ vecs[piv, :k].conj()
+        vecs[:, k] = col / np.sqrt(e)
+        err -= np.abs(vecs[:, k]) ** 2
+        k += 1
+    return vecs[:, :k]
+
+
+def double_factorized(two_body_tensor: np.ndarray, *, tol: float = 1e-8, max_vecs: int | None = None,
+                      optimize: bool = False, method: str = "L-BFGS-B", callback=None, options: dict | None = None,
+                      diag_coulomb_indices=None, return_optimize_result: bool = False, cholesky: bool = True):
+    r"""Double factorization :math:`h_{pqrs} = \sum_t \sum_{ij} U^t_{pi} U^{t*}_{qi} J^t_{ij} U^t_{rj} U^{t*}_{sj}`
+    of a real two-body tensor (python/ffsim/linalg/double_factorized_decomposition.py:145-309).
+
+    The (norb², norb²) matrix h[(p,q),(r,s)] is factored as a sum of outer
+    products of vectors L_t (pivoted Cholesky, or its truncated
+    eigendecomposition with ``cholesky=False``).  Each L_t, reshaped to a
+    norb × norb matrix, is diagonalised, L_t = U_t diag(μ) U_t^dag, giving
+    J_t = μ μ^T (times the eigenvalue on the eigendecomposition path).
+    ``tol`` bounds the largest element error (Cholesky) or the discarded
+    eigenvalue weight; ``max_vecs`` (default norb(norb+1)/2) caps the terms.
+    Returns (diag_coulomb_mats, orbital_rotations).  The compressed form
+    (``optimize=True``) fits the factors by gradient descent on a JAX loss in
+    the reference and is not available here.
+    """
+    two_body_tensor = np.asarray(two_body_tensor)
+    if np.iscomplexobj(two_body_tensor):
+        raise ValueError("Double factorization of complex two-body tensors is not supported.")
+    norb = two_body_tensor.shape[0]
+    if not norb:
+        return np.empty((0, 0, 0)), np.empty((0, 0, 0))
+    if max_vecs is None:
+        max_vecs = norb * (norb + 1) // 2
+    if optimize:
+        raise NotImplementedError("the compressed (optimize=True) double factorization is not available")
+    flat = two_body_tensor.reshape(norb * norb, norb * norb)
+    if cholesky:
+        vecs = modified_cholesky(flat, tol=tol, max_vecs=max_vecs)
+        mats = vecs.T.reshape(-1, norb, norb)
+        mu, rots = np.linalg.eigh(mats)
+        return mu[:, :, None] * mu[:, None, :], rots
+    w, v = scipy.linalg.eigh(flat)
+    order = np.argsort(np.abs(w))[::-1]
+    w, v = w[order], v[:, order]
+    n_drop = int(np.searchsorted(np.cumsum(np.abs(w[::-1])), tol))
+    keep = min(max_vecs, len(w) - n_drop)
+    w, v = w[:keep], v[:, :keep]
+    mu, rots = np.linalg.eigh(v.T.reshape(-1, norb, norb))
+    return w[:, None, None] * mu[:, :, None] * mu[:, None, :], rots
+
+
+def rotate_one_body_tensor(tensor: np.ndarray, orbital_rotation: np.ndarray | None) -> np.ndarray:
+    r""":math:`\sum_{ab} U_{Aa} \overline{U_{Bb}} t_{ab}`, the one-body tensor of
+    :math:`\mathcal{U} H \mathcal{U}^\dagger` (python/ffsim/linalg/util.py:743-803)."""
+    if orbital_rotation is None:
+        return tensor
+    u = np.asarray(orbital_rotation)
+    return u @ np.asarray(tensor) @ u.conj().T
+
+
+def rotate_two_body_tensor(tensor: np.ndarray, orbital_rotation_1: np.ndarray | None,
+                           orbital_rotation_2: np.ndarray | None) -> np.ndarray:
+    r""":math:`\sum_{abcd} U_{Aa} \overline{U_{Bb}} V_{Cc} \overline{V_{Dd}} t_{abcd}`
+    (python/ffsim/linalg/util.py:813-900); ``None`` is the identity."""
+    t = np.asarray(tensor)
+    if orbital_rotation_1 is not None:
+        u = np.asarray(orbital_rotation_1)
+        t = np.einsum("abcd,Aa,Bb->ABcd", t, u, u.conj(), optimize=True)
+    if orbital_rotation_2 is not None:
+        v = np.asarray(orbital_rotation_2)
+        t = np.einsum("abcd,Cc,Dd->abCD", t, v, v.conj(), optimize=True)
+    return t

@@ -184,7 +184,22 @@ def install_stubs():
         _module("ffsim.states", is_pkg=True)
     _load("ffsim.states.dimensions", "states/dimensions.py")
     dch = _load("ffsim.hamiltonians.diagonal_coulomb_hamiltonian", "hamiltonians/diagonal_coulomb_hamiltonian.py")
+    # the molecular and double-factorized Hamiltonian dataclasses and the
+    # explicit double factorization; pyscf's make_hdiag and the two-body
+    # contraction (pyscf-backed) are never called
+    _module("pyscf.fci.direct_nosym", {"make_hdiag": None})
+    _module("pyscf.fci.direct_uhf", {"make_hdiag": None})
+    _module("ffsim.contract.two_body", {"two_body_linop": None, "two_body_linop_unrestricted": None})
+    sys.modules["ffsim.operators"].FermionAction = None
+    ldf = _load("ffsim.linalg.double_factorized_decomposition", "linalg/double_factorized_decomposition.py")
+    sys.modules["ffsim.linalg"].double_factorized = ldf.double_factorized
+    mol = _load("ffsim.hamiltonians.molecular_hamiltonian", "hamiltonians/molecular_hamiltonian.py")
+    dfh = _load("ffsim.hamiltonians.double_factorized_hamiltonian", "hamiltonians/double_factorized_hamiltonian.py")
     return types.SimpleNamespace(
+        modified_cholesky=ldf.modified_cholesky,
+        double_factorized=ldf.double_factorized,
+        MolecularHamiltonian=mol.MolecularHamiltonian,
+        DoubleFactorizedHamiltonian=dfh.DoubleFactorizedHamiltonian,
         simulate_trotter_double_factorized=tdf.simulate_trotter_double_factorized,
         simulate_trotter_diag_coulomb_split_op=tsplit.simulate_trotter_diag_coulomb_split_op,
         DiagonalCoulombHamiltonian=dch.DiagonalCoulombHamiltonian,
@@ -503,6 +518,40 @@ def main():
         out[f"split{idx}_out"] = ref.simulate_trotter_diag_coulomb_split_op(
             vec, ham, t, norb=norb, nelec=nelec, n_steps=n_steps, order=order)
     out["split_cases"] = np.asarray([[n, a, b, t, s, o] for n, (a, b), t, s, o in split_cases])
+
+    # double factorization of molecular two-body tensors
+    # (linalg/double_factorized_decomposition.py:70-309), the conversions of
+    # hamiltonians/double_factorized_hamiltonian.py:140-242 and
+    # MolecularHamiltonian.rotated (molecular_hamiltonian.py:119-144).  The
+    # tensors are sums of L (x) L over real symmetric L: positive
+    # semidefinite with the symmetries of molecular integrals.
+    rm = np.random.default_rng(20261209)
+    mol_norbs = [3, 4, 5]
+    for idx, norb in enumerate(mol_norbs):
+        g = rm.standard_normal((norb, norb))
+        one_body = (g + g.T) / 2
+        ls = [(x + x.T) / 2 for x in rm.standard_normal((norb + 1, norb, norb))]
+        two_body = sum(np.einsum("pq,rs->pqrs", x, x) for x in ls)
+        const = float(rm.standard_normal())
+        mol = ref.MolecularHamiltonian(one_body, two_body, constant=const)
+        out[f"mol{idx}_h1"], out[f"mol{idx}_h2"], out[f"mol{idx}_const"] = one_body, two_body, np.asarray(const)
+        out[f"mol{idx}_chol"] = ref.modified_cholesky(two_body.reshape(norb**2, norb**2), tol=1e-8)
+        out[f"mol{idx}_chol_max2"] = ref.modified_cholesky(two_body.reshape(norb**2, norb**2), tol=1e-8, max_vecs=2)
+        for tag, kw in [("c", {}), ("c3", {"max_vecs": 3}), ("e", {"cholesky": False}),
+                        ("e3", {"cholesky": False, "max_vecs": 3})]:
+            mats, rots = ref.double_factorized(two_body, tol=1e-8, **kw)
+            out[f"mol{idx}_df{tag}_mats"], out[f"mol{idx}_df{tag}_rots"] = mats, rots
+        for z in (False, True):
+            df = ref.DoubleFactorizedHamiltonian.from_molecular_hamiltonian(mol, z_representation=z)
+            out[f"mol{idx}_from{int(z)}_h1"] = df.one_body_tensor
+            out[f"mol{idx}_from{int(z)}_const"] = np.asarray(df.constant)
+            out[f"mol{idx}_from{int(z)}_mats"] = df.diag_coulomb_mats
+            back = df.to_molecular_hamiltonian()
+            out[f"mol{idx}_back{int(z)}_h1"], out[f"mol{idx}_back{int(z)}_h2"] = back.one_body_tensor, back.two_body_tensor
+        u = orc.random_unitary(norb, seed=rm)
+        rot = mol.rotated(u)
+        out[f"mol{idx}_u"], out[f"mol{idx}_rot_h1"], out[f"mol{idx}_rot_h2"] = u, rot.one_body_tensor, rot.two_body_tensor
+    out["mol_cases"] = np.asarray(mol_norbs)
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
