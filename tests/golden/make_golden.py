@@ -195,7 +195,17 @@ def install_stubs():
     sys.modules["ffsim.linalg"].double_factorized = ldf.double_factorized
     mol = _load("ffsim.hamiltonians.molecular_hamiltonian", "hamiltonians/molecular_hamiltonian.py")
     dfh = _load("ffsim.hamiltonians.double_factorized_hamiltonian", "hamiltonians/double_factorized_hamiltonian.py")
+    # the seeded random constructors, over the real dataclasses
+    for name, cls in [("DiagonalCoulombHamiltonian", dch.DiagonalCoulombHamiltonian),
+                      ("DoubleFactorizedHamiltonian", dfh.DoubleFactorizedHamiltonian),
+                      ("MolecularHamiltonian", mol.MolecularHamiltonian)]:
+        setattr(sys.modules["ffsim.hamiltonians"], name, cls)
+    for name, cls in [("UCJOpSpinBalanced", ucj.UCJOpSpinBalanced), ("UCJOpSpinUnbalanced", ucju.UCJOpSpinUnbalanced),
+                      ("UCJOpSpinless", ucjs.UCJOpSpinless)]:
+        setattr(sys.modules["ffsim.variational"], name, cls)
+    rnd = _load("ffsim.random_module", "random/random.py")
     return types.SimpleNamespace(
+        random=rnd,
         modified_cholesky=ldf.modified_cholesky,
         double_factorized=ldf.double_factorized,
         MolecularHamiltonian=mol.MolecularHamiltonian,
@@ -552,6 +562,45 @@ def main():
         rot = mol.rotated(u)
         out[f"mol{idx}_u"], out[f"mol{idx}_rot_h1"], out[f"mol{idx}_rot_h2"] = u, rot.one_body_tensor, rot.two_body_tensor
     out["mol_cases"] = np.asarray(mol_norbs)
+
+    # seeded random constructors (random/random.py): the same seed gives the
+    # same inputs here and in the reference
+    r = ref.random
+    out["rnd_density"] = r.random_density_matrix(4, seed=1)
+    out["rnd_orth"] = r.random_orthogonal(5, seed=2)
+    out["rnd_sorth"] = r.random_special_orthogonal(5, seed=3)
+    out["rnd_herm"] = r.random_hermitian(4, seed=4)
+    out["rnd_antiherm"] = r.random_antihermitian(4, seed=5)
+    out["rnd_tbt"] = r.random_two_body_tensor(3, seed=6)
+    out["rnd_tbt_real_r2"] = r.random_two_body_tensor(3, rank=2, seed=7, dtype=float)
+    for tag, dt in [("c", complex), ("r", float)]:
+        m = r.random_molecular_hamiltonian(3, seed=8, dtype=dt)
+        out[f"rnd_mol{tag}_h1"], out[f"rnd_mol{tag}_h2"] = m.one_body_tensor, m.two_body_tensor
+        out[f"rnd_mol{tag}_const"] = np.asarray(m.constant)
+    for tag, real in [("c", False), ("r", True)]:
+        h = r.random_diagonal_coulomb_hamiltonian(4, real=real, seed=9)
+        out[f"rnd_dch{tag}_h1"], out[f"rnd_dch{tag}_dcm"] = h.one_body_tensor, h.diag_coulomb_mats
+        out[f"rnd_dch{tag}_const"] = np.asarray(h.constant)
+        h = r.random_double_factorized_hamiltonian(3, rank=2, real=real, seed=10)
+        out[f"rnd_df{tag}_h1"], out[f"rnd_df{tag}_dcm"] = h.one_body_tensor, h.diag_coulomb_mats
+        out[f"rnd_df{tag}_rots"], out[f"rnd_df{tag}_const"] = h.orbital_rotations, np.asarray(h.constant)
+    h = r.random_double_factorized_hamiltonian(3, seed=11, z_representation=True)
+    out["rnd_dfz_rots"] = h.orbital_rotations
+    ucj_kw = [dict(n_reps=2, seed=12), dict(n_reps=1, with_final_orbital_rotation=True, diag_coulomb_normal=True,
+                                             diag_coulomb_scale=0.3, seed=13)]
+    for k, kw in enumerate(ucj_kw):
+        for tag, fn in [("bal", r.random_ucj_op_spin_balanced), ("unb", r.random_ucj_op_spin_unbalanced),
+                        ("sl", r.random_ucj_op_spinless)]:
+            op = fn(4, **kw)
+            out[f"rnd_{tag}{k}_dcm"], out[f"rnd_{tag}{k}_rots"] = op.diag_coulomb_mats, op.orbital_rotations
+            if op.final_orbital_rotation is not None:
+                out[f"rnd_{tag}{k}_final"] = op.final_orbital_rotation
+    op = r.random_ucj_op_spin_balanced(4, n_reps=2, interaction_pairs=([(0, 0), (1, 2)], [(0, 0), (3, 3)]), seed=14)
+    out["rnd_balp_dcm"] = op.diag_coulomb_mats
+    op = r.random_ucj_op_spin_unbalanced(4, interaction_pairs=([(0, 1)], [(2, 0), (1, 1)], []), seed=15)
+    out["rnd_unbp_dcm"] = op.diag_coulomb_mats
+    op = r.random_ucj_op_spinless(4, interaction_pairs=[(0, 3), (2, 2)], seed=16)
+    out["rnd_slp_dcm"] = op.diag_coulomb_mats
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
