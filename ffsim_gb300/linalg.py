@@ -191,3 +191,48 @@ def rotate_two_body_tensor(tensor: np.ndarray, orbital_rotation_1: np.ndarray | 
         v = np.asarray(orbital_rotation_2)
         t = np.einsum("abcd,Cc,Dd->abCD", t, v, v.conj(), optimize=True)
     return t
+
+
+def double_factorized_t2(t2_amplitudes: np.ndarray, *, tol: float = 1e-8, max_terms: int | None = None,
+                         optimize: bool = False, method: str = "L-BFGS-B", callback=None, options: dict | None = None,
+                         diag_coulomb_indices=None, regularization: float = 0, multi_stage_start: int | None = None,
+                         multi_stage_step: int | None = None, return_optimize_result: bool = False):
+    r"""Double factorization of t2 amplitudes into diagonal Coulomb terms
+    (python/ffsim/linalg/double_factorized_decomposition.py:467-659).
+
+    The matrix T[(i, a), (j, b)] = t2[i, j, a, b] is diagonalised and
+    truncated (largest |eigenvalues| first; the dropped tail's total |weight|
+    stays below ``tol``).  Each eigenvector becomes the norb x norb matrix K
+    with K[nocc + a, i] = v[(i, a)], and K splits into the two Hermitian
+    quadratures Q_s = (1 - i s)(K + i s K^dag) / 2, s = +1, -1.  With
+    Q_s = U diag(mu) U^dag the term is J = s lambda mu mu^T with rotation U.
+    The terms (each eigenvector's + then -) are cut to ``max_terms``.  As in
+    the reference, K is real: complex eigenvectors keep their real part.
+    Returns (diag_coulomb_mats, orbital_rotations).  The compressed form
+    (``optimize=True``) is fitted with a JAX gradient in the reference and is
+    not available here.
+    """
+    if max_terms is not None and max_terms < 1:
+        raise ValueError(f"max_terms must be at least 1. Got {max_terms}.")
+    if optimize:
+        raise NotImplementedError("the compressed (optimize=True) t2 factorization is not available")
+    t2 = np.asarray(t2_amplitudes)
+    nocc, _, nvrt, _ = t2.shape
+    norb = nocc + nvrt
+    w, v = scipy.linalg.eigh(t2.transpose(0, 2, 1, 3).reshape(nocc * nvrt, nocc * nvrt))
+    order = np.argsort(np.abs(w))[::-1]
+    w, v = w[order], v[:, order]
+    keep = len(w) - int(np.searchsorted(np.cumsum(np.abs(w[::-1])), tol))
+    w, v = w[:keep], v[:, :keep]
+    occ = np.repeat(np.arange(nocc), nvrt)
+    vrt = np.tile(np.arange(nocc, norb), nocc)
+    quads = np.zeros((keep, 2, norb, norb), dtype=complex)
+    for t in range(keep):
+        k = np.zeros((norb, norb))
+        k[vrt, occ] = v[:, t].real
+        for m, sgn in enumerate((1, -1)):
+            quads[t, m] = 0.5 * (1 - sgn * 1j) * (k + sgn * 1j * k.conj().T)
+    mu, rots = np.linalg.eigh(quads)
+    coeff = np.array([1, -1]) * w[:, None]
+    mats = coeff[:, :, None, None] * mu[:, :, :, None] * mu[:, :, None, :]
+    return mats.reshape(-1, norb, norb)[:max_terms], rots.reshape(-1, norb, norb)[:max_terms]

@@ -97,6 +97,29 @@ def random_two_body_tensor(dim: int, *, rank: int | None = None, seed=None, dtyp
     return np.tensordot(mats, mats, axes=(0, 0))
 
 
+def random_t2_amplitudes(norb: int, nocc: int, *, seed=None, dtype=complex) -> np.ndarray:
+    """t2[i, j, a, b] = t2[j, i, b, a], one normal draw per unordered pair of
+    (occupied, virtual) pairs; complex amplitudes are then rotated by a Haar
+    unitary in the full orbital space (random.py:240-276)."""
+    import itertools
+
+    rng = np.random.default_rng(seed)
+    nvrt = norb - nocc
+    t2 = np.zeros((nocc, nocc, nvrt, nvrt), dtype=dtype)
+    pairs = list(itertools.product(range(nocc), range(nocc, norb)))
+    for (i, a), (j, b) in itertools.combinations_with_replacement(pairs, 2):
+        val = rng.standard_normal()
+        t2[i, j, a - nocc, b - nocc] = val
+        t2[j, i, b - nocc, a - nocc] = val
+    if np.issubdtype(dtype, np.complexfloating):
+        big = np.zeros((norb, norb, norb, norb), dtype=dtype)
+        big[:nocc, :nocc, nocc:, nocc:] = t2
+        u = random_unitary(norb, seed=rng)
+        big = np.einsum("ijab,iI,jJ,aA,bB->IJAB", big, u.conj(), u.conj(), u, u, optimize=True)
+        t2 = big[:nocc, :nocc, nocc:, nocc:]
+    return t2
+
+
 def random_molecular_hamiltonian(norb: int, seed=None, dtype=complex) -> MolecularHamiltonian:
     """Random molecular Hamiltonian (random.py:279-305)."""
     rng = np.random.default_rng(seed)

@@ -27,6 +27,34 @@ def validate_interaction_pairs(interaction_pairs, ordered: bool) -> None:
                     f"only upper triangular pairs. Got {(i, j)}, which is a lower triangular pair.")
 
 
+def orbital_rotation_from_t1_amplitudes(t1: np.ndarray) -> np.ndarray:
+    """exp(t1 - t1^dag) embedded in the occupied-virtual block
+    (python/ffsim/variational/util.py:38-54)."""
+    import scipy.linalg
+
+    t1 = np.asarray(t1)
+    nocc, nvrt = t1.shape
+    norb = nocc + nvrt
+    gen = np.zeros((norb, norb), dtype=t1.dtype)
+    gen[:nocc, nocc:] = -t1.conj()
+    gen[nocc:, :nocc] = t1.T
+    return scipy.linalg.expm(gen)
+
+
+def interaction_pairs_spin_balanced(connectivity: str, norb: int):
+    """Alpha-alpha and alpha-beta interaction pairs of a qubit layout
+    (python/ffsim/variational/util.py:57-75): all-to-all (no restriction),
+    square (a chain plus every ab on-site pair), hex (on-site every second
+    orbital), heavy-hex (every fourth)."""
+    if connectivity == "all-to-all":
+        return None, None
+    chain = [(p, p + 1) for p in range(norb - 1)]
+    stride = {"square": 1, "hex": 2, "heavy-hex": 4}.get(connectivity)
+    if stride is None:
+        raise ValueError(f"Invalid connectivity: {connectivity}")
+    return chain, [(p, p) for p in range(0, norb, stride)]
+
+
 def _triu(norb: int) -> list:
     return list(itertools.combinations_with_replacement(range(norb), 2))
 
@@ -127,6 +155,47 @@ class UCJOpSpinBalanced:
         final = None
         if with_final_orbital_rotation:
             final = linalg.unitary_from_parameters(params[index:], norb)
+        return UCJOpSpinBalanced(dcm, rots, final)
+
+    @staticmethod
+    def from_t_amplitudes(t2: np.ndarray, *, t1: np.ndarray | None = None, n_reps: int | None = None,
+                          interaction_pairs=None, tol: float = 1e-8, optimize: bool = False,
+                          method: str = "L-BFGS-B", callback=None, options: dict | None = None,
+                          regularization: float = 0, multi_stage_start: int | None = None,
+                          multi_stage_step: int | None = None) -> "UCJOpSpinBalanced":
+        """UCJ operator from (CCSD) t2 and optional t1 amplitudes
+        (ucj_spin_balanced.py:377-532): the t2 double factorization gives one
+        layer per term (the same matrix for aa and ab), padded with identity
+        layers up to ``n_reps``; t1 gives the final rotation exp(t1 - t1^dag);
+        entries outside the interaction pairs are zeroed."""
+        if isinstance(n_reps, int) and n_reps <= 0:
+            raise ValueError(f"n_reps must be at least 1. Got {n_reps}.")
+        pairs_aa, pairs_ab = (None, None) if interaction_pairs is None else interaction_pairs
+        validate_interaction_pairs(pairs_aa, ordered=False)
+        validate_interaction_pairs(pairs_ab, ordered=False)
+        nocc, _, nvrt, _ = np.asarray(t2).shape
+        norb = nocc + nvrt
+        indices = None
+        if pairs_aa is not None or pairs_ab is not None:
+            indices = list(set((pairs_aa or []) + (pairs_ab or [])))
+        mats, rots = linalg.double_factorized_t2(
+            t2, tol=tol, max_terms=n_reps, optimize=optimize, method=method, callback=callback, options=options,
+            diag_coulomb_indices=indices, regularization=regularization, multi_stage_start=multi_stage_start,
+            multi_stage_step=multi_stage_step)
+        dcm = np.stack([mats, mats], axis=1)
+        if n_reps is not None and dcm.shape[0] < n_reps:
+            pad = n_reps - dcm.shape[0]
+            dcm = np.concatenate([dcm, np.zeros((pad, 2, norb, norb))])
+            rots = np.concatenate([rots, np.stack([np.eye(norb)] * pad)])
+        final = orbital_rotation_from_t1_amplitudes(t1) if t1 is not None else None
+        for t, pairs in enumerate((pairs_aa, pairs_ab)):
+            if pairs is not None:
+                mask = np.zeros((norb, norb), dtype=bool)
+                if pairs:
+                    rows, cols = zip(*pairs)
+                    mask[rows, cols] = True
+                    mask[cols, rows] = True
+                dcm[:, t] *= mask
         return UCJOpSpinBalanced(dcm, rots, final)
 
     def to_parameters(self, *, interaction_pairs=None) -> np.ndarray:

@@ -193,6 +193,7 @@ def install_stubs():
     sys.modules["ffsim.operators"].FermionAction = None
     ldf = _load("ffsim.linalg.double_factorized_decomposition", "linalg/double_factorized_decomposition.py")
     sys.modules["ffsim.linalg"].double_factorized = ldf.double_factorized
+    sys.modules["ffsim.linalg"].double_factorized_t2 = ldf.double_factorized_t2
     mol = _load("ffsim.hamiltonians.molecular_hamiltonian", "hamiltonians/molecular_hamiltonian.py")
     dfh = _load("ffsim.hamiltonians.double_factorized_hamiltonian", "hamiltonians/double_factorized_hamiltonian.py")
     # the seeded random constructors, over the real dataclasses
@@ -206,6 +207,8 @@ def install_stubs():
     rnd = _load("ffsim.random_module", "random/random.py")
     return types.SimpleNamespace(
         random=rnd,
+        double_factorized_t2=ldf.double_factorized_t2,
+        orbital_rotation_from_t1_amplitudes=sys.modules["ffsim.variational.util"].orbital_rotation_from_t1_amplitudes,
         modified_cholesky=ldf.modified_cholesky,
         double_factorized=ldf.double_factorized,
         MolecularHamiltonian=mol.MolecularHamiltonian,
@@ -601,6 +604,27 @@ def main():
     out["rnd_unbp_dcm"] = op.diag_coulomb_mats
     op = r.random_ucj_op_spinless(4, interaction_pairs=[(0, 3), (2, 2)], seed=16)
     out["rnd_slp_dcm"] = op.diag_coulomb_mats
+
+    # UCJ from t amplitudes (variational/ucj_spin_balanced.py:377-532) over the
+    # explicit t2 factorization (linalg/double_factorized_decomposition.py:467-659)
+    t2_cases = [(5, 2, float, 17), (6, 3, float, 18), (5, 2, complex, 19)]
+    for idx, (norb, nocc, dt, seed) in enumerate(t2_cases):
+        t2 = r.random_t2_amplitudes(norb, nocc, seed=seed, dtype=dt)
+        t1 = np.random.default_rng(seed).standard_normal((nocc, norb - nocc))
+        out[f"t2{idx}_t2"], out[f"t2{idx}_t1"] = t2, t1
+        mats, rots = ref.double_factorized_t2(t2)
+        out[f"t2{idx}_mats"], out[f"t2{idx}_rots"] = mats, rots
+        mats, rots = ref.double_factorized_t2(t2, max_terms=3)
+        out[f"t2{idx}_mats3"] = mats
+        out[f"t2{idx}_t1rot"] = ref.orbital_rotation_from_t1_amplitudes(t1)
+        for tag, kw in [("a", {}), ("b", {"n_reps": 2, "t1": t1}), ("c", {"n_reps": 40}),
+                        ("d", {"interaction_pairs": ([(0, 1), (1, 2)], [(0, 0)]), "n_reps": 3})]:
+            op = ref.UCJOpSpinBalanced.from_t_amplitudes(t2, **kw)
+            out[f"t2{idx}_op{tag}_dcm"], out[f"t2{idx}_op{tag}_rots"] = op.diag_coulomb_mats, op.orbital_rotations
+            vec = orc.random_state_vector(orc.dim(norb, (nocc, nocc)), seed=seed)
+            out[f"t2{idx}_op{tag}_in"] = vec
+            out[f"t2{idx}_op{tag}_out"] = op._apply_unitary_(vec, norb, (nocc, nocc), copy=True)
+    out["t2_cases"] = np.asarray([[n, o, int(d is complex), sd] for n, o, d, sd in t2_cases])
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")

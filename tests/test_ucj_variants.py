@@ -141,3 +141,87 @@ def test_interaction_pair_validation():
     with pytest.raises(ValueError):  # duplicates
         f.UCJOpSpinUnbalanced.n_params(4, 1, interaction_pairs=(None, [(1, 0), (1, 0)], None))
     assert f.UCJOpSpinUnbalanced.n_params(4, 1, interaction_pairs=(None, [(1, 0)], None)) == 10 + 1 + 10 + 32
+
+
+def _t2_case(golden, idx):
+    norb, nocc, _, _ = (int(x) for x in golden["t2_cases"][idx])
+    return norb, nocc, golden[f"t2{idx}_t2"], golden[f"t2{idx}_t1"]
+
+
+def test_double_factorized_t2_golden(golden):
+    """Coulomb matrices entry by entry; rotations up to each eigenvector's phase,
+    through the reconstructed amplitudes."""
+    import ffsim_gb300 as f
+
+    for idx in range(len(golden["t2_cases"])):
+        norb, nocc, t2, _ = _t2_case(golden, idx)
+        mats, rots = f.linalg.double_factorized_t2(t2)
+        np.testing.assert_allclose(mats, golden[f"t2{idx}_mats"], atol=1e-10)
+        gr = golden[f"t2{idx}_rots"]
+        np.testing.assert_allclose(np.abs(rots), np.abs(gr), atol=1e-8)
+        rec = lambda m, u: 1j * np.einsum("kpq,kap,kip,kbq,kjq->ijab", m, u, u.conj(), u, u.conj())[  # noqa: E731
+            :nocc, :nocc, nocc:, nocc:]
+        np.testing.assert_allclose(rec(mats, rots), rec(golden[f"t2{idx}_mats"], gr), atol=1e-10)
+        np.testing.assert_allclose(f.linalg.double_factorized_t2(t2, max_terms=3)[0], golden[f"t2{idx}_mats3"],
+                                   atol=1e-10)
+    with pytest.raises(ValueError):
+        f.linalg.double_factorized_t2(golden["t20_t2"], max_terms=0)
+    with pytest.raises(NotImplementedError):
+        f.linalg.double_factorized_t2(golden["t20_t2"], optimize=True)
+
+
+def test_from_t_amplitudes_golden(golden):
+    """The operators' matrices, and their action (through the oracle) against
+    the reference's own apply_unitary on the same vectors."""
+    import ffsim_gb300 as f
+
+    for idx in range(len(golden["t2_cases"])):
+        norb, nocc, t2, t1 = _t2_case(golden, idx)
+        np.testing.assert_allclose(f.variational.orbital_rotation_from_t1_amplitudes(t1), golden[f"t2{idx}_t1rot"],
+                                   atol=1e-12)
+        for tag, kw in [("a", {}), ("b", {"n_reps": 2, "t1": t1}), ("c", {"n_reps": 40}),
+                        ("d", {"interaction_pairs": ([(0, 1), (1, 2)], [(0, 0)]), "n_reps": 3})]:
+            op = f.UCJOpSpinBalanced.from_t_amplitudes(t2, **kw)
+            np.testing.assert_allclose(op.diag_coulomb_mats, golden[f"t2{idx}_op{tag}_dcm"], atol=1e-10)
+            assert op.orbital_rotations.shape == golden[f"t2{idx}_op{tag}_rots"].shape
+            got = o.ucj_spin_balanced_apply(golden[f"t2{idx}_op{tag}_in"], op.diag_coulomb_mats, op.orbital_rotations,
+                                            op.final_orbital_rotation, norb, (nocc, nocc))
+            np.testing.assert_allclose(got, golden[f"t2{idx}_op{tag}_out"], atol=1e-10)
+    with pytest.raises(ValueError):
+        f.UCJOpSpinBalanced.from_t_amplitudes(golden["t20_t2"], n_reps=0)
+
+
+def test_random_t2_amplitudes_symmetry():
+    import ffsim_gb300 as f
+
+    t2 = f.random.random_t2_amplitudes(6, 2, seed=3)
+    np.testing.assert_allclose(t2, t2.transpose(1, 0, 3, 2), atol=1e-12)
+
+
+def test_interaction_pair_layouts():
+    import ffsim_gb300 as f
+
+    ip = f.variational.interaction_pairs_spin_balanced
+    assert ip("all-to-all", 4) == (None, None)
+    assert ip("square", 3) == ([(0, 1), (1, 2)], [(0, 0), (1, 1), (2, 2)])
+    assert ip("heavy-hex", 6)[1] == [(0, 0), (4, 4)]
+    with pytest.raises(ValueError):
+        ip("ring", 4)
+
+
+@pytest.mark.gpu
+def test_gpu_from_t_amplitudes_golden(cuda, golden):
+    import torch
+
+    import ffsim_gb300 as f
+
+    for idx in range(len(golden["t2_cases"])):
+        norb, nocc, t2, t1 = _t2_case(golden, idx)
+        for tag, kw in [("a", {}), ("b", {"n_reps": 2, "t1": t1}), ("c", {"n_reps": 40})]:
+            op = f.UCJOpSpinBalanced.from_t_amplitudes(t2, **kw)
+            vin = golden[f"t2{idx}_op{tag}_in"]
+            for dtype, tol in [(torch.complex128, 1e-10), (torch.complex64, 5e-5)]:
+                v = torch.from_numpy(vin).to("cuda").to(dtype)
+                out = f.apply_unitary(v, op, norb, (nocc, nocc))
+                np.testing.assert_allclose(out.cpu().numpy().astype(complex), golden[f"t2{idx}_op{tag}_out"],
+                                           atol=tol)
