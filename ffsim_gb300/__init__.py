@@ -22,7 +22,13 @@ from ffsim_gb300.gates import (
 from ffsim_gb300.hamiltonians import DiagonalCoulombHamiltonian, DoubleFactorizedHamiltonian, MolecularHamiltonian
 from ffsim_gb300.protocols import LinearOperator, apply_unitary, diag, linear_operator, trace
 from ffsim_gb300.rdm import rdms
-from ffsim_gb300.states import hartree_fock_state, vdot
+from ffsim_gb300.states import (
+    hartree_fock_state,
+    slater_determinant,
+    slater_determinant_amplitudes,
+    slater_determinant_rdms,
+    vdot,
+)
 from ffsim_gb300.trotter import simulate_trotter_diag_coulomb_split_op, simulate_trotter_double_factorized
 from ffsim_gb300.variational import GivensAnsatzOp, UCJOpSpinBalanced, UCJOpSpinless, UCJOpSpinUnbalanced
 
@@ -56,6 +62,9 @@ __all__ = [
     "linear_operator",
     "lucj_energy",
     "random",
+    "slater_determinant",
+    "slater_determinant_amplitudes",
+    "slater_determinant_rdms",
     "states",
     "trace",
     "vdot",

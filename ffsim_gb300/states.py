@@ -12,7 +12,8 @@ import torch
 from ffsim_gb300 import _lib
 from ffsim_gb300._state import dim, dims, stream_ptr
 
-__all__ = ["dim", "dims", "make_strings", "hartree_fock_state", "vdot", "addresses_to_strings"]
+__all__ = ["dim", "dims", "make_strings", "hartree_fock_state", "vdot", "addresses_to_strings",
+           "slater_determinant", "slater_determinant_rdms", "slater_determinant_amplitudes"]
 
 
 @lru_cache(maxsize=None)
@@ -53,3 +54,112 @@ def vdot(x: torch.Tensor, y: torch.Tensor) -> complex:
     _lib.call("ffgb_vdot", x.data_ptr(), y.data_ptr(), code, x.numel(), _lib.dptr(out), stream_ptr(x))
     return complex(out[0], out[1])
 
+
+
+def _spinless(occupied_orbitals) -> bool:
+    return not occupied_orbitals or isinstance(occupied_orbitals[0], (int, np.integer))
+
+
+def _permutation_parity(orbitals) -> int:
+    """+1 or -1: the sign of sorting ``orbitals`` (the number of inversions)."""
+    orbs = list(orbitals)
+    inv = sum(1 for i in range(len(orbs)) for j in range(i + 1, len(orbs)) if orbs[i] > orbs[j])
+    return -1 if inv % 2 else 1
+
+
+def _address(norb: int, orbitals) -> int:
+    bits = sum(1 << int(i) for i in orbitals)
+    return int(np.searchsorted(make_strings(norb, len(orbitals)), bits))
+
+
+def slater_determinant(norb: int, occupied_orbitals, orbital_rotation=None, *, dtype=torch.complex128,
+                       device="cuda") -> torch.Tensor:
+    r""":math:`\mathcal{U} |x\rangle` for the configuration x of
+    ``occupied_orbitals`` (a list, spinless, or an (alpha, beta) pair of lists),
+    as a device tensor (python/ffsim/states/slater.py:32-103).  The one-hot
+    vector is signed by the parity of the listed orbital order and rotated by
+    ``orbital_rotation`` (one matrix, or a pair with ``None`` entries) on the GPU."""
+    from ffsim_gb300.gates import apply_orbital_rotation
+
+    if norb == 0:
+        return torch.ones(1, dtype=dtype, device=device)
+    if _spinless(occupied_orbitals):
+        orbs = list(occupied_orbitals)
+        nelec = len(orbs)
+        index = _address(norb, orbs)
+        sign = _permutation_parity(orbs)
+    else:
+        alpha, beta = (list(x) for x in occupied_orbitals)
+        nelec = (len(alpha), len(beta))
+        index = _address(norb, alpha) * math.comb(norb, len(beta)) + _address(norb, beta)
+        sign = _permutation_parity(alpha) * _permutation_parity(beta)
+    vec = torch.zeros(dim(norb, nelec), dtype=dtype, device=device)
+    vec[index] = sign
+    if orbital_rotation is not None:
+        vec = apply_orbital_rotation(vec, orbital_rotation, norb, nelec, copy=False)
+    return vec
+
+
+def _rdm1_rotated(norb, orbitals, rot):
+    rdm = np.zeros((norb, norb))
+    if orbitals:
+        rdm[orbitals, orbitals] = 1
+    if rot is not None:
+        rot = np.asarray(rot)
+        rdm = rot.conj() @ rdm @ rot.T
+    return rdm
+
+
+def _rdm2_same(rdm, reorder, norb):
+    out = np.einsum("pq,rs->pqrs", rdm, rdm) - np.einsum("ps,rq->pqrs", rdm, rdm)
+    if not reorder:
+        out = out + np.einsum("ps,qr->pqrs", rdm, np.eye(norb))
+    return out
+
+
+def slater_determinant_rdms(norb: int, occupied_orbitals, orbital_rotation=None, *, rank: int = 1,
+                            reorder: bool = True):
+    """Closed-form 1- and 2-RDMs of a Slater determinant (python/ffsim/states/slater.py:141-300):
+    rdm1 = conj(U) P U^T with P the occupied projector; rdm2 from Wick's
+    theorem (direct minus exchange, plus rdm1 (x) 1 when ``reorder`` is
+    False).  Spinful results are stacked (a, b) and (aa, ab, bb)."""
+    if rank not in (1, 2):
+        raise NotImplementedError(f"Returning the rank {rank} reduced density matrix is currently not supported.")
+    if _spinless(occupied_orbitals):
+        rdm1 = _rdm1_rotated(norb, list(occupied_orbitals), orbital_rotation)
+        return rdm1 if rank == 1 else (rdm1, _rdm2_same(rdm1, reorder, norb))
+    if isinstance(orbital_rotation, np.ndarray) and orbital_rotation.ndim == 2:
+        rot_a = rot_b = orbital_rotation
+    else:
+        rot_a, rot_b = orbital_rotation if orbital_rotation is not None else (None, None)
+    alpha, beta = (list(x) for x in occupied_orbitals)
+    rdm_a = _rdm1_rotated(norb, alpha, rot_a)
+    rdm_b = _rdm1_rotated(norb, beta, rot_b)
+    rdm1 = np.stack([rdm_a, rdm_b])
+    if rank == 1:
+        return rdm1
+    rdm2 = np.stack([_rdm2_same(rdm_a, reorder, norb), np.einsum("pq,rs->pqrs", rdm_a, rdm_b),
+                     _rdm2_same(rdm_b, reorder, norb)])
+    return rdm1, rdm2
+
+
+def slater_determinant_amplitudes(bitstrings, norb: int, occupied_orbitals, orbital_rotation) -> np.ndarray:
+    """Amplitudes of given bitstrings in a Slater determinant: determinants of
+    the rotation's occupied columns restricted to the bitstring's rows
+    (python/ffsim/states/slater.py:303-350); spinful amplitudes are the
+    products of the two sectors'."""
+    import scipy.linalg
+
+    def sector(strings, orbs, rot):
+        cols = np.asarray(rot)[:, list(orbs)]
+        return np.array([scipy.linalg.det(cols[[i for i in range(norb) if (int(b) >> i) & 1]]) for b in strings])
+
+    if _spinless(occupied_orbitals):
+        return sector(bitstrings, occupied_orbitals, orbital_rotation)
+    strings_a, strings_b = bitstrings
+    orbs_a, orbs_b = occupied_orbitals
+    if isinstance(orbital_rotation, np.ndarray) and orbital_rotation.ndim == 2:
+        rot_a = rot_b = orbital_rotation
+    else:
+        rot_a, rot_b = orbital_rotation
+    return sector(strings_a, orbs_a, rot_a) * sector(strings_b, orbs_b, rot_b)

@@ -96,10 +96,16 @@ def _gen_occslst(orb_list, nocc):
     return np.asarray(occ, dtype=np.int32).reshape(len(strings), nocc)
 
 
+def _str2addr(norb, nocc, string):
+    """Address of a bitstring: its rank among the ascending strings of its popcount."""
+    return int(np.searchsorted(_make_strings(range(norb), nocc), int(string)))
+
+
 def install_stubs():
     _module("pyscf", is_pkg=True)
     _module("pyscf.fci", is_pkg=True)
-    _module("pyscf.fci.cistring", {"make_strings": _make_strings, "gen_occslst": _gen_occslst})
+    _module("pyscf.fci.cistring", {"make_strings": _make_strings, "gen_occslst": _gen_occslst,
+                                   "str2addr": _str2addr})
     _module("pyscf.ci", is_pkg=True)
     jax = _module("jax", {"config": types.SimpleNamespace(update=lambda *a, **k: None)})
     jax.numpy = _module("jax.numpy")
@@ -205,8 +211,12 @@ def install_stubs():
                       ("UCJOpSpinless", ucjs.UCJOpSpinless)]:
         setattr(sys.modules["ffsim.variational"], name, cls)
     rnd = _load("ffsim.random_module", "random/random.py")
+    sys.modules["ffsim.linalg"].one_hot = _load("ffsim.linalg.linalg", "linalg/linalg.py").one_hot
+    _load("ffsim.states.bitstring", "states/bitstring.py")
+    slater = _load("ffsim.states.slater", "states/slater.py")
     return types.SimpleNamespace(
         random=rnd,
+        slater=slater,
         double_factorized_t2=ldf.double_factorized_t2,
         orbital_rotation_from_t1_amplitudes=sys.modules["ffsim.variational.util"].orbital_rotation_from_t1_amplitudes,
         modified_cholesky=ldf.modified_cholesky,
@@ -625,6 +635,30 @@ def main():
             out[f"t2{idx}_op{tag}_in"] = vec
             out[f"t2{idx}_op{tag}_out"] = op._apply_unitary_(vec, norb, (nocc, nocc), copy=True)
     out["t2_cases"] = np.asarray([[n, o, int(d is complex), sd] for n, o, d, sd in t2_cases])
+
+    # Slater determinants (states/slater.py:32-350): state vectors, closed-form
+    # RDMs and amplitudes, spinful and spinless, with unsorted orbital lists
+    rs = np.random.default_rng(20261210)
+    sl = ref.slater
+    u, v = orc.random_unitary(5, seed=rs), orc.random_unitary(5, seed=rs)
+    out["sl_u"], out["sl_v"] = u, v
+    out["sl_vec_plain"] = sl.slater_determinant(5, ([3, 0], [4, 1, 2]))
+    out["sl_vec_plain_spinless"] = sl.slater_determinant(5, [2, 4, 0])
+    out["sl_vec_rot"] = sl.slater_determinant(5, ([1, 3], [0, 4, 2]), u)
+    out["sl_vec_pair"] = sl.slater_determinant(5, ([2, 0], [1]), (u, None))
+    out["sl_vec_spinless_rot"] = sl.slater_determinant(5, [4, 1], v)
+    for tag, occ, rot in [("a", ([0, 2], [1, 3, 4]), u), ("b", ([1], [0, 3]), (u, v)), ("c", [0, 3, 1], v),
+                          ("d", ([0, 1], []), (None, v))]:
+        for rank in (1, 2):
+            for reorder in (True, False):
+                res = sl.slater_determinant_rdms(5, occ, rot, rank=rank, reorder=reorder)
+                if rank == 1:
+                    out[f"sl_rdm_{tag}_1"] = res
+                else:
+                    out[f"sl_rdm_{tag}_2_{int(reorder)}"] = res[1]
+    out["sl_amp_spinful"] = sl.slater_determinant_amplitudes(([0b00011, 0b10100], [0b01010, 0b11000]), 5,
+                                                             ([0, 1], [2, 3]), (u, v))
+    out["sl_amp_spinless"] = sl.slater_determinant_amplitudes([0b00111, 0b11010], 5, [0, 2, 4], v)
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
