@@ -128,13 +128,23 @@ def dptr(arr: np.ndarray | None):
     return arr.ctypes.data_as(_dp)
 
 
-def cmat(mat) -> np.ndarray | None:
-    if mat is None:
-        return None
-    return np.ascontiguousarray(np.asarray(mat, dtype=np.complex128))
+def _checked(arr: np.ndarray, shape, what: str) -> np.ndarray:
+    """The library reads exactly ``shape`` elements through the pointer, so a
+    mis-sized array is rejected here instead of read past its end."""
+    if shape is not None and arr.shape != tuple(shape):
+        raise ValueError(f"{what} must have shape {tuple(shape)}, got {arr.shape}")
+    return arr
 
 
-def rmat(mat) -> np.ndarray | None:
+def cmat(mat, shape=None, what: str = "matrix") -> np.ndarray | None:
+    """Contiguous complex128 copy of ``mat`` (None stays None), optionally shape-checked."""
     if mat is None:
         return None
-    return np.ascontiguousarray(np.asarray(mat, dtype=np.float64))
+    return _checked(np.ascontiguousarray(np.asarray(mat, dtype=np.complex128)), shape, what)
+
+
+def rmat(mat, shape=None, what: str = "matrix") -> np.ndarray | None:
+    """Contiguous float64 copy of ``mat`` (None stays None), optionally shape-checked."""
+    if mat is None:
+        return None
+    return _checked(np.ascontiguousarray(np.asarray(mat, dtype=np.float64)), shape, what)

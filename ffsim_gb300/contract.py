@@ -27,7 +27,7 @@ def contract_diag_coulomb(vec, mat, norb: int, nelec: tuple[int, int], *, z_repr
     (python/ffsim/contract/diag_coulomb.py:41-99)."""
     p = prepare(vec, norb, nelec, copy=False)
     out = torch.empty_like(p.tensor)
-    aa, ab, bb = (_lib.rmat(m) for m in _mats(mat))
+    aa, ab, bb = (_lib.rmat(m, (norb, norb), "diagonal Coulomb matrix") for m in _mats(mat))
     n_alpha, n_beta = nelec
     _lib.call("ffgb_contract_diag_coulomb", p.ptr(), out.data_ptr(), p.dtype_code, norb, n_alpha, n_beta,
               _lib.dptr(aa), _lib.dptr(ab), _lib.dptr(bb), int(bool(z_representation)), 0,
@@ -40,7 +40,7 @@ def contract_num_op_sum(vec, coeffs, norb: int, nelec: tuple[int, int]):
     (python/ffsim/contract/num_op_sum.py:27-72)."""
     p = prepare(vec, norb, nelec, copy=False)
     out = torch.empty_like(p.tensor)
-    c = _lib.rmat(coeffs)
+    c = _lib.rmat(coeffs, (norb,), "coefficients")
     n_alpha, n_beta = nelec
     _lib.call("ffgb_contract_num_op_sum", p.ptr(), out.data_ptr(), p.dtype_code, norb, n_alpha, n_beta,
               _lib.dptr(c), 0, stream_ptr(p.tensor))
@@ -53,7 +53,9 @@ def _rotated_matvec(vec: torch.Tensor, norb, nelec, one_body, mat, z_rep, rot):
     out = torch.empty_like(t)
     code = _lib.FFGB_C64 if t.dtype == torch.complex64 else _lib.FFGB_C128
     buf, nbytes = scratch(t, 1, norb, n_alpha, n_beta)
-    ob, m, r = _lib.rmat(one_body), _lib.rmat(mat), _lib.cmat(rot)
+    ob = _lib.rmat(one_body, (norb,), "coefficients")
+    m = _lib.rmat(mat, (norb, norb), "diagonal Coulomb matrix")
+    r = _lib.cmat(rot, (norb, norb), "orbital rotation")
     _lib.call("ffgb_rotated_diag_matvec", t.data_ptr(), out.data_ptr(), code, norb, n_alpha, n_beta,
               _lib.dptr(ob), _lib.dptr(m), int(bool(z_rep)), _lib.dptr(r), 0, buf.data_ptr(), nbytes,
               stream_ptr(t))

@@ -31,9 +31,13 @@ class LUCJEnergy:
 
     def __call__(self, ucj: UCJOpSpinBalanced, ham: DoubleFactorizedHamiltonian, vec=None) -> float:
         n_alpha, n_beta = self.nelec
-        dcm = _lib.rmat(ucj.diag_coulomb_mats)
-        rots = _lib.cmat(ucj.orbital_rotations)
-        final = _lib.cmat(ucj.final_orbital_rotation)
+        norb = self.norb
+        if ucj.norb != norb or ham.norb != norb:
+            raise ValueError(f"the evaluator is for {norb} orbitals; got an operator on {ucj.norb} "
+                             f"and a Hamiltonian on {ham.norb}")
+        dcm = _lib.rmat(ucj.diag_coulomb_mats, (ucj.n_reps, 2, norb, norb), "diag_coulomb_mats")
+        rots = _lib.cmat(ucj.orbital_rotations, (ucj.n_reps, norb, norb), "orbital_rotations")
+        final = _lib.cmat(ucj.final_orbital_rotation, (norb, norb), "final_orbital_rotation")
         if ham.z_representation:
             ham = ham.to_number_representation()
         one_body, hdcm, hrots = ham._arrays()

@@ -44,7 +44,8 @@ def apply_orbital_rotation(vec, mat, norb: int, nelec, *, copy: bool = True):
         ma, mb = np.asarray(mat), None
     else:
         ma, mb = _split_pair(mat)
-    ma, mb = _lib.cmat(ma), _lib.cmat(mb)
+    ma = _lib.cmat(ma, (norb, norb), "orbital rotation")
+    mb = _lib.cmat(mb, (norb, norb), "orbital rotation")
     buf, nbytes = scratch(p.tensor, 0, norb, n_alpha, n_beta)
     _lib.call(
         "ffgb_apply_orbital_rotation", p.ptr(), p.dtype_code, norb, n_alpha, n_beta,
@@ -72,14 +73,14 @@ def apply_diag_coulomb_evolution(vec, mat, time: float, norb: int, nelec, *, orb
         raise NotImplementedError
     p = prepare(vec, norb, nelec, copy=copy)
     aa, ab, bb = _split_three(mat)
-    aa, ab, bb = _lib.rmat(aa), _lib.rmat(ab), _lib.rmat(bb)
+    aa, ab, bb = (_lib.rmat(m, (norb, norb), "diagonal Coulomb matrix") for m in (aa, ab, bb))
     ra = rb = None
     if orbital_rotation is not None:
         if n_beta < 0:
             ra = np.asarray(orbital_rotation)
         else:
             ra, rb = _split_pair(orbital_rotation)
-    ra, rb = _lib.cmat(ra), _lib.cmat(rb)
+    ra, rb = (_lib.cmat(r, (norb, norb), "orbital rotation") for r in (ra, rb))
     buf, nbytes = scratch(p.tensor, 0, norb, n_alpha, n_beta)
     _lib.call(
         "ffgb_apply_diag_coulomb_evolution", p.ptr(), p.dtype_code, norb, n_alpha, n_beta,
@@ -101,14 +102,14 @@ def apply_num_op_sum_evolution(vec, coeffs, time: float, norb: int, nelec, *, or
         ca = cb = np.asarray(coeffs)
     else:
         ca, cb = coeffs
-    ca, cb = _lib.rmat(ca), _lib.rmat(cb)
+    ca, cb = (_lib.rmat(c, (norb,), "coefficients") for c in (ca, cb))
     ra = rb = None
     if orbital_rotation is not None:
         if n_beta < 0:
             ra = np.asarray(orbital_rotation)
         else:
             ra, rb = _split_pair(orbital_rotation)
-    ra, rb = _lib.cmat(ra), _lib.cmat(rb)
+    ra, rb = (_lib.cmat(r, (norb, norb), "orbital rotation") for r in (ra, rb))
     buf, nbytes = scratch(p.tensor, 0, norb, n_alpha, n_beta)
     _lib.call(
         "ffgb_apply_num_op_sum_evolution", p.ptr(), p.dtype_code, norb, n_alpha, n_beta,

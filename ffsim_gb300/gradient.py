@@ -106,6 +106,8 @@ class LUCJGradient:
                        with_final_orbital_rotation: bool = False) -> tuple[float, np.ndarray]:
         norb = self.norb
         na, nb = self.nelec
+        if ham.norb != norb:
+            raise ValueError(f"the evaluator is for {norb} orbitals; got a Hamiltonian on {ham.norb}")
         params = np.asarray(params, dtype=float)
         ucj = UCJOpSpinBalanced.from_parameters(params, norb=norb, n_reps=n_reps,
                                                 with_final_orbital_rotation=with_final_orbital_rotation)

@@ -34,10 +34,14 @@ class DoubleFactorizedHamiltonian:
         return self.one_body_tensor.shape[0]
 
     def _arrays(self):
+        n = self.norb
+        dcm = _lib.rmat(self.diag_coulomb_mats)
+        rots = _lib.cmat(self.orbital_rotations)
+        n_terms = dcm.shape[0] if dcm.ndim == 3 else -1
         return (
-            _lib.cmat(self.one_body_tensor),
-            _lib.rmat(self.diag_coulomb_mats).reshape(-1, self.norb, self.norb),
-            _lib.cmat(self.orbital_rotations).reshape(-1, self.norb, self.norb),
+            _lib.cmat(self.one_body_tensor, (n, n), "one_body_tensor"),
+            _lib.rmat(dcm, (n_terms, n, n), "diag_coulomb_mats"),
+            _lib.cmat(rots, (n_terms, n, n), "orbital_rotations"),
         )
 
     def to_z_representation(self) -> "DoubleFactorizedHamiltonian":
@@ -99,6 +103,8 @@ class DoubleFactorizedHamiltonian:
         """GPU counterpart of double_factorized_hamiltonian.py:244-275 (matvec = rmatvec),
         with a fused FP64 ``expectation``."""
         assert isinstance(nelec, tuple)
+        if norb != self.norb:
+            raise ValueError(f"the Hamiltonian acts on {self.norb} orbitals, but norb={norb} was given")
         d = _dim(norb, nelec)
         n_alpha, n_beta = nelec
         one_body, dcm, rots = self._arrays()

@@ -27,6 +27,11 @@ def validate_interaction_pairs(interaction_pairs, ordered: bool) -> None:
                     f"only upper triangular pairs. Got {(i, j)}, which is a lower triangular pair.")
 
 
+def _check_norb(own: int, norb: int) -> None:
+    if own != norb:
+        raise ValueError(f"the operator acts on {own} orbitals, but norb={norb} was given")
+
+
 def orbital_rotation_from_t1_amplitudes(t1: np.ndarray) -> np.ndarray:
     """exp(t1 - t1^dag) embedded in the occupied-virtual block
     (python/ffsim/variational/util.py:38-54)."""
@@ -220,11 +225,12 @@ class UCJOpSpinBalanced:
         merged rotation U_k^dag U_{k-1} then exp(-i(-1) J_k), then the final rotation."""
         if isinstance(nelec, (int, np.integer)):
             return NotImplemented
+        _check_norb(self.norb, norb)
         n_alpha, n_beta = split_nelec(nelec)
         p = prepare(vec, norb, nelec, copy=copy)
-        dcm = _lib.rmat(self.diag_coulomb_mats)
-        rots = _lib.cmat(self.orbital_rotations)
-        final = _lib.cmat(self.final_orbital_rotation)
+        dcm = _lib.rmat(self.diag_coulomb_mats, (self.n_reps, 2, norb, norb), "diag_coulomb_mats")
+        rots = _lib.cmat(self.orbital_rotations, (self.n_reps, norb, norb), "orbital_rotations")
+        final = _lib.cmat(self.final_orbital_rotation, (norb, norb), "final_orbital_rotation")
         buf, nbytes = scratch(p.tensor, 0, norb, n_alpha, n_beta)
         _lib.call("ffgb_ucj_spin_balanced_apply", p.ptr(), p.dtype_code, norb, n_alpha, n_beta,
                   self.n_reps, _lib.dptr(dcm), rots.ctypes.data_as(_lib._dp), _lib.dptr(final),

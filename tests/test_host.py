@@ -196,3 +196,24 @@ def test_argument_errors_map_to_python_exceptions():
     with pytest.raises(NotImplementedError):
         _lib.call("ffgb_apply_orbital_rotation", None, 0, 40, 2, 2, None, None, None, 0, None)
     assert f.dim(16, (8, 8)) == 12870**2
+
+
+def test_mis_sized_inputs_are_rejected_on_the_host():
+    """The C ABI reads norb x norb (or norb) elements through each pointer; the
+    Python layer rejects arrays of another size before any call or launch."""
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _lib
+
+    with pytest.raises(ValueError, match="orbital rotation"):
+        _lib.cmat(np.eye(3), (4, 4), "orbital rotation")
+    assert _lib.cmat(None, (4, 4)) is None
+    assert _lib.rmat(np.zeros(4), (4,)).shape == (4,)
+    ham = f.random.random_double_factorized_hamiltonian(4, rank=2, seed=1)
+    with pytest.raises(ValueError):
+        f.linear_operator(ham, 5, (2, 2))
+    bad = f.DoubleFactorizedHamiltonian(np.eye(4), np.zeros((2, 4, 4)), np.zeros((3, 4, 4), dtype=complex))
+    with pytest.raises(ValueError):
+        bad._arrays()
+    ucj = f.random.random_ucj_op_spin_balanced(4, n_reps=1, seed=2)
+    with pytest.raises(ValueError):
+        f.apply_unitary(np.zeros(100, dtype=complex), ucj, 5, (2, 2))
