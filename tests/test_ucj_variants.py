@@ -220,7 +220,7 @@ def test_gpu_from_t_amplitudes_golden(cuda, golden):
         for tag, kw in [("a", {}), ("b", {"n_reps": 2, "t1": t1}), ("c", {"n_reps": 40})]:
             op = f.UCJOpSpinBalanced.from_t_amplitudes(t2, **kw)
             vin = golden[f"t2{idx}_op{tag}_in"]
-            for dtype, tol in [(torch.complex128, 1e-10), (torch.complex64, 5e-5)]:
+            for dtype, tol in [(torch.complex128, 1e-10), (torch.complex64, 1e-4)]:
                 v = torch.from_numpy(vin).to("cuda").to(dtype)
                 out = f.apply_unitary(v, op, norb, (nocc, nocc))
                 np.testing.assert_allclose(out.cpu().numpy().astype(complex), golden[f"t2{idx}_op{tag}_out"],
