@@ -27,6 +27,7 @@ from ffsim_gb300.states import (
     slater_determinant,
     slater_determinant_amplitudes,
     slater_determinant_rdms,
+    spin_square,
     vdot,
 )
 from ffsim_gb300.trotter import simulate_trotter_diag_coulomb_split_op, simulate_trotter_double_factorized
@@ -65,6 +66,7 @@ __all__ = [
     "slater_determinant",
     "slater_determinant_amplitudes",
     "slater_determinant_rdms",
+    "spin_square",
     "states",
     "trace",
     "vdot",

@@ -10,10 +10,10 @@ import numpy as np
 import torch
 
 from ffsim_gb300 import _lib
-from ffsim_gb300._state import dim, dims, stream_ptr
+from ffsim_gb300._state import dim, dims, prepare, split_nelec, stream_ptr
 
 __all__ = ["dim", "dims", "make_strings", "hartree_fock_state", "vdot", "addresses_to_strings",
-           "slater_determinant", "slater_determinant_rdms", "slater_determinant_amplitudes"]
+           "slater_determinant", "slater_determinant_rdms", "slater_determinant_amplitudes", "spin_square"]
 
 
 @lru_cache(maxsize=None)
@@ -163,3 +163,31 @@ def slater_determinant_amplitudes(bitstrings, norb: int, occupied_orbitals, orbi
     else:
         rot_a, rot_b = orbital_rotation
     return sector(strings_a, orbs_a, rot_a) * sector(strings_b, orbs_b, rot_b)
+
+
+def spin_square(fcivec, norb: int, nelec: tuple[int, int]) -> float:
+    r""":math:`\langle\psi|S^2|\psi\rangle` of an unnormalised state
+    (python/ffsim/states/states.py:52-59).
+
+    :math:`S^2 = S_- S_+ + S_z(S_z + 1)` and :math:`S_- S_+ = N_\beta - \sum_{pq}
+    E^\alpha_{qp} E^\beta_{pq}`, so :math:`\langle S^2\rangle = (S_z(S_z+1) + N_\beta)
+    \langle\psi|\psi\rangle - \sum_{pq} \langle E^\alpha_{pq}\psi | E^\beta_{pq}\psi\rangle`:
+    per orbital pair two single-excitation launches (``ffgb_apply_excitation``)
+    and one FP64 inner product (``ffgb_vdot``) on the device."""
+    n_alpha, n_beta = split_nelec(nelec)
+    if n_beta < 0:
+        raise ValueError("spin_square needs the electron numbers of both spin sectors")
+    p = prepare(fcivec, norb, (n_alpha, n_beta), copy=False)
+    t = p.tensor.reshape(-1)
+    code = _lib.FFGB_C64 if t.dtype == torch.complex64 else _lib.FFGB_C128
+    xa, xb = torch.empty_like(t), torch.empty_like(t)
+    cross = 0.0
+    if n_alpha and n_beta:
+        for orb_p in range(norb):
+            for orb_q in range(norb):
+                for spin, x in ((0, xa), (1, xb)):
+                    _lib.call("ffgb_apply_excitation", t.data_ptr(), x.data_ptr(), code, norb, n_alpha, n_beta,
+                              spin, orb_p, orb_q, stream_ptr(t))
+                cross += vdot(xa, xb).real
+    sz = 0.5 * (n_alpha - n_beta)
+    return (sz * (sz + 1) + n_beta) * vdot(t, t).real - cross

@@ -646,6 +646,37 @@ def _apply_excitation(v2, norb, nelec, p, q, spin):
     return out
 
 
+def spin_square(vec, norb, nelec):
+    """<psi|S^2|psi> (unnormalised, python/ffsim/states/states.py:52-59) from
+    S^2 = S_- S_+ + S_z (S_z + 1), with <psi|S_- S_+|psi> = |S_+ psi|^2 and
+    S_+ = sum_p a+_{p alpha} a_{p beta} applied string by string into the
+    (n_alpha + 1, n_beta - 1) sector.  States are a+_alpha... a+_beta... |0>,
+    so a_{p beta} passes all n_alpha alpha operators and the beta ones below
+    p, and a+_{p alpha} the alpha ones below p."""
+    na, nb = nelec
+    v2 = np.asarray(vec, dtype=complex).reshape(math.comb(norb, na), math.comb(norb, nb))
+    sz = 0.5 * (na - nb)
+    norm2 = float(np.vdot(v2, v2).real)
+    if nb == 0 or na == norb:
+        return sz * (sz + 1) * norm2
+    sa, sb = make_strings(norb, na), make_strings(norb, nb)
+    ta, tb = make_strings(norb, na + 1), make_strings(norb, nb - 1)
+    ia = {int(x): k for k, x in enumerate(ta)}
+    ib = {int(x): k for k, x in enumerate(tb)}
+    out = np.zeros((len(ta), len(tb)), dtype=complex)
+    for i, a in enumerate(sa):
+        a = int(a)
+        for j, b in enumerate(sb):
+            b = int(b)
+            for orb in range(norb):
+                if not (b >> orb) & 1 or (a >> orb) & 1:
+                    continue
+                below = (1 << orb) - 1
+                sign = (-1) ** (na + bin(b & below).count("1") + bin(a & below).count("1"))
+                out[ia[a | (1 << orb)], ib[b & ~(1 << orb)]] += sign * v2[i, j]
+    return float(np.vdot(out, out).real) + sz * (sz + 1) * norm2
+
+
 def one_body_action(vec, mat, norb, nelec):
     """sum_{pq} M_pq (a+_{p alpha} a_{q alpha} + a+_{p beta} a_{q beta}) vec."""
     na, nb = nelec

@@ -64,3 +64,75 @@ def test_gpu_rotated_vectors(cuda, golden):
                          (f.slater_determinant(5, ([2, 0], [1]), (u, None), dtype=dtype), "sl_vec_pair"),
                          (f.slater_determinant(5, [4, 1], v, dtype=dtype), "sl_vec_spinless_rot")]:
             np.testing.assert_allclose(got.cpu().numpy().astype(complex), golden[key], atol=tol)
+
+
+def test_spin_square_oracle_known_answers():
+    """S^2 of high-spin and closed-shell configurations and of the two
+    open-shell combinations (the oracle builds S_+ psi string by string)."""
+    from oracle import ffsim_oracle as o
+
+    assert abs(o.spin_square(o.hartree_fock_state(3, (2, 0)), 3, (2, 0)) - 2.0) < 1e-12
+    assert abs(o.spin_square(o.hartree_fock_state(4, (2, 2)), 4, (2, 2))) < 1e-12
+    vals = []
+    for sgn in (1, -1):
+        v = np.zeros(4, dtype=complex)
+        v[1], v[2] = 1 / np.sqrt(2), sgn / np.sqrt(2)
+        vals.append(o.spin_square(v, 2, (1, 1)))
+    np.testing.assert_allclose(sorted(vals), [0.0, 2.0], atol=1e-12)
+
+
+def test_spin_square_host_sequence(monkeypatch):
+    """The commutator form the GPU composition evaluates, with the excitation
+    and inner-product entry points replaced by the oracle's, equals the
+    oracle's S_+ construction."""
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _state
+    from ffsim_gb300 import states as st
+    from oracle import ffsim_oracle as o
+
+    tensors = {}
+
+    def keep(t):
+        tensors[t.data_ptr()] = t
+        return t
+
+    def fake_call(name, src, dst, _code, norb, na, nb, spin, p, q, _stream):
+        assert name == "ffgb_apply_excitation"
+        v2 = tensors[src].numpy().reshape(o.dim(norb, na), o.dim(norb, nb))
+        tensors[dst].copy_(torch.from_numpy(o._apply_excitation(v2, norb, (na, nb), p, q, spin).reshape(-1)))
+
+    def prep(vec, norb, nelec, *, copy):
+        arr = np.array(vec, dtype=complex)
+        return _state.Prepared(keep(torch.from_numpy(arr)), arr.shape, True)
+
+    real_empty_like = torch.empty_like
+    monkeypatch.setattr(st._lib, "call", fake_call)
+    monkeypatch.setattr(st, "prepare", prep)
+    monkeypatch.setattr(st, "stream_ptr", lambda t: 0)
+    monkeypatch.setattr(st, "vdot", lambda x, y: complex(np.vdot(x.numpy(), y.numpy())))
+    monkeypatch.setattr(st.torch, "empty_like", lambda t: keep(real_empty_like(t)))
+    rng = np.random.default_rng(5)
+    for norb, ne in [(4, (2, 2)), (5, (3, 2)), (4, (1, 3)), (3, (0, 2))]:
+        d = o.dim(norb, ne)
+        v = rng.standard_normal(d) + 1j * rng.standard_normal(d)
+        assert abs(f.spin_square(v, norb, ne) - o.spin_square(v, norb, ne)) < 1e-10
+
+
+@pytest.mark.gpu
+def test_gpu_spin_square(cuda):
+    import torch
+
+    import ffsim_gb300 as f
+    from oracle import ffsim_oracle as o
+
+    rng = np.random.default_rng(6)
+    for norb, ne in [(4, (2, 2)), (5, (3, 2)), (6, (1, 4))]:
+        d = o.dim(norb, ne)
+        v = rng.standard_normal(d) + 1j * rng.standard_normal(d)
+        exp = o.spin_square(v, norb, ne)
+        assert abs(f.spin_square(v, norb, ne) - exp) < 1e-10 * max(1.0, abs(exp))
+        t = torch.from_numpy(v / np.linalg.norm(v)).to("cuda").to(torch.complex64)
+        assert abs(f.spin_square(t, norb, ne) - exp / np.vdot(v, v).real) < 1e-4
+    assert abs(f.spin_square(f.hartree_fock_state(6, (3, 3)), 6, (3, 3))) < 1e-12
