@@ -334,3 +334,28 @@ def test_banded_and_near_identity_rotations(cuda, norb, nelec):
         np.testing.assert_allclose(_n(out), ref, atol=TOL64)
         out = f.apply_orbital_rotation(_t(vec, torch.complex128), (u, u.conj()), norb, nelec)
         np.testing.assert_allclose(_n(out), ref, atol=TOL128)
+
+
+@pytest.mark.parametrize("norb, nelec", NORB_NELEC_CASES)
+def test_num_op_sum_eigenphase_kat(cuda, norb, nelec):
+    """Every configuration is an eigenvector: exp(-i t sum of its occupied
+    coefficients), per spin selection (tests/python/gates/num_op_sum_test.py:27-72),
+    in both precisions, one configuration per call."""
+    import itertools
+
+    import ffsim_gb300 as f
+
+    rng = np.random.default_rng(norb * 13 + sum(nelec))
+    coeffs = rng.standard_normal(norb)
+    time = rng.standard_normal()
+    na, nb = nelec
+    for spin in (1, 2, 3):
+        pair = (coeffs if spin & 1 else None, coeffs if spin & 2 else None)
+        for occ_a in itertools.combinations(range(norb), na):
+            for occ_b in itertools.combinations(range(norb), nb):
+                eig = (coeffs[list(occ_a)].sum() if spin & 1 else 0.0) + (coeffs[list(occ_b)].sum() if spin & 2 else 0.0)
+                for dtype, tol in DTYPES:
+                    state = f.slater_determinant(norb, (list(occ_a), list(occ_b)), dtype=dtype)
+                    exp = np.exp(-1j * eig * time) * _n(state)
+                    out = f.apply_num_op_sum_evolution(state, pair, time, norb, nelec)
+                    np.testing.assert_allclose(_n(out), exp, atol=tol)

@@ -155,6 +155,29 @@ def test_diag_coulomb_eigenphase_kat(norb, nelec):
             np.testing.assert_allclose(res, np.exp(-1j * eig * time) * state, atol=1e-12)
 
 
+@pytest.mark.parametrize("norb, nelec", NORB_NELEC_CASES)
+def test_num_op_sum_eigenphase_kat(norb, nelec):
+    """Closed form on Slater determinants (tests/python/gates/num_op_sum_test.py:27-72):
+    each configuration picks up exp(-i t sum of its occupied coefficients) in
+    the sectors the coefficients act on; spinless as the (n, 0) sector."""
+    rng = np.random.default_rng(norb * 11 + sum(nelec))
+    coeffs = rng.standard_normal(norb)
+    time = rng.standard_normal()
+    na, nb = nelec
+    da, db = math.comb(norb, na), math.comb(norb, nb)
+    for spin in (1, 2, 3):
+        pair = (coeffs if spin & 1 else np.zeros(norb), coeffs if spin & 2 else np.zeros(norb))
+        for occ_a in itertools.combinations(range(norb), na):
+            for occ_b in itertools.combinations(range(norb), nb):
+                a_addr = list(o.make_strings(norb, na)).index(sum(1 << i for i in occ_a))
+                b_addr = list(o.make_strings(norb, nb)).index(sum(1 << i for i in occ_b))
+                state = np.zeros(da * db, dtype=complex)
+                state[a_addr * db + b_addr] = 1
+                eig = pair[0][list(occ_a)].sum() + pair[1][list(occ_b)].sum()
+                res = o.apply_num_op_sum_evolution(state, pair, time, norb, nelec)
+                np.testing.assert_allclose(res, np.exp(-1j * eig * time) * state, atol=1e-12)
+
+
 def _trotter_case(golden, idx, row):
     n, a, b, t, steps, order, z = row
     g = lambda s: golden[f"trot{idx}_{s}"]  # noqa: E731
