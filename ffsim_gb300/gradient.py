@@ -34,7 +34,7 @@ import numpy as np
 import torch
 
 from ffsim_gb300 import _lib
-from ffsim_gb300._state import dim, scratch
+from ffsim_gb300._state import dim
 from ffsim_gb300.hamiltonians import DoubleFactorizedHamiltonian
 from ffsim_gb300.linalg import antihermitians_from_parameters
 from ffsim_gb300.variational import UCJOpSpinBalanced
