@@ -11,6 +11,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <initializer_list>
 #include <vector>
 
 #include "../../include/ffsim_gb300.h"
@@ -1134,6 +1135,14 @@ static int df_terms(int norb, const double* one_body, int n_terms, const double*
   return FFGB_OK;
 }
 
+// Every state has at least one amplitude, so its device buffers are never
+// optional: a NULL pointer is refused here instead of reaching a kernel.
+static int need_buffers(std::initializer_list<const void*> ptrs) {
+  for (const void* ptr : ptrs)
+    if (!ptr) return fail(FFGB_ERR_ARG, "a required buffer is NULL");
+  return FFGB_OK;
+}
+
 static int check_shape(int dtype, int norb, int na, int nb) {
   if (dtype != FFGB_C64 && dtype != FFGB_C128) return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
   if (norb < 0 || norb > FFGB_MAXN) return fail(FFGB_ERR_UNSUPPORTED, "norb must be in [0, 18]");
@@ -1255,6 +1264,7 @@ static int contract_static_impl(const void* vec, void* out, int norb, int na, in
                                   "ffgb_contract_diag_coulomb_static holds " +
                                   std::to_string((size_t)FFGB_STATIC_SCRATCH_BYTES) +
                                   " (use ffgb_contract_diag_coulomb)");
+  FFGB_TRY(need_buffers({vec, out}));
   if (da <= 0 || db <= 0) return FFGB_OK;
   void* base = nullptr;
   FFGB_TRY(static_scratch(&base));
@@ -1432,6 +1442,7 @@ int ffgb_debug_stage(void* vec, int dtype, int norb, int na, int nb, const doubl
                      void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec}));
   if (dtype != FFGB_C64 || nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "stage kernels run on spinful complex64 states");
   if (!mat) return fail(FFGB_ERR_ARG, "mat must not be NULL");
   SectorPlan p;
@@ -1464,6 +1475,7 @@ int ffgb_apply_givens_rotation(void* vec, int dtype, int norb, int na, int nb, i
                                double s_re, double s_im, int i, int j, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec}));
   if (spin != 0 && spin != 1) return fail(FFGB_ERR_ARG, "spin must be 0 (alpha) or 1 (beta)");
   if (nb < 0 && spin != 0) return fail(FFGB_ERR_ARG, "spinless systems have one sector");
   cudaStream_t st = (cudaStream_t)stream;
@@ -1475,6 +1487,7 @@ int ffgb_apply_phase_shift(void* vec, int dtype, int norb, int na, int nb, int s
                            double pi, int orb, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec}));
   if (orb < 0 || orb >= norb) return fail(FFGB_ERR_ARG, "orbital index out of range");
   cudaStream_t st = (cudaStream_t)stream;
   const int nocc = (spin == 0 || nb < 0) ? na : nb;
@@ -1523,6 +1536,7 @@ int ffgb_apply_orbital_rotation(void* vec, int dtype, int norb, int na, int nb, 
                                 const double* mb, void* scratch, size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec}));
   Scratch scr(scratch, scratch_bytes);
   cudaStream_t st = (cudaStream_t)stream;
   return FFGB_DISPATCH(dtype, orbital_rotation_impl<float>(vec, norb, na, nb, ma, mb, scr, st),
@@ -1536,6 +1550,7 @@ int ffgb_apply_diag_coulomb_evolution(void* vec, int dtype, int norb, int na, in
                                       void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec}));
   if (nb < 0 && zrep) return fail(FFGB_ERR_UNSUPPORTED, "Z representation needs a spinful system");
   DiagSpec spec = diag_coulomb_spec(norb, aa, nb < 0 ? nullptr : ab, nb < 0 ? nullptr : bb, zrep,
                                     -time, DIAG_PHASE);
@@ -1552,6 +1567,7 @@ int ffgb_apply_num_op_sum_evolution(void* vec, int dtype, int norb, int na, int 
                                     size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec}));
   DiagSpec spec = one_body_spec(norb, ca, nb < 0 ? nullptr : cb, -time, DIAG_PHASE);
   Scratch scr(scratch, scratch_bytes);
   cudaStream_t st = (cudaStream_t)stream;
@@ -1565,6 +1581,7 @@ int ffgb_ucj_spin_balanced_apply(void* vec, int dtype, int norb, int na, int nb,
                                  void* scratch, size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "spin-balanced UCJ needs a spinful system");
   Scratch scr(scratch, scratch_bytes);
   cudaStream_t st = (cudaStream_t)stream;
@@ -1598,6 +1615,7 @@ int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, 
                                int accumulate, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec, out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "contraction needs a spinful system");
   DiagSpec spec = diag_coulomb_spec(norb, aa, ab, bb, zrep, 1.0, DIAG_COEF);
   char buf[1];
@@ -1631,6 +1649,7 @@ int ffgb_contract_num_op_sum(const void* vec, void* out, int dtype, int norb, in
                              const double* coeffs, int accumulate, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec, out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "contraction needs a spinful system");
   DiagSpec spec = one_body_spec(norb, coeffs, coeffs, 1.0, DIAG_COEF);
   cudaStream_t st = (cudaStream_t)stream;
@@ -1649,6 +1668,7 @@ int ffgb_rotated_diag_matvec(const void* vec, void* out, int dtype, int norb, in
                              int accumulate, void* scratch, size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec, out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "linear operator needs a spinful system");
   DiagSpec spec;
   spec.mode = DIAG_COEF;
@@ -1668,6 +1688,7 @@ int ffgb_df_matvec(const void* vec, void* out, int dtype, int norb, int na, int 
                    double constant, int zrep, void* scratch, size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec, out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "linear operator needs a spinful system");
   if (vec == out) return fail(FFGB_ERR_ARG, "out must not alias vec");
   std::vector<Term> terms;
@@ -1699,6 +1720,7 @@ int ffgb_df_expectation(const void* vec, int dtype, int norb, int na, int nb, co
                         size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec, energy_out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "expectation needs a spinful system");
   std::vector<Term> terms;
   df_terms(norb, one_body, n_terms, dcm, rots, zrep, terms);
@@ -1718,6 +1740,7 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
                      void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({work, energy_out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "LUCJ energy needs a spinful system");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t el = dtype == FFGB_C128 ? 16 : 8;
@@ -1763,6 +1786,7 @@ int ffgb_transition_rdm1(const void* x, const void* y, int dtype, int norb, int 
                          void* scratch, size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({x, y, out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "densities need a spinful system");
   if (!out) return fail(FFGB_ERR_ARG, "out must not be NULL");
   Scratch scr(scratch, scratch_bytes);
@@ -1775,6 +1799,7 @@ int ffgb_pair_density(const void* x, const void* y, int dtype, int norb, int na,
                       void* scratch, size_t scratch_bytes, void* stream) {
   g_err.clear();
   FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({x, y, out}));
   if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "densities need a spinful system");
   if (!out) return fail(FFGB_ERR_ARG, "out must not be NULL");
   Scratch scr(scratch, scratch_bytes);
@@ -1785,6 +1810,7 @@ int ffgb_pair_density(const void* x, const void* y, int dtype, int norb, int na,
 
 int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out, void* stream) {
   g_err.clear();
+  FFGB_TRY(need_buffers({x, y, out}));
   cudaStream_t st = (cudaStream_t)stream;
   const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 1024));
   if (dtype != FFGB_C64 && dtype != FFGB_C128)
@@ -1813,6 +1839,9 @@ int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out,
 
 int ffgb_hartree_fock(void* vec, int dtype, long long n, void* stream) {
   g_err.clear();
+  if (dtype != FFGB_C64 && dtype != FFGB_C128)
+    return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
+  FFGB_TRY(need_buffers({vec}));
   cudaStream_t st = (cudaStream_t)stream;
   const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4096));
   if (dtype == FFGB_C64)

@@ -6,7 +6,10 @@
  * run asynchronously on the given CUDA stream (cudaStream_t passed as void*,
  * NULL = legacy default stream).  Complex arrays are interleaved
  * (re, im) pairs.  Host matrices are row-major complex128 (norb*norb*2
- * doubles) unless stated otherwise.
+ * doubles) unless stated otherwise.  State, output and result buffers are
+ * never optional (a state has at least one amplitude): NULL for any of them
+ * returns FFGB_ERR_ARG before anything is launched; only the arguments
+ * documented as "NULL = ..." may be NULL.
  *
  * State layout (identical to ffsim): a spinful state is a C-contiguous
  * (dim_a, dim_b) array; row = alpha string address, column = beta string

@@ -217,3 +217,21 @@ def test_mis_sized_inputs_are_rejected_on_the_host():
     ucj = f.random.random_ucj_op_spin_balanced(4, n_reps=1, seed=2)
     with pytest.raises(ValueError):
         f.apply_unitary(np.zeros(100, dtype=complex), ucj, 5, (2, 2))
+
+
+def test_null_buffers_are_refused_before_any_launch():
+    """A NULL state, output or result pointer is an argument error on the host
+    (this runs without a GPU: the check comes before any CUDA call)."""
+    from ffsim_gb300 import _lib
+
+    with pytest.raises(ValueError):
+        _lib.call("ffgb_apply_orbital_rotation", None, 0, 4, 2, 2, None, None, None, 0, None)
+    with pytest.raises(ValueError):
+        _lib.call("ffgb_apply_diag_coulomb_evolution", None, 1, 4, 2, 2, None, None, None, 0.5, 0, None, None,
+                  None, 0, None)
+    with pytest.raises(ValueError):
+        _lib.call("ffgb_vdot", None, None, 0, 10, None, None)
+    with pytest.raises(ValueError):
+        _lib.call("ffgb_hartree_fock", None, 0, 10, None)
+    with pytest.raises(TypeError):
+        _lib.call("ffgb_hartree_fock", None, 5, 10, None)
