@@ -65,11 +65,17 @@ def trace(obj: Any, norb: int, nelec) -> float:
 class LinearOperator:
     """A (dim x dim) operator acting on CUDA state vectors.
 
-    ``matvec`` / ``rmatvec`` / ``@`` accept torch CUDA complex tensors (the
-    result has the same dtype) or numpy arrays (moved to the GPU; a numpy
-    array is returned).  Like the reference's SciPy operators, the shape is
-    ``(dim, dim)`` and ``dtype`` is complex.
+    ``matvec`` / ``rmatvec`` / ``@`` accept torch complex tensors (the result
+    has the same dtype and device) or numpy arrays (a numpy array is
+    returned).  A vector has ``dim`` entries in any shape; a ``(dim, k)``
+    array is applied column by column.  Anything else raises ``ValueError``
+    before the library sees a pointer.  Like the reference's SciPy operators,
+    the shape is ``(dim, dim)`` and ``dtype`` is complex, and
+    ``scipy.sparse.linalg`` routines accept the object through
+    ``aslinearoperator``.
     """
+
+    device = "cuda"  # where the library's kernels run
 
     def __init__(self, shape: tuple[int, int], matvec: Callable, rmatvec: Callable | None = None,
                  expectation: Callable | None = None, dtype=complex):
@@ -79,16 +85,26 @@ class LinearOperator:
         self._rmatvec = rmatvec or matvec
         self._expectation = expectation
 
+    def _on_device(self, t: torch.Tensor) -> torch.Tensor:
+        if t.dtype not in (torch.complex64, torch.complex128):
+            t = t.to(torch.complex128)
+        return t.to(self.device)
+
+    def _apply(self, fn, t: torch.Tensor) -> torch.Tensor:
+        n = self.shape[1]
+        if t.dim() == 2 and t.shape[0] == n and t.shape[1] != 1:
+            return torch.stack([fn(self._on_device(t[:, k]).contiguous()) for k in range(t.shape[1])], dim=1)
+        if t.numel() != n:
+            raise ValueError(f"dimension mismatch: the operator is {self.shape}, the input has shape {tuple(t.shape)}")
+        return fn(self._on_device(t).reshape(-1)).reshape(t.shape)
+
     def _run(self, fn, vec):
         if isinstance(vec, torch.Tensor):
-            return fn(vec)
+            return self._apply(fn, vec).to(vec.device)
         arr = np.asarray(vec)
-        if arr.ndim == 2 and arr.shape[1] == 1:
-            arr = arr[:, 0]
         if not np.iscomplexobj(arr):
             arr = arr.astype(np.complex128)
-        t = torch.from_numpy(np.ascontiguousarray(arr)).to("cuda")
-        return fn(t).cpu().numpy()
+        return self._apply(fn, torch.from_numpy(np.ascontiguousarray(arr))).cpu().numpy()
 
     def matvec(self, vec):
         return self._run(self._matvec, vec)
@@ -101,11 +117,13 @@ class LinearOperator:
 
     def expectation(self, vec) -> float:
         """Real part of <vec|A|vec> in FP64 (fused when the operator supports it)."""
+        t = vec if isinstance(vec, torch.Tensor) else torch.from_numpy(
+            np.ascontiguousarray(np.asarray(vec, dtype=complex)))
+        if t.numel() != self.shape[1]:
+            raise ValueError(f"dimension mismatch: the operator is {self.shape}, the input has shape {tuple(t.shape)}")
+        v = self._on_device(t).reshape(-1).contiguous()
         if self._expectation is not None:
-            if not isinstance(vec, torch.Tensor):
-                vec = torch.from_numpy(np.ascontiguousarray(np.asarray(vec, dtype=complex))).to("cuda")
-            return float(self._expectation(vec))
+            return float(self._expectation(v))
         from ffsim_gb300.states import vdot
 
-        v = vec if isinstance(vec, torch.Tensor) else torch.from_numpy(np.asarray(vec, dtype=complex)).to("cuda")
         return float(vdot(v, self._matvec(v)).real)

@@ -235,3 +235,48 @@ def test_null_buffers_are_refused_before_any_launch():
         _lib.call("ffgb_hartree_fock", None, 0, 10, None)
     with pytest.raises(TypeError):
         _lib.call("ffgb_hartree_fock", None, 5, 10, None)
+
+
+def test_linear_operator_inputs_and_scipy_interop(monkeypatch):
+    """Vector-length checks, column-by-column application, device and dtype
+    round trips, and SciPy's aslinearoperator / eigsh / expm_multiply on the
+    operator (a dense Hermitian matrix stands in for the kernels, on the CPU)."""
+    import scipy.sparse.linalg as sla
+    import torch
+
+    from ffsim_gb300.protocols import LinearOperator
+
+    monkeypatch.setattr(LinearOperator, "device", "cpu")
+    rng = np.random.default_rng(4)
+    n = 12
+    g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    h = (g + g.conj().T) / 2
+    ht = torch.from_numpy(h)
+
+    def mv(t):
+        assert t.dim() == 1 and t.numel() == n
+        return (ht.to(t.dtype) @ t)
+
+    op = LinearOperator((n, n), mv, expectation=lambda v: float(torch.vdot(v, mv(v)).real))
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    np.testing.assert_allclose(op @ x, h @ x, atol=1e-12)
+    np.testing.assert_allclose(op @ x[:, None], (h @ x)[:, None], atol=1e-12)
+    xs = rng.standard_normal((n, 3)) + 0j
+    np.testing.assert_allclose(op.matvec(xs), h @ xs, atol=1e-12)
+    np.testing.assert_allclose(op @ x.real, h @ x.real, atol=1e-12)  # real input promoted
+    got = op @ torch.from_numpy(x).to(torch.complex64)
+    assert got.dtype == torch.complex64 and got.device.type == "cpu"
+    assert abs(op.expectation(x) - np.vdot(x, h @ x).real) < 1e-10
+    for bad in (np.zeros(n + 1, dtype=complex), np.zeros((n - 1, 2), dtype=complex)):
+        with pytest.raises(ValueError, match="dimension mismatch"):
+            op @ bad
+    with pytest.raises(ValueError, match="dimension mismatch"):
+        op.expectation(np.zeros(n - 1, dtype=complex))
+    # SciPy routines take the object as it is
+    lo = sla.aslinearoperator(op)
+    w = sla.eigsh(lo, k=1, which="SA", return_eigenvectors=False)
+    assert abs(w[0] - np.linalg.eigvalsh(h)[0]) < 1e-8
+    import scipy.linalg
+
+    np.testing.assert_allclose(sla.expm_multiply(-0.3j * lo, x, traceA=0.0),
+                               scipy.linalg.expm(-0.3j * h) @ x, atol=1e-10)
