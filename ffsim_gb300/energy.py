@@ -47,6 +47,8 @@ class LUCJEnergy:
             vin = vec.contiguous()
             if vin.dtype != self.dtype:
                 raise TypeError("vec dtype must match the evaluator dtype")
+            if vin.device != self.work.device or vin.numel() != self.work.numel():
+                raise ValueError(f"vec must be a tensor of {self.work.numel()} entries on {self.work.device}")
         stream = torch.cuda.current_stream(self.work.device).cuda_stream
         _lib.call("ffgb_lucj_energy", None if vin is None else vin.data_ptr(), self.work.data_ptr(),
                   self.code, self.norb, n_alpha, n_beta, ucj.n_reps, _lib.dptr(dcm),

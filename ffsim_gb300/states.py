@@ -47,6 +47,8 @@ def vdot(x: torch.Tensor, y: torch.Tensor) -> complex:
     """sum conj(x) y accumulated in FP64 on the device."""
     if x.dtype != y.dtype or x.numel() != y.numel():
         raise ValueError("vdot needs two vectors of the same dtype and size")
+    if not (x.is_cuda and y.is_cuda) or x.dtype not in (torch.complex64, torch.complex128):
+        raise ValueError("vdot needs complex CUDA tensors")
     x = x.contiguous()
     y = y.contiguous()
     out = np.zeros(2)
