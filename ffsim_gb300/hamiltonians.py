@@ -37,6 +37,10 @@ class DoubleFactorizedHamiltonian:
         n = self.norb
         dcm = _lib.rmat(self.diag_coulomb_mats)
         rots = _lib.cmat(self.orbital_rotations)
+        if dcm.ndim == 2:  # one term given as a single matrix
+            dcm = dcm[None]
+        if rots.ndim == 2:
+            rots = rots[None]
         n_terms = dcm.shape[0] if dcm.ndim == 3 else -1
         return (
             _lib.cmat(self.one_body_tensor, (n, n), "one_body_tensor"),
