@@ -75,8 +75,6 @@ class LinearOperator:
     ``aslinearoperator``.
     """
 
-    device = "cuda"  # where the library's kernels run
-
     def __init__(self, shape: tuple[int, int], matvec: Callable, rmatvec: Callable | None = None,
                  expectation: Callable | None = None, dtype=complex):
         self.shape = shape
@@ -86,9 +84,10 @@ class LinearOperator:
         self._expectation = expectation
 
     def _on_device(self, t: torch.Tensor) -> torch.Tensor:
+        """The library's kernels read CUDA memory: a complex CUDA tensor."""
         if t.dtype not in (torch.complex64, torch.complex128):
             t = t.to(torch.complex128)
-        return t.to(self.device)
+        return t.to("cuda")
 
     def _apply(self, fn, t: torch.Tensor) -> torch.Tensor:
         n = self.shape[1]

@@ -237,16 +237,19 @@ def test_null_buffers_are_refused_before_any_launch():
         _lib.call("ffgb_hartree_fock", None, 5, 10, None)
 
 
-def test_linear_operator_inputs_and_scipy_interop(monkeypatch):
+def test_linear_operator_inputs_and_scipy_interop():
     """Vector-length checks, column-by-column application, device and dtype
     round trips, and SciPy's aslinearoperator / eigsh / expm_multiply on the
-    operator (a dense Hermitian matrix stands in for the kernels, on the CPU)."""
+    operator (a dense Hermitian matrix stands in for the kernels, and a
+    subclass keeps the vectors on the CPU)."""
     import scipy.sparse.linalg as sla
     import torch
 
-    from ffsim_gb300.protocols import LinearOperator
+    from ffsim_gb300.protocols import LinearOperator as GpuOperator
 
-    monkeypatch.setattr(LinearOperator, "device", "cpu")
+    class LinearOperator(GpuOperator):
+        def _on_device(self, t):
+            return t.to(torch.complex128) if t.dtype not in (torch.complex64, torch.complex128) else t
     rng = np.random.default_rng(4)
     n = 12
     g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
