@@ -283,3 +283,23 @@ def test_linear_operator_inputs_and_scipy_interop():
 
     np.testing.assert_allclose(sla.expm_multiply(-0.3j * lo, x, traceA=0.0),
                                scipy.linalg.expm(-0.3j * h) @ x, atol=1e-10)
+
+
+@pytest.mark.parametrize("norb, nocc", [(13, 3), (16, 2), (17, 2), (18, 2)])
+def test_stage_sequence_permutations_and_blocks(norb, nocc):
+    """Permutations (cosines and sines exactly 0 or 1) and block-diagonal
+    unitaries take the stage sequence above 12 orbitals too, and the emulated
+    kernels reproduce W(U)."""
+    rng = np.random.default_rng(norb * 5 + nocc)
+    h = norb // 2
+    blk = np.zeros((norb, norb), dtype=complex)
+    blk[:h, :h] = o.random_unitary(h, seed=rng)
+    blk[h:, h:] = o.random_unitary(norb - h, seed=rng)
+    mats = [np.eye(norb)[rng.permutation(norb)].astype(complex), np.eye(norb)[::-1].astype(complex), blk,
+            blk @ np.eye(norb)[rng.permutation(norb)]]
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=rng)
+    for u in mats:
+        plan = _plan(u, True)
+        assert plan["kind"] == 3 and plan["err"] < 1e-10
+        np.testing.assert_allclose(pe.apply_ops(plan, vec, norb, nocc), o.apply_orbital_rotation(vec, u, norb, nocc),
+                                   atol=1e-11)
