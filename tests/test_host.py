@@ -303,3 +303,19 @@ def test_stage_sequence_permutations_and_blocks(norb, nocc):
         assert plan["kind"] == 3 and plan["err"] < 1e-10
         np.testing.assert_allclose(pe.apply_ops(plan, vec, norb, nocc), o.apply_orbital_rotation(vec, u, norb, nocc),
                                    atol=1e-11)
+
+
+@pytest.mark.parametrize("norb, nocc", [(14, 2), (16, 2), (15, 3)])
+def test_sector_kernel_plan_structured_matrices(norb, nocc):
+    """The five-stage form the shared-memory sector kernel runs (complex128 and
+    single-sector calls up to 16 orbitals), for banded, near-identity and
+    permutation unitaries, emulated with the kernel's addressing."""
+    rng = np.random.default_rng(norb * 9 + nocc)
+    mats = [_hopping_evolution(norb, 0.05, 1, seed=norb), _hopping_evolution(norb, 1.0, 2, seed=norb + 1),
+            np.eye(norb)[rng.permutation(norb)].astype(complex), o.random_unitary(norb, seed=rng)]
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=rng)
+    for u in mats:
+        plan = _plan(u, True)  # carries the five-stage fields beside the stage sequence
+        assert plan["kind"] == 3 and plan["err"] < 1e-10
+        np.testing.assert_allclose(pe.apply_plan(plan, vec, norb, nocc), o.apply_orbital_rotation(vec, u, norb, nocc),
+                                   atol=1e-11)
