@@ -20,7 +20,7 @@ from ffsim_gb300.gates import (
     apply_phase_shift_in_place,
 )
 from ffsim_gb300.hamiltonians import DiagonalCoulombHamiltonian, DoubleFactorizedHamiltonian, MolecularHamiltonian
-from ffsim_gb300.protocols import LinearOperator, apply_unitary, diag, linear_operator, trace
+from ffsim_gb300.protocols import LinearOperator, apply_unitary, approx_eq, diag, linear_operator, trace
 from ffsim_gb300.rdm import rdms
 from ffsim_gb300.states import (
     hartree_fock_state,
@@ -51,6 +51,7 @@ __all__ = [
     "apply_orbital_rotation",
     "apply_phase_shift_in_place",
     "apply_unitary",
+    "approx_eq",
     "rdms",
     "simulate_trotter_diag_coulomb_split_op",
     "simulate_trotter_double_factorized",

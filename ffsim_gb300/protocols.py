@@ -39,6 +39,19 @@ def linear_operator(obj: Any, norb: int, nelec):
     raise TypeError(f"Object of type {type(obj)} has no _linear_operator_ method.")
 
 
+def approx_eq(obj: Any, other: Any, rtol: float = 1e-5, atol: float = 1e-8) -> bool:
+    """Whether two objects are equal to the given tolerances (``np.isclose``
+    semantics): ``obj``'s ``_approx_eq_``, else ``other``'s, else ``==``
+    (python/ffsim/protocols/approximate_equality_protocol.py:39-68)."""
+    for a, b in ((obj, other), (other, obj)):
+        method = getattr(a, "_approx_eq_", None)
+        if method is not None:
+            result = method(b, rtol=rtol, atol=atol)
+            if result is not NotImplemented:
+                return result
+    return obj == other
+
+
 def diag(obj: Any, norb: int, nelec) -> np.ndarray:
     """Diagonal entries of ``obj``'s operator
     (python/ffsim/protocols/diagonal_protocol.py:42-50)."""

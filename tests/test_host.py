@@ -319,3 +319,15 @@ def test_sector_kernel_plan_structured_matrices(norb, nocc):
         assert plan["kind"] == 3 and plan["err"] < 1e-10
         np.testing.assert_allclose(pe.apply_plan(plan, vec, norb, nocc), o.apply_orbital_rotation(vec, u, norb, nocc),
                                    atol=1e-11)
+
+
+def test_approx_eq_protocol():
+    import ffsim_gb300 as f
+
+    a = f.random.random_double_factorized_hamiltonian(3, rank=2, seed=1)
+    b = f.DoubleFactorizedHamiltonian(a.one_body_tensor + 1e-10, a.diag_coulomb_mats, a.orbital_rotations,
+                                      constant=a.constant)
+    assert f.approx_eq(a, b) and not f.approx_eq(a, b, rtol=0, atol=1e-12)
+    ucj = f.random.random_ucj_op_spin_balanced(3, seed=2)
+    assert f.approx_eq(ucj, ucj) and not f.approx_eq(ucj, a)
+    assert f.approx_eq(1, 1) and not f.approx_eq(1, 2)
