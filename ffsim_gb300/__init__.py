@@ -10,6 +10,20 @@ hand-written sm_103a kernels through the C ABI in ``include/ffsim_gb300.h``.
 
 from ffsim_gb300 import contract, linalg, random, states
 from ffsim_gb300._state import dim, dims
+from ffsim_gb300.basic_gates import (
+    Spin,
+    apply_fsim_gate,
+    apply_fswap_gate,
+    apply_givens_rotation,
+    apply_hop_gate,
+    apply_num_interaction,
+    apply_num_num_interaction,
+    apply_num_op_prod_interaction,
+    apply_on_site_interaction,
+    apply_quad_ham_evolution,
+    apply_tunneling_interaction,
+    pair_for_spin,
+)
 from ffsim_gb300.energy import LUCJEnergy, lucj_energy
 from ffsim_gb300.gradient import LUCJGradient, lucj_energy_autograd
 from ffsim_gb300.gates import (
@@ -45,7 +59,19 @@ __all__ = [
     "UCJOpSpinBalanced",
     "UCJOpSpinUnbalanced",
     "UCJOpSpinless",
+    "Spin",
     "apply_diag_coulomb_evolution",
+    "apply_fsim_gate",
+    "apply_fswap_gate",
+    "apply_givens_rotation",
+    "apply_hop_gate",
+    "apply_num_interaction",
+    "apply_num_num_interaction",
+    "apply_num_op_prod_interaction",
+    "apply_on_site_interaction",
+    "apply_quad_ham_evolution",
+    "apply_tunneling_interaction",
+    "pair_for_spin",
     "apply_givens_rotation_in_place",
     "apply_num_op_sum_evolution",
     "apply_orbital_rotation",

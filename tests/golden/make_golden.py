@@ -214,8 +214,14 @@ def install_stubs():
     sys.modules["ffsim.linalg"].one_hot = _load("ffsim.linalg.linalg", "linalg/linalg.py").one_hot
     _load("ffsim.states.bitstring", "states/bitstring.py")
     slater = _load("ffsim.states.slater", "states/slater.py")
+    spin_mod = _load("ffsim.states.spin", "states/spin.py")
+    bg = _load("ffsim.gates.basic_gates", "gates/basic_gates.py")
+    qh = _load("ffsim.gates.quad_ham", "gates/quad_ham.py")
     return types.SimpleNamespace(
         random=rnd,
+        Spin=spin_mod.Spin,
+        basic_gates=bg,
+        apply_quad_ham_evolution=qh.apply_quad_ham_evolution,
         slater=slater,
         double_factorized_t2=ldf.double_factorized_t2,
         orbital_rotation_from_t1_amplitudes=sys.modules["ffsim.variational.util"].orbital_rotation_from_t1_amplitudes,
@@ -659,6 +665,33 @@ def main():
     out["sl_amp_spinful"] = sl.slater_determinant_amplitudes(([0b00011, 0b10100], [0b01010, 0b11000]), 5,
                                                              ([0, 1], [2, 3]), (u, v))
     out["sl_amp_spinless"] = sl.slater_determinant_amplitudes([0b00111, 0b11010], 5, [0, 2, 4], v)
+
+    # two-orbital gates (gates/basic_gates.py) and quadratic-Hamiltonian
+    # evolution (gates/quad_ham.py), every spin selection
+    rb = np.random.default_rng(20261211)
+    bgm, spins = ref.basic_gates, [ref.Spin.ALPHA, ref.Spin.BETA, ref.Spin.ALPHA_AND_BETA]
+    for tag, norb, nelec in [("s", 5, (2, 2)), ("u", 4, (2, 1)), ("l", 5, 3)]:
+        vec = orc.random_state_vector(orc.dim(norb, nelec), seed=rb)
+        out[f"bg{tag}_in"] = vec
+        spin_list = spins if isinstance(nelec, tuple) else [ref.Spin.ALPHA_AND_BETA]
+        for k, sp in enumerate(spin_list):
+            out[f"bg{tag}_givens{k}"] = bgm.apply_givens_rotation(vec, 0.7, (0, 2), norb, nelec, sp, phi=0.3)
+            out[f"bg{tag}_num{k}"] = bgm.apply_num_interaction(vec, 0.9, 1, norb, nelec, sp)
+            out[f"bg{tag}_tunnel{k}"] = bgm.apply_tunneling_interaction(vec, 0.4, (3, 1), norb, nelec, sp)
+            out[f"bg{tag}_numnum{k}"] = bgm.apply_num_num_interaction(vec, 1.1, (0, 3), norb, nelec, sp)
+            out[f"bg{tag}_hop{k}"] = bgm.apply_hop_gate(vec, 0.5, (1, 2), norb, nelec, sp)
+            out[f"bg{tag}_fsim{k}"] = bgm.apply_fsim_gate(vec, 0.6, 0.8, (2, 0), norb, nelec, sp)
+            out[f"bg{tag}_fswap{k}"] = bgm.apply_fswap_gate(vec, (1, 3), norb, nelec, sp)
+        m = rb.standard_normal((norb, norb)) + 1j * rb.standard_normal((norb, norb))
+        m = (m + m.conj().T) / 2
+        out[f"bg{tag}_qmat"] = m
+        out[f"bg{tag}_quad"] = ref.apply_quad_ham_evolution(vec, m, 0.4, norb, nelec)
+        if isinstance(nelec, tuple):
+            out[f"bg{tag}_quadpair"] = ref.apply_quad_ham_evolution(vec, (m, None), 0.4, norb, nelec)
+            out[f"bg{tag}_onsite"] = bgm.apply_on_site_interaction(vec, 0.8, 2, norb, nelec)
+            for k, orbs in enumerate([((0, 2), (1,)), ((0, 1, 3), (2, 3)), ((), ()), ((1,), ()), ((0, 1), ()),
+                                      ((), (2, 3)), ((0,), (1,)), ((0, 1, 2), ())]):
+                out[f"bg{tag}_prod{k}"] = bgm.apply_num_op_prod_interaction(vec, 0.45, orbs, norb, nelec)
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
