@@ -24,6 +24,12 @@ from ffsim_gb300.basic_gates import (
     apply_tunneling_interaction,
     pair_for_spin,
 )
+from ffsim_gb300.bitstring import (
+    BitstringType,
+    addresses_to_strings,
+    bitstring_to_occupied_orbitals,
+    strings_to_addresses,
+)
 from ffsim_gb300.energy import LUCJEnergy, lucj_energy
 from ffsim_gb300.gradient import LUCJGradient, lucj_energy_autograd
 from ffsim_gb300.gates import (
@@ -38,6 +44,7 @@ from ffsim_gb300.protocols import LinearOperator, apply_unitary, approx_eq, diag
 from ffsim_gb300.rdm import rdms
 from ffsim_gb300.states import (
     hartree_fock_state,
+    init_cache,
     slater_determinant,
     slater_determinant_amplitudes,
     slater_determinant_rdms,
@@ -59,7 +66,11 @@ __all__ = [
     "UCJOpSpinBalanced",
     "UCJOpSpinUnbalanced",
     "UCJOpSpinless",
+    "BitstringType",
     "Spin",
+    "addresses_to_strings",
+    "bitstring_to_occupied_orbitals",
+    "strings_to_addresses",
     "apply_diag_coulomb_evolution",
     "apply_fsim_gate",
     "apply_fswap_gate",
@@ -86,6 +97,7 @@ __all__ = [
     "dim",
     "dims",
     "hartree_fock_state",
+    "init_cache",
     "linalg",
     "linear_operator",
     "lucj_energy",

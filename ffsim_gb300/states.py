@@ -12,7 +12,7 @@ import torch
 from ffsim_gb300 import _lib
 from ffsim_gb300._state import dim, dims, prepare, split_nelec, stream_ptr
 
-__all__ = ["dim", "dims", "make_strings", "hartree_fock_state", "vdot", "addresses_to_strings",
+__all__ = ["dim", "dims", "make_strings", "init_cache", "hartree_fock_state", "vdot",
            "slater_determinant", "slater_determinant_rdms", "slater_determinant_amplitudes", "spin_square"]
 
 
@@ -29,9 +29,13 @@ def make_strings(norb: int, nocc: int) -> np.ndarray:
     return out
 
 
-def addresses_to_strings(addresses, norb: int, nocc: int) -> np.ndarray:
-    """Bitstrings of the given addresses within one spin sector."""
-    return make_strings(norb, nocc)[np.asarray(addresses)]
+def init_cache(norb: int, nelec: tuple[int, int]) -> None:
+    """Build the host string tables of both sectors ahead of timing
+    (python/ffsim/init_cache.py:25-41).  The kernels rank strings in registers
+    and the library builds its device tables on first use, so only the host
+    tables used by the bitstring and Slater-determinant helpers are made here."""
+    for nocc in nelec:
+        make_strings(norb, int(nocc))
 
 
 def hartree_fock_state(norb: int, nelec, *, dtype=torch.complex128, device="cuda") -> torch.Tensor:

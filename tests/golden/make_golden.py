@@ -101,11 +101,19 @@ def _str2addr(norb, nocc, string):
     return int(np.searchsorted(_make_strings(range(norb), nocc), int(string)))
 
 
+def _addrs2str(norb, nelec, addrs):
+    return _make_strings(range(norb), nelec)[np.asarray(addrs, dtype=np.int64)]
+
+
+def _strs2addr(norb, nelec, strings):
+    return np.searchsorted(_make_strings(range(norb), nelec), np.asarray(strings, dtype=np.int64)).astype(np.int32)
+
+
 def install_stubs():
     _module("pyscf", is_pkg=True)
     _module("pyscf.fci", is_pkg=True)
     _module("pyscf.fci.cistring", {"make_strings": _make_strings, "gen_occslst": _gen_occslst,
-                                   "str2addr": _str2addr})
+                                   "str2addr": _str2addr, "addrs2str": _addrs2str, "strs2addr": _strs2addr})
     _module("pyscf.ci", is_pkg=True)
     jax = _module("jax", {"config": types.SimpleNamespace(update=lambda *a, **k: None)})
     jax.numpy = _module("jax.numpy")
@@ -215,10 +223,12 @@ def install_stubs():
     _load("ffsim.states.bitstring", "states/bitstring.py")
     slater = _load("ffsim.states.slater", "states/slater.py")
     spin_mod = _load("ffsim.states.spin", "states/spin.py")
+    bits = sys.modules["ffsim.states.bitstring"]
     bg = _load("ffsim.gates.basic_gates", "gates/basic_gates.py")
     qh = _load("ffsim.gates.quad_ham", "gates/quad_ham.py")
     return types.SimpleNamespace(
         random=rnd,
+        bitstring=bits,
         Spin=spin_mod.Spin,
         basic_gates=bg,
         apply_quad_ham_evolution=qh.apply_quad_ham_evolution,
@@ -692,6 +702,20 @@ def main():
             for k, orbs in enumerate([((0, 2), (1,)), ((0, 1, 3), (2, 3)), ((), ()), ((1,), ()), ((0, 1), ()),
                                       ((), (2, 3)), ((0,), (1,)), ((0, 1, 2), ())]):
                 out[f"bg{tag}_prod{k}"] = bgm.apply_num_op_prod_interaction(vec, 0.45, orbs, norb, nelec)
+
+    # addresses <-> bitstrings (states/bitstring.py:173-361), every representation
+    bs = ref.bitstring
+    addr_sets = {"s": (5, (2, 3), [0, 7, 42, 99]), "l": (6, 3, [0, 5, 19])}
+    for tag, (norb, nelec, addrs) in addr_sets.items():
+        out[f"bits{tag}_addrs"] = np.asarray(addrs)
+        for t in bs.BitstringType:
+            res = bs.addresses_to_strings(addrs, norb, nelec, bitstring_type=t)
+            out[f"bits{tag}_{t.name}"] = np.asarray(res)
+            if isinstance(nelec, tuple):
+                a, b = bs.addresses_to_strings(addrs, norb, nelec, concatenate=False, bitstring_type=t)
+                out[f"bits{tag}_{t.name}_a"], out[f"bits{tag}_{t.name}_b"] = np.asarray(a), np.asarray(b)
+            back = bs.strings_to_addresses(res, norb, nelec)
+            out[f"bits{tag}_{t.name}_back"] = np.asarray(back)
 
     np.savez_compressed(HERE / "golden.npz", **out)
     print(f"wrote {len(out)} arrays to {HERE / 'golden.npz'}")
