@@ -49,6 +49,9 @@ from ffsim_gb300.states import (
     slater_determinant_amplitudes,
     slater_determinant_rdms,
     spin_square,
+    spinful_to_spinless_rdm1,
+    spinful_to_spinless_rdm2,
+    spinful_to_spinless_vec,
     vdot,
 )
 from ffsim_gb300.trotter import simulate_trotter_diag_coulomb_split_op, simulate_trotter_double_factorized
@@ -106,6 +109,9 @@ __all__ = [
     "slater_determinant_amplitudes",
     "slater_determinant_rdms",
     "spin_square",
+    "spinful_to_spinless_rdm1",
+    "spinful_to_spinless_rdm2",
+    "spinful_to_spinless_vec",
     "states",
     "trace",
     "vdot",

@@ -13,7 +13,8 @@ from ffsim_gb300 import _lib
 from ffsim_gb300._state import dim, dims, prepare, split_nelec, stream_ptr
 
 __all__ = ["dim", "dims", "make_strings", "init_cache", "hartree_fock_state", "vdot",
-           "slater_determinant", "slater_determinant_rdms", "slater_determinant_amplitudes", "spin_square"]
+           "slater_determinant", "slater_determinant_rdms", "slater_determinant_amplitudes", "spin_square",
+           "spinful_to_spinless_vec", "spinful_to_spinless_rdm1", "spinful_to_spinless_rdm2"]
 
 
 @lru_cache(maxsize=None)
@@ -197,3 +198,50 @@ def spin_square(fcivec, norb: int, nelec: tuple[int, int]) -> float:
                 cross += vdot(xa, xb).real
     sz = 0.5 * (n_alpha - n_beta)
     return (sz * (sz + 1) + n_beta) * vdot(t, t).real - cross
+
+
+def spinful_to_spinless_vec(vec, norb: int, nelec: tuple[int, int]):
+    """The same state on 2 norb spinless orbitals, alpha orbitals first
+    (python/ffsim/states/states.py): the amplitude of (alpha string a, beta
+    string b) moves to the spinless string (b << norb) | a.  numpy in, numpy
+    out; a torch tensor stays on its device."""
+    from ffsim_gb300.bitstring import addresses_to_strings, strings_to_addresses
+
+    n_old = dim(norb, nelec)
+    strings = addresses_to_strings(range(n_old), norb, nelec)
+    addrs = strings_to_addresses(strings, 2 * norb, sum(nelec))
+    n_new = dim(2 * norb, sum(nelec))
+    if isinstance(vec, torch.Tensor):
+        out = torch.zeros(n_new, dtype=vec.dtype, device=vec.device)
+        out[torch.from_numpy(addrs).to(vec.device)] = vec.reshape(-1)
+        return out
+    vec = np.asarray(vec)
+    out = np.zeros(n_new, dtype=vec.dtype)
+    out[addrs] = vec.reshape(-1)
+    return out
+
+
+def spinful_to_spinless_rdm1(mat_a: np.ndarray, mat_b: np.ndarray) -> np.ndarray:
+    """The spinless 1-RDM: the two spin blocks on the diagonal (states/states.py)."""
+    n = mat_a.shape[0]
+    out = np.zeros((2 * n, 2 * n), dtype=np.result_type(mat_a, mat_b))
+    out[:n, :n], out[n:, n:] = mat_a, mat_b
+    return out
+
+
+def spinful_to_spinless_rdm2(mat_aa: np.ndarray, mat_ab: np.ndarray, mat_bb: np.ndarray) -> np.ndarray:
+    """The spinless 2-RDM, G[p, q, r, s] = <a+_p a+_r a_s a_q> over 2 norb
+    orbitals (alpha first), from the spin blocks (states/states.py).  The
+    alpha-beta block fills (a a | b b) directly, (b b | a a) with its pairs
+    swapped, and the two exchange-ordered blocks (a b | b a), (b a | a b)
+    with a minus sign from reordering the operators."""
+    n = mat_aa.shape[0]
+    a, b = slice(0, n), slice(n, 2 * n)
+    out = np.zeros((2 * n,) * 4, dtype=np.result_type(mat_aa, mat_ab, mat_bb))
+    out[a, a, a, a] = mat_aa
+    out[b, b, b, b] = mat_bb
+    out[a, a, b, b] = mat_ab
+    out[b, b, a, a] = np.einsum("pqrs->rspq", mat_ab)
+    out[a, b, b, a] = -np.einsum("psrq->pqrs", mat_ab)
+    out[b, a, a, b] = -np.einsum("rqps->pqrs", mat_ab)
+    return out

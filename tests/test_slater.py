@@ -136,3 +136,25 @@ def test_gpu_spin_square(cuda):
         t = torch.from_numpy(v / np.linalg.norm(v)).to("cuda").to(torch.complex64)
         assert abs(f.spin_square(t, norb, ne) - exp / np.vdot(v, v).real) < 1e-4
     assert abs(f.spin_square(f.hartree_fock_state(6, (3, 3)), 6, (3, 3))) < 1e-12
+
+
+@pytest.mark.parametrize("norb, nelec", [(3, (2, 1)), (4, (2, 2)), (3, (1, 2))])
+def test_spinful_to_spinless(norb, nelec):
+    """The spinless RDMs of the converted vector (a (n_a + n_b, 0) system on
+    2 norb orbitals, from the oracle's definition) equal the converted spinful
+    RDMs: this fixes the address map and every block's sign."""
+    import torch
+
+    import ffsim_gb300 as f
+    from oracle import ffsim_oracle as o
+
+    v = o.random_state_vector(o.dim(norb, nelec), seed=norb + nelec[0])
+    w = f.spinful_to_spinless_vec(v, norb, nelec)
+    assert np.isclose(np.linalg.norm(w), 1.0)
+    n2, ne = 2 * norb, (sum(nelec), 0)
+    rdm1 = o.rdm1s(v, norb, nelec)
+    np.testing.assert_allclose(f.spinful_to_spinless_rdm1(rdm1[0], rdm1[1]), o.rdm1s(w, n2, ne)[0], atol=1e-12)
+    aa, ab, bb = o.rdm2s(v, norb, nelec)
+    np.testing.assert_allclose(f.spinful_to_spinless_rdm2(aa, ab, bb), o.rdm2s(w, n2, ne)[0], atol=1e-12)
+    wt = f.spinful_to_spinless_vec(torch.from_numpy(v), norb, nelec)
+    np.testing.assert_allclose(wt.numpy(), w)
