@@ -55,7 +55,14 @@ from ffsim_gb300.states import (
     vdot,
 )
 from ffsim_gb300.trotter import simulate_trotter_diag_coulomb_split_op, simulate_trotter_double_factorized
-from ffsim_gb300.variational import GivensAnsatzOp, UCJOpSpinBalanced, UCJOpSpinless, UCJOpSpinUnbalanced
+from ffsim_gb300.variational import (
+    GivensAnsatzOp,
+    HopGateAnsatzOperator,
+    NumNumAnsatzOpSpinBalanced,
+    UCJOpSpinBalanced,
+    UCJOpSpinless,
+    UCJOpSpinUnbalanced,
+)
 
 __all__ = [
     "LUCJGradient",
@@ -63,6 +70,8 @@ __all__ = [
     "DiagonalCoulombHamiltonian",
     "DoubleFactorizedHamiltonian",
     "GivensAnsatzOp",
+    "HopGateAnsatzOperator",
+    "NumNumAnsatzOpSpinBalanced",
     "LUCJEnergy",
     "LinearOperator",
     "MolecularHamiltonian",

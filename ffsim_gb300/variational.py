@@ -618,3 +618,121 @@ class GivensAnsatzOp:
         return (bool(np.allclose(self.thetas, other.thetas, rtol=rtol, atol=atol))
                 and _allclose_or_none(self.phis, other.phis, rtol, atol)
                 and _allclose_or_none(self.phase_angles, other.phase_angles, rtol, atol))
+
+
+@dataclass(frozen=True)
+class NumNumAnsatzOpSpinBalanced:
+    """Number-number interactions exp(i theta n_p n_q) on given same-spin and
+    opposite-spin orbital pairs (python/ffsim/variational/num_num.py:42-193).
+    Applying it is one diagonal Coulomb evolution with the matrices
+    (J_aa, J_ab, J_aa) of the angles and time -1."""
+
+    norb: int
+    interaction_pairs: tuple
+    thetas: tuple
+
+    def __post_init__(self):
+        for pairs, angles in zip(self.interaction_pairs, self.thetas):
+            validate_interaction_pairs(pairs, ordered=False)
+            if len(pairs) != len(angles):
+                raise ValueError("The number of interaction pairs must be equal to the number of rotation angles."
+                                 f"Got {len(pairs)}, and {len(angles)}.")
+
+    @staticmethod
+    def n_params(interaction_pairs) -> int:
+        return sum(len(pairs) for pairs in interaction_pairs)
+
+    def to_parameters(self) -> np.ndarray:
+        return np.concatenate(self.thetas)
+
+    @staticmethod
+    def from_parameters(params: np.ndarray, norb: int, interaction_pairs) -> "NumNumAnsatzOpSpinBalanced":
+        pairs_aa, pairs_ab = interaction_pairs
+        params = _check_params(params, len(pairs_aa) + len(pairs_ab))
+        return NumNumAnsatzOpSpinBalanced(norb, (pairs_aa, pairs_ab),
+                                          (params[: len(pairs_aa)], params[len(pairs_aa):]))
+
+    @staticmethod
+    def from_diag_coulomb_mats(diag_coulomb_mats) -> "NumNumAnsatzOpSpinBalanced":
+        """The pairs with a nonzero upper-triangle entry, in row-major order."""
+        mat_aa, mat_ab = diag_coulomb_mats
+        norb = mat_aa.shape[0]
+        pairs, thetas = ([], []), ([], [])
+        for t, mat in enumerate((mat_aa, mat_ab)):
+            for i, j in itertools.combinations_with_replacement(range(norb), 2):
+                if mat[i, j]:
+                    pairs[t].append((i, j))
+                    thetas[t].append(mat[i, j])
+        return NumNumAnsatzOpSpinBalanced(norb, pairs, (np.array(thetas[0]), np.array(thetas[1])))
+
+    def to_diag_coulomb_mats(self) -> np.ndarray:
+        mats = np.zeros((2, self.norb, self.norb))
+        for mat, pairs, thetas in zip(mats, self.interaction_pairs, self.thetas):
+            for (i, j), theta in zip(pairs, thetas):
+                mat[i, j] = mat[j, i] = theta
+        return mats
+
+    def _apply_unitary_(self, vec, norb: int, nelec, copy: bool):
+        from ffsim_gb300 import gates
+
+        if isinstance(nelec, (int, np.integer)):
+            return NotImplemented
+        _check_norb(self.norb, norb)
+        aa, ab = self.to_diag_coulomb_mats()
+        return gates.apply_diag_coulomb_evolution(vec, (aa, ab, aa), -1.0, norb, nelec, copy=copy)
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, NumNumAnsatzOpSpinBalanced):
+            return NotImplemented
+        return (self.norb == other.norb and list(map(list, self.interaction_pairs)) == list(
+                    map(list, other.interaction_pairs))
+                and all(bool(np.allclose(a, b, rtol=rtol, atol=atol)) for a, b in zip(self.thetas, other.thetas)))
+
+
+@dataclass(frozen=True)
+class HopGateAnsatzOperator:
+    """Hop gates on a cycle of orbital pairs, one angle each, then an optional
+    final orbital rotation (python/ffsim/variational/hopgate.py:27-137)."""
+
+    norb: int
+    interaction_pairs: list
+    thetas: np.ndarray
+    final_orbital_rotation: np.ndarray | None = None
+
+    def _apply_unitary_(self, vec, norb: int, nelec, copy: bool):
+        from ffsim_gb300 import basic_gates, gates
+
+        _check_norb(self.norb, norb)
+        first = True
+        for target_orbs, theta in zip(itertools.cycle(self.interaction_pairs), self.thetas):
+            vec = basic_gates.apply_hop_gate(vec, theta, target_orbs, norb, nelec, copy=copy and first)
+            first = False
+        if self.final_orbital_rotation is not None:
+            vec = gates.apply_orbital_rotation(vec, self.final_orbital_rotation, norb, nelec, copy=copy and first)
+            first = False
+        if first and copy:
+            vec = vec.clone() if hasattr(vec, "clone") else np.array(vec, copy=True)
+        return vec
+
+    def to_parameters(self) -> np.ndarray:
+        parts = [np.asarray(self.thetas, dtype=float)]
+        if self.final_orbital_rotation is not None:
+            parts.append(linalg.unitary_to_parameters(self.final_orbital_rotation))
+        return np.concatenate(parts)
+
+    @staticmethod
+    def from_parameters(params: np.ndarray, norb: int, interaction_pairs,
+                        with_final_orbital_rotation: bool = False) -> "HopGateAnsatzOperator":
+        params = np.asarray(params, dtype=float)
+        final = None
+        if with_final_orbital_rotation:
+            final = linalg.unitary_from_parameters(params[-(norb**2):], norb)
+            params = params[: -(norb**2)]
+        return HopGateAnsatzOperator(norb, interaction_pairs, params, final)
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        if not isinstance(other, HopGateAnsatzOperator):
+            return NotImplemented
+        return (self.norb == other.norb and list(self.interaction_pairs) == list(other.interaction_pairs)
+                and bool(np.allclose(self.thetas, other.thetas, rtol=rtol, atol=atol))
+                and _allclose_or_none(self.final_orbital_rotation, other.final_orbital_rotation, rtol, atol))

@@ -226,12 +226,17 @@ def install_stubs():
     bits = sys.modules["ffsim.states.bitstring"]
     bg = _load("ffsim.gates.basic_gates", "gates/basic_gates.py")
     qh = _load("ffsim.gates.quad_ham", "gates/quad_ham.py")
+    sys.modules["ffsim.gates"].apply_hop_gate = bg.apply_hop_gate
+    nn = _load("ffsim.variational.num_num", "variational/num_num.py")
+    hop = _load("ffsim.variational.hopgate", "variational/hopgate.py")
     return types.SimpleNamespace(
         random=rnd,
         bitstring=bits,
         Spin=spin_mod.Spin,
         basic_gates=bg,
         apply_quad_ham_evolution=qh.apply_quad_ham_evolution,
+        NumNumAnsatzOpSpinBalanced=nn.NumNumAnsatzOpSpinBalanced,
+        HopGateAnsatzOperator=hop.HopGateAnsatzOperator,
         slater=slater,
         double_factorized_t2=ldf.double_factorized_t2,
         orbital_rotation_from_t1_amplitudes=sys.modules["ffsim.variational.util"].orbital_rotation_from_t1_amplitudes,
@@ -702,6 +707,26 @@ def main():
             for k, orbs in enumerate([((0, 2), (1,)), ((0, 1, 3), (2, 3)), ((), ()), ((1,), ()), ((0, 1), ()),
                                       ((), (2, 3)), ((0,), (1,)), ((0, 1, 2), ())]):
                 out[f"bg{tag}_prod{k}"] = bgm.apply_num_op_prod_interaction(vec, 0.45, orbs, norb, nelec)
+
+    # number-number and hop-gate ansatz operators (variational/num_num.py, hopgate.py)
+    ra = np.random.default_rng(20261212)
+    nn_pairs = ([(0, 1), (1, 3), (2, 2)], [(0, 0), (1, 2)])
+    nn_params = ra.uniform(-1, 1, size=5)
+    op = ref.NumNumAnsatzOpSpinBalanced.from_parameters(nn_params, norb=4, interaction_pairs=nn_pairs)
+    vec = orc.random_state_vector(orc.dim(4, (2, 1)), seed=ra)
+    out["nn_params"], out["nn_in"] = nn_params, vec
+    out["nn_mats"] = op.to_diag_coulomb_mats()
+    out["nn_out"] = op._apply_unitary_(vec, 4, (2, 1), copy=True)
+    hop_pairs = [(0, 1), (2, 3), (1, 2)]
+    for k, final in enumerate((False, True)):
+        n = 5 + (16 if final else 0)
+        params = ra.uniform(-1, 1, size=n)
+        op = ref.HopGateAnsatzOperator.from_parameters(params, norb=4, interaction_pairs=hop_pairs,
+                                                       with_final_orbital_rotation=final)
+        vec = orc.random_state_vector(orc.dim(4, (2, 2)), seed=ra)
+        out[f"hop{k}_params"], out[f"hop{k}_in"] = params, vec
+        out[f"hop{k}_out"] = op._apply_unitary_(vec, 4, (2, 2), copy=True)
+        out[f"hop{k}_to"] = op.to_parameters()
 
     # addresses <-> bitstrings (states/bitstring.py:173-361), every representation
     bs = ref.bitstring

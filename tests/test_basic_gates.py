@@ -79,3 +79,44 @@ def test_argument_errors(bg):
     with pytest.raises(ValueError):
         bg.apply_num_num_interaction(vec, 0.1, (2, 2), 4, (2, 1))
     assert bg.pair_for_spin("x", bg.Spin.BETA) == (None, "x")
+
+
+@pytest.fixture
+def routed(bg, monkeypatch):
+    """The gates module's entry points routed to the oracle too (the ansatz
+    operators call them through the module)."""
+    from ffsim_gb300 import gates
+
+    monkeypatch.setattr(gates, "apply_orbital_rotation",
+                        lambda vec, mat, norb, nelec, copy=True: o.apply_orbital_rotation(vec, mat, norb, nelec))
+    monkeypatch.setattr(gates, "apply_diag_coulomb_evolution",
+                        lambda vec, m, t, norb, nelec, copy=True: o.apply_diag_coulomb_evolution(vec, m, t, norb, nelec))
+    return bg
+
+
+def test_num_num_ansatz_golden(routed, golden):
+    import ffsim_gb300 as f
+
+    pairs = ([(0, 1), (1, 3), (2, 2)], [(0, 0), (1, 2)])
+    op = f.NumNumAnsatzOpSpinBalanced.from_parameters(golden["nn_params"], norb=4, interaction_pairs=pairs)
+    np.testing.assert_allclose(op.to_diag_coulomb_mats(), golden["nn_mats"], atol=1e-15)
+    np.testing.assert_allclose(op._apply_unitary_(golden["nn_in"], 4, (2, 1), copy=True), golden["nn_out"], atol=1e-12)
+    np.testing.assert_allclose(op.to_parameters(), golden["nn_params"])
+    back = f.NumNumAnsatzOpSpinBalanced.from_diag_coulomb_mats(op.to_diag_coulomb_mats())
+    assert f.approx_eq(back, op)
+    assert f.NumNumAnsatzOpSpinBalanced.n_params(pairs) == 5
+    with pytest.raises(ValueError):
+        f.NumNumAnsatzOpSpinBalanced(4, ([(1, 0)], []), (np.ones(1), np.ones(0)))
+
+
+def test_hop_gate_ansatz_golden(routed, golden):
+    import ffsim_gb300 as f
+
+    pairs = [(0, 1), (2, 3), (1, 2)]
+    for k, final in enumerate((False, True)):
+        op = f.HopGateAnsatzOperator.from_parameters(golden[f"hop{k}_params"], norb=4, interaction_pairs=pairs,
+                                                     with_final_orbital_rotation=final)
+        np.testing.assert_allclose(op._apply_unitary_(golden[f"hop{k}_in"], 4, (2, 2), copy=True),
+                                   golden[f"hop{k}_out"], atol=1e-12)
+        np.testing.assert_allclose(op.to_parameters(), golden[f"hop{k}_to"], atol=1e-10)
+        assert f.approx_eq(op, op)
