@@ -40,7 +40,19 @@ from ffsim_gb300.gates import (
     apply_phase_shift_in_place,
 )
 from ffsim_gb300.hamiltonians import DiagonalCoulombHamiltonian, DoubleFactorizedHamiltonian, MolecularHamiltonian
-from ffsim_gb300.protocols import LinearOperator, apply_unitary, approx_eq, diag, linear_operator, trace
+from ffsim_gb300.protocols import (
+    LinearOperator,
+    SupportsApplyUnitary,
+    SupportsApproximateEquality,
+    SupportsDiagonal,
+    SupportsLinearOperator,
+    SupportsTrace,
+    apply_unitary,
+    approx_eq,
+    diag,
+    linear_operator,
+    trace,
+)
 from ffsim_gb300.rdm import rdms
 from ffsim_gb300.states import (
     hartree_fock_state,
@@ -80,6 +92,11 @@ __all__ = [
     "UCJOpSpinless",
     "BitstringType",
     "Spin",
+    "SupportsApplyUnitary",
+    "SupportsApproximateEquality",
+    "SupportsDiagonal",
+    "SupportsLinearOperator",
+    "SupportsTrace",
     "addresses_to_strings",
     "bitstring_to_occupied_orbitals",
     "strings_to_addresses",

@@ -8,10 +8,45 @@ python/ffsim/protocols/linear_operator_protocol.py:40-60.
 
 from __future__ import annotations
 
-from typing import Any, Callable
+from typing import Any, Callable, Protocol, runtime_checkable
 
 import numpy as np
 import torch
+
+
+@runtime_checkable
+class SupportsApplyUnitary(Protocol):
+    """An object with a unitary effect on state vectors (apply_unitary_protocol.py)."""
+
+    def _apply_unitary_(self, vec, norb: int, nelec, copy: bool): ...
+
+
+@runtime_checkable
+class SupportsLinearOperator(Protocol):
+    """An object with a linear operator on state vectors (linear_operator_protocol.py)."""
+
+    def _linear_operator_(self, norb: int, nelec): ...
+
+
+@runtime_checkable
+class SupportsApproximateEquality(Protocol):
+    """An object comparable to tolerances (approximate_equality_protocol.py)."""
+
+    def _approx_eq_(self, other: Any, rtol: float, atol: float) -> bool: ...
+
+
+@runtime_checkable
+class SupportsDiagonal(Protocol):
+    """An operator whose diagonal can be returned (diagonal_protocol.py)."""
+
+    def _diag_(self, norb: int, nelec): ...
+
+
+@runtime_checkable
+class SupportsTrace(Protocol):
+    """An operator whose trace can be returned (trace_protocol.py)."""
+
+    def _trace_(self, norb: int, nelec) -> float: ...
 
 
 def apply_unitary(vec, obj: Any, norb: int, nelec, copy: bool = True):
