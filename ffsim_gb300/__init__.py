@@ -39,6 +39,7 @@ from ffsim_gb300.gates import (
     apply_orbital_rotation,
     apply_phase_shift_in_place,
 )
+from ffsim_gb300.multireference import multireference_state
 from ffsim_gb300.hamiltonians import DiagonalCoulombHamiltonian, DoubleFactorizedHamiltonian, MolecularHamiltonian
 from ffsim_gb300.protocols import (
     LinearOperator,
@@ -129,6 +130,7 @@ __all__ = [
     "init_cache",
     "linalg",
     "linear_operator",
+    "multireference_state",
     "lucj_energy",
     "random",
     "slater_determinant",

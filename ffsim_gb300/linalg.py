@@ -236,3 +236,10 @@ def double_factorized_t2(t2_amplitudes: np.ndarray, *, tol: float = 1e-8, max_te
     coeff = np.array([1, -1]) * w[:, None]
     mats = coeff[:, :, None, None] * mu[:, :, :, None] * mu[:, :, None, :]
     return mats.reshape(-1, norb, norb)[:max_terms], rots.reshape(-1, norb, norb)[:max_terms]
+
+
+def reduced_matrix(mat, vecs) -> np.ndarray:
+    """M[i, j] = <v_i| mat |v_j> (python/ffsim/linalg/linalg.py:50-69)."""
+    from ffsim_gb300.multireference import reduced_matrix as _reduced
+
+    return _reduced(mat, vecs)

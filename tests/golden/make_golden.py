@@ -229,6 +229,15 @@ def install_stubs():
     sys.modules["ffsim.gates"].apply_hop_gate = bg.apply_hop_gate
     nn = _load("ffsim.variational.num_num", "variational/num_num.py")
     hop = _load("ffsim.variational.hopgate", "variational/hopgate.py")
+    # multireference states: the single-factorized Hamiltonian, product states
+    # and the FermionOperator conversion it imports are never called here
+    _module("ffsim.hamiltonians.single_factorized_hamiltonian", {"SingleFactorizedHamiltonian": type("SF", (), {})})
+    _module("ffsim.operators.fermion_operator", {"_fermion_operator_to_linear_operator": None})
+    _load("ffsim.protocols.apply_unitary_protocol", "protocols/apply_unitary_protocol.py")
+    _load("ffsim.protocols.linear_operator_protocol", "protocols/linear_operator_protocol.py")
+    sys.modules["ffsim.states"].slater_determinant = slater.slater_determinant
+    sys.modules["ffsim.states"].ProductStateSum = types.SimpleNamespace
+    mref = _load("ffsim.variational.multireference", "variational/multireference.py")
     return types.SimpleNamespace(
         random=rnd,
         bitstring=bits,
@@ -237,6 +246,7 @@ def install_stubs():
         apply_quad_ham_evolution=qh.apply_quad_ham_evolution,
         NumNumAnsatzOpSpinBalanced=nn.NumNumAnsatzOpSpinBalanced,
         HopGateAnsatzOperator=hop.HopGateAnsatzOperator,
+        multireference_state=mref.multireference_state,
         slater=slater,
         double_factorized_t2=ldf.double_factorized_t2,
         orbital_rotation_from_t1_amplitudes=sys.modules["ffsim.variational.util"].orbital_rotation_from_t1_amplitudes,
@@ -727,6 +737,22 @@ def main():
         out[f"hop{k}_params"], out[f"hop{k}_in"] = params, vec
         out[f"hop{k}_out"] = op._apply_unitary_(vec, 4, (2, 2), copy=True)
         out[f"hop{k}_to"] = op.to_parameters()
+
+    # multireference state (variational/multireference.py:28-76): a UCJ ansatz on
+    # three reference determinants, a double-factorized Hamiltonian's operator
+    rmr = np.random.default_rng(20261213)
+    ucj = ref.UCJOpSpinBalanced.from_parameters(rmr.uniform(-0.5, 0.5, size=ref.UCJOpSpinBalanced.n_params(4, 2)),
+                                                norb=4, n_reps=2)
+    g = rmr.standard_normal((4, 4)) + 1j * rmr.standard_normal((4, 4))
+    dcm = np.stack([orc.random_symmetric_normal(4, seed=rmr) for _ in range(3)])
+    rots = np.stack([orc.random_unitary(4, seed=rmr) for _ in range(3)])
+    dfh = ref.DoubleFactorizedHamiltonian((g + g.conj().T) / 2, dcm, rots, constant=0.7)
+    occs = [([0, 1], [0, 1]), ([0, 2], [0, 1]), ([0, 1], [1, 3])]
+    out["mr_params"] = ucj.to_parameters()
+    out["mr_h1"], out["mr_dcm"], out["mr_rots"] = dfh.one_body_tensor, dcm, rots
+    for root in (0, 1):
+        e, state = ref.multireference_state(dfh._linear_operator_(4, (2, 2)), ucj, occs, 4, (2, 2), root=root)
+        out[f"mr{root}_energy"], out[f"mr{root}_state"] = np.asarray(e), state
 
     # addresses <-> bitstrings (states/bitstring.py:173-361), every representation
     bs = ref.bitstring
