@@ -72,6 +72,7 @@ from ffsim_gb300.variational import (
     GivensAnsatzOp,
     HopGateAnsatzOperator,
     NumNumAnsatzOpSpinBalanced,
+    UCJAnglesOpSpinBalanced,
     UCJOpSpinBalanced,
     UCJOpSpinless,
     UCJOpSpinUnbalanced,
@@ -88,6 +89,7 @@ __all__ = [
     "LUCJEnergy",
     "LinearOperator",
     "MolecularHamiltonian",
+    "UCJAnglesOpSpinBalanced",
     "UCJOpSpinBalanced",
     "UCJOpSpinUnbalanced",
     "UCJOpSpinless",

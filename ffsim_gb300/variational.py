@@ -736,3 +736,117 @@ class HopGateAnsatzOperator:
         return (self.norb == other.norb and list(self.interaction_pairs) == list(other.interaction_pairs)
                 and bool(np.allclose(self.thetas, other.thetas, rtol=rtol, atol=atol))
                 and _allclose_or_none(self.final_orbital_rotation, other.final_orbital_rotation, rtol, atol))
+
+
+def brickwork(norb: int, n_layers: int):
+    """Adjacent pairs layer by layer, (0,1),(2,3),... then (1,2),(3,4),...
+    (python/ffsim/variational/ucj_angles_spin_balanced.py:247-250)."""
+    for i in range(n_layers):
+        for j in range(i % 2, norb - 1, 2):
+            yield (j, j + 1)
+
+
+@dataclass(frozen=True)
+class UCJAnglesOpSpinBalanced:
+    """Spin-balanced UCJ operator parameterized by gate angles
+    (python/ffsim/variational/ucj_angles_spin_balanced.py:26-244): per
+    repetition a Givens-ansatz orbital rotation and a number-number ansatz,
+    then an optional final Givens-ansatz rotation.  Applied like the matrix
+    form: consecutive rotations merged into one orbital rotation on the GPU."""
+
+    norb: int
+    num_num_ansatz_ops: list
+    givens_ansatz_ops: list
+    final_givens_ansatz_op: "GivensAnsatzOp | None" = None
+
+    def __post_init__(self):
+        if len(self.num_num_ansatz_ops) != len(self.givens_ansatz_ops):
+            raise ValueError("The number of number-number ansatz operations must equal the number of Givens ansatz "
+                             f"operations. Got {len(self.num_num_ansatz_ops)} and {len(self.givens_ansatz_ops)}.")
+
+    @property
+    def n_reps(self) -> int:
+        return len(self.num_num_ansatz_ops)
+
+    @staticmethod
+    def n_params(norb: int, n_reps: int, num_num_interaction_pairs, givens_interaction_pairs,
+                 with_final_givens_ansatz_op: bool = False) -> int:
+        per_rep = sum(len(p) for p in num_num_interaction_pairs) + 2 * len(givens_interaction_pairs) + norb
+        return n_reps * per_rep + with_final_givens_ansatz_op * norb**2
+
+    @staticmethod
+    def from_parameters(params: np.ndarray, *, norb: int, n_reps: int, num_num_interaction_pairs,
+                        givens_interaction_pairs, with_final_givens_ansatz_op: bool = False
+                        ) -> "UCJAnglesOpSpinBalanced":
+        """Per repetition the Givens ansatz's 2 len(pairs) + norb parameters,
+        then the number-number angles; then the final brickwork Givens ansatz."""
+        params = _check_params(params, UCJAnglesOpSpinBalanced.n_params(
+            norb, n_reps, num_num_interaction_pairs, givens_interaction_pairs, with_final_givens_ansatz_op))
+        n_nn = sum(len(p) for p in num_num_interaction_pairs)
+        n_giv = 2 * len(givens_interaction_pairs) + norb
+        nn_ops, giv_ops, index = [], [], 0
+        for _ in range(n_reps):
+            giv_ops.append(GivensAnsatzOp.from_parameters(params[index: index + n_giv], norb,
+                                                          givens_interaction_pairs))
+            index += n_giv
+            nn_ops.append(NumNumAnsatzOpSpinBalanced.from_parameters(params[index: index + n_nn], norb,
+                                                                     num_num_interaction_pairs))
+            index += n_nn
+        final = None
+        if with_final_givens_ansatz_op:
+            final = GivensAnsatzOp.from_parameters(params[index:], norb, list(brickwork(norb, norb)))
+        return UCJAnglesOpSpinBalanced(norb, nn_ops, giv_ops, final)
+
+    def to_parameters(self) -> np.ndarray:
+        parts = []
+        for giv, nn in zip(self.givens_ansatz_ops, self.num_num_ansatz_ops):
+            parts += [giv.to_parameters(), nn.to_parameters()]
+        if self.final_givens_ansatz_op is not None:
+            parts.append(self.final_givens_ansatz_op.to_parameters())
+        return np.concatenate(parts)
+
+    @staticmethod
+    def from_ucj_op(ucj_op: UCJOpSpinBalanced) -> "UCJAnglesOpSpinBalanced":
+        """Angles of a matrix-form UCJ operator: its Coulomb matrices as
+        number-number ansätze, its rotations as Givens ansätze."""
+        nn_ops = [NumNumAnsatzOpSpinBalanced.from_diag_coulomb_mats(m) for m in ucj_op.diag_coulomb_mats]
+        giv_ops = [GivensAnsatzOp.from_orbital_rotation(u) for u in ucj_op.orbital_rotations]
+        final = None
+        if ucj_op.final_orbital_rotation is not None:
+            final = GivensAnsatzOp.from_orbital_rotation(ucj_op.final_orbital_rotation)
+        return UCJAnglesOpSpinBalanced(ucj_op.norb, nn_ops, giv_ops, final)
+
+    @staticmethod
+    def from_t_amplitudes(t2: np.ndarray, *, t1: np.ndarray | None = None, n_reps: int | None = None,
+                          interaction_pairs=None, tol: float = 1e-8) -> "UCJAnglesOpSpinBalanced":
+        return UCJAnglesOpSpinBalanced.from_ucj_op(UCJOpSpinBalanced.from_t_amplitudes(
+            t2, t1=t1, n_reps=n_reps, interaction_pairs=interaction_pairs, tol=tol))
+
+    def _apply_unitary_(self, vec, norb: int, nelec, copy: bool):
+        from ffsim_gb300 import gates
+
+        if isinstance(nelec, (int, np.integer)):
+            return NotImplemented
+        _check_norb(self.norb, norb)
+        basis = np.eye(norb)
+        first = copy
+        for nn, giv in zip(self.num_num_ansatz_ops, self.givens_ansatz_ops):
+            u = giv.to_orbital_rotation()
+            vec = gates.apply_orbital_rotation(vec, u.conj().T @ basis, norb, nelec, copy=first)
+            vec = nn._apply_unitary_(vec, norb, nelec, copy=False)
+            basis, first = u, False
+        if self.final_givens_ansatz_op is not None:
+            basis = self.final_givens_ansatz_op.to_orbital_rotation() @ basis
+        return gates.apply_orbital_rotation(vec, basis, norb, nelec, copy=first)
+
+    def _approx_eq_(self, other, rtol: float, atol: float) -> bool:
+        from ffsim_gb300.protocols import approx_eq
+
+        if not isinstance(other, UCJAnglesOpSpinBalanced):
+            return NotImplemented
+        if self.norb != other.norb or self.n_reps != other.n_reps:
+            return False
+        if not approx_eq(self.final_givens_ansatz_op, other.final_givens_ansatz_op):
+            return False
+        return all(approx_eq(a, b, rtol=rtol, atol=atol) for a, b in
+                   zip(self.num_num_ansatz_ops + self.givens_ansatz_ops, other.num_num_ansatz_ops + other.givens_ansatz_ops))

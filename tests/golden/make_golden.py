@@ -238,6 +238,10 @@ def install_stubs():
     sys.modules["ffsim.states"].slater_determinant = slater.slater_determinant
     sys.modules["ffsim.states"].ProductStateSum = types.SimpleNamespace
     mref = _load("ffsim.variational.multireference", "variational/multireference.py")
+    proto.apply_unitary = sys.modules["ffsim.protocols.apply_unitary_protocol"].apply_unitary
+    proto.approx_eq = _load("ffsim.protocols.approximate_equality_protocol",
+                            "protocols/approximate_equality_protocol.py").approx_eq
+    angles = _load("ffsim.variational.ucj_angles_spin_balanced", "variational/ucj_angles_spin_balanced.py")
     return types.SimpleNamespace(
         random=rnd,
         bitstring=bits,
@@ -247,6 +251,7 @@ def install_stubs():
         NumNumAnsatzOpSpinBalanced=nn.NumNumAnsatzOpSpinBalanced,
         HopGateAnsatzOperator=hop.HopGateAnsatzOperator,
         multireference_state=mref.multireference_state,
+        UCJAnglesOpSpinBalanced=angles.UCJAnglesOpSpinBalanced,
         slater=slater,
         double_factorized_t2=ldf.double_factorized_t2,
         orbital_rotation_from_t1_amplitudes=sys.modules["ffsim.variational.util"].orbital_rotation_from_t1_amplitudes,
@@ -753,6 +758,24 @@ def main():
     for root in (0, 1):
         e, state = ref.multireference_state(dfh._linear_operator_(4, (2, 2)), ucj, occs, 4, (2, 2), root=root)
         out[f"mr{root}_energy"], out[f"mr{root}_state"] = np.asarray(e), state
+
+    # UCJ operator parameterized by gate angles (variational/ucj_angles_spin_balanced.py)
+    rua = np.random.default_rng(20261214)
+    nn_pairs, giv_pairs = ([(0, 1), (2, 3)], [(0, 0), (1, 1), (0, 2)]), [(0, 1), (2, 3), (1, 2)]
+    cls = ref.UCJAnglesOpSpinBalanced
+    n = cls.n_params(4, 2, nn_pairs, giv_pairs, with_final_givens_ansatz_op=True)
+    params = rua.uniform(-1, 1, size=n)
+    op = cls.from_parameters(params, norb=4, n_reps=2, num_num_interaction_pairs=nn_pairs,
+                             givens_interaction_pairs=giv_pairs, with_final_givens_ansatz_op=True)
+    vec = orc.random_state_vector(orc.dim(4, (2, 2)), seed=rua)
+    out["ang_params"], out["ang_in"] = params, vec
+    out["ang_out"] = op._apply_unitary_(vec, 4, (2, 2), copy=True)
+    out["ang_to"] = op.to_parameters()
+    ucj = ref.UCJOpSpinBalanced.from_parameters(rua.uniform(-1, 1, size=ref.UCJOpSpinBalanced.n_params(
+        4, 2, with_final_orbital_rotation=True)), norb=4, n_reps=2, with_final_orbital_rotation=True)
+    out["ang_ucj_params"] = ucj.to_parameters()
+    out["ang_from_ucj_to"] = cls.from_ucj_op(ucj).to_parameters()
+    out["ang_from_ucj_out"] = cls.from_ucj_op(ucj)._apply_unitary_(vec, 4, (2, 2), copy=True)
 
     # addresses <-> bitstrings (states/bitstring.py:173-361), every representation
     bs = ref.bitstring

@@ -120,3 +120,25 @@ def test_hop_gate_ansatz_golden(routed, golden):
                                    golden[f"hop{k}_out"], atol=1e-12)
         np.testing.assert_allclose(op.to_parameters(), golden[f"hop{k}_to"], atol=1e-10)
         assert f.approx_eq(op, op)
+
+
+def test_ucj_angles_golden(routed, golden):
+    """UCJ operator in gate angles: parameter layout, action and the conversion
+    from the matrix form, against the reference's own code."""
+    import ffsim_gb300 as f
+
+    nn_pairs, giv_pairs = ([(0, 1), (2, 3)], [(0, 0), (1, 1), (0, 2)]), [(0, 1), (2, 3), (1, 2)]
+    cls = f.variational.UCJAnglesOpSpinBalanced
+    assert cls.n_params(4, 2, nn_pairs, giv_pairs, with_final_givens_ansatz_op=True) == len(golden["ang_params"])
+    op = cls.from_parameters(golden["ang_params"], norb=4, n_reps=2, num_num_interaction_pairs=nn_pairs,
+                             givens_interaction_pairs=giv_pairs, with_final_givens_ansatz_op=True)
+    np.testing.assert_allclose(op._apply_unitary_(golden["ang_in"], 4, (2, 2), copy=True), golden["ang_out"],
+                               atol=1e-12)
+    np.testing.assert_allclose(op.to_parameters(), golden["ang_to"], atol=1e-12)
+    assert f.approx_eq(op, op)
+    ucj = f.UCJOpSpinBalanced.from_parameters(golden["ang_ucj_params"], norb=4, n_reps=2,
+                                              with_final_orbital_rotation=True)
+    conv = cls.from_ucj_op(ucj)
+    np.testing.assert_allclose(conv.to_parameters(), golden["ang_from_ucj_to"], atol=1e-10)
+    np.testing.assert_allclose(conv._apply_unitary_(golden["ang_in"], 4, (2, 2), copy=True),
+                               golden["ang_from_ucj_out"], atol=1e-10)
