@@ -331,3 +331,30 @@ def test_approx_eq_protocol():
     ucj = f.random.random_ucj_op_spin_balanced(3, seed=2)
     assert f.approx_eq(ucj, ucj) and not f.approx_eq(ucj, a)
     assert f.approx_eq(1, 1) and not f.approx_eq(1, 2)
+
+
+@pytest.mark.parametrize("norb, nocc", [(13, 6), (14, 7), (15, 7), (16, 8), (17, 8), (17, 9), (18, 9)])
+def test_stage_sequence_full_size_sectors(norb, nocc):
+    """The stage sequence with the kernels' addressing on whole half-filled
+    sectors (48,620 strings at norb 18): the group bases, member offsets and
+    cross-half partner tables the full-size launches use, for a random and a
+    banded unitary."""
+    rng = np.random.default_rng(norb * 3 + nocc)
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=rng)
+    for u in (o.random_unitary(norb, seed=rng), _hopping_evolution(norb, 0.2, 1, seed=norb)):
+        plan = _plan(u, True)
+        assert plan["kind"] == 3 and plan["err"] < 1e-10
+        np.testing.assert_allclose(pe.apply_ops(plan, vec, norb, nocc), o.apply_orbital_rotation(vec, u, norb, nocc),
+                                   atol=1e-12)
+
+
+@pytest.mark.parametrize("norb, nocc", [(13, 6), (14, 7), (15, 8), (16, 8)])
+def test_sector_kernel_plan_full_size_sectors(norb, nocc):
+    """The shared-memory sector kernel's five-stage form (complex128 and
+    single-sector calls) on whole half-filled sectors, random and banded."""
+    rng = np.random.default_rng(norb * 7 + nocc)
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=rng)
+    for u in (o.random_unitary(norb, seed=rng), _hopping_evolution(norb, 0.2, 1, seed=norb)):
+        plan = _plan(u, True)
+        np.testing.assert_allclose(pe.apply_plan(plan, vec, norb, nocc), o.apply_orbital_rotation(vec, u, norb, nocc),
+                                   atol=1e-12)
