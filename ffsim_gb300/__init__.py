@@ -68,6 +68,7 @@ from ffsim_gb300.states import (
     vdot,
 )
 from ffsim_gb300.trotter import simulate_trotter_diag_coulomb_split_op, simulate_trotter_double_factorized
+from ffsim_gb300.wick import expectation_one_body_power, expectation_one_body_product
 from ffsim_gb300.variational import (
     GivensAnsatzOp,
     HopGateAnsatzOperator,
@@ -128,6 +129,8 @@ __all__ = [
     "diag",
     "dim",
     "dims",
+    "expectation_one_body_power",
+    "expectation_one_body_product",
     "hartree_fock_state",
     "init_cache",
     "linalg",

@@ -242,6 +242,7 @@ def install_stubs():
     proto.approx_eq = _load("ffsim.protocols.approximate_equality_protocol",
                             "protocols/approximate_equality_protocol.py").approx_eq
     angles = _load("ffsim.variational.ucj_angles_spin_balanced", "variational/ucj_angles_spin_balanced.py")
+    wick = _load("ffsim.states.wick", "states/wick.py")
     return types.SimpleNamespace(
         random=rnd,
         bitstring=bits,
@@ -252,6 +253,7 @@ def install_stubs():
         HopGateAnsatzOperator=hop.HopGateAnsatzOperator,
         multireference_state=mref.multireference_state,
         UCJAnglesOpSpinBalanced=angles.UCJAnglesOpSpinBalanced,
+        wick=wick,
         slater=slater,
         double_factorized_t2=ldf.double_factorized_t2,
         orbital_rotation_from_t1_amplitudes=sys.modules["ffsim.variational.util"].orbital_rotation_from_t1_amplitudes,
@@ -776,6 +778,15 @@ def main():
     out["ang_ucj_params"] = ucj.to_parameters()
     out["ang_from_ucj_to"] = cls.from_ucj_op(ucj).to_parameters()
     out["ang_from_ucj_out"] = cls.from_ucj_op(ucj)._apply_unitary_(vec, 4, (2, 2), copy=True)
+
+    # Wick's theorem on a Slater determinant (states/wick.py)
+    rw = np.random.default_rng(20261215)
+    u = orc.random_unitary(6, seed=rw)
+    rho = ref.slater.slater_determinant_rdms(6, [0, 2, 3], u)
+    mats = [rw.standard_normal((6, 6)) + 1j * rw.standard_normal((6, 6)) for _ in range(4)]
+    out["wick_rho"], out["wick_mats"] = rho, np.stack(mats)
+    out["wick_prod"] = np.asarray([ref.wick.expectation_one_body_product(rho, mats[:k]) for k in range(5)])
+    out["wick_pow"] = np.asarray([ref.wick.expectation_one_body_power(rho, mats[0], k) for k in range(4)])
 
     # addresses <-> bitstrings (states/bitstring.py:173-361), every representation
     bs = ref.bitstring

@@ -158,3 +158,36 @@ def test_spinful_to_spinless(norb, nelec):
     np.testing.assert_allclose(f.spinful_to_spinless_rdm2(aa, ab, bb), o.rdm2s(w, n2, ne)[0], atol=1e-12)
     wt = f.spinful_to_spinless_vec(torch.from_numpy(v), norb, nelec)
     np.testing.assert_allclose(wt.numpy(), w)
+
+
+def test_wick_golden(golden):
+    """Products and powers of one-body operators on a Slater determinant
+    against the reference's own Wick code."""
+    import ffsim_gb300 as f
+
+    rho, mats = golden["wick_rho"], list(golden["wick_mats"])
+    for k in range(5):
+        assert abs(f.expectation_one_body_product(rho, mats[:k]) - golden["wick_prod"][k]) < 1e-10
+    for k in range(4):
+        assert abs(f.expectation_one_body_power(rho, mats[0], k) - golden["wick_pow"][k]) < 1e-10
+
+
+def test_wick_against_state_vectors():
+    """The same expectations from the state vector itself (oracle), for a
+    determinant of 2 electrons in 5 spin orbitals."""
+    import ffsim_gb300 as f
+    from oracle import ffsim_oracle as o
+
+    norb, ne = 5, (2, 0)
+    rng = np.random.default_rng(1)
+    u = o.random_unitary(norb, seed=rng)
+    vec = np.zeros(o.dim(norb, ne), dtype=complex)
+    vec[0] = 1
+    vec = o.apply_orbital_rotation(vec, (u, None), norb, ne)
+    rho = o.rdm1s(vec, norb, ne)[0]
+    mats = [rng.standard_normal((norb, norb)) + 1j * rng.standard_normal((norb, norb)) for _ in range(3)]
+    for k in range(1, 4):
+        v = vec
+        for m in reversed(mats[:k]):
+            v = o.one_body_action(v, m, norb, ne)
+        assert abs(np.vdot(vec, v) - f.expectation_one_body_product(rho, mats[:k])) < 1e-12
