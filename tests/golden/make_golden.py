@@ -17,14 +17,19 @@ the hot path from their source files and satisfies their imports with:
   reference; pinned separately by reconstruction and determinant checks);
 * ``pyscf.fci.cistring`` -> ``make_strings`` / ``gen_occslst`` restated from
   their combinatorial definition (subsets of the orbital list in colexicographic
-  order of positions, which gives ascending integers for ``range(norb)``);
-* ``jax`` / ``opt_einsum`` / ``pyscf.ci`` -> inert placeholders (only used off
-  the path).
+  order of positions, which gives ascending integers for ``range(norb)``), and
+  ``str2addr`` / ``addrs2str`` / ``strs2addr`` as lookups in those tables;
+* ``jax`` / ``opt_einsum`` / ``pyscf.ci`` / ``pyscf.fci.direct_nosym`` /
+  ``pyscf.fci.direct_uhf``, the FermionOperator names, the two-body
+  contraction and the single-factorized Hamiltonian -> inert placeholders
+  (imported by the loaded modules, never called by the cases here).
 
 Everything above the kernels -- reshapes, transposes, the ``s.conjugate()``
 convention, pair slices, diagonal halving, ``None`` handling, linear operator
-composition, UCJ rotation merging -- is the reference's own code.  The
-outputs are written to ``tests/golden/golden.npz``.
+composition, UCJ rotation merging, and the Hamiltonian, ansatz, decomposition,
+random, Slater, bitstring, gate and Wick modules -- is the reference's own
+code.  The outputs are written to ``tests/golden/golden.npz``; each new group
+of cases uses its own seed, so regenerating leaves earlier arrays unchanged.
 """
 
 from __future__ import annotations
