@@ -42,8 +42,17 @@ import sys
 import types
 from pathlib import Path
 
-import numpy as np
-import scipy.linalg
+# Reproducible summation order, and so every output bit: one BLAS thread, and a
+# fixed string-hash seed (einsum's contraction-path search iterates sets of
+# index letters).  The hash seed only takes effect at start-up, so re-execute.
+for _var in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(_var, "1")
+if __name__ == "__main__" and os.environ.get("PYTHONHASHSEED") != "0":
+    os.environ["PYTHONHASHSEED"] = "0"
+    os.execv(sys.executable, [sys.executable, *sys.argv])
+
+import numpy as np  # noqa: E402
+import scipy.linalg  # noqa: E402
 
 REF = Path(os.environ.get("FFSIM_REF", "/root/reference"))
 PKG = REF / "python" / "ffsim"
