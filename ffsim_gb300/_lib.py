@@ -42,6 +42,8 @@ SIGNATURES = {
     "ffgb_version": [],
     "ffgb_last_error": [],
     "ffgb_launch_count": [],
+    "ffgb_device_alloc_count": [],
+    "ffgb_debug_fma_rate": [_c_int, _dp, _c_void_p],
     "ffgb_givens_decomposition": [_dp, _c_int, _c_double, _dp, _ip, _ip, _dp],
     "ffgb_eigh": [_dp, _c_int, _dp, _dp],
     "ffgb_debug_plan": [_dp, _c_int, _c_int, _dp, _c_int, _ip],
@@ -107,6 +109,7 @@ def load() -> ctypes.CDLL:
         lib.ffgb_last_error.restype = ctypes.c_char_p
         lib.ffgb_scratch_bytes.restype = _c_size_t
         lib.ffgb_launch_count.restype = _c_ll
+        lib.ffgb_device_alloc_count.restype = _c_ll
         _lib = lib
         return lib
 

@@ -17,6 +17,10 @@ int fail(int code, const std::string& msg);
 // Count one kernel launch (reported by ffgb_launch_count()).
 void count_launch();
 
+// Count one device allocation made by the library (reported by
+// ffgb_device_alloc_count()).
+void count_alloc();
+
 #define FFGB_CUDA(call)                                                              \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \

@@ -33,6 +33,8 @@ int fail(int code, const std::string& msg) {
 
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static std::atomic<long long> g_allocs{0};
+void count_alloc() { g_allocs.fetch_add(1, std::memory_order_relaxed); }
 
 static long long binom_h(int n, int k) {
   if (k < 0 || n < 0 || k > n) return 0;
@@ -72,20 +74,27 @@ static int device_strings(int norb, int nocc, const unsigned** out) {
   }
   unsigned* d = nullptr;
   FFGB_CUDA(cudaMalloc(&d, h.size() * sizeof(unsigned)));
+  count_alloc();
   FFGB_CUDA(cudaMemcpy(d, h.data(), h.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
   g_strings[key] = d;
   *out = d;
   return FFGB_OK;
 }
 
+// SM count of the current device, looked up once per device ordinal.
 static int num_sms() {
-  static const int sms = [] {  // initialised once, thread-safe
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 132;
-  }();
-  return sms;
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  n = n > 0 ? n : 132;
+  if (dev >= 0 && dev < 64) cache[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 // ---------------------------------------------------------------------------
@@ -140,6 +149,12 @@ struct DiagSpec {
 
 // Diagonal Coulomb operator sum J^{st}_ij n_is n_jt / 2 (num rep) or the
 // Z-rep form, scaled by `scale`; rows = alpha, columns = beta.
+static SameTable same_table(const double (&m)[FFGB_MAXN][FFGB_MAXN]) {
+  SameTable t;
+  std::memcpy(t.v, m, sizeof(t.v));
+  return t;
+}
+
 static DiagSpec diag_coulomb_spec(int norb, const double* aa, const double* ab, const double* bb,
                                   int zrep, double scale, int mode) {
   DiagSpec d;
@@ -340,12 +355,9 @@ static int run_pass(const PassArgs<T>& A, Scratch& scr, cudaStream_t st) {
         if (A.diag->col_same[i][j] != 0.0) col_nonzero = true;
     if (col_nonzero) {
       void* tab = scr.take((size_t)dim * sizeof(C));
-      double* same = (double*)scr.take(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
-      if (!tab || !same) return fail(FFGB_ERR_OOM, "scratch too small for the column table");
-      FFGB_CUDA(cudaMemcpyAsync(same, A.diag->col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN,
-                                cudaMemcpyHostToDevice, st));
+      if (!tab) return fail(FFGB_ERR_OOM, "scratch too small for the column table");
       col_table_kernel<T><<<(dim + 255) / 256, 256, 0, st>>>(P->col_strings, dim, norb, P->zrep,
-                                                             diag_mode, same, tab);
+                                                             diag_mode, same_table(A.diag->col_same), tab);
       count_launch();
       FFGB_CUDA(cudaGetLastError());
       P->col_table = tab;
@@ -541,11 +553,9 @@ static int diag_rows(const void* in, void* out, int norb, int row_nocc, int col_
   FFGB_TRY(device_strings(norb, row_nocc, &rs));
   FFGB_TRY(device_strings(norb, col_nocc, &cs));
   void* tab = scr.take((size_t)cols * (spec.mode == DIAG_PHASE ? sizeof(C) : sizeof(T)));
-  double* same = (double*)scr.take(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
-  if (!tab || !same) return fail(FFGB_ERR_OOM, "scratch too small for the column table");
-  FFGB_CUDA(cudaMemcpyAsync(same, spec.col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN, cudaMemcpyHostToDevice, st));
+  if (!tab) return fail(FFGB_ERR_OOM, "scratch too small for the column table");
   col_table_kernel<T><<<(unsigned)((cols + 255) / 256), 256, 0, st>>>(cs, (int)cols, norb, spec.zrep, spec.mode,
-                                                                      same, tab);
+                                                                      same_table(spec.col_same), tab);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   auto A = std::make_unique<DiagRowsArgs<T>>();
@@ -634,12 +644,10 @@ static int big_expect(const void* x, int norb, int na, int nb, const DiagSpec& s
   FFGB_TRY(device_strings(norb, nb, &cs));
   const long long grid = (rows + DIAG_ROWS_PER_CTA - 1) / DIAG_ROWS_PER_CTA;
   void* tab = scr.take((size_t)cols * sizeof(T));
-  double* same = (double*)scr.take(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
   double* partials = (double*)scr.take(sizeof(double) * (size_t)grid);
-  if (!tab || !same || !partials) return fail(FFGB_ERR_OOM, "scratch too small for the expectation tables");
-  FFGB_CUDA(cudaMemcpyAsync(same, spec.col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN, cudaMemcpyHostToDevice, st));
+  if (!tab || !partials) return fail(FFGB_ERR_OOM, "scratch too small for the expectation tables");
   col_table_kernel<T><<<(unsigned)((cols + 255) / 256), 256, 0, st>>>(cs, (int)cols, norb, spec.zrep, DIAG_COEF,
-                                                                      same, tab);
+                                                                      same_table(spec.col_same), tab);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   auto A = std::make_unique<DiagRowsArgs<T>>();
@@ -983,17 +991,13 @@ static int expect_tables(int norb, int na, int nb, const DiagSpec& spec, Scratch
   FFGB_TRY(device_strings(norb, nb, &sb));
   float* zrow = (float*)scr.take(sizeof(float) * (size_t)db);
   float* zcol = (float*)scr.take(sizeof(float) * (size_t)da);
-  double* same = (double*)scr.take(2 * sizeof(double) * FFGB_MAXN * FFGB_MAXN);
-  if (!zrow || !zcol || !same) return fail(FFGB_ERR_OOM, "scratch too small for the expectation tables");
-  FFGB_CUDA(cudaMemcpyAsync(same, dt.row_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN, cudaMemcpyHostToDevice, st));
-  FFGB_CUDA(cudaMemcpyAsync(same + FFGB_MAXN * FFGB_MAXN, dt.col_same, sizeof(double) * FFGB_MAXN * FFGB_MAXN,
-                            cudaMemcpyHostToDevice, st));
+  if (!zrow || !zcol) return fail(FFGB_ERR_OOM, "scratch too small for the expectation tables");
   col_table_kernel<float><<<(unsigned)((db + 255) / 256), 256, 0, st>>>(sb, (int)db, norb, dt.zrep, DIAG_COEF,
-                                                                         same, zrow);
+                                                                         same_table(dt.row_same), zrow);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   col_table_kernel<float><<<(unsigned)((da + 255) / 256), 256, 0, st>>>(
-      sa, (int)da, norb, dt.zrep, DIAG_COEF, same + FFGB_MAXN * FFGB_MAXN, zcol);
+      sa, (int)da, norb, dt.zrep, DIAG_COEF, same_table(dt.col_same), zcol);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   ex.zrow = zrow;
@@ -1257,8 +1261,13 @@ static int contract_static_impl(const void* vec, void* out, int norb, int na, in
                                 int accumulate, cudaStream_t st) {
   using C = typename CT<T>::type;
   const long long da = binom_h(norb, na), db = binom_h(norb, nb);
-  const size_t need = round256((size_t)da * 4) + round256((size_t)db * 4) + round256((size_t)db * sizeof(C)) +
-                      round256(sizeof(double) * FFGB_MAXN * FFGB_MAXN);
+  // the column table is built only when the beta-beta block is nonzero (run_pass)
+  bool col_nonzero = false;
+  for (int i = 0; i < FFGB_MAXN && !col_nonzero; ++i)
+    for (int j = 0; j < FFGB_MAXN; ++j)
+      if (spec.col_same[i][j] != 0.0) col_nonzero = true;
+  const size_t need = round256((size_t)da * 4) + round256((size_t)db * 4) +
+                      (col_nonzero ? round256((size_t)db * sizeof(C)) : 0);
   if (need > FFGB_STATIC_SCRATCH_BYTES)
     return fail(FFGB_ERR_ARG, "this shape needs " + std::to_string(need) + " bytes of scratch; the fixed scratch of "
                                   "ffgb_contract_diag_coulomb_static holds " +
@@ -1336,6 +1345,8 @@ int ffgb_version(void) { return 100; }
 const char* ffgb_last_error(void) { return ffgb::g_err.c_str(); }
 
 long long ffgb_launch_count(void) { return g_launches.load(); }
+
+long long ffgb_device_alloc_count(void) { return g_allocs.load(); }
 
 int ffgb_givens_decomposition(const double* mat, int n, double tol, double* rot_cs, int* rot_ij,
                               int* n_rot, double* diag) {
@@ -1626,6 +1637,7 @@ int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, 
   const size_t need = (size_t)binom_h(norb, nb) * 16 + 8192;
   void* tmp = nullptr;
   FFGB_CUDA(cudaMallocAsync(&tmp, need, st));
+  count_alloc();
   Scratch s2(tmp, need);
   int s = FFGB_DISPATCH(dtype, rotated_matvec_impl<float>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st),
                         rotated_matvec_impl<double>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st));
@@ -1656,6 +1668,7 @@ int ffgb_contract_num_op_sum(const void* vec, void* out, int dtype, int norb, in
   const size_t need = (size_t)binom_h(norb, nb) * 16 + 8192;
   void* tmp = nullptr;
   FFGB_CUDA(cudaMallocAsync(&tmp, need, st));
+  count_alloc();
   Scratch s2(tmp, need);
   int s = FFGB_DISPATCH(dtype, rotated_matvec_impl<float>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st),
                         rotated_matvec_impl<double>(vec, out, norb, na, nb, spec, nullptr, accumulate, s2, st));
@@ -1817,6 +1830,7 @@ int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out,
     return fail(FFGB_ERR_DTYPE, "dtype must be complex64 or complex128");
   double* part = nullptr;
   FFGB_CUDA(cudaMallocAsync(&part, sizeof(double) * (2 * blocks + 2), st));
+  count_alloc();
   if (dtype == FFGB_C64)
     vdot_kernel<float><<<blocks, 256, 0, st>>>((const float2*)x, (const float2*)y, n, part);
   else

@@ -957,9 +957,15 @@ __global__ void excitation_kernel(const typename CT<T>::type* __restrict__ in, t
 }
 
 // F_C(j) of the rotated sector: phase exp(i F) (mode 1) or coefficient F (mode 2)
+// Same-sector coefficients of a diagonal operator, passed by value as a
+// kernel parameter (no device copy, nothing read from host memory).
+struct SameTable {
+  double v[FFGB_MAXN * FFGB_MAXN];
+};
+
 template <typename T>
 __global__ void col_table_kernel(const unsigned* __restrict__ strings, int dim, int norb, int zrep,
-                                 int mode, const double* __restrict__ same, void* out) {
+                                 int mode, const __grid_constant__ SameTable same, void* out) {
   using C = typename CT<T>::type;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= dim) return;
@@ -970,7 +976,7 @@ __global__ void col_table_kernel(const unsigned* __restrict__ strings, int dim, 
     if (gi == 0.0) continue;
     for (int i2 = i; i2 < norb; ++i2) {
       const double gj = zrep ? ((s >> i2) & 1u ? -1.0 : 1.0) : (double)((s >> i2) & 1u);
-      f += same[i * FFGB_MAXN + i2] * gi * gj;
+      f += same.v[i * FFGB_MAXN + i2] * gi * gj;
     }
   }
   if (mode == DIAG_PHASE)

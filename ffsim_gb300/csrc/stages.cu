@@ -195,6 +195,7 @@ int cs_pass_tables(int norb, int nocc, int lo, int hh, const CsPass** out) {
   for (int m = 4; m >= 1; --m) add(m, n_sub_b[m], sub_b[m]);
   const size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(int);
   FFGB_CUDA(cudaMalloc(&P.tab, bytes));
+  count_alloc();
   if (!host.empty()) FFGB_CUDA(cudaMemcpy(P.tab, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice));
   g_cs[key] = std::move(P);
   *out = &g_cs[key];
@@ -332,6 +333,7 @@ int win_layout(int norb, int nocc, int lo, int B, const WinLayout** out) {
     }
   const size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(int);
   FFGB_CUDA(cudaMalloc(&W.dev_base, bytes));
+  count_alloc();
   if (!host.empty())
     FFGB_CUDA(cudaMemcpy(W.dev_base, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice));
   g_win[key] = std::move(W);

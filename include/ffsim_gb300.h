@@ -53,6 +53,17 @@ int ffgb_version(void);
 const char* ffgb_last_error(void);
 /* Number of CUDA kernels this library has launched in the process. */
 long long ffgb_launch_count(void);
+/* Number of device allocations (cudaMalloc, cudaMallocAsync) this library
+ * has made in the process: its cached string and stage tables and the
+ * temporary buffers of the entry points that take no workspace.  Test and
+ * accounting aid; no counterpart in the reference. */
+long long ffgb_device_alloc_count(void);
+/* Measured fused multiply-add rate of the CUDA cores (TFLOP/s, 2 flops per
+ * FMA): FP64 for FFGB_C128, FP32 for FFGB_C64.  Two launches of an
+ * FMA-chain kernel over every SM on `stream`, the second timed with CUDA
+ * events; about 10-20 ms.  The compute ceiling of the rotation kernels;
+ * no counterpart in the reference. */
+int ffgb_debug_fma_rate(int dtype, double* tflops, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* Host-side linear algebra                                             */
@@ -178,9 +189,10 @@ int ffgb_contract_diag_coulomb(const void* vec, void* out, int dtype, int norb, 
  * in the reference: it exists for callers that cannot allocate device memory
  * (all of it is held by another allocator, or cudaMalloc/cudaFree would stall
  * a latency-bound loop).  Same arguments and results as
- * ffgb_contract_diag_coulomb.  Its scratch (occupation strings and a column
- * table, 4*dim_a + (4 + element size)*dim_b bytes plus 3 KB, each part rounded
- * up to 256 bytes) lives in one FFGB_STATIC_SCRATCH_BYTES array per device;
+ * ffgb_contract_diag_coulomb.  Its scratch (occupation strings, 4*dim_a +
+ * 4*dim_b bytes, and, when mat_bb is nonzero, a column table of element
+ * size * dim_b bytes, each part rounded up to 256 bytes) lives in one
+ * FFGB_STATIC_SCRATCH_BYTES array per device;
  * larger shapes return FFGB_ERR_ARG with the byte counts.  Nothing in that
  * array has to start at zero: the call writes every byte it reads.  Calls on
  * one device that overlap in time (different streams or host threads) share
