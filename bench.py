@@ -50,6 +50,13 @@ METRIC = "LUCJ energy evals/s norb=16 (8,8) c64 vs c128 at |dE|<=1e-6 Ha; p50/p9
 WORKLOAD = "LUCJ n_reps=2 from HF + DF Hamiltonian rank 32 energy, norb=16, nelec=(8,8)"
 
 
+def run_config(world: int) -> dict:
+    """The workload's config block, identical in both arms."""
+    return {"workload": WORKLOAD, "norb": NORB, "nelec": list(NELEC), "n_reps": N_REPS, "df_rank": RANK,
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (state 1.32 GB in complex64, 2.65 GB in complex128)"}
+
+
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -166,10 +173,34 @@ def time_e2e(steps, ucj, ham):
     return (t1 - t0) / steps
 
 
-# DRAM bytes (read + write) of one 8-orbital window stage at norb=16 (8,8)
-# complex64, summed over its class launches, from the ncu launch list in
-# profiles/window_stage_norb16_c64.md.
-WINDOW_STAGE_TRAFFIC = 2.389e9
+def window_stage_traffic():
+    """DRAM bytes (read + write) of one 8-orbital window stage at norb=16 (8,8)
+    complex64: the sum over its class launches of dram__bytes_read.sum +
+    dram__bytes_write.sum in the committed ncu capture
+    profiles/window_stage_norb16_c64_traffic.txt (the command that made it is
+    in its header).  None when that capture is absent."""
+    p = ROOT / "profiles" / "window_stage_norb16_c64_traffic.txt"
+    if not p.exists():
+        return None, None
+    total = 0.0
+    for line in p.read_text().splitlines():  # kernel | time_us | dram_read_bytes | dram_write_bytes
+        parts = [x.strip() for x in line.split("|")]
+        if len(parts) >= 4 and parts[0].startswith("win_class_kernel"):
+            total += float(parts[2]) + float(parts[3])
+    return (total if total > 0 else None), str(p.relative_to(ROOT))
+
+
+def rotation_flops(norb: int, nelec) -> float:
+    """Floating-point operations of the complex128 two-sector rotation: the
+    adjacent-Givens network has norb (norb - 1) / 2 rotations per sector, each
+    touching the strings with exactly one of its two orbitals occupied
+    (2 C(norb-2, n-1) of C(norb, n)) with 6 FMA = 12 flops per amplitude."""
+    d = math.comb(norb, nelec[0]) * math.comb(norb, nelec[1])
+    flops = 0.0
+    for n in nelec:
+        frac = 2 * math.comb(norb - 2, n - 1) / math.comb(norb, n)
+        flops += norb * (norb - 1) / 2 * frac * d * 12
+    return flops
 
 
 def stage_rooflines(stream, reps: int = 8):
@@ -221,6 +252,39 @@ def stage_rooflines(stream, reps: int = 8):
     torch.cuda.empty_cache()
     out["S"] = S
     return out
+
+
+def time_rotation_c128(stream, reps: int = 2) -> float:
+    """CUDA-event time (ms) of one complex128 two-sector orbital rotation on a
+    resident norb=16 (8,8) state."""
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _lib
+    from ffsim_gb300._state import scratch
+
+    d = f.dim(NORB, NELEC)
+    u = _lib.cmat(f.random.random_unitary(NORB, seed=98))
+    with torch.cuda.stream(stream):
+        v = torch.randn(d, dtype=torch.complex128, device="cuda")
+        v /= torch.linalg.vector_norm(v)
+        buf, nbytes = scratch(v, 0, NORB, *NELEC)
+
+        def rot():
+            _lib.call("ffgb_apply_orbital_rotation", v.data_ptr(), _lib.FFGB_C128, NORB, NELEC[0], NELEC[1],
+                      _lib.dptr(u), _lib.dptr(u), buf.data_ptr(), nbytes, stream.cuda_stream)
+
+        rot()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            rot()
+        b.record(stream)
+        torch.cuda.synchronize()
+    del v, buf
+    torch.cuda.empty_cache()
+    return a.elapsed_time(b) / reps
 
 
 def run_ops(args) -> None:
@@ -477,8 +541,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "evals/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "norb": NORB, "nelec": list(NELEC), "n_reps": N_REPS,
-                   "df_rank": RANK, "l2": "state (2.65 GB) larger than L2"},
+        "config": run_config(world),
         "cpu_baseline": {"value": val, "unit": "evals/s", "cores": cores, "kind": "port",
                          "sample": f"one orbital rotation ({t_rot:.2f} s) + one diag-Coulomb evolution "
                                    f"({t_dc:.2f} s) at norb=16 complex128 per step, extrapolated to "
@@ -591,6 +654,12 @@ def main():
 
     # dominant kernel roofline
     st = stage_rooflines(stream)
+    traffic, traffic_src = window_stage_traffic()
+    # the complex128 path against the measured FP64 FMA rate
+    fp = np.zeros(2)
+    lib.ffgb_debug_fma_rate(1, _lib.dptr(fp[:1]), stream.cuda_stream)
+    lib.ffgb_debug_fma_rate(0, _lib.dptr(fp[1:]), stream.cuda_stream)
+    rot128_ms = time_rotation_c128(stream)
     S = st["S"]
     peak, peak_kind = _peaks()
     gbs = 2 * S / (st["window_stage_ms"] * 1e-3) / 1e9
@@ -614,18 +683,21 @@ def main():
             "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "norb": NORB, "nelec": list(NELEC), "n_reps": N_REPS,
-                       "df_rank": RANK, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (state 1.32 GB c64)"},
+            "config": run_config(world),
             "p50_ms": statistics.median(times64),
             "p99_ms": float(np.percentile(times64, 99)),
             "energy_c64": e64, "energy_c128": e128, "abs_dE_c64_vs_c128": abs(e64 - e128),
             "c128": {"value": 1e3 / statistics.mean(times128), "unit": "evals/s",
-                     "ms_per_step": statistics.mean(times128), "steps": len(times128)},
+                     "ms_per_step": statistics.mean(times128), "steps": len(times128),
+                     "bound": "fp64",
+                     "fp64_peak_tflops": fp[0], "fp64_peak_kind": "measured in-run (FMA-chain kernel, CUDA events)",
+                     "rotation_ms": rot128_ms, "rotation_tflops": rotation_flops(NORB, NELEC) / rot128_ms / 1e9,
+                     "rotation_frac_of_fp64": rotation_flops(NORB, NELEC) / rot128_ms / 1e9 / fp[0]},
+            "fp32_peak_tflops": fp[1],
             "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": 8 * (RANK + 2)},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
-                         "frac": gbs / peak, "traffic": WINDOW_STAGE_TRAFFIC,
+                         "frac": gbs / peak, "traffic": traffic, "traffic_source": traffic_src,
                          "kernel": "win_class_kernel: one 8-orbital window stage (one launch per electron-count "
                                    "class), 2 S algorithmic bytes",
                          "algorithmic_bytes": 2 * S, "ms": st["window_stage_ms"],

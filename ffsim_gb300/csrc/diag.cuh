@@ -28,6 +28,10 @@ struct DiagRowsArgs {
   double cross[FFGB_MAXN][FFGB_MAXN];
   int norb, zrep, mode, accumulate;
   double* partials;  // COEF only: when set, sum f |in|^2 per CTA here instead of writing out
+  // when both are set the input is the outer product outer_row[r] * outer_col[c]
+  // (a product state, e.g. a rotated Hartree-Fock state) and `in` is not read
+  const C* outer_row;
+  const C* outer_col;
 };
 
 // Per row, the row term and the cross term are tabulated over the two halves
@@ -99,9 +103,10 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
     __syncthreads();
     const C* xin = A.in + r * A.cols;
     C* xout = A.out + r * A.cols;
+    const C orow = A.outer_row ? A.outer_row[r] : cmake<C>(0.0, 0.0);
     for (long long c = tid; c < A.cols; c += DIAG_THREADS) {
       const unsigned s = A.cstr[c];
-      C v = xin[c];
+      C v = A.outer_row ? cmul(orow, A.outer_col[c]) : xin[c];
       if (!phase) {
         const T z = ul[s & lmask] + uh[s >> h] + ((const T*)A.col_table)[c];
         if (A.partials) {
@@ -133,6 +138,72 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
       A.partials[blockIdx.x] = t;
     }
   }
+}
+
+// The occupied-orbital matrix of a rotated Hartree-Fock sector: for every
+// string s (ascending occupied orbitals o_0 < ... < o_{n-1}) the amplitude of
+// W(V) applied to the n lowest orbitals, det V[o_i][j] (i, j < n).  Gaussian
+// elimination with partial pivoting in FP64, one string per thread; V is a
+// kernel parameter (norb x norb complex, row-major).
+struct SlaterMat {
+  double v[FFGB_MAXN * FFGB_MAXN * 2];
+};
+
+template <typename C>
+__global__ void __launch_bounds__(128) slater_dets_kernel(const unsigned* __restrict__ strings, long long dim,
+                                                          int norb, int n, const __grid_constant__ SlaterMat V,
+                                                          C* __restrict__ out) {
+  const long long t = blockIdx.x * 128LL + threadIdx.x;
+  if (t >= dim) return;
+  const unsigned s = strings[t];
+  double mr[FFGB_MAXN][FFGB_MAXN], mi[FFGB_MAXN][FFGB_MAXN];
+  int row = 0;
+  for (int o = 0; o < norb && row < n; ++o) {
+    if (!((s >> o) & 1u)) continue;
+    for (int j = 0; j < n; ++j) {
+      mr[row][j] = V.v[2 * (o * norb + j)];
+      mi[row][j] = V.v[2 * (o * norb + j) + 1];
+    }
+    ++row;
+  }
+  double dr = 1.0, di = 0.0;
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    double best = mr[k][k] * mr[k][k] + mi[k][k] * mi[k][k];
+    for (int r = k + 1; r < n; ++r) {
+      const double a = mr[r][k] * mr[r][k] + mi[r][k] * mi[r][k];
+      if (a > best) {
+        best = a;
+        piv = r;
+      }
+    }
+    if (piv != k) {
+      for (int j = 0; j < n; ++j) {
+        const double xr = mr[k][j], xi = mi[k][j];
+        mr[k][j] = mr[piv][j];
+        mi[k][j] = mi[piv][j];
+        mr[piv][j] = xr;
+        mi[piv][j] = xi;
+      }
+      dr = -dr;
+      di = -di;
+    }
+    const double pr = mr[k][k], pi = mi[k][k];
+    const double nr = dr * pr - di * pi, ni = dr * pi + di * pr;
+    dr = nr;
+    di = ni;
+    if (best == 0.0) break;
+    const double inv = 1.0 / best;  // 1 / p = conj(p) / |p|^2
+    const double ir = pr * inv, ii = -pi * inv;
+    for (int r = k + 1; r < n; ++r) {
+      const double fr = mr[r][k] * ir - mi[r][k] * ii, fi = mr[r][k] * ii + mi[r][k] * ir;
+      for (int j = k + 1; j < n; ++j) {
+        mr[r][j] -= fr * mr[k][j] - fi * mi[k][j];
+        mi[r][j] -= fr * mi[k][j] + fi * mr[k][j];
+      }
+    }
+  }
+  out[t] = cmake<C>(dr, di);
 }
 
 // x[r][c] *= row_ph[r] * col_ph[c] (either table optional).

@@ -543,7 +543,8 @@ static void fold_col_phases(DiagSpec& spec, const SectorPlan& p, int norb) {
 // with these rows.  Streams rows (any sector size).
 template <typename T>
 static int diag_rows(const void* in, void* out, int norb, int row_nocc, int col_nocc, const DiagSpec& spec,
-                     bool accumulate, Scratch& scr, cudaStream_t st) {
+                     bool accumulate, Scratch& scr, cudaStream_t st, const void* outer_row = nullptr,
+                     const void* outer_col = nullptr) {
   using C = typename CT<T>::type;
   const long long rows = binom_h(norb, row_nocc), cols = binom_h(norb, col_nocc);
   if (rows <= 0 || cols <= 0) return FFGB_OK;
@@ -573,6 +574,10 @@ static int diag_rows(const void* in, void* out, int norb, int row_nocc, int col_
   A->zrep = spec.zrep;
   A->mode = spec.mode;
   A->accumulate = accumulate ? 1 : 0;
+  if (outer_row && outer_col) {
+    A->outer_row = (const C*)outer_row;
+    A->outer_col = (const C*)outer_col;
+  }
   const long long grid = (rows + DIAG_ROWS_PER_CTA - 1) / DIAG_ROWS_PER_CTA;
   diag_rows_kernel<T><<<(unsigned)grid, DIAG_THREADS, 0, st>>>(*A);
   count_launch();
@@ -1108,6 +1113,41 @@ static int ucj_layer(void* x, void* tmp, int norb, int na, int nb, const SectorP
     return FFGB_OK;
   }
   return rotate_both<T>(x, tmp, norb, na, nb, &p, &p, spec, scr, st, sizeof(T) == 4);
+}
+
+// First UCJ layer from the Hartree-Fock state: W(V) |HF> is the product of
+// one determinant vector per sector, amp(a, b) = det V[occ(a), :n_a] *
+// det V[occ(b), :n_b], so the layer's rotation is one write pass (the
+// determinants in FP64, then the diagonal phase on the outer product) instead
+// of a two-sector rotation.
+template <typename T>
+static int slater_layer(void* x, int norb, int na, int nb, const std::vector<cd>& V, const DiagSpec& spec,
+                        Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const size_t mark = scr.off;
+  SlaterMat M;
+  std::memset(&M, 0, sizeof(M));
+  for (int i = 0; i < norb; ++i)
+    for (int j = 0; j < norb; ++j) {
+      M.v[2 * (i * norb + j)] = V[(size_t)i * norb + j].real();
+      M.v[2 * (i * norb + j) + 1] = V[(size_t)i * norb + j].imag();
+    }
+  void* vecs[2] = {nullptr, nullptr};
+  const int nocc[2] = {na, nb};
+  for (int sct = 0; sct < 2; ++sct) {
+    const long long dim = binom_h(norb, nocc[sct]);
+    const unsigned* strs = nullptr;
+    FFGB_TRY(device_strings(norb, nocc[sct], &strs));
+    vecs[sct] = scr.take((size_t)dim * sizeof(C));
+    if (!vecs[sct]) return fail(FFGB_ERR_OOM, "scratch too small for the determinant vectors");
+    slater_dets_kernel<C><<<(unsigned)((dim + 127) / 128), 128, 0, st>>>(strs, dim, norb, nocc[sct], M,
+                                                                          (C*)vecs[sct]);
+    count_launch();
+    FFGB_CUDA(cudaGetLastError());
+  }
+  FFGB_TRY(diag_rows<T>(nullptr, x, norb, na, nb, spec, false, scr, st, vecs[0], vecs[1]));
+  scr.off = mark;
+  return FFGB_OK;
 }
 
 // DF Hamiltonian terms as (Z spec, rotation V = term basis)
@@ -1758,9 +1798,11 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
   cudaStream_t st = (cudaStream_t)stream;
   const size_t el = dtype == FFGB_C128 ? 16 : 8;
   const long long n = binom_h(norb, na) * binom_h(norb, nb);
+  // from the Hartree-Fock state the first layer is a Slater determinant (below)
+  const bool slater_start = !vec_in && n_reps >= 1;
   if (vec_in) {
     FFGB_CUDA(cudaMemcpyAsync(work, vec_in, (size_t)n * el, cudaMemcpyDeviceToDevice, st));
-  } else {
+  } else if (!slater_start) {
     const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
     if (dtype == FFGB_C64)
       one_hot_kernel<float><<<blocks, 256, 0, st>>>((float2*)work, n);
@@ -1778,6 +1820,12 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
     std::vector<cd> V = matmul(dagger(U, norb), current, norb);
     const double* J = ucj_dcm + (size_t)k * 2 * norb * norb;
     DiagSpec spec = diag_coulomb_spec(norb, J, J + norb * norb, J, 0, 1.0, DIAG_PHASE);
+    if (k == 0 && slater_start) {
+      FFGB_TRY(FFGB_DISPATCH(dtype, slater_layer<float>(work, norb, na, nb, V, spec, scr, st),
+                             slater_layer<double>(work, norb, na, nb, V, spec, scr, st)));
+      current = U;
+      continue;
+    }
     SectorPlan p;
     int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
     if (s) return s;

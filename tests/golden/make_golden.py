@@ -1,9 +1,9 @@
 """Generate golden vectors by running the reference's own Python code.
 
 Run in a container that has the ffsim source tree (read-only) at
-``FFSIM_REF`` (default ``/root/reference``)::
+``FFSIM_REF`` (required: the root of the ffsim source tree)::
 
-    python tests/golden/make_golden.py
+    FFSIM_REF=/path/to/ffsim python tests/golden/make_golden.py
 
 The reference package cannot be imported whole here: its Rust extension
 ``ffsim._lib`` is not built (no Rust toolchain) and ``pyscf`` / ``jax`` are not
@@ -54,7 +54,10 @@ if __name__ == "__main__" and os.environ.get("PYTHONHASHSEED") != "0":
 import numpy as np  # noqa: E402
 import scipy.linalg  # noqa: E402
 
-REF = Path(os.environ.get("FFSIM_REF", "/root/reference"))
+if "FFSIM_REF" not in os.environ:
+    raise SystemExit("set FFSIM_REF to the root of an ffsim source checkout "
+                     "(the directory holding python/ffsim), e.g. FFSIM_REF=/path/to/ffsim python make_golden.py")
+REF = Path(os.environ["FFSIM_REF"])
 PKG = REF / "python" / "ffsim"
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
