@@ -410,15 +410,16 @@ def run_ops(args) -> None:
 
 def run_grad(args) -> None:
     """Gradient workload: norb=12 (6,6), UCJ n_reps=3, DF rank 24, a batch of
-    parameter vectors; energies and adjoint gradients per second, with the
-    directional derivative of one vector checked against central finite
+    parameter vectors: energies and adjoint gradients per second.  The batch
+    runs the Hamiltonian matvec once over all its states
+    (LUCJGradient.value_and_grad_batch); one vector at a time beside it.  The
+    directional derivative of one vector is checked against central finite
     differences of the complex128 energy (h = 1e-5)."""
     import numpy as np
     import torch
 
     import ffsim_gb300 as f
     from ffsim_gb300.gradient import LUCJGradient
-    from ffsim_gb300.serving import LUCJServer, Request
 
     norb, nelec, L, R, B = 12, (6, 6), 3, 24, args.batch
     rng = np.random.default_rng(2026)
@@ -435,16 +436,16 @@ def run_grad(args) -> None:
     grads = [ev.value_and_grad(row, L, ham)[1] for row in batch]
     torch.cuda.synchronize()
     t_seq = time.perf_counter() - t0
-    # the same batch through the serving loop (concurrent streams)
-    srv = LUCJServer(workers=args.workers)
-    reqs = [Request(i, "gradient", norb, nelec, L, row, ham) for i, row in enumerate(batch)]
-    t0 = time.perf_counter()
-    for r in reqs:
-        srv.submit(r)
-    res = srv.drain(B)
-    t_srv = time.perf_counter() - t0
-    srv.close()
-    same = max(float(np.max(np.abs(r.grad - g))) for r, g in zip(res, grads))
+    ev.value_and_grad_batch(batch, L, ham)  # warm: buffers and tables of the batch shape
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(args.steps, 1)):
+        t0 = time.perf_counter()
+        _, gb = ev.value_and_grad_batch(batch, L, ham)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t_batch = statistics.median(times)
+    same = max(float(np.max(np.abs(gb[i] - grads[i]))) for i in range(B))
     # accuracy: directional derivative against FD of the complex128 energy
     d = rng.normal(size=n)
     d /= np.linalg.norm(d)
@@ -455,12 +456,12 @@ def run_grad(args) -> None:
         return f.lucj_energy(op, ham, norb, nelec, dtype=torch.complex128)
 
     fd = (e128(batch[0] + h * d) - e128(batch[0] - h * d)) / (2 * h)
-    rel = abs(grads[0] @ d - fd) / abs(fd)
+    rel = abs(gb[0] @ d - fd) / abs(fd)
     print(json.dumps({
         "metric": "LUCJ energy+gradient evals/s norb=12 (6,6) n_reps=3 rank 24 (complex64, FP64 reductions)",
-        "value": B / t_srv, "unit": "evals/s", "batch": B, "n_params": n, "dtype": "c64",
-        "sequential_evals_per_s": B / t_seq, "concurrent_workers": args.workers,
-        "max_abs_diff_concurrent_vs_sequential": same,
+        "value": B / t_batch, "unit": "evals/s", "batch": B, "n_params": n, "dtype": "c64",
+        "ms_per_batch": 1e3 * t_batch, "sequential_evals_per_s": B / t_seq,
+        "max_abs_diff_batched_vs_sequential": same,
         "fd_check": {"h": h, "directional_rel_err": rel, "bar": 1e-4},
         "data": "synthetic (seeded UCJ parameters near a random operator; Haar term rotations)"}), flush=True)
 
@@ -468,33 +469,82 @@ def run_grad(args) -> None:
 def run_serve(args) -> None:
     """Serving workload: Poisson arrivals of LUCJ energy (80%) and gradient
     (20%) requests, norb uniform over {8,10,12,14,16} at half filling,
-    n_reps in {1,2,3}, DF rank 2*norb; p50/p99 latency and throughput."""
+    n_reps in {1,2,3}, DF rank 2*norb (one Hamiltonian per norb); p50/p99
+    latency and served evaluations per second."""
     import torch
 
     from ffsim_gb300.serving import LUCJServer, latency_stats, replay, synthetic_stream
 
     offsets, reqs = synthetic_stream(args.requests, rate=args.rate, seed=2026)
     # warm the shapes (plans, string tables, kernels) outside the measurement
-    warm = LUCJServer(workers=1)
-    _, wreqs = synthetic_stream(10, rate=1e6, seed=7)
+    warm = LUCJServer(workers=1, max_batch=2)
+    _, wreqs = synthetic_stream(15, rate=1e6, seed=7)
     for r in wreqs:
         warm.submit(r)
     warm.drain(len(wreqs))
     warm.close()
+    del warm
+    torch.cuda.empty_cache()
     torch.cuda.synchronize()
-    srv = LUCJServer(workers=args.workers)
+    srv = LUCJServer(workers=args.workers, max_batch=args.max_batch)
     res = replay(srv, offsets, reqs)
     srv.close()
     st = latency_stats(res)
     n_grad = sum(r.kind == "gradient" for r in reqs)
+    by_norb = {}
+    for r, q in zip(res, reqs):
+        if r.ok:
+            by_norb.setdefault(q.norb, []).append(r.latency)
     print(json.dumps({
         "metric": "LUCJ serving evals/s, mixed norb {8..16} half filling, n_reps {1,2,3}, 80% energy / 20% "
                   "gradient, Poisson arrivals; p50/p99 ms",
         "value": st["evals_per_s"], "unit": "evals/s", "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-        "requests": len(reqs), "gradients": n_grad, "arrival_rate_per_s": args.rate,
-        "workers": args.workers, "max_concurrent": srv.max_concurrent, "span_s": st["span_s"],
-        "dtype": "c64", "sample": f"{len(reqs)} requests of the 10,000-request stream (seed 2026)",
+        "requests": len(reqs), "completed": st["completed"], "gradients": n_grad,
+        "arrival_rate_per_s": args.rate, "workers": args.workers, "max_batch": args.max_batch,
+        "mean_batch": statistics.mean(srv.batch_sizes), "max_concurrent": srv.max_concurrent,
+        "span_s": st["span_s"],
+        "p50_ms_by_norb": {m: 1e3 * statistics.median(v) for m, v in sorted(by_norb.items())},
+        "dtype": "c64", "sample": f"{len(reqs)} requests of the stream (seed 2026)",
         "data": "synthetic"}), flush=True)
+
+
+def time_served(ucj_seed: int, n_requests: int, workers: int, max_batch: int) -> dict:
+    """Served complex64 LUCJ energies of the metric's workload (norb=16, (8,8),
+    n_reps=2, one rank-32 Hamiltonian) through the serving loop, every request
+    submitted at once (the server saturated): evaluations per second from the
+    first submission to the last result, with p50/p99 latency."""
+    import numpy as np
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300.serving import LUCJServer, Request, latency_stats
+
+    ham = f.random.random_df_hamiltonian_normal(NORB, rank=RANK, seed=ucj_seed + 1)
+    base = f.random.random_ucj_op_spin_balanced(NORB, n_reps=N_REPS, diag_coulomb_normal=True,
+                                                diag_coulomb_scale=0.1, seed=ucj_seed).to_parameters()
+    rng = np.random.default_rng(ucj_seed)
+    srv = LUCJServer(workers=workers, max_batch=max_batch)
+    warm = [Request(-1 - i, "energy", NORB, NELEC, N_REPS, base, ham) for i in range(max_batch)]
+    for r in warm:
+        srv.submit(r)
+    srv.drain(len(warm))
+    torch.cuda.synchronize()
+    srv._results.clear()
+    srv.batch_sizes.clear()
+    reqs = [Request(i, "energy", NORB, NELEC, N_REPS, base + 0.01 * rng.normal(size=base.size), ham)
+            for i in range(n_requests)]
+    t0 = time.perf_counter()
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(n_requests)
+    t1 = time.perf_counter()
+    srv.close()
+    del srv
+    torch.cuda.empty_cache()
+    st = latency_stats(res)
+    return {"value": n_requests / (t1 - t0), "unit": "evals/s", "requests": n_requests, "workers": workers,
+            "max_batch": max_batch, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+            "completed": st["completed"]}
 
 
 def cpu_reference_sample(threads: int | None = None):
@@ -587,7 +637,9 @@ def main():
     ap.add_argument("--serve", action="store_true", help="serving workload (mixed requests, Poisson arrivals)")
     ap.add_argument("--requests", type=int, default=300, help="--serve: requests")
     ap.add_argument("--rate", type=float, default=4.0, help="--serve: mean arrivals per second")
-    ap.add_argument("--workers", type=int, default=6, help="--serve/--grad: concurrent requests")
+    ap.add_argument("--workers", type=int, default=2, help="--serve: batches in flight")
+    ap.add_argument("--max-batch", type=int, default=16, help="--serve: states per batch")
+    ap.add_argument("--served", type=int, default=8, help="norb-16 requests of the served measurement (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.ops:
@@ -652,6 +704,9 @@ def main():
     h2d = sum(np.asarray(x).nbytes for x in (ucj.diag_coulomb_mats, ucj.orbital_rotations,
                                               ham.one_body_tensor, ham.diag_coulomb_mats, ham.orbital_rotations))
 
+    # served through the continuous-batching loop (the same workload, saturated)
+    served = time_served(2026 + rank, args.served, workers=2, max_batch=4) if args.served > 0 else None
+
     # dominant kernel roofline
     st = stage_rooflines(stream)
     traffic, traffic_src = window_stage_traffic()
@@ -694,6 +749,7 @@ def main():
                      "rotation_ms": rot128_ms, "rotation_tflops": rotation_flops(NORB, NELEC) / rot128_ms / 1e9,
                      "rotation_frac_of_fp64": rotation_flops(NORB, NELEC) / rot128_ms / 1e9 / fp[0]},
             "fp32_peak_tflops": fp[1],
+            "served": served,
             "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": 8 * (RANK + 2)},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",

@@ -30,7 +30,7 @@ from ffsim_gb300.bitstring import (
     bitstring_to_occupied_orbitals,
     strings_to_addresses,
 )
-from ffsim_gb300.energy import LUCJEnergy, lucj_energy
+from ffsim_gb300.energy import BatchLUCJEnergy, LUCJEnergy, lucj_energies, lucj_energy
 from ffsim_gb300.gradient import LUCJGradient, lucj_energy_autograd
 from ffsim_gb300.gates import (
     apply_diag_coulomb_evolution,
@@ -88,6 +88,7 @@ __all__ = [
     "HopGateAnsatzOperator",
     "NumNumAnsatzOpSpinBalanced",
     "LUCJEnergy",
+    "BatchLUCJEnergy",
     "LinearOperator",
     "MolecularHamiltonian",
     "UCJAnglesOpSpinBalanced",
@@ -137,6 +138,7 @@ __all__ = [
     "linear_operator",
     "multireference_state",
     "lucj_energy",
+    "lucj_energies",
     "random",
     "slater_determinant",
     "slater_determinant_amplitudes",

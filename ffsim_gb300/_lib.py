@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes
 import threading
+from concurrent.futures import CancelledError
 from pathlib import Path
 
 import numpy as np
@@ -27,6 +28,7 @@ _ERRORS = {
     5: TimeoutError,
     6: NotImplementedError,
     7: ArithmeticError,
+    8: CancelledError,
 }
 
 _c_void_p = ctypes.c_void_p
@@ -78,6 +80,11 @@ SIGNATURES = {
                             _c_double, _c_int, _dp, _dp, _c_void_p, _c_size_t, _c_void_p],
     "ffgb_lucj_energy": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _dp, _dp, _dp,
                          _dp, _c_int, _dp, _dp, _c_double, _dp, _c_void_p, _c_size_t, _c_void_p],
+    "ffgb_batch_scratch_bytes": [_c_int, _c_int, _c_int, _c_int, _c_int, _c_ll],
+    "ffgb_batch_lucj_energy": [_c_void_p, _c_ll, _c_int, _c_int, _c_int, _c_int, _c_int, _dp, _dp, _dp, _dp, _c_int,
+                               _dp, _dp, _c_double, _dp, _c_void_p, _c_size_t, _c_void_p, _c_void_p],
+    "ffgb_batch_df_matvec": [_c_void_p, _c_void_p, _c_ll, _c_int, _c_int, _c_int, _c_int, _dp, _c_int, _dp, _dp,
+                             _c_double, _c_int, _c_void_p, _c_size_t, _c_void_p, _c_void_p],
     "ffgb_transition_rdm1": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _c_void_p, _c_size_t,
                              _c_void_p],
     "ffgb_pair_density": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _c_void_p, _c_size_t,
@@ -85,6 +92,27 @@ SIGNATURES = {
     "ffgb_vdot": [_c_void_p, _c_void_p, _c_int, _c_ll, _dp, _c_void_p],
     "ffgb_hartree_fock": [_c_void_p, _c_int, _c_ll, _c_void_p],
 }
+
+class Control(ctypes.Structure):
+    """``ffgb_control`` of a batch call: a cancellation flag that another
+    thread sets with ``request_cancel()`` and a deadline in seconds (<= 0:
+    none).  Pass ``control.ptr``."""
+
+    _fields_ = [("cancel", ctypes.POINTER(ctypes.c_int)), ("timeout_s", ctypes.c_double)]
+
+    def __init__(self, timeout_s: float = 0.0):
+        super().__init__()
+        self._flag = ctypes.c_int(0)
+        self.cancel = ctypes.pointer(self._flag)
+        self.timeout_s = float(timeout_s)
+
+    def request_cancel(self) -> None:
+        self._flag.value = 1
+
+    @property
+    def ptr(self):
+        return ctypes.byref(self)
+
 
 _lock = threading.Lock()
 _lib = None
@@ -108,6 +136,7 @@ def load() -> ctypes.CDLL:
             fn.restype = _c_int
         lib.ffgb_last_error.restype = ctypes.c_char_p
         lib.ffgb_scratch_bytes.restype = _c_size_t
+        lib.ffgb_batch_scratch_bytes.restype = _c_size_t
         lib.ffgb_launch_count.restype = _c_ll
         lib.ffgb_device_alloc_count.restype = _c_ll
         _lib = lib

@@ -55,6 +55,8 @@ struct StageExpectArgs {
   long long partial_cap = 0;
   float X[FFGB_MAXN][FFGB_MAXN] = {};
   int zrep = 0;
+  long long col_period = 0;  // stacked states: column c is string c mod col_period (0: one state)
+  long long col_valid = 0;   // strings per state (columns col_valid..col_period-1 are zero padding)
 };
 
 struct StageOpts {
@@ -63,6 +65,7 @@ struct StageOpts {
   const StageExpectArgs* expect = nullptr;  // last stage reduces instead of storing
   int* expect_ctas = nullptr;               // partials written by the fused expectation
   int only_stage = -1;  // >= 0: run only this stage (0 B1, 1 B2, 2 cross-half, 3 A1, 4 A2), in place
+  long long col_period = 0;  // stacked states: dither column c as column c mod col_period
 };
 
 // Stage-major complex64 rotation of the sector whose strings index the rows
@@ -74,6 +77,11 @@ int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long l
 // Upper bound of the partial sums written by a fused expectation on a state
 // of `rows` rows (the rotated sector's strings) and ncols columns.
 long long stage_expect_partials(long long rows, long long ncols);
+
+// States stacked side by side along the columns are padded to whole column
+// tiles of the stage kernels, so that no tile holds two states.
+constexpr long long STACK_TILE = 128;
+inline long long stack_pad(long long n) { return (n + STACK_TILE - 1) / STACK_TILE * STACK_TILE; }
 
 // Densities between two states (grad.cu); results summed on the host in FP64.
 template <typename T>
@@ -87,6 +95,22 @@ size_t density_partial_bytes(int norb, long long rows);
 template <typename T>
 int launch_transpose(const void* in, void* out, long long rows, long long cols, const void* row_ph,
                      const void* col_ph, cudaStream_t st);
+// The same for n_states states side by side along the columns: state b is
+// columns [b * in_pad, b * in_pad + cols) of `in` (row stride n_states *
+// in_pad) and becomes columns [b * out_pad, b * out_pad + rows) of `out`
+// (row stride n_states * out_pad).  Padding columns are not written.
+template <typename T>
+int launch_transpose_stacked(const void* in, void* out, long long rows, long long cols, long long n_states,
+                             long long in_pad, long long out_pad, const void* row_ph, cudaStream_t st);
+// Contiguous states x[b] (rows x cols) <-> stacked y (pad columns per state):
+// dir 0 x -> y, dir 1 y -> x (accumulate: x += y).
+template <typename T>
+int launch_stack(void* x, void* y, long long n_states, long long rows, long long cols, long long pad, int dir,
+                 int accumulate, cudaStream_t st);
+// Per-state sums of n per-CTA partials of a stacked stage (tiles column tiles
+// per stage, tiles_per_state per state) into out[0..n_states).
+int launch_state_partials(const double* partials, long long n, long long tiles, long long tiles_per_state,
+                          long long n_states, double* out, cudaStream_t st);
 template <typename T>
 int launch_string_phases(const unsigned* strings, long long dim, int norb, const double* d_host, void* out,
                          cudaStream_t st);

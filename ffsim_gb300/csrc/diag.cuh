@@ -32,6 +32,10 @@ struct DiagRowsArgs {
   // (a product state, e.g. a rotated Hartree-Fock state) and `in` is not read
   const C* outer_row;
   const C* outer_col;
+  // stacked states (0: one state): each row holds ld columns, column c is
+  // string c mod col_period, and columns whose index is >= cols (zero
+  // padding) read the last string's entries
+  long long ld, col_period;
 };
 
 // Per row, the row term and the cross term are tabulated over the two halves
@@ -101,12 +105,14 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
       }
     }
     __syncthreads();
-    const C* xin = A.in + r * A.cols;
-    C* xout = A.out + r * A.cols;
+    const long long ld = A.col_period ? A.ld : A.cols;
+    const C* xin = A.in + r * ld;
+    C* xout = A.out + r * ld;
     const C orow = A.outer_row ? A.outer_row[r] : cmake<C>(0.0, 0.0);
-    for (long long c = tid; c < A.cols; c += DIAG_THREADS) {
+    for (long long c0 = tid; c0 < ld; c0 += DIAG_THREADS) {
+      const long long c = A.col_period ? min(c0 % A.col_period, A.cols - 1) : c0;
       const unsigned s = A.cstr[c];
-      C v = A.outer_row ? cmul(orow, A.outer_col[c]) : xin[c];
+      C v = A.outer_row ? cmul(orow, A.outer_col[c]) : xin[c0];
       if (!phase) {
         const T z = ul[s & lmask] + uh[s >> h] + ((const T*)A.col_table)[c];
         if (A.partials) {
@@ -119,12 +125,12 @@ __global__ void __launch_bounds__(DIAG_THREADS) diag_rows_kernel(const __grid_co
         v = cmul(cmul(v, ((const C*)A.col_table)[c]), cmul(tl[s & lmask], th[s >> h]));
       }
       if (A.accumulate) {
-        C o = xout[c];
+        C o = xout[c0];
         o.x += v.x;
         o.y += v.y;
         v = o;
       }
-      xout[c] = v;
+      xout[c0] = v;
     }
     __syncthreads();  // the next row overwrites the tables
   }

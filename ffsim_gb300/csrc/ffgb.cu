@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -42,6 +43,10 @@ static long long binom_h(int n, int k) {
   for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
   return r;
 }
+
+// the complex64 or complex128 instantiation of a templated call
+#define FFGB_DISPATCH(dtype, call_f, call_d) \
+  ((dtype) == FFGB_C64 ? (call_f) : (call_d))
 
 // ---------------------------------------------------------------------------
 // per-device occupation-string tables
@@ -544,7 +549,7 @@ static void fold_col_phases(DiagSpec& spec, const SectorPlan& p, int norb) {
 template <typename T>
 static int diag_rows(const void* in, void* out, int norb, int row_nocc, int col_nocc, const DiagSpec& spec,
                      bool accumulate, Scratch& scr, cudaStream_t st, const void* outer_row = nullptr,
-                     const void* outer_col = nullptr) {
+                     const void* outer_col = nullptr, long long n_stacked = 0) {
   using C = typename CT<T>::type;
   const long long rows = binom_h(norb, row_nocc), cols = binom_h(norb, col_nocc);
   if (rows <= 0 || cols <= 0) return FFGB_OK;
@@ -577,6 +582,10 @@ static int diag_rows(const void* in, void* out, int norb, int row_nocc, int col_
   if (outer_row && outer_col) {
     A->outer_row = (const C*)outer_row;
     A->outer_col = (const C*)outer_col;
+  }
+  if (n_stacked > 0) {  // n_stacked states side by side, padded to whole column tiles
+    A->col_period = stack_pad(cols);
+    A->ld = n_stacked * A->col_period;
   }
   const long long grid = (rows + DIAG_ROWS_PER_CTA - 1) / DIAG_ROWS_PER_CTA;
   diag_rows_kernel<T><<<(unsigned)grid, DIAG_THREADS, 0, st>>>(*A);
@@ -1150,6 +1159,36 @@ static int slater_layer(void* x, int norb, int na, int nb, const std::vector<cd>
   return FFGB_OK;
 }
 
+// The UCJ layers of ffgb_lucj_energy on `work` (from the Hartree-Fock state
+// when slater_start, the first layer then a Slater determinant; otherwise from
+// the state already in `work`), with the circuit's last rotation left out:
+// `basis` returns it (U_L), to be applied or merged into what follows.
+static int ucj_layers(void* work, void* tmp, int dtype, int norb, int na, int nb, int n_reps, const double* ucj_dcm,
+                      const double* ucj_rots, bool slater_start, Scratch& scr, cudaStream_t st,
+                      std::vector<cd>& basis) {
+  basis = eye(norb);
+  for (int k = 0; k < n_reps; ++k) {
+    std::vector<cd> U = load_mat(ucj_rots + (size_t)k * norb * norb * 2, norb);
+    std::vector<cd> V = matmul(dagger(U, norb), basis, norb);
+    const double* J = ucj_dcm + (size_t)k * 2 * norb * norb;
+    DiagSpec spec = diag_coulomb_spec(norb, J, J + norb * norb, J, 0, 1.0, DIAG_PHASE);
+    if (k == 0 && slater_start) {
+      FFGB_TRY(dtype == FFGB_C64 ? slater_layer<float>(work, norb, na, nb, V, spec, scr, st)
+                                 : slater_layer<double>(work, norb, na, nb, V, spec, scr, st));
+      basis = U;
+      continue;
+    }
+    SectorPlan p;
+    int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
+    if (s) return s;
+    s = dtype == FFGB_C64 ? ucj_layer<float>(work, tmp, norb, na, nb, p, &spec, 20u + (unsigned)k, scr, st)
+                          : ucj_layer<double>(work, tmp, norb, na, nb, p, &spec, 0, scr, st);
+    if (s) return s;
+    basis = U;
+  }
+  return FFGB_OK;
+}
+
 // DF Hamiltonian terms as (Z spec, rotation V = term basis)
 struct Term {
   DiagSpec spec;
@@ -1248,6 +1287,222 @@ static int df_expectation_impl(const void* vec, int norb, int na, int nb, const 
   for (size_t k = 0; k < terms.size(); ++k) e += h[k];
   *energy = e;
   return FFGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batches: n states of one shape under one Hamiltonian
+// ---------------------------------------------------------------------------
+// The Hamiltonian's terms are shared by every state of a batch, so each term
+// runs once over all of them: the states sit side by side along the columns
+// ("stacked"), alpha rows [dim_a][n * pad_b] or beta rows [dim_b][n * pad_a],
+// each state padded with zero columns to whole column tiles.  The stage
+// kernels act on every column independently, so one launch per stage covers
+// the batch; zero columns stay zero.  The coefficient dithering of a column
+// is that of its column within its state and each column tile belongs to one
+// state, so a state's result is the same as when it runs alone (up to the
+// order of the final FP64 sums).
+struct Stack {
+  long long n, da, db, pa, pb;
+  size_t ybytes() const { return (size_t)(da * n * pb) * sizeof(float2); }  // alpha rows
+  size_t tbytes() const { return (size_t)(db * n * pa) * sizeof(float2); }  // beta rows
+};
+
+static StageOpts stack_opts(unsigned salt, long long period) {
+  StageOpts o;
+  o.mode = STAGE_MODE;
+  o.salt = salt;
+  o.col_period = period;
+  return o;
+}
+
+// <phi_b| Z |phi_b> for every state b of the stack Y (alpha rows, not
+// modified), phi_b = W(V) psi_b, into slots[0..n) (device).  Y1 and T are
+// stacked scratch; T's padding columns must be zero.
+static int stack_expectation_term(const void* Y, void* Y1, void* T, const Stack& d, int norb, int na, int nb,
+                                  const DiagSpec& spec, const SectorPlan& pv, double* slots, unsigned salt,
+                                  Scratch& scr, cudaStream_t st) {
+  const size_t mark = scr.off;
+  FFGB_TRY(stage_rotate_rows(Y, Y1, norb, na, d.n * d.pb, d.n * d.pb, pv, stack_opts(2 * salt, d.pb), st));
+  FFGB_TRY(launch_transpose_stacked<float>(Y1, T, d.da, d.db, d.n, d.pb, d.pa, nullptr, st));
+  StageExpectArgs ex;
+  FFGB_TRY(expect_tables(norb, na, nb, spec, scr, st, ex));
+  ex.col_period = d.pa;
+  ex.col_valid = d.da;
+  ex.partial_cap = stage_expect_partials(d.db, d.n * d.pa);
+  ex.partials = (double*)scr.take(sizeof(double) * (size_t)ex.partial_cap);
+  if (!ex.partials) return fail(FFGB_ERR_OOM, "scratch too small for partial sums");
+  int nct = 0;
+  StageOpts o = stack_opts(2 * salt + 1, d.pa);
+  o.expect = &ex;
+  o.expect_ctas = &nct;
+  FFGB_TRY(stage_rotate_rows(T, T, norb, nb, d.n * d.pa, d.n * d.pa, pv, o, st));
+  FFGB_TRY(launch_state_partials(ex.partials, nct, d.n * d.pa / STACK_TILE, d.pa / STACK_TILE, d.n, slots, st));
+  scr.off = mark;
+  return FFGB_OK;
+}
+
+// Yacc += W(U) Z W(U)^dag psi_b for every state of the stack Y (alpha rows,
+// not modified); the stage path of rotated_matvec_impl over the whole stack.
+// Y1 and T are stacked scratch; T's padding columns must be zero.
+static int stack_rotated_matvec(const void* Y, void* Yacc, void* Y1, void* T, const Stack& d, int norb, int na,
+                                int nb, const DiagSpec& spec, const SectorPlan& pd, const SectorPlan& pu,
+                                Scratch& scr, cudaStream_t st) {
+  const size_t mark = scr.off;
+  const long long ya = d.n * d.pb, tb = d.n * d.pa;  // row lengths of the two layouts
+  const void *fa = nullptr, *fb = nullptr;
+  FFGB_TRY(phase_table(&pd, norb, na, scr, st, &fa));
+  FFGB_TRY(phase_table(&pd, norb, nb, scr, st, &fb));
+  FFGB_TRY(stage_rotate_rows(Y, Y1, norb, na, ya, ya, pd, stack_opts(8, d.pb), st));
+  FFGB_TRY(launch_transpose_stacked<float>(Y1, T, d.da, d.db, d.n, d.pb, d.pa, fa, st));
+  FFGB_TRY(stage_rotate_rows(T, T, norb, nb, tb, tb, pd, stack_opts(9, d.pa), st));
+  if (fb) FFGB_TRY(launch_row_scale<float>(T, d.db, tb, fb, st));
+  FFGB_TRY(diag_rows<float>(T, T, norb, nb, na, spec.transposed(), false, scr, st, nullptr, nullptr, d.n));
+  scr.off = mark;
+  FFGB_TRY(phase_table(&pu, norb, na, scr, st, &fa));
+  FFGB_TRY(phase_table(&pu, norb, nb, scr, st, &fb));
+  FFGB_TRY(stage_rotate_rows(T, T, norb, nb, tb, tb, pu, stack_opts(11, d.pa), st));
+  FFGB_TRY(launch_transpose_stacked<float>(T, Y1, d.db, d.da, d.n, d.pa, d.pb, fb, st));
+  FFGB_TRY(stage_rotate_rows(Y1, Y1, norb, na, ya, ya, pu, stack_opts(10, d.pb), st));
+  if (fa) FFGB_TRY(launch_row_scale<float>(Y1, d.da, ya, fa, st));
+  FFGB_TRY(launch_axpy<float>(Y1, Yacc, d.da * ya, 1.0, st));
+  scr.off = mark;
+  return FFGB_OK;
+}
+
+// Host-side control of a batch call: cancellation and deadline checks
+// between units of work (a state's circuit, a Hamiltonian term), with at most
+// two units queued on the stream ahead of the GPU so that a check acts within
+// about two units.
+class Pacer {
+ public:
+  Pacer(const ffgb_control* c, cudaStream_t st) : c_(c), st_(st), t0_(std::chrono::steady_clock::now()) {}
+  ~Pacer() {
+    for (cudaEvent_t e : ev_)
+      if (e) cudaEventDestroy(e);
+  }
+  // before enqueueing unit k
+  int before(long long k) {
+    if (!c_) return FFGB_OK;
+    if (k >= 2 && ev_[k % 2]) FFGB_CUDA(cudaEventSynchronize(ev_[k % 2]));  // unit k - 2 has finished
+    if (c_->cancel && *c_->cancel) return fail(FFGB_ERR_CANCELLED, "cancelled after " + std::to_string(k) + " units");
+    if (c_->timeout_s > 0) {
+      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
+      if (dt > c_->timeout_s)
+        return fail(FFGB_ERR_TIMEOUT, "deadline of " + std::to_string(c_->timeout_s) + " s passed after " +
+                                          std::to_string(k) + " units");
+    }
+    return FFGB_OK;
+  }
+  // after enqueueing unit k
+  int after(long long k) {
+    if (!c_) return FFGB_OK;
+    cudaEvent_t& e = ev_[k % 2];
+    if (!e) FFGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    FFGB_CUDA(cudaEventRecord(e, st_));
+    return FFGB_OK;
+  }
+
+ private:
+  const ffgb_control* c_;
+  cudaStream_t st_;
+  std::chrono::steady_clock::time_point t0_;
+  cudaEvent_t ev_[2] = {nullptr, nullptr};
+};
+
+// Whether a batch runs stacked: complex64 on the stage path (every term's
+// rotation a cosine-sine plan); otherwise the states run one by one.
+static int stack_plans(int dtype, int norb, int na, int nb, const std::vector<Term>& terms, bool both_ways,
+                       std::vector<SectorPlan>& pd, std::vector<SectorPlan>& pu, bool& stacked) {
+  stacked = dtype == FFGB_C64 && nb >= 0 && !big_rows<float>(norb, na, nb);
+  if (!stacked) return FFGB_OK;
+  pd.resize(terms.size());
+  pu.resize(both_ways ? terms.size() : 0);
+  for (size_t k = 0; k < terms.size(); ++k) {
+    FFGB_TRY(make_plan<float>(norb, dagger(terms[k].rot, norb), pd[k]));
+    if (both_ways) FFGB_TRY(make_plan<float>(norb, terms[k].rot, pu[k]));
+    if (!staged<float>(&pd[k], &pd[k]) || (both_ways && !staged<float>(&pu[k], &pu[k]))) stacked = false;
+  }
+  return FFGB_OK;
+}
+
+static Stack make_stack(long long n, int norb, int na, int nb) {
+  Stack d;
+  d.n = n;
+  d.da = binom_h(norb, na);
+  d.db = binom_h(norb, nb);
+  d.pa = stack_pad(d.da);
+  d.pb = stack_pad(d.db);
+  return d;
+}
+
+// Energies of n contiguous states x[b] (complex64 stacked, else one by one).
+static int batch_df_energy(const void* x, long long n, int dtype, int norb, int na, int nb,
+                           const std::vector<Term>& terms, double constant, double* energies, Scratch& scr,
+                           cudaStream_t st, Pacer& pace, long long unit0) {
+  std::vector<SectorPlan> pd, pu;
+  bool stacked = false;
+  FFGB_TRY(stack_plans(dtype, norb, na, nb, terms, false, pd, pu, stacked));
+  const long long dim = binom_h(norb, na) * binom_h(norb, nb);
+  if (!stacked) {
+    const size_t el = dtype == FFGB_C128 ? 16 : 8;
+    for (long long b = 0; b < n; ++b) {
+      FFGB_TRY(pace.before(unit0 + b));
+      const size_t mark = scr.off;
+      const void* xb = (const char*)x + (size_t)(b * dim) * el;
+      FFGB_TRY(FFGB_DISPATCH(dtype,
+                             df_expectation_impl<float>(xb, norb, na, nb, terms, nullptr, constant, energies + b,
+                                                        scr, st),
+                             df_expectation_impl<double>(xb, norb, na, nb, terms, nullptr, constant, energies + b,
+                                                         scr, st)));
+      scr.off = mark;
+      FFGB_TRY(pace.after(unit0 + b));
+    }
+    return FFGB_OK;
+  }
+  const Stack d = make_stack(n, norb, na, nb);
+  void* Y = scr.take(d.ybytes());
+  void* Y1 = scr.take(d.ybytes());
+  void* T = scr.take(d.tbytes());
+  double* slots = (double*)scr.take(sizeof(double) * (size_t)(n * std::max<size_t>(terms.size(), 1)));
+  if (!Y || !Y1 || !T || !slots) return fail(FFGB_ERR_OOM, "scratch too small for the stacked batch");
+  FFGB_CUDA(cudaMemsetAsync(Y, 0, d.ybytes(), st));
+  FFGB_CUDA(cudaMemsetAsync(T, 0, d.tbytes(), st));
+  FFGB_TRY(launch_stack<float>(const_cast<void*>(x), Y, n, d.da, d.db, d.pb, 0, 0, st));
+  for (size_t k = 0; k < terms.size(); ++k) {
+    FFGB_TRY(pace.before(unit0 + (long long)k));
+    FFGB_TRY(stack_expectation_term(Y, Y1, T, d, norb, na, nb, terms[k].spec, pd[k], slots + k * n,
+                                    100u + (unsigned)k, scr, st));
+    FFGB_TRY(pace.after(unit0 + (long long)k));
+  }
+  std::vector<double> h((size_t)n * terms.size(), 0.0);
+  if (!terms.empty())
+    FFGB_CUDA(cudaMemcpyAsync(h.data(), slots, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+  FFGB_CUDA(cudaStreamSynchronize(st));
+  for (long long b = 0; b < n; ++b) {
+    double e = constant;
+    for (size_t k = 0; k < terms.size(); ++k) e += h[k * n + b];
+    energies[b] = e;
+  }
+  return FFGB_OK;
+}
+
+static size_t batch_scratch(int op, int dtype, int norb, int na, int nb, long long n) {
+  const size_t el = dtype == FFGB_C128 ? 16 : 8;
+  const long long da = binom_h(norb, na), db = nb >= 0 ? binom_h(norb, nb) : 1;
+  const size_t S = (size_t)(da * db) * el;
+  const size_t ex = extras_bytes(norb, na, nb) + 4096;
+  const Stack d = make_stack(n, norb, na, std::max(nb, 0));
+  // per-state path (a circuit, or states that do not stack): two states
+  size_t need = 2 * S + ex;
+  if (dtype == FFGB_C64 && nb >= 0) {
+    const size_t partials = sizeof(double) * (size_t)stage_expect_partials(d.db, d.n * d.pa);
+    // energy slots: n per term, for up to 2 norb^2 + 1 terms (a molecular
+    // Hamiltonian's exact factorization has at most 2 norb^2)
+    const size_t slots = (size_t)n * 8 * (2 * (size_t)norb * norb + 2);
+    const size_t stack = op == 0 ? 2 * d.ybytes() + d.tbytes() + partials + slots : 3 * d.ybytes() + d.tbytes();
+    need = std::max(need, stack + ex + 4096);
+  }
+  return need;
 }
 
 // ---------------------------------------------------------------------------
@@ -1519,8 +1774,6 @@ size_t ffgb_scratch_bytes(int op, int dtype, int norb, int na, int nb) {
   return S + ex;
 }
 
-#define FFGB_DISPATCH(dtype, call_f, call_d) \
-  ((dtype) == FFGB_C64 ? (call_f) : (call_d))
 
 int ffgb_apply_givens_rotation(void* vec, int dtype, int norb, int na, int nb, int spin, double c,
                                double s_re, double s_im, int i, int j, void* stream) {
@@ -1814,26 +2067,8 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
   Scratch scr(scratch, scratch_bytes);
   void* tmp = scr.take((size_t)n * el);
   if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
-  std::vector<cd> current = eye(norb);
-  for (int k = 0; k < n_reps; ++k) {
-    std::vector<cd> U = load_mat(ucj_rots + (size_t)k * norb * norb * 2, norb);
-    std::vector<cd> V = matmul(dagger(U, norb), current, norb);
-    const double* J = ucj_dcm + (size_t)k * 2 * norb * norb;
-    DiagSpec spec = diag_coulomb_spec(norb, J, J + norb * norb, J, 0, 1.0, DIAG_PHASE);
-    if (k == 0 && slater_start) {
-      FFGB_TRY(FFGB_DISPATCH(dtype, slater_layer<float>(work, norb, na, nb, V, spec, scr, st),
-                             slater_layer<double>(work, norb, na, nb, V, spec, scr, st)));
-      current = U;
-      continue;
-    }
-    SectorPlan p;
-    int s = dtype == FFGB_C64 ? make_plan<float>(norb, V, p) : make_plan<double>(norb, V, p);
-    if (s) return s;
-    s = dtype == FFGB_C64 ? ucj_layer<float>(work, tmp, norb, na, nb, p, &spec, 20u + (unsigned)k, scr, st)
-                          : ucj_layer<double>(work, tmp, norb, na, nb, p, &spec, 0, scr, st);
-    if (s) return s;
-    current = U;
-  }
+  std::vector<cd> current;
+  FFGB_TRY(ucj_layers(work, tmp, dtype, norb, na, nb, n_reps, ucj_dcm, ucj_rots, slater_start, scr, st, current));
   std::vector<cd> final_basis = ucj_final ? matmul(load_mat(ucj_final, norb), current, norb) : current;
   std::vector<Term> terms;
   df_terms(norb, one_body, n_terms, dcm, rots, 0, terms);
@@ -1841,6 +2076,113 @@ int ffgb_lucj_energy(const void* vec_in, void* work, int dtype, int norb, int na
   return FFGB_DISPATCH(dtype,
                        df_expectation_impl<float>(work, norb, na, nb, terms, &final_basis, constant, energy_out, scr, st),
                        df_expectation_impl<double>(work, norb, na, nb, terms, &final_basis, constant, energy_out, scr, st));
+}
+
+size_t ffgb_batch_scratch_bytes(int op, int dtype, int norb, int na, int nb, long long n_states) {
+  if (n_states <= 0 || norb < 0 || norb > FFGB_MAXN) return 0;
+  return batch_scratch(op, dtype, norb, na, nb, n_states);
+}
+
+int ffgb_batch_lucj_energy(void* work, long long n_states, int dtype, int norb, int na, int nb, int n_reps,
+                           const double* ucj_dcm, const double* ucj_rots, const double* ucj_final,
+                           const double* one_body, int n_terms, const double* dcm, const double* rots,
+                           double constant, double* energies_out, void* scratch, size_t scratch_bytes,
+                           const ffgb_control* control, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({work, energies_out}));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "LUCJ energy needs a spinful system");
+  if (n_states <= 0) return fail(FFGB_ERR_ARG, "n_states must be positive");
+  if (n_reps < 1) return fail(FFGB_ERR_ARG, "a batch needs n_reps >= 1");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t el = dtype == FFGB_C128 ? 16 : 8;
+  const long long dim = binom_h(norb, na) * binom_h(norb, nb);
+  Scratch scr(scratch, scratch_bytes);
+  Pacer pace(control, st);
+  {
+    // each state's circuit, with its last rotation applied (it cannot merge
+    // into the shared Hamiltonian terms)
+    const size_t mark = scr.off;
+    void* tmp = scr.take((size_t)dim * el);
+    if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
+    const size_t per_dcm = (size_t)n_reps * 2 * norb * norb, per_rot = (size_t)n_reps * norb * norb * 2;
+    for (long long b = 0; b < n_states; ++b) {
+      FFGB_TRY(pace.before(b));
+      void* xb = (char*)work + (size_t)(b * dim) * el;
+      std::vector<cd> basis;
+      FFGB_TRY(ucj_layers(xb, tmp, dtype, norb, na, nb, n_reps, ucj_dcm + b * per_dcm, ucj_rots + b * per_rot, true,
+                          scr, st, basis));
+      if (ucj_final) basis = matmul(load_mat(ucj_final + (size_t)b * norb * norb * 2, norb), basis, norb);
+      std::vector<double> m(2 * (size_t)norb * norb);
+      for (size_t i = 0; i < basis.size(); ++i) {
+        m[2 * i] = basis[i].real();
+        m[2 * i + 1] = basis[i].imag();
+      }
+      const size_t mark2 = scr.off;
+      FFGB_TRY(FFGB_DISPATCH(dtype,
+                             orbital_rotation_impl<float>(xb, norb, na, nb, m.data(), m.data(), scr, st),
+                             orbital_rotation_impl<double>(xb, norb, na, nb, m.data(), m.data(), scr, st)));
+      scr.off = mark2;
+      FFGB_TRY(pace.after(b));
+    }
+    scr.off = mark;
+  }
+  std::vector<Term> terms;
+  df_terms(norb, one_body, n_terms, dcm, rots, 0, terms);
+  return batch_df_energy(work, n_states, dtype, norb, na, nb, terms, constant, energies_out, scr, st, pace,
+                         n_states);
+}
+
+int ffgb_batch_df_matvec(const void* vec, void* out, long long n_states, int dtype, int norb, int na, int nb,
+                         const double* one_body, int n_terms, const double* dcm, const double* rots, double constant,
+                         int zrep, void* scratch, size_t scratch_bytes, const ffgb_control* control, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({vec, out}));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "linear operator needs a spinful system");
+  if (n_states <= 0) return fail(FFGB_ERR_ARG, "n_states must be positive");
+  if (vec == out) return fail(FFGB_ERR_ARG, "out must not alias vec");
+  std::vector<Term> terms;
+  df_terms(norb, one_body, n_terms, dcm, rots, zrep, terms);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<SectorPlan> pd, pu;
+  bool stacked = false;
+  FFGB_TRY(stack_plans(dtype, norb, na, nb, terms, true, pd, pu, stacked));
+  const long long dim = binom_h(norb, na) * binom_h(norb, nb);
+  Pacer pace(control, st);
+  if (!stacked) {
+    const size_t el = dtype == FFGB_C128 ? 16 : 8;
+    for (long long b = 0; b < n_states; ++b) {
+      FFGB_TRY(pace.before(b));
+      FFGB_TRY(ffgb_df_matvec((const char*)vec + (size_t)(b * dim) * el, (char*)out + (size_t)(b * dim) * el,
+                              dtype, norb, na, nb, one_body, n_terms, dcm, rots, constant, zrep, scratch,
+                              scratch_bytes, stream));
+      FFGB_TRY(pace.after(b));
+    }
+    return FFGB_OK;
+  }
+  Scratch scr(scratch, scratch_bytes);
+  const Stack d = make_stack(n_states, norb, na, nb);
+  void* Y = scr.take(d.ybytes());
+  void* Yacc = scr.take(d.ybytes());
+  void* Y1 = scr.take(d.ybytes());
+  void* T = scr.take(d.tbytes());
+  if (!Y || !Yacc || !Y1 || !T) return fail(FFGB_ERR_OOM, "scratch too small for the stacked batch");
+  FFGB_CUDA(cudaMemsetAsync(Y, 0, d.ybytes(), st));
+  FFGB_CUDA(cudaMemsetAsync(Yacc, 0, d.ybytes(), st));
+  FFGB_CUDA(cudaMemsetAsync(T, 0, d.tbytes(), st));
+  FFGB_TRY(launch_stack<float>(const_cast<void*>(vec), Y, n_states, d.da, d.db, d.pb, 0, 0, st));
+  const long long n = n_states * dim;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+  scale_copy_kernel<float><<<blocks, 256, 0, st>>>((const float2*)vec, (float2*)out, n, (float)constant, 0.f);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  for (size_t k = 0; k < terms.size(); ++k) {
+    FFGB_TRY(pace.before((long long)k));
+    FFGB_TRY(stack_rotated_matvec(Y, Yacc, Y1, T, d, norb, na, nb, terms[k].spec, pd[k], pu[k], scr, st));
+    FFGB_TRY(pace.after((long long)k));
+  }
+  return launch_stack<float>(out, Yacc, n_states, d.da, d.db, d.pb, 1, 1, st);
 }
 
 int ffgb_transition_rdm1(const void* x, const void* y, int dtype, int norb, int na, int nb, double* out,

@@ -216,7 +216,7 @@ int launch_cs(const CsStageParams& P, int grid, int mode, cudaStream_t st) {
 }
 
 int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int lo, int hh,
-             const std::vector<Pair2>& cs, int mode, unsigned salt, cudaStream_t st) {
+             const std::vector<Pair2>& cs, int mode, unsigned salt, long long col_period, cudaStream_t st) {
   if (hh > CS_MAX_SITES) return fail(FFGB_ERR_UNSUPPORTED, "too many cross-half sites");
   const CsPass* T = nullptr;
   FFGB_TRY(cs_pass_tables(norb, nocc, lo, hh, &T));
@@ -226,6 +226,7 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int l
   P.ld = ld;
   P.ncols = ncols;
   P.tiles = (int)((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
+  P.col_period = col_period;
   double v[3 * CS_MAX_SITES] = {};
   for (int i = 0; i < hh; ++i) {
     v[3 * i] = cs[i].g00.real();
@@ -346,7 +347,7 @@ int win_layout(int norb, int nocc, int lo, int B, const WinLayout** out) {
 // their registers fit, and k = B/2 is packed within its groups.
 int window_stage(const float2* in, float2* out, long long ld, long long ncols, int norb, int nocc, int lo, int B,
                  const std::vector<Givens>& net, unsigned salt, const StageExpectArgs* ex, int* ex_ctas,
-                 cudaStream_t st) {
+                 long long col_period, cudaStream_t st) {
   if (B < 4 || B > 8) return fail(FFGB_ERR_UNSUPPORTED, "window size outside [4, 8]");
   const WinLayout* L = nullptr;
   FFGB_TRY(win_layout(norb, nocc, lo, B, &L));
@@ -361,6 +362,7 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
   base->norb = norb;
   base->lo = lo;
   base->salt = salt;
+  base->col_period = col_period;
   const int epi = ex ? EPI_EXPECT : EPI_STORE;
   std::vector<double> v(3 * net.size());
   for (size_t g = 0; g < net.size(); ++g) {
@@ -377,6 +379,8 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
     E.row_str = ex->row_str;
     E.col_str = ex->col_str;
     E.zrep = ex->zrep;
+    E.col_period = ex->col_period;
+    E.col_valid = ex->col_valid;
     for (int i = 0; i < FFGB_MAXN; ++i)
       for (int l = 0; l < FFGB_MAXN; ++l) {
         E.X[i][l] = ex->X[i][l];
@@ -450,6 +454,8 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
 
 }  // namespace
 
+static_assert(STACK_TILE == STAGE_THREADS, "stacked states are padded to the stage kernels' column tile");
+
 long long stage_expect_partials(long long rows, long long ncols) {
   return std::max<long long>(rows, 1) * ((ncols + STAGE_THREADS - 1) / STAGE_THREADS);
 }
@@ -475,9 +481,9 @@ int stage_rotate_rows(const void* in, void* out, int norb, int nocc, long long l
     if (op.type == 0) {
       const bool fused = o.expect && i == n_ops - 1 && o.only_stage < 0;
       FFGB_TRY(window_stage(src, dst, ld, ncols, norb, nocc, op.lo, op.b, op.net, s + 1 + i,
-                            fused ? o.expect : nullptr, fused ? o.expect_ctas : nullptr, st));
+                            fused ? o.expect : nullptr, fused ? o.expect_ctas : nullptr, o.col_period, st));
     } else {
-      FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, op.lo, op.b, op.pairs, o.mode, s + 1 + i, st));
+      FFGB_TRY(cs_stage(dst, ld, ncols, norb, nocc, op.lo, op.b, op.pairs, o.mode, s + 1 + i, o.col_period, st));
     }
   }
   return FFGB_OK;
@@ -491,14 +497,58 @@ int launch_transpose(const void* in, void* out, long long rows, long long cols, 
   const long long gy = (rows + 63) / 64;
   if (gy > 65535) return fail(FFGB_ERR_UNSUPPORTED, "transpose: too many rows");
   dim3 grid((unsigned)((cols + 31) / 32), (unsigned)gy);
-  transpose_kernel<Cx><<<grid, 256, 0, st>>>((const Cx*)in, (Cx*)out, rows, cols, (const Cx*)row_ph,
-                                             (const Cx*)col_ph);
+  transpose_kernel<Cx><<<grid, 256, 0, st>>>((const Cx*)in, (Cx*)out, rows, cols, cols, rows, 0, 0,
+                                             (const Cx*)row_ph, (const Cx*)col_ph);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }
 template int launch_transpose<float>(const void*, void*, long long, long long, const void*, const void*,
                                      cudaStream_t);
+
+template <typename T>
+int launch_transpose_stacked(const void* in, void* out, long long rows, long long cols, long long n_states,
+                             long long in_pad, long long out_pad, const void* row_ph, cudaStream_t st) {
+  using Cx = typename CT<T>::type;
+  if (rows <= 0 || cols <= 0 || n_states <= 0) return FFGB_OK;
+  const long long gy = (rows + 63) / 64;
+  if (gy > 65535 || n_states > 65535) return fail(FFGB_ERR_UNSUPPORTED, "stacked transpose: grid too large");
+  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)gy, (unsigned)n_states);
+  transpose_kernel<Cx><<<grid, 256, 0, st>>>((const Cx*)in, (Cx*)out, rows, cols, n_states * in_pad,
+                                             n_states * out_pad, in_pad, out_pad, (const Cx*)row_ph, nullptr);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+template int launch_transpose_stacked<float>(const void*, void*, long long, long long, long long, long long,
+                                             long long, const void*, cudaStream_t);
+template int launch_transpose_stacked<double>(const void*, void*, long long, long long, long long, long long,
+                                              long long, const void*, cudaStream_t);
+
+template <typename T>
+int launch_stack(void* x, void* y, long long n_states, long long rows, long long cols, long long pad, int dir,
+                 int accumulate, cudaStream_t st) {
+  using Cx = typename CT<T>::type;
+  const long long n = n_states * rows * cols;
+  if (n <= 0) return FFGB_OK;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8192));
+  stack_kernel<Cx><<<blocks, 256, 0, st>>>((Cx*)x, (Cx*)y, n_states, rows, cols, pad, dir, accumulate);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+template int launch_stack<float>(void*, void*, long long, long long, long long, long long, int, int, cudaStream_t);
+template int launch_stack<double>(void*, void*, long long, long long, long long, long long, int, int, cudaStream_t);
+
+int launch_state_partials(const double* partials, long long n, long long tiles, long long tiles_per_state,
+                          long long n_states, double* out, cudaStream_t st) {
+  if (n_states <= 0) return FFGB_OK;
+  if (n_states > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "too many states");
+  state_partials_kernel<<<(unsigned)n_states, 256, 0, st>>>(partials, n, tiles, tiles_per_state, out);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
 template int launch_transpose<double>(const void*, void*, long long, long long, const void*, const void*,
                                       cudaStream_t);
 

@@ -25,6 +25,10 @@ struct StageExpect {
   const unsigned* row_str;
   const unsigned* col_str;
   double* partials;  // one FP64 partial sum per CTA
+  // states side by side along the columns: column c is string c mod
+  // col_period of its state (0: one state); padded columns (string index
+  // >= col_valid) hold zero amplitudes and read the last string's entries
+  long long col_period, col_valid;
   float X[FFGB_MAXN][FFGB_MAXN];
   float Xsum[FFGB_MAXN];  // sum_i X[i][l]
   int zrep;
@@ -48,6 +52,7 @@ struct WinJob {
   float gp[84], gl[84];        // window network coefficients (see win_coef)
   unsigned gt[84];
   unsigned salt;
+  long long col_period;  // > 0: the dithering of column c is that of column c mod col_period
   StageExpect ex;        // partials of this launch start at ex.partials
   int n_groups;          // groups (or group pairs) of this launch
 };
@@ -144,8 +149,10 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
   if (!EXPECT && !active) return;
   const long long ra = P.gbase_a[g];
   const long long rb = P.gbase_b ? (long long)P.gbase_b[g] : ra;
-  unsigned rng = dither_seed((unsigned long long)col, P.salt);
+  unsigned rng = dither_seed((unsigned long long)(P.col_period ? col % P.col_period : col), P.salt);
   const long long ld = P.ld;
+  // string index of this column (states side by side along the columns)
+  const long long cidx = !EXPECT || !P.ex.col_period ? col : min(col % P.ex.col_period, P.ex.col_valid - 1);
   // member j of group A (class K) / group B (class B - K): row offset from the group's base
 #define ROW_A(j) (LOW ? (long long)(j) : (long long)P.off_a[(j)])
 #define ROW_B(j) (LOW ? (long long)(j) : (long long)P.off_b[(j)])
@@ -197,7 +204,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
       } else {
         const StageExpect& E = P.ex;
         ZCtx za, zb;
-        zctx_make<B>(sxw, sxs, sya, sya, P.norb, E.zrep, E.col_str[col], za, zb, E.zcol[col]);
+        zctx_make<B>(sxw, sxs, sya, sya, P.norb, E.zrep, E.col_str[cidx], za, zb, E.zcol[cidx]);
         float acc = 0.f, cmp = 0.f;
         // member patterns in colex order = ascending integers with K bits set,
         // stepped with the next-same-popcount recurrence (folds to constants)
@@ -242,7 +249,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, win_min_blocks(B, K, KIND, EPI)
       } else {
         const StageExpect& E = P.ex;
         ZCtx za, zb;
-        zctx_make<B>(sxw, sxs, sya, syb, P.norb, E.zrep, E.col_str[col], za, zb, E.zcol[col]);
+        zctx_make<B>(sxw, sxs, sya, syb, P.norb, E.zrep, E.col_str[cidx], za, zb, E.zcol[cidx]);
         float acc = 0.f, cmp = 0.f;
 #pragma unroll
         for (int q = 0; q < NP; ++q) {
@@ -291,6 +298,7 @@ struct CsStageParams {
   float gp[3 * CS_MAX_SITES], gl[3 * CS_MAX_SITES];  // per site (c, Re t, Im t), see win_coef
   unsigned gt[3 * CS_MAX_SITES];
   unsigned salt;
+  long long col_period;  // > 0: the dithering of column c is that of column c mod col_period
 };
 
 // One group's cross-half rotations on registers; e[j] = row | sign bits.
@@ -333,7 +341,7 @@ __global__ void __launch_bounds__(STAGE_THREADS, M >= 5 ? 3 : (M >= 4 ? 4 : 6))
   for (int i = threadIdx.x; i < n_ent; i += STAGE_THREADS) sent[i] = src[i];
   __syncthreads();
   if (col >= P.ncols) return;
-  const unsigned rng = dither_seed((unsigned long long)col, P.salt);
+  const unsigned rng = dither_seed((unsigned long long)(P.col_period ? col % P.col_period : col), P.salt);
   float2* xc = P.x + col;
   const long long ld = P.ld;
   for (int g = g0; g < g1; g += TWO ? 2 : 1) {
@@ -365,22 +373,28 @@ __global__ void __launch_bounds__(STAGE_THREADS, M >= 5 ? 3 : (M >= 4 ? 4 : 6))
   }
 }
 
-// out[c][r] = in[r][c] * row_ph[r] * col_ph[c] (phase tables optional).  A CTA
-// moves a 64-row x 32-column tile through shared memory (padded rows: no bank
-// conflicts); each thread has eight loads in flight.
+// out[c][r] = in[r][c] * row_ph[r] * col_ph[c] (phase tables optional), row
+// strides ld_in / ld_out.  A CTA moves a 64-row x 32-column tile through
+// shared memory (padded rows: no bank conflicts); each thread has eight loads
+// in flight.  blockIdx.z indexes states side by side along the columns of
+// both arrays: state z starts at column z * in_step of `in` and z * out_step
+// of `out`.
 template <typename C>
 __global__ void __launch_bounds__(256) transpose_kernel(const C* __restrict__ in, C* __restrict__ out,
-                                                        long long rows, long long cols,
+                                                        long long rows, long long cols, long long ld_in,
+                                                        long long ld_out, long long in_step, long long out_step,
                                                         const C* __restrict__ row_ph,
                                                         const C* __restrict__ col_ph) {
   __shared__ C tile[64][33];
+  in += (long long)blockIdx.z * in_step;
+  out += (long long)blockIdx.z * out_step;
   const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 64;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
 #pragma unroll
   for (int j = ty; j < 64; j += 8) {
     const long long r = r0 + j, c = c0 + tx;
     if (r < rows && c < cols) {
-      C v = in[r * cols + c];
+      C v = in[r * ld_in + c];
       if (row_ph) v = cmul(v, row_ph[r]);
       if (col_ph) v = cmul(v, col_ph[c]);
       tile[j][tx] = v;
@@ -393,7 +407,7 @@ __global__ void __launch_bounds__(256) transpose_kernel(const C* __restrict__ in
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const long long r = r0 + tx + 32 * h;
-      if (c < cols && r < rows) out[c * rows + r] = tile[tx + 32 * h][j];
+      if (c < cols && r < rows) out[c * ld_out + r] = tile[tx + 32 * h][j];
     }
   }
 }
@@ -428,6 +442,54 @@ __global__ void row_scale_kernel(C* __restrict__ x, long long rows, long long ld
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     x[i] = cmul(x[i], ph[i / ld]);
+}
+
+// States side by side along the columns ("stacked"): state b of a block of
+// contiguous states x[b][r][c] (rows x cols each) is columns
+// [b * pad, b * pad + cols) of y[r][...] (row stride n_states * pad).
+// dir 0: y <- x (padding columns untouched); dir 1: x <- y, or x += y with
+// accumulate.
+template <typename C>
+__global__ void stack_kernel(C* __restrict__ x, C* __restrict__ y, long long n_states, long long rows,
+                             long long cols, long long pad, int dir, int accumulate) {
+  const long long per = rows * cols, n = n_states * per, ld = n_states * pad;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long b = i / per, rem = i - b * per, r = rem / cols, c = rem - r * cols;
+    C* yy = y + r * ld + b * pad + c;
+    if (dir == 0) {
+      *yy = x[i];
+    } else if (accumulate) {
+      C o = x[i];
+      const C v = *yy;
+      o.x += v.x;
+      o.y += v.y;
+      x[i] = o;
+    } else {
+      x[i] = *yy;
+    }
+  }
+}
+
+// Per-state sums of the fused expectation's per-CTA partials for stacked
+// states: partial p of a stage belongs to column tile p mod tiles, and tile
+// t to state t / tiles_per_state.  Block b sums its state's partials in a
+// fixed order into out[b].
+static __global__ void __launch_bounds__(256) state_partials_kernel(const double* __restrict__ partials, long long n,
+                                                             long long tiles, long long tiles_per_state,
+                                                             double* __restrict__ out) {
+  __shared__ double sh[256];
+  const long long b = blockIdx.x;
+  double a = 0.0;
+  for (long long p = threadIdx.x; p < n; p += blockDim.x)
+    if ((p % tiles) / tiles_per_state == b) a += partials[p];
+  sh[threadIdx.x] = a;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[b] = sh[0];
 }
 
 // y += a * x

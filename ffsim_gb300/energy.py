@@ -62,3 +62,71 @@ def lucj_energy(ucj: UCJOpSpinBalanced, ham: DoubleFactorizedHamiltonian, norb: 
                 nelec: tuple[int, int], *, dtype=torch.complex64, vec=None) -> float:
     """One LUCJ energy evaluation (allocates its buffers; use LUCJEnergy to reuse them)."""
     return LUCJEnergy(norb, nelec, dtype=dtype)(ucj, ham, vec)
+
+
+class BatchLUCJEnergy:
+    """LUCJ energies of many parameter sets of one shape under one
+    double-factorized Hamiltonian (``ffgb_batch_lucj_energy``): each UCJ
+    circuit runs on its own state, then every Hamiltonian term runs once over
+    all the states.  Holds device buffers for up to ``max_states`` states.
+
+    Per state the energy equals ``LUCJEnergy`` to rounding; the reference
+    evaluates such energies one parameter vector at a time
+    (python/ffsim/optimize/linear_method.py:181-243).
+    """
+
+    def __init__(self, norb: int, nelec: tuple[int, int], max_states: int, *, dtype=torch.complex64,
+                 device="cuda"):
+        if max_states < 1:
+            raise ValueError("max_states must be positive")
+        self.norb = norb
+        self.nelec = tuple(nelec)
+        self.dtype = dtype
+        self.max_states = max_states
+        self.code = _lib.FFGB_C64 if dtype == torch.complex64 else _lib.FFGB_C128
+        self.work = torch.empty((max_states, dim(norb, nelec)), dtype=dtype, device=device)
+        self.nbytes = _lib.load().ffgb_batch_scratch_bytes(0, self.code, norb, *self.nelec, max_states)
+        self.buf = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+
+    def __call__(self, ucjs: list[UCJOpSpinBalanced], ham: DoubleFactorizedHamiltonian,
+                 control: _lib.Control | None = None) -> np.ndarray:
+        """Energies of the operators; ``control`` (optional) can cancel the
+        batch from another thread or give it a deadline (CancelledError /
+        TimeoutError, checked between states and Hamiltonian terms)."""
+        n = len(ucjs)
+        norb = self.norb
+        if not 1 <= n <= self.max_states:
+            raise ValueError(f"between 1 and {self.max_states} operators are accepted, got {n}")
+        n_reps = ucjs[0].n_reps
+        for u in ucjs:
+            if u.norb != norb or u.n_reps != n_reps:
+                raise ValueError("every operator of a batch must have the evaluator's norb and the same n_reps")
+        if ham.norb != norb:
+            raise ValueError(f"the evaluator is for {norb} orbitals; got a Hamiltonian on {ham.norb}")
+        dcm = np.ascontiguousarray(np.stack([_lib.rmat(u.diag_coulomb_mats, (n_reps, 2, norb, norb),
+                                                       "diag_coulomb_mats") for u in ucjs]))
+        rots = np.ascontiguousarray(np.stack([_lib.cmat(u.orbital_rotations, (n_reps, norb, norb),
+                                                        "orbital_rotations") for u in ucjs]))
+        final = None
+        if any(u.final_orbital_rotation is not None for u in ucjs):
+            eye = np.eye(norb, dtype=complex)
+            final = np.ascontiguousarray(np.stack([
+                _lib.cmat(u.final_orbital_rotation if u.final_orbital_rotation is not None else eye,
+                          (norb, norb), "final_orbital_rotation") for u in ucjs]))
+        if ham.z_representation:
+            ham = ham.to_number_representation()
+        one_body, hdcm, hrots = ham._arrays()
+        e = np.zeros(n)
+        stream = torch.cuda.current_stream(self.work.device).cuda_stream
+        _lib.call("ffgb_batch_lucj_energy", self.work.data_ptr(), n, self.code, norb, *self.nelec, n_reps,
+                  _lib.dptr(dcm), rots.ctypes.data_as(_lib._dp), None if final is None else final.ctypes.data_as(_lib._dp),
+                  _lib.dptr(one_body), hdcm.shape[0], _lib.dptr(hdcm), hrots.ctypes.data_as(_lib._dp),
+                  float(ham.constant), _lib.dptr(e), self.buf.data_ptr(), self.nbytes,
+                  None if control is None else control.ptr, stream)
+        return e
+
+
+def lucj_energies(ucjs: list[UCJOpSpinBalanced], ham: DoubleFactorizedHamiltonian, norb: int,
+                  nelec: tuple[int, int], *, dtype=torch.complex64) -> np.ndarray:
+    """Energies of several UCJ operators under one Hamiltonian in one batch."""
+    return BatchLUCJEnergy(norb, nelec, len(ucjs), dtype=dtype)(ucjs, ham)

@@ -29,6 +29,8 @@ energy.
 from __future__ import annotations
 
 import itertools
+import threading
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import torch
@@ -64,8 +66,16 @@ class LUCJGradient:
     """Energy and gradient of the LUCJ ansatz for one (norb, nelec) shape,
     holding its device buffers (two states and scratch)."""
 
-    def __init__(self, norb: int, nelec: tuple[int, int], *, dtype=torch.complex64, device="cuda"):
+    def __init__(self, norb: int, nelec: tuple[int, int], *, dtype=torch.complex64, device="cuda",
+                 workers: int = 4):
         self.norb = norb
+        # batches: per-state gates run on `workers` host threads, each with its
+        # own CUDA stream and scratch, so that their launches and host syncs
+        # overlap; the Hamiltonian matvec runs once over the whole batch
+        self.workers = max(1, int(workers))
+        self._tls = threading.local()
+        self._lanes = None
+        self._pool = None
         self.nelec = tuple(nelec)
         self.dtype = dtype
         self.code = _lib.FFGB_C64 if dtype == torch.complex64 else _lib.FFGB_C128
@@ -81,36 +91,37 @@ class LUCJGradient:
     def _stream(self):
         return torch.cuda.current_stream(self.cur.device).cuda_stream
 
+    def _buf(self) -> int:
+        """Scratch of the calling thread (a batch lane's own, else the evaluator's)."""
+        b = getattr(self._tls, "buf", None)
+        return (self.buf if b is None else b).data_ptr()
+
     def _rotate(self, vec: torch.Tensor, mat: np.ndarray) -> None:
         m = _lib.cmat(mat)
         na, nb = self.nelec
         _lib.call("ffgb_apply_orbital_rotation", vec.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(m),
-                  _lib.dptr(m), self.buf.data_ptr(), self.nbytes, self._stream())
+                  _lib.dptr(m), self._buf(), self.nbytes, self._stream())
 
     def _phase(self, vec: torch.Tensor, jaa: np.ndarray, jab: np.ndarray, time: float) -> None:
         aa, ab = _lib.rmat(jaa), _lib.rmat(jab)
         na, nb = self.nelec
         _lib.call("ffgb_apply_diag_coulomb_evolution", vec.data_ptr(), self.code, self.norb, na, nb,
-                  _lib.dptr(aa), _lib.dptr(ab), _lib.dptr(aa), float(time), 0, None, None, self.buf.data_ptr(),
+                  _lib.dptr(aa), _lib.dptr(ab), _lib.dptr(aa), float(time), 0, None, None, self._buf(),
                   self.nbytes, self._stream())
 
     def _density(self, name: str, x: torch.Tensor, y: torch.Tensor, blocks: int) -> np.ndarray:
         out = np.zeros(2 * blocks * self.norb * self.norb)
         na, nb = self.nelec
         _lib.call(name, x.data_ptr(), y.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(out),
-                  self.buf.data_ptr(), self.nbytes, self._stream())
+                  self._buf(), self.nbytes, self._stream())
         return out.view(np.complex128).reshape(blocks, self.norb, self.norb)
 
     # -- energy and gradient -------------------------------------------------
-    def value_and_grad(self, params: np.ndarray, n_reps: int, ham: DoubleFactorizedHamiltonian, *,
-                       with_final_orbital_rotation: bool = False) -> tuple[float, np.ndarray]:
+    def _circuit(self, params: np.ndarray, n_reps: int, with_final: bool):
+        """The merged rotations V_j and diagonal matrices of the circuit."""
         norb = self.norb
-        na, nb = self.nelec
-        if ham.norb != norb:
-            raise ValueError(f"the evaluator is for {norb} orbitals; got a Hamiltonian on {ham.norb}")
-        params = np.asarray(params, dtype=float)
         ucj = UCJOpSpinBalanced.from_parameters(params, norb=norb, n_reps=n_reps,
-                                                with_final_orbital_rotation=with_final_orbital_rotation)
+                                                with_final_orbital_rotation=with_final)
         L = n_reps
         U = [np.eye(norb, dtype=complex)] + [np.asarray(u) for u in ucj.orbital_rotations]
         Uf = (np.asarray(ucj.final_orbital_rotation) if ucj.final_orbital_rotation is not None
@@ -118,44 +129,37 @@ class LUCJGradient:
         V = [None] + [U[k].conj().T @ U[k - 1] for k in range(1, L + 1)] + [Uf @ U[L]]
         jaa = [None] + [ucj.diag_coulomb_mats[k, 0] for k in range(L)]
         jab = [None] + [ucj.diag_coulomb_mats[k, 1] for k in range(L)]
+        return U, Uf, V, jaa, jab
 
-        # forward: psi from the Hartree-Fock state
-        _lib.call("ffgb_hartree_fock", self.cur.data_ptr(), self.code, self.cur.numel(), self._stream())
+    def _forward(self, cur: torch.Tensor, V, jaa, jab, L: int) -> None:
+        """psi from the Hartree-Fock state."""
+        _lib.call("ffgb_hartree_fock", cur.data_ptr(), self.code, cur.numel(), self._stream())
         for k in range(1, L + 1):
-            self._rotate(self.cur, V[k])
-            self._phase(self.cur, jaa[k], jab[k], -1.0)
-        self._rotate(self.cur, V[L + 1])
+            self._rotate(cur, V[k])
+            self._phase(cur, jaa[k], jab[k], -1.0)
+        self._rotate(cur, V[L + 1])
 
-        # lambda = (H - c) psi: the constant c changes neither the gradient (the
-        # gates keep the norm) nor needs the states' precision, so it is added
-        # to the energy exactly: E = c + <psi|lambda>
-        if ham.z_representation:
-            ham = ham.to_number_representation()
-        one_body, hdcm, hrots = ham._arrays()
-        _lib.call("ffgb_df_matvec", self.cur.data_ptr(), self.lam.data_ptr(), self.code, norb, na, nb,
-                  _lib.dptr(one_body), hdcm.shape[0], _lib.dptr(hdcm), hrots.ctypes.data_as(_lib._dp),
-                  0.0, 0, self.buf.data_ptr(), self.nbytes, self._stream())
-        e = np.zeros(2)
-        _lib.call("ffgb_vdot", self.cur.data_ptr(), self.lam.data_ptr(), self.code, self.cur.numel(),
-                  _lib.dptr(e), self._stream())
-        energy = float(ham.constant) + float(e[0])
-
-        # backward: undo the gates on psi and lambda
-        gamma = [None] * (L + 2)  # generator gradients of V_j
-        pdens = [None] * (L + 1)  # pair densities at D_k
+    def _backward(self, cur: torch.Tensor, lam: torch.Tensor, V, jaa, jab, L: int):
+        """Undo the gates on psi and lambda; generator gradients of the V_j and
+        pair densities at the D_k."""
+        gamma = [None] * (L + 2)
+        pdens = [None] * (L + 1)
         for j in range(L + 1, 0, -1):
             vd = V[j].conj().T
-            self._rotate(self.cur, vd)
-            self._rotate(self.lam, vd)
-            g = self._density("ffgb_transition_rdm1", self.lam, self.cur, 2)
+            self._rotate(cur, vd)
+            self._rotate(lam, vd)
+            g = self._density("ffgb_transition_rdm1", lam, cur, 2)
             gamma[j] = g[0] + g[1]
             if j > 1:
                 k = j - 1
-                pdens[k] = self._density("ffgb_pair_density", self.lam, self.cur, 3)
-                self._phase(self.cur, jaa[k], jab[k], 1.0)
-                self._phase(self.lam, jaa[k], jab[k], 1.0)
+                pdens[k] = self._density("ffgb_pair_density", lam, cur, 3)
+                self._phase(cur, jaa[k], jab[k], 1.0)
+                self._phase(lam, jaa[k], jab[k], 1.0)
+        return gamma, pdens
 
-        # chain rule to the parameters
+    def _chain(self, params: np.ndarray, U, Uf, gamma, pdens, L: int, with_final: bool) -> np.ndarray:
+        """Chain rule from the generator gradients to the parameters."""
+        norb = self.norb
         grad = np.zeros_like(params)
         triu = list(itertools.combinations_with_replacement(range(norb), 2))
         n_triu = len(triu)
@@ -181,13 +185,124 @@ class LUCJGradient:
                 grad[index + t] = -2 * daa.imag
                 grad[index + n_triu + t] = -2 * dab.imag
             index += 2 * n_triu
-        if with_final_orbital_rotation:
+        if with_final:
             Kf = antihermitians_from_parameters(params[index:], norb, 1)[0]
             dUf = _dexp(Kf, self.basis)
             # V_{L+1} = U_final U_L:  G = U_L^dag U_final^dag dU_final U_L
             Gf = (U[L].conj().T @ Uf.conj().T) @ dUf @ U[L]
             grad[index:] = 2 * (Gf * gamma[L + 1]).sum(axis=(1, 2)).real
-        return energy, grad
+        return grad
+
+    def _vdot(self, x: torch.Tensor, y: torch.Tensor) -> float:
+        e = np.zeros(2)
+        _lib.call("ffgb_vdot", x.data_ptr(), y.data_ptr(), self.code, x.numel(), _lib.dptr(e), self._stream())
+        return float(e[0])
+
+    @staticmethod
+    def _ham_arrays(ham: DoubleFactorizedHamiltonian):
+        # lambda = (H - c) psi: the constant c changes neither the gradient (the
+        # gates keep the norm) nor needs the states' precision, so it is added
+        # to the energy exactly: E = c + <psi|lambda>
+        if ham.z_representation:
+            ham = ham.to_number_representation()
+        return ham, ham._arrays()
+
+    def value_and_grad(self, params: np.ndarray, n_reps: int, ham: DoubleFactorizedHamiltonian, *,
+                       with_final_orbital_rotation: bool = False) -> tuple[float, np.ndarray]:
+        norb = self.norb
+        na, nb = self.nelec
+        if ham.norb != norb:
+            raise ValueError(f"the evaluator is for {norb} orbitals; got a Hamiltonian on {ham.norb}")
+        params = np.asarray(params, dtype=float)
+        L = n_reps
+        U, Uf, V, jaa, jab = self._circuit(params, n_reps, with_final_orbital_rotation)
+        self._forward(self.cur, V, jaa, jab, L)
+        ham, (one_body, hdcm, hrots) = self._ham_arrays(ham)
+        _lib.call("ffgb_df_matvec", self.cur.data_ptr(), self.lam.data_ptr(), self.code, norb, na, nb,
+                  _lib.dptr(one_body), hdcm.shape[0], _lib.dptr(hdcm), hrots.ctypes.data_as(_lib._dp),
+                  0.0, 0, self._buf(), self.nbytes, self._stream())
+        energy = float(ham.constant) + self._vdot(self.cur, self.lam)
+        gamma, pdens = self._backward(self.cur, self.lam, V, jaa, jab, L)
+        return energy, self._chain(params, U, Uf, gamma, pdens, L, with_final_orbital_rotation)
+
+    def value_and_grad_batch(self, params: np.ndarray, n_reps: int, ham: DoubleFactorizedHamiltonian, *,
+                             with_final_orbital_rotation: bool = False,
+                             control: _lib.Control | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """Energies and gradients of a batch of parameter vectors (rows of
+        ``params``).  The Hamiltonian matvec -- every term's rotations and
+        diagonal pass, most of the work -- runs once over all the states of
+        the batch (ffgb_batch_df_matvec); the circuit's gates run per state.
+        ``control`` (optional) can cancel the matvec from another thread or give
+        it a deadline.  Returns (energies (batch,), gradients (batch, n_params))."""
+        norb = self.norb
+        na, nb = self.nelec
+        if ham.norb != norb:
+            raise ValueError(f"the evaluator is for {norb} orbitals; got a Hamiltonian on {ham.norb}")
+        params = np.atleast_2d(np.asarray(params, dtype=float))
+        B = params.shape[0]
+        L = n_reps
+        self._ensure_batch(B)
+        cur, lam = self._bcur[:B], self._blam[:B]
+        circuits = [self._circuit(p, n_reps, with_final_orbital_rotation) for p in params]
+
+        def forward(b):
+            _, _, V, jaa, jab = circuits[b]
+            self._forward(cur[b], V, jaa, jab, L)
+
+        self._on_lanes(forward, B)
+        ham, (one_body, hdcm, hrots) = self._ham_arrays(ham)
+        _lib.call("ffgb_batch_df_matvec", cur.data_ptr(), lam.data_ptr(), B, self.code, norb, na, nb,
+                  _lib.dptr(one_body), hdcm.shape[0], _lib.dptr(hdcm), hrots.ctypes.data_as(_lib._dp), 0.0, 0,
+                  self._bbuf.data_ptr(), self._bbytes, None if control is None else control.ptr, self._stream())
+
+        def backward(b):
+            U, Uf, V, jaa, jab = circuits[b]
+            e = float(ham.constant) + self._vdot(cur[b], lam[b])
+            gamma, pdens = self._backward(cur[b], lam[b], V, jaa, jab, L)
+            return e, self._chain(params[b], U, Uf, gamma, pdens, L, with_final_orbital_rotation)
+
+        out = self._on_lanes(backward, B)
+        return np.array([o[0] for o in out]), np.stack([o[1] for o in out])
+
+    def _on_lanes(self, fn, n: int) -> list:
+        """fn(0), ..., fn(n - 1), spread over the worker lanes (state b on lane
+        b mod workers, in order), each lane on its own stream after the work
+        already queued on the current stream; the current stream then waits
+        for every lane."""
+        dev = self.cur.device
+        main = torch.cuda.current_stream(dev)
+        if self._lanes is None:
+            self._lanes = [(torch.cuda.Stream(dev), torch.empty(self.nbytes, dtype=torch.uint8, device=dev))
+                           for _ in range(self.workers)]
+            self._pool = ThreadPoolExecutor(self.workers, thread_name_prefix="lucj-grad")
+        W = len(self._lanes)
+
+        def lane(i):
+            stream, buf = self._lanes[i]
+            self._tls.buf = buf
+            stream.wait_stream(main)
+            with torch.cuda.stream(stream):
+                return [(b, fn(b)) for b in range(i, n, W)]
+
+        results = [None] * n
+        for part in self._pool.map(lane, range(min(W, n))):
+            for b, r in part:
+                results[b] = r
+        for stream, _ in self._lanes:
+            main.wait_stream(stream)
+        return results
+
+    def _ensure_batch(self, B: int) -> None:
+        """Device buffers for B states (kept for later batches of at most B)."""
+        if getattr(self, "_bcap", 0) >= B:
+            return
+        d = self.cur.numel()
+        dev = self.cur.device
+        self._bcur = torch.empty((B, d), dtype=self.dtype, device=dev)
+        self._blam = torch.empty((B, d), dtype=self.dtype, device=dev)
+        self._bbytes = _lib.load().ffgb_batch_scratch_bytes(1, self.code, self.norb, *self.nelec, B)
+        self._bbuf = torch.empty(self._bbytes, dtype=torch.uint8, device=dev)
+        self._bcap = B
 
 
 class LUCJEnergyFunction(torch.autograd.Function):
@@ -200,11 +315,13 @@ class LUCJEnergyFunction(torch.autograd.Function):
                 with_final_orbital_rotation: bool = False):
         p = params.detach().cpu().numpy().astype(float)
         batch = p.reshape(-1, p.shape[-1])
-        es, gs = [], []
-        for row in batch:
-            e, g = evaluator.value_and_grad(row, n_reps, ham, with_final_orbital_rotation=with_final_orbital_rotation)
-            es.append(e)
-            gs.append(g)
+        if batch.shape[0] > 1:
+            es, gs = evaluator.value_and_grad_batch(batch, n_reps, ham,
+                                                    with_final_orbital_rotation=with_final_orbital_rotation)
+        else:
+            e, g = evaluator.value_and_grad(batch[0], n_reps, ham,
+                                            with_final_orbital_rotation=with_final_orbital_rotation)
+            es, gs = [e], [g]
         grad = torch.as_tensor(np.array(gs).reshape(p.shape), dtype=params.dtype, device=params.device)
         ctx.save_for_backward(grad)
         out = torch.as_tensor(np.array(es), dtype=params.dtype, device=params.device)

@@ -127,6 +127,23 @@ class DoubleFactorizedHamiltonian:
                       stream_ptr(t))
             return out
 
+        def matmat(rows: torch.Tensor) -> torch.Tensor:
+            """H on every row of a contiguous (k, dim) tensor: each term once
+            over all k states (ffgb_batch_df_matvec)."""
+            t = rows.contiguous()
+            if t.dtype not in (torch.complex64, torch.complex128):
+                t = t.to(torch.complex128)
+            out = torch.empty_like(t)
+            code = _lib.FFGB_C64 if t.dtype == torch.complex64 else _lib.FFGB_C128
+            k = t.shape[0]
+            nbytes = _lib.load().ffgb_batch_scratch_bytes(1, code, norb, n_alpha, n_beta, k)
+            buf = torch.empty(nbytes, dtype=torch.uint8, device=t.device)
+            _lib.call("ffgb_batch_df_matvec", t.data_ptr(), out.data_ptr(), k, code, norb, n_alpha, n_beta,
+                      _lib.dptr(one_body), n_terms, _lib.dptr(dcm), rots.ctypes.data_as(_lib._dp),
+                      float(self.constant), int(bool(self.z_representation)), buf.data_ptr(), nbytes, None,
+                      stream_ptr(t))
+            return out
+
         def expectation(vec: torch.Tensor) -> float:
             t = vec.contiguous()
             code = _lib.FFGB_C64 if t.dtype == torch.complex64 else _lib.FFGB_C128
@@ -138,7 +155,7 @@ class DoubleFactorizedHamiltonian:
                       buf.data_ptr(), nbytes, stream_ptr(t))
             return float(e[0])
 
-        return LinearOperator((d, d), matvec, matvec, expectation)
+        return LinearOperator((d, d), matvec, None, expectation, matmat=matmat)
 
 
 def _df_z_representation(diag_coulomb_mats, orbital_rotations):

@@ -116,7 +116,8 @@ class LinearOperator:
     ``matvec`` / ``rmatvec`` / ``@`` accept torch complex tensors (the result
     has the same dtype and device) or numpy arrays (a numpy array is
     returned).  A vector has ``dim`` entries in any shape; a ``(dim, k)``
-    array is applied column by column.  Anything else raises ``ValueError``
+    array is applied to every column (in one batched call when the operator
+    provides ``matmat``, else column by column).  Anything else raises ``ValueError``
     before the library sees a pointer.  Like the reference's SciPy operators,
     the shape is ``(dim, dim)`` and ``dtype`` is complex, and
     ``scipy.sparse.linalg`` routines accept the object through
@@ -124,12 +125,16 @@ class LinearOperator:
     """
 
     def __init__(self, shape: tuple[int, int], matvec: Callable, rmatvec: Callable | None = None,
-                 expectation: Callable | None = None, dtype=complex):
+                 expectation: Callable | None = None, dtype=complex, matmat: Callable | None = None):
         self.shape = shape
         self.dtype = np.dtype(dtype)
         self._matvec = matvec
         self._rmatvec = rmatvec or matvec
         self._expectation = expectation
+        # matmat(rows): the operator on every row of a contiguous (k, dim)
+        # tensor in one call; also the adjoint's when rmatvec is matvec
+        self._matmat = matmat
+        self._rmatmat = matmat if rmatvec is None else None
 
     def _on_device(self, t: torch.Tensor) -> torch.Tensor:
         """The library's kernels read CUDA memory: a complex CUDA tensor."""
@@ -137,27 +142,29 @@ class LinearOperator:
             t = t.to(torch.complex128)
         return t.to("cuda")
 
-    def _apply(self, fn, t: torch.Tensor) -> torch.Tensor:
+    def _apply(self, fn, t: torch.Tensor, block_fn=None) -> torch.Tensor:
         n = self.shape[1]
         if t.dim() == 2 and t.shape[0] == n and t.shape[1] != 1:
+            if block_fn is not None:
+                return block_fn(self._on_device(t).transpose(0, 1).contiguous()).transpose(0, 1)
             return torch.stack([fn(self._on_device(t[:, k]).contiguous()) for k in range(t.shape[1])], dim=1)
         if t.numel() != n:
             raise ValueError(f"dimension mismatch: the operator is {self.shape}, the input has shape {tuple(t.shape)}")
         return fn(self._on_device(t).reshape(-1)).reshape(t.shape)
 
-    def _run(self, fn, vec):
+    def _run(self, fn, vec, block_fn=None):
         if isinstance(vec, torch.Tensor):
-            return self._apply(fn, vec).to(vec.device)
+            return self._apply(fn, vec, block_fn).to(vec.device)
         arr = np.asarray(vec)
         if not np.iscomplexobj(arr):
             arr = arr.astype(np.complex128)
-        return self._apply(fn, torch.from_numpy(np.ascontiguousarray(arr))).cpu().numpy()
+        return self._apply(fn, torch.from_numpy(np.ascontiguousarray(arr)), block_fn).cpu().numpy()
 
     def matvec(self, vec):
-        return self._run(self._matvec, vec)
+        return self._run(self._matvec, vec, self._matmat)
 
     def rmatvec(self, vec):
-        return self._run(self._rmatvec, vec)
+        return self._run(self._rmatvec, vec, self._rmatmat)
 
     def __matmul__(self, vec):
         return self.matvec(vec)

@@ -1,18 +1,30 @@
 """Serving loop for LUCJ energy and gradient requests of mixed shapes.
 
-Continuous batching on one GPU: every worker thread owns a CUDA stream and
-takes the oldest pending request that it can admit -- a free worker, and
-device buffers for the request's shape either idle in the pool or allocatable
-within the HBM budget.  Requests that arrive while others run are admitted as
-workers and memory free up, so their kernels overlap on the device with the
-ones already running.  Device buffers (states and scratch) stay resident in a
-per-shape pool and are reused by later requests of the same shape; idle
-buffers of other shapes are released when a new shape needs their memory.
+Continuous batching on one GPU.  Requests that share a batch key -- kind
+(energy or gradient), shape (norb, nelec), n_reps and Hamiltonian -- are
+evaluated together: every term of the Hamiltonian runs once over all the
+states of the batch (``BatchLUCJEnergy``, ``LUCJGradient.value_and_grad_batch``).
+Worker threads, each with its own CUDA stream, take the oldest pending request
+together with every pending request of its key (up to ``max_batch``), so
+requests that arrive while others run join the next batch of their key, and
+batches of different keys overlap on the device.
 
-The library calls release the Python interpreter lock while they run (ctypes
-foreign calls), so the workers' host orchestration proceeds in parallel.
-Results do not depend on what else runs: every kernel's reductions have a
-fixed order and the coefficient dithering depends only on the request.
+Admission is by device memory: an engine (the device buffers of one key's
+shape for ``capacity`` states) is taken idle from the pool or allocated within
+the HBM budget, releasing the least recently used idle engines of other shapes
+when needed; a batch shrinks to what fits.
+
+Every request gets its own result: a value, or the error that stopped it
+(``ValueError`` for an invalid request, ``MemoryError`` when even one state
+does not fit the budget, ``TimeoutError`` when its deadline passed while it
+waited, ``CancelledError`` after ``cancel``, or what the engine raised).  An
+engine whose call raised (other than a cancellation) is not reused.  A batch
+whose requests are all cancelled stops within about two Hamiltonian terms
+(``ffgb_control``).
+
+Results do not depend on what else runs: a state's result is the same alone
+and in any batch (the dithering of a state's coefficients and the order of
+its reductions do not depend on its neighbours).
 """
 
 from __future__ import annotations
@@ -22,6 +34,7 @@ import dataclasses
 import statistics
 import threading
 import time
+from concurrent.futures import CancelledError
 from typing import Callable
 
 import numpy as np
@@ -30,7 +43,9 @@ import numpy as np
 @dataclasses.dataclass
 class Request:
     """One evaluation: kind is "energy" or "gradient"; params in the
-    ``UCJOpSpinBalanced.from_parameters`` layout for (norb, n_reps)."""
+    ``UCJOpSpinBalanced.from_parameters`` layout for (norb, n_reps).
+    deadline: seconds after arrival by which it must have started (None: no
+    deadline)."""
 
     rid: int
     kind: str
@@ -40,51 +55,83 @@ class Request:
     params: np.ndarray
     ham: object
     arrival: float = 0.0
+    deadline: float | None = None
 
 
 @dataclasses.dataclass
 class Result:
     rid: int
-    energy: float
+    energy: float | None
     grad: np.ndarray | None
     arrival: float
     start: float
     end: float
+    error: BaseException | None = None
+    batch: int = 0  # size of the batch it ran in (0: it did not run)
+
+    @property
+    def ok(self) -> bool:
+        return self.error is None
 
     @property
     def latency(self) -> float:
         return self.end - self.arrival
 
 
-class _Evaluator:
-    """Device buffers of one (kind, shape) and the call that uses them."""
+def batch_key(req: Request) -> tuple:
+    return (req.kind, req.norb, tuple(req.nelec), req.n_reps, id(req.ham))
 
-    def __init__(self, kind: str, norb: int, nelec: tuple[int, int], dtype):
-        import torch
 
-        from ffsim_gb300.energy import LUCJEnergy
+def validate(req: Request) -> None:
+    """Checks a request before it is queued (raises ValueError)."""
+    from ffsim_gb300.variational import UCJOpSpinBalanced
+
+    if req.kind not in ("energy", "gradient"):
+        raise ValueError(f"request {req.rid}: kind must be 'energy' or 'gradient', got {req.kind!r}")
+    if not 1 <= req.norb <= 18:
+        raise ValueError(f"request {req.rid}: norb must be in [1, 18], got {req.norb}")
+    nelec = tuple(req.nelec)
+    if len(nelec) != 2 or not all(0 <= n <= req.norb for n in nelec):
+        raise ValueError(f"request {req.rid}: nelec must be two occupations in [0, norb], got {req.nelec}")
+    if req.n_reps < 1:
+        raise ValueError(f"request {req.rid}: n_reps must be positive, got {req.n_reps}")
+    n = UCJOpSpinBalanced.n_params(req.norb, req.n_reps)
+    if np.shape(req.params) != (n,):
+        raise ValueError(f"request {req.rid}: expected {n} parameters, got shape {np.shape(req.params)}")
+    if getattr(req.ham, "norb", req.norb) != req.norb:
+        raise ValueError(f"request {req.rid}: the Hamiltonian acts on {req.ham.norb} orbitals, not {req.norb}")
+
+
+class _Engine:
+    """Device buffers of one (kind, norb, nelec) for up to `capacity` states."""
+
+    def __init__(self, kind: str, norb: int, nelec: tuple[int, int], capacity: int, dtype):
+        from ffsim_gb300.energy import BatchLUCJEnergy
         from ffsim_gb300.gradient import LUCJGradient
 
-        self.key = (kind, norb, tuple(nelec))
+        self.capacity = capacity
+        self.kind = kind
         if kind == "energy":
-            self.impl = LUCJEnergy(norb, nelec, dtype=dtype)
-            self.nbytes = self.impl.work.numel() * self.impl.work.element_size() + self.impl.nbytes
+            self.impl = BatchLUCJEnergy(norb, nelec, capacity, dtype=dtype)
         else:
             self.impl = LUCJGradient(norb, nelec, dtype=dtype)
-            self.nbytes = 2 * self.impl.cur.numel() * self.impl.cur.element_size() + self.impl.nbytes
-        self._torch = torch
+            self.impl._ensure_batch(capacity)
+        self.nbytes = engine_bytes(kind, norb, nelec, capacity, dtype)
 
-    def run(self, req: Request) -> tuple[float, np.ndarray | None]:
+    def run(self, reqs: list[Request], control) -> list[tuple[float, np.ndarray | None]]:
         from ffsim_gb300.variational import UCJOpSpinBalanced
 
-        if req.kind == "energy":
-            op = UCJOpSpinBalanced.from_parameters(req.params, norb=req.norb, n_reps=req.n_reps)
-            return self.impl(op, req.ham), None
-        return self.impl.value_and_grad(req.params, req.n_reps, req.ham)
+        r0 = reqs[0]
+        if self.kind == "energy":
+            ops = [UCJOpSpinBalanced.from_parameters(r.params, norb=r.norb, n_reps=r.n_reps) for r in reqs]
+            return [(float(e), None) for e in self.impl(ops, r0.ham, control)]
+        params = np.stack([r.params for r in reqs])
+        es, gs = self.impl.value_and_grad_batch(params, r0.n_reps, r0.ham, control=control)
+        return [(float(e), g) for e, g in zip(es, gs)]
 
 
-def evaluator_bytes(kind: str, norb: int, nelec: tuple[int, int], dtype) -> int:
-    """Device bytes an evaluator of this shape holds (states + scratch)."""
+def engine_bytes(kind: str, norb: int, nelec: tuple[int, int], capacity: int, dtype) -> int:
+    """Device bytes an engine of this shape and capacity holds."""
     import torch
 
     from ffsim_gb300 import _lib
@@ -95,23 +142,27 @@ def evaluator_bytes(kind: str, norb: int, nelec: tuple[int, int], dtype) -> int:
     lib = _lib.load()
     d = dim(norb, nelec)
     if kind == "energy":
-        return d * el + lib.ffgb_scratch_bytes(2, code, norb, *nelec)
-    return 2 * d * el + max(lib.ffgb_scratch_bytes(op, code, norb, *nelec) for op in (0, 1, 3))
+        return capacity * d * el + lib.ffgb_batch_scratch_bytes(0, code, norb, *nelec, capacity)
+    per_state = max(lib.ffgb_scratch_bytes(op, code, norb, *nelec) for op in (0, 1, 3))
+    workers = 4  # LUCJGradient's lanes, each with its own scratch
+    return ((2 + 2 * capacity) * d * el + (1 + workers) * per_state
+            + lib.ffgb_batch_scratch_bytes(1, code, norb, *nelec, capacity))
 
 
 class LUCJServer:
     """Continuous-batching server.
 
-    workers: concurrent requests (one CUDA stream each).
-    budget_bytes: device memory the pooled buffers may hold (default: 85% of
+    workers: batches in flight at once (one CUDA stream each).
+    max_batch: states per batch (at most).
+    budget_bytes: device memory the pooled engines may hold (default: 85% of
     the free HBM when the server starts).
-    make_evaluator / size_of: injection points (the defaults build the GPU
-    evaluators); tests substitute host-only fakes.
+    make_engine(kind, norb, nelec, capacity) / size_of(kind, norb, nelec,
+    capacity): injection points (the defaults build GPU engines); tests
+    substitute host-only fakes.
     """
 
-    def __init__(self, workers: int = 6, *, dtype=None, budget_bytes: int | None = None,
-                 make_evaluator: Callable | None = None, size_of: Callable | None = None,
-                 use_streams: bool = True):
+    def __init__(self, workers: int = 2, *, max_batch: int = 64, dtype=None, budget_bytes: int | None = None,
+                 make_engine: Callable | None = None, size_of: Callable | None = None, use_streams: bool = True):
         import torch
 
         self.dtype = dtype if dtype is not None else torch.complex64
@@ -119,43 +170,70 @@ class LUCJServer:
             free, _ = torch.cuda.mem_get_info()
             budget_bytes = int(0.85 * free)
         self.budget = int(budget_bytes)
-        self.make_evaluator = make_evaluator or (lambda k, n, ne: _Evaluator(k, n, ne, self.dtype))
-        self.size_of = size_of or (lambda k, n, ne: evaluator_bytes(k, n, ne, self.dtype))
+        self.max_batch = max(1, int(max_batch))
+        self.make_engine = make_engine or (lambda k, n, ne, c: _Engine(k, n, ne, c, self.dtype))
+        self.size_of = size_of or (lambda k, n, ne, c: engine_bytes(k, n, ne, c, self.dtype))
         self.use_streams = use_streams
         self._cv = threading.Condition()
         self._pending: collections.deque[Request] = collections.deque()
-        self._idle: dict[tuple, list] = collections.defaultdict(list)
-        self._idle_order: collections.OrderedDict = collections.OrderedDict()  # id -> (key, ev), LRU
-        self._in_use = 0  # bytes held by pooled + running evaluators
-        self._results: list[Result] = []
-        self._errors: list[BaseException] = []
+        self._idle: dict[tuple, list] = collections.defaultdict(list)  # (kind, norb, nelec) -> engines
+        self._idle_order: collections.OrderedDict = collections.OrderedDict()  # id -> (shape, engine), LRU
+        self._in_use = 0  # bytes held by pooled and running engines
+        self._results: dict[int, Result] = {}
+        self._running: dict[int, tuple] = {}  # rid -> (batch requests, control)
+        self._cancelled: set[int] = set()
         self._stop = False
         self.max_concurrent = 0
-        self._running = 0
-        self._threads = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(workers)]
+        self.batch_sizes: list[int] = []
+        self._n_running = 0
+        self._threads = [threading.Thread(target=self._worker, daemon=True) for _ in range(workers)]
         for t in self._threads:
             t.start()
 
     # -- client side -------------------------------------------------------
     def submit(self, req: Request) -> None:
+        """Queue a request; an invalid one gets its error result at once."""
+        if not req.arrival:
+            req.arrival = time.perf_counter()
+        try:
+            validate(req)
+        except ValueError as exc:
+            self._finish_one(req, None, exc, 0, time.perf_counter())
+            return
         with self._cv:
-            if not req.arrival:
-                req.arrival = time.perf_counter()
             self._pending.append(req)
             self._cv.notify_all()
 
+    def cancel(self, rid: int) -> bool:
+        """Cancel a request: a pending one is dropped at once, a running one
+        gets a cancellation result (and its batch stops early when every
+        request of the batch is cancelled).  False if it already finished."""
+        with self._cv:
+            if rid in self._results:
+                return False
+            for i, req in enumerate(self._pending):
+                if req.rid == rid:
+                    del self._pending[i]
+                    self._record(req, None, CancelledError(f"request {rid} was cancelled"), 0, time.perf_counter())
+                    return True
+            self._cancelled.add(rid)
+            if rid in self._running:
+                batch, control = self._running[rid]
+                if control is not None and all(r.rid in self._cancelled for r in batch):
+                    control.request_cancel()
+            return True
+
     def drain(self, n_expected: int, timeout: float = 3600.0) -> list[Result]:
-        """Wait until n_expected results exist; returns them sorted by rid."""
+        """Wait until n_expected results exist; returns them sorted by rid
+        (each with its value or its error)."""
         deadline = time.perf_counter() + timeout
         with self._cv:
-            while len(self._results) + len(self._errors) < n_expected:
+            while len(self._results) < n_expected:
                 left = deadline - time.perf_counter()
                 if left <= 0:
                     raise TimeoutError(f"{len(self._results)} of {n_expected} requests finished")
                 self._cv.wait(timeout=min(left, 1.0))
-            if self._errors:
-                raise self._errors[0]
-            return sorted(self._results, key=lambda r: r.rid)
+            return sorted(self._results.values(), key=lambda r: r.rid)
 
     def close(self) -> None:
         with self._cv:
@@ -165,35 +243,92 @@ class LUCJServer:
             t.join(timeout=60)
 
     # -- scheduling -----------------------------------------------------------
-    def _take(self):
-        """Under the lock: the oldest admissible request with its evaluator."""
-        for i, req in enumerate(self._pending):
-            key = (req.kind, req.norb, tuple(req.nelec))
-            if self._idle[key]:
-                ev = self._idle[key].pop()
-                self._idle_order.pop(id(ev), None)
-                del self._pending[i]
-                return req, ev, 0
-            need = self.size_of(*key)
-            if need > self.budget:
-                del self._pending[i]
-                self._errors.append(MemoryError(f"request {req.rid} needs {need} bytes; the budget is "
-                                                f"{self.budget}"))
-                self._cv.notify_all()
-                return self._take()
-            # release idle buffers of other shapes (least recently used first)
-            while self._in_use + need > self.budget and self._idle_order:
-                _, (k2, ev2) = self._idle_order.popitem(last=False)
-                self._idle[k2].remove(ev2)
-                self._in_use -= ev2.nbytes
+    def _record(self, req: Request, value, error, batch: int, start: float) -> None:
+        """Under the lock: the result of one request."""
+        energy, grad = value if value is not None else (None, None)
+        if req.rid in self._cancelled and error is None:
+            error = CancelledError(f"request {req.rid} was cancelled")
+        self._results[req.rid] = Result(req.rid, energy, grad, req.arrival, start, time.perf_counter(), error, batch)
+        self._cv.notify_all()
+
+    def _finish_one(self, req, value, error, batch, start) -> None:
+        with self._cv:
+            self._record(req, value, error, batch, start)
+
+    def _expire(self, now: float) -> None:
+        """Under the lock: pending requests past their deadline."""
+        keep = collections.deque()
+        for req in self._pending:
+            if req.deadline is not None and now > req.arrival + req.deadline:
+                self._record(req, None, TimeoutError(f"request {req.rid} waited past its deadline"), 0, now)
+            else:
+                keep.append(req)
+        self._pending = keep
+
+    def _reserve(self, shape: tuple, cap: int) -> int:
+        """Under the lock: bytes for a new engine of `shape` and capacity
+        `cap`, releasing idle engines of other shapes (least recently used
+        first) as needed; 0 if it does not fit."""
+        need = self.size_of(shape[0], shape[1], shape[2], cap)
+        if need > self.budget:
+            return 0
+        for oid, (s2, e2) in list(self._idle_order.items()):
             if self._in_use + need <= self.budget:
-                del self._pending[i]
-                self._in_use += need  # reserved; replaced by the real size after allocation
-                return req, None, need
+                break
+            if s2 == shape:
+                continue
+            del self._idle_order[oid]
+            self._idle[s2].remove(e2)
+            self._in_use -= e2.nbytes
+        if self._in_use + need > self.budget:
+            return 0
+        self._in_use += need
+        return need
+
+    def _take(self):
+        """Under the lock: the oldest admissible request with the pending
+        requests of its key that join it, and an idle engine or the bytes
+        reserved for a new one: (group, engine or None, reserved bytes,
+        capacity)."""
+        self._expire(time.perf_counter())
+        for req in list(self._pending):
+            key = batch_key(req)
+            shape = key[:3]
+            group = [r for r in self._pending if batch_key(r) == key][: self.max_batch]
+            idle = sorted(self._idle[shape], key=lambda e: e.capacity)
+            fit = [e for e in idle if e.capacity >= len(group)]
+            ev, reserved, cap = (fit[0] if fit else None), 0, 0
+            if ev is None:
+                # a new engine for the whole group (capacities are powers of two) ...
+                cap = min(1 << (len(group) - 1).bit_length(), self.max_batch)
+                reserved = self._reserve(shape, cap)
+                if not reserved and idle:  # ... else the largest idle one
+                    ev = idle[-1]
+                while not reserved and ev is None and cap > 1:  # ... else a smaller new one
+                    cap //= 2
+                    reserved = self._reserve(shape, cap)
+                if not reserved and ev is None:
+                    if self.size_of(shape[0], shape[1], shape[2], 1) > self.budget:
+                        self._pending.remove(req)
+                        self._record(req, None, MemoryError(
+                            f"request {req.rid} needs {self.size_of(shape[0], shape[1], shape[2], 1)} bytes; "
+                            f"the budget is {self.budget}"), 0, time.perf_counter())
+                        return self._take()
+                    continue  # waits for memory held by running batches
+            if ev is not None:
+                self._idle[shape].remove(ev)
+                self._idle_order.pop(id(ev), None)
+                cap = ev.capacity
+            group = group[:cap]
+            for r in group:
+                self._pending.remove(r)
+            return group, ev, reserved, cap
         return None
 
-    def _worker(self, index: int) -> None:
+    def _worker(self) -> None:
         import torch
+
+        from ffsim_gb300 import _lib
 
         stream = torch.cuda.Stream() if self.use_streams else None
         while True:
@@ -204,53 +339,58 @@ class LUCJServer:
                     got = self._take()
                     if got is not None:
                         break
-                    self._cv.wait()
-                self._running += 1
-                self.max_concurrent = max(self.max_concurrent, self._running)
-            req, ev, reserved = got
+                    self._cv.wait(timeout=0.5)
+                group, ev, reserved, cap = got
+                control = _lib.Control()
+                for r in group:
+                    self._running[r.rid] = (group, control)
+                self._n_running += 1
+                self.max_concurrent = max(self.max_concurrent, self._n_running)
+                self.batch_sizes.append(len(group))
+            start = time.perf_counter()
+            values, err = None, None
             try:
-                start = time.perf_counter()
+                shape = batch_key(group[0])[:3]
                 if stream is not None:
                     with torch.cuda.stream(stream):
                         if ev is None:
-                            ev = self.make_evaluator(req.kind, req.norb, tuple(req.nelec))
-                        energy, grad = ev.run(req)
+                            ev = self.make_engine(shape[0], shape[1], shape[2], cap)
+                        values = ev.run(group, control)
                         stream.synchronize()
                 else:
                     if ev is None:
-                        ev = self.make_evaluator(req.kind, req.norb, tuple(req.nelec))
-                    energy, grad = ev.run(req)
-                end = time.perf_counter()
-                res = Result(req.rid, energy, grad, req.arrival, start, end)
-                err = None
+                        ev = self.make_engine(shape[0], shape[1], shape[2], cap)
+                    values = ev.run(group, control)
             except BaseException as exc:  # noqa: BLE001
-                res, err = None, exc
+                err = exc
             with self._cv:
-                self._running -= 1
-                if ev is not None:
+                self._n_running -= 1
+                for r in group:
+                    self._running.pop(r.rid, None)
+                keep = ev is not None and (err is None or isinstance(err, CancelledError))
+                if keep:
                     if reserved:
                         self._in_use += ev.nbytes - reserved
-                    key = (req.kind, req.norb, tuple(req.nelec))
-                    self._idle[key].append(ev)
-                    self._idle_order[id(ev)] = (key, ev)
-                elif reserved:
-                    self._in_use -= reserved
-                if err is not None:
-                    self._errors.append(err)
-                else:
-                    self._results.append(res)
-                self._cv.notify_all()
+                    self._idle[shape].append(ev)
+                    self._idle_order[id(ev)] = (shape, ev)
+                else:  # never built, or failed: its memory is released
+                    self._in_use -= reserved if ev is None or reserved else ev.nbytes
+                    ev = None
+                for i, r in enumerate(group):
+                    self._record(r, None if err is not None else values[i], err, len(group), start)
 
 
 def latency_stats(results: list[Result]) -> dict:
-    lat = sorted(r.latency for r in results)
-    t0 = min(r.arrival for r in results)
-    t1 = max(r.end for r in results)
+    ok = [r for r in results if r.ok]
+    lat = sorted(r.latency for r in ok)
+    t0 = min(r.arrival for r in ok)
+    t1 = max(r.end for r in ok)
     return {
         "requests": len(results),
+        "completed": len(ok),
         "p50_ms": 1e3 * statistics.median(lat),
         "p99_ms": 1e3 * float(np.percentile(lat, 99)),
-        "evals_per_s": len(results) / (t1 - t0),
+        "evals_per_s": len(ok) / (t1 - t0),
         "span_s": t1 - t0,
     }
 

@@ -40,10 +40,24 @@ typedef enum {
   FFGB_ERR_DTYPE = 2,       /* unsupported dtype (TypeError) */
   FFGB_ERR_OOM = 3,         /* scratch too small / allocation failed (MemoryError) */
   FFGB_ERR_CUDA = 4,        /* CUDA runtime error (RuntimeError) */
-  FFGB_ERR_TIMEOUT = 5,     /* reserved for bounded device waits (TimeoutError); no kernel waits now */
+  FFGB_ERR_TIMEOUT = 5,     /* a batch passed its deadline (TimeoutError) */
   FFGB_ERR_UNSUPPORTED = 6, /* shape not supported (NotImplementedError) */
-  FFGB_ERR_NUMERIC = 7      /* host factorization failed (ArithmeticError) */
+  FFGB_ERR_NUMERIC = 7,     /* host factorization failed (ArithmeticError) */
+  FFGB_ERR_CANCELLED = 8    /* a batch was cancelled through its control (CancelledError) */
 } ffgb_status;
+
+/* Control of a long batch call (a NULL control pointer means none).
+ * Between its states' circuits and between Hamiltonian terms the call reads
+ * *cancel (when not NULL; written by another host thread) and the elapsed
+ * time; it returns FFGB_ERR_CANCELLED once *cancel is nonzero and
+ * FFGB_ERR_TIMEOUT once timeout_s seconds have passed since it started
+ * (timeout_s <= 0: no deadline).  So that either acts promptly, the call then
+ * keeps at most two such units of work queued on the stream ahead of the GPU.
+ * After either error the stream stays usable and the outputs are undefined. */
+typedef struct {
+  const volatile int* cancel;
+  double timeout_s;
+} ffgb_control;
 
 typedef enum { FFGB_C64 = 0, FFGB_C128 = 1 } ffgb_dtype;
 
@@ -254,6 +268,45 @@ int ffgb_lucj_energy(const void* vec_in, void* work_state, int dtype, int norb, 
                      const double* one_body_tensor, int n_terms, const double* diag_coulomb_mats,
                      const double* orbital_rotations, double constant, double* energy_out,
                      void* scratch, size_t scratch_bytes, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Batches: n_states states of one shape under one Hamiltonian          */
+/* ------------------------------------------------------------------ */
+/* Scratch bytes of the batch entry points (op 0: ffgb_batch_lucj_energy,
+ * op 1: ffgb_batch_df_matvec) for n_states states; 0 for invalid shapes. */
+size_t ffgb_batch_scratch_bytes(int op, int dtype, int norb, int n_alpha, int n_beta, long long n_states);
+
+/* LUCJ energies of n_states parameter sets under one double-factorized
+ * Hamiltonian: state b (the UCJ circuit of ucj_diag_coulomb_mats[b],
+ * ucj_orbital_rotations[b] and, if not NULL, ucj_final_orbital_rotations[b],
+ * applied to the Hartree-Fock state) is built in work_states[b] (n_states
+ * contiguous states), then every Hamiltonian term runs once over all the
+ * states.  energies_out: n_states host doubles.  Per state it equals
+ * ffgb_lucj_energy to rounding.  The reference evaluates such energies one at a
+ * time (np.vdot(psi, H @ psi).real, tests/python/variational/
+ * ucj_spin_balanced_test.py:152-158; one parameter vector per call in the
+ * line searches of python/ffsim/optimize/linear_method.py:181-243); complex64
+ * with 9 <= norb <= 16
+ * runs the terms on all states at once, other shapes state by state.
+ * Arrays are per state, stacked: n_states * n_reps * 2 * norb^2 doubles and
+ * n_states * n_reps * norb^2 complex.  Synchronizes the stream. */
+int ffgb_batch_lucj_energy(void* work_states, long long n_states, int dtype, int norb, int n_alpha, int n_beta,
+                           int n_reps, const double* ucj_diag_coulomb_mats, const double* ucj_orbital_rotations,
+                           const double* ucj_final_orbital_rotations, const double* one_body_tensor, int n_terms,
+                           const double* diag_coulomb_mats, const double* orbital_rotations, double constant,
+                           double* energies_out, void* scratch, size_t scratch_bytes, const ffgb_control* control,
+                           void* stream);
+
+/* out[b] = H vec[b] for n_states contiguous states: the double-factorized
+ * Hamiltonian's linear operator (python/ffsim/hamiltonians/
+ * double_factorized_hamiltonian.py:244-275) applied to the columns of a
+ * matrix, as in `hamiltonian @ jac` of python/ffsim/optimize/
+ * linear_method.py:294 (SciPy applies the matvec column by column there).  complex64 with 9 <= norb <= 16 runs
+ * every term once over all the states; other shapes state by state. */
+int ffgb_batch_df_matvec(const void* vec, void* out, long long n_states, int dtype, int norb, int n_alpha,
+                         int n_beta, const double* one_body_tensor, int n_terms, const double* diag_coulomb_mats,
+                         const double* orbital_rotations, double constant, int z_representation, void* scratch,
+                         size_t scratch_bytes, const ffgb_control* control, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* Reductions and helpers                                               */

@@ -1,109 +1,240 @@
-"""Serving loop: scheduling and admission on the host (fake evaluators), and
-on the GPU that every result is the same alone and in the mix."""
+"""Serving loop: batching, admission and failure handling on the host (fake
+engines, no GPU), and on the GPU that every result is the same alone and in
+the mix."""
 
 from __future__ import annotations
 
 import threading
 import time
+from concurrent.futures import CancelledError
 
 import numpy as np
 import pytest
 
 
-class _FakeEval:
+class _FakeEngine:
+    """Host-only engine: records its batches; run() returns rid / 2."""
+
     live = 0
     peak = 0
+    made = []
     lock = threading.Lock()
 
-    def __init__(self, kind, norb, nelec):
-        self.key = (kind, norb, nelec)
-        self.nbytes = norb * 100
+    def __init__(self, kind, norb, nelec, capacity, fail_rids=(), delay=0.01):
+        self.kind, self.norb, self.capacity = kind, norb, capacity
+        self.nbytes = norb * 100 * capacity
+        self.fail_rids = set(fail_rids)
+        self.delay = delay
+        self.batches = []
+        with _FakeEngine.lock:
+            _FakeEngine.made.append(self)
 
-    def run(self, req):
-        with _FakeEval.lock:
-            _FakeEval.live += 1
-            _FakeEval.peak = max(_FakeEval.peak, _FakeEval.live)
-        time.sleep(0.01 * req.norb / 8)
-        with _FakeEval.lock:
-            _FakeEval.live -= 1
-        return float(req.rid) * 0.5, None
+    def run(self, reqs, control):
+        with _FakeEngine.lock:
+            _FakeEngine.live += 1
+            _FakeEngine.peak = max(_FakeEngine.peak, _FakeEngine.live)
+        try:
+            self.batches.append([r.rid for r in reqs])
+            t_end = time.perf_counter() + self.delay * reqs[0].norb / 8
+            while time.perf_counter() < t_end:  # a long batch that checks its control, as the library does
+                if control is not None and control._flag.value:
+                    raise CancelledError("cancelled")
+                time.sleep(0.001)
+            if any(r.rid in self.fail_rids for r in reqs):
+                raise RuntimeError("engine failed")
+            return [(r.rid * 0.5, None) for r in reqs]
+        finally:
+            with _FakeEngine.lock:
+                _FakeEngine.live -= 1
 
 
-def _reqs(n, norbs=(8, 10, 12)):
+def _reset():
+    _FakeEngine.live = _FakeEngine.peak = 0
+    _FakeEngine.made = []
+
+
+def _reqs(n, norbs=(8, 10, 12), seed=0, n_reps=1):
     from ffsim_gb300.serving import Request
+    from ffsim_gb300.variational import UCJOpSpinBalanced
 
-    rng = np.random.default_rng(0)
+    rng = np.random.default_rng(seed)
+    hams = {m: object() for m in norbs}
     out = []
     for i in range(n):
         m = int(rng.choice(norbs))
-        out.append(Request(i, "energy", m, (m // 2, m // 2), 1, np.zeros(3), None))
+        out.append(Request(i, "energy", m, (m // 2, m // 2), n_reps, np.zeros(UCJOpSpinBalanced.n_params(m, n_reps)),
+                           hams[m]))
     return out
 
 
-def test_server_overlaps_and_returns_every_result():
-    from ffsim_gb300.serving import LUCJServer, latency_stats
+def _server(workers=3, budget=10**9, max_batch=64, **kw):
+    from ffsim_gb300.serving import LUCJServer
 
-    _FakeEval.live = _FakeEval.peak = 0
-    srv = LUCJServer(workers=4, budget_bytes=10**9, make_evaluator=_FakeEval,
-                     size_of=lambda k, n, ne: n * 100, use_streams=False)
-    reqs = _reqs(40)
+    return LUCJServer(workers=workers, budget_bytes=budget, max_batch=max_batch,
+                      make_engine=lambda k, n, ne, c: _FakeEngine(k, n, ne, c, **kw),
+                      size_of=lambda k, n, ne, c: n * 100 * c, use_streams=False)
+
+
+def test_server_batches_overlaps_and_returns_every_result():
+    from ffsim_gb300.serving import latency_stats
+
+    _reset()
+    srv = _server(workers=3)
+    reqs = _reqs(60)
     for r in reqs:
         srv.submit(r)
     res = srv.drain(len(reqs), timeout=60)
     srv.close()
-    assert [r.rid for r in res] == list(range(40))
-    assert all(r.energy == r.rid * 0.5 for r in res)
-    assert srv.max_concurrent > 1 and _FakeEval.peak > 1
+    assert [r.rid for r in res] == list(range(60))
+    assert all(r.ok and r.energy == r.rid * 0.5 for r in res)
+    assert max(srv.batch_sizes) > 1  # requests of one key ran together
+    assert _FakeEngine.peak > 1  # batches of different keys overlapped
+    # every batch holds one key only
+    by_rid = {r.rid: r for r in reqs}
+    for eng in _FakeEngine.made:
+        for b in eng.batches:
+            assert len({by_rid[i].norb for i in b}) == 1
     st = latency_stats(res)
-    assert st["requests"] == 40 and st["p99_ms"] >= st["p50_ms"] > 0
+    assert st["requests"] == 60 and st["p99_ms"] >= st["p50_ms"] > 0
 
 
 def test_server_admits_by_memory_budget():
-    """A budget that holds one evaluator at a time serialises the requests and
-    swaps buffers between shapes."""
-    from ffsim_gb300.serving import LUCJServer
-
-    _FakeEval.live = _FakeEval.peak = 0
-    srv = LUCJServer(workers=4, budget_bytes=1200, make_evaluator=_FakeEval,
-                     size_of=lambda k, n, ne: n * 100, use_streams=False)
+    """A budget that holds one small engine at a time runs the batches one
+    after the other and swaps engines between shapes."""
+    _reset()
+    srv = _server(workers=4, budget=1200, max_batch=1)
     reqs = _reqs(12)
     for r in reqs:
         srv.submit(r)
     res = srv.drain(len(reqs), timeout=60)
     srv.close()
-    assert len(res) == 12
-    assert _FakeEval.peak == 1
+    assert all(r.ok for r in res)
+    assert _FakeEngine.peak == 1
 
 
-def test_server_rejects_requests_larger_than_the_budget():
-    from ffsim_gb300.serving import LUCJServer
-
-    srv = LUCJServer(workers=2, budget_bytes=500, make_evaluator=_FakeEval,
-                     size_of=lambda k, n, ne: n * 100, use_streams=False)
-    srv.submit(_reqs(1, norbs=(8,))[0])
-    with pytest.raises(MemoryError):
-        srv.drain(1, timeout=30)
+def test_server_shrinks_a_batch_to_the_budget():
+    _reset()
+    srv = _server(workers=1, budget=8 * 100 * 4, max_batch=64)
+    reqs = _reqs(10, norbs=(8,))
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(len(reqs), timeout=60)
     srv.close()
+    assert all(r.ok for r in res)
+    assert max(srv.batch_sizes) <= 4
+
+
+def test_request_larger_than_the_budget_fails_alone():
+    _reset()
+    srv = _server(workers=2, budget=900)
+    big, small = _reqs(1, norbs=(12,))[0], _reqs(2, norbs=(8,))[1]
+    small.rid = 1
+    srv.submit(big)
+    srv.submit(small)
+    res = srv.drain(2, timeout=30)
+    srv.close()
+    assert isinstance(res[0].error, MemoryError)
+    assert res[1].ok and res[1].energy == 0.5
+
+
+def test_invalid_requests_fail_alone():
+    from ffsim_gb300.serving import Request
+
+    _reset()
+    srv = _server()
+    good = _reqs(3, norbs=(8,))
+    bad_nelec = Request(10, "energy", 8, (9, 4), 1, good[0].params, good[0].ham)
+    bad_params = Request(11, "gradient", 8, (4, 4), 1, np.zeros(3), good[0].ham)
+    bad_kind = Request(12, "density", 8, (4, 4), 1, good[0].params, good[0].ham)
+    for r in good + [bad_nelec, bad_params, bad_kind]:
+        srv.submit(r)
+    res = {r.rid: r for r in srv.drain(6, timeout=30)}
+    srv.close()
+    assert all(res[i].ok for i in range(3))
+    assert all(isinstance(res[i].error, ValueError) for i in (10, 11, 12))
+
+
+def test_failing_engine_fails_its_batch_only_and_is_not_reused():
+    _reset()
+    srv = _server(workers=2, fail_rids={3})
+    reqs = _reqs(12, norbs=(8, 10))
+    for r in reqs:
+        srv.submit(r)
+    res = {r.rid: r for r in srv.drain(12, timeout=60)}
+    srv.close()
+    failed = [i for i, r in res.items() if not r.ok]
+    assert 3 in failed
+    assert all(isinstance(res[i].error, RuntimeError) for i in failed)
+    assert all(res[i].ok for i in res if i not in failed)
+    # the engine that raised was dropped: none of the idle pool's engines ran rid 3
+    for engines in srv._idle.values():
+        for e in engines:
+            assert all(3 not in b for b in e.batches)
+
+
+def test_cancel_pending_and_running():
+    _reset()
+    srv = _server(workers=1, delay=0.5)
+    reqs = _reqs(3, norbs=(8,), n_reps=1)
+    reqs[2].n_reps = 2  # another key: waits behind the first batch
+    from ffsim_gb300.variational import UCJOpSpinBalanced
+
+    reqs[2].params = np.zeros(UCJOpSpinBalanced.n_params(8, 2))
+    srv.submit(reqs[0])
+    srv.submit(reqs[1])
+    time.sleep(0.05)  # the first batch (rids 0, 1) is running
+    srv.submit(reqs[2])
+    assert srv.cancel(2)  # pending: dropped
+    assert srv.cancel(0) and srv.cancel(1)  # the whole running batch: stopped early
+    t0 = time.perf_counter()
+    res = srv.drain(3, timeout=30)
+    srv.close()
+    assert time.perf_counter() - t0 < 0.4
+    assert all(isinstance(r.error, CancelledError) for r in res)
+
+
+def test_deadline_while_pending():
+    _reset()
+    srv = _server(workers=1, delay=0.3)
+    reqs = _reqs(2, norbs=(8,))
+    reqs[1].norb = 10  # another key
+    reqs[1].nelec = (5, 5)
+    from ffsim_gb300.variational import UCJOpSpinBalanced
+
+    reqs[1].params = np.zeros(UCJOpSpinBalanced.n_params(10, 1))
+    reqs[1].ham = type("H", (), {"norb": 10})()
+    reqs[1].deadline = 0.05
+    srv.submit(reqs[0])
+    time.sleep(0.02)
+    srv.submit(reqs[1])
+    res = srv.drain(2, timeout=30)
+    srv.close()
+    assert res[0].ok
+    assert isinstance(res[1].error, TimeoutError)
 
 
 @pytest.mark.gpu
 def test_results_alone_and_in_the_mix(cuda):
+    """Each request's result through the server equals the same request run
+    alone (a batch of one), energies and gradients."""
     import torch
 
-    from ffsim_gb300.serving import LUCJServer, _Evaluator, replay, synthetic_stream
+    from ffsim_gb300.serving import LUCJServer, _Engine, replay, synthetic_stream
 
-    offsets, reqs = synthetic_stream(16, rate=200.0, seed=3, norbs=(8, 10, 12), gradient_fraction=0.3)
+    offsets, reqs = synthetic_stream(24, rate=400.0, seed=3, norbs=(8, 10, 12), reps=(1, 2),
+                                     gradient_fraction=0.3)
     alone = {}
     for r in reqs:
-        ev = _Evaluator(r.kind, r.norb, r.nelec, torch.complex64)
-        alone[r.rid] = ev.run(r)
-        del ev
-    srv = LUCJServer(workers=4)
+        eng = _Engine(r.kind, r.norb, r.nelec, 1, torch.complex64)
+        alone[r.rid] = eng.run([r], None)[0]
+        del eng
+    srv = LUCJServer(workers=2)
     res = replay(srv, offsets, reqs)
     srv.close()
-    assert srv.max_concurrent > 1
+    assert all(r.ok for r in res)
+    assert max(srv.batch_sizes) > 1
     for r in res:
         e, g = alone[r.rid]
-        assert abs(r.energy - e) <= 1e-9
+        assert abs(r.energy - e) <= 1e-9, (r.rid, r.energy, e)
         if g is not None:
             np.testing.assert_allclose(r.grad, g, rtol=0, atol=1e-9)
