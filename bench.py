@@ -6,14 +6,19 @@ Hartree-Fock state (Haar orbital rotations, diag-Coulomb entries N(0,0.1)),
 then <psi|H|psi> for a synthetic double-factorized Hamiltonian (Hermitian
 one-body N(0,1)/16, rank 32, Haar term rotations, J_t entries N(0,0.05),
 constant -100).  Inputs are seeded synthetic data (the reference publishes no
-dataset).  A step is one energy evaluation.
+dataset).  A step is one batch: the energies of --batch-states (default 4)
+UCJ parameter sets under the Hamiltonian, as the serving loop evaluates
+them (BatchLUCJEnergy: every Hamiltonian term runs once over all the states).
 
 Reported:
 * value      complex64 evaluations/s, device time (CUDA events on the
              launching stream), inputs resident; max over ranks, summed over
              ranks (replicas).
-* e2e        the same through the public API ``ffsim_gb300.lucj_energy`` with
-             host (numpy) inputs and the energy read back every step.
+* single     one evaluation per step (LUCJEnergy) beside it.
+* served     the same workload through the continuous-batching serving loop,
+             every request submitted at once (wall clock).
+* e2e        the batch step through the public API ``BatchLUCJEnergy`` with
+             host (numpy) inputs and the energies read back every step.
 * complex128 the plain complex128 GPU path on the same GPU (fewer steps).
 * roofline   the dominant kernel (one window stage of the stage-major
              rotation: 2 S algorithmic bytes, S the state size, timed with
@@ -50,10 +55,10 @@ METRIC = "LUCJ energy evals/s norb=16 (8,8) c64 vs c128 at |dE|<=1e-6 Ha; p50/p9
 WORKLOAD = "LUCJ n_reps=2 from HF + DF Hamiltonian rank 32 energy, norb=16, nelec=(8,8)"
 
 
-def run_config(world: int) -> dict:
+def run_config(world: int, batch: int) -> dict:
     """The workload's config block, identical in both arms."""
     return {"workload": WORKLOAD, "norb": NORB, "nelec": list(NELEC), "n_reps": N_REPS, "df_rank": RANK,
-            "parallelism": f"replicas x{world}",
+            "batch_states": batch, "parallelism": f"replicas x{world}",
             "l2": "inputs larger than L2 (state 1.32 GB in complex64, 2.65 GB in complex128)"}
 
 
@@ -153,6 +158,61 @@ def time_energy(dtype, steps, warmup, ucj, ham, stream):
     del ev
     torch.cuda.empty_cache()
     return times, energies
+
+
+def make_batch_ops(seed: int, n: int, first):
+    """The operators of a batch step: the single-evaluation workload's
+    operator first, then n - 1 more drawn the same way (other seeds)."""
+    import ffsim_gb300 as f
+
+    return [first] + [f.random.random_ucj_op_spin_balanced(NORB, n_reps=N_REPS, diag_coulomb_normal=True,
+                                                           diag_coulomb_scale=0.1, seed=seed + 1000 * k)
+                      for k in range(1, n)]
+
+
+def time_batch_energy(dtype, steps, warmup, ops, ham, stream):
+    """Per-step CUDA-event times (ms) of batched LUCJ energy evaluations (one
+    step = the energies of every operator of `ops`, BatchLUCJEnergy) on
+    `stream`; returns (times, energies of the last step)."""
+    import torch
+
+    import ffsim_gb300 as f
+
+    ev = f.BatchLUCJEnergy(NORB, NELEC, len(ops), dtype=dtype)
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            energies = ev(ops, ham)
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for k in range(steps):
+            starts[k].record(stream)
+            energies = ev(ops, ham)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    del ev
+    torch.cuda.empty_cache()
+    return times, energies
+
+
+def time_batch_e2e(steps, ops, ham):
+    """Wall time per batch step through the public API (host parameter arrays
+    in, energies read back)."""
+    import torch
+
+    import ffsim_gb300 as f
+
+    ev = f.BatchLUCJEnergy(NORB, NELEC, len(ops), dtype=torch.complex64)
+    ev(ops, ham)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ev(ops, ham)
+    t1 = time.perf_counter()
+    del ev
+    torch.cuda.empty_cache()
+    return (t1 - t0) / steps
 
 
 def time_e2e(steps, ucj, ham):
@@ -591,7 +651,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "evals/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": run_config(world),
+        "config": run_config(world, args.batch_states),
         "cpu_baseline": {"value": val, "unit": "evals/s", "cores": cores, "kind": "port",
                          "sample": f"one orbital rotation ({t_rot:.2f} s) + one diag-Coulomb evolution "
                                    f"({t_dc:.2f} s) at norb=16 complex128 per step, extrapolated to "
@@ -640,6 +700,7 @@ def main():
     ap.add_argument("--workers", type=int, default=2, help="--serve: batches in flight")
     ap.add_argument("--max-batch", type=int, default=16, help="--serve: states per batch")
     ap.add_argument("--served", type=int, default=8, help="norb-16 requests of the served measurement (0: skip)")
+    ap.add_argument("--batch-states", type=int, default=4, help="evaluations per step (one batch)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.ops:
@@ -681,28 +742,31 @@ def main():
     ucj, ham = make_inputs(2026 + rank)
     stream = torch.cuda.Stream()
 
-    # complex64: the headline
+    # complex64 batches of B evaluations: the headline (a step is one batch)
+    B = args.batch_states
+    ops = make_batch_ops(2026 + rank, B, ucj)
     barrier()
     clocks = ClockSampler(local)
     clocks.start()
     n0 = lib.ffgb_launch_count()
     t_wall0 = time.perf_counter()
-    times64, energies64 = time_energy(torch.complex64, args.steps, args.warmup, ucj, ham, stream)
+    times64, energies64 = time_batch_energy(torch.complex64, args.steps, args.warmup, ops, ham, stream)
     t_wall1 = time.perf_counter()
     launches = (lib.ffgb_launch_count() - n0) // (args.steps + args.warmup)
     clk = clocks.stop()
     barrier()
     total_ms = replica_max_ms(sum(times64), dist, "cuda")
-    value = replica_throughput(world, args.steps, total_ms)
+    value = replica_throughput(world, args.steps * B, total_ms)
 
-    # complex128 on the same GPU (fewer steps: FP64 bound)
+    # one evaluation per step (LUCJEnergy), the complex128 path on the same GPU
+    times1, energies1 = time_energy(torch.complex64, args.steps, args.warmup, ucj, ham, stream)
     times128, energies128 = time_energy(torch.complex128, args.c128_steps, 1, ucj, ham, stream)
-    e64, e128 = energies64[-1], energies128[-1]
+    e64, e64_single, e128 = float(energies64[0]), energies1[-1], energies128[-1]
 
-    # end to end through the public API (host inputs, energy read back each step)
-    e2e_s = time_e2e(max(2, min(args.steps, 5)), ucj, ham)
-    h2d = sum(np.asarray(x).nbytes for x in (ucj.diag_coulomb_mats, ucj.orbital_rotations,
-                                              ham.one_body_tensor, ham.diag_coulomb_mats, ham.orbital_rotations))
+    # end to end through the public API (host inputs, energies read back each step)
+    e2e_s = time_batch_e2e(max(2, min(args.steps, 5)), ops, ham)
+    h2d = sum(np.asarray(x).nbytes for o in ops for x in (o.diag_coulomb_mats, o.orbital_rotations)) + sum(
+        np.asarray(x).nbytes for x in (ham.one_body_tensor, ham.diag_coulomb_mats, ham.orbital_rotations))
 
     # served through the continuous-batching loop (the same workload, saturated)
     served = time_served(2026 + rank, args.served, workers=2, max_batch=4) if args.served > 0 else None
@@ -738,10 +802,16 @@ def main():
             "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": run_config(world),
+            "config": run_config(world, args.batch_states),
+            "batch_states": B,
             "p50_ms": statistics.median(times64),
             "p99_ms": float(np.percentile(times64, 99)),
             "energy_c64": e64, "energy_c128": e128, "abs_dE_c64_vs_c128": abs(e64 - e128),
+            "energy_c64_single": e64_single, "abs_dE_c64_single_vs_c128": abs(e64_single - e128),
+            "single": {"value": 1e3 / statistics.mean(times1), "unit": "evals/s",
+                       "ms_per_step": statistics.mean(times1), "p50_ms": statistics.median(times1),
+                       "p99_ms": float(np.percentile(times1, 99)), "steps": len(times1),
+                       "note": "one evaluation per step (LUCJEnergy), the final UCJ rotation merged into every term"},
             "c128": {"value": 1e3 / statistics.mean(times128), "unit": "evals/s",
                      "ms_per_step": statistics.mean(times128), "steps": len(times128),
                      "bound": "fp64",
@@ -750,8 +820,8 @@ def main():
                      "rotation_frac_of_fp64": rotation_flops(NORB, NELEC) / rot128_ms / 1e9 / fp[0]},
             "fp32_peak_tflops": fp[1],
             "served": served,
-            "e2e": {"value": world / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": 8 * (RANK + 2)},
+            "e2e": {"value": world * B / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": 8 * B},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                          "frac": gbs / peak, "traffic": traffic, "traffic_source": traffic_src,
                          "kernel": "win_class_kernel: one 8-orbital window stage (one launch per electron-count "
@@ -763,9 +833,9 @@ def main():
                                                   "GB/s": 2 * S / (st["cross_half_stage_ms"] * 1e-3) / 1e9},
                              "orbital_rotation": {"ms": st["rotation_ms"], "algorithmic_bytes": 4 * S,
                                                   "GB/s": 4 * S / (st["rotation_ms"] * 1e-3) / 1e9},
-                             "energy_eval": {"ms": total_ms / args.steps, "algorithmic_bytes": eval_bytes,
-                                             "GB/s": eval_bytes / (total_ms / args.steps * 1e-3) / 1e9,
-                                             "frac": eval_bytes / (total_ms / args.steps * 1e-3) / 1e9 / peak}}},
+                             "energy_eval": {"ms": total_ms / args.steps / B, "algorithmic_bytes": eval_bytes,
+                                             "GB/s": B * eval_bytes / (total_ms / args.steps * 1e-3) / 1e9,
+                                             "frac": B * eval_bytes / (total_ms / args.steps * 1e-3) / 1e9 / peak}}},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(launches),
