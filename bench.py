@@ -250,6 +250,20 @@ def window_stage_traffic():
     return (total if total > 0 else None), str(p.relative_to(ROOT))
 
 
+def eval_bytes_moved():
+    """DRAM bytes (read + write) of one whole evaluation at norb=16 (8,8),
+    summed over its launches in the committed ncu capture
+    profiles/lucj_energy_norb16_c64_dram.txt.  None when absent."""
+    p = ROOT / "profiles" / "lucj_energy_norb16_c64_dram.txt"
+    if not p.exists():
+        return None, None
+    for line in p.read_text().splitlines():
+        parts = [x.strip() for x in line.split("|")]
+        if len(parts) >= 3 and parts[0] == "total":
+            return float(parts[2]), str(p.relative_to(ROOT))
+    return None, None
+
+
 def rotation_flops(norb: int, nelec) -> float:
     """Floating-point operations of the complex128 two-sector rotation: the
     adjacent-Givens network has norb (norb - 1) / 2 rotations per sector, each
@@ -347,6 +361,32 @@ def time_rotation_c128(stream, reps: int = 2) -> float:
     return a.elapsed_time(b) / reps
 
 
+def run_profile_eval(args) -> None:
+    """Two single LUCJ energy evaluations of the metric's workload shape at
+    --norb (half filling), nothing timed: the second is the one a profiler
+    captures (its launches follow the first's, the same number)."""
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _lib
+
+    norb = args.norb
+    nelec = (norb // 2, norb - norb // 2)
+    ucj = f.random.random_ucj_op_spin_balanced(norb, n_reps=N_REPS, diag_coulomb_normal=True,
+                                               diag_coulomb_scale=0.1, seed=2026)
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=2 * norb, seed=2027)
+    ev = f.LUCJEnergy(norb, nelec, dtype=torch.complex64)
+    lib = _lib.load()
+    counts = []
+    for _ in range(2):
+        n0 = lib.ffgb_launch_count()
+        e = ev(ucj, ham)
+        torch.cuda.synchronize()
+        counts.append(lib.ffgb_launch_count() - n0)
+    print(json.dumps({"profile_eval": norb, "energy": e, "launches_per_evaluation": counts,
+                      "state_bytes": f.dim(norb, nelec) * 8, "df_rank": 2 * norb}), flush=True)
+
+
 def run_ops(args) -> None:
     """Per-operation GB/s on a resident state (--ops): one JSON line per op,
     each against its algorithmic bytes (S = state bytes)."""
@@ -377,7 +417,7 @@ def run_ops(args) -> None:
         v = torch.randn(d, dtype=dtype, device="cuda")
         v /= torch.linalg.vector_norm(v)
         out = torch.empty_like(v)
-        buf, nbytes = scratch(v, 2, norb, *nelec)
+        buf, nbytes = scratch(v, 3, norb, *nelec)  # the largest: two states plus density partials
 
     def timed(fn):
         for _ in range(min(args.warmup, 2)):
@@ -435,6 +475,14 @@ def run_ops(args) -> None:
     ops["ucj_spin_unbalanced_apply_L2"] = (3 * 4 * S + 2 * 2 * S, on_stream(
         lambda: f.apply_unitary(v, ucju, norb, nelec, copy=False)))
     ops["rdm1"] = (S, on_stream(lambda: f.rdms(v, norb, nelec)))
+    # the adjoint gradient's densities between two states (each reads both once)
+    dens_out = np.zeros(2 * 3 * norb * norb)
+    ops["density_transition_rdm1"] = (2 * S, lambda: _lib.call(
+        "ffgb_transition_rdm1", v.data_ptr(), out.data_ptr(), code, norb, nelec[0], nelec[1], _lib.dptr(dens_out),
+        buf.data_ptr(), nbytes, sptr))
+    ops["density_pair"] = (2 * S, lambda: _lib.call(
+        "ffgb_pair_density", v.data_ptr(), out.data_ptr(), code, norb, nelec[0], nelec[1], _lib.dptr(dens_out),
+        buf.data_ptr(), nbytes, sptr))
     # split-operator step of a Hubbard chain (hopping 1, U 4): one rotation by
     # the banded near-identity exp(-i 0.1 h) and one diagonal evolution (the
     # closing rotation by the identity is skipped)
@@ -692,6 +740,8 @@ def main():
     ap.add_argument("--dtype", default="c64", choices=["c64", "c128"], help="--ops: state dtype")
     ap.add_argument("--reps", type=int, default=5, help="--ops: timed repetitions per op")
     ap.add_argument("--op", default="", help="--ops: only the ops whose name contains this text")
+    ap.add_argument("--profile-eval", action="store_true",
+                    help="two single evaluations at --norb, untimed (for a profiler's launch list)")
     ap.add_argument("--grad", action="store_true", help="gradient workload (norb=12, batch of parameters)")
     ap.add_argument("--batch", type=int, default=64, help="--grad: parameter vectors")
     ap.add_argument("--serve", action="store_true", help="serving workload (mixed requests, Poisson arrivals)")
@@ -705,6 +755,9 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.ops:
         run_ops(args)
+        return
+    if args.profile_eval:
+        run_profile_eval(args)
         return
     if args.grad:
         run_grad(args)
@@ -774,6 +827,7 @@ def main():
     # dominant kernel roofline
     st = stage_rooflines(stream)
     traffic, traffic_src = window_stage_traffic()
+    moved, moved_src = eval_bytes_moved()
     # the complex128 path against the measured FP64 FMA rate
     fp = np.zeros(2)
     lib.ffgb_debug_fma_rate(1, _lib.dptr(fp[:1]), stream.cuda_stream)
@@ -834,6 +888,7 @@ def main():
                              "orbital_rotation": {"ms": st["rotation_ms"], "algorithmic_bytes": 4 * S,
                                                   "GB/s": 4 * S / (st["rotation_ms"] * 1e-3) / 1e9},
                              "energy_eval": {"ms": total_ms / args.steps / B, "algorithmic_bytes": eval_bytes,
+                                             "bytes_moved_single": moved, "bytes_moved_source": moved_src,
                                              "GB/s": B * eval_bytes / (total_ms / args.steps * 1e-3) / 1e9,
                                              "frac": B * eval_bytes / (total_ms / args.steps * 1e-3) / 1e9 / peak}}},
             "cpu_baseline": cpu,

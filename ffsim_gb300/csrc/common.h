@@ -86,12 +86,14 @@ inline long long stack_pad(long long n) { return (n + STACK_TILE - 1) / STACK_TI
 // Densities between two states (grad.cu); results summed on the host in FP64.
 template <typename T>
 int rdm1_rows(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
-              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st);
+              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st, int nocc,
+              const unsigned* sub, int n_sub);
 template <typename T>
 int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
               int norb, void* partial_buf, size_t partial_bytes, std::vector<double>& rr, std::vector<double>& rc,
               cudaStream_t st);
 size_t density_partial_bytes(int norb, long long rows);
+size_t density_sub_bytes(int norb, long long n_sub, int nv);
 template <typename T>
 int launch_transpose(const void* in, void* out, long long rows, long long cols, const void* row_ph,
                      const void* col_ph, cudaStream_t st);

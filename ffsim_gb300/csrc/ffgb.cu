@@ -1595,6 +1595,15 @@ static int contract_static_impl(const void* vec, void* out, int norb, int na, in
   return run_pass<T>(A, scr, st);
 }
 
+// Partial-sum bytes of densities() for both sectors and both kernel forms.
+static size_t density_scratch(int norb, int na, int nb) {
+  size_t b = std::max(density_partial_bytes(norb, binom_h(norb, na)),
+                      density_partial_bytes(norb, binom_h(norb, std::max(nb, 0))));
+  for (int n : {na, nb})
+    if (n >= 1) b = std::max(b, density_sub_bytes(norb, binom_h(norb, n - 1), norb - n + 1));
+  return b;
+}
+
 // Densities between two states: the beta sector runs on transposed copies.
 template <typename T>
 static int densities(const void* x, const void* y, int norb, int na, int nb, bool pair, double* out,
@@ -1607,16 +1616,22 @@ static int densities(const void* x, const void* y, int norb, int na, int nb, boo
   const size_t S = (size_t)(da * db) * sizeof(C);
   void* tx = scr.take(S);
   void* ty = scr.take(S);
-  const size_t pbytes = std::max(density_partial_bytes(norb, da), density_partial_bytes(norb, db));
+  const size_t pbytes = density_scratch(norb, na, nb);
   void* part = scr.take(pbytes);
+  // strings with one electron fewer (the transition density's sub-string form)
+  const unsigned *sa1 = nullptr, *sb1 = nullptr;
+  if (na >= 1) FFGB_TRY(device_strings(norb, na - 1, &sa1));
+  if (nb >= 1) FFGB_TRY(device_strings(norb, nb - 1, &sb1));
   if (!tx || !ty || !part) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
   FFGB_TRY(launch_transpose<T>(x, tx, da, db, nullptr, nullptr, st));
   FFGB_TRY(launch_transpose<T>(y, ty, da, db, nullptr, nullptr, st));
   const size_t n2 = 2 * (size_t)norb * norb;
   if (!pair) {
     std::vector<double> ga, gb;
-    FFGB_TRY(rdm1_rows<T>(x, y, sa, (int)da, (int)db, norb, part, pbytes, ga, st));
-    FFGB_TRY(rdm1_rows<T>(tx, ty, sb, (int)db, (int)da, norb, part, pbytes, gb, st));
+    FFGB_TRY(rdm1_rows<T>(x, y, sa, (int)da, (int)db, norb, part, pbytes, ga, st, na, sa1,
+                          na >= 1 ? (int)binom_h(norb, na - 1) : 0));
+    FFGB_TRY(rdm1_rows<T>(tx, ty, sb, (int)db, (int)da, norb, part, pbytes, gb, st, nb, sb1,
+                          nb >= 1 ? (int)binom_h(norb, nb - 1) : 0));
     std::memcpy(out, ga.data(), n2 * sizeof(double));
     std::memcpy(out + n2, gb.data(), n2 * sizeof(double));
   } else {
@@ -1767,10 +1782,7 @@ size_t ffgb_scratch_bytes(int op, int dtype, int norb, int na, int nb) {
   const size_t S = (size_t)da * db * el;
   const size_t ex = extras_bytes(norb, na, nb) + 4096;
   if (op == 1 || op == 2) return 2 * S + ex;
-  if (op == 3) {
-    const long long m = std::max<long long>(std::max(da, db), 1);
-    return 2 * S + density_partial_bytes(norb, m) + ex;
-  }
+  if (op == 3) return 2 * S + density_scratch(norb, na, std::max(nb, 0)) + ex;
   return S + ex;
 }
 

@@ -102,6 +102,141 @@ __global__ void __launch_bounds__(DTHREADS) rdm1_kernel(const typename CT<T>::ty
   if (threadIdx.x == 0) partial[(long long)pair * gridDim.x + blockIdx.x] = s;
 }
 
+// The same density from the strings with one electron fewer: for every
+// (n-1)-string s and column c,
+//   G_pq += conj(sg_p(s) x[s + p][c]) sg_q(s) y[s + q][c]   (p, q not in s),
+// sg_p(s) = (-1)^(electrons of s below p) the sign of a_p on s + p.  One CTA
+// per s holds the (NV x NV) block over the vacancies of s (NV = norb - n + 1),
+// so every row is read n times instead of once per (p, q) pair; the CTA's
+// block goes to partial[s] (FP64) and rdm1_sub_reduce_kernel sums the blocks
+// into G in a fixed order.  complex64 states, per-thread sums in FP32.
+// NI = rows of the block per CTA: the block's rows [blockIdx.y * NI, ...) (all
+// NV rows in one CTA when NI == NV; two CTAs for large NV, which would spill).
+template <int NV, int NI>
+__global__ void __launch_bounds__(DTHREADS) rdm1_sub_kernel(const float2* __restrict__ x,
+                                                            const float2* __restrict__ y,
+                                                            const unsigned* __restrict__ sub, int cols, int norb,
+                                                            double2* __restrict__ partial) {
+  __shared__ int sB[FFGB_BST * FFGB_BST];
+  __shared__ long long srow[NV];
+  __shared__ float ssg[NV];
+  for (int idx = threadIdx.x; idx < FFGB_BST * FFGB_BST; idx += DTHREADS) {
+    const int a = idx / FFGB_BST, b = idx % FFGB_BST;
+    long long r = 0;
+    if (b <= a) {
+      r = 1;
+      for (int i = 1; i <= b; ++i) r = r * (a - b + i) / i;
+    }
+    sB[idx] = (int)r;
+  }
+  __syncthreads();
+  const unsigned s = sub[blockIdx.x];
+  if (threadIdx.x < NV) {  // the j-th vacancy of s, its row and sign
+    int v = -1;
+    for (int o = 0, k = 0; o < norb; ++o)
+      if (!((s >> o) & 1u)) {
+        if (k == (int)threadIdx.x) {
+          v = o;
+          break;
+        }
+        ++k;
+      }
+    srow[threadIdx.x] = (long long)rank_colex(s | (1u << v), sB) * cols;
+    ssg[threadIdx.x] = (__popc(s & ((1u << v) - 1u)) & 1) ? -1.f : 1.f;
+  }
+  __syncthreads();
+  const int i0 = blockIdx.y * NI;
+  float2 acc[NI][NV];
+#pragma unroll
+  for (int i = 0; i < NI; ++i)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) acc[i][j] = make_float2(0.f, 0.f);
+  for (int c = threadIdx.x; c < cols; c += DTHREADS) {
+    float2 xv[NI], yv[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      const float2 b = y[srow[j] + c];
+      yv[j] = make_float2(ssg[j] * b.x, ssg[j] * b.y);
+    }
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      if (i0 + i < NV) {  // uniform over the CTA
+        const float2 a = x[srow[i0 + i] + c];
+        xv[i] = make_float2(ssg[i0 + i] * a.x, ssg[i0 + i] * a.y);
+      } else {
+        xv[i] = make_float2(0.f, 0.f);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NI; ++i)
+#pragma unroll
+      for (int j = 0; j < NV; ++j) acc[i][j] = cdot_row(acc[i][j], xv[i], yv[j]);
+  }
+  // every warp sums its lanes' blocks, then one thread per entry sums the
+  // warps (fixed order): one barrier for the whole block
+  __shared__ double2 wsum[DTHREADS / 32][NI * NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NI; ++i)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double2 v = to_d2(acc[i][j]);
+      for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+      }
+      if (lane == 0) wsum[warp][i * NV + j] = v;
+    }
+  __syncthreads();
+  double2* out = partial + (long long)blockIdx.x * NV * NV;
+  for (int e = threadIdx.x; e < NI * NV; e += DTHREADS) {
+    const int i = e / NV, j = e - i * NV;
+    if (i0 + i >= NV) continue;
+    double2 t = make_double2(0.0, 0.0);
+    for (int w = 0; w < DTHREADS / 32; ++w) {
+      t.x += wsum[w][e].x;
+      t.y += wsum[w][e].y;
+    }
+    out[(i0 + i) * NV + j] = t;
+  }
+}
+
+// G_pq = sum over the (n-1)-strings s with p, q not in s of block[s][i][j],
+// i / j the positions of p / q among the vacancies of s; one CTA per (p, q),
+// fixed order.
+__global__ void __launch_bounds__(DTHREADS) rdm1_sub_reduce_kernel(const double2* __restrict__ partial,
+                                                                   const unsigned* __restrict__ sub, int n_sub,
+                                                                   int nv, int norb, double2* __restrict__ g) {
+  __shared__ double2 sh[DTHREADS / 32];
+  const int p = blockIdx.x / norb, q = blockIdx.x - p * norb;
+  double2 a = make_double2(0.0, 0.0);
+  for (int t = threadIdx.x; t < n_sub; t += DTHREADS) {
+    const unsigned s = sub[t];
+    if (((s >> p) & 1u) || ((s >> q) & 1u)) continue;
+    const int i = p - __popc(s & ((1u << p) - 1u)), j = q - __popc(s & ((1u << q) - 1u));
+    const double2 v = partial[(long long)t * nv * nv + i * nv + j];
+    a.x += v.x;
+    a.y += v.y;
+  }
+  const double2 r = block_sum2(a, sh);
+  if (threadIdx.x == 0) g[blockIdx.x] = r;
+}
+
+template <int NV>
+int launch_rdm1_sub(const void* x, const void* y, const unsigned* sub, int n_sub, int cols, int norb,
+                    double2* partial, double2* g, cudaStream_t st) {
+  constexpr int NI = NV >= 7 ? 3 : NV;  // at most 3 x 10 accumulators: two CTAs per SM
+  const dim3 grid((unsigned)n_sub, (unsigned)((NV + NI - 1) / NI));
+  rdm1_sub_kernel<NV, NI><<<grid, DTHREADS, 0, st>>>((const float2*)x, (const float2*)y, sub, cols, norb,
+                                                     partial);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  rdm1_sub_reduce_kernel<<<norb * norb, DTHREADS, 0, st>>>(partial, sub, n_sub, NV, norb, g);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+
 // Pair densities within the row sector (P^rr_ij, rows i, j) and between the
 // row and column sectors (P^rc_ij) over a chunk of rows.
 template <typename T>
@@ -176,9 +311,41 @@ __global__ void __launch_bounds__(DTHREADS) pair_density_kernel(const typename C
 }  // namespace
 
 // Transition one-body density of the sector on the rows of x, y (rows x cols).
+// complex64 sectors with 1 <= nocc and at most 10 vacancies per (nocc-1)-string
+// run rdm1_sub_kernel over `sub` (the nocc-1 strings); others rdm1_kernel.
 template <typename T>
 int rdm1_rows(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
-              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st) {
+              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st, int nocc,
+              const unsigned* sub, int n_sub) {
+  const int nv = norb - nocc + 1;
+  // small sectors stay on rdm1_kernel: there the sub-string form's per-CTA
+  // overhead outweighs its fewer row reads (measured: 1.0 against 0.5 ms at
+  // norb 12, 33 against 58 ms at norb 16)
+  const bool large = (long long)rows * cols >= (1LL << 23);
+  if (sizeof(T) == 4 && large && sub && nocc >= 1 && nv >= 1 && nv <= 10 && n_sub > 0 && cols > 0) {
+    const size_t need = sizeof(double2) * ((size_t)n_sub * nv * nv + (size_t)norb * norb);
+    if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
+    double2* part = (double2*)partial_buf;
+    double2* g = part + (size_t)n_sub * nv * nv;
+    int s = FFGB_OK;
+    switch (nv) {
+      case 1: s = launch_rdm1_sub<1>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 2: s = launch_rdm1_sub<2>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 3: s = launch_rdm1_sub<3>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 4: s = launch_rdm1_sub<4>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 5: s = launch_rdm1_sub<5>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 6: s = launch_rdm1_sub<6>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 7: s = launch_rdm1_sub<7>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 8: s = launch_rdm1_sub<8>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 9: s = launch_rdm1_sub<9>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      default: s = launch_rdm1_sub<10>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+    }
+    if (s) return s;
+    out.assign(2 * (size_t)norb * norb, 0.0);
+    FFGB_CUDA(cudaMemcpyAsync(out.data(), g, sizeof(double2) * (size_t)norb * norb, cudaMemcpyDeviceToHost, st));
+    FFGB_CUDA(cudaStreamSynchronize(st));
+    return FFGB_OK;
+  }
   const int chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
   const size_t need = sizeof(double2) * (size_t)chunks * norb * norb;
   if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
@@ -233,18 +400,24 @@ int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned
 }
 
 template int rdm1_rows<float>(const void*, const void*, const unsigned*, int, int, int, void*, size_t,
-                              std::vector<double>&, cudaStream_t);
+                              std::vector<double>&, cudaStream_t, int, const unsigned*, int);
 template int rdm1_rows<double>(const void*, const void*, const unsigned*, int, int, int, void*, size_t,
-                               std::vector<double>&, cudaStream_t);
+                               std::vector<double>&, cudaStream_t, int, const unsigned*, int);
 template int pair_rows<float>(const void*, const void*, const unsigned*, const unsigned*, int, int, int, void*,
                               size_t, std::vector<double>&, std::vector<double>&, cudaStream_t);
 template int pair_rows<double>(const void*, const void*, const unsigned*, const unsigned*, int, int, int, void*,
                                size_t, std::vector<double>&, std::vector<double>&, cudaStream_t);
 
-// Partial-sum bytes the density kernels need for a sector of `rows` strings.
+// Partial-sum bytes the density kernels need for a sector of `rows` strings
+// (also enough for rdm1_sub_kernel's blocks: at most rows * norb * ... see below).
 size_t density_partial_bytes(int norb, long long rows) {
   const long long chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
   return sizeof(double2) * (size_t)chunks * 2 * norb * norb + 256;
+}
+
+// Partial-sum bytes of rdm1_sub_kernel for n_sub strings with nv vacancies.
+size_t density_sub_bytes(int norb, long long n_sub, int nv) {
+  return sizeof(double2) * ((size_t)n_sub * nv * nv + (size_t)norb * norb) + 256;
 }
 
 }  // namespace ffgb

@@ -62,6 +62,22 @@ def _dexp(K: np.ndarray, dK: np.ndarray) -> np.ndarray:
     return W @ (M * phi[None]) @ Wd
 
 
+def _dexp_adjoint(K: np.ndarray, gam: np.ndarray) -> np.ndarray:
+    """The matrix G with Re <dexp(K)[dK], gam> = Re <dK, G> for every dK
+    (<X, Y> = sum_pq X_pq Y_pq): the adjoint of _dexp.  With K = W diag(i w)
+    W^dag and dexp(K)[dK] = W ((W^dag dK W) o Phi) W^dag, G = conj(W)
+    (Phi o (W^T gam conj(W))) W^T."""
+    w, W = np.linalg.eigh(-1j * K)
+    e = np.exp(1j * w)
+    diff = 1j * (w[:, None] - w[None, :])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        phi = (e[:, None] - e[None, :]) / diff
+    close = np.abs(diff) < 1e-12
+    phi[close] = np.broadcast_to(e[:, None], phi.shape)[close]
+    Wc = W.conj()
+    return Wc @ (phi * (W.T @ gam @ Wc)) @ W.T
+
+
 class LUCJGradient:
     """Energy and gradient of the LUCJ ansatz for one (norb, nelec) shape,
     holding its device buffers (two states and scratch)."""
@@ -86,6 +102,8 @@ class LUCJGradient:
         self.buf = torch.empty(need, dtype=torch.uint8, device=device)
         self.nbytes = need
         self.basis = _antihermitian_basis(norb)
+        # upper-triangle index pairs (i <= j) in the parameter order of from_parameters
+        self._triu = tuple(np.array(v) for v in zip(*itertools.combinations_with_replacement(range(norb), 2)))
 
     # -- device helpers ----------------------------------------------------
     def _stream(self):
@@ -161,36 +179,36 @@ class LUCJGradient:
         """Chain rule from the generator gradients to the parameters."""
         norb = self.norb
         grad = np.zeros_like(params)
-        triu = list(itertools.combinations_with_replacement(range(norb), 2))
-        n_triu = len(triu)
+        ti, tj = self._triu
+        n_triu = len(ti)
+        diag = ti == tj
         index = 0
         for k in range(1, L + 1):
             Kk = antihermitians_from_parameters(params[index: index + norb * norb], norb, 1)[0]
-            dU = _dexp(Kk, self.basis)  # (norb**2, norb, norb)
-            # V_k = U_k^dag U_{k-1}:  G = U_{k-1}^dag U_k dU_k^dag U_{k-1}
-            Gk = (U[k - 1].conj().T @ U[k]) @ dU.conj().transpose(0, 2, 1) @ U[k - 1]
-            # V_{k+1} = U_{k+1}^dag U_k (or U_final U_L):  G = U_k^dag dU_k
-            Gk1 = U[k].conj().T @ dU
-            grad[index: index + norb * norb] = 2 * (
-                (Gk * gamma[k]).sum(axis=(1, 2)).real + (Gk1 * gamma[k + 1]).sum(axis=(1, 2)).real)
+            # V_k = U_k^dag U_{k-1} is perturbed as A dU_k^dag C (A = U_{k-1}^dag U_k,
+            # C = U_{k-1}) and V_{k+1} = U_{k+1}^dag U_k (or U_final U_L) as D dU_k
+            # (D = U_k^dag); sum_pq (A X C)_pq g_pq = <X, A^T g C^T>, so both
+            # contributions are 2 Re <dU_k, Gam> with one matrix Gam
+            A = U[k - 1].conj().T @ U[k]
+            g1 = A.T @ gamma[k] @ U[k - 1].T
+            gam = g1.conj().T + U[k].conj() @ gamma[k + 1]
+            grad[index: index + norb * norb] = 2 * np.einsum(
+                "nab,ab->n", self.basis, _dexp_adjoint(Kk, gam)).real
             index += norb * norb
             P = pdens[k]
-            for t, (i, j) in enumerate(triu):
-                if i == j:
-                    daa = 0.5 * (P[0, i, i] + P[2, i, i])
-                    dab = P[1, i, i]
-                else:
-                    daa = P[0, i, j] + P[2, i, j]
-                    dab = P[1, i, j] + P[1, j, i]
-                grad[index + t] = -2 * daa.imag
-                grad[index + n_triu + t] = -2 * dab.imag
+            # same-spin: the pair (i, j) of both sectors, halved on the diagonal;
+            # opposite-spin: both orders of (i, j), once on the diagonal
+            daa = np.where(diag, 0.5, 1.0) * (P[0, ti, tj] + P[2, ti, tj])
+            dab = np.where(diag, P[1, ti, tj], P[1, ti, tj] + P[1, tj, ti])
+            grad[index: index + n_triu] = -2 * daa.imag
+            grad[index + n_triu: index + 2 * n_triu] = -2 * dab.imag
             index += 2 * n_triu
         if with_final:
             Kf = antihermitians_from_parameters(params[index:], norb, 1)[0]
-            dUf = _dexp(Kf, self.basis)
-            # V_{L+1} = U_final U_L:  G = U_L^dag U_final^dag dU_final U_L
-            Gf = (U[L].conj().T @ Uf.conj().T) @ dUf @ U[L]
-            grad[index:] = 2 * (Gf * gamma[L + 1]).sum(axis=(1, 2)).real
+            # V_{L+1} = U_final U_L perturbed as A dU_final C (A = U_L^dag U_final^dag, C = U_L)
+            A = U[L].conj().T @ Uf.conj().T
+            gam = A.T @ gamma[L + 1] @ U[L].T
+            grad[index:] = 2 * np.einsum("nab,ab->n", self.basis, _dexp_adjoint(Kf, gam)).real
         return grad
 
     def _vdot(self, x: torch.Tensor, y: torch.Tensor) -> float:
