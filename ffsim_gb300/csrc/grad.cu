@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "common.h"
@@ -238,36 +239,46 @@ int launch_rdm1_sub(const void* x, const void* y, const unsigned* sub, int n_sub
 }
 
 // Pair densities within the row sector (P^rr_ij, rows i, j) and between the
-// row and column sectors (P^rc_ij) over a chunk of rows.
+// row and column sectors (P^rc_ij) over a chunk of PAIR_ROWS rows, one row per
+// warp: per row the lanes sum w = conj(x) y over their columns (in the
+// state's precision), in total and per occupied column orbital, reduce across
+// the warp in FP64 by shuffles (no block barrier), and add the row's terms to
+// the warp's own FP64 accumulators in shared memory; the CTA then sums its
+// warps in a fixed order.
+constexpr int PAIR_THREADS = 128;
+constexpr int PAIR_ROWS = PAIR_THREADS / 32;
+
 template <typename T>
-__global__ void __launch_bounds__(DTHREADS) pair_density_kernel(const typename CT<T>::type* __restrict__ x,
-                                                                const typename CT<T>::type* __restrict__ y,
-                                                                const unsigned* __restrict__ rstr,
-                                                                const unsigned* __restrict__ cstr, int rows,
-                                                                int cols, int norb, double2* __restrict__ partial) {
-  __shared__ double2 sh[DTHREADS / 32];
-  __shared__ double2 acc_rr[FFGB_MAXN * FFGB_MAXN], acc_rc[FFGB_MAXN * FFGB_MAXN];
-  __shared__ double2 red[FFGB_MAXN + 1];
-  for (int i = threadIdx.x; i < FFGB_MAXN * FFGB_MAXN; i += DTHREADS) {
-    acc_rr[i] = make_double2(0.0, 0.0);
-    acc_rc[i] = make_double2(0.0, 0.0);
+__global__ void __launch_bounds__(PAIR_THREADS) pair_density_kernel(const typename CT<T>::type* __restrict__ x,
+                                                                    const typename CT<T>::type* __restrict__ y,
+                                                                    const unsigned* __restrict__ rstr,
+                                                                    const unsigned* __restrict__ cstr, int rows,
+                                                                    int cols, int norb,
+                                                                    double2* __restrict__ partial) {
+  using Cx = typename CT<T>::type;
+  constexpr int NW = PAIR_THREADS / 32;
+  __shared__ double2 acc_rr[NW][FFGB_MAXN * FFGB_MAXN], acc_rc[NW][FFGB_MAXN * FFGB_MAXN];
+  __shared__ double2 vsh[NW][FFGB_MAXN + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nn = norb * norb;
+  for (int i = lane; i < nn; i += 32) {
+    acc_rr[warp][i] = make_double2(0.0, 0.0);
+    acc_rc[warp][i] = make_double2(0.0, 0.0);
   }
-  __syncthreads();
-  const int a0 = blockIdx.x * RDM_ROWS, a1 = min(a0 + RDM_ROWS, rows);
-  for (int a = a0; a < a1; ++a) {
-    const auto* xr = x + (long long)a * cols;
-    const auto* yr = y + (long long)a * cols;
-    using Cx = typename CT<T>::type;
-    Cx r, cj[FFGB_MAXN];
-    r.x = r.y = (T)0;
+  const int r = blockIdx.x * PAIR_ROWS + warp;
+  if (r < rows) {
+    const Cx* xr = x + (long long)r * cols;
+    const Cx* yr = y + (long long)r * cols;
+    Cx tot, cj[FFGB_MAXN];
+    tot.x = tot.y = (T)0;
 #pragma unroll
     for (int j = 0; j < FFGB_MAXN; ++j) cj[j].x = cj[j].y = (T)0;
-    for (int c = threadIdx.x; c < cols; c += DTHREADS) {
+    for (int c = lane; c < cols; c += 32) {
       Cx w;
       w.x = w.y = (T)0;
       w = cdot_row(w, xr[c], yr[c]);
-      r.x += w.x;
-      r.y += w.y;
+      tot.x += w.x;
+      tot.y += w.y;
       const unsigned sc = cstr[c];
 #pragma unroll
       for (int j = 0; j < FFGB_MAXN; ++j)
@@ -276,36 +287,64 @@ __global__ void __launch_bounds__(DTHREADS) pair_density_kernel(const typename C
           cj[j].y += w.y;
         }
     }
-    const double2 rs = block_sum2(to_d2(r), sh);
-    if (threadIdx.x == 0) red[FFGB_MAXN] = rs;
+    // butterfly sums in FP64: every lane ends with the row's totals
+    double2 R = to_d2(tot);
+    for (int o = 16; o > 0; o >>= 1) {
+      R.x += __shfl_xor_sync(0xffffffffu, R.x, o);
+      R.y += __shfl_xor_sync(0xffffffffu, R.y, o);
+    }
 #pragma unroll
     for (int j = 0; j < FFGB_MAXN; ++j) {
-      if (j < norb) {  // uniform: every thread takes the same branch
-        const double2 v = block_sum2(to_d2(cj[j]), sh);
-        if (threadIdx.x == 0) red[j] = v;
+      if (j < norb) {  // uniform
+        double2 v = to_d2(cj[j]);
+        for (int o = 16; o > 0; o >>= 1) {
+          v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+          v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        if (lane == 0) vsh[warp][j] = v;
       }
     }
-    __syncthreads();
-    const unsigned sr = rstr[a];
-    for (int idx = threadIdx.x; idx < norb * norb; idx += DTHREADS) {
+    __syncwarp();
+    const unsigned sr = rstr[r];
+    for (int idx = lane; idx < nn; idx += 32) {
       const int i = idx / norb, j = idx - i * norb;
       if (!((sr >> i) & 1u)) continue;
-      const double2 c = red[j];
-      acc_rc[i * FFGB_MAXN + j].x += c.x;
-      acc_rc[i * FFGB_MAXN + j].y += c.y;
+      const double2 v = vsh[warp][j];
+      acc_rc[warp][idx].x += v.x;
+      acc_rc[warp][idx].y += v.y;
       if ((sr >> j) & 1u) {
-        acc_rr[i * FFGB_MAXN + j].x += red[FFGB_MAXN].x;
-        acc_rr[i * FFGB_MAXN + j].y += red[FFGB_MAXN].y;
+        acc_rr[warp][idx].x += R.x;
+        acc_rr[warp][idx].y += R.y;
       }
     }
-    __syncthreads();
   }
-  double2* out = partial + (long long)blockIdx.x * 2 * norb * norb;
-  for (int idx = threadIdx.x; idx < norb * norb; idx += DTHREADS) {
-    const int i = idx / norb, j = idx - i * norb;
-    out[idx] = acc_rr[i * FFGB_MAXN + j];
-    out[norb * norb + idx] = acc_rc[i * FFGB_MAXN + j];
+  __syncthreads();
+  double2* out = partial + (long long)blockIdx.x * 2 * nn;
+  for (int idx = threadIdx.x; idx < nn; idx += PAIR_THREADS) {
+    double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+    for (int w = 0; w < NW; ++w) {
+      a.x += acc_rr[w][idx].x;
+      a.y += acc_rr[w][idx].y;
+      b.x += acc_rc[w][idx].x;
+      b.y += acc_rc[w][idx].y;
+    }
+    out[idx] = a;
+    out[nn + idx] = b;
   }
+}
+
+// out[k] = sum over c < chunks of partial[c * per + k], in order of c.
+__global__ void __launch_bounds__(256) sum_blocks_kernel(const double2* __restrict__ partial, long long chunks,
+                                                         int per, double2* __restrict__ out) {
+  const int k = blockIdx.x * 256 + threadIdx.x;
+  if (k >= per) return;
+  double2 a = make_double2(0.0, 0.0);
+  for (long long c = 0; c < chunks; ++c) {
+    const double2 v = partial[c * per + k];
+    a.x += v.x;
+    a.y += v.y;
+  }
+  out[k] = a;
 }
 
 }  // namespace
@@ -373,29 +412,28 @@ template <typename T>
 int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
               int norb, void* partial_buf, size_t partial_bytes, std::vector<double>& rr, std::vector<double>& rc,
               cudaStream_t st) {
-  const int chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
-  const size_t per = (size_t)2 * norb * norb;
-  const size_t need = sizeof(double2) * (size_t)chunks * per;
+  const long long chunks = (rows + PAIR_ROWS - 1) / PAIR_ROWS;
+  const int per = 2 * norb * norb;
+  const size_t need = sizeof(double2) * ((size_t)chunks * per + per);
   if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
-  if (rows > 0 && cols > 0 && norb > 0) {
-    pair_density_kernel<T><<<chunks, DTHREADS, 0, st>>>((const typename CT<T>::type*)x,
-                                                       (const typename CT<T>::type*)y, rstr, cstr, rows, cols,
-                                                       norb, (double2*)partial_buf);
-    count_launch();
-    FFGB_CUDA(cudaGetLastError());
-  }
-  std::vector<double> h(2 * (size_t)chunks * per, 0.0);
-  if (!h.empty()) FFGB_CUDA(cudaMemcpyAsync(h.data(), partial_buf, need, cudaMemcpyDeviceToHost, st));
-  FFGB_CUDA(cudaStreamSynchronize(st));
   rr.assign(2 * (size_t)norb * norb, 0.0);
   rc.assign(2 * (size_t)norb * norb, 0.0);
-  for (int c = 0; c < chunks; ++c)
-    for (size_t k = 0; k < (size_t)norb * norb; ++k) {
-      rr[2 * k] += h[2 * (c * per + k)];
-      rr[2 * k + 1] += h[2 * (c * per + k) + 1];
-      rc[2 * k] += h[2 * (c * per + norb * norb + k)];
-      rc[2 * k + 1] += h[2 * (c * per + norb * norb + k) + 1];
-    }
+  if (rows <= 0 || cols <= 0 || norb <= 0) return FFGB_OK;
+  double2* part = (double2*)partial_buf;
+  double2* sums = part + (size_t)chunks * per;
+  pair_density_kernel<T><<<(unsigned)chunks, PAIR_THREADS, 0, st>>>((const typename CT<T>::type*)x,
+                                                                    (const typename CT<T>::type*)y, rstr, cstr,
+                                                                    rows, cols, norb, part);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  sum_blocks_kernel<<<(per + 255) / 256, 256, 0, st>>>(part, chunks, per, sums);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  std::vector<double> h(2 * (size_t)per, 0.0);
+  FFGB_CUDA(cudaMemcpyAsync(h.data(), sums, sizeof(double2) * per, cudaMemcpyDeviceToHost, st));
+  FFGB_CUDA(cudaStreamSynchronize(st));
+  std::memcpy(rr.data(), h.data(), sizeof(double) * 2 * norb * norb);
+  std::memcpy(rc.data(), h.data() + 2 * (size_t)norb * norb, sizeof(double) * 2 * norb * norb);
   return FFGB_OK;
 }
 
@@ -411,8 +449,8 @@ template int pair_rows<double>(const void*, const void*, const unsigned*, const 
 // Partial-sum bytes the density kernels need for a sector of `rows` strings
 // (also enough for rdm1_sub_kernel's blocks: at most rows * norb * ... see below).
 size_t density_partial_bytes(int norb, long long rows) {
-  const long long chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
-  return sizeof(double2) * (size_t)chunks * 2 * norb * norb + 256;
+  const long long chunks = std::max((rows + RDM_ROWS - 1) / RDM_ROWS, (rows + PAIR_ROWS - 1) / PAIR_ROWS);
+  return sizeof(double2) * ((size_t)chunks + 1) * 2 * norb * norb + 256;
 }
 
 // Partial-sum bytes of rdm1_sub_kernel for n_sub strings with nv vacancies.
