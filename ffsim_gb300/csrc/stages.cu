@@ -21,6 +21,61 @@ int launch_win_bk(const WinJob& P, int kind, bool low, int epi, long long items,
 
 namespace {
 
+// Fork/join of a stage's independent launches (its classes touch disjoint
+// rows) over auxiliary streams, so that one class's last partial wave
+// overlaps the next class instead of leaving SMs idle.  One set of streams and
+// events per (device, calling stream), created on first use.
+constexpr int FORK_LANES = 3;
+
+struct ForkSet {
+  cudaStream_t lane[FORK_LANES] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t done[FORK_LANES] = {};
+};
+
+std::mutex g_fork_mu;
+std::map<std::pair<int, cudaStream_t>, ForkSet> g_fork;
+
+class StageFork {
+ public:
+  // n_jobs <= 1 runs everything on the calling stream
+  int begin(cudaStream_t main, int n_jobs) {
+    main_ = main;
+    if (n_jobs <= 1) return FFGB_OK;
+    int dev = 0;
+    FFGB_CUDA(cudaGetDevice(&dev));
+    {
+      std::lock_guard<std::mutex> lk(g_fork_mu);
+      ForkSet& f = g_fork[std::make_pair(dev, main)];
+      if (!f.fork) {
+        for (int i = 0; i < FORK_LANES; ++i) {
+          FFGB_CUDA(cudaStreamCreateWithFlags(&f.lane[i], cudaStreamNonBlocking));
+          FFGB_CUDA(cudaEventCreateWithFlags(&f.done[i], cudaEventDisableTiming));
+        }
+        FFGB_CUDA(cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming));
+      }
+      set_ = &f;
+    }
+    FFGB_CUDA(cudaEventRecord(set_->fork, main));
+    for (int i = 0; i < FORK_LANES; ++i) FFGB_CUDA(cudaStreamWaitEvent(set_->lane[i], set_->fork, 0));
+    return FFGB_OK;
+  }
+  cudaStream_t lane(int i) const { return set_ ? set_->lane[i % FORK_LANES] : main_; }
+  int end() {
+    if (!set_) return FFGB_OK;
+    for (int i = 0; i < FORK_LANES; ++i) {
+      FFGB_CUDA(cudaEventRecord(set_->done[i], set_->lane[i]));
+      FFGB_CUDA(cudaStreamWaitEvent(main_, set_->done[i], 0));
+    }
+    set_ = nullptr;
+    return FFGB_OK;
+  }
+
+ private:
+  cudaStream_t main_ = nullptr;
+  ForkSet* set_ = nullptr;
+};
+
 long long C(int n, int k) {
   if (k < 0 || n < 0 || k > n) return 0;
   long long r = 1;
@@ -91,6 +146,7 @@ void put_coefs(const double* v, int n, int mode, float* gp, float* gl, unsigned*
 struct CsClass {
   int m = 0, groups = 0;
   long long base = 0;
+  bool sub = false;  // a sub-pass class (ordered: sub-pass A before the B classes)
 };
 
 struct CsPass {
@@ -181,18 +237,19 @@ int cs_pass_tables(int norb, int nocc, int lo, int hh, const CsPass** out) {
   }
   CsPass P;
   std::vector<int> host;
-  auto add = [&](int m, int groups, const std::vector<int>& T) {
+  auto add = [&](int m, int groups, const std::vector<int>& T, bool sub) {
     if (groups == 0) return;
     CsClass c;
     c.m = m;
     c.groups = groups;
+    c.sub = sub;
     c.base = (long long)host.size();
     host.insert(host.end(), T.begin(), T.end());
     P.cls.push_back(c);
   };
-  for (int m = CS_MAX_M; m >= 1; --m) add(m, n_direct[m], direct[m]);
-  add(4, n_sub_a, sub_a[0]);
-  for (int m = 4; m >= 1; --m) add(m, n_sub_b[m], sub_b[m]);
+  for (int m = CS_MAX_M; m >= 1; --m) add(m, n_direct[m], direct[m], false);
+  add(4, n_sub_a, sub_a[0], true);
+  for (int m = 4; m >= 1; --m) add(m, n_sub_b[m], sub_b[m], true);
   const size_t bytes = std::max<size_t>(host.size(), 1) * sizeof(int);
   FFGB_CUDA(cudaMalloc(&P.tab, bytes));
   count_alloc();
@@ -234,8 +291,14 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int l
     v[3 * i + 2] = cs[i].g01.imag();
   }
   put_coefs(v, 3 * CS_MAX_SITES, mode, P.gp, P.gl, P.gt);
+  // direct classes round-robin over the fork's lanes; every sub-pass class on
+  // the last lane, in order
+  StageFork fork;
+  FFGB_TRY(fork.begin(st, (int)T->cls.size()));
+  int n_direct = 0;
   for (size_t c = 0; c < T->cls.size(); ++c) {
     const CsClass& k = T->cls[c];
+    const cudaStream_t ls = fork.lane(k.sub ? FORK_LANES - 1 : n_direct++);
     P.tab = T->tab + k.base;
     P.n_groups = k.groups;
     P.gpc = k.m >= 5 ? CS_MAX_GPC / 2 : CS_MAX_GPC;
@@ -245,16 +308,16 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int l
     if (grid <= 0) continue;
     if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
     switch (k.m) {
-      case 1: FFGB_TRY(launch_cs<1>(P, (int)grid, mode, st)); break;
-      case 2: FFGB_TRY(launch_cs<2>(P, (int)grid, mode, st)); break;
-      case 3: FFGB_TRY(launch_cs<3>(P, (int)grid, mode, st)); break;
-      case 4: FFGB_TRY(launch_cs<4>(P, (int)grid, mode, st)); break;
-      case 5: FFGB_TRY(launch_cs<5>(P, (int)grid, mode, st)); break;
-      case 6: FFGB_TRY(launch_cs<6>(P, (int)grid, mode, st)); break;
+      case 1: FFGB_TRY(launch_cs<1>(P, (int)grid, mode, ls)); break;
+      case 2: FFGB_TRY(launch_cs<2>(P, (int)grid, mode, ls)); break;
+      case 3: FFGB_TRY(launch_cs<3>(P, (int)grid, mode, ls)); break;
+      case 4: FFGB_TRY(launch_cs<4>(P, (int)grid, mode, ls)); break;
+      case 5: FFGB_TRY(launch_cs<5>(P, (int)grid, mode, ls)); break;
+      case 6: FFGB_TRY(launch_cs<6>(P, (int)grid, mode, ls)); break;
       default: return fail(FFGB_ERR_ARG, "bad cross-half class");
     }
   }
-  return FFGB_OK;
+  return fork.end();
 }
 
 template <int B, int K = 0>
@@ -421,6 +484,10 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
   std::stable_sort(jobs.begin(), jobs.end(), [](const Job& x, const Job& y) { return x.work > y.work; });
   long long pbase = 0;
   WinJob P;
+  // the jobs touch disjoint rows (and disjoint partial sums): forked over lanes
+  StageFork fork;
+  FFGB_TRY(fork.begin(st, (int)jobs.size()));
+  int lane = 0;
   for (const Job& jb : jobs) {
     std::memcpy(&P, base.get(), sizeof(WinJob));
     if (jb.a->off.size() > 72) return fail(FFGB_ERR_UNSUPPORTED, "window member table overflow");
@@ -445,9 +512,10 @@ int window_stage(const float2* in, float2* out, long long ld, long long ncols, i
       P.ex.partials = ex->partials + pbase;
     }
     int used = 0;
-    FFGB_TRY(launch_job_b(B, P, jb.a->k, jb.kind, low, epi, items, st, &used));
+    FFGB_TRY(launch_job_b(B, P, jb.a->k, jb.kind, low, epi, items, fork.lane(lane++), &used));
     pbase += used;
   }
+  FFGB_TRY(fork.end());
   if (ex_ctas) *ex_ctas = (int)pbase;
   return FFGB_OK;
 }

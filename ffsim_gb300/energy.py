@@ -88,6 +88,10 @@ class BatchLUCJEnergy:
         self.nbytes = _lib.load().ffgb_batch_scratch_bytes(0, self.code, norb, *self.nelec, max_states)
         self.buf = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
 
+    def close(self) -> None:
+        """Release the device buffers now."""
+        self.work = self.buf = None
+
     def __call__(self, ucjs: list[UCJOpSpinBalanced], ham: DoubleFactorizedHamiltonian,
                  control: _lib.Control | None = None) -> np.ndarray:
         """Energies of the operators; ``control`` (optional) can cancel the

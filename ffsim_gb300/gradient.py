@@ -310,6 +310,19 @@ class LUCJGradient:
             main.wait_stream(stream)
         return results
 
+    def close(self) -> None:
+        """Release the device buffers and the worker lanes now (instead of
+        when the object is collected)."""
+        if self._pool is not None:
+            self._pool.shutdown(wait=True)
+            self._pool = None
+        self._lanes = None
+        for name in ("_bcur", "_blam", "_bbuf"):
+            if hasattr(self, name):
+                delattr(self, name)
+        self._bcap = 0
+        self.cur = self.lam = self.buf = None
+
     def _ensure_batch(self, B: int) -> None:
         """Device buffers for B states (kept for later batches of at most B)."""
         if getattr(self, "_bcap", 0) >= B:

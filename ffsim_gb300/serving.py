@@ -12,7 +12,8 @@ batches of different keys overlap on the device.
 Admission is by device memory: an engine (the device buffers of one key's
 shape for ``capacity`` states) is taken idle from the pool or allocated within
 the HBM budget, releasing the least recently used idle engines of other shapes
-when needed; a batch shrinks to what fits.
+when needed (their memory is freed at once); an engine for a batch takes at
+most its worker's share of the budget, and a batch shrinks to what fits.
 
 Every request gets its own result: a value, or the error that stopped it
 (``ValueError`` for an invalid request, ``MemoryError`` when even one state
@@ -118,6 +119,12 @@ class _Engine:
             self.impl._ensure_batch(capacity)
         self.nbytes = engine_bytes(kind, norb, nelec, capacity, dtype)
 
+    def close(self) -> None:
+        """Release the device buffers now."""
+        if self.impl is not None:
+            self.impl.close()
+            self.impl = None
+
     def run(self, reqs: list[Request], control) -> list[tuple[float, np.ndarray | None]]:
         from ffsim_gb300.variational import UCJOpSpinBalanced
 
@@ -170,6 +177,9 @@ class LUCJServer:
             free, _ = torch.cuda.mem_get_info()
             budget_bytes = int(0.85 * free)
         self.budget = int(budget_bytes)
+        # an engine for a batch (more than one state) may take at most its
+        # worker's share of the budget, so that every worker can hold one
+        self.engine_limit = self.budget // max(1, workers)
         self.max_batch = max(1, int(max_batch))
         self.make_engine = make_engine or (lambda k, n, ne, c: _Engine(k, n, ne, c, self.dtype))
         self.size_of = size_of or (lambda k, n, ne, c: engine_bytes(k, n, ne, c, self.dtype))
@@ -265,12 +275,19 @@ class LUCJServer:
                 keep.append(req)
         self._pending = keep
 
+    @staticmethod
+    def _release(ev) -> None:
+        """An engine leaves the pool: free its device memory now."""
+        close = getattr(ev, "close", None)
+        if close is not None:
+            close()
+
     def _reserve(self, shape: tuple, cap: int) -> int:
         """Under the lock: bytes for a new engine of `shape` and capacity
         `cap`, releasing idle engines of other shapes (least recently used
         first) as needed; 0 if it does not fit."""
         need = self.size_of(shape[0], shape[1], shape[2], cap)
-        if need > self.budget:
+        if need > (self.engine_limit if cap > 1 else self.budget):
             return 0
         for oid, (s2, e2) in list(self._idle_order.items()):
             if self._in_use + need <= self.budget:
@@ -280,6 +297,7 @@ class LUCJServer:
             del self._idle_order[oid]
             self._idle[s2].remove(e2)
             self._in_use -= e2.nbytes
+            self._release(e2)
         if self._in_use + need > self.budget:
             return 0
         self._in_use += need
@@ -375,6 +393,8 @@ class LUCJServer:
                     self._idle_order[id(ev)] = (shape, ev)
                 else:  # never built, or failed: its memory is released
                     self._in_use -= reserved if ev is None or reserved else ev.nbytes
+                    if ev is not None:
+                        self._release(ev)
                     ev = None
                 for i, r in enumerate(group):
                     self._record(r, None if err is not None else values[i], err, len(group), start)

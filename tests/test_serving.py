@@ -26,8 +26,12 @@ class _FakeEngine:
         self.fail_rids = set(fail_rids)
         self.delay = delay
         self.batches = []
+        self.closed = False
         with _FakeEngine.lock:
             _FakeEngine.made.append(self)
+
+    def close(self):
+        self.closed = True
 
     def run(self, reqs, control):
         with _FakeEngine.lock:
@@ -110,6 +114,9 @@ def test_server_admits_by_memory_budget():
     srv.close()
     assert all(r.ok for r in res)
     assert _FakeEngine.peak == 1
+    # engines swapped out for other shapes were released at once
+    assert any(e.closed for e in _FakeEngine.made)
+    assert not any(e.closed for engines in srv._idle.values() for e in engines)
 
 
 def test_server_shrinks_a_batch_to_the_budget():
@@ -166,10 +173,12 @@ def test_failing_engine_fails_its_batch_only_and_is_not_reused():
     assert 3 in failed
     assert all(isinstance(res[i].error, RuntimeError) for i in failed)
     assert all(res[i].ok for i in res if i not in failed)
-    # the engine that raised was dropped: none of the idle pool's engines ran rid 3
+    # the engine that raised was dropped and released: none of the idle pool's
+    # engines ran rid 3
     for engines in srv._idle.values():
         for e in engines:
             assert all(3 not in b for b in e.batches)
+    assert all(e.closed for e in _FakeEngine.made if any(3 in b for b in e.batches))
 
 
 def test_cancel_pending_and_running():
