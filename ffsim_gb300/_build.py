@@ -53,7 +53,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
     nvcc = _nvcc()
     inc = ["-I", str(BUILD), "-I", str(CSRC)]
     flags = NVFLAGS + (extra_flags or [])
-    units = [("ffgb.cu", "ffgb.o", []), ("plan.cpp", "plan.o", []), ("stages.cu", "stages.o", []), ("grad.cu", "grad.o", []), ("peaks.cu", "peaks.o", [])] + [
+    units = [("ffgb.cu", "ffgb.o", []), ("plan.cpp", "plan.o", []), ("stages.cu", "stages.o", []), ("grad.cu", "grad.o", []), ("peaks.cu", "peaks.o", []), ("resident.cu", "resident.o", [])] + [
         (f"inst_{i}.cu", f"inst_{i}.o", []) for i in range(5)] + [
         ("stage_inst.cu", f"stage_b{b}_k{k0}.o", [f"-DWIN_B={b}", f"-DWIN_K0={k0}", f"-DWIN_K1={k1}"])
         for b, k0, k1 in STAGE_UNITS]

@@ -91,7 +91,18 @@ SIGNATURES = {
                           _c_void_p],
     "ffgb_vdot": [_c_void_p, _c_void_p, _c_int, _c_ll, _dp, _c_void_p],
     "ffgb_hartree_fock": [_c_void_p, _c_int, _c_ll, _c_void_p],
+    "ffgb_resident_open": [_c_int, _c_int, _c_double, ctypes.POINTER(_c_void_p)],
+    "ffgb_resident_hamiltonian": [_c_void_p, _c_int, _dp, _c_int, _dp, _dp, _c_double, _c_int, _ip],
+    "ffgb_resident_submit": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _dp, _dp, _dp,
+                             ctypes.POINTER(_c_ll)],
+    "ffgb_resident_poll": [_c_void_p, _c_ll, _dp],
+    "ffgb_resident_cancel": [_c_void_p, _c_ll],
+    "ffgb_resident_start": [_c_void_p],
+    "ffgb_resident_status": [_c_void_p, _ip, _ip],
+    "ffgb_resident_close": [_c_void_p],
 }
+
+FFGB_PENDING = 9
 
 class Control(ctypes.Structure):
     """``ffgb_control`` of a batch call: a cancellation flag that another

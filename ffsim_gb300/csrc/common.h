@@ -14,6 +14,10 @@ namespace ffgb {
 // Record an error message for ffgb_last_error() and return `code`.
 int fail(int code, const std::string& msg);
 
+// Message of the calling thread's last error (cleared at the start of every
+// entry point).
+extern thread_local std::string g_err;
+
 // Count one kernel launch (reported by ffgb_launch_count()).
 void count_launch();
 

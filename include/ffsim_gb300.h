@@ -43,7 +43,8 @@ typedef enum {
   FFGB_ERR_TIMEOUT = 5,     /* a batch passed its deadline (TimeoutError) */
   FFGB_ERR_UNSUPPORTED = 6, /* shape not supported (NotImplementedError) */
   FFGB_ERR_NUMERIC = 7,     /* host factorization failed (ArithmeticError) */
-  FFGB_ERR_CANCELLED = 8    /* a batch was cancelled through its control (CancelledError) */
+  FFGB_ERR_CANCELLED = 8,   /* a batch was cancelled through its control (CancelledError) */
+  FFGB_PENDING = 9          /* ffgb_resident_poll: the request has not finished yet (not an error) */
 } ffgb_status;
 
 /* Control of a long batch call (a NULL control pointer means none).
@@ -334,6 +335,53 @@ int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out,
 
 /* vec <- one-hot at address 0 (Hartree-Fock state, states/slater.py:122-138). */
 int ffgb_hartree_fock(void* vec, int dtype, long long n, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Resident evaluator: LUCJ energies of small shapes from a work queue.
+ *
+ * A persistent kernel (one CTA per request at a time, the state in shared
+ * memory) evaluates <psi|H|psi> for psi = the spin-balanced UCJ operator
+ * applied to Hartree-Fock (python/ffsim/variational/ucj_spin_balanced.py:657-696,
+ * states/slater.py:122-138) and H a double-factorized Hamiltonian
+ * (hamiltonians/double_factorized_hamiltonian.py:244-275), for norb <= 8, any
+ * nelec and n_reps <= 4, in complex64 with FP64 energies.  Requests of
+ * different shapes and Hamiltonians share one queue.  The queue lives in
+ * host-mapped memory: submit writes a request and publishes it, the kernel's
+ * CTAs claim requests in order, and poll reads the result.  A CTA that finds
+ * no work for idle_seconds exits; when all have, the kernel's status is
+ * FFGB_ERR_TIMEOUT and the next submit (or a poll of an unfinished request)
+ * launches it again.  The reference evaluates these energies one call at a
+ * time on the CPU; no counterpart in its interface. */
+typedef struct ffgb_resident ffgb_resident;
+
+/* Queue of n_slots requests served by n_ctas CTAs on a stream of its own
+ * (the calling thread's current device).  Allocates host-mapped memory and a
+ * small device block; launches nothing yet. */
+int ffgb_resident_open(int n_slots, int n_ctas, double idle_seconds, ffgb_resident** out);
+/* Register a double-factorized Hamiltonian (arguments as ffgb_df_expectation;
+ * norb <= 8); *ham_id names it in submit.  Synchronous copy to the device. */
+int ffgb_resident_hamiltonian(ffgb_resident* r, int norb, const double* one_body, int n_terms, const double* dcm,
+                              const double* rots, double constant, int zrep, int* ham_id);
+/* Queue the energy of one UCJ operator (arguments as ffgb_lucj_energy; from
+ * Hartree-Fock) under Hamiltonian ham_id; *ticket identifies the request.
+ * FFGB_ERR_OOM when the request's slot still holds an uncollected result. */
+int ffgb_resident_submit(ffgb_resident* r, int ham_id, int norb, int n_alpha, int n_beta, int n_reps,
+                         const double* ucj_dcm, const double* ucj_rots, const double* ucj_final, long long* ticket);
+/* FFGB_OK with *energy once the request has finished (its slot is then free
+ * again), FFGB_PENDING before, FFGB_ERR_CANCELLED if it was cancelled. */
+int ffgb_resident_poll(ffgb_resident* r, long long ticket, double* energy);
+/* Ask the kernel to stop a request: it checks between gates and terms. */
+int ffgb_resident_cancel(ffgb_resident* r, long long ticket);
+/* Launch the kernel now if it is not running (it otherwise starts with the
+ * first request). */
+int ffgb_resident_start(ffgb_resident* r);
+/* *running: whether the kernel is running; *kernel_status: FFGB_OK while it
+ * runs or after it was stopped, FFGB_ERR_TIMEOUT after it exited because no
+ * work came within idle_seconds. */
+int ffgb_resident_status(ffgb_resident* r, int* running, int* kernel_status);
+/* Stop the kernel (between requests), wait for it and free everything.
+ * Results not yet collected are lost. */
+int ffgb_resident_close(ffgb_resident* r);
 
 #ifdef __cplusplus
 }
