@@ -614,11 +614,69 @@ def run_serve(args) -> None:
         "requests": len(reqs), "completed": st["completed"], "gradients": n_grad,
         "arrival_rate_per_s": args.rate, "workers": args.workers, "max_batch": args.max_batch,
         "mean_batch": statistics.mean(srv.batch_sizes), "max_concurrent": srv.max_concurrent,
-        "span_s": st["span_s"],
+        "span_s": st["span_s"], "resident_served": srv.resident_served,
         "p50_ms_by_norb": {m: 1e3 * statistics.median(v) for m, v in sorted(by_norb.items())},
         "errors": errors,
         "dtype": "c64", "sample": f"{len(reqs)} requests of the stream (seed 2026)",
         "data": "synthetic"}), flush=True)
+
+
+def run_resident(args) -> None:
+    """Small-shape energies through the resident kernel against the batch
+    path: norb=--norb (default 8) at half filling, n_reps=2, one DF
+    Hamiltonian of rank 2*norb; --requests requests submitted at once, then
+    collected (evaluations per second from the first submission to the last
+    result, p50/p99 latency); the batch path evaluates the same operators in
+    batches of --max-batch (BatchLUCJEnergy), and one at a time (LUCJEnergy)."""
+    import numpy as np
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300.resident import ResidentEvaluator
+
+    norb = args.norb if args.norb != NORB else 8
+    nelec = (norb // 2, norb - norb // 2)
+    n = args.requests
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=2 * norb, seed=17)
+    ops = [f.random.random_ucj_op_spin_balanced(norb, n_reps=2, diag_coulomb_normal=True, diag_coulomb_scale=0.1,
+                                                seed=100 + i) for i in range(n)]
+    ev = ResidentEvaluator(n_slots=max(n, 16), n_ctas=args.resident_ctas, idle_seconds=2.0)
+    ev.energies(ops[:16], ham, nelec)  # plans, kernel launch and Hamiltonian upload outside the timing
+    t0 = time.perf_counter()
+    tickets = [(ev.submit(op, ham, nelec), time.perf_counter()) for op in ops]
+    lat, energies = [], []
+    for t, t_sub in tickets:
+        energies.append(ev.wait(t))
+        lat.append(time.perf_counter() - t_sub)
+    t1 = time.perf_counter()
+    ev.close()
+    res_rate = n / (t1 - t0)
+    batch = f.BatchLUCJEnergy(norb, nelec, args.max_batch)
+    batch(ops[: args.max_batch], ham)
+    torch.cuda.synchronize()
+    b0 = time.perf_counter()
+    eb = []
+    for i in range(0, n, args.max_batch):
+        eb.extend(batch(ops[i:i + args.max_batch], ham))
+    torch.cuda.synchronize()
+    b1 = time.perf_counter()
+    single = f.LUCJEnergy(norb, nelec)
+    m = min(n, 64)
+    s0 = time.perf_counter()
+    for op in ops[:m]:
+        single(op, ham)
+    torch.cuda.synchronize()
+    s1 = time.perf_counter()
+    e128 = [f.lucj_energy(op, ham, norb, nelec, dtype=torch.complex128) for op in ops[:8]]
+    print(json.dumps({
+        "metric": f"resident-kernel LUCJ energy evals/s, norb={norb} {nelec}, n_reps=2, DF rank {2 * norb}",
+        "value": res_rate, "unit": "evals/s", "requests": n, "ctas": args.resident_ctas,
+        "p50_ms": 1e3 * float(np.median(lat)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+        "batch_path_evals_per_s": n / (b1 - b0), "batch_states": args.max_batch,
+        "single_path_evals_per_s": m / (s1 - s0),
+        "max_abs_dE_vs_c128": float(max(abs(a - b) for a, b in zip(energies[:8], e128))),
+        "max_abs_dE_vs_batch_c64": float(np.max(np.abs(np.array(energies) - np.array(eb)))),
+        "dtype": "c64", "data": "synthetic"}), flush=True)
 
 
 def time_served(ucj_seed: int, n_requests: int, workers: int, max_batch: int) -> dict:
@@ -754,6 +812,9 @@ def main():
     ap.add_argument("--grad", action="store_true", help="gradient workload (norb=12, batch of parameters)")
     ap.add_argument("--batch", type=int, default=64, help="--grad: parameter vectors")
     ap.add_argument("--serve", action="store_true", help="serving workload (mixed requests, Poisson arrivals)")
+    ap.add_argument("--resident", action="store_true",
+                    help="small-shape energies through the resident kernel (--norb, --requests, --max-batch)")
+    ap.add_argument("--resident-ctas", type=int, default=8, help="--resident: CTAs of the resident kernel")
     ap.add_argument("--requests", type=int, default=300, help="--serve: requests")
     ap.add_argument("--rate", type=float, default=4.0, help="--serve: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=2, help="--serve: batches in flight")
@@ -770,6 +831,9 @@ def main():
         return
     if args.grad:
         run_grad(args)
+        return
+    if args.resident:
+        run_resident(args)
         return
     if args.serve:
         run_serve(args)

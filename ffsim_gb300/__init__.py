@@ -31,6 +31,7 @@ from ffsim_gb300.bitstring import (
     strings_to_addresses,
 )
 from ffsim_gb300.energy import BatchLUCJEnergy, LUCJEnergy, lucj_energies, lucj_energy
+from ffsim_gb300.resident import ResidentEvaluator
 from ffsim_gb300.gradient import LUCJGradient, lucj_energy_autograd
 from ffsim_gb300.gates import (
     apply_diag_coulomb_evolution,
@@ -89,6 +90,7 @@ __all__ = [
     "NumNumAnsatzOpSpinBalanced",
     "LUCJEnergy",
     "BatchLUCJEnergy",
+    "ResidentEvaluator",
     "LinearOperator",
     "MolecularHamiltonian",
     "UCJAnglesOpSpinBalanced",

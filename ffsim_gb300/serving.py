@@ -23,9 +23,18 @@ engine whose call raised (other than a cancellation) is not reused.  A batch
 whose requests are all cancelled stops within about two Hamiltonian terms
 (``ffgb_control``).
 
+Energy requests of small shapes (norb <= 8, n_reps <= 4) go instead to a
+resident evaluator (``resident.ResidentEvaluator``): one persistent kernel
+that takes them from a queue in host-mapped memory and evaluates each inside
+one CTA, next to the batches on the device.  A resident lane thread submits
+them in arrival order while the queue has room and collects the results;
+cancellation and deadlines apply to them as to the others.  A request the
+resident kernel cannot plan falls back to the batch path.
+
 Results do not depend on what else runs: a state's result is the same alone
 and in any batch (the dithering of a state's coefficients and the order of
-its reductions do not depend on its neighbours).
+its reductions do not depend on its neighbours), and a resident request's
+result is the same alone and in any queue.
 """
 
 from __future__ import annotations
@@ -69,6 +78,7 @@ class Result:
     end: float
     error: BaseException | None = None
     batch: int = 0  # size of the batch it ran in (0: it did not run)
+    path: str = "batch"  # "batch" or "resident"
 
     @property
     def ok(self) -> bool:
@@ -166,10 +176,14 @@ class LUCJServer:
     make_engine(kind, norb, nelec, capacity) / size_of(kind, norb, nelec,
     capacity): injection points (the defaults build GPU engines); tests
     substitute host-only fakes.
+    resident: route small energy requests to a resident evaluator (default:
+    when the engines are the GPU ones and the dtype is complex64);
+    make_resident() builds it (injection point, like make_engine).
     """
 
     def __init__(self, workers: int = 2, *, max_batch: int = 64, dtype=None, budget_bytes: int | None = None,
-                 make_engine: Callable | None = None, size_of: Callable | None = None, use_streams: bool = True):
+                 make_engine: Callable | None = None, size_of: Callable | None = None, use_streams: bool = True,
+                 resident: bool | None = None, make_resident: Callable | None = None):
         import torch
 
         self.dtype = dtype if dtype is not None else torch.complex64
@@ -196,7 +210,17 @@ class LUCJServer:
         self.max_concurrent = 0
         self.batch_sizes: list[int] = []
         self._n_running = 0
+        if resident is None:
+            resident = make_resident is not None or (make_engine is None and self.dtype == torch.complex64)
+        self.resident = bool(resident)
+        self._make_resident = make_resident or (lambda: _default_resident())
+        self._res_pending: collections.deque[Request] = collections.deque()
+        self._res_inflight: dict[int, tuple[Request, float]] = {}  # ticket -> (request, start)
+        self._res_ticket: dict[int, int] = {}  # rid -> ticket
+        self.resident_served = 0
         self._threads = [threading.Thread(target=self._worker, daemon=True) for _ in range(workers)]
+        if self.resident:
+            self._threads.append(threading.Thread(target=self._resident_lane, daemon=True))
         for t in self._threads:
             t.start()
 
@@ -211,8 +235,16 @@ class LUCJServer:
             self._finish_one(req, None, exc, 0, time.perf_counter())
             return
         with self._cv:
-            self._pending.append(req)
+            if self._for_resident(req):
+                self._res_pending.append(req)
+            else:
+                self._pending.append(req)
             self._cv.notify_all()
+
+    def _for_resident(self, req: Request) -> bool:
+        from ffsim_gb300 import resident as res
+
+        return self.resident and req.kind == "energy" and res.accepts(req.norb, req.n_reps)
 
     def cancel(self, rid: int) -> bool:
         """Cancel a request: a pending one is dropped at once, a running one
@@ -221,12 +253,15 @@ class LUCJServer:
         with self._cv:
             if rid in self._results:
                 return False
-            for i, req in enumerate(self._pending):
-                if req.rid == rid:
-                    del self._pending[i]
-                    self._record(req, None, CancelledError(f"request {rid} was cancelled"), 0, time.perf_counter())
-                    return True
+            for queue in (self._pending, self._res_pending):
+                for i, req in enumerate(queue):
+                    if req.rid == rid:
+                        del queue[i]
+                        self._record(req, None, CancelledError(f"request {rid} was cancelled"), 0,
+                                     time.perf_counter())
+                        return True
             self._cancelled.add(rid)
+            self._cv.notify_all()
             if rid in self._running:
                 batch, control = self._running[rid]
                 if control is not None and all(r.rid in self._cancelled for r in batch):
@@ -253,12 +288,13 @@ class LUCJServer:
             t.join(timeout=60)
 
     # -- scheduling -----------------------------------------------------------
-    def _record(self, req: Request, value, error, batch: int, start: float) -> None:
+    def _record(self, req: Request, value, error, batch: int, start: float, path: str = "batch") -> None:
         """Under the lock: the result of one request."""
         energy, grad = value if value is not None else (None, None)
         if req.rid in self._cancelled and error is None:
             error = CancelledError(f"request {req.rid} was cancelled")
-        self._results[req.rid] = Result(req.rid, energy, grad, req.arrival, start, time.perf_counter(), error, batch)
+        self._results[req.rid] = Result(req.rid, energy, grad, req.arrival, start, time.perf_counter(), error, batch,
+                                        path)
         self._cv.notify_all()
 
     def _finish_one(self, req, value, error, batch, start) -> None:
@@ -267,13 +303,16 @@ class LUCJServer:
 
     def _expire(self, now: float) -> None:
         """Under the lock: pending requests past their deadline."""
+        self._pending = self._expired(self._pending, now)
+
+    def _expired(self, queue, now: float):
         keep = collections.deque()
-        for req in self._pending:
+        for req in queue:
             if req.deadline is not None and now > req.arrival + req.deadline:
                 self._record(req, None, TimeoutError(f"request {req.rid} waited past its deadline"), 0, now)
             else:
                 keep.append(req)
-        self._pending = keep
+        return keep
 
     @staticmethod
     def _release(ev) -> None:
@@ -398,6 +437,82 @@ class LUCJServer:
                     ev = None
                 for i, r in enumerate(group):
                     self._record(r, None if err is not None else values[i], err, len(group), start)
+
+    def _resident_lane(self) -> None:
+        """Feeds the resident evaluator in arrival order while its queue has
+        room, forwards cancellations, and collects the results."""
+        from ffsim_gb300.variational import UCJOpSpinBalanced
+
+        ev = None
+        try:
+            while True:
+                with self._cv:
+                    if self._stop:
+                        return
+                    self._res_pending = self._expired(self._res_pending, time.perf_counter())
+                    if not self._res_pending and not self._res_inflight:
+                        self._cv.wait(timeout=0.5)
+                        continue
+                    # taken out of the pending queue under the lock: a cancel()
+                    # from now on finds them through self._cancelled
+                    todo = list(self._res_pending)
+                    self._res_pending.clear()
+                    cancel = [t for rid, t in self._res_ticket.items() if rid in self._cancelled]
+                if ev is None:
+                    ev = self._make_resident()
+                for t in cancel:
+                    ev.cancel(t)
+                for i, req in enumerate(todo):
+                    start = time.perf_counter()
+                    try:
+                        op = UCJOpSpinBalanced.from_parameters(req.params, norb=req.norb, n_reps=req.n_reps)
+                        ticket = ev.submit(op, req.ham, req.nelec)
+                    except MemoryError:
+                        with self._cv:  # the queue is full: the rest wait for collected results
+                            self._res_pending.extendleft(reversed(todo[i:]))
+                        break
+                    except NotImplementedError:
+                        with self._cv:  # the resident kernel cannot plan it: the batch path takes it
+                            self._pending.append(req)
+                            self._cv.notify_all()
+                        continue
+                    except BaseException as exc:  # noqa: BLE001
+                        with self._cv:
+                            self._record(req, None, exc, 0, start, "resident")
+                        continue
+                    with self._cv:
+                        self._res_inflight[ticket] = (req, start)
+                        self._res_ticket[req.rid] = ticket
+                        cancelled = req.rid in self._cancelled
+                    if cancelled:
+                        ev.cancel(ticket)
+                done = []
+                for ticket, (req, start) in list(self._res_inflight.items()):
+                    try:
+                        e = ev.poll(ticket)
+                    except BaseException as exc:  # noqa: BLE001
+                        done.append((ticket, req, start, None, exc))
+                        continue
+                    if e is not None:
+                        done.append((ticket, req, start, (e, None), None))
+                if done:
+                    with self._cv:
+                        for ticket, req, start, value, err in done:
+                            del self._res_inflight[ticket]
+                            self._res_ticket.pop(req.rid, None)
+                            self._record(req, value, err, 1, start, "resident")
+                            self.resident_served += err is None
+                else:
+                    time.sleep(50e-6)
+        finally:
+            if ev is not None:
+                ev.close()
+
+
+def _default_resident():
+    from ffsim_gb300.resident import ResidentEvaluator
+
+    return ResidentEvaluator(n_slots=1024, n_ctas=8, idle_seconds=1.0)
 
 
 def latency_stats(results: list[Result]) -> dict:

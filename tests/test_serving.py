@@ -71,12 +71,59 @@ def _reqs(n, norbs=(8, 10, 12), seed=0, n_reps=1):
     return out
 
 
-def _server(workers=3, budget=10**9, max_batch=64, **kw):
+def _server(workers=3, budget=10**9, max_batch=64, resident=None, **kw):
     from ffsim_gb300.serving import LUCJServer
 
     return LUCJServer(workers=workers, budget_bytes=budget, max_batch=max_batch,
                       make_engine=lambda k, n, ne, c: _FakeEngine(k, n, ne, c, **kw),
-                      size_of=lambda k, n, ne, c: n * 100 * c, use_streams=False)
+                      size_of=lambda k, n, ne, c: n * 100 * c, use_streams=False,
+                      make_resident=(lambda: resident) if resident is not None else None)
+
+
+class _FakeResident:
+    """Host-only resident evaluator: `cap` requests in flight, each done
+    `delay` s after submission with energy norb + 0.5; tickets of cancelled
+    requests end with CancelledError; unplannable norbs raise
+    NotImplementedError at submission."""
+
+    def __init__(self, cap=1000, delay=0.005, unplannable=()):
+        self.cap, self.delay, self.unplannable = cap, delay, set(unplannable)
+        self.inflight = {}
+        self.next = 0
+        self.cancelled = set()
+        self.peak = 0
+        self.closed = False
+        self.lock = threading.Lock()
+
+    def submit(self, op, ham, nelec):
+        with self.lock:
+            if op.norb in self.unplannable:
+                raise NotImplementedError("no plan")
+            if len(self.inflight) >= self.cap:
+                raise MemoryError("queue full")
+            t = self.next
+            self.next += 1
+            self.inflight[t] = (op.norb, time.perf_counter() + self.delay)
+            self.peak = max(self.peak, len(self.inflight))
+            return t
+
+    def poll(self, ticket):
+        with self.lock:
+            norb, t_done = self.inflight[ticket]
+            if ticket in self.cancelled:
+                del self.inflight[ticket]
+                raise CancelledError("cancelled")
+            if time.perf_counter() < t_done:
+                return None
+            del self.inflight[ticket]
+            return norb + 0.5
+
+    def cancel(self, ticket):
+        with self.lock:
+            self.cancelled.add(ticket)
+
+    def close(self):
+        self.closed = True
 
 
 def test_server_batches_overlaps_and_returns_every_result():
@@ -222,6 +269,91 @@ def test_deadline_while_pending():
     assert isinstance(res[1].error, TimeoutError)
 
 
+def _mixed(n, seed=0):
+    """Energy requests of norb 6, 8 (resident) and 10 (batch), and norb-8
+    gradients (batch)."""
+    from ffsim_gb300.serving import Request
+    from ffsim_gb300.variational import UCJOpSpinBalanced
+
+    rng = np.random.default_rng(seed)
+    hams = {m: object() for m in (6, 8, 10)}
+    out = []
+    for i in range(n):
+        m = int(rng.choice((6, 8, 10)))
+        kind = "gradient" if m == 8 and rng.random() < 0.3 else "energy"
+        out.append(Request(i, kind, m, (m // 2, m // 2), 1, np.zeros(UCJOpSpinBalanced.n_params(m, 1)), hams[m]))
+    return out
+
+
+def _is_resident(req):
+    return req.kind == "energy" and req.norb <= 8
+
+
+def test_resident_lane_takes_small_energy_requests():
+    _reset()
+    fake = _FakeResident()
+    srv = _server(resident=fake)
+    reqs = _mixed(60)
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(len(reqs), timeout=60)
+    srv.close()
+    assert all(r.ok for r in res)
+    for req, r in zip(reqs, res):
+        if _is_resident(req):
+            assert r.path == "resident" and r.energy == req.norb + 0.5
+        else:
+            assert r.path == "batch" and r.energy == req.rid * 0.5
+    assert srv.resident_served == sum(_is_resident(q) for q in reqs)
+    assert fake.closed
+
+
+def test_resident_queue_full_waits_for_room():
+    _reset()
+    fake = _FakeResident(cap=3, delay=0.01)
+    srv = _server(resident=fake)
+    reqs = [r for r in _mixed(80, seed=1) if _is_resident(r)]
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(len(reqs), timeout=60)
+    srv.close()
+    assert all(r.ok and r.path == "resident" for r in res)
+    assert fake.peak <= 3
+
+
+def test_resident_cancel_and_unplannable_fallback():
+    _reset()
+    fake = _FakeResident(delay=0.5, unplannable={6})
+    srv = _server(resident=fake)
+    reqs = [r for r in _mixed(40, seed=2) if _is_resident(r)]
+    eight = [r for r in reqs if r.norb == 8]
+    six = [r for r in reqs if r.norb == 6]
+    for r in reqs:
+        srv.submit(r)
+    time.sleep(0.1)
+    assert srv.cancel(eight[0].rid)
+    res = {r.rid: r for r in srv.drain(len(reqs), timeout=60)}
+    srv.close()
+    assert isinstance(res[eight[0].rid].error, CancelledError)
+    assert all(res[r.rid].ok and res[r.rid].path == "resident" for r in eight[1:])
+    # the resident kernel could not plan them: served by the batch path
+    assert all(res[r.rid].ok and res[r.rid].path == "batch" and res[r.rid].energy == r.rid * 0.5 for r in six)
+
+
+def test_resident_deadline_while_pending():
+    _reset()
+    fake = _FakeResident(cap=1, delay=0.3)
+    srv = _server(resident=fake)
+    reqs = [r for r in _mixed(30, seed=4) if _is_resident(r)][:3]
+    reqs[2].deadline = 0.05
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(len(reqs), timeout=60)
+    srv.close()
+    assert res[0].ok and res[1].ok
+    assert isinstance(res[2].error, TimeoutError)
+
+
 @pytest.mark.gpu
 def test_results_alone_and_in_the_mix(cuda):
     """Each request's result through the server equals the same request run
@@ -232,16 +364,26 @@ def test_results_alone_and_in_the_mix(cuda):
 
     offsets, reqs = synthetic_stream(24, rate=400.0, seed=3, norbs=(8, 10, 12), reps=(1, 2),
                                      gradient_fraction=0.3)
+    from ffsim_gb300.resident import ResidentEvaluator, accepts
+    from ffsim_gb300.variational import UCJOpSpinBalanced
+
     alone = {}
+    ev = ResidentEvaluator(n_slots=8, n_ctas=1)
     for r in reqs:
+        if r.kind == "energy" and accepts(r.norb, r.n_reps):  # served by the resident kernel
+            op = UCJOpSpinBalanced.from_parameters(r.params, norb=r.norb, n_reps=r.n_reps)
+            alone[r.rid] = (ev.wait(ev.submit(op, r.ham, r.nelec)), None)
+            continue
         eng = _Engine(r.kind, r.norb, r.nelec, 1, torch.complex64)
         alone[r.rid] = eng.run([r], None)[0]
         del eng
+    ev.close()
     srv = LUCJServer(workers=2)
     res = replay(srv, offsets, reqs)
     srv.close()
     assert all(r.ok for r in res)
     assert max(srv.batch_sizes) > 1
+    assert srv.resident_served == sum(r.kind == "energy" and r.norb <= 8 for r in reqs) > 0
     for r in res:
         e, g = alone[r.rid]
         assert abs(r.energy - e) <= 1e-9, (r.rid, r.energy, e)
