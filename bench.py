@@ -594,7 +594,7 @@ def run_serve(args) -> None:
     del warm
     torch.cuda.empty_cache()
     torch.cuda.synchronize()
-    srv = LUCJServer(workers=args.workers, max_batch=args.max_batch)
+    srv = LUCJServer(workers=args.workers, max_batch=args.max_batch, resident=not args.no_resident)
     res = replay(srv, offsets, reqs)
     srv.close()
     st = latency_stats(res)
@@ -613,6 +613,7 @@ def run_serve(args) -> None:
         "value": st["evals_per_s"], "unit": "evals/s", "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
         "requests": len(reqs), "completed": st["completed"], "gradients": n_grad,
         "arrival_rate_per_s": args.rate, "workers": args.workers, "max_batch": args.max_batch,
+        "resident": not args.no_resident,
         "mean_batch": statistics.mean(srv.batch_sizes), "max_concurrent": srv.max_concurrent,
         "span_s": st["span_s"], "resident_served": srv.resident_served,
         "p50_ms_by_norb": {m: 1e3 * statistics.median(v) for m, v in sorted(by_norb.items())},
@@ -815,6 +816,8 @@ def main():
     ap.add_argument("--resident", action="store_true",
                     help="small-shape energies through the resident kernel (--norb, --requests, --max-batch)")
     ap.add_argument("--resident-ctas", type=int, default=8, help="--resident: CTAs of the resident kernel")
+    ap.add_argument("--no-resident", action="store_true",
+                    help="--serve: every request through the batch path (no resident kernel)")
     ap.add_argument("--requests", type=int, default=300, help="--serve: requests")
     ap.add_argument("--rate", type=float, default=4.0, help="--serve: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=2, help="--serve: batches in flight")

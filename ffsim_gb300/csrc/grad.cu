@@ -333,18 +333,36 @@ __global__ void __launch_bounds__(PAIR_THREADS) pair_density_kernel(const typena
   }
 }
 
-// out[k] = sum over c < chunks of partial[c * per + k], in order of c.
-__global__ void __launch_bounds__(256) sum_blocks_kernel(const double2* __restrict__ partial, long long chunks,
-                                                         int per, double2* __restrict__ out) {
-  const int k = blockIdx.x * 256 + threadIdx.x;
-  if (k >= per) return;
+// out[k] = sum over c < chunks of partial[c * per + k] in a fixed order: a
+// CTA takes 32 consecutive k (coalesced 512-byte rows) and 32 interleaved
+// subsets of c (c = g, g + 32, ...), each summed in order of c, then the 32
+// subset sums in order of g.
+constexpr int SUMB_K = 32, SUMB_G = 32;
+__global__ void __launch_bounds__(SUMB_K * SUMB_G) sum_blocks_kernel(const double2* __restrict__ partial,
+                                                                     long long chunks, int per,
+                                                                     double2* __restrict__ out) {
+  __shared__ double2 sh[SUMB_G][SUMB_K + 1];
+  const int kl = threadIdx.x % SUMB_K, g = threadIdx.x / SUMB_K;
+  const int k = blockIdx.x * SUMB_K + kl;
   double2 a = make_double2(0.0, 0.0);
-  for (long long c = 0; c < chunks; ++c) {
-    const double2 v = partial[c * per + k];
-    a.x += v.x;
-    a.y += v.y;
+  if (k < per) {
+#pragma unroll 4
+    for (long long c = g; c < chunks; c += SUMB_G) {
+      const double2 v = partial[c * per + k];
+      a.x += v.x;
+      a.y += v.y;
+    }
   }
-  out[k] = a;
+  sh[g][kl] = a;
+  __syncthreads();
+  if (g == 0 && k < per) {
+    double2 t = sh[0][kl];
+    for (int j = 1; j < SUMB_G; ++j) {
+      t.x += sh[j][kl].x;
+      t.y += sh[j][kl].y;
+    }
+    out[k] = t;
+  }
 }
 
 }  // namespace
@@ -426,7 +444,7 @@ int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned
                                                                     rows, cols, norb, part);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
-  sum_blocks_kernel<<<(per + 255) / 256, 256, 0, st>>>(part, chunks, per, sums);
+  sum_blocks_kernel<<<(per + SUMB_K - 1) / SUMB_K, SUMB_K * SUMB_G, 0, st>>>(part, chunks, per, sums);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   std::vector<double> h(2 * (size_t)per, 0.0);

@@ -503,7 +503,7 @@ class LUCJServer:
                             self._record(req, value, err, 1, start, "resident")
                             self.resident_served += err is None
                 else:
-                    time.sleep(50e-6)
+                    time.sleep(200e-6)
         finally:
             if ev is not None:
                 ev.close()
@@ -512,7 +512,9 @@ class LUCJServer:
 def _default_resident():
     from ffsim_gb300.resident import ResidentEvaluator
 
-    return ResidentEvaluator(n_slots=1024, n_ctas=8, idle_seconds=1.0)
+    # the kernel lives only while requests come (it exits 5 ms after the
+    # last), so between bursts it holds no SM resources the batches could use
+    return ResidentEvaluator(n_slots=1024, n_ctas=8, idle_seconds=0.005)
 
 
 def latency_stats(results: list[Result]) -> dict:
