@@ -536,7 +536,7 @@ def run_grad(args) -> None:
                                                 diag_coulomb_scale=0.1, seed=2026).to_parameters()
     batch = base[None, :] + 0.05 * rng.normal(size=(B, n))
     ham = f.random.random_df_hamiltonian_normal(norb, rank=R, seed=2027)
-    ev = LUCJGradient(norb, nelec, dtype=torch.complex64)
+    ev = LUCJGradient(norb, nelec, dtype=torch.complex64, workers=args.grad_workers)
     for row in batch[:2]:
         ev.value_and_grad(row, L, ham)
     torch.cuda.synchronize()
@@ -567,7 +567,7 @@ def run_grad(args) -> None:
     rel = abs(gb[0] @ d - fd) / abs(fd)
     print(json.dumps({
         "metric": "LUCJ energy+gradient evals/s norb=12 (6,6) n_reps=3 rank 24 (complex64, FP64 reductions)",
-        "value": B / t_batch, "unit": "evals/s", "batch": B, "n_params": n, "dtype": "c64",
+        "value": B / t_batch, "unit": "evals/s", "batch": B, "lanes": args.grad_workers, "n_params": n, "dtype": "c64",
         "ms_per_batch": 1e3 * t_batch, "sequential_evals_per_s": B / t_seq,
         "max_abs_diff_batched_vs_sequential": same,
         "fd_check": {"h": h, "directional_rel_err": rel, "bar": 1e-4},
@@ -613,7 +613,8 @@ def run_serve(args) -> None:
         "value": st["evals_per_s"], "unit": "evals/s", "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
         "requests": len(reqs), "completed": st["completed"], "gradients": n_grad,
         "arrival_rate_per_s": args.rate, "workers": args.workers, "max_batch": args.max_batch,
-        "resident": not args.no_resident,
+        "resident": not args.no_resident, "oom_retries": srv.oom_retries,
+        "allocator": os.environ.get("PYTORCH_CUDA_ALLOC_CONF", ""),
         "mean_batch": statistics.mean(srv.batch_sizes), "max_concurrent": srv.max_concurrent,
         "span_s": st["span_s"], "resident_served": srv.resident_served,
         "p50_ms_by_norb": {m: 1e3 * statistics.median(v) for m, v in sorted(by_norb.items())},
@@ -812,6 +813,7 @@ def main():
                     help="two single evaluations at --norb, untimed (for a profiler's launch list)")
     ap.add_argument("--grad", action="store_true", help="gradient workload (norb=12, batch of parameters)")
     ap.add_argument("--batch", type=int, default=64, help="--grad: parameter vectors")
+    ap.add_argument("--grad-workers", type=int, default=4, help="--grad: host lanes (streams) of a batch")
     ap.add_argument("--serve", action="store_true", help="serving workload (mixed requests, Poisson arrivals)")
     ap.add_argument("--resident", action="store_true",
                     help="small-shape energies through the resident kernel (--norb, --requests, --max-batch)")
@@ -826,6 +828,11 @@ def main():
     ap.add_argument("--batch-states", type=int, default=4, help="evaluations per step (one batch)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.serve and "PYTORCH_CUDA_ALLOC_CONF" not in os.environ:
+        # engines of many shapes come and go: expandable segments let the
+        # caching allocator return a released engine's pages to the device
+        # instead of keeping partly used segments
+        os.environ["PYTORCH_CUDA_ALLOC_CONF"] = "expandable_segments:True"
     if args.ops:
         run_ops(args)
         return

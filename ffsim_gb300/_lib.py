@@ -89,6 +89,8 @@ SIGNATURES = {
                              _c_void_p],
     "ffgb_pair_density": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _dp, _c_void_p, _c_size_t,
                           _c_void_p],
+    "ffgb_gate_densities": [_c_void_p, _c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _c_void_p, _c_void_p,
+                            _c_size_t, _c_void_p],
     "ffgb_vdot": [_c_void_p, _c_void_p, _c_int, _c_ll, _dp, _c_void_p],
     "ffgb_hartree_fock": [_c_void_p, _c_int, _c_ll, _c_void_p],
     "ffgb_resident_open": [_c_int, _c_int, _c_double, ctypes.POINTER(_c_void_p)],

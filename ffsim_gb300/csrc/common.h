@@ -96,6 +96,15 @@ template <typename T>
 int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
               int norb, void* partial_buf, size_t partial_bytes, std::vector<double>& rr, std::vector<double>& rc,
               cudaStream_t st);
+// The same into device memory, without synchronizing: g_dev gets norb * norb
+// complex values, sums_dev 2 * norb * norb (row-row, then row-column).
+template <typename T>
+int rdm1_rows_dev(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
+                  void* partial_buf, size_t partial_bytes, double2* g_dev, cudaStream_t st, int nocc,
+                  const unsigned* sub, int n_sub);
+template <typename T>
+int pair_rows_dev(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
+                  int norb, void* partial_buf, size_t partial_bytes, double2* sums_dev, cudaStream_t st);
 size_t density_partial_bytes(int norb, long long rows);
 size_t density_sub_bytes(int norb, long long n_sub, int nv);
 template <typename T>

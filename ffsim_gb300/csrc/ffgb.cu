@@ -748,14 +748,26 @@ static int rotate_both(void* vec, void* tmp, int norb, int na, int nb, const Sec
   return run_pass<T>(B, scr, st);
 }
 
+// Plans of both sectors' rotations; a spin-balanced rotation (the same
+// matrix for both) is planned once.
+template <typename T>
+static int plan_pair(int norb, const double* ma, const double* mb, SectorPlan& pa, SectorPlan& pb) {
+  if (ma) FFGB_TRY(make_plan<T>(norb, load_mat(ma, norb), pa));
+  if (!mb) return FFGB_OK;
+  if (ma && (ma == mb || std::memcmp(ma, mb, sizeof(double) * 2 * (size_t)norb * norb) == 0)) {
+    pb = pa;
+    return FFGB_OK;
+  }
+  return make_plan<T>(norb, load_mat(mb, norb), pb);
+}
+
 template <typename T>
 static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const double* ma,
                                  const double* mb, Scratch& scr, cudaStream_t st) {
   using C = typename CT<T>::type;
   if (big_rows<T>(norb, na, nb)) {
     SectorPlan pa, pb;
-    if (ma) FFGB_TRY(make_plan<T>(norb, load_mat(ma, norb), pa));
-    if (mb && nb >= 0) FFGB_TRY(make_plan<T>(norb, load_mat(mb, norb), pb));
+    FFGB_TRY(plan_pair<T>(norb, ma, nb >= 0 ? mb : nullptr, pa, pb));
     return big_rotate<T>(vec, norb, na, nb, ma ? &pa : nullptr, mb && nb >= 0 ? &pb : nullptr, true, scr, st);
   }
   if (nb < 0) {  // spinless
@@ -774,8 +786,7 @@ static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const doub
     return run_pass<T>(A, scr, st);
   }
   SectorPlan pa, pb;
-  if (ma) FFGB_TRY(make_plan<T>(norb, load_mat(ma, norb), pa));
-  if (mb) FFGB_TRY(make_plan<T>(norb, load_mat(mb, norb), pb));
+  FFGB_TRY(plan_pair<T>(norb, ma, mb, pa, pb));
   if (!ma && !mb) return FFGB_OK;
   if (!ma) {  // beta only: rows are alpha strings, in place
     if (sizeof(T) == 4 && ops_only(pb)) {
@@ -802,6 +813,27 @@ static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const doub
   return rotate_both<T>(vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, nullptr, scr, st);
 }
 
+// Plans of U^dag and U for both sectors (rotations conjugating a diagonal
+// operator); the same matrix for both sectors is planned once.
+template <typename T>
+static int plan_conj_pair(int norb, const double* rot_a, const double* rot_b, SectorPlan& pad, SectorPlan& pau,
+                          SectorPlan& pbd, SectorPlan& pbu) {
+  if (rot_a) {
+    auto U = load_mat(rot_a, norb);
+    FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pad));
+    FFGB_TRY(make_plan<T>(norb, U, pau));
+  }
+  if (!rot_b) return FFGB_OK;
+  if (rot_a && (rot_a == rot_b || std::memcmp(rot_a, rot_b, sizeof(double) * 2 * (size_t)norb * norb) == 0)) {
+    pbd = pad;
+    pbu = pau;
+    return FFGB_OK;
+  }
+  auto U = load_mat(rot_b, norb);
+  FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pbd));
+  return make_plan<T>(norb, U, pbu);
+}
+
 // W(U) D W(U)^dag vec with D a diagonal phase operator (evolution)
 template <typename T>
 static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSpec& spec,
@@ -811,16 +843,7 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
   if (big_rows<T>(norb, na, nb)) {
     const bool rb = rot_b && nb >= 0;
     SectorPlan pad, pbd, pau, pbu;
-    if (rot_a) {
-      auto U = load_mat(rot_a, norb);
-      FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pad));
-      FFGB_TRY(make_plan<T>(norb, U, pau));
-    }
-    if (rb) {
-      auto U = load_mat(rot_b, norb);
-      FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pbd));
-      FFGB_TRY(make_plan<T>(norb, U, pbu));
-    }
+    FFGB_TRY(plan_conj_pair<T>(norb, rot_a, rb ? rot_b : nullptr, pad, pau, pbd, pbu));
     FFGB_TRY(big_rotate<T>(vec, norb, na, nb, rot_a ? &pad : nullptr, rb ? &pbd : nullptr, true, scr, st));
     if (nb < 0) {  // spinless: one row whose columns are the strings
       DiagSpec d = spec;
@@ -871,16 +894,7 @@ static int diag_evolution_impl(void* vec, int norb, int na, int nb, const DiagSp
   const long long da = binom_h(norb, na);
   if (!rot_a && !rot_b) return diag_rows<T>(vec, vec, norb, na, nb, spec, false, scr, st);
   SectorPlan pad, pbd, pau, pbu;
-  if (rot_a) {
-    auto U = load_mat(rot_a, norb);
-    FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pad));
-    FFGB_TRY(make_plan<T>(norb, U, pau));
-  }
-  if (rot_b) {
-    auto U = load_mat(rot_b, norb);
-    FFGB_TRY(make_plan<T>(norb, dagger(U, norb), pbd));
-    FFGB_TRY(make_plan<T>(norb, U, pbu));
-  }
+  FFGB_TRY(plan_conj_pair<T>(norb, rot_a, rot_b, pad, pau, pbd, pbu));
   const size_t S = (size_t)da * binom_h(norb, nb) * sizeof(C);
   void* tmp = scr.take(S);
   if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
@@ -1645,6 +1659,43 @@ static int densities(const void* x, const void* y, int norb, int na, int nb, boo
   return FFGB_OK;
 }
 
+// Both densities of one gate between x and y into device memory (no
+// synchronization): out_dev = [G^alpha, G^beta] (transition 1-RDM) and, with
+// `pair`, [P^aa, P^ab, P^bb] after them; norb * norb complex values each.
+// One pair of transposes serves both.
+template <typename T>
+static int densities_dev(const void* x, const void* y, int norb, int na, int nb, bool pair, double2* out_dev,
+                         Scratch& scr, cudaStream_t st) {
+  using C = typename CT<T>::type;
+  const long long da = binom_h(norb, na), db = binom_h(norb, nb);
+  const unsigned *sa = nullptr, *sb = nullptr;
+  FFGB_TRY(device_strings(norb, na, &sa));
+  FFGB_TRY(device_strings(norb, nb, &sb));
+  const size_t S = (size_t)(da * db) * sizeof(C);
+  const size_t n2 = (size_t)norb * norb;
+  void* tx = scr.take(S);
+  void* ty = scr.take(S);
+  const size_t pbytes = density_scratch(norb, na, nb);
+  void* part = scr.take(pbytes);
+  void* bbuf = scr.take(sizeof(double2) * 2 * n2);  // the beta pass's (bb, ba) sums
+  const unsigned *sa1 = nullptr, *sb1 = nullptr;
+  if (na >= 1) FFGB_TRY(device_strings(norb, na - 1, &sa1));
+  if (nb >= 1) FFGB_TRY(device_strings(norb, nb - 1, &sb1));
+  if (!tx || !ty || !part || !bbuf) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
+  FFGB_TRY(launch_transpose<T>(x, tx, da, db, nullptr, nullptr, st));
+  FFGB_TRY(launch_transpose<T>(y, ty, da, db, nullptr, nullptr, st));
+  FFGB_TRY(rdm1_rows_dev<T>(x, y, sa, (int)da, (int)db, norb, part, pbytes, out_dev, st, na, sa1,
+                            na >= 1 ? (int)binom_h(norb, na - 1) : 0));
+  FFGB_TRY(rdm1_rows_dev<T>(tx, ty, sb, (int)db, (int)da, norb, part, pbytes, out_dev + n2, st, nb, sb1,
+                            nb >= 1 ? (int)binom_h(norb, nb - 1) : 0));
+  if (pair) {
+    FFGB_TRY(pair_rows_dev<T>(x, y, sa, sb, (int)da, (int)db, norb, part, pbytes, out_dev + 2 * n2, st));
+    FFGB_TRY(pair_rows_dev<T>(tx, ty, sb, sa, (int)db, (int)da, norb, part, pbytes, (double2*)bbuf, st));
+    FFGB_CUDA(cudaMemcpyAsync(out_dev + 4 * n2, bbuf, sizeof(double2) * n2, cudaMemcpyDeviceToDevice, st));
+  }
+  return FFGB_OK;
+}
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
@@ -1782,7 +1833,7 @@ size_t ffgb_scratch_bytes(int op, int dtype, int norb, int na, int nb) {
   const size_t S = (size_t)da * db * el;
   const size_t ex = extras_bytes(norb, na, nb) + 4096;
   if (op == 1 || op == 2) return 2 * S + ex;
-  if (op == 3) return 2 * S + density_scratch(norb, na, std::max(nb, 0)) + ex;
+  if (op == 3) return 2 * S + density_scratch(norb, na, std::max(nb, 0)) + 32 * (size_t)norb * norb + 256 + ex;
   return S + ex;
 }
 
@@ -2221,6 +2272,18 @@ int ffgb_pair_density(const void* x, const void* y, int dtype, int norb, int na,
   cudaStream_t st = (cudaStream_t)stream;
   return FFGB_DISPATCH(dtype, densities<float>(x, y, norb, na, nb, true, out, scr, st),
                        densities<double>(x, y, norb, na, nb, true, out, scr, st));
+}
+
+int ffgb_gate_densities(const void* x, const void* y, int dtype, int norb, int na, int nb, int pair, void* out_dev,
+                        void* scratch, size_t scratch_bytes, void* stream) {
+  g_err.clear();
+  FFGB_TRY(check_shape(dtype, norb, na, nb));
+  FFGB_TRY(need_buffers({x, y, out_dev}));
+  if (nb < 0) return fail(FFGB_ERR_UNSUPPORTED, "densities need a spinful system");
+  Scratch scr(scratch, scratch_bytes);
+  cudaStream_t st = (cudaStream_t)stream;
+  return FFGB_DISPATCH(dtype, densities_dev<float>(x, y, norb, na, nb, pair != 0, (double2*)out_dev, scr, st),
+                       densities_dev<double>(x, y, norb, na, nb, pair != 0, (double2*)out_dev, scr, st));
 }
 
 int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out, void* stream) {

@@ -202,6 +202,67 @@ __global__ void __launch_bounds__(DTHREADS) rdm1_sub_kernel(const float2* __rest
   }
 }
 
+// Small sectors (the state a few MB, in L2): the same (NV x NV) block per
+// (n-1)-string s as rdm1_sub_kernel, one CTA per s, one warp per entry of
+// the block at a time (lanes over the columns, sums in FP32 per lane and
+// FP64 across the warp by shuffles, no block barrier); rows are read from L2
+// by the NV warps that need them.
+__device__ __forceinline__ long long binom_ll(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  long long r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+
+template <int NV>
+__global__ void __launch_bounds__(DTHREADS) rdm1_small_kernel(const float2* __restrict__ x,
+                                                              const float2* __restrict__ y,
+                                                              const unsigned* __restrict__ sub, int cols, int norb,
+                                                              double2* __restrict__ partial) {
+  __shared__ long long srow[NV];
+  __shared__ float ssg[NV];
+  const unsigned s = sub[blockIdx.x];
+  if (threadIdx.x < NV) {  // the j-th vacancy of s, its row and sign
+    int v = -1;
+    for (int o = 0, k = 0; o < norb; ++o)
+      if (!((s >> o) & 1u)) {
+        if (k == (int)threadIdx.x) {
+          v = o;
+          break;
+        }
+        ++k;
+      }
+    unsigned t = s | (1u << v);
+    long long r = 0;
+    for (int k = 1; t; ++k) {  // colex rank
+      const int pos = __ffs(t) - 1;
+      t &= t - 1;
+      r += binom_ll(pos, k);
+    }
+    srow[threadIdx.x] = r * cols;
+    ssg[threadIdx.x] = (__popc(s & ((1u << v) - 1u)) & 1) ? -1.f : 1.f;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double2* out = partial + (long long)blockIdx.x * NV * NV;
+  for (int e = warp; e < NV * NV; e += DTHREADS / 32) {
+    const int i = e / NV, j = e - i * NV;
+    const float2* xr = x + srow[i];
+    const float2* yr = y + srow[j];
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = lane; c < cols; c += 32) acc = cdot_row(acc, xr[c], yr[c]);
+    double2 v = to_d2(acc);
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    if (lane == 0) {
+      const double sg = (double)(ssg[i] * ssg[j]);
+      out[e] = make_double2(sg * v.x, sg * v.y);
+    }
+  }
+}
+
 // G_pq = sum over the (n-1)-strings s with p, q not in s of block[s][i][j],
 // i / j the positions of p / q among the vacancies of s; one CTA per (p, q),
 // fixed order.
@@ -225,11 +286,16 @@ __global__ void __launch_bounds__(DTHREADS) rdm1_sub_reduce_kernel(const double2
 
 template <int NV>
 int launch_rdm1_sub(const void* x, const void* y, const unsigned* sub, int n_sub, int cols, int norb,
-                    double2* partial, double2* g, cudaStream_t st) {
+                    double2* partial, double2* g, bool small, cudaStream_t st) {
   constexpr int NI = NV >= 7 ? 3 : NV;  // at most 3 x 10 accumulators: two CTAs per SM
-  const dim3 grid((unsigned)n_sub, (unsigned)((NV + NI - 1) / NI));
-  rdm1_sub_kernel<NV, NI><<<grid, DTHREADS, 0, st>>>((const float2*)x, (const float2*)y, sub, cols, norb,
-                                                     partial);
+  if (small) {
+    rdm1_small_kernel<NV><<<(unsigned)n_sub, DTHREADS, 0, st>>>((const float2*)x, (const float2*)y, sub, cols,
+                                                                norb, partial);
+  } else {
+    const dim3 grid((unsigned)n_sub, (unsigned)((NV + NI - 1) / NI));
+    rdm1_sub_kernel<NV, NI><<<grid, DTHREADS, 0, st>>>((const float2*)x, (const float2*)y, sub, cols, norb,
+                                                       partial);
+  }
   count_launch();
   FFGB_CUDA(cudaGetLastError());
   rdm1_sub_reduce_kernel<<<norb * norb, DTHREADS, 0, st>>>(partial, sub, n_sub, NV, norb, g);
@@ -365,89 +431,138 @@ __global__ void __launch_bounds__(SUMB_K * SUMB_G) sum_blocks_kernel(const doubl
   }
 }
 
+// out[k] = sum over c < chunks of partial[k * chunks + c]: one warp per k,
+// lanes over c (in order within a lane), then a fixed shuffle tree.
+__global__ void __launch_bounds__(256) sum_chunks_kernel(const double2* __restrict__ partial, int chunks, int n,
+                                                         double2* __restrict__ out) {
+  const int k = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (k >= n) return;
+  double2 a = make_double2(0.0, 0.0);
+  for (int c = lane; c < chunks; c += 32) {
+    const double2 v = partial[(long long)k * chunks + c];
+    a.x += v.x;
+    a.y += v.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a.x += __shfl_down_sync(0xffffffffu, a.x, o);
+    a.y += __shfl_down_sync(0xffffffffu, a.y, o);
+  }
+  if (lane == 0) out[k] = a;
+}
+
 }  // namespace
 
-// Transition one-body density of the sector on the rows of x, y (rows x cols).
+// Transition one-body density of the sector on the rows of x, y (rows x cols)
+// into g_dev (norb * norb complex, device memory), without synchronizing.
 // complex64 sectors with 1 <= nocc and at most 10 vacancies per (nocc-1)-string
-// run rdm1_sub_kernel over `sub` (the nocc-1 strings); others rdm1_kernel.
+// run rdm1_sub_kernel (large) or rdm1_small_kernel over `sub` (the nocc-1
+// strings); others rdm1_kernel, whose partials sum_chunks_kernel reduces.
 template <typename T>
-int rdm1_rows(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
-              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st, int nocc,
-              const unsigned* sub, int n_sub) {
+int rdm1_rows_dev(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
+                  void* partial_buf, size_t partial_bytes, double2* g_dev, cudaStream_t st, int nocc,
+                  const unsigned* sub, int n_sub) {
   const int nv = norb - nocc + 1;
-  // small sectors stay on rdm1_kernel: there the sub-string form's per-CTA
-  // overhead outweighs its fewer row reads (measured: 1.0 against 0.5 ms at
-  // norb 12, 33 against 58 ms at norb 16)
+  // large sectors: rdm1_sub_kernel (registers hold a third of the block per
+  // thread, columns split over the CTA); small ones, whose states sit in L2:
+  // rdm1_small_kernel (a warp per block entry)
   const bool large = (long long)rows * cols >= (1LL << 23);
-  if (sizeof(T) == 4 && large && sub && nocc >= 1 && nv >= 1 && nv <= 10 && n_sub > 0 && cols > 0) {
-    const size_t need = sizeof(double2) * ((size_t)n_sub * nv * nv + (size_t)norb * norb);
+  if (norb <= 0) return FFGB_OK;
+  if (sizeof(T) == 4 && sub && nocc >= 1 && nv >= 1 && nv <= 10 && n_sub > 0 && cols > 0) {
+    const size_t need = sizeof(double2) * (size_t)n_sub * nv * nv;
     if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
     double2* part = (double2*)partial_buf;
-    double2* g = part + (size_t)n_sub * nv * nv;
-    int s = FFGB_OK;
     switch (nv) {
-      case 1: s = launch_rdm1_sub<1>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 2: s = launch_rdm1_sub<2>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 3: s = launch_rdm1_sub<3>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 4: s = launch_rdm1_sub<4>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 5: s = launch_rdm1_sub<5>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 6: s = launch_rdm1_sub<6>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 7: s = launch_rdm1_sub<7>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 8: s = launch_rdm1_sub<8>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      case 9: s = launch_rdm1_sub<9>(x, y, sub, n_sub, cols, norb, part, g, st); break;
-      default: s = launch_rdm1_sub<10>(x, y, sub, n_sub, cols, norb, part, g, st); break;
+      case 1: return launch_rdm1_sub<1>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 2: return launch_rdm1_sub<2>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 3: return launch_rdm1_sub<3>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 4: return launch_rdm1_sub<4>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 5: return launch_rdm1_sub<5>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 6: return launch_rdm1_sub<6>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 7: return launch_rdm1_sub<7>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 8: return launch_rdm1_sub<8>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      case 9: return launch_rdm1_sub<9>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
+      default: return launch_rdm1_sub<10>(x, y, sub, n_sub, cols, norb, part, g_dev, !large, st);
     }
-    if (s) return s;
-    out.assign(2 * (size_t)norb * norb, 0.0);
-    FFGB_CUDA(cudaMemcpyAsync(out.data(), g, sizeof(double2) * (size_t)norb * norb, cudaMemcpyDeviceToHost, st));
-    FFGB_CUDA(cudaStreamSynchronize(st));
-    return FFGB_OK;
   }
   const int chunks = (rows + RDM_ROWS - 1) / RDM_ROWS;
   const size_t need = sizeof(double2) * (size_t)chunks * norb * norb;
   if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
-  if (rows > 0 && cols > 0 && norb > 0) {
-    dim3 grid((unsigned)chunks, (unsigned)(norb * norb));
-    rdm1_kernel<T><<<grid, DTHREADS, 0, st>>>((const typename CT<T>::type*)x, (const typename CT<T>::type*)y,
-                                              strings, rows, cols, norb, (double2*)partial_buf);
-    count_launch();
-    FFGB_CUDA(cudaGetLastError());
+  if (rows <= 0 || cols <= 0) {
+    FFGB_CUDA(cudaMemsetAsync(g_dev, 0, sizeof(double2) * (size_t)norb * norb, st));
+    return FFGB_OK;
   }
-  std::vector<double> h(2 * (size_t)chunks * norb * norb, 0.0);
-  if (!h.empty()) FFGB_CUDA(cudaMemcpyAsync(h.data(), partial_buf, need, cudaMemcpyDeviceToHost, st));
-  FFGB_CUDA(cudaStreamSynchronize(st));
-  out.assign(2 * (size_t)norb * norb, 0.0);
-  for (int pq = 0; pq < norb * norb; ++pq)
-    for (int c = 0; c < chunks; ++c) {
-      out[2 * pq] += h[2 * ((size_t)pq * chunks + c)];
-      out[2 * pq + 1] += h[2 * ((size_t)pq * chunks + c) + 1];
-    }
+  dim3 grid((unsigned)chunks, (unsigned)(norb * norb));
+  rdm1_kernel<T><<<grid, DTHREADS, 0, st>>>((const typename CT<T>::type*)x, (const typename CT<T>::type*)y,
+                                            strings, rows, cols, norb, (double2*)partial_buf);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  sum_chunks_kernel<<<(unsigned)((norb * norb + 7) / 8), 256, 0, st>>>((const double2*)partial_buf, chunks,
+                                                                      norb * norb, g_dev);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
   return FFGB_OK;
 }
 
-// Pair densities (row-row and row-column) of x, y with rows indexed by rstr.
+// The same, read back to the host (synchronizes).
 template <typename T>
-int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
-              int norb, void* partial_buf, size_t partial_bytes, std::vector<double>& rr, std::vector<double>& rc,
-              cudaStream_t st) {
+int rdm1_rows(const void* x, const void* y, const unsigned* strings, int rows, int cols, int norb,
+              void* partial_buf, size_t partial_bytes, std::vector<double>& out, cudaStream_t st, int nocc,
+              const unsigned* sub, int n_sub) {
+  const size_t n2 = (size_t)norb * norb;
+  if (partial_bytes < sizeof(double2) * n2 + 256) return fail(FFGB_ERR_OOM, "scratch too small for densities");
+  // the result at the end of the partial buffer
+  const size_t tail = (partial_bytes - sizeof(double2) * n2) / 256 * 256;
+  double2* g = (double2*)((char*)partial_buf + tail);
+  FFGB_TRY(rdm1_rows_dev<T>(x, y, strings, rows, cols, norb, partial_buf, tail, g, st, nocc, sub, n_sub));
+  out.assign(2 * n2, 0.0);
+  if (n2) {
+    FFGB_CUDA(cudaMemcpyAsync(out.data(), g, sizeof(double2) * n2, cudaMemcpyDeviceToHost, st));
+    FFGB_CUDA(cudaStreamSynchronize(st));
+  }
+  return FFGB_OK;
+}
+
+// Pair densities (row-row and row-column) of x, y with rows indexed by rstr
+// into sums_dev (2 * norb * norb complex: row-row, then row-column), without
+// synchronizing.
+template <typename T>
+int pair_rows_dev(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
+                  int norb, void* partial_buf, size_t partial_bytes, double2* sums_dev, cudaStream_t st) {
   const long long chunks = (rows + PAIR_ROWS - 1) / PAIR_ROWS;
   const int per = 2 * norb * norb;
-  const size_t need = sizeof(double2) * ((size_t)chunks * per + per);
+  const size_t need = sizeof(double2) * (size_t)chunks * per;
   if (need > partial_bytes) return fail(FFGB_ERR_OOM, "scratch too small for density partial sums");
-  rr.assign(2 * (size_t)norb * norb, 0.0);
-  rc.assign(2 * (size_t)norb * norb, 0.0);
-  if (rows <= 0 || cols <= 0 || norb <= 0) return FFGB_OK;
+  if (per == 0) return FFGB_OK;
+  if (rows <= 0 || cols <= 0) {
+    FFGB_CUDA(cudaMemsetAsync(sums_dev, 0, sizeof(double2) * per, st));
+    return FFGB_OK;
+  }
   double2* part = (double2*)partial_buf;
-  double2* sums = part + (size_t)chunks * per;
   pair_density_kernel<T><<<(unsigned)chunks, PAIR_THREADS, 0, st>>>((const typename CT<T>::type*)x,
                                                                     (const typename CT<T>::type*)y, rstr, cstr,
                                                                     rows, cols, norb, part);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
-  sum_blocks_kernel<<<(per + SUMB_K - 1) / SUMB_K, SUMB_K * SUMB_G, 0, st>>>(part, chunks, per, sums);
+  sum_blocks_kernel<<<(per + SUMB_K - 1) / SUMB_K, SUMB_K * SUMB_G, 0, st>>>(part, chunks, per, sums_dev);
   count_launch();
   FFGB_CUDA(cudaGetLastError());
-  std::vector<double> h(2 * (size_t)per, 0.0);
+  return FFGB_OK;
+}
+
+// The same, read back to the host (synchronizes).
+template <typename T>
+int pair_rows(const void* x, const void* y, const unsigned* rstr, const unsigned* cstr, int rows, int cols,
+              int norb, void* partial_buf, size_t partial_bytes, std::vector<double>& rr, std::vector<double>& rc,
+              cudaStream_t st) {
+  const size_t per = 2 * (size_t)norb * norb;
+  if (partial_bytes < sizeof(double2) * per + 256) return fail(FFGB_ERR_OOM, "scratch too small for densities");
+  const size_t tail = (partial_bytes - sizeof(double2) * per) / 256 * 256;
+  double2* sums = (double2*)((char*)partial_buf + tail);
+  FFGB_TRY(pair_rows_dev<T>(x, y, rstr, cstr, rows, cols, norb, partial_buf, tail, sums, st));
+  rr.assign(2 * (size_t)norb * norb, 0.0);
+  rc.assign(2 * (size_t)norb * norb, 0.0);
+  if (!per) return FFGB_OK;
+  std::vector<double> h(2 * per, 0.0);
   FFGB_CUDA(cudaMemcpyAsync(h.data(), sums, sizeof(double2) * per, cudaMemcpyDeviceToHost, st));
   FFGB_CUDA(cudaStreamSynchronize(st));
   std::memcpy(rr.data(), h.data(), sizeof(double) * 2 * norb * norb);
@@ -463,6 +578,14 @@ template int pair_rows<float>(const void*, const void*, const unsigned*, const u
                               size_t, std::vector<double>&, std::vector<double>&, cudaStream_t);
 template int pair_rows<double>(const void*, const void*, const unsigned*, const unsigned*, int, int, int, void*,
                                size_t, std::vector<double>&, std::vector<double>&, cudaStream_t);
+template int rdm1_rows_dev<float>(const void*, const void*, const unsigned*, int, int, int, void*, size_t,
+                                  double2*, cudaStream_t, int, const unsigned*, int);
+template int rdm1_rows_dev<double>(const void*, const void*, const unsigned*, int, int, int, void*, size_t,
+                                   double2*, cudaStream_t, int, const unsigned*, int);
+template int pair_rows_dev<float>(const void*, const void*, const unsigned*, const unsigned*, int, int, int,
+                                  void*, size_t, double2*, cudaStream_t);
+template int pair_rows_dev<double>(const void*, const void*, const unsigned*, const unsigned*, int, int, int,
+                                   void*, size_t, double2*, cudaStream_t);
 
 // Partial-sum bytes the density kernels need for a sector of `rows` strings
 // (also enough for rdm1_sub_kernel's blocks: at most rows * norb * ... see below).

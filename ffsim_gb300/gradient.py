@@ -159,20 +159,31 @@ class LUCJGradient:
 
     def _backward(self, cur: torch.Tensor, lam: torch.Tensor, V, jaa, jab, L: int):
         """Undo the gates on psi and lambda; generator gradients of the V_j and
-        pair densities at the D_k."""
-        gamma = [None] * (L + 2)
-        pdens = [None] * (L + 1)
+        pair densities at the D_k.  Every gate's densities go to one device
+        buffer (ffgb_gate_densities, no synchronization) that is read back
+        once at the end."""
+        norb = self.norb
+        na, nb = self.nelec
+        n2 = norb * norb
+        dens = torch.empty((L + 2, 10 * n2), dtype=torch.float64, device=cur.device)
         for j in range(L + 1, 0, -1):
             vd = V[j].conj().T
             self._rotate(cur, vd)
             self._rotate(lam, vd)
-            g = self._density("ffgb_transition_rdm1", lam, cur, 2)
-            gamma[j] = g[0] + g[1]
+            _lib.call("ffgb_gate_densities", lam.data_ptr(), cur.data_ptr(), self.code, norb, na, nb, int(j > 1),
+                      dens[j].data_ptr(), self._buf(), self.nbytes, self._stream())
             if j > 1:
                 k = j - 1
-                pdens[k] = self._density("ffgb_pair_density", lam, cur, 3)
                 self._phase(cur, jaa[k], jab[k], 1.0)
                 self._phase(lam, jaa[k], jab[k], 1.0)
+        h = dens.cpu().numpy()
+        gamma = [None] * (L + 2)
+        pdens = [None] * (L + 1)
+        for j in range(1, L + 2):
+            blk = h[j].view(np.complex128).reshape(5, norb, norb)
+            gamma[j] = blk[0] + blk[1]
+            if j > 1:
+                pdens[j - 1] = blk[2:5].copy()
         return gamma, pdens
 
     def _chain(self, params: np.ndarray, U, Uf, gamma, pdens, L: int, with_final: bool) -> np.ndarray:

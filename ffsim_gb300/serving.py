@@ -13,7 +13,10 @@ Admission is by device memory: an engine (the device buffers of one key's
 shape for ``capacity`` states) is taken idle from the pool or allocated within
 the HBM budget, releasing the least recently used idle engines of other shapes
 when needed (their memory is freed at once); an engine for a batch takes at
-most its worker's share of the budget, and a batch shrinks to what fits.
+most its worker's share of the budget, and a batch shrinks to what fits.  The
+budget is an estimate: if the device cannot hold a new engine after all (the
+caching allocator's segments fragment), the budget shrinks to the memory the
+device reports free and the batch waits for its turn again.
 
 Every request gets its own result: a value, or the error that stopped it
 (``ValueError`` for an invalid request, ``MemoryError`` when even one state
@@ -195,7 +198,10 @@ class LUCJServer:
         # worker's share of the budget, so that every worker can hold one
         self.engine_limit = self.budget // max(1, workers)
         self.max_batch = max(1, int(max_batch))
-        self.make_engine = make_engine or (lambda k, n, ne, c: _Engine(k, n, ne, c, self.dtype))
+        self._default_make = lambda k, n, ne, c: _Engine(k, n, ne, c, self.dtype)
+        self.make_engine = make_engine or self._default_make
+        self._evicted = False  # idle engines were released since the last build
+        self.oom_retries = 0  # engine builds that found less device memory than the budget
         self.size_of = size_of or (lambda k, n, ne, c: engine_bytes(k, n, ne, c, self.dtype))
         self.use_streams = use_streams
         self._cv = threading.Condition()
@@ -337,6 +343,7 @@ class LUCJServer:
             self._idle[s2].remove(e2)
             self._in_use -= e2.nbytes
             self._release(e2)
+            self._evicted = True
         if self._in_use + need > self.budget:
             return 0
         self._in_use += need
@@ -406,17 +413,21 @@ class LUCJServer:
                 self.batch_sizes.append(len(group))
             start = time.perf_counter()
             values, err = None, None
+            shape = batch_key(group[0])[:3]
+            if ev is None:
+                ev = self._build(shape, cap, reserved, group)
+                if ev is None:  # no device memory after all: the group waits again
+                    with self._cv:
+                        self._n_running -= 1
+                        for r in group:
+                            self._running.pop(r.rid, None)
+                    continue
             try:
-                shape = batch_key(group[0])[:3]
                 if stream is not None:
                     with torch.cuda.stream(stream):
-                        if ev is None:
-                            ev = self.make_engine(shape[0], shape[1], shape[2], cap)
                         values = ev.run(group, control)
                         stream.synchronize()
                 else:
-                    if ev is None:
-                        ev = self.make_engine(shape[0], shape[1], shape[2], cap)
                     values = ev.run(group, control)
             except BaseException as exc:  # noqa: BLE001
                 err = exc
@@ -430,13 +441,49 @@ class LUCJServer:
                         self._in_use += ev.nbytes - reserved
                     self._idle[shape].append(ev)
                     self._idle_order[id(ev)] = (shape, ev)
-                else:  # never built, or failed: its memory is released
-                    self._in_use -= reserved if ev is None or reserved else ev.nbytes
-                    if ev is not None:
-                        self._release(ev)
+                else:  # failed: its memory is released
+                    self._in_use -= reserved if reserved else ev.nbytes
+                    self._release(ev)
+                    self._evicted = True
                     ev = None
                 for i, r in enumerate(group):
                     self._record(r, None if err is not None else values[i], err, len(group), start)
+
+    def _build(self, shape: tuple, cap: int, reserved: int, group: list[Request]):
+        """A new engine for `group`, or None when the device cannot hold it
+        now.  The caching allocator keeps released engines' memory unless it
+        is emptied, so it is emptied after evictions.  If the allocation
+        still fails, the budget shrinks to what the device really has, the
+        reservation is returned and the group goes back to the front of the
+        queue; after three such failures its requests fail with MemoryError."""
+        import torch
+
+        if self._evicted and self.make_engine is self._default_make:
+            self._evicted = False
+            torch.cuda.empty_cache()
+        try:
+            return self.make_engine(shape[0], shape[1], shape[2], cap)
+        except BaseException as exc:  # noqa: BLE001
+            oom = isinstance(exc, MemoryError) or type(exc).__name__ == "OutOfMemoryError"
+            with self._cv:
+                self._in_use -= reserved
+                tries = max(getattr(r, "_oom_tries", 0) for r in group) + 1
+                if not oom or tries >= 3:
+                    for r in group:
+                        self._record(r, None, exc, 0, time.perf_counter())
+                    return None
+                for r in group:
+                    r._oom_tries = tries
+                self._pending.extendleft(reversed(group))
+                self.oom_retries += 1
+            if self.make_engine is self._default_make:
+                torch.cuda.empty_cache()
+                free, _ = torch.cuda.mem_get_info()
+                with self._cv:
+                    self.budget = min(self.budget, self._in_use + int(0.9 * free))
+                    self.engine_limit = min(self.engine_limit, self.budget)
+                    self._cv.notify_all()
+            return None
 
     def _resident_lane(self) -> None:
         """Feeds the resident evaluator in arrival order while its queue has

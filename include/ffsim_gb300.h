@@ -330,6 +330,17 @@ int ffgb_transition_rdm1(const void* x, const void* y, int dtype, int norb, int 
 int ffgb_pair_density(const void* x, const void* y, int dtype, int norb, int n_alpha, int n_beta, double* out,
                       void* scratch, size_t scratch_bytes, void* stream);
 
+/* Both densities of one gate of the adjoint gradient, into DEVICE memory
+ * out_dev, without synchronizing: the transition one-body densities of
+ * ffgb_transition_rdm1 (alpha, beta) and, when pair != 0, the pair densities
+ * of ffgb_pair_density (aa, ab, bb) after them -- 2 or 5 blocks of
+ * norb*norb complex values (interleaved FP64).  One pair of transposes
+ * serves both, and the caller reads every gate's densities after one
+ * synchronization.  Scratch: ffgb_scratch_bytes(3, ...).  No counterpart in
+ * the reference. */
+int ffgb_gate_densities(const void* x, const void* y, int dtype, int norb, int n_alpha, int n_beta, int pair,
+                        void* out_dev, void* scratch, size_t scratch_bytes, void* stream);
+
 /* out[0..1] = sum conj(x) y in FP64 (host pointer; synchronizes). */
 int ffgb_vdot(const void* x, const void* y, int dtype, long long n, double* out, void* stream);
 

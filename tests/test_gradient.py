@@ -107,3 +107,44 @@ def test_autograd_function_batch(cuda):
         e, g = ev.value_and_grad(batch[row].detach().numpy(), n_reps, ham)
         assert abs(energies[row].item() - e) < 1e-12
         np.testing.assert_allclose(batch.grad[row].numpy(), g, atol=1e-12)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("norb,nelec", [(6, (3, 2)), (8, (4, 4)), (12, (6, 6)), (14, (7, 7))])
+def test_gate_densities_match_the_single_density_calls(cuda, norb, nelec):
+    """ffgb_gate_densities (both densities of a gate into device memory, one
+    pair of transposes, no synchronization) equals ffgb_transition_rdm1 and
+    ffgb_pair_density, in both precisions and on the small-sector and
+    large-sector transition-density kernels (norb 14 is a large sector)."""
+    import torch
+
+    import ffsim_gb300 as f
+    from ffsim_gb300 import _lib
+    from ffsim_gb300._state import scratch
+
+    rng = np.random.default_rng(norb)
+    d = f.dim(norb, nelec)
+    n2 = norb * norb
+    for dtype, code in ((torch.complex64, _lib.FFGB_C64), (torch.complex128, _lib.FFGB_C128)):
+        if norb == 14 and dtype == torch.complex128:
+            continue
+        x = torch.from_numpy(rng.standard_normal(d) + 1j * rng.standard_normal(d)).to("cuda").to(dtype)
+        y = torch.from_numpy(rng.standard_normal(d) + 1j * rng.standard_normal(d)).to("cuda").to(dtype)
+        buf, nbytes = scratch(x, 3, norb, *nelec)
+        st = torch.cuda.current_stream().cuda_stream
+        g = np.zeros(4 * n2)
+        p = np.zeros(6 * n2)
+        _lib.call("ffgb_transition_rdm1", x.data_ptr(), y.data_ptr(), code, norb, *nelec, _lib.dptr(g),
+                  buf.data_ptr(), nbytes, st)
+        _lib.call("ffgb_pair_density", x.data_ptr(), y.data_ptr(), code, norb, *nelec, _lib.dptr(p),
+                  buf.data_ptr(), nbytes, st)
+        for pair in (0, 1):
+            out = torch.full((10 * n2,), np.nan, dtype=torch.float64, device="cuda")
+            _lib.call("ffgb_gate_densities", x.data_ptr(), y.data_ptr(), code, norb, *nelec, pair,
+                      out.data_ptr(), buf.data_ptr(), nbytes, st)
+            h = out.cpu().numpy()
+            np.testing.assert_array_equal(h[: 4 * n2], g)
+            if pair:
+                np.testing.assert_array_equal(h[4 * n2:], p)
+            else:
+                assert np.isnan(h[4 * n2:]).all()

@@ -269,6 +269,45 @@ def test_deadline_while_pending():
     assert isinstance(res[1].error, TimeoutError)
 
 
+def test_engine_build_out_of_memory_requeues_then_fails():
+    """An engine whose allocation fails (the device held less than the
+    budget said) sends its batch back to the queue; a later build serves it.
+    A batch whose engine fails three times gets MemoryError."""
+    from ffsim_gb300.serving import LUCJServer
+
+    _reset()
+    fails = {"left": 2}
+
+    def make(k, n, ne, c):
+        if fails["left"] > 0:
+            fails["left"] -= 1
+            raise MemoryError("device full")
+        return _FakeEngine(k, n, ne, c)
+
+    srv = LUCJServer(workers=1, budget_bytes=10**9, max_batch=8, make_engine=make,
+                     size_of=lambda k, n, ne, c: n * 100 * c, use_streams=False)
+    reqs = _reqs(6, norbs=(8,))
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(len(reqs), timeout=30)
+    srv.close()
+    assert all(r.ok for r in res)
+    assert srv.oom_retries == 2
+
+    def never(k, n, ne, c):
+        raise MemoryError("device full")
+
+    srv = LUCJServer(workers=1, budget_bytes=10**9, max_batch=8, make_engine=never,
+                     size_of=lambda k, n, ne, c: n * 100 * c, use_streams=False)
+    reqs = _reqs(3, norbs=(8,))
+    for r in reqs:
+        srv.submit(r)
+    res = srv.drain(len(reqs), timeout=30)
+    srv.close()
+    assert all(isinstance(r.error, MemoryError) for r in res)
+    assert srv._in_use == 0
+
+
 def _mixed(n, seed=0):
     """Energy requests of norb 6, 8 (resident) and 10 (batch), and norb-8
     gradients (batch)."""
