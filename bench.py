@@ -614,7 +614,7 @@ def run_serve(args) -> None:
         "requests": len(reqs), "completed": st["completed"], "gradients": n_grad,
         "arrival_rate_per_s": args.rate, "workers": args.workers, "max_batch": args.max_batch,
         "resident": not args.no_resident, "oom_retries": srv.oom_retries,
-        "allocator": os.environ.get("PYTORCH_CUDA_ALLOC_CONF", ""),
+        "allocator": os.environ.get("PYTORCH_ALLOC_CONF", os.environ.get("PYTORCH_CUDA_ALLOC_CONF", "")),
         "mean_batch": statistics.mean(srv.batch_sizes), "max_concurrent": srv.max_concurrent,
         "span_s": st["span_s"], "resident_served": srv.resident_served,
         "p50_ms_by_norb": {m: 1e3 * statistics.median(v) for m, v in sorted(by_norb.items())},
@@ -828,11 +828,11 @@ def main():
     ap.add_argument("--batch-states", type=int, default=4, help="evaluations per step (one batch)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.serve and "PYTORCH_CUDA_ALLOC_CONF" not in os.environ:
+    if args.serve and "PYTORCH_ALLOC_CONF" not in os.environ and "PYTORCH_CUDA_ALLOC_CONF" not in os.environ:
         # engines of many shapes come and go: expandable segments let the
         # caching allocator return a released engine's pages to the device
         # instead of keeping partly used segments
-        os.environ["PYTORCH_CUDA_ALLOC_CONF"] = "expandable_segments:True"
+        os.environ["PYTORCH_ALLOC_CONF"] = "expandable_segments:True"
     if args.ops:
         run_ops(args)
         return

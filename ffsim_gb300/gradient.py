@@ -62,20 +62,21 @@ def _dexp(K: np.ndarray, dK: np.ndarray) -> np.ndarray:
     return W @ (M * phi[None]) @ Wd
 
 
-def _dexp_adjoint(K: np.ndarray, gam: np.ndarray) -> np.ndarray:
-    """The matrix G with Re <dexp(K)[dK], gam> = Re <dK, G> for every dK
-    (<X, Y> = sum_pq X_pq Y_pq): the adjoint of _dexp.  With K = W diag(i w)
-    W^dag and dexp(K)[dK] = W ((W^dag dK W) o Phi) W^dag, G = conj(W)
-    (Phi o (W^T gam conj(W))) W^T."""
-    w, W = np.linalg.eigh(-1j * K)
+def _dexp_adjoint(w: np.ndarray, W: np.ndarray, gam: np.ndarray) -> np.ndarray:
+    """For a stack of antihermitian K = W diag(i w) W^dag ((B, n), (B, n, n))
+    and gam (B, n, n): the matrices G with Re <dexp(K)[dK], gam> = Re <dK, G>
+    for every dK (<X, Y> = sum_pq X_pq Y_pq), the adjoint of _dexp.  With
+    dexp(K)[dK] = W ((W^dag dK W) o Phi) W^dag, G = conj(W) (Phi o (W^T gam
+    conj(W))) W^T."""
     e = np.exp(1j * w)
-    diff = 1j * (w[:, None] - w[None, :])
+    diff = 1j * (w[:, :, None] - w[:, None, :])
     with np.errstate(divide="ignore", invalid="ignore"):
-        phi = (e[:, None] - e[None, :]) / diff
+        phi = (e[:, :, None] - e[:, None, :]) / diff
     close = np.abs(diff) < 1e-12
-    phi[close] = np.broadcast_to(e[:, None], phi.shape)[close]
+    phi[close] = np.broadcast_to(e[:, :, None], phi.shape)[close]
     Wc = W.conj()
-    return Wc @ (phi * (W.T @ gam @ Wc)) @ W.T
+    WT = np.swapaxes(W, -1, -2)
+    return Wc @ (phi * (WT @ gam @ Wc)) @ WT
 
 
 class LUCJGradient:
@@ -135,19 +136,49 @@ class LUCJGradient:
         return out.view(np.complex128).reshape(blocks, self.norb, self.norb)
 
     # -- energy and gradient -------------------------------------------------
-    def _circuit(self, params: np.ndarray, n_reps: int, with_final: bool):
-        """The merged rotations V_j and diagonal matrices of the circuit."""
+    def _circuits(self, params: np.ndarray, n_reps: int, with_final: bool) -> list:
+        """The circuits of a batch of parameter rows (B, n_params), computed
+        together: per state (U, Uf, V, jaa, jab, eig) with U[k] the layer
+        rotations (U[0] = 1), V[j] the merged rotations V_j, the diagonal
+        matrices of each layer and eig[k] = (w, W) with U[k] = W diag(e^{iw}) W^dag
+        (the eigendecomposition the chain rule reuses).  Every step acts on each
+        state on its own (stacked LAPACK and GEMM calls), so a state's circuit
+        does not depend on the batch."""
         norb = self.norb
-        ucj = UCJOpSpinBalanced.from_parameters(params, norb=norb, n_reps=n_reps,
-                                                with_final_orbital_rotation=with_final)
         L = n_reps
-        U = [np.eye(norb, dtype=complex)] + [np.asarray(u) for u in ucj.orbital_rotations]
-        Uf = (np.asarray(ucj.final_orbital_rotation) if ucj.final_orbital_rotation is not None
-              else np.eye(norb, dtype=complex))
-        V = [None] + [U[k].conj().T @ U[k - 1] for k in range(1, L + 1)] + [Uf @ U[L]]
-        jaa = [None] + [ucj.diag_coulomb_mats[k, 0] for k in range(L)]
-        jab = [None] + [ucj.diag_coulomb_mats[k, 1] for k in range(L)]
-        return U, Uf, V, jaa, jab
+        P = np.atleast_2d(np.asarray(params, dtype=float))
+        B = P.shape[0]
+        n2 = norb * norb
+        ti, tj = self._triu
+        nt = len(ti)
+        per = n2 + 2 * nt
+        body = P[:, : L * per].reshape(B, L, per)
+        K = antihermitians_from_parameters(body[:, :, :n2].reshape(-1), norb, B * L).reshape(B, L, norb, norb)
+        mats = [K[:, k] for k in range(L)]
+        if with_final:
+            mats.append(antihermitians_from_parameters(P[:, L * per:].reshape(-1), norb, B))
+        w, W = np.linalg.eigh(-1j * np.stack(mats, axis=1))  # (B, L(+1), n), (B, L(+1), n, n)
+        Us = W @ (np.exp(1j * w)[..., None] * np.swapaxes(W, -1, -2).conj())
+        J = np.zeros((B, L, 2, norb, norb))
+        for t in range(2):
+            vals = body[:, :, n2 + t * nt: n2 + (t + 1) * nt]
+            J[:, :, t, tj, ti] = vals
+            J[:, :, t, ti, tj] = vals
+        eye = np.eye(norb, dtype=complex)
+        out = []
+        for b in range(B):
+            U = [eye] + [Us[b, k] for k in range(L)]
+            Uf = Us[b, L] if with_final else eye
+            V = [None] + [U[k].conj().T @ U[k - 1] for k in range(1, L + 1)] + [Uf @ U[L]]
+            jaa = [None] + [J[b, k, 0] for k in range(L)]
+            jab = [None] + [J[b, k, 1] for k in range(L)]
+            eig = [None] + [(w[b, k], W[b, k]) for k in range(w.shape[1])]
+            out.append((U, Uf, V, jaa, jab, eig))
+        return out
+
+    def _circuit(self, params: np.ndarray, n_reps: int, with_final: bool):
+        """The merged rotations V_j and diagonal matrices of one circuit."""
+        return self._circuits(np.asarray(params, dtype=float)[None, :], n_reps, with_final)[0]
 
     def _forward(self, cur: torch.Tensor, V, jaa, jab, L: int) -> None:
         """psi from the Hartree-Fock state."""
@@ -186,40 +217,57 @@ class LUCJGradient:
                 pdens[j - 1] = blk[2:5].copy()
         return gamma, pdens
 
-    def _chain(self, params: np.ndarray, U, Uf, gamma, pdens, L: int, with_final: bool) -> np.ndarray:
-        """Chain rule from the generator gradients to the parameters."""
+    def _chains(self, n_params: int, circuits: list, dens: list, L: int, with_final: bool) -> np.ndarray:
+        """Chain rule from the generator gradients to the parameters, for a
+        batch: circuits[b] from _circuits, dens[b] = (gamma, pdens) from
+        _backward.  Returns (B, n_params).  Per state the same operations in
+        the same order whatever the batch (stacked small GEMMs, a per-state
+        projection onto the parameter basis)."""
         norb = self.norb
-        grad = np.zeros_like(params)
+        B = len(circuits)
+        grad = np.zeros((B, n_params))
         ti, tj = self._triu
         n_triu = len(ti)
         diag = ti == tj
+        basis_t = self.basis.reshape(norb * norb, norb * norb).T
         index = 0
+
+        def project(eigs, gam):
+            # 2 Re <basis_n, G> for every rotation parameter n
+            G = _dexp_adjoint(np.stack([e[0] for e in eigs]), np.stack([e[1] for e in eigs]), gam)
+            flat = G.reshape(B, -1)
+            return np.stack([2 * (flat[b] @ basis_t).real for b in range(B)])
+
         for k in range(1, L + 1):
-            Kk = antihermitians_from_parameters(params[index: index + norb * norb], norb, 1)[0]
+            Ukm1 = np.stack([c[0][k - 1] for c in circuits])
+            Uk = np.stack([c[0][k] for c in circuits])
+            gk = np.stack([d[0][k] for d in dens])
+            gk1 = np.stack([d[0][k + 1] for d in dens])
             # V_k = U_k^dag U_{k-1} is perturbed as A dU_k^dag C (A = U_{k-1}^dag U_k,
             # C = U_{k-1}) and V_{k+1} = U_{k+1}^dag U_k (or U_final U_L) as D dU_k
             # (D = U_k^dag); sum_pq (A X C)_pq g_pq = <X, A^T g C^T>, so both
             # contributions are 2 Re <dU_k, Gam> with one matrix Gam
-            A = U[k - 1].conj().T @ U[k]
-            g1 = A.T @ gamma[k] @ U[k - 1].T
-            gam = g1.conj().T + U[k].conj() @ gamma[k + 1]
-            grad[index: index + norb * norb] = 2 * np.einsum(
-                "nab,ab->n", self.basis, _dexp_adjoint(Kk, gam)).real
+            A = np.swapaxes(Ukm1, -1, -2).conj() @ Uk
+            g1 = np.swapaxes(A, -1, -2) @ gk @ np.swapaxes(Ukm1, -1, -2)
+            gam = np.swapaxes(g1, -1, -2).conj() + Uk.conj() @ gk1
+            grad[:, index: index + norb * norb] = project([c[5][k] for c in circuits], gam)
             index += norb * norb
-            P = pdens[k]
+            P = np.stack([d[1][k] for d in dens])
             # same-spin: the pair (i, j) of both sectors, halved on the diagonal;
             # opposite-spin: both orders of (i, j), once on the diagonal
-            daa = np.where(diag, 0.5, 1.0) * (P[0, ti, tj] + P[2, ti, tj])
-            dab = np.where(diag, P[1, ti, tj], P[1, ti, tj] + P[1, tj, ti])
-            grad[index: index + n_triu] = -2 * daa.imag
-            grad[index + n_triu: index + 2 * n_triu] = -2 * dab.imag
+            daa = np.where(diag, 0.5, 1.0) * (P[:, 0, ti, tj] + P[:, 2, ti, tj])
+            dab = np.where(diag, P[:, 1, ti, tj], P[:, 1, ti, tj] + P[:, 1, tj, ti])
+            grad[:, index: index + n_triu] = -2 * daa.imag
+            grad[:, index + n_triu: index + 2 * n_triu] = -2 * dab.imag
             index += 2 * n_triu
         if with_final:
-            Kf = antihermitians_from_parameters(params[index:], norb, 1)[0]
+            UL = np.stack([c[0][L] for c in circuits])
+            Uf = np.stack([c[1] for c in circuits])
+            gL = np.stack([d[0][L + 1] for d in dens])
             # V_{L+1} = U_final U_L perturbed as A dU_final C (A = U_L^dag U_final^dag, C = U_L)
-            A = U[L].conj().T @ Uf.conj().T
-            gam = A.T @ gamma[L + 1] @ U[L].T
-            grad[index:] = 2 * np.einsum("nab,ab->n", self.basis, _dexp_adjoint(Kf, gam)).real
+            A = np.swapaxes(UL, -1, -2).conj() @ np.swapaxes(Uf, -1, -2).conj()
+            gam = np.swapaxes(A, -1, -2) @ gL @ np.swapaxes(UL, -1, -2)
+            grad[:, index:] = project([c[5][L + 1] for c in circuits], gam)
         return grad
 
     def _vdot(self, x: torch.Tensor, y: torch.Tensor) -> float:
@@ -244,15 +292,16 @@ class LUCJGradient:
             raise ValueError(f"the evaluator is for {norb} orbitals; got a Hamiltonian on {ham.norb}")
         params = np.asarray(params, dtype=float)
         L = n_reps
-        U, Uf, V, jaa, jab = self._circuit(params, n_reps, with_final_orbital_rotation)
+        circ = self._circuit(params, n_reps, with_final_orbital_rotation)
+        V, jaa, jab = circ[2], circ[3], circ[4]
         self._forward(self.cur, V, jaa, jab, L)
         ham, (one_body, hdcm, hrots) = self._ham_arrays(ham)
         _lib.call("ffgb_df_matvec", self.cur.data_ptr(), self.lam.data_ptr(), self.code, norb, na, nb,
                   _lib.dptr(one_body), hdcm.shape[0], _lib.dptr(hdcm), hrots.ctypes.data_as(_lib._dp),
                   0.0, 0, self._buf(), self.nbytes, self._stream())
         energy = float(ham.constant) + self._vdot(self.cur, self.lam)
-        gamma, pdens = self._backward(self.cur, self.lam, V, jaa, jab, L)
-        return energy, self._chain(params, U, Uf, gamma, pdens, L, with_final_orbital_rotation)
+        dens = self._backward(self.cur, self.lam, V, jaa, jab, L)
+        return energy, self._chains(params.size, [circ], [dens], L, with_final_orbital_rotation)[0]
 
     def value_and_grad_batch(self, params: np.ndarray, n_reps: int, ham: DoubleFactorizedHamiltonian, *,
                              with_final_orbital_rotation: bool = False,
@@ -272,10 +321,10 @@ class LUCJGradient:
         L = n_reps
         self._ensure_batch(B)
         cur, lam = self._bcur[:B], self._blam[:B]
-        circuits = [self._circuit(p, n_reps, with_final_orbital_rotation) for p in params]
+        circuits = self._circuits(params, n_reps, with_final_orbital_rotation)
 
         def forward(b):
-            _, _, V, jaa, jab = circuits[b]
+            V, jaa, jab = circuits[b][2], circuits[b][3], circuits[b][4]
             self._forward(cur[b], V, jaa, jab, L)
 
         self._on_lanes(forward, B)
@@ -285,13 +334,13 @@ class LUCJGradient:
                   self._bbuf.data_ptr(), self._bbytes, None if control is None else control.ptr, self._stream())
 
         def backward(b):
-            U, Uf, V, jaa, jab = circuits[b]
+            V, jaa, jab = circuits[b][2], circuits[b][3], circuits[b][4]
             e = float(ham.constant) + self._vdot(cur[b], lam[b])
-            gamma, pdens = self._backward(cur[b], lam[b], V, jaa, jab, L)
-            return e, self._chain(params[b], U, Uf, gamma, pdens, L, with_final_orbital_rotation)
+            return e, self._backward(cur[b], lam[b], V, jaa, jab, L)
 
         out = self._on_lanes(backward, B)
-        return np.array([o[0] for o in out]), np.stack([o[1] for o in out])
+        grads = self._chains(params.shape[1], circuits, [o[1] for o in out], L, with_final_orbital_rotation)
+        return np.array([o[0] for o in out]), grads
 
     def _on_lanes(self, fn, n: int) -> list:
         """fn(0), ..., fn(n - 1), spread over the worker lanes (state b on lane

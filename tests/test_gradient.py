@@ -148,3 +148,52 @@ def test_gate_densities_match_the_single_density_calls(cuda, norb, nelec):
                 np.testing.assert_array_equal(h[4 * n2:], p)
             else:
                 assert np.isnan(h[4 * n2:]).all()
+
+
+def test_batched_circuits_and_chain_rule_on_the_host():
+    """The gradient's host side: the circuit's rotations equal expm of the
+    parameters' antihermitian matrices; the chain rule's dexp adjoint is the
+    adjoint of dexp; and a state's circuit and chain rule are bit-identical
+    alone and inside a batch."""
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    import itertools
+
+    import ffsim_gb300 as f
+    from ffsim_gb300.gradient import LUCJGradient, _antihermitian_basis, _dexp, _dexp_adjoint
+    from ffsim_gb300.linalg import antihermitians_from_parameters
+
+    norb, L = 5, 2
+    g = LUCJGradient.__new__(LUCJGradient)
+    g.norb = norb
+    g._triu = tuple(np.array(v) for v in zip(*itertools.combinations_with_replacement(range(norb), 2)))
+    g.basis = _antihermitian_basis(norb)
+    rng = np.random.default_rng(9)
+    n = f.UCJOpSpinBalanced.n_params(norb, L, with_final_orbital_rotation=True)
+    P = rng.normal(scale=0.5, size=(4, n))
+    batch = g._circuits(P, L, True)
+    op = f.UCJOpSpinBalanced.from_parameters(P[2], norb=norb, n_reps=L, with_final_orbital_rotation=True)
+    U, Uf = batch[2][0], batch[2][1]
+    for k in range(L):
+        np.testing.assert_allclose(U[k + 1], op.orbital_rotations[k], atol=1e-13)
+        np.testing.assert_allclose(batch[2][3][k + 1], op.diag_coulomb_mats[k, 0], atol=0)
+        np.testing.assert_allclose(batch[2][4][k + 1], op.diag_coulomb_mats[k, 1], atol=0)
+    np.testing.assert_allclose(Uf, op.final_orbital_rotation, atol=1e-13)
+    # adjoint of dexp
+    K = antihermitians_from_parameters(P[0, : norb * norb], norb, 1)[0]
+    w, W = np.linalg.eigh(-1j * K)
+    gam = rng.normal(size=(norb, norb)) + 1j * rng.normal(size=(norb, norb))
+    G = _dexp_adjoint(w[None], W[None], gam[None])[0]
+    for dK in g.basis[::3]:
+        lhs = np.sum(_dexp(K, dK[None])[0] * gam).real
+        assert abs(lhs - np.sum(dK * G).real) < 1e-12
+    np.testing.assert_allclose(scipy_linalg.expm(K), W @ np.diag(np.exp(1j * w)) @ W.conj().T, atol=1e-13)
+    # alone and in a batch
+    dens = [([None] + [rng.normal(size=(norb, norb)) + 1j * rng.normal(size=(norb, norb)) for _ in range(L + 1)],
+             [None] + [rng.normal(size=(3, norb, norb)) + 1j * rng.normal(size=(3, norb, norb)) for _ in range(L)])
+            for _ in range(4)]
+    grads = g._chains(n, batch, dens, L, True)
+    for b in range(4):
+        alone = g._circuits(P[b:b + 1], L, True)
+        for a, c in zip(alone[0][:2], batch[b][:2]):
+            assert np.array_equal(np.asarray(a), np.asarray(c))
+        assert np.array_equal(g._chains(n, alone, [dens[b]], L, True)[0], grads[b])
