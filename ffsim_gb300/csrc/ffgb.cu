@@ -808,7 +808,11 @@ static int orbital_rotation_impl(void* vec, int norb, int na, int nb, const doub
   const size_t S = (size_t)binom_h(norb, na) * binom_h(norb, nb) * sizeof(C);
   void* tmp = scr.take(S);
   if (!tmp) return fail(FFGB_ERR_OOM, "scratch too small (needs one state)");
-  if (staged<T>(&pa, mb ? &pb : nullptr))
+  // Up to 12 orbitals a state is at most 6.8 MB and the time goes to launches:
+  // the two transposing sector-kernel passes beat the stage path's ~40
+  // launches (measured: 0.068 against 0.123 ms at norb 10, 0.145 against
+  // 0.169 ms at norb 12)
+  if (norb > 12 && staged<T>(&pa, mb ? &pb : nullptr))
     return staged_rotate(vec, vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, true, false, 1, scr, st);
   return rotate_both<T>(vec, tmp, norb, na, nb, &pa, mb ? &pb : nullptr, nullptr, scr, st);
 }
