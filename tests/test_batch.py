@@ -65,6 +65,26 @@ def test_batch_energy_matches_per_state(cuda, norb, nelec, dtype_name):
         assert abs(got[k] - want) <= tol, (k, got[k], want)
 
 
+@pytest.mark.parametrize("norb, nelec", [(13, (6, 7)), (14, (7, 7)), (16, (8, 7))])
+def test_stage_path_energies_match_complex128(cuda, norb, nelec):
+    """For 13-16 orbitals (five-stage plans, windows of 6-8 orbitals) the
+    complex64 energies of the stage path, alone and in a batch, against the
+    complex128 path (sector kernel, no stage kernels)."""
+    import torch
+
+    import ffsim_gb300 as f
+
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=3, seed=norb + 7)
+    ops = [f.random.random_ucj_op_spin_balanced(norb, n_reps=1, diag_coulomb_normal=True, diag_coulomb_scale=0.1,
+                                                seed=300 + k) for k in range(2)]
+    want = [f.lucj_energy(op, ham, norb, nelec, dtype=torch.complex128) for op in ops]
+    single = [f.lucj_energy(op, ham, norb, nelec, dtype=torch.complex64) for op in ops]
+    batch = f.lucj_energies(ops, ham, norb, nelec, dtype=torch.complex64)
+    for k in range(2):
+        assert abs(single[k] - want[k]) <= 1e-6, (k, single[k], want[k])
+        assert abs(batch[k] - want[k]) <= 1e-6, (k, batch[k], want[k])
+
+
 def test_batch_energy_alone_equals_in_batch(cuda):
     """A state's energy does not depend on the other states of its batch."""
     import torch
