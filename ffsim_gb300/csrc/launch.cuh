@@ -1,6 +1,8 @@
 // Definition of launch_sector; included by the instantiation units only.
 #pragma once
 
+#include <atomic>
+
 #include "common.h"
 
 namespace ffgb {
@@ -8,13 +10,16 @@ namespace ffgb {
 template <typename T, int NW>
 int launch_sector(const SectorParams<T>& P, long long n_chunks, int block, int smem, cudaStream_t st,
                   int* grid_out) {
-  static int dev_sms = 0;
+  // per device: the shared-memory opt-in and the SM count
+  static std::atomic<int> sms[64];
+  int dev = 0;
+  FFGB_CUDA(cudaGetDevice(&dev));
+  int dev_sms = (dev >= 0 && dev < 64) ? sms[dev].load() : 0;
   if (dev_sms == 0) {
     FFGB_CUDA(cudaFuncSetAttribute(sector_kernel<T, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    227 * 1024));
-    int dev = 0;
-    FFGB_CUDA(cudaGetDevice(&dev));
     FFGB_CUDA(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev));
+    if (dev >= 0 && dev < 64) sms[dev].store(dev_sms);
   }
   int per_sm = 0;
   FFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sector_kernel<T, NW>, block, smem));
