@@ -264,6 +264,20 @@ def eval_bytes_moved():
     return None, None
 
 
+def window_stage_flops(norb: int, nocc: int, b: int = 8) -> float:
+    """FP32 flops of one b-orbital window stage on the orbitals [0, b) of a
+    sector with nocc of norb orbitals occupied, per column: a class with K
+    electrons in the window has C(b, K) members per group, and each of the
+    b (b - 1) / 2 rotations of its network takes the C(b-2, K-1) member pairs
+    with exactly one of its two orbitals occupied, 12 FMA (24 flops) per pair."""
+    out = 0.0
+    for k in range(0, b + 1):
+        groups = math.comb(norb - b, nocc - k)
+        pairs = math.comb(b - 2, k - 1) if 1 <= k <= b - 1 else 0
+        out += groups * (b * (b - 1) // 2) * pairs * 24
+    return out
+
+
 def rotation_flops(norb: int, nelec) -> float:
     """Floating-point operations of the complex128 two-sector rotation: the
     adjacent-Givens network has norb (norb - 1) / 2 rotations per sector, each
@@ -920,6 +934,7 @@ def main():
     peak, peak_kind = _peaks()
     gbs = 2 * S / (st["window_stage_ms"] * 1e-3) / 1e9
     eval_bytes = (6 * N_REPS + 3 * (RANK + 1)) * S
+    win_flops = window_stage_flops(NORB, NELEC[0]) * math.comb(NORB, NELEC[1])
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -961,6 +976,10 @@ def main():
                     "d2h_bytes_per_step": 8 * B},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                          "frac": gbs / peak, "traffic": traffic, "traffic_source": traffic_src,
+                         # the window stage is bound by FP32 as much as by HBM: its
+                         # Givens network's FMA work against the measured FP32 rate
+                         "fp32_tflops": win_flops / (st["window_stage_ms"] * 1e-3) / 1e12,
+                         "fp32_frac": (win_flops / (st["window_stage_ms"] * 1e-3) / 1e12 / fp[1]) if fp[1] else None,
                          "kernel": "win_class_kernel: one 8-orbital window stage (one launch per electron-count "
                                    "class), 2 S algorithmic bytes",
                          "algorithmic_bytes": 2 * S, "ms": st["window_stage_ms"],
