@@ -98,6 +98,9 @@ SIGNATURES = {
     "ffgb_resident_submit": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _dp, _dp, _dp,
                              ctypes.POINTER(_c_ll)],
     "ffgb_resident_poll": [_c_void_p, _c_ll, _dp],
+    "ffgb_resident_submit_grad": [_c_void_p, _c_int, _c_int, _c_int, _c_int, _c_int, _dp, _dp,
+                                  ctypes.POINTER(_c_ll)],
+    "ffgb_resident_poll_densities": [_c_void_p, _c_ll, _dp, _dp],
     "ffgb_resident_cancel": [_c_void_p, _c_ll],
     "ffgb_resident_start": [_c_void_p],
     "ffgb_resident_status": [_c_void_p, _ip, _ip],

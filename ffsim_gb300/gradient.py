@@ -79,63 +79,20 @@ def _dexp_adjoint(w: np.ndarray, W: np.ndarray, gam: np.ndarray) -> np.ndarray:
     return Wc @ (phi * (WT @ gam @ Wc)) @ WT
 
 
-class LUCJGradient:
-    """Energy and gradient of the LUCJ ansatz for one (norb, nelec) shape,
-    holding its device buffers (two states and scratch)."""
+class GradientHost:
+    """The host side of the adjoint gradient for one norb: the circuits of
+    parameter rows (the merged rotations, the diagonal gates and the
+    eigendecompositions the chain rule reuses) and the chain rule from a
+    circuit's gate densities to its parameters.  The device part (forward
+    circuit, Hamiltonian matvec, backward pass with densities) is
+    LUCJGradient's (batch path) or the resident kernel's (small shapes)."""
 
-    def __init__(self, norb: int, nelec: tuple[int, int], *, dtype=torch.complex64, device="cuda",
-                 workers: int = 4):
+    def __init__(self, norb: int):
         self.norb = norb
-        # batches: per-state gates run on `workers` host threads, each with its
-        # own CUDA stream and scratch, so that their launches and host syncs
-        # overlap; the Hamiltonian matvec runs once over the whole batch
-        self.workers = max(1, int(workers))
-        self._tls = threading.local()
-        self._lanes = None
-        self._pool = None
-        self.nelec = tuple(nelec)
-        self.dtype = dtype
-        self.code = _lib.FFGB_C64 if dtype == torch.complex64 else _lib.FFGB_C128
-        d = dim(norb, nelec)
-        self.cur = torch.empty(d, dtype=dtype, device=device)
-        self.lam = torch.empty(d, dtype=dtype, device=device)
-        need = max(_lib.load().ffgb_scratch_bytes(op, self.code, norb, *self.nelec) for op in (0, 1, 3))
-        self.buf = torch.empty(need, dtype=torch.uint8, device=device)
-        self.nbytes = need
         self.basis = _antihermitian_basis(norb)
         # upper-triangle index pairs (i <= j) in the parameter order of from_parameters
         self._triu = tuple(np.array(v) for v in zip(*itertools.combinations_with_replacement(range(norb), 2)))
 
-    # -- device helpers ----------------------------------------------------
-    def _stream(self):
-        return torch.cuda.current_stream(self.cur.device).cuda_stream
-
-    def _buf(self) -> int:
-        """Scratch of the calling thread (a batch lane's own, else the evaluator's)."""
-        b = getattr(self._tls, "buf", None)
-        return (self.buf if b is None else b).data_ptr()
-
-    def _rotate(self, vec: torch.Tensor, mat: np.ndarray) -> None:
-        m = _lib.cmat(mat)
-        na, nb = self.nelec
-        _lib.call("ffgb_apply_orbital_rotation", vec.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(m),
-                  _lib.dptr(m), self._buf(), self.nbytes, self._stream())
-
-    def _phase(self, vec: torch.Tensor, jaa: np.ndarray, jab: np.ndarray, time: float) -> None:
-        aa, ab = _lib.rmat(jaa), _lib.rmat(jab)
-        na, nb = self.nelec
-        _lib.call("ffgb_apply_diag_coulomb_evolution", vec.data_ptr(), self.code, self.norb, na, nb,
-                  _lib.dptr(aa), _lib.dptr(ab), _lib.dptr(aa), float(time), 0, None, None, self._buf(),
-                  self.nbytes, self._stream())
-
-    def _density(self, name: str, x: torch.Tensor, y: torch.Tensor, blocks: int) -> np.ndarray:
-        out = np.zeros(2 * blocks * self.norb * self.norb)
-        na, nb = self.nelec
-        _lib.call(name, x.data_ptr(), y.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(out),
-                  self._buf(), self.nbytes, self._stream())
-        return out.view(np.complex128).reshape(blocks, self.norb, self.norb)
-
-    # -- energy and gradient -------------------------------------------------
     def _circuits(self, params: np.ndarray, n_reps: int, with_final: bool) -> list:
         """The circuits of a batch of parameter rows (B, n_params), computed
         together: per state (U, Uf, V, jaa, jab, eig) with U[k] the layer
@@ -179,43 +136,6 @@ class LUCJGradient:
     def _circuit(self, params: np.ndarray, n_reps: int, with_final: bool):
         """The merged rotations V_j and diagonal matrices of one circuit."""
         return self._circuits(np.asarray(params, dtype=float)[None, :], n_reps, with_final)[0]
-
-    def _forward(self, cur: torch.Tensor, V, jaa, jab, L: int) -> None:
-        """psi from the Hartree-Fock state."""
-        _lib.call("ffgb_hartree_fock", cur.data_ptr(), self.code, cur.numel(), self._stream())
-        for k in range(1, L + 1):
-            self._rotate(cur, V[k])
-            self._phase(cur, jaa[k], jab[k], -1.0)
-        self._rotate(cur, V[L + 1])
-
-    def _backward(self, cur: torch.Tensor, lam: torch.Tensor, V, jaa, jab, L: int):
-        """Undo the gates on psi and lambda; generator gradients of the V_j and
-        pair densities at the D_k.  Every gate's densities go to one device
-        buffer (ffgb_gate_densities, no synchronization) that is read back
-        once at the end."""
-        norb = self.norb
-        na, nb = self.nelec
-        n2 = norb * norb
-        dens = torch.empty((L + 2, 10 * n2), dtype=torch.float64, device=cur.device)
-        for j in range(L + 1, 0, -1):
-            vd = V[j].conj().T
-            self._rotate(cur, vd)
-            self._rotate(lam, vd)
-            _lib.call("ffgb_gate_densities", lam.data_ptr(), cur.data_ptr(), self.code, norb, na, nb, int(j > 1),
-                      dens[j].data_ptr(), self._buf(), self.nbytes, self._stream())
-            if j > 1:
-                k = j - 1
-                self._phase(cur, jaa[k], jab[k], 1.0)
-                self._phase(lam, jaa[k], jab[k], 1.0)
-        h = dens.cpu().numpy()
-        gamma = [None] * (L + 2)
-        pdens = [None] * (L + 1)
-        for j in range(1, L + 2):
-            blk = h[j].view(np.complex128).reshape(5, norb, norb)
-            gamma[j] = blk[0] + blk[1]
-            if j > 1:
-                pdens[j - 1] = blk[2:5].copy()
-        return gamma, pdens
 
     def _chains(self, n_params: int, circuits: list, dens: list, L: int, with_final: bool) -> np.ndarray:
         """Chain rule from the generator gradients to the parameters, for a
@@ -269,6 +189,98 @@ class LUCJGradient:
             gam = np.swapaxes(A, -1, -2) @ gL @ np.swapaxes(UL, -1, -2)
             grad[:, index:] = project([c[5][L + 1] for c in circuits], gam)
         return grad
+
+
+class LUCJGradient(GradientHost):
+    """Energy and gradient of the LUCJ ansatz for one (norb, nelec) shape,
+    holding its device buffers (two states and scratch)."""
+
+    def __init__(self, norb: int, nelec: tuple[int, int], *, dtype=torch.complex64, device="cuda",
+                 workers: int = 4):
+        GradientHost.__init__(self, norb)
+        # batches: per-state gates run on `workers` host threads, each with its
+        # own CUDA stream and scratch, so that their launches and host syncs
+        # overlap; the Hamiltonian matvec runs once over the whole batch
+        self.workers = max(1, int(workers))
+        self._tls = threading.local()
+        self._lanes = None
+        self._pool = None
+        self.nelec = tuple(nelec)
+        self.dtype = dtype
+        self.code = _lib.FFGB_C64 if dtype == torch.complex64 else _lib.FFGB_C128
+        d = dim(norb, nelec)
+        self.cur = torch.empty(d, dtype=dtype, device=device)
+        self.lam = torch.empty(d, dtype=dtype, device=device)
+        need = max(_lib.load().ffgb_scratch_bytes(op, self.code, norb, *self.nelec) for op in (0, 1, 3))
+        self.buf = torch.empty(need, dtype=torch.uint8, device=device)
+        self.nbytes = need
+
+    # -- device helpers ----------------------------------------------------
+    def _stream(self):
+        return torch.cuda.current_stream(self.cur.device).cuda_stream
+
+    def _buf(self) -> int:
+        """Scratch of the calling thread (a batch lane's own, else the evaluator's)."""
+        b = getattr(self._tls, "buf", None)
+        return (self.buf if b is None else b).data_ptr()
+
+    def _rotate(self, vec: torch.Tensor, mat: np.ndarray) -> None:
+        m = _lib.cmat(mat)
+        na, nb = self.nelec
+        _lib.call("ffgb_apply_orbital_rotation", vec.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(m),
+                  _lib.dptr(m), self._buf(), self.nbytes, self._stream())
+
+    def _phase(self, vec: torch.Tensor, jaa: np.ndarray, jab: np.ndarray, time: float) -> None:
+        aa, ab = _lib.rmat(jaa), _lib.rmat(jab)
+        na, nb = self.nelec
+        _lib.call("ffgb_apply_diag_coulomb_evolution", vec.data_ptr(), self.code, self.norb, na, nb,
+                  _lib.dptr(aa), _lib.dptr(ab), _lib.dptr(aa), float(time), 0, None, None, self._buf(),
+                  self.nbytes, self._stream())
+
+    def _density(self, name: str, x: torch.Tensor, y: torch.Tensor, blocks: int) -> np.ndarray:
+        out = np.zeros(2 * blocks * self.norb * self.norb)
+        na, nb = self.nelec
+        _lib.call(name, x.data_ptr(), y.data_ptr(), self.code, self.norb, na, nb, _lib.dptr(out),
+                  self._buf(), self.nbytes, self._stream())
+        return out.view(np.complex128).reshape(blocks, self.norb, self.norb)
+
+    # -- energy and gradient -------------------------------------------------
+    def _forward(self, cur: torch.Tensor, V, jaa, jab, L: int) -> None:
+        """psi from the Hartree-Fock state."""
+        _lib.call("ffgb_hartree_fock", cur.data_ptr(), self.code, cur.numel(), self._stream())
+        for k in range(1, L + 1):
+            self._rotate(cur, V[k])
+            self._phase(cur, jaa[k], jab[k], -1.0)
+        self._rotate(cur, V[L + 1])
+
+    def _backward(self, cur: torch.Tensor, lam: torch.Tensor, V, jaa, jab, L: int):
+        """Undo the gates on psi and lambda; generator gradients of the V_j and
+        pair densities at the D_k.  Every gate's densities go to one device
+        buffer (ffgb_gate_densities, no synchronization) that is read back
+        once at the end."""
+        norb = self.norb
+        na, nb = self.nelec
+        n2 = norb * norb
+        dens = torch.empty((L + 2, 10 * n2), dtype=torch.float64, device=cur.device)
+        for j in range(L + 1, 0, -1):
+            vd = V[j].conj().T
+            self._rotate(cur, vd)
+            self._rotate(lam, vd)
+            _lib.call("ffgb_gate_densities", lam.data_ptr(), cur.data_ptr(), self.code, norb, na, nb, int(j > 1),
+                      dens[j].data_ptr(), self._buf(), self.nbytes, self._stream())
+            if j > 1:
+                k = j - 1
+                self._phase(cur, jaa[k], jab[k], 1.0)
+                self._phase(lam, jaa[k], jab[k], 1.0)
+        h = dens.cpu().numpy()
+        gamma = [None] * (L + 2)
+        pdens = [None] * (L + 1)
+        for j in range(1, L + 2):
+            blk = h[j].view(np.complex128).reshape(5, norb, norb)
+            gamma[j] = blk[0] + blk[1]
+            if j > 1:
+                pdens[j - 1] = blk[2:5].copy()
+        return gamma, pdens
 
     def _vdot(self, x: torch.Tensor, y: torch.Tensor) -> float:
         e = np.zeros(2)

@@ -1,4 +1,4 @@
-"""Resident evaluator: LUCJ energies of small shapes served by a persistent kernel.
+"""Resident evaluator: LUCJ energies and gradients of small shapes served by a persistent kernel.
 
 ``ResidentEvaluator`` wraps the ``ffgb_resident_*`` entry points.  One
 persistent kernel takes requests from a queue in host-mapped memory; each of
@@ -49,6 +49,8 @@ class ResidentEvaluator:
         _lib.check(lib.ffgb_resident_open(int(n_slots), int(n_ctas), float(idle_seconds), ctypes.byref(h)))
         self._h = h
         self._hams: dict[int, tuple[int, object]] = {}  # id(ham) -> (ham_id, ham kept alive)
+        self._grad_hosts: dict = {}  # norb -> GradientHost
+        self._grad_jobs: dict = {}  # ticket -> what the chain rule needs at collection
 
     def _ham_id(self, ham: DoubleFactorizedHamiltonian) -> int:
         got = self._hams.get(id(ham))
@@ -106,6 +108,66 @@ class ResidentEvaluator:
         """Submit every operator, then wait for all the energies."""
         tickets = [self.submit(u, ham, nelec) for u in ucjs]
         return np.array([self.wait(t, timeout) for t in tickets])
+
+    # -- gradients -----------------------------------------------------------
+    def _host(self, norb: int):
+        from ffsim_gb300.gradient import GradientHost
+
+        h = self._grad_hosts.get(norb)
+        if h is None:
+            h = self._grad_hosts[norb] = GradientHost(norb)
+        return h
+
+    def submit_grad(self, params: np.ndarray, n_reps: int, ham: DoubleFactorizedHamiltonian,
+                    nelec: tuple[int, int], *, with_final_orbital_rotation: bool = False) -> int:
+        """Queue the energy and adjoint gradient of the spin-balanced UCJ
+        operator with these parameters (the ``from_parameters`` layout) under
+        ``ham``; collect with ``poll_grad``.  The kernel runs the circuit, the
+        Hamiltonian matvec and the backward pass with its densities; the chain
+        rule to the parameters runs on the host at collection."""
+        norb = ham.norb
+        if not accepts(norb, n_reps):
+            raise NotImplementedError(f"the resident kernel takes norb <= {MAX_NORB} and n_reps <= {MAX_REPS}")
+        params = np.asarray(params, dtype=float)
+        n = UCJOpSpinBalanced.n_params(norb, n_reps, with_final_orbital_rotation=with_final_orbital_rotation)
+        if params.shape != (n,):
+            raise ValueError(f"expected {n} parameters, got shape {params.shape}")
+        circ = self._host(norb)._circuits(params[None, :], n_reps, with_final_orbital_rotation)[0]
+        V = np.ascontiguousarray(np.stack(circ[2][1:]), dtype=np.complex128)
+        J = np.ascontiguousarray(np.stack([np.stack([circ[3][k], circ[4][k]]) for k in range(1, n_reps + 1)]),
+                                 dtype=np.float64)
+        ticket = ctypes.c_longlong(-1)
+        _lib.call("ffgb_resident_submit_grad", self._h, self._ham_id(ham), norb, int(nelec[0]), int(nelec[1]),
+                  n_reps, V.ctypes.data_as(_lib._dp), _lib.dptr(J), ctypes.byref(ticket))
+        self._grad_jobs[ticket.value] = (n, n_reps, with_final_orbital_rotation, circ, norb)
+        return ticket.value
+
+    def poll_grad(self, ticket: int) -> tuple[float, np.ndarray] | None:
+        """(energy, gradient) once the gradient request has finished, None
+        while it runs; CancelledError if it was cancelled."""
+        n, L, with_final, circ, norb = self._grad_jobs[ticket]
+        e = ctypes.c_double(0.0)
+        dens = np.zeros(2 * (L + 1) * 5 * norb * norb)
+        status = _lib.load().ffgb_resident_poll_densities(self._h, int(ticket), ctypes.byref(e), _lib.dptr(dens))
+        if status == _lib.FFGB_PENDING:
+            return None
+        del self._grad_jobs[ticket]
+        _lib.check(status)
+        blocks = dens.view(np.complex128).reshape(L + 1, 5, norb, norb)
+        gamma = [None] + [blocks[j - 1, 0] + blocks[j - 1, 1] for j in range(1, L + 2)]
+        pdens = [None] + [blocks[j, 2:5].copy() for j in range(1, L + 1)]
+        grad = self._host(norb)._chains(n, [circ], [(gamma, pdens)], L, with_final)[0]
+        return e.value, grad
+
+    def wait_grad(self, ticket: int, timeout: float = 60.0) -> tuple[float, np.ndarray]:
+        deadline = time.perf_counter() + timeout
+        while True:
+            got = self.poll_grad(ticket)
+            if got is not None:
+                return got
+            if time.perf_counter() > deadline:
+                raise TimeoutError(f"resident request {ticket} did not finish within {timeout} s")
+            time.sleep(20e-6)
 
     def cancel(self, ticket: int) -> None:
         _lib.call("ffgb_resident_cancel", self._h, int(ticket))

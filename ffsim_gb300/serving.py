@@ -26,10 +26,12 @@ engine whose call raised (other than a cancellation) is not reused.  A batch
 whose requests are all cancelled stops within about two Hamiltonian terms
 (``ffgb_control``).
 
-Energy requests of small shapes (norb <= 8, n_reps <= 4) go instead to a
-resident evaluator (``resident.ResidentEvaluator``): one persistent kernel
-that takes them from a queue in host-mapped memory and evaluates each inside
-one CTA, next to the batches on the device.  A resident lane thread submits
+Requests of small shapes (norb <= 8, n_reps <= 4), energies and gradients,
+go instead to a resident evaluator (``resident.ResidentEvaluator``): one
+persistent kernel that takes them from a queue in host-mapped memory and
+evaluates each inside one CTA, next to the batches on the device (for a
+gradient the kernel runs the circuit, the Hamiltonian matvec and the backward
+pass with its densities; the chain rule runs on the host at collection).  A resident lane thread submits
 them in arrival order while the queue has room and collects the results;
 cancellation and deadlines apply to them as to the others.  A request the
 resident kernel cannot plan falls back to the batch path.
@@ -250,7 +252,7 @@ class LUCJServer:
     def _for_resident(self, req: Request) -> bool:
         from ffsim_gb300 import resident as res
 
-        return self.resident and req.kind == "energy" and res.accepts(req.norb, req.n_reps)
+        return self.resident and res.accepts(req.norb, req.n_reps)
 
     def cancel(self, rid: int) -> bool:
         """Cancel a request: a pending one is dropped at once, a running one
@@ -512,8 +514,11 @@ class LUCJServer:
                 for i, req in enumerate(todo):
                     start = time.perf_counter()
                     try:
-                        op = UCJOpSpinBalanced.from_parameters(req.params, norb=req.norb, n_reps=req.n_reps)
-                        ticket = ev.submit(op, req.ham, req.nelec)
+                        if req.kind == "gradient":
+                            ticket = ev.submit_grad(req.params, req.n_reps, req.ham, req.nelec)
+                        else:
+                            op = UCJOpSpinBalanced.from_parameters(req.params, norb=req.norb, n_reps=req.n_reps)
+                            ticket = ev.submit(op, req.ham, req.nelec)
                     except MemoryError:
                         with self._cv:  # the queue is full: the rest wait for collected results
                             self._res_pending.extendleft(reversed(todo[i:]))
@@ -536,12 +541,16 @@ class LUCJServer:
                 done = []
                 for ticket, (req, start) in list(self._res_inflight.items()):
                     try:
-                        e = ev.poll(ticket)
+                        if req.kind == "gradient":
+                            got = ev.poll_grad(ticket)
+                        else:
+                            e = ev.poll(ticket)
+                            got = None if e is None else (e, None)
                     except BaseException as exc:  # noqa: BLE001
                         done.append((ticket, req, start, None, exc))
                         continue
-                    if e is not None:
-                        done.append((ticket, req, start, (e, None), None))
+                    if got is not None:
+                        done.append((ticket, req, start, got, None))
                 if done:
                     with self._cv:
                         for ticket, req, start, value, err in done:

@@ -381,6 +381,23 @@ int ffgb_resident_submit(ffgb_resident* r, int ham_id, int norb, int n_alpha, in
 /* FFGB_OK with *energy once the request has finished (its slot is then free
  * again), FFGB_PENDING before, FFGB_ERR_CANCELLED if it was cancelled. */
 int ffgb_resident_poll(ffgb_resident* r, long long ticket, double* energy);
+/* Queue the device part of an adjoint gradient (norb <= 8, n_reps <= 4): the
+ * circuit of the merged rotations rots (n_reps + 1 complex norb x norb
+ * matrices V_1 .. V_{n_reps+1}: psi = W(V_{L+1}) D_L W(V_L) ... D_1 W(V_1)
+ * |HF>) and phase gates D_k = exp(i sum J_k n n / 2) (ucj_dcm as in
+ * ffgb_lucj_energy), then lambda = (H - c) psi, the energy, and the gates
+ * undone on psi and lambda with the densities of every gate (as
+ * ffgb_gate_densities).  The chain rule to the parameters is the caller's
+ * (ffsim_gb300.gradient does it on the host).  No counterpart in the
+ * reference, which differentiates by finite differences
+ * (python/ffsim/optimize/_util.py:60-110). */
+int ffgb_resident_submit_grad(ffgb_resident* r, int ham_id, int norb, int n_alpha, int n_beta, int n_reps,
+                              const double* rots, const double* ucj_dcm, long long* ticket);
+/* Collect a gradient request: *energy and dens[(n_reps + 1) x 5 x norb x
+ * norb] complex (per gate j = 1 .. n_reps + 1: the transition one-body
+ * densities of the alpha and beta sectors, then the pair densities aa, ab,
+ * bb; zero for j = 1).  Return codes as ffgb_resident_poll. */
+int ffgb_resident_poll_densities(ffgb_resident* r, long long ticket, double* energy, double* dens);
 /* Ask the kernel to stop a request: it checks between gates and terms. */
 int ffgb_resident_cancel(ffgb_resident* r, long long ticket);
 /* Launch the kernel now if it is not running (it otherwise starts with the

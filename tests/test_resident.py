@@ -1,6 +1,7 @@
 """Resident evaluator (persistent kernel, host-mapped work queue): energies
-against the batch path and the FP64 oracle, results independent of the mix,
-the bounded wait for work, cancellation and a full queue."""
+against the complex128 path and the FP64 oracle, gradients against the batch
+path and finite differences, results independent of the mix, the bounded
+wait for work, cancellation and a full queue."""
 
 from __future__ import annotations
 
@@ -131,3 +132,69 @@ def test_full_queue_and_invalid_requests():
             r.submit(ucj, ham, (7, 3))
     finally:
         r.close()
+
+
+@pytest.mark.parametrize("norb,nelec,n_reps,final", [(6, (3, 3), 2, False), (8, (4, 4), 1, True), (5, (3, 2), 3, False)])
+def test_gradient_matches_the_batch_path(ev, norb, nelec, n_reps, final):
+    """The resident kernel's energy and adjoint gradient (the circuit, the
+    Hamiltonian matvec and the backward pass on the device, the chain rule on
+    the host) against LUCJGradient's."""
+    from ffsim_gb300.gradient import LUCJGradient
+
+    rng = np.random.default_rng(40 + norb)
+    n = f.UCJOpSpinBalanced.n_params(norb, n_reps, with_final_orbital_rotation=final)
+    params = rng.normal(scale=0.4, size=n)
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=norb, seed=norb + 50)
+    e, g = ev.wait_grad(ev.submit_grad(params, n_reps, ham, nelec, with_final_orbital_rotation=final))
+    e_ref, g_ref = LUCJGradient(norb, nelec, dtype=torch.complex64).value_and_grad(
+        params, n_reps, ham, with_final_orbital_rotation=final)
+    assert abs(e - e_ref) <= 1e-6
+    assert np.linalg.norm(g - g_ref) <= 1e-4 * np.linalg.norm(g_ref)
+
+
+def test_gradient_against_finite_differences(ev):
+    """Every coordinate of the resident gradient against central differences
+    of the complex128 energy (h = 1e-5)."""
+    norb, nelec, n_reps = 4, (2, 2), 2
+    rng = np.random.default_rng(3)
+    n = f.UCJOpSpinBalanced.n_params(norb, n_reps)
+    params = rng.normal(scale=0.5, size=n)
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=4, seed=8)
+    _, g = ev.wait_grad(ev.submit_grad(params, n_reps, ham, nelec))
+
+    def energy(p):
+        op = f.UCJOpSpinBalanced.from_parameters(p, norb=norb, n_reps=n_reps)
+        return f.lucj_energy(op, ham, norb, nelec, dtype=torch.complex128)
+
+    h = 1e-5
+    fd = np.array([(energy(params + h * np.eye(n)[i]) - energy(params - h * np.eye(n)[i])) / (2 * h)
+                   for i in range(n)])
+    assert np.linalg.norm(g - fd) <= 1e-4 * np.linalg.norm(fd)
+
+
+def test_gradient_requests_mix_with_energies(ev):
+    """Energies and gradients of several shapes in one queue: each equals the
+    same request alone, bit for bit."""
+    reqs = []
+    for i in range(12):
+        norb, nelec, n_reps = SHAPES[i % 4]
+        ucj, ham = _case(norb, n_reps, seed=900 + i)
+        if i % 3 == 0:
+            reqs.append(("grad", ucj.to_parameters(), n_reps, ham, nelec))
+        else:
+            reqs.append(("energy", ucj, n_reps, ham, nelec))
+
+    def submit(r):
+        if r[0] == "grad":
+            return ev.submit_grad(r[1], r[2], r[3], r[4])
+        return ev.submit(r[1], r[3], r[4])
+
+    def wait(r, t):
+        if r[0] == "grad":
+            e, g = ev.wait_grad(t)
+            return (e, tuple(g))
+        return ev.wait(t)
+
+    alone = [wait(r, submit(r)) for r in reqs]
+    tickets = [submit(r) for r in reqs]
+    assert [wait(r, t) for r, t in zip(reqs, tickets)] == alone

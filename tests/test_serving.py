@@ -118,6 +118,15 @@ class _FakeResident:
             del self.inflight[ticket]
             return norb + 0.5
 
+    def submit_grad(self, params, n_reps, ham, nelec):
+        class _Op:  # n_params = n_reps (2 norb^2 + norb) without a final rotation
+            norb = int(round((-1 + (1 + 8 * len(params) / n_reps) ** 0.5) / 4))
+        return self.submit(_Op, ham, nelec)
+
+    def poll_grad(self, ticket):
+        e = self.poll(ticket)
+        return None if e is None else (e, np.full(3, e))
+
     def cancel(self, ticket):
         with self.lock:
             self.cancelled.add(ticket)
@@ -325,7 +334,7 @@ def _mixed(n, seed=0):
 
 
 def _is_resident(req):
-    return req.kind == "energy" and req.norb <= 8
+    return req.norb <= 8
 
 
 def test_resident_lane_takes_small_energy_requests():
@@ -409,9 +418,12 @@ def test_results_alone_and_in_the_mix(cuda):
     alone = {}
     ev = ResidentEvaluator(n_slots=8, n_ctas=1)
     for r in reqs:
-        if r.kind == "energy" and accepts(r.norb, r.n_reps):  # served by the resident kernel
-            op = UCJOpSpinBalanced.from_parameters(r.params, norb=r.norb, n_reps=r.n_reps)
-            alone[r.rid] = (ev.wait(ev.submit(op, r.ham, r.nelec)), None)
+        if accepts(r.norb, r.n_reps):  # served by the resident kernel
+            if r.kind == "gradient":
+                alone[r.rid] = ev.wait_grad(ev.submit_grad(r.params, r.n_reps, r.ham, r.nelec))
+            else:
+                op = UCJOpSpinBalanced.from_parameters(r.params, norb=r.norb, n_reps=r.n_reps)
+                alone[r.rid] = (ev.wait(ev.submit(op, r.ham, r.nelec)), None)
             continue
         eng = _Engine(r.kind, r.norb, r.nelec, 1, torch.complex64)
         alone[r.rid] = eng.run([r], None)[0]
@@ -422,7 +434,7 @@ def test_results_alone_and_in_the_mix(cuda):
     srv.close()
     assert all(r.ok for r in res)
     assert max(srv.batch_sizes) > 1
-    assert srv.resident_served == sum(r.kind == "energy" and r.norb <= 8 for r in reqs) > 0
+    assert srv.resident_served == sum(r.norb <= 8 for r in reqs) > 0
     for r in res:
         e, g = alone[r.rid]
         assert abs(r.energy - e) <= 1e-9, (r.rid, r.energy, e)
