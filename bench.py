@@ -684,6 +684,30 @@ def run_resident(args) -> None:
     torch.cuda.synchronize()
     s1 = time.perf_counter()
     e128 = [f.lucj_energy(op, ham, norb, nelec, dtype=torch.complex128) for op in ops[:8]]
+    # gradients: the resident kernel (the chain rule on the host at collection)
+    # against LUCJGradient's batch path, on the same parameter vectors
+    from ffsim_gb300.gradient import LUCJGradient
+
+    m_grad = min(n, 256)
+    params = [op.to_parameters() for op in ops[:m_grad]]
+    ev = ResidentEvaluator(n_slots=max(m_grad, 16), n_ctas=args.resident_ctas, idle_seconds=2.0)
+    ev.wait_grad(ev.submit_grad(params[0], 2, ham, nelec))
+    g0 = time.perf_counter()
+    gt = [ev.submit_grad(p, 2, ham, nelec) for p in params]
+    grads = [ev.wait_grad(t)[1] for t in gt]
+    g1 = time.perf_counter()
+    ev.close()
+    lg = LUCJGradient(norb, nelec)
+    lg.value_and_grad_batch(np.stack(params[: args.max_batch]), 2, ham)
+    torch.cuda.synchronize()
+    b2 = time.perf_counter()
+    gb = []
+    for i in range(0, m_grad, args.max_batch):
+        gb.extend(lg.value_and_grad_batch(np.stack(params[i:i + args.max_batch]), 2, ham)[1])
+    torch.cuda.synchronize()
+    b3 = time.perf_counter()
+    lg.close()
+    grad_rel = max(float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(grads, gb))
     print(json.dumps({
         "metric": f"resident-kernel LUCJ energy evals/s, norb={norb} {nelec}, n_reps=2, DF rank {2 * norb}",
         "value": res_rate, "unit": "evals/s", "requests": n, "ctas": args.resident_ctas,
@@ -692,6 +716,8 @@ def run_resident(args) -> None:
         "single_path_evals_per_s": m / (s1 - s0),
         "max_abs_dE_vs_c128": float(max(abs(a - b) for a, b in zip(energies[:8], e128))),
         "max_abs_dE_vs_batch_c64": float(np.max(np.abs(np.array(energies) - np.array(eb)))),
+        "gradient": {"resident_evals_per_s": m_grad / (g1 - g0), "batch_path_evals_per_s": m_grad / (b3 - b2),
+                     "requests": m_grad, "max_rel_diff_vs_batch_path": grad_rel},
         "dtype": "c64", "data": "synthetic"}), flush=True)
 
 
