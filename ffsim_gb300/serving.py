@@ -570,7 +570,7 @@ def _default_resident():
 
     # the kernel lives only while requests come (it exits 5 ms after the
     # last), so between bursts it holds no SM resources the batches could use
-    return ResidentEvaluator(n_slots=1024, n_ctas=8, idle_seconds=0.005)
+    return ResidentEvaluator(n_slots=256, n_ctas=8, idle_seconds=0.005)
 
 
 def latency_stats(results: list[Result]) -> dict:
