@@ -345,6 +345,25 @@ __device__ __forceinline__ unsigned dither_seed(unsigned long long col, unsigned
 }  // namespace ffgb
 
 namespace ffgb {
+// The two halves of rot_pair, for a pair whose members sit in different
+// threads: x <- c x + s y (the thread holding x) and y <- -conj(s) x + c y
+// (the thread holding y), with the same operations and rounding as rot_pair
+// with plain or dithered coefficients.
+__device__ __forceinline__ void rot_half_x(float2& x, float2 y, float c, float sr, float si) {
+  const float2 ys = make_float2(y.y, y.x);
+  float2 nx = __fmul2_rn(make_float2(c, c), x);
+  nx = __ffma2_rn(make_float2(sr, sr), y, nx);
+  nx = __ffma2_rn(make_float2(-si, si), ys, nx);
+  x = nx;
+}
+__device__ __forceinline__ void rot_half_y(float2& y, float2 x, float c, float sr, float si) {
+  const float2 xs = make_float2(x.y, x.x);
+  float2 ny = __fmul2_rn(make_float2(c, c), y);
+  ny = __ffma2_rn(make_float2(-sr, -sr), x, ny);
+  ny = __ffma2_rn(make_float2(-si, si), xs, ny);
+  y = ny;
+}
+
 #include "windows_gen.cuh"
 }
 

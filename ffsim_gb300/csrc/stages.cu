@@ -259,6 +259,20 @@ int cs_pass_tables(int norb, int nocc, int lo, int hh, const CsPass** out) {
   return FFGB_OK;
 }
 
+// Groups of 5 and 6 active sites with dithered coefficients run on two lanes
+// per column (cs_pair_kernel, 64-column tiles).
+template <int M>
+int launch_cs_pair(const CsStageParams& P0, long long n_chunks, cudaStream_t st) {
+  CsStageParams P = P0;
+  P.tiles = (int)((P.ncols + STAGE_THREADS / 2 - 1) / (STAGE_THREADS / 2));
+  const long long grid = n_chunks * P.tiles;
+  if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
+  cs_pair_kernel<M, 2><<<(unsigned)grid, STAGE_THREADS, 0, st>>>(P);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+
 template <int M>
 int launch_cs(const CsStageParams& P, int grid, int mode, cudaStream_t st) {
   if (mode == 0)
@@ -307,6 +321,11 @@ int cs_stage(float2* x, long long ld, long long ncols, int norb, int nocc, int l
     const long long grid = (long long)((P.n_groups + P.gpc - 1) / P.gpc) * P.tiles;
     if (grid <= 0) continue;
     if (grid > 0x7fffffffLL) return fail(FFGB_ERR_UNSUPPORTED, "cross-half stage grid too large");
+    if (mode == 2 && k.m >= 5) {
+      const long long n_chunks = (P.n_groups + P.gpc - 1) / P.gpc;
+      FFGB_TRY(k.m == 5 ? launch_cs_pair<5>(P, n_chunks, ls) : launch_cs_pair<6>(P, n_chunks, ls));
+      continue;
+    }
     switch (k.m) {
       case 1: FFGB_TRY(launch_cs<1>(P, (int)grid, mode, ls)); break;
       case 2: FFGB_TRY(launch_cs<2>(P, (int)grid, mode, ls)); break;

@@ -373,6 +373,76 @@ __global__ void __launch_bounds__(STAGE_THREADS, M >= 5 ? 3 : (M >= 4 ? 4 : 6))
   }
 }
 
+// Groups with M = 5 or 6 active sites on two lanes per column: lane 2c holds
+// the members with the last active site's bit clear, lane 2c + 1 the others,
+// so a thread keeps 2^(M-1) amplitudes (four CTAs per SM instead of three).
+// The sites below the last act within a lane; the last one pairs member j of
+// the even lane with member j of the odd lane through a shuffle.  Both lanes
+// of a column draw the same dithered coefficients, in the same order as
+// cs_rotate, and the arithmetic of every pair is rot_pair's, so the result
+// equals cs_stage_kernel's.  A CTA covers 64 columns (P.tiles counts 64-column
+// tiles); columns beyond ncols run on zeros and store nothing.
+template <int M, int MODE>
+__global__ void __launch_bounds__(STAGE_THREADS, 4) cs_pair_kernel(const __grid_constant__ CsStageParams P) {
+  static_assert(M >= 2 && MODE != 1, "plain or dithered coefficients, at least two sites");
+  constexpr int NM = 1 << M, NH = NM / 2, STRIDE = 1 + NM, TL = M - 1;
+  constexpr int GPC = CS_MAX_GPC / 2;
+  const int chunk = blockIdx.x / P.tiles, tile = blockIdx.x - chunk * P.tiles;
+  const int half = threadIdx.x & 1;
+  const long long col = (long long)tile * (STAGE_THREADS / 2) + (threadIdx.x >> 1);
+  const int g0 = chunk * P.gpc, g1 = min(g0 + P.gpc, P.n_groups);
+  __shared__ int sent[GPC * STRIDE];
+  const int n_ent = (g1 - g0) * STRIDE;
+  const int* src = P.tab + (long long)g0 * STRIDE;
+  for (int i = threadIdx.x; i < n_ent; i += STAGE_THREADS) sent[i] = src[i];
+  __syncthreads();
+  const bool active = col < P.ncols;
+  const unsigned rng = dither_seed((unsigned long long)(P.col_period ? col % P.col_period : col), P.salt);
+  float2* xc = P.x + (active ? col : 0);
+  const long long ld = P.ld;
+  for (int g = g0; g < g1; ++g) {
+    const int* e = sent + (g - g0) * STRIDE;
+    const int sites = e[0];
+    const int* em = e + 1;
+    float2 v[NH];
+#pragma unroll
+    for (int j = 0; j < NH; ++j)
+      v[j] = active ? xc[(long long)(em[half * NH + j] & 0xffffff) * ld] : make_float2(0.f, 0.f);
+    unsigned r = rng;
+#pragma unroll
+    for (int t = 0; t < TL; ++t) {
+      const int site = (sites >> (4 * t)) & 15;
+      float c, sr, si, cl, srl, sil;
+      win_coef<MODE>(P.gp, P.gl, P.gt, site, r, c, sr, si, cl, srl, sil);
+#pragma unroll
+      for (int j = 0; j < NH; ++j) {
+        if (j & (1 << t)) continue;
+        const float sg = ((em[half * NH + j] >> (24 + t)) & 1) ? -1.f : 1.f;
+        rot_pair<false>(v[j], v[j | (1 << t)], c, sg * sr, sg * si, 0.f, 0.f, 0.f);
+      }
+    }
+    {
+      const int site = (sites >> (4 * TL)) & 15;
+      float c, sr, si, cl, srl, sil;
+      win_coef<MODE>(P.gp, P.gl, P.gt, site, r, c, sr, si, cl, srl, sil);
+#pragma unroll
+      for (int j = 0; j < NH; ++j) {
+        // the sign is read on the member whose lower orbital is occupied: the even lane's
+        const float sg = ((em[j] >> (24 + TL)) & 1) ? -1.f : 1.f;
+        const float2 o = make_float2(__shfl_xor_sync(0xffffffffu, v[j].x, 1), __shfl_xor_sync(0xffffffffu, v[j].y, 1));
+        if (half == 0)
+          rot_half_x(v[j], o, c, sg * sr, sg * si);
+        else
+          rot_half_y(v[j], o, c, sg * sr, sg * si);
+      }
+    }
+    if (active) {
+#pragma unroll
+      for (int j = 0; j < NH; ++j) xc[(long long)(em[half * NH + j] & 0xffffff) * ld] = v[j];
+    }
+  }
+}
+
 // out[c][r] = in[r][c] * row_ph[r] * col_ph[c] (phase tables optional), row
 // strides ld_in / ld_out.  A CTA moves a 64-row x 32-column tile through
 // shared memory (padded rows: no bank conflicts); each thread has eight loads
