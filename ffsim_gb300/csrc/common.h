@@ -133,5 +133,8 @@ template <typename T>
 int launch_row_scale(void* x, long long rows, long long ld, const void* ph, cudaStream_t st);
 template <typename T>
 int launch_axpy(const void* x, void* y, long long n, double a, cudaStream_t st);
+// y += ph[r] * x for rows r of length ld (ph nullptr: y += x).
+template <typename T>
+int launch_row_axpy(const void* x, void* y, long long rows, long long ld, const void* ph, cudaStream_t st);
 
 }  // namespace ffgb

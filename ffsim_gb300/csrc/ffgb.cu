@@ -409,6 +409,14 @@ static std::vector<cd> dagger(const std::vector<cd>& m, int n) {
     for (int c = 0; c < n; ++c) v[(size_t)r * n + c] = std::conj(m[(size_t)c * n + r]);
   return v;
 }
+// V diag(d): column j of V times d[j].
+static std::vector<cd> scale_cols(const std::vector<cd>& v, const std::vector<cd>& d, int n) {
+  std::vector<cd> o(v);
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) o[(size_t)r * n + c] *= d[c];
+  return o;
+}
+
 static std::vector<cd> matmul(const std::vector<cd>& a, const std::vector<cd>& b, int n) {
   std::vector<cd> v((size_t)n * n, cd(0));
   for (int r = 0; r < n; ++r)
@@ -441,6 +449,25 @@ static bool staged(const SectorPlan* a, const SectorPlan* b) {
   if (a && a->kind != PLAN_CSD) return false;
   if (b && b->kind != PLAN_CSD) return false;
   return true;
+}
+
+// Plans of W(U^dag) and W(U) around a diagonal operator Z.  The stage path's
+// plan of U^dag = diag(d) N leaves out its final orbital phases: they commute
+// with Z, and W(U) W(diag(d)) = W(U diag(d)), so the second plan is that of
+// U diag(d) and no pass over the state applies d.  Returns whether both plans
+// run on the stage path (otherwise pu is the plan of U itself).
+template <typename T>
+static int sandwich_plans(int norb, const std::vector<cd>& rot, SectorPlan& pd, SectorPlan& pu, bool* stage) {
+  FFGB_TRY(make_plan<T>(norb, dagger(rot, norb), pd));
+  *stage = false;
+  if (staged<T>(&pd, nullptr)) {
+    FFGB_TRY(make_plan<T>(norb, scale_cols(rot, pd.diag, norb), pu));
+    if (staged<T>(&pu, nullptr)) {
+      *stage = true;
+      return FFGB_OK;
+    }
+  }
+  return make_plan<T>(norb, rot, pu);
 }
 
 // Per-string table of a plan's final orbital phases (nullptr when they are all 1),
@@ -956,16 +983,15 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
   }
   if (!rot) return diag_rows<T>(vec, out, norb, na, nb, spec, accumulate != 0, scr, st);
   SectorPlan pd, pu;
-  FFGB_TRY(make_plan<T>(norb, dagger(*rot, norb), pd));
-  FFGB_TRY(make_plan<T>(norb, *rot, pu));
+  bool stage = false;
+  FFGB_TRY(sandwich_plans<T>(norb, *rot, pd, pu, &stage));
   const size_t S = (size_t)da * db * sizeof(C);
   void* t1 = scr.take(S);
   void* t2 = scr.take(S);
   if (!t1 || !t2) return fail(FFGB_ERR_OOM, "scratch too small (needs two states)");
-  if (staged<T>(&pd, &pu)) {
-    const void* fbp = nullptr;
-    FFGB_TRY(staged_rotate(vec, t1, t2, norb, na, nb, &pd, &pd, true, true, 4, scr, st, &fbp));
-    if (fbp) FFGB_TRY(launch_row_scale<float>(t2, db, da, fbp, st));
+  if (stage) {
+    // W(N) without the phases of the U^dag plan, which pu carries
+    FFGB_TRY(staged_rotate(vec, t1, t2, norb, na, nb, &pd, &pd, false, true, 4, scr, st));
     FFGB_TRY(diag_pass_t<T>(t2, norb, na, nb, spec, OUT_STORE, nullptr, nullptr, scr, st));
     const void *fa = nullptr, *fb = nullptr;
     FFGB_TRY(phase_table(&pu, norb, na, scr, st, &fa));
@@ -977,8 +1003,7 @@ static int rotated_matvec_impl(const void* vec, void* out, int norb, int na, int
       return fa ? launch_row_scale<float>(out, da, db, fa, st) : FFGB_OK;
     }
     FFGB_TRY(stage_sector(t1, t1, norb, na, db, db, pu, 10, st));
-    if (fa) FFGB_TRY(launch_row_scale<float>(t1, da, db, fa, st));
-    return launch_axpy<float>(t1, out, da * db, 1.0, st);
+    return launch_row_axpy<float>(t1, out, da, db, fa, st);
   }
   PassArgs<T> A;
   A.norb = norb;
@@ -1368,21 +1393,17 @@ static int stack_rotated_matvec(const void* Y, void* Yacc, void* Y1, void* T, co
   const size_t mark = scr.off;
   const long long ya = d.n * d.pb, tb = d.n * d.pa;  // row lengths of the two layouts
   const void *fa = nullptr, *fb = nullptr;
-  FFGB_TRY(phase_table(&pd, norb, na, scr, st, &fa));
-  FFGB_TRY(phase_table(&pd, norb, nb, scr, st, &fb));
+  // the final phases of pd are carried by pu (sandwich_plans)
   FFGB_TRY(stage_rotate_rows(Y, Y1, norb, na, ya, ya, pd, stack_opts(8, d.pb), st));
-  FFGB_TRY(launch_transpose_stacked<float>(Y1, T, d.da, d.db, d.n, d.pb, d.pa, fa, st));
+  FFGB_TRY(launch_transpose_stacked<float>(Y1, T, d.da, d.db, d.n, d.pb, d.pa, nullptr, st));
   FFGB_TRY(stage_rotate_rows(T, T, norb, nb, tb, tb, pd, stack_opts(9, d.pa), st));
-  if (fb) FFGB_TRY(launch_row_scale<float>(T, d.db, tb, fb, st));
   FFGB_TRY(diag_rows<float>(T, T, norb, nb, na, spec.transposed(), false, scr, st, nullptr, nullptr, d.n));
-  scr.off = mark;
   FFGB_TRY(phase_table(&pu, norb, na, scr, st, &fa));
   FFGB_TRY(phase_table(&pu, norb, nb, scr, st, &fb));
   FFGB_TRY(stage_rotate_rows(T, T, norb, nb, tb, tb, pu, stack_opts(11, d.pa), st));
   FFGB_TRY(launch_transpose_stacked<float>(T, Y1, d.db, d.da, d.n, d.pa, d.pb, fb, st));
   FFGB_TRY(stage_rotate_rows(Y1, Y1, norb, na, ya, ya, pu, stack_opts(10, d.pb), st));
-  if (fa) FFGB_TRY(launch_row_scale<float>(Y1, d.da, ya, fa, st));
-  FFGB_TRY(launch_axpy<float>(Y1, Yacc, d.da * ya, 1.0, st));
+  FFGB_TRY(launch_row_axpy<float>(Y1, Yacc, d.da, ya, fa, st));
   scr.off = mark;
   return FFGB_OK;
 }
@@ -1436,9 +1457,15 @@ static int stack_plans(int dtype, int norb, int na, int nb, const std::vector<Te
   pd.resize(terms.size());
   pu.resize(both_ways ? terms.size() : 0);
   for (size_t k = 0; k < terms.size(); ++k) {
-    FFGB_TRY(make_plan<float>(norb, dagger(terms[k].rot, norb), pd[k]));
-    if (both_ways) FFGB_TRY(make_plan<float>(norb, terms[k].rot, pu[k]));
-    if (!staged<float>(&pd[k], &pd[k]) || (both_ways && !staged<float>(&pu[k], &pu[k]))) stacked = false;
+    bool stage = false;
+    if (both_ways) {
+      // pu[k] carries the final phases of pd[k] (sandwich_plans)
+      FFGB_TRY(sandwich_plans<float>(norb, terms[k].rot, pd[k], pu[k], &stage));
+    } else {
+      FFGB_TRY(make_plan<float>(norb, dagger(terms[k].rot, norb), pd[k]));
+      stage = staged<float>(&pd[k], nullptr);
+    }
+    if (!stage) stacked = false;
   }
   return FFGB_OK;
 }

@@ -668,6 +668,19 @@ template int launch_row_scale<float>(void*, long long, long long, const void*, c
 template int launch_row_scale<double>(void*, long long, long long, const void*, cudaStream_t);
 
 template <typename T>
+int launch_row_axpy(const void* x, void* y, long long rows, long long ld, const void* ph, cudaStream_t st) {
+  using Cx = typename CT<T>::type;
+  const long long n = rows * ld;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8192));
+  row_axpy_kernel<Cx><<<blocks, 256, 0, st>>>((const Cx*)x, (Cx*)y, rows, ld, (const Cx*)ph);
+  count_launch();
+  FFGB_CUDA(cudaGetLastError());
+  return FFGB_OK;
+}
+template int launch_row_axpy<float>(const void*, void*, long long, long long, const void*, cudaStream_t);
+template int launch_row_axpy<double>(const void*, void*, long long, long long, const void*, cudaStream_t);
+
+template <typename T>
 int launch_axpy(const void* x, void* y, long long n, double a, cudaStream_t st) {
   const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8192));
   axpy_kernel<T><<<blocks, 256, 0, st>>>((const typename CT<T>::type*)x, (typename CT<T>::type*)y, n, (T)a,

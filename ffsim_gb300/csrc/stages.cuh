@@ -514,6 +514,21 @@ __global__ void row_scale_kernel(C* __restrict__ x, long long rows, long long ld
     x[i] = cmul(x[i], ph[i / ld]);
 }
 
+// y += ph[row] * x over rows of length ld (ph optional: y += x)
+template <typename C>
+__global__ void row_axpy_kernel(const C* __restrict__ x, C* __restrict__ y, long long rows, long long ld,
+                                const C* __restrict__ ph) {
+  const long long n = rows * ld;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const C v = ph ? cmul(x[i], ph[i / ld]) : x[i];
+    C o = y[i];
+    o.x += v.x;
+    o.y += v.y;
+    y[i] = o;
+  }
+}
+
 // States side by side along the columns ("stacked"): state b of a block of
 // contiguous states x[b][r][c] (rows x cols each) is columns
 // [b * pad, b * pad + cols) of y[r][...] (row stride n_states * pad).

@@ -46,6 +46,29 @@ def test_batch_matvec_matches_per_state(cuda, norb, nelec, dtype_name):
         assert err <= tol, (b, err)
 
 
+@pytest.mark.parametrize("norb, nelec", [(10, (5, 5)), (12, (6, 6)), (14, (7, 6))])
+def test_stage_path_matvec_matches_complex128(cuda, norb, nelec):
+    """complex64 matvecs on the stage path, one state and three side by side,
+    against complex128: each term's W(U) Z W(U^dag) runs with the phases of
+    the U^dag plan carried by the plan of U diag(d) and the last row phases
+    fused into the accumulation."""
+    import torch
+
+    import ffsim_gb300 as f
+
+    ham = f.random.random_df_hamiltonian_normal(norb, rank=3, seed=40 + norb)
+    lin = f.linear_operator(ham, norb, nelec)
+    x = _states(3, f.dim(norb, nelec), torch.complex128, norb, cuda)
+    want = torch.stack([lin @ x[b] for b in range(3)])
+    one = lin @ x[0].to(torch.complex64)
+    many = (lin @ x.to(torch.complex64).T).T
+    scale = float(torch.linalg.vector_norm(want[0]))
+    assert float(torch.linalg.vector_norm(one.to(torch.complex128) - want[0])) <= 1e-5 * scale
+    for b in range(3):
+        err = float(torch.linalg.vector_norm(many[b].to(torch.complex128) - want[b]))
+        assert err <= 1e-5 * float(torch.linalg.vector_norm(want[b])), (b, err)
+
+
 @pytest.mark.parametrize("norb, nelec", STACKED + [(8, (4, 4))])
 @pytest.mark.parametrize("dtype_name", ["complex64", "complex128"])
 def test_batch_energy_matches_per_state(cuda, norb, nelec, dtype_name):
