@@ -116,6 +116,26 @@ def test_stage_sequence_matches_oracle(norb, nocc, n_stages):
     np.testing.assert_allclose(got, o.apply_orbital_rotation(vec, u, norb, nocc), atol=1e-11)
 
 
+@pytest.mark.parametrize("norb, nocc", [(10, 4), (12, 6), (14, 5)])
+def test_sandwich_plans_carry_the_phases(norb, nocc):
+    """The stage-path matvec term W(U) Z W(U^dag): with the plan of U^dag =
+    diag(d) N run without its final phases, the plan of U diag(d) gives the
+    same vector (Z diagonal in the strings, so it commutes with W(diag(d)))."""
+    rng = np.random.default_rng(norb * 13 + nocc)
+    u = o.random_unitary(norb, seed=rng)
+    vec = o.random_state_vector(math.comb(norb, nocc), seed=rng)
+    z = rng.normal(size=vec.size)
+    pd = _plan(u.conj().T, True)
+    d = pd["ops_diag"]
+    assert np.abs(d - 1).max() > 1e-3  # the phases are not trivial
+    pu = _plan(u * d[None, :], True)
+    assert pu["kind"] == 3 and pu["err"] < 1e-10
+    half = pe.apply_ops(dict(pd, ops_diag=np.ones(norb)), vec, norb, nocc)
+    got = pe.apply_ops(pu, z * half, norb, nocc)
+    want = o.apply_orbital_rotation(z * o.apply_orbital_rotation(vec, u.conj().T, norb, nocc), u, norb, nocc)
+    np.testing.assert_allclose(got, want, atol=1e-11)
+
+
 def test_stage_sequence_special_matrices():
     """Block-diagonal, permutation and identity unitaries take the three-window form."""
     for norb, nocc in [(9, 3), (10, 4), (12, 2)]:
