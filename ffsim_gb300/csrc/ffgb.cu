@@ -1398,6 +1398,7 @@ static int stack_rotated_matvec(const void* Y, void* Yacc, void* Y1, void* T, co
   FFGB_TRY(launch_transpose_stacked<float>(Y1, T, d.da, d.db, d.n, d.pb, d.pa, nullptr, st));
   FFGB_TRY(stage_rotate_rows(T, T, norb, nb, tb, tb, pd, stack_opts(9, d.pa), st));
   FFGB_TRY(diag_rows<float>(T, T, norb, nb, na, spec.transposed(), false, scr, st, nullptr, nullptr, d.n));
+  scr.off = mark;
   FFGB_TRY(phase_table(&pu, norb, na, scr, st, &fa));
   FFGB_TRY(phase_table(&pu, norb, nb, scr, st, &fb));
   FFGB_TRY(stage_rotate_rows(T, T, norb, nb, tb, tb, pu, stack_opts(11, d.pa), st));
