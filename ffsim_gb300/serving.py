@@ -34,7 +34,8 @@ gradient the kernel runs the circuit, the Hamiltonian matvec and the backward
 pass with its densities; the chain rule runs on the host at collection).  A resident lane thread submits
 them in arrival order while the queue has room and collects the results;
 cancellation and deadlines apply to them as to the others.  A request the
-resident kernel cannot plan falls back to the batch path.
+resident kernel cannot plan falls back to the batch path, and so do all small
+requests if the resident evaluator cannot be created.
 
 Results do not depend on what else runs: a state's result is the same alone
 and in any batch (the dithering of a state's coefficients and the order of
@@ -508,7 +509,18 @@ class LUCJServer:
                     self._res_pending.clear()
                     cancel = [t for rid, t in self._res_ticket.items() if rid in self._cancelled]
                 if ev is None:
-                    ev = self._make_resident()
+                    try:
+                        ev = self._make_resident()
+                    except BaseException:  # noqa: BLE001
+                        # no resident evaluator on this device: its requests,
+                        # and every small one from now on, take the batch path
+                        with self._cv:
+                            self.resident = False
+                            self._pending.extend(todo)
+                            self._pending.extend(self._res_pending)
+                            self._res_pending.clear()
+                            self._cv.notify_all()
+                        return
                 for t in cancel:
                     ev.cancel(t)
                 for i, req in enumerate(todo):

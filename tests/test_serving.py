@@ -388,6 +388,28 @@ def test_resident_cancel_and_unplannable_fallback():
     assert all(res[r.rid].ok and res[r.rid].path == "batch" and res[r.rid].energy == r.rid * 0.5 for r in six)
 
 
+def test_resident_evaluator_that_cannot_start_sends_requests_to_the_batch_path():
+    _reset()
+    from ffsim_gb300.serving import LUCJServer
+
+    def broken():
+        raise RuntimeError("no device memory for the resident queue")
+
+    srv = LUCJServer(workers=2, budget_bytes=10**9, make_engine=lambda k, n, ne, c: _FakeEngine(k, n, ne, c),
+                     size_of=lambda k, n, ne, c: n * 100 * c, use_streams=False, make_resident=broken)
+    reqs = _mixed(40, seed=5)
+    first, rest = reqs[:20], reqs[20:]
+    for r in first:
+        srv.submit(r)
+    time.sleep(0.2)
+    for r in rest:
+        srv.submit(r)
+    res = srv.drain(len(reqs), timeout=60)
+    srv.close()
+    assert not srv.resident
+    assert all(r.ok and r.path == "batch" and r.energy == r.rid * 0.5 for r in res)
+
+
 def test_resident_deadline_while_pending():
     _reset()
     fake = _FakeResident(cap=1, delay=0.3)
