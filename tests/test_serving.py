@@ -319,7 +319,7 @@ def test_engine_build_out_of_memory_requeues_then_fails():
 
 def _mixed(n, seed=0):
     """Energy requests of norb 6, 8 (resident) and 10 (batch), and norb-8
-    gradients (batch)."""
+    gradients (resident)."""
     from ffsim_gb300.serving import Request
     from ffsim_gb300.variational import UCJOpSpinBalanced
 
