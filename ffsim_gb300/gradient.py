@@ -374,12 +374,22 @@ class LUCJGradient(GradientHost):
             with torch.cuda.stream(stream):
                 return [(b, fn(b)) for b in range(i, n, W)]
 
+        # every lane finishes enqueueing, and the current stream waits for
+        # all of them, before an error from one lane is raised: no lane's
+        # work on the batch buffers outlives the call
+        futures = [self._pool.submit(lane, i) for i in range(min(W, n))]
         results = [None] * n
-        for part in self._pool.map(lane, range(min(W, n))):
-            for b, r in part:
-                results[b] = r
+        err = None
+        for fut in futures:
+            try:
+                for b, r in fut.result():
+                    results[b] = r
+            except BaseException as exc:  # noqa: BLE001
+                err = err or exc
         for stream, _ in self._lanes:
             main.wait_stream(stream)
+        if err is not None:
+            raise err
         return results
 
     def close(self) -> None:

@@ -89,6 +89,35 @@ def test_gradient_norb12_directional(cuda):
 
 
 @pytest.mark.gpu
+def test_a_failing_lane_raises_and_the_evaluator_stays_usable(cuda):
+    """A state whose backward pass raises on one worker lane: the batch call
+    raises that error once every lane has finished, and the next batch on the
+    same evaluator gives the same results as before."""
+    import torch
+
+    from ffsim_gb300.gradient import LUCJGradient
+
+    norb, nelec, n_reps = 6, (3, 3), 2
+    p0, ham = _setup(norb, n_reps, 3, 41, False)
+    params = np.stack([p0, 0.5 * p0, -0.3 * p0, 0.8 * p0, 0.1 * p0])
+    ev = LUCJGradient(norb, nelec, dtype=torch.complex64, workers=3)
+    e_ref, g_ref = ev.value_and_grad_batch(params, n_reps, ham)
+    orig = ev._backward
+
+    def failing(cur, lam, V, jaa, jab, L):
+        if cur.data_ptr() == ev._bcur[1].data_ptr():
+            raise RuntimeError("lane failure")
+        return orig(cur, lam, V, jaa, jab, L)
+
+    ev._backward = failing
+    with pytest.raises(RuntimeError, match="lane failure"):
+        ev.value_and_grad_batch(params, n_reps, ham)
+    ev._backward = orig
+    e2, g2 = ev.value_and_grad_batch(params, n_reps, ham)
+    assert np.array_equal(e2, e_ref) and np.array_equal(g2, g_ref)
+
+
+@pytest.mark.gpu
 def test_autograd_function_batch(cuda):
     import torch
 
